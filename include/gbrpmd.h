@@ -1,0 +1,206 @@
+/*
+ * gbrpmd.h -- C ABI of the GB300 ring-polymer force-and-propagation library.
+ *
+ * The library replaces the reference's per-step RPMD path
+ * (DCM-UPB/RPMD_Mainz, Fortran 90) behind the same argument lists.  Every
+ * drop-in entry point takes its arguments by reference exactly like the
+ * Fortran routine it replaces (double* / int*), arrays in Fortran column-major
+ * order:  r(3,na,nb)  ->  r[i + 3*(j + na*k)]  (i = xyz, j = atom, k = bead).
+ * Atoms are ordered O,H,H per molecule.  Units are atomic (bohr, hartree,
+ * electron masses).  dvdr is +grad V per bead.
+ *
+ * The COMMON-block state the Fortran routines read implicitly
+ * (/oo_param/, /ew_param/, /ew_setup/, /beaddiabatic/, /intra_param/,
+ * /geometry/, /correct/, /multiple_ts/, /symmetry/, /constraint/ and the
+ * thermostat / barostat module variables, main.f90:53-72) is passed once
+ * through gbrpmd_init() so that no COMMON symbol is read from C.
+ *
+ * Every entry point returns an int status: GB_OK (0) or one of the GB_E*
+ * codes below, which stand in for the reference's `stop` statements.
+ * gbrpmd_last_error() returns the message of the last failure.
+ *
+ * Threading: one host thread per library instance (the reference is serial).
+ * All device work runs on the library's own CUDA stream; every drop-in call
+ * synchronises that stream before it returns.
+ */
+#ifndef GBRPMD_H
+#define GBRPMD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (reference `stop` sites in comments) ------------------ */
+#define GB_OK 0
+#define GB_E_ARG 1           /* invalid argument / unsupported option          */
+#define GB_E_NOINIT 2        /* gbrpmd_init not called                          */
+#define GB_E_CUDA 3          /* CUDA runtime error or no device                 */
+#define GB_E_LIST 4          /* neighbour list too small  (neigh_list.f90:63)   */
+#define GB_E_RATTLE1 5       /* RATTLE stage 1 iterations (md_rattle.f90:149)   */
+#define GB_E_RATTLE2 6       /* RATTLE stage 2 iterations (md_rattle.f90:258)   */
+#define GB_E_CONTRACT 7      /* contraction count not odd (evolve_pi.f90:344)   */
+#define GB_E_NONFINITE 8     /* non-finite force or energy                      */
+#define GB_E_CUTOFF 9        /* ewc cut-off larger than half box (correct_tem)  */
+#define GB_E_NOMEM 10        /* device memory exhausted / over a size limit     */
+#define GB_E_UNSUPPORTED 11  /* option not implemented on the device            */
+
+/* thermostat selector (module thermostat, `therm`, module_thermostat.f90:4) */
+#define GB_THERM_NONE 0
+#define GB_THERM_AND 1  /* Andersen: resampling happens in the caller (md_eq.f90:311) */
+#define GB_THERM_PRG 2  /* global Parrinello kick inside evolve_pi (evolve_pi.f90:73) */
+#define GB_THERM_PRL 3  /* local Langevin kick inside evolve_pi  (evolve_pi.f90:75) */
+
+/* intramolecular model selector */
+#define GB_INTRA_REFERENCE 0 /* potenl_opt dispatch (md_forces.f90:254-263)         */
+#define GB_INTRA_SPCFW 1     /* intra_spcfw (intra_spcfw.f90), commented out in ref */
+
+/* precision selector */
+#define GB_PREC_FP64 0  /* plain FP64 everywhere                               */
+#define GB_PREC_MIXED 1 /* FP32 pair / reciprocal / transform arithmetic, FP64 totals */
+
+/* Hidden inputs of the reference path (COMMON blocks and module variables). */
+typedef struct gb_params {
+  /* common /oo_param/ oo_eps,oo_sig,oo_gam,rcut  (main.f90:57); rcut in bohr,
+     already clamped to half the shortest box side as main.f90:615-616 does */
+  double oo_eps, oo_sig, oo_gam, rcut;
+  /* common /ew_param/ alpha,ecut,wm,wh  (main.f90:58) */
+  double alpha, ecut, wm, wh;
+  /* common /ew_setup/ wrcut,walpha,rkmax,kmax  (setup_options.f90:122) */
+  double wrcut, walpha, rkmax;
+  int32_t kmax;
+  /* common /beaddiabatic/ nbdf1,nbdf2  (main.f90:54) */
+  int32_t nbdf1, nbdf2;
+  /* common /intra_param/ apot,bpot,alp,alpb  (main.f90:59) */
+  double apot, bpot, alp, alpb;
+  /* common /geometry/ theta,reoh  (main.f90:55); theta in radians */
+  double theta, reoh;
+  /* common /correct/ sig  (main.f90:60); bohr */
+  double sig;
+  /* common /multiple_ts/ mts  (main.f90:56) */
+  int32_t mts;
+  /* common /symmetry/ iamcub  (main.f90:62) */
+  int32_t iamcub;
+  /* common /constraint/ nctot,nbond  (main.f90:65) */
+  int32_t nctot, nbond;
+  /* module thermostat: therm, ttau  (module_thermostat.f90:3-4) */
+  int32_t therm;
+  double ttau;
+  /* module barostat: taub, patm (module_barostat.f90:3-5); the barostat
+     itself is not part of the device path, these are carried for callers */
+  double taub, patm;
+  /* selectors of this library */
+  int32_t intra_model; /* GB_INTRA_* */
+  int32_t precision;   /* GB_PREC_*  */
+} gb_params;
+
+/* ---- set-up --------------------------------------------------------------- */
+
+/* Stores the hidden inputs; call once after setup_ewald (main.f90:631) and
+   again whenever one of them changes.  Replaces the COMMON blocks. */
+int gbrpmd_init(const gb_params *params);
+
+/* Reads back the stored hidden inputs. */
+int gbrpmd_get_params(gb_params *params);
+
+/* Message of the last failing call (static storage, never NULL). */
+const char *gbrpmd_last_error(void);
+
+/* Releases every device context and buffer the library holds. */
+int gbrpmd_finalize(void);
+
+/* ---- drop-in entry points ------------------------------------------------ */
+
+/* replaces subroutine forces(r,v,dvdr,nb,na,boxlxyz,z,virial,iopt)
+   (md_forces.f90:1-110).  iopt: 0 full, 1 Ewald+LJ, 2 Ewald, 3 LJ,
+   4 intramolecular, 5 TEM short-range Coulomb correction.  v and virial are
+   bead-averaged, dvdr is per bead.  r is not modified. */
+int gbrpmd_forces(double *r, double *v, double *dvdr, const int *nb, const int *na,
+                  const double *boxlxyz, const double *z, double *virial, const int *iopt);
+
+/* replaces subroutine full_forces(r,na,nb,v,vew,voo,vint,vir,z,boxlxyz,dvdr,dvdr2)
+   (md_forces.f90:305-472): low-frequency (Ewald + LJ, with ring-polymer
+   contraction when nbdf1/nbdf2 > 0) into dvdr, intramolecular into dvdr2. */
+int gbrpmd_full_forces(double *r, const int *na, const int *nb, double *v, double *vew,
+                       double *voo, double *vint, double *vir, const double *z,
+                       const double *boxlxyz, double *dvdr, double *dvdr2);
+
+/* replaces subroutine evolve_pi(p,r,v,vew,vlj,vint,dvdr,dvdr2,dt,mass,na,nb,
+   boxlxyz,z,beta,vir,vir_lf,irun,nbaro)  (evolve_pi.f90:1-322): one outer
+   multiple-time-step RPMD step in the normal-mode representation.
+   nbaro must be 0 (barostats are outside the device path). */
+int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj,
+                     double *vint, double *dvdr, double *dvdr2, const double *dt,
+                     const double *mass, const int *na, const int *nb, double *boxlxyz,
+                     const double *z, const double *beta, double *vir, double *vir_lf,
+                     int *irun, const int *nbaro);
+
+/* replaces subroutine rattle_setup(nm)  (md_rattle.f90:1-31); sets nctot and
+   nbond of the stored parameters. */
+int gbrpmd_rattle_setup(const int *nm);
+
+/* replaces subroutine rattle_s1(r,rold,p,nm,mass,dt,dvdr,vir,na)
+   (md_rattle.f90:33-162) for one bead. */
+int gbrpmd_rattle_s1(double *r, const double *rold, double *p, const int *nm,
+                     const double *mass, const double *dt, double *dvdr, double *vir,
+                     const int *na);
+
+/* replaces subroutine rattle_s2(r,p,nm,mass,dt,dvdr,vir,na)
+   (md_rattle.f90:164-271) for one bead. */
+int gbrpmd_rattle_s2(double *r, double *p, const int *nm, const double *mass,
+                     const double *dt, double *dvdr, double *vir, const int *na);
+
+/* replaces subroutine evolve_rig_pi(p,r,v,v_lf,v_hf,dvdr,dvdr2,dt,mass,na,nb,
+   boxlxyz,z,beta,vir,vir_lf,irun,nbaro)  (evolve_rigid.f90:100-224): rigid
+   ring-polymer step with primitive bead springs and RATTLE. nbaro must be 0. */
+int gbrpmd_evolve_rig_pi(double *p, double *r, double *v, double *v_lf, double *v_hf,
+                         double *dvdr, double *dvdr2, const double *dt, const double *mass,
+                         const int *na, const int *nb, double *boxlxyz, const double *z,
+                         const double *beta, double *vir, double *vir_lf, int *irun,
+                         const int *nbaro);
+
+/* ---- serial random stream (random.f90:1-72) ----------------------------- */
+/* The thermostat kicks inside evolve_pi draw from the reference's global
+   ran2/gaussian stream.  The library owns that stream; a Fortran host routes
+   its own ran2/gaussian calls here so there is exactly one stream. */
+
+/* replaces function ran2(idum,rmin,rmax)  (random.f90:28-72) */
+double gbrpmd_ran2(int *idum, const double *rmin, const double *rmax);
+/* replaces function gaussian(idum,sigma)  (random.f90:1-26) */
+double gbrpmd_gaussian(int *idum, const double *sigma);
+
+/* ---- resident (device-state) interface ------------------------------------
+ * A context keeps p, r, dvdr, dvdr2 of one trajectory in device memory so that
+ * repeated steps need no host transfers; the drop-in calls above are built on
+ * it.  Arrays passed here use the same r(3,na,nb) layout. */
+typedef struct gb_context gb_context;
+
+int gbrpmd_ctx_create(gb_context **ctx, int na, int nb, const double *mass, const double *z);
+int gbrpmd_ctx_destroy(gb_context *ctx);
+/* uploads r, p, dvdr, dvdr2 (any may be NULL to keep the device copy) and box */
+int gbrpmd_ctx_upload(gb_context *ctx, const double *r, const double *p, const double *dvdr,
+                      const double *dvdr2, const double *boxlxyz);
+/* downloads the device state (any pointer may be NULL) */
+int gbrpmd_ctx_download(gb_context *ctx, double *r, double *p, double *dvdr, double *dvdr2);
+/* full_forces on the device state: fills dvdr and dvdr2, returns energies */
+int gbrpmd_ctx_full_forces(gb_context *ctx, double *v, double *vew, double *voo,
+                           double *vint, double *vir);
+/* `nsteps` evolve_pi steps on the device state; energies of the last step.
+   Asynchronous: results are valid after gbrpmd_ctx_sync. */
+int gbrpmd_ctx_evolve(gb_context *ctx, int nsteps, double dt, double beta);
+/* waits for the context's stream and reports any device-side status */
+int gbrpmd_ctx_sync(gb_context *ctx);
+/* energies and virials of the last step: out[0..4] = v, vew, vlj, vint, tv;
+   vir[9], vir_lf[9] column-major */
+int gbrpmd_ctx_energies(gb_context *ctx, double *out5, double *vir, double *vir_lf);
+/* the CUDA stream (cudaStream_t) the context launches on */
+void *gbrpmd_ctx_stream(gb_context *ctx);
+/* number of kernel launches issued by this context since creation */
+int64_t gbrpmd_ctx_launch_count(gb_context *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBRPMD_H */

@@ -1,0 +1,96 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's own
+regression run (test/cmp/gentest.cmp of DCM-UPB/RPMD_Mainz) and its param files.
+
+Run in a checkout where the reference tree is available:
+
+    python tests/golden/make_golden.py /path/to/RPMD_Mainz
+
+Writes
+  params/*                 the namelist files the tests use (data, unchanged)
+  gentest_frames.npz       bead positions (Angstrom), forces -(dvdr+dvdr2)
+                           (hartree/bohr) and velocities p/m (a.u.) of both
+                           beads for a few frames of the NVE trajectories, the
+                           box, and the initial CUB lattice vmd_start.xyz
+  gentest_kat.json         the set-up values and initial energy printed in
+                           `output`
+Frames are written every pb = 20 steps of the two 2*nt = 250-step NVE
+trajectories of md_dynamics.f90 (trajectory(), lines 517-546): file frames
+0..11 belong to trajectory 1, 12..23 to trajectory 2.
+"""
+import json
+import os
+import re
+import shutil
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FRAMES = [0, 1, 2, 12, 13]
+
+
+def read_xyz_frames(path):
+    frames, boxes = [], []
+    with open(path) as f:
+        lines = f.read().splitlines()
+    i = 0
+    while i < len(lines):
+        if not lines[i].strip():
+            i += 1
+            continue
+        na = int(lines[i].split()[0])
+        box = [float(x) for x in lines[i + 1].split()[1:4]]
+        rows = []
+        for ln in lines[i + 2:i + 2 + na]:
+            parts = ln.split()
+            rows.append([float(x) for x in parts[1:4]])
+        frames.append(rows)
+        boxes.append(box)
+        i += 2 + na
+    return np.array(frames), np.array(boxes)
+
+
+def main(ref):
+    cmp_dir = os.path.join(ref, "test", "cmp", "gentest.cmp")
+    os.makedirs(os.path.join(HERE, "params"), exist_ok=True)
+    for name in ["param_qspcfw", "param_scott", "param_tipice_rigid", "param_tip05_rigid", "param_spce_rigid"]:
+        shutil.copyfile(os.path.join(ref, "params", name), os.path.join(HERE, "params", name))
+    shutil.copyfile(os.path.join(cmp_dir, "input"), os.path.join(HERE, "params", "gentest_input"))
+
+    data = {}
+    for bead in (1, 2):
+        for kind in ("xyz", "frc", "vel"):
+            arr, box = read_xyz_frames(os.path.join(cmp_dir, f"vmd_bead-{bead}.{kind}"))
+            data[f"{kind}{bead}"] = arr[FRAMES]
+            if kind == "xyz":
+                data[f"box{bead}"] = box[FRAMES]
+    start, sbox = read_xyz_frames(os.path.join(cmp_dir, "vmd_start.xyz"))
+    data["start"] = start[0]
+    data["start_box"] = sbox[0]
+    data["frames"] = np.array(FRAMES)
+    np.savez_compressed(os.path.join(HERE, "gentest_frames.npz"), **data)
+
+    out = open(os.path.join(cmp_dir, "output")).read()
+
+    def grab(pattern):
+        m = re.search(pattern, out)
+        return float(m.group(1))
+
+    kat = {
+        "boxlx_bohr": grab(r"\bboxlx\s*=\s*([\d.]+)"),
+        "rcut_bohr": grab(r"\brcut\s*=\s*([\d.]+)"),
+        "wrcut_bohr": grab(r"\bwrcut\s*=\s*([\d.]+)"),
+        "walpha_per_bohr": grab(r"\bwalpha\s*=\s*([\d.]+)"),
+        "rkmax_per_bohr": grab(r"\brkmax\s*=\s*([\d.]+)"),
+        "kmax": int(grab(r"\bkmax\s*=\s*(\d+)")),
+        "initial_energy_per_atom": grab(r"Initial energy =\s*([-\d.]+)"),
+        "sigma_bohr": grab(r"with sigma =\s*([\d.]+)"),
+        "na": int(grab(r"\bna\s*=\s*(\d+)")),
+    }
+    with open(os.path.join(HERE, "gentest_kat.json"), "w") as f:
+        json.dump(kat, f, indent=1)
+    print("wrote", sorted(data), kat)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
