@@ -1,0 +1,458 @@
+// api.cpp -- C ABI of the library (include/gbrpmd.h): parameter store,
+// device contexts, drop-in entry points and the serial random stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+
+#include "gb_common.h"
+#include "gb_context.h"
+
+namespace {
+
+gb_params g_params;
+bool g_init = false;
+thread_local std::string g_err = "no error";
+std::map<std::pair<int, int>, gb_context *> g_dropin;  // drop-in contexts by (na, nb)
+
+#define CK(x)                                             \
+  do {                                                    \
+    cudaError_t e_ = (x);                                 \
+    if (e_ != cudaSuccess) return ctx_check_cuda(e_, #x); \
+  } while (0)
+
+template <typename T>
+int dalloc(gb_context *c, T **p, size_t n) {
+  CK(cudaMalloc((void **)p, sizeof(T) * (n ? n : 1)));
+  c->allocs.push_back((void *)*p);
+  return GB_OK;
+}
+
+// drop-in calls keep one device context per (na, nb)
+int dropin_ctx(int na, int nb, gb_context **out) {
+  if (!g_init) return ctx_set_error(GB_E_NOINIT, "gbrpmd_init has not been called");
+  auto key = std::make_pair(na, nb);
+  auto it = g_dropin.find(key);
+  if (it != g_dropin.end()) {
+    *out = it->second;
+    (*out)->P = g_params;
+    return GB_OK;
+  }
+  gb_context *c = new gb_context();
+  int st = ctx_alloc(c, na, nb);
+  if (st) {
+    ctx_free(c);
+    delete c;
+    return st;
+  }
+  c->P = g_params;
+  g_dropin[key] = c;
+  *out = c;
+  return GB_OK;
+}
+
+int upload(gb_context *c, double *dst, const double *src, size_t n) {
+  if (!src) return GB_OK;
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  return GB_OK;
+}
+
+int download(gb_context *c, double *dst, const double *src, size_t n) {
+  if (!dst) return GB_OK;
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  return GB_OK;
+}
+
+int set_charges(gb_context *c, const double *z) {
+  if (!z) return GB_OK;
+  double qq = 0.0;
+  for (int i = 0; i < c->na; ++i) qq = qq + z[i] * z[i];
+  c->qq = qq;
+  return upload(c, c->z, z, (size_t)c->na);
+}
+
+int check_sizes(int na, int nb) {
+  if (na <= 0 || na % 3 != 0) return ctx_set_error(GB_E_ARG, "potenl 1: na is not 3*nm");
+  if (nb <= 0 || nb > 256) return ctx_set_error(GB_E_ARG, "nb must be 1..256 (fourier.f90 nmax)");
+  return GB_OK;
+}
+
+}  // namespace
+
+const gb_params &current_params() { return g_params; }
+
+int ctx_set_error(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+int ctx_check_cuda(cudaError_t e, const char *what) {
+  g_err = std::string("CUDA error ") + cudaGetErrorString(e) + " at " + what;
+  return e == cudaErrorMemoryAllocation ? GB_E_NOMEM : GB_E_CUDA;
+}
+
+int ctx_alloc(gb_context *c, int na, int nb) {
+  int st = check_sizes(na, nb);
+  if (st) return st;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return ctx_set_error(GB_E_CUDA, "no CUDA device");
+  CK(cudaGetDevice(&c->device));
+  c->na = na;
+  c->nb = nb;
+  c->nm = na / 3;
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  const size_t N = 3 * (size_t)na * nb, S = 3 * (size_t)na;
+  if ((st = dalloc(c, &c->p, N)) || (st = dalloc(c, &c->r, N)) || (st = dalloc(c, &c->dvdr, N)) ||
+      (st = dalloc(c, &c->dvdr2, N)) || (st = dalloc(c, &c->rst, N)) || (st = dalloc(c, &c->rnm, N)) ||
+      (st = dalloc(c, &c->mass, (size_t)na)) || (st = dalloc(c, &c->z, (size_t)na)) ||
+      (st = dalloc(c, &c->f_a, N)) || (st = dalloc(c, &c->f_b, N)) || (st = dalloc(c, &c->f_c, N)) ||
+      (st = dalloc(c, &c->rb1, N)) || (st = dalloc(c, &c->fb1, N)) || (st = dalloc(c, &c->rb2, N)) ||
+      (st = dalloc(c, &c->fb2, N)) || (st = dalloc(c, &c->g, N)) || (st = dalloc(c, &c->rs, N)) ||
+      (st = dalloc(c, &c->rs32, (size_t)na * nb)) || (st = dalloc(c, &c->rc, S)) ||
+      (st = dalloc(c, &c->monod, 12 * (size_t)nb)) ||
+      (st = dalloc(c, &c->acc, (size_t)ACC_NSLOT * ACC_STRIDE)) || (st = dalloc(c, &c->status, 1)))
+    return st;
+  CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  CK(cudaMemsetAsync(c->dvdr, 0, sizeof(double) * N, c->stream));
+  CK(cudaMemsetAsync(c->dvdr2, 0, sizeof(double) * N, c->stream));
+  CK(cudaMemsetAsync(c->p, 0, sizeof(double) * N, c->stream));
+  CK(cudaMallocHost(&c->h_acc, sizeof(double) * ACC_NSLOT * ACC_STRIDE));
+  CK(cudaMallocHost(&c->h_status, sizeof(unsigned)));
+  CK(cudaStreamSynchronize(c->stream));
+  return GB_OK;
+}
+
+void ctx_free(gb_context *c) {
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void *p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+  for (void *p : {(void *)c->pl.idx, (void *)c->pl.count, (void *)c->kxy, (void *)c->kxy_koff,
+                  (void *)c->klist, (void *)c->kw, (void *)c->sk_part, (void *)c->sk,
+                  (void *)c->tw_nb, (void *)c->tw_c1, (void *)c->tw_c2})
+    if (p) cudaFree(p);
+  if (c->h_acc) cudaFreeHost(c->h_acc);
+  if (c->h_status) cudaFreeHost(c->h_status);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  c->stream = nullptr;
+}
+
+extern "C" {
+
+int gbrpmd_init(const gb_params *params) {
+  if (!params) return ctx_set_error(GB_E_ARG, "null params");
+  if (params->mts < 1) return ctx_set_error(GB_E_ARG, "mts must be >= 1");
+  g_params = *params;
+  g_init = true;
+  return GB_OK;
+}
+
+int gbrpmd_get_params(gb_params *params) {
+  if (!g_init) return ctx_set_error(GB_E_NOINIT, "gbrpmd_init has not been called");
+  *params = g_params;
+  return GB_OK;
+}
+
+const char *gbrpmd_last_error(void) { return g_err.c_str(); }
+
+int gbrpmd_finalize(void) {
+  for (auto &kv : g_dropin) {
+    ctx_free(kv.second);
+    delete kv.second;
+  }
+  g_dropin.clear();
+  return GB_OK;
+}
+
+// ---- drop-in entry points ----
+
+int gbrpmd_forces(double *r, double *v, double *dvdr, const int *nb, const int *na,
+                  const double *boxlxyz, const double *z, double *virial, const int *iopt) {
+  gb_context *c;
+  int st = dropin_ctx(*na, *nb, &c);
+  if (st) return st;
+  const size_t N = 3 * (size_t)(*na) * (*nb);
+  std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
+  if ((st = upload(c, c->r, r, N)) || (st = set_charges(c, z))) return st;
+  if ((st = dev_forces(c, c->r, *nb, c->dvdr, *iopt))) return st;
+  if ((st = download(c, dvdr, c->dvdr, N))) return st;
+  if ((st = dev_collect(c, 0, 0.0, 1.0))) return st;
+  *v = c->e_v;
+  for (int i = 0; i < 9; ++i) virial[i] = c->e_vir[i];
+  return GB_OK;
+}
+
+int gbrpmd_full_forces(double *r, const int *na, const int *nb, double *v, double *vew,
+                       double *voo, double *vint, double *vir, const double *z,
+                       const double *boxlxyz, double *dvdr, double *dvdr2) {
+  gb_context *c;
+  int st = dropin_ctx(*na, *nb, &c);
+  if (st) return st;
+  const size_t N = 3 * (size_t)(*na) * (*nb);
+  std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
+  if ((st = upload(c, c->r, r, N)) || (st = set_charges(c, z))) return st;
+  if ((st = dev_full_forces(c))) return st;
+  if ((st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N))) return st;
+  if ((st = dev_collect(c, 0, 0.0, 1.0))) return st;
+  *v = c->e_v;
+  *vew = c->e_vew;
+  *voo = c->e_vlj;
+  *vint = c->e_vint;
+  for (int i = 0; i < 9; ++i) vir[i] = c->e_vir[i];
+  return GB_OK;
+}
+
+int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj, double *vint,
+                     double *dvdr, double *dvdr2, const double *dt, const double *mass,
+                     const int *na, const int *nb, double *boxlxyz, const double *z,
+                     const double *beta, double *vir, double *vir_lf, int *irun,
+                     const int *nbaro) {
+  (void)irun;
+  if (*nbaro != 0) return ctx_set_error(GB_E_UNSUPPORTED, "barostats are not on the device path (nbaro must be 0)");
+  gb_context *c;
+  int st = dropin_ctx(*na, *nb, &c);
+  if (st) return st;
+  const size_t N = 3 * (size_t)(*na) * (*nb);
+  std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
+  if ((st = upload(c, c->p, p, N)) || (st = upload(c, c->r, r, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||
+      (st = upload(c, c->dvdr2, dvdr2, N)) || (st = upload(c, c->mass, mass, (size_t)*na)) ||
+      (st = set_charges(c, z)))
+    return st;
+  if (c->monod_dt > 0.0) {  // masses may have changed: rebuild the monodromy table
+    c->monod_dt = -1.0;
+  }
+  if ((st = dev_evolve_pi(c, *dt, *beta))) return st;
+  if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
+      (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N)))
+    return st;
+  if ((st = dev_collect(c, 1, *dt, *beta))) return st;
+  *v = c->e_v;
+  *vew = c->e_vew;
+  *vlj = c->e_vlj;
+  *vint = c->e_vint;
+  for (int i = 0; i < 9; ++i) {
+    vir[i] = c->e_vir[i];
+    vir_lf[i] = c->e_vir_lf[i];
+  }
+  return GB_OK;
+}
+
+// ---- resident interface ----
+
+int gbrpmd_ctx_create(gb_context **ctx, int na, int nb, const double *mass, const double *z) {
+  if (!g_init) return ctx_set_error(GB_E_NOINIT, "gbrpmd_init has not been called");
+  gb_context *c = new gb_context();
+  int st = ctx_alloc(c, na, nb);
+  if (st) {
+    ctx_free(c);
+    delete c;
+    return st;
+  }
+  c->P = g_params;
+  if ((st = upload(c, c->mass, mass, (size_t)na)) || (st = set_charges(c, z))) {
+    ctx_free(c);
+    delete c;
+    return st;
+  }
+  cudaStreamSynchronize(c->stream);
+  *ctx = c;
+  return GB_OK;
+}
+
+int gbrpmd_ctx_destroy(gb_context *ctx) {
+  if (!ctx) return GB_OK;
+  ctx_free(ctx);
+  delete ctx;
+  return GB_OK;
+}
+
+int gbrpmd_ctx_upload(gb_context *c, const double *r, const double *p, const double *dvdr,
+                      const double *dvdr2, const double *boxlxyz) {
+  const size_t N = 3 * (size_t)c->na * c->nb;
+  int st;
+  if (boxlxyz) std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
+  if ((st = upload(c, c->r, r, N)) || (st = upload(c, c->p, p, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||
+      (st = upload(c, c->dvdr2, dvdr2, N)))
+    return st;
+  return GB_OK;
+}
+
+int gbrpmd_ctx_download(gb_context *c, double *r, double *p, double *dvdr, double *dvdr2) {
+  const size_t N = 3 * (size_t)c->na * c->nb;
+  int st;
+  if ((st = download(c, r, c->r, N)) || (st = download(c, p, c->p, N)) || (st = download(c, dvdr, c->dvdr, N)) ||
+      (st = download(c, dvdr2, c->dvdr2, N)))
+    return st;
+  CK(cudaStreamSynchronize(c->stream));
+  return GB_OK;
+}
+
+int gbrpmd_ctx_full_forces(gb_context *c, double *v, double *vew, double *voo, double *vint,
+                           double *vir) {
+  c->P = g_params;
+  int st = dev_full_forces(c);
+  if (st) return st;
+  if ((st = dev_collect(c, 0, 0.0, 1.0))) return st;
+  if (v) *v = c->e_v;
+  if (vew) *vew = c->e_vew;
+  if (voo) *voo = c->e_vlj;
+  if (vint) *vint = c->e_vint;
+  if (vir)
+    for (int i = 0; i < 9; ++i) vir[i] = c->e_vir[i];
+  return GB_OK;
+}
+
+int gbrpmd_ctx_evolve(gb_context *c, int nsteps, double dt, double beta) {
+  c->P = g_params;
+  for (int s = 0; s < nsteps; ++s) {
+    int st = dev_evolve_pi(c, dt, beta);
+    if (st) return st;
+  }
+  return GB_OK;
+}
+
+int gbrpmd_ctx_sync(gb_context *c) { return dev_collect(c, 1, 0.0, c->last_beta); }
+
+int gbrpmd_ctx_energies(gb_context *c, double *out5, double *vir, double *vir_lf) {
+  if (out5) {
+    out5[0] = c->e_v;
+    out5[1] = c->e_vew;
+    out5[2] = c->e_vlj;
+    out5[3] = c->e_vint;
+    out5[4] = c->e_tv;
+  }
+  if (vir)
+    for (int i = 0; i < 9; ++i) vir[i] = c->e_vir[i];
+  if (vir_lf)
+    for (int i = 0; i < 9; ++i) vir_lf[i] = c->e_vir_lf[i];
+  return GB_OK;
+}
+
+void *gbrpmd_ctx_stream(gb_context *c) { return (void *)c->stream; }
+
+int64_t gbrpmd_ctx_launch_count(gb_context *c) { return c->launches; }
+
+// ---- serial random stream (random.f90:1-72) ----
+static struct {
+  int iv[32] = {0};
+  int iy = 0;
+  int idum2 = 123456789;
+  int iset = 0;
+  double gset = 0.0;
+} g_rng;
+
+double gbrpmd_ran2(int *idum, const double *rmin, const double *rmax) {
+  const int im1 = 2147483563, im2 = 2147483399, imm1 = im1 - 1;
+  const int ia1 = 40014, ia2 = 40692, iq1 = 53668, iq2 = 52774, ir1 = 12211, ir2 = 3791;
+  const int ntab = 32, ndiv = 1 + imm1 / ntab;
+  const double am = 1.0 / im1, eps = 1.2e-7, rnmx = 1.0 - eps;
+  int k, j;
+  if (*idum <= 0) {
+    *idum = (-*idum) > 1 ? -*idum : 1;
+    g_rng.idum2 = *idum;
+    for (j = ntab + 8; j >= 1; --j) {
+      k = *idum / iq1;
+      *idum = ia1 * (*idum - k * iq1) - k * ir1;
+      if (*idum < 0) *idum += im1;
+      if (j <= ntab) g_rng.iv[j - 1] = *idum;
+    }
+    g_rng.iy = g_rng.iv[0];
+  }
+  k = *idum / iq1;
+  *idum = ia1 * (*idum - k * iq1) - k * ir1;
+  if (*idum < 0) *idum += im1;
+  k = g_rng.idum2 / iq2;
+  g_rng.idum2 = ia2 * (g_rng.idum2 - k * iq2) - k * ir2;
+  if (g_rng.idum2 < 0) g_rng.idum2 += im2;
+  j = 1 + g_rng.iy / ndiv;
+  g_rng.iy = g_rng.iv[j - 1] - g_rng.idum2;
+  g_rng.iv[j - 1] = *idum;
+  if (g_rng.iy < 1) g_rng.iy += imm1;
+  double u = am * g_rng.iy;
+  return ((*rmax - *rmin) * (u < rnmx ? u : rnmx)) + *rmin;
+}
+
+double gbrpmd_gaussian(int *idum, const double *sigma) {
+  const double zero = 0.0, one = 1.0;
+  if (g_rng.iset == 0) {
+    double v1, v2, rsq;
+    do {
+      v1 = 2.0 * gbrpmd_ran2(idum, &zero, &one) - 1.0;
+      v2 = 2.0 * gbrpmd_ran2(idum, &zero, &one) - 1.0;
+      rsq = v1 * v1 + v2 * v2;
+    } while (rsq >= 1.0 || rsq == 0.0);
+    double fac = std::sqrt(-2.0 * std::log(rsq) / rsq);
+    g_rng.gset = v1 * fac;
+    g_rng.iset = 1;
+    return *sigma * v2 * fac;
+  }
+  g_rng.iset = 0;
+  return *sigma * g_rng.gset;
+}
+
+}  // extern "C"
+
+// ---- rigid path entry points (device implementation in rattle.cpp) ----
+int dev_rattle_setup(int nm, const gb_params &P);
+int dev_rattle_s1(double *r, const double *rold, double *p, int nm, const double *mass, double dt,
+                  double *dvdr, double *vir, int na);
+int dev_rattle_s2(double *r, double *p, int nm, const double *mass, double dt, double *dvdr,
+                  double *vir, int na);
+int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout);
+
+extern "C" {
+
+int gbrpmd_rattle_setup(const int *nm) {
+  if (!g_init) return ctx_set_error(GB_E_NOINIT, "gbrpmd_init has not been called");
+  if (*nm <= 0) return ctx_set_error(GB_E_ARG, "nm must be positive");
+  g_params.nctot = 3 * (*nm);
+  g_params.nbond = 3;
+  return dev_rattle_setup(*nm, g_params);
+}
+
+int gbrpmd_rattle_s1(double *r, const double *rold, double *p, const int *nm, const double *mass,
+                     const double *dt, double *dvdr, double *vir, const int *na) {
+  if (!g_init) return ctx_set_error(GB_E_NOINIT, "gbrpmd_init has not been called");
+  return dev_rattle_s1(r, rold, p, *nm, mass, *dt, dvdr, vir, *na);
+}
+
+int gbrpmd_rattle_s2(double *r, double *p, const int *nm, const double *mass, const double *dt,
+                     double *dvdr, double *vir, const int *na) {
+  if (!g_init) return ctx_set_error(GB_E_NOINIT, "gbrpmd_init has not been called");
+  return dev_rattle_s2(r, p, *nm, mass, *dt, dvdr, vir, *na);
+}
+
+int gbrpmd_evolve_rig_pi(double *p, double *r, double *v, double *v_lf, double *v_hf, double *dvdr,
+                         double *dvdr2, const double *dt, const double *mass, const int *na,
+                         const int *nb, double *boxlxyz, const double *z, const double *beta,
+                         double *vir, double *vir_lf, int *irun, const int *nbaro) {
+  (void)irun;
+  if (*nbaro != 0) return ctx_set_error(GB_E_UNSUPPORTED, "barostats are not on the device path (nbaro must be 0)");
+  gb_context *c;
+  int st = dropin_ctx(*na, *nb, &c);
+  if (st) return st;
+  const size_t N = 3 * (size_t)(*na) * (*nb);
+  std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
+  if ((st = upload(c, c->p, p, N)) || (st = upload(c, c->r, r, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||
+      (st = upload(c, c->dvdr2, dvdr2, N)) || (st = upload(c, c->mass, mass, (size_t)*na)) ||
+      (st = set_charges(c, z)))
+    return st;
+  if ((st = dev_evolve_rig_pi(c, *dt, *beta, vir))) return st;
+  if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
+      (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N)))
+    return st;
+  if ((st = dev_collect(c, 2, *dt, *beta))) return st;
+  *v = c->e_v;
+  *v_lf = c->e_v;
+  *v_hf = 0.0;
+  for (int i = 0; i < 9; ++i) {
+    vir_lf[i] = c->e_vir_lf[i];
+    vir[i] = c->e_vir_lf[i] + c->e_vir_hf[i] + vir[i];
+  }
+  return GB_OK;
+}
+
+}  // extern "C"

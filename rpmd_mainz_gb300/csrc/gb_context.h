@@ -1,0 +1,98 @@
+// gb_context.h -- device context of one ring-polymer trajectory.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gbrpmd.h"
+
+// One pair list: for each of `nconf` configurations and each of `npt` points,
+// up to `cap` partner indices; the pair (i, j) is stored once, in the list of
+// i when (i < j) == ((i + j) odd), which halves and balances the lists.
+struct PairList {
+  int nconf = 0, npt = 0, cap = 0;
+  int *count = nullptr;  // [nconf][npt]
+  int *idx = nullptr;    // [nconf][npt][cap]
+  size_t bytes = 0;
+};
+
+// Which accumulator slots the last evaluation filled and with how many
+// configurations, so that the bead-averaged energies can be formed.
+struct EnergyPlan {
+  int B_ew = 0, B_tem = 0, B_lj = 0, B_ew2 = 0, B_tem2 = 0, B_lj2 = 0, B_int = 0;
+  int evolve = 0, mts = 1;
+};
+
+struct gb_context {
+  int na = 0, nb = 0, nm = 0;
+  EnergyPlan plan;
+  double qq = 0.0;  // sum of squared charges (Ewald self term)
+  double last_beta = 1.0;  // beta of the last evolve_pi (virial kinetic energy)
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  gb_params P{};  // parameters in force for this context (copied at each call)
+
+  // trajectory state, layout r(3,na,nb)
+  double *p = nullptr, *r = nullptr, *dvdr = nullptr, *dvdr2 = nullptr;
+  double *rst = nullptr;   // bead positions scratch (swapped with r)
+  double *rnm = nullptr;   // normal-mode positions
+  double *mass = nullptr, *z = nullptr;
+  double box[3] = {0, 0, 0};
+
+  // force scratch
+  double *f_a = nullptr, *f_b = nullptr, *f_c = nullptr;  // bead-rep term forces [nb][na][3]
+  double *rb1 = nullptr, *fb1 = nullptr;  // contracted Ewald configurations and forces
+  double *rb2 = nullptr, *fb2 = nullptr;  // contracted LJ configurations and forces
+  double *fb3 = nullptr;                  // contracted TEM forces
+  double *g = nullptr;     // unit-box gradient scratch [nb][na][3]
+  double *rs = nullptr;    // site positions scratch [nb][na][3]
+  float4 *rs32 = nullptr;  // FP32 fractional coordinates for list prefilters [nb][na]
+  double *rc = nullptr;    // centroid scratch [na][3]
+  PairList pl;             // shared pair-list storage (re-sized on demand)
+  size_t pl_idx_bytes = 0, pl_cnt_bytes = 0;
+
+  // reciprocal space
+  int kmax_alloc = -1;
+  int nkxy = 0, nk = 0;          // (kx,ky) pairs and k vectors of the half space
+  int *kxy = nullptr;            // [nkxy][4]: kx, ky, kz_lo, kz_hi, sorted by kz range
+  int *kxy_koff = nullptr;       // [nkxy] offset of the pair's first k in the k list
+  int4 *klist = nullptr;         // [nk]: kx, ky, kz, pair index
+  double *sk_part = nullptr;     // [nconf][nchunk][nk][2]
+  double *sk = nullptr;          // [nconf][nk][2] weighted structure factors
+  size_t sk_part_bytes = 0, sk_bytes = 0;
+  double *kw = nullptr;          // [nk] weights (f / k^2) exp(-b k^2)
+
+  // tables and accumulators
+  double *tw_nb = nullptr, *tw_c1 = nullptr, *tw_c2 = nullptr;  // twiddles for nb, nbdf1, nbdf2
+  int tw_c1_n = 0, tw_c2_n = 0;
+  double *monod = nullptr;  // [nb][4][3]
+  double monod_dt = -1.0, monod_beta = -1.0;
+  double *acc = nullptr;    // ACC_NSLOT * ACC_STRIDE
+  unsigned *status = nullptr;
+  double *h_acc = nullptr;  // pinned host mirror
+  unsigned *h_status = nullptr;
+
+  // last step energies (host)
+  double e_v = 0, e_vew = 0, e_vlj = 0, e_vint = 0, e_tv = 0;
+  double e_vir[9] = {0}, e_vir_lf[9] = {0}, e_vir_hf[9] = {0};
+  double vir_lf_in[9] = {0};
+
+  int64_t launches = 0;
+  std::vector<void *> allocs;
+};
+
+// ---- context lifetime and helpers (api.cpp) ----
+int ctx_alloc(gb_context *c, int na, int nb);
+void ctx_free(gb_context *c);
+int ctx_set_error(int code, const std::string &msg);
+int ctx_check_cuda(cudaError_t e, const char *what);
+
+// ---- device orchestration (step.cu) ----
+int dev_prepare(gb_context *c, double dt, double beta);  // twiddles, monodromy, k lists
+int dev_full_forces(gb_context *c);                      // dvdr, dvdr2 from r
+int dev_evolve_pi(gb_context *c, double dt, double beta);
+int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt);  // drop-in `forces`
+int dev_collect(gb_context *c, int mode, double dt, double beta);  // sync, read accumulators

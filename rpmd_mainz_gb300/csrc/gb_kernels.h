@@ -1,0 +1,77 @@
+// gb_kernels.h -- launchers of the device kernels (host-callable).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gb_context.h"
+
+// Geometry of one pair search.  Point i of configuration c sits at
+// pos[c * cstride + i * pstride + {0,1,2}] (doubles).  `unit` selects the
+// unit-box minimum image dx - nint(dx) (rwald, ewald_cubic.f90:121-126);
+// otherwise dx - box * nint(dx / box) with dx/box computed as onbox * dx
+// (neigh_list.f90:336-342).  Membership is decided by the FP64 test
+// dx*dx + dy*dy + dz*dz < rcutsq rounded exactly as the reference rounds it.
+struct PairGeom {
+  const double *pos;
+  long long cstride;
+  int pstride;
+  int npt;
+  int unit;
+  double box[3], onbox[3];
+  double rcutsq;
+  int excl_mol;  // skip pairs with i/3 == j/3 (same molecule; TEM correction)
+};
+
+// ---- pair lists (k_pairs.cu) ----
+void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac);
+void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
+                       PairList &pl, unsigned *status);
+
+// ---- Ewald, unit box (k_pairs.cu, k_recip.cu) ----
+// rs: M-site substituted positions scaled by 1/L, [B][na][3]
+void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, double alpha,
+                  double scale);
+void launch_ewald_real(cudaStream_t s, const double *rs, const double *q, int na, int B,
+                       const PairList &pl, double alpha, double *g, double *acc);
+void launch_recip_sk(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);
+void launch_recip_weights(cudaStream_t s, gb_context *c, int B, double *acc);
+void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B,
+                        double *g);
+// out[b] = sign * chain_rule(scale * g[b]) (+= when accumulate)
+void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, int B, double alpha,
+                        double scale, double sign, int accumulate);
+
+// ---- Lennard-Jones O-O (k_pairs.cu) ----
+// r: [B][na][3] box units; list over oxygen points (shared if pl.nconf == 1)
+void launch_lj(cudaStream_t s, const double *r, int na, int B, const PairList &pl, double sigsq,
+               double rcutsq, const double *box, double dscale, double *out, double *acc);
+
+// ---- TEM-switched correction (k_pairs.cu) ----
+void launch_tem(cudaStream_t s, const double *rs, const double *q, int na, int B,
+                const PairList &pl, double sig, const double *box, double *g, double *acc);
+
+// ---- centroid of B configurations: rc = (sum_b r_b) / B, sequential in b ----
+void launch_centroid(cudaStream_t s, const double *r, double *rc, int na, int B);
+
+// ---- per-molecule terms (k_modes.cu) ----
+// model: 0 intra_harmonic, 1 intra_spcfw, 2 intra_morse_harm
+void launch_intra(cudaStream_t s, const double *r, double *out, int na, int B, int model,
+                  const gb_params &P, double *acc, int accumulate);
+void launch_virial_ke(cudaStream_t s, const double *r, const double *dvdr, const double *dvdr2,
+                      int na, int nb, double *acc);
+
+// ---- normal modes (k_modes.cu) ----
+void launch_realft(cudaStream_t s, const double *in, double *out, int m, int n, int mode,
+                   const double *tw);
+void launch_rotate(cudaStream_t s, double *p, double *r, const double *monod, int na, int nb);
+void launch_axpy(cudaStream_t s, double *y, const double *x, double a, long long n);
+void launch_copy(cudaStream_t s, double *dst, const double *src, long long n);
+void launch_ring_contract(cudaStream_t s, const double *rnm, double *rb, int na, int nb, int nbc,
+                          const double *tw_c);
+// dvdr (bead rep) = HC2R_nb( expand(fb1) + expand(fb2) ) [+ bead-rep extras], then
+// p -= halfdt * dvdr when p != nullptr
+void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int nbc1,
+                          const double *tw_c1, const double *fb2, int nbc2, const double *tw_c2,
+                          const double *e1, const double *e2, const double *e3, double *p,
+                          double halfdt, int na, int nb, const double *tw_nb);
+void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used);

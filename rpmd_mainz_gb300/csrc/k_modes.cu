@@ -1,0 +1,251 @@
+// k_modes.cu -- normal-mode transforms, free ring-polymer propagation,
+// ring-polymer contraction, intramolecular forces and the virial kinetic
+// energy estimator (FP64), one thread per coordinate row or per molecule.
+#include "gb_common.cuh"
+#include "gb_fft.cuh"
+#include "gb_intra.cuh"
+#include "gb_kernels.h"
+
+namespace {
+
+inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// realft on rows: data(m, n) column-major, row k = data[k + m*j] (fourier.f90:47-61)
+template <int N>
+__global__ void k_realft_pow2(const double *in, double *out, int m, int mode, const double *tw,
+                              double scale) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= m) return;
+  double x[N], y[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) x[j] = in[row + (long long)m * j];
+  if (mode == 1) gb_r2hc<N>(x, y, tw); else gb_hc2r<N>(x, y, tw);
+#pragma unroll
+  for (int j = 0; j < N; ++j) out[row + (long long)m * j] = scale * y[j];
+}
+
+constexpr int NMAX_DIRECT = 256;  // longest generic transform (fourier.f90:19, nmax)
+constexpr int NMAXC = 64;         // longest contracted ring on the device (nbdf1, nbdf2)
+
+__global__ void k_realft_direct(const double *in, double *out, int m, int n, int mode,
+                                const double *tw, double scale) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= m) return;
+  double x[NMAX_DIRECT], y[NMAX_DIRECT];
+  for (int j = 0; j < n; ++j) x[j] = in[row + (long long)m * j];
+  if (mode == 1) gb_r2hc_direct(x, y, n, tw); else gb_hc2r_direct(x, y, n, tw);
+  for (int j = 0; j < n; ++j) out[row + (long long)m * j] = scale * y[j];
+}
+
+// free ring-polymer step in normal modes (evolve_pi.f90:109-125):
+// p' = p m1 + r m2, r' = p m3 + r m4 with the atom type's monodromy of mode k
+__global__ void k_rotate(double *p, double *r, const double *monod, int na, int nb) {
+  const long long S = 3LL * na;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S * nb) return;
+  const int k = (int)(t / S);
+  const int row = (int)(t % S);
+  const int ic = (row / 3) % 3;
+  const double *m = monod + ic + 12 * k;  // monod(ic, c, k) at ic + 3*(c + 4*k)
+  const double pv = p[t], rv = r[t];
+  const double pprime = pv * m[0] + rv * m[3];
+  r[t] = pv * m[6] + rv * m[9];
+  p[t] = pprime;
+}
+
+__global__ void k_axpy(double *y, const double *x, double a, long long n) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] = y[t] + a * x[t];
+}
+
+__global__ void k_copy(double *dst, const double *src, long long n) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = src[t];
+}
+
+// ring_contract (evolve_pi.f90:405-431): keep modes 0, 1..h, nb-h..nb-1 of
+// rnm, HC2R of length nbc, scale 1/sqrt(nbc) then sqrt(nbc/nb)
+__global__ void k_ring_contract(const double *rnm, double *rb, int na, int nb, int nbc,
+                                const double *tw_c) {
+  const long long S = 3LL * na;
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= S) return;
+  double x[NMAXC], y[NMAXC];
+  const int h = (nbc - 1) / 2;
+  x[0] = rnm[row];
+  for (int k = 1; k <= h; ++k) {
+    x[k] = rnm[row + S * k];
+    x[nbc - k] = rnm[row + S * (nb - k)];
+  }
+  gb_hc2r_direct(x, y, nbc, tw_c);
+  const double s1 = sqrt(1.0 / (double)nbc), s2 = sqrt((double)nbc / (double)nb);
+  for (int j = 0; j < nbc; ++j) rb[row + S * j] = s2 * (s1 * y[j]);
+}
+
+// force_contract (evolve_pi.f90:377-403) of up to two contracted terms, sum in
+// normal modes, HC2R of length nb (evolve_pi.f90:238-247), bead-rep extras
+// added, optional kick p -= halfdt * dvdr (evolve_pi.f90:279)
+__global__ void k_expand_forces(double *dvdr, const double *fb1, int nbc1, const double *tw_c1,
+                                const double *fb2, int nbc2, const double *tw_c2, const double *e1,
+                                const double *e2, const double *e3, double *p, double halfdt,
+                                int na, int nb, const double *tw_nb) {
+  const long long S = 3LL * na;
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= S) return;
+  double xr[NMAXC / 2 + 1], xi[NMAXC / 2 + 1];  // X_k, k = 0..hmax
+  int hmax = 0;
+  double tmp[NMAXC], hc[NMAXC];
+  const double *fbs[2] = {fb1, fb2};
+  const int nbcs[2] = {nbc1, nbc2};
+  const double *tws[2] = {tw_c1, tw_c2};
+  for (int k = 0; k <= NMAXC / 2; ++k) xr[k] = xi[k] = 0.0;
+  for (int t = 0; t < 2; ++t) {
+    if (!fbs[t]) continue;
+    const int nbc = nbcs[t], h = (nbc - 1) / 2;
+    for (int j = 0; j < nbc; ++j) tmp[j] = fbs[t][row + S * j];
+    gb_r2hc_direct(tmp, hc, nbc, tws[t]);
+    const double s1 = sqrt(1.0 / (double)nbc), s2 = sqrt((double)nb / (double)nbc);
+    xr[0] += s2 * (s1 * hc[0]);
+    for (int k = 1; k <= h; ++k) {
+      xr[k] += s2 * (s1 * hc[k]);
+      xi[k] += s2 * (s1 * hc[nbc - k]);
+    }
+    hmax = max(hmax, h);
+  }
+  const double sc = sqrt(1.0 / (double)nb);
+  for (int j = 0; j < nb; ++j) {
+    double s = xr[0];
+    int m = 0;
+    for (int k = 1; k <= hmax; ++k) {
+      m += j;
+      if (m >= nb) m -= nb;
+      s += 2.0 * (xr[k] * tw_nb[m] - xi[k] * tw_nb[nb + m]);
+    }
+    double v = (fb1 || fb2) ? sc * s : 0.0;
+    const long long o = row + S * j;
+    if (e1) v += e1[o];
+    if (e2) v += e2[o];
+    if (e3) v += e3[o];
+    dvdr[o] = v;
+    if (p) p[o] = p[o] - halfdt * v;
+  }
+}
+
+// intramolecular forces on B configurations (potenl_opt iopt = 4 path)
+__global__ void __launch_bounds__(128) k_intra(const double *r, double *out, int nm, int B, int model,
+                                               IntraPar ip, double *acc, int accumulate) {
+  __shared__ double sh[32 * 10];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (t < (long long)nm * B) {
+    const double *x = r + t * 9;
+    double xl[9], f[9], vir[9];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) xl[d] = x[d];
+    vals[0] = intra_molecule(model, xl, f, vir, ip);
+#pragma unroll
+    for (int d = 0; d < 9; ++d) vals[1 + d] = vir[d];
+    double *o = out + t * 9;
+    if (accumulate) {
+#pragma unroll
+      for (int d = 0; d < 9; ++d) o[d] += f[d];
+    } else {
+#pragma unroll
+      for (int d = 0; d < 9; ++d) o[d] = f[d];
+    }
+  }
+  block_sum_atomic<10>(vals, sh, acc);
+}
+
+// virial_ke partial sums (kinetic.f90:1-54) per coordinate row:
+// acc[0] += sum (r - rc) dvdr, acc[1] += sum (r - rc) dvdr2, acc[2+xyz], acc[5+xyz]
+__global__ void __launch_bounds__(128) k_virial_ke(const double *r, const double *dvdr,
+                                                   const double *dvdr2, int na, int nb, double *acc) {
+  __shared__ double sh[32 * 8];
+  const long long S = 3LL * na;
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double vals[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (row < S) {
+    double rc = 0.0;
+    for (int k = 0; k < nb; ++k) rc = rc + r[row + S * k];
+    rc = rc / (double)nb;
+    double q1 = 0.0, q2 = 0.0;
+    for (int k = 0; k < nb; ++k) {
+      const double dr = r[row + S * k] - rc;
+      q1 += dr * dvdr[row + S * k];
+      q2 += dr * dvdr2[row + S * k];
+    }
+    const int x = (int)(row % 3);
+    vals[0] = q1;
+    vals[1] = q2;
+    vals[2 + x] = q1;
+    vals[5 + x] = q2;
+  }
+  block_sum_atomic<8>(vals, sh, acc);
+}
+
+}  // namespace
+
+void launch_realft(cudaStream_t s, const double *in, double *out, int m, int n, int mode,
+                   const double *tw) {
+  const double scale = sqrt(1.0 / (double)n);
+  const unsigned g = nblk(m, 128);
+  switch (n) {
+    case 1: k_copy<<<nblk(m, 256), 256, 0, s>>>(out, in, m); return;
+    case 2: k_realft_pow2<2><<<g, 128, 0, s>>>(in, out, m, mode, tw, scale); return;
+    case 4: k_realft_pow2<4><<<g, 128, 0, s>>>(in, out, m, mode, tw, scale); return;
+    case 8: k_realft_pow2<8><<<g, 128, 0, s>>>(in, out, m, mode, tw, scale); return;
+    case 16: k_realft_pow2<16><<<g, 128, 0, s>>>(in, out, m, mode, tw, scale); return;
+    case 32: k_realft_pow2<32><<<g, 128, 0, s>>>(in, out, m, mode, tw, scale); return;
+    case 64: k_realft_pow2<64><<<g, 64, 0, s>>>(in, out, m, mode, tw, scale); return;
+    default: k_realft_direct<<<nblk(m, 64), 64, 0, s>>>(in, out, m, n, mode, tw, scale); return;
+  }
+}
+
+void launch_rotate(cudaStream_t s, double *p, double *r, const double *monod, int na, int nb) {
+  long long n = 3LL * na * nb;
+  k_rotate<<<nblk(n, 256), 256, 0, s>>>(p, r, monod, na, nb);
+}
+
+void launch_axpy(cudaStream_t s, double *y, const double *x, double a, long long n) {
+  k_axpy<<<nblk(n, 256), 256, 0, s>>>(y, x, a, n);
+}
+
+void launch_copy(cudaStream_t s, double *dst, const double *src, long long n) {
+  k_copy<<<nblk(n, 256), 256, 0, s>>>(dst, src, n);
+}
+
+void launch_ring_contract(cudaStream_t s, const double *rnm, double *rb, int na, int nb, int nbc,
+                          const double *tw_c) {
+  long long n = 3LL * na;
+  k_ring_contract<<<nblk(n, 128), 128, 0, s>>>(rnm, rb, na, nb, nbc, tw_c);
+}
+
+void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int nbc1,
+                          const double *tw_c1, const double *fb2, int nbc2, const double *tw_c2,
+                          const double *e1, const double *e2, const double *e3, double *p,
+                          double halfdt, int na, int nb, const double *tw_nb) {
+  long long n = 3LL * na;
+  k_expand_forces<<<nblk(n, 64), 64, 0, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p,
+                                             halfdt, na, nb, tw_nb);
+}
+
+void launch_intra(cudaStream_t s, const double *r, double *out, int na, int B, int model,
+                  const gb_params &P, double *acc, int accumulate) {
+  IntraPar ip;
+  ip.reoh = P.reoh;
+  ip.theta = P.theta;
+  ip.rehh = 2.0 * sin(0.5 * P.theta) * P.reoh;
+  ip.apot = P.apot;
+  ip.bpot = P.bpot;
+  ip.alp = P.alp;
+  const int nm = na / 3;
+  long long n = (long long)nm * B;
+  k_intra<<<nblk(n, 128), 128, 0, s>>>(r, out, nm, B, model, ip, acc, accumulate);
+}
+
+void launch_virial_ke(cudaStream_t s, const double *r, const double *dvdr, const double *dvdr2,
+                      int na, int nb, double *acc) {
+  long long n = 3LL * na;
+  k_virial_ke<<<nblk(n, 128), 128, 0, s>>>(r, dvdr, dvdr2, na, nb, acc);
+}

@@ -1,0 +1,393 @@
+// k_pairs.cu -- pair lists and pair-force kernels (FP64).
+//
+// Pair lists.  The reference finds pairs through head/chain linked cells
+// (linked_cell.f90) or O(N^2) loops (neigh_list.f90, ewc_basic_tem); the set
+// of pairs is always "minimum-image distance below the cut-off", so the device
+// builds that set directly: a tiled all-pairs scan whose FP32 prefilter on
+// wrapped fractional coordinates rejects far pairs and accepts near ones, and
+// whose FP64 test, rounded exactly like the reference's
+// dx*dx + dy*dy + dz*dz < rcut*rcut, decides the pairs inside a narrow band
+// around the cut-off.  Each pair is stored once, in the list of i when
+// (i < j) == ((i + j) odd), which halves the lists and balances their lengths.
+//
+// Pair forces.  One thread per (configuration, point) walks its list, keeps the
+// point's own force in registers and scatters the partner's force with FP64
+// atomics; energy and virial are reduced per block and added to an
+// accumulator slot.
+#include "gb_common.cuh"
+#include "gb_kernels.h"
+
+namespace {
+
+constexpr int LB_T = 128;
+
+__global__ void k_frac32(PairGeom g, int nconf, float4 *frac) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nconf * g.npt) return;
+  int c = (int)(t / g.npt), i = (int)(t % g.npt);
+  const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
+  float f[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double u = g.unit ? x[d] : x[d] * g.onbox[d];
+    u -= floor(u);
+    float uf = (float)u;
+    f[d] = uf >= 1.0f ? 0.0f : uf;
+  }
+  frac[t] = make_float4(f[0], f[1], f[2], 0.0f);
+}
+
+// exact FP64 minimum-image test, rounded as the reference rounds it
+GB_D bool exact_pair_in(const PairGeom &g, const double *a, const double *b) {
+  double dx = __dsub_rn(a[0], b[0]), dy = __dsub_rn(a[1], b[1]), dz = __dsub_rn(a[2], b[2]);
+  if (g.unit) {
+    dx = __dsub_rn(dx, nint_d(dx));
+    dy = __dsub_rn(dy, nint_d(dy));
+    dz = __dsub_rn(dz, nint_d(dz));
+  } else {
+    dx = __dsub_rn(dx, __dmul_rn(g.box[0], nint_d(__dmul_rn(g.onbox[0], dx))));
+    dy = __dsub_rn(dy, __dmul_rn(g.box[1], nint_d(__dmul_rn(g.onbox[1], dy))));
+    dz = __dsub_rn(dz, __dmul_rn(g.box[2], nint_d(__dmul_rn(g.onbox[2], dz))));
+  }
+  return dsq3(dx, dy, dz) < g.rcutsq;
+}
+
+__global__ void __launch_bounds__(LB_T) k_build_list(PairGeom g, const float4 *frac, int *count,
+                                                     int *idx, int cap, float3 len, float thr_lo,
+                                                     float thr_hi, unsigned *status) {
+  __shared__ float4 tile[LB_T];
+  const int c = blockIdx.y;
+  const int i = blockIdx.x * LB_T + threadIdx.x;
+  const int npt = g.npt;
+  const float4 *fr = frac + (long long)c * npt;
+  const double *base = g.pos + c * g.cstride;
+  float4 fi = make_float4(0.f, 0.f, 0.f, 0.f);
+  double pi[3] = {0, 0, 0};
+  if (i < npt) {
+    fi = fr[i];
+    const double *x = base + (long long)i * g.pstride;
+    pi[0] = x[0];
+    pi[1] = x[1];
+    pi[2] = x[2];
+  }
+  int n = 0;
+  int *my = idx + ((long long)c * npt + (i < npt ? i : 0)) * cap;
+  for (int jt = 0; jt < npt; jt += LB_T) {
+    const int jl = jt + threadIdx.x;
+    tile[threadIdx.x] = jl < npt ? fr[jl] : make_float4(0.5f, 0.5f, 0.5f, 0.f);
+    __syncthreads();
+    if (i < npt) {
+      const int jmax = min(LB_T, npt - jt);
+      for (int jj = 0; jj < jmax; ++jj) {
+        const int j = jt + jj;
+        if (j == i) continue;
+        if ((i < j) != (((i + j) & 1) != 0)) continue;
+        if (g.excl_mol && (i / 3) == (j / 3)) continue;
+        const float4 fj = tile[jj];
+        float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
+        dx = (dx - rintf(dx)) * len.x;
+        dy = (dy - rintf(dy)) * len.y;
+        dz = (dz - rintf(dz)) * len.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 >= thr_hi) continue;
+        bool ok = d2 < thr_lo;
+        if (!ok) ok = exact_pair_in(g, pi, base + (long long)j * g.pstride);
+        if (ok) {
+          if (n < cap) my[n] = j;
+          ++n;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (i < npt) {
+    count[(long long)c * npt + i] = min(n, cap);
+    if (n > cap) atomicOr(status, ST_LIST_OVERFLOW);
+  }
+}
+
+// ---- M-site substitution and scaling (md_forces.f90:179-188, ewald_cubic.f90:20-22) ----
+__global__ void k_msite(const double *r, double *rs, int nm, int B, double alpha, double alpha2,
+                        double scale) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nm * B * 3) return;
+  const int d = (int)(t % 3);
+  const long long mb = t / 3;  // molecule index over all configurations
+  const double *m = r + mb * 9;
+  double *o = rs + mb * 9;
+  const double ro = alpha * m[d] + alpha2 * (m[3 + d] + m[6 + d]);
+  o[d] = scale * ro;
+  o[3 + d] = scale * m[3 + d];
+  o[6 + d] = scale * m[6 + d];
+}
+
+// out = sign * chain_rule(scale * g)  (md_forces.f90:206-215)
+__global__ void k_msite_chain(const double *g, double *out, int nm, int B, double alpha,
+                              double alpha2, double scale, double sign, int accumulate) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nm * B * 3) return;
+  const int d = (int)(t % 3);
+  const long long mb = t / 3;
+  const double *m = g + mb * 9;
+  double *o = out + mb * 9;
+  const double go = scale * m[d];
+  const double h1 = scale * m[3 + d] + alpha2 * go;
+  const double h2 = scale * m[6 + d] + alpha2 * go;
+  const double oo = alpha * go;
+  if (accumulate) {
+    o[d] += sign * oo;
+    o[3 + d] += sign * h1;
+    o[6 + d] += sign * h2;
+  } else {
+    o[d] = sign * oo;
+    o[3 + d] = sign * h1;
+    o[6 + d] = sign * h2;
+  }
+}
+
+// ---- real-space Ewald (rwald, ewald_cubic.f90:78-233) in the unit box ----
+__global__ void __launch_bounds__(128) k_ewald_real(const double *rs, const double *q, int na,
+                                                    const int *count, const int *idx, int cap,
+                                                    double alpha, double *g, double *acc) {
+  __shared__ double sh[32 * 10];
+  const double p = 3.0525860, a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741,
+               a4 = -1.453152027, a5 = 1.061405429;
+  const double sfac = -2.0 * alpha / sqrt(acos(-1.0));
+  const int c = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // v, vir(1..9) column-major
+  if (i < na) {
+    const double *R = rs + (long long)c * na * 3;
+    double *G = g + (long long)c * na * 3;
+    const double xi = R[3 * i], yi = R[3 * i + 1], zi = R[3 * i + 2], qi = q[i];
+    const int mi = i / 3;
+    const int n = count[(long long)c * na + i];
+    const int *L = idx + ((long long)c * na + i) * cap;
+    double fx = 0, fy = 0, fz = 0;
+    for (int t = 0; t < n; ++t) {
+      const int j = L[t];
+      double dx = xi - R[3 * j], dy = yi - R[3 * j + 1], dz = zi - R[3 * j + 2];
+      dx -= nint_d(dx);
+      dy -= nint_d(dy);
+      dz -= nint_d(dz);
+      const double drsq = dx * dx + dy * dy + dz * dz;
+      const double dr = sqrt(drsq);
+      const double x = alpha * dr;
+      const double e = exp(-x * x);
+      const double tt = p / (p + x);
+      double erfc = e * tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5))));
+      if (mi == j / 3) erfc -= 1.0;
+      const double du = erfc / dr;
+      const double dur = (sfac * e - du) / drsq;
+      const double qij = qi * q[j];
+      const double dv = qij * du, dvr = qij * dur;
+      const double dvx = dvr * dx, dvy = dvr * dy, dvz = dvr * dz;
+      fx += dvx;
+      fy += dvy;
+      fz += dvz;
+      atomicAdd(G + 3 * j, -dvx);
+      atomicAdd(G + 3 * j + 1, -dvy);
+      atomicAdd(G + 3 * j + 2, -dvz);
+      vals[0] += dv;
+      vals[1] += dx * dvx; vals[2] += dy * dvx; vals[3] += dz * dvx;
+      vals[4] += dx * dvy; vals[5] += dy * dvy; vals[6] += dz * dvy;
+      vals[7] += dx * dvz; vals[8] += dy * dvz; vals[9] += dz * dvz;
+    }
+    atomicAdd(G + 3 * i, fx);
+    atomicAdd(G + 3 * i + 1, fy);
+    atomicAdd(G + 3 * i + 2, fz);
+  }
+  block_sum_atomic<10>(vals, sh, acc);
+}
+
+// ---- Lennard-Jones O-O (lj_list / lj_basic / lj_cell, ljones.f90) ----
+// points are the oxygens; bead test with the same rounding as the reference
+__global__ void __launch_bounds__(128) k_lj(const double *r, int na, int npt, int nconf_list,
+                                            const int *count, const int *idx, int cap,
+                                            double sigsq, double rcutsq, double3 box, double3 onbox,
+                                            double dscale, double *out, double *acc) {
+  __shared__ double sh[32 * 10];
+  const int c = blockIdx.y;
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (o < npt) {
+    const double *R = r + (long long)c * na * 3;
+    double *F = out + (long long)c * na * 3;
+    const int lc = nconf_list == 1 ? 0 : c;
+    const int n = count[(long long)lc * npt + o];
+    const int *L = idx + ((long long)lc * npt + o) * cap;
+    const double xo = R[9 * o], yo = R[9 * o + 1], zo = R[9 * o + 2];
+    double fx = 0, fy = 0, fz = 0;
+    for (int t = 0; t < n; ++t) {
+      const int j = L[t];
+      double dx = __dsub_rn(R[9 * j], xo), dy = __dsub_rn(R[9 * j + 1], yo), dz = __dsub_rn(R[9 * j + 2], zo);
+      dx = __dsub_rn(dx, __dmul_rn(box.x, nint_d(__dmul_rn(onbox.x, dx))));
+      dy = __dsub_rn(dy, __dmul_rn(box.y, nint_d(__dmul_rn(onbox.y, dy))));
+      dz = __dsub_rn(dz, __dmul_rn(box.z, nint_d(__dmul_rn(onbox.z, dz))));
+      const double drsq = dsq3(dx, dy, dz);
+      if (drsq < rcutsq) {
+        const double onr2 = 1.0 / drsq;
+        const double sr2 = sigsq * onr2;
+        const double sr6 = sr2 * sr2 * sr2;
+        const double vij = sr6 * (sr6 - 1.0);
+        const double wij = sr6 * (sr6 - 0.5);
+        const double fij = wij * onr2;
+        const double dfx = fij * dx, dfy = fij * dy, dfz = fij * dz;
+        atomicAdd(F + 9 * j, -dscale * dfx);
+        atomicAdd(F + 9 * j + 1, -dscale * dfy);
+        atomicAdd(F + 9 * j + 2, -dscale * dfz);
+        fx += dfx;
+        fy += dfy;
+        fz += dfz;
+        vals[0] += vij;
+        vals[1] -= dx * dfx; vals[2] -= dy * dfx; vals[3] -= dz * dfx;
+        vals[4] -= dx * dfy; vals[5] -= dy * dfy; vals[6] -= dz * dfy;
+        vals[7] -= dx * dfz; vals[8] -= dy * dfz; vals[9] -= dz * dfz;
+      }
+    }
+    atomicAdd(F + 9 * o, dscale * fx);
+    atomicAdd(F + 9 * o + 1, dscale * fy);
+    atomicAdd(F + 9 * o + 2, dscale * fz);
+  }
+  block_sum_atomic<10>(vals, sh, acc);
+}
+
+// ---- TEM-switched correction (ewc_basic_tem / ewc_list_tem, correct_tem.f90) ----
+__global__ void __launch_bounds__(128) k_tem(const double *rs, const double *q, int na,
+                                             int nconf_list, const int *count, const int *idx,
+                                             int cap, double rcutsq, double ta1, double ta2,
+                                             double ta3, double3 box, double3 onbox, double *g,
+                                             double *acc) {
+  __shared__ double sh[32 * 10];
+  const int c = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (i < na) {
+    const double *R = rs + (long long)c * na * 3;
+    double *G = g + (long long)c * na * 3;
+    const int lc = nconf_list == 1 ? 0 : c;
+    const int n = count[(long long)lc * na + i];
+    const int *L = idx + ((long long)lc * na + i) * cap;
+    const double xo = R[3 * i], yo = R[3 * i + 1], zo = R[3 * i + 2], qo = q[i];
+    double fx = 0, fy = 0, fz = 0;
+    for (int t = 0; t < n; ++t) {
+      const int j = L[t];
+      double dx = __dsub_rn(R[3 * j], xo), dy = __dsub_rn(R[3 * j + 1], yo), dz = __dsub_rn(R[3 * j + 2], zo);
+      dx = __dsub_rn(dx, __dmul_rn(box.x, nint_d(__dmul_rn(onbox.x, dx))));
+      dy = __dsub_rn(dy, __dmul_rn(box.y, nint_d(__dmul_rn(onbox.y, dy))));
+      dz = __dsub_rn(dz, __dmul_rn(box.z, nint_d(__dmul_rn(onbox.z, dz))));
+      const double drsq = dsq3(dx, dy, dz);
+      if (drsq < rcutsq) {
+        const double dr = sqrt(drsq);
+        const double onr = 1.0 / dr;
+        const double zij = q[j] * qo;
+        const double vc = zij * onr;
+        const double dvc = -vc * onr;
+        const double dr3 = drsq * dr, dr4 = dr3 * dr;
+        const double f = 1.0 - ta1 * dr + ta2 * dr3 - ta3 * dr4;
+        const double df = -ta1 + 3.0 * ta2 * drsq - 4.0 * ta3 * dr3;
+        const double dv = vc * f;
+        const double dvr = vc * df + dvc * f;
+        const double dvx = dvr * dx * onr, dvy = dvr * dy * onr, dvz = dvr * dz * onr;
+        atomicAdd(G + 3 * j, dvx);
+        atomicAdd(G + 3 * j + 1, dvy);
+        atomicAdd(G + 3 * j + 2, dvz);
+        fx -= dvx;
+        fy -= dvy;
+        fz -= dvz;
+        vals[0] += dv;
+        vals[1] += dx * dvx; vals[2] += dy * dvx; vals[3] += dz * dvx;
+        vals[4] += dx * dvy; vals[5] += dy * dvy; vals[6] += dz * dvy;
+        vals[7] += dx * dvz; vals[8] += dy * dvz; vals[9] += dz * dvz;
+      }
+    }
+    atomicAdd(G + 3 * i, fx);
+    atomicAdd(G + 3 * i + 1, fy);
+    atomicAdd(G + 3 * i + 2, fz);
+  }
+  block_sum_atomic<10>(vals, sh, acc);
+}
+
+// centroid rc = (sum_b r_b) / B per coordinate row, beads summed in order
+__global__ void k_centroid(const double *r, double *rc, int na, int B) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long S = 3LL * na;
+  if (t >= S) return;
+  double s = 0.0;
+  for (int b = 0; b < B; ++b) s = s + r[t + S * b];
+  rc[t] = s / (double)B;
+}
+
+inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac) {
+  long long n = (long long)nconf * g.npt;
+  k_frac32<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac);
+}
+
+void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
+                       PairList &pl, unsigned *status) {
+  float3 len;
+  double lmax;
+  if (g.unit) {
+    len = make_float3(1.f, 1.f, 1.f);
+    lmax = 1.0;
+  } else {
+    len = make_float3((float)g.box[0], (float)g.box[1], (float)g.box[2]);
+    lmax = fmax(g.box[0], fmax(g.box[1], g.box[2]));
+  }
+  // FP32 error of d^2 is below 1e-6 * lmax^2 for wrapped fractional coordinates;
+  // pairs within 4e-6 * lmax^2 of the cut-off go to the exact FP64 test
+  const double band = 4e-6 * lmax * lmax;
+  const float thr_lo = (float)(g.rcutsq - band), thr_hi = (float)(g.rcutsq + band);
+  dim3 grid(nblk(g.npt, LB_T), nconf);
+  k_build_list<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status);
+}
+
+void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, double alpha,
+                  double scale) {
+  int nm = na / 3;
+  long long n = (long long)nm * B * 3;
+  k_msite<<<nblk(n, 256), 256, 0, s>>>(r, rs, nm, B, alpha, 0.5 * (1.0 - alpha), scale);
+}
+
+void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, int B, double alpha,
+                        double scale, double sign, int accumulate) {
+  int nm = na / 3;
+  long long n = (long long)nm * B * 3;
+  k_msite_chain<<<nblk(n, 256), 256, 0, s>>>(g, out, nm, B, alpha, 0.5 * (1.0 - alpha), scale, sign,
+                                             accumulate);
+}
+
+void launch_ewald_real(cudaStream_t s, const double *rs, const double *q, int na, int B,
+                       const PairList &pl, double alpha, double *g, double *acc) {
+  dim3 grid(nblk(na, 128), B);
+  k_ewald_real<<<grid, 128, 0, s>>>(rs, q, na, pl.count, pl.idx, pl.cap, alpha, g, acc);
+}
+
+void launch_lj(cudaStream_t s, const double *r, int na, int B, const PairList &pl, double sigsq,
+               double rcutsq, const double *box, double dscale, double *out, double *acc) {
+  int npt = na / 3;
+  dim3 grid(nblk(npt, 128), B);
+  double3 bx = make_double3(box[0], box[1], box[2]);
+  double3 ob = make_double3(1.0 / box[0], 1.0 / box[1], 1.0 / box[2]);
+  k_lj<<<grid, 128, 0, s>>>(r, na, npt, pl.nconf, pl.count, pl.idx, pl.cap, sigsq, rcutsq, bx, ob,
+                            dscale, out, acc);
+}
+
+void launch_tem(cudaStream_t s, const double *rs, const double *q, int na, int B,
+                const PairList &pl, double sig, const double *box, double *g, double *acc) {
+  dim3 grid(nblk(na, 128), B);
+  double3 bx = make_double3(box[0], box[1], box[2]);
+  double3 ob = make_double3(1.0 / box[0], 1.0 / box[1], 1.0 / box[2]);
+  const double a1 = 2.0 / sig, a2 = 2.0 / (sig * sig * sig), a3 = 1.0 / (sig * sig * sig * sig);
+  k_tem<<<grid, 128, 0, s>>>(rs, q, na, pl.nconf, pl.count, pl.idx, pl.cap, sig * sig, a1, a2, a3,
+                             bx, ob, g, acc);
+}
+
+void launch_centroid(cudaStream_t s, const double *r, double *rc, int na, int B) {
+  long long n = 3LL * na;
+  k_centroid<<<nblk(n, 256), 256, 0, s>>>(r, rc, na, B);
+}

@@ -1,0 +1,416 @@
+// k_rattle.cu -- RATTLE and the rigid ring-polymer step on the device (FP64).
+//
+// rattle_s1 / rattle_s2 (md_rattle.f90:33-271): three distance constraints per
+// water (O-H1, O-H2, H1-H2; rattle_setup, md_rattle.f90:1-31), relative
+// tolerance 1e-6, Gauss-Seidel sweeps over the molecule's bonds, at most 1000
+// sweeps.  Molecules are independent, so one thread takes one molecule of one
+// bead and runs the reference's sweep sequence.  The reference's constraint
+// virial keeps a running quirk: vir(1,3) = vir(1,2) - gdx*dz is assigned, not
+// accumulated, so the final vir(1,3) is vir(1,2) at the last correction minus
+// that correction's term (md_rattle.f90:124, 233).  Each thread records its
+// molecule's sums and last correction; a per-bead reduction rebuilds the value.
+// The reference stops when the LAST molecule's sweep count reaches the limit
+// (the counter is reset per molecule, md_rattle.f90:149, 258); the device
+// raises the same status.
+//
+// evolve_rig_pi (evolve_rigid.f90:100-224): the nb velocity-Verlet substeps
+// with primitive bead springs (bead_forces, evolve_rigid.f90:226-278) and
+// RATTLE touch only one molecule's beads, so one block holds whole ring
+// polymers and runs all substeps; the springs exchange bead positions through
+// shared memory.
+#include <cmath>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "gb_context.h"
+#include "gb_kernels.h"
+
+namespace {
+
+constexpr int ITMAX = 1000;
+constexpr double RTOL = 1e-6;
+
+struct RatPar {
+  double rcb[3];  // squared constrained lengths: reoh^2, reoh^2, rehh^2
+  double rm[3];   // 1/mass of O, H1, H2
+};
+
+// bond b of a molecule: atoms (ii, jj)
+GB_D void bond_atoms(int b, int &ii, int &jj) {
+  ii = b == 2 ? 1 : 0;
+  jj = b == 0 ? 1 : 2;
+}
+
+// one molecule, stage 1; returns sweeps used; rec[0..4] = v11, v12, v22, v33, v23
+// sums, rec[5] = last gdx*dz term, rec[6] = 1 if any correction
+GB_D int rattle1_mol(double *r, const double *rold, double *p, double *f, double dt,
+                     const RatPar &rp, double *rec) {
+  bool done = false;
+  int it = 0;
+  while (!done && it < ITMAX) {
+    done = true;
+    for (int b = 0; b < 3; ++b) {
+      int ii, jj;
+      bond_atoms(b, ii, jj);
+      const double dx1 = r[3 * jj] - r[3 * ii], dy1 = r[3 * jj + 1] - r[3 * ii + 1], dz1 = r[3 * jj + 2] - r[3 * ii + 2];
+      const double d2 = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;
+      const double diff = rp.rcb[b] - d2;
+      if (fabs(diff) > rp.rcb[b] * RTOL) {
+        const double rm1 = rp.rm[jj], rm2 = rp.rm[ii];
+        const double dx2 = rold[3 * jj] - rold[3 * ii], dy2 = rold[3 * jj + 1] - rold[3 * ii + 1],
+                     dz2 = rold[3 * jj + 2] - rold[3 * ii + 2];
+        const double dot = dx1 * dx2 + dy1 * dy2 + dz1 * dz2;
+        const double gamma = diff / (2.0 * (rm1 + rm2) * dot);
+        double gdx = gamma * dx2, gdy = gamma * dy2, gdz = gamma * dz2;
+        r[3 * jj] += rm1 * gdx; r[3 * jj + 1] += rm1 * gdy; r[3 * jj + 2] += rm1 * gdz;
+        r[3 * ii] -= rm2 * gdx; r[3 * ii + 1] -= rm2 * gdy; r[3 * ii + 2] -= rm2 * gdz;
+        gdx = gdx / dt; gdy = gdy / dt; gdz = gdz / dt;
+        p[3 * jj] += gdx; p[3 * jj + 1] += gdy; p[3 * jj + 2] += gdz;
+        p[3 * ii] -= gdx; p[3 * ii + 1] -= gdy; p[3 * ii + 2] -= gdz;
+        gdx = 2.0 * gdx; gdy = 2.0 * gdy; gdz = 2.0 * gdz;
+        rec[0] -= gdx * dx2;
+        rec[1] -= gdx * dy2;
+        rec[5] = gdx * dz2;
+        rec[6] = 1.0;
+        rec[4] -= gdy * dz2;
+        rec[2] -= gdy * dy2;
+        rec[3] -= gdz * dz2;
+        f[3 * jj] += gdx; f[3 * jj + 1] += gdy; f[3 * jj + 2] += gdz;
+        f[3 * ii] -= gdx; f[3 * ii + 1] -= gdy; f[3 * ii + 2] -= gdz;
+        done = false;
+      }
+    }
+    ++it;
+  }
+  return it;
+}
+
+// one molecule, stage 2 (velocity constraints)
+GB_D int rattle2_mol(const double *r, double *p, double *f, double dt, const RatPar &rp,
+                     double *rec) {
+  const double halfdt = 0.5 * dt;
+  bool done = false;
+  int it = 0;
+  while (!done && it <= ITMAX) {
+    done = true;
+    for (int b = 0; b < 3; ++b) {
+      int ii, jj;
+      bond_atoms(b, ii, jj);
+      const double dx1 = r[3 * jj] - r[3 * ii], dy1 = r[3 * jj + 1] - r[3 * ii + 1], dz1 = r[3 * jj + 2] - r[3 * ii + 2];
+      const double rm1 = rp.rm[jj], rm2 = rp.rm[ii];
+      const double dvx1 = p[3 * jj] * rm1 - p[3 * ii] * rm2;
+      const double dvy1 = p[3 * jj + 1] * rm1 - p[3 * ii + 1] * rm2;
+      const double dvz1 = p[3 * jj + 2] * rm1 - p[3 * ii + 2] * rm2;
+      const double dot = dx1 * dvx1 + dy1 * dvy1 + dz1 * dvz1;
+      const double gamma = -dot / ((rm1 + rm2) * rp.rcb[b]);
+      if (fabs(gamma) > RTOL) {
+        double gdx = gamma * dx1, gdy = gamma * dy1, gdz = gamma * dz1;
+        p[3 * jj] += gdx; p[3 * jj + 1] += gdy; p[3 * jj + 2] += gdz;
+        p[3 * ii] -= gdx; p[3 * ii + 1] -= gdy; p[3 * ii + 2] -= gdz;
+        gdx = gdx / halfdt; gdy = gdy / halfdt; gdz = gdz / halfdt;
+        rec[0] -= gdx * dx1;
+        rec[1] -= gdx * dy1;
+        rec[5] = gdx * dz1;
+        rec[6] = 1.0;
+        rec[4] -= gdy * dz1;
+        rec[2] -= gdy * dy1;
+        rec[3] -= gdz * dz1;
+        f[3 * jj] += gdx; f[3 * jj + 1] += gdy; f[3 * jj + 2] += gdz;
+        f[3 * ii] -= gdx; f[3 * ii + 1] -= gdy; f[3 * ii + 2] -= gdz;
+        done = false;
+      }
+    }
+    ++it;
+  }
+  return it;
+}
+
+// RATTLE on B beads x nm molecules; records[b][m][8]
+__global__ void k_rattle(int stage, double *r, const double *rold, double *p, double *f, int nm,
+                         int B, double dt, RatPar rp, double *records, unsigned *status) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nm * B) return;
+  const int m = (int)(t % nm);
+  double rl[9], pl[9], fl[9], ro[9];
+  double rec[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < 9; ++d) {
+    rl[d] = r[t * 9 + d];
+    pl[d] = p[t * 9 + d];
+    fl[d] = f[t * 9 + d];
+  }
+  int it;
+  if (stage == 1) {
+#pragma unroll
+    for (int d = 0; d < 9; ++d) ro[d] = rold[t * 9 + d];
+    it = rattle1_mol(rl, ro, pl, fl, dt, rp, rec);
+    if (m == nm - 1 && it >= ITMAX) atomicOr(status, ST_RATTLE1);
+  } else {
+    it = rattle2_mol(rl, pl, fl, dt, rp, rec);
+    if (m == nm - 1 && it >= ITMAX) atomicOr(status, ST_RATTLE2);
+  }
+#pragma unroll
+  for (int d = 0; d < 9; ++d) {
+    r[t * 9 + d] = rl[d];
+    p[t * 9 + d] = pl[d];
+    f[t * 9 + d] = fl[d];
+  }
+  double *o = records + t * 8;
+#pragma unroll
+  for (int d = 0; d < 8; ++d) o[d] = rec[d];
+}
+
+// per-bead constraint virial with the running vir(1,3) of the reference;
+// vir_out[b][9] (written, or added with weight `w` when accumulate)
+__global__ void k_rattle_virial(const double *records, int nm, int B, double *vir_out, double w,
+                                int accumulate) {
+  const int b = blockIdx.x;
+  __shared__ double sh[5][256];
+  __shared__ int shlast[256];
+  double s[5] = {0, 0, 0, 0, 0};
+  int last = -1;
+  for (int m = threadIdx.x; m < nm; m += blockDim.x) {
+    const double *rec = records + ((long long)b * nm + m) * 8;
+#pragma unroll
+    for (int d = 0; d < 5; ++d) s[d] += rec[d];
+    if (rec[6] != 0.0) last = m;
+  }
+#pragma unroll
+  for (int d = 0; d < 5; ++d) sh[d][threadIdx.x] = s[d];
+  shlast[threadIdx.x] = last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot[5] = {0, 0, 0, 0, 0};
+    int lm = -1;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+#pragma unroll
+      for (int d = 0; d < 5; ++d) tot[d] += sh[d][t];
+      lm = max(lm, shlast[t]);
+    }
+    const double v13 = lm >= 0 ? tot[1] - records[((long long)b * nm + lm) * 8 + 5] : 0.0;
+    double v[9];
+    v[0] = tot[0];            // (1,1)
+    v[3] = tot[1];            // (1,2)
+    v[6] = v13;               // (1,3)
+    v[4] = tot[2];            // (2,2)
+    v[8] = tot[3];            // (3,3)
+    v[7] = tot[4];            // (2,3)
+    v[1] = v[3];              // (2,1) = (1,2)
+    v[2] = v[6];              // (3,1) = (1,3)
+    v[5] = v[7];              // (3,2) = (2,3)
+    double *o = vir_out + (accumulate ? 0 : (long long)b * 9);
+    if (accumulate) {
+      for (int d = 0; d < 9; ++d) atomicAdd(o + d, w * v[d]);
+    } else {
+      for (int d = 0; d < 9; ++d) o[d] = v[d];
+    }
+  }
+}
+
+// evolve_rig_pi substeps (evolve_rigid.f90:132-170) for whole ring polymers:
+// thread = (molecule, bead), block = mpb molecules x nb beads
+__global__ void k_rig_substeps(double *r, double *p, double *f2, int nm, int nb, int mpb, double smalldt,
+                               double omegan2, RatPar rp, const double *mass3, unsigned *status) {
+  extern __shared__ double shr[];  // [mpb][nb][9]
+  const int ml = threadIdx.x / nb, k = threadIdx.x % nb;
+  const int m = blockIdx.x * mpb + ml;
+  const bool valid = ml < mpb && m < nm;
+  const double halfsmalldt = 0.5 * smalldt;
+  double rl[9], pl[9], fl[9], ro[9], rec[8];
+  const long long S = 9LL * nm;  // doubles per bead
+  if (valid) {
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+      rl[d] = r[S * k + 9LL * m + d];
+      pl[d] = p[S * k + 9LL * m + d];
+    }
+  }
+  auto springs = [&]() {
+    if (valid) {
+#pragma unroll
+      for (int d = 0; d < 9; ++d) shr[(ml * nb + k) * 9 + d] = rl[d];
+    }
+    __syncthreads();
+    if (valid) {
+      const int km = k == 0 ? nb - 1 : k - 1, kp = k == nb - 1 ? 0 : k + 1;
+#pragma unroll
+      for (int d = 0; d < 9; ++d) {
+        const double x1 = rl[d], x2 = shr[(ml * nb + km) * 9 + d], x3 = shr[(ml * nb + kp) * 9 + d];
+        fl[d] = nb > 1 ? mass3[d / 3] * omegan2 * (2.0 * x1 - x2 - x3) : 0.0;
+      }
+    }
+    __syncthreads();
+  };
+  springs();
+  for (int is = 0; is < nb; ++is) {
+    if (valid) {
+#pragma unroll
+      for (int d = 0; d < 9; ++d) {
+        ro[d] = rl[d];
+        pl[d] = pl[d] - halfsmalldt * fl[d];
+        rl[d] = rl[d] + pl[d] * smalldt / mass3[d / 3];
+      }
+#pragma unroll
+      for (int d = 0; d < 8; ++d) rec[d] = 0.0;
+      const int it = rattle1_mol(rl, ro, pl, fl, smalldt, rp, rec);
+      if (m == nm - 1 && it >= ITMAX) atomicOr(status, ST_RATTLE1);
+    }
+    springs();
+    if (valid) {
+#pragma unroll
+      for (int d = 0; d < 9; ++d) pl[d] = pl[d] - halfsmalldt * fl[d];
+#pragma unroll
+      for (int d = 0; d < 8; ++d) rec[d] = 0.0;
+      const int it = rattle2_mol(rl, pl, fl, smalldt, rp, rec);
+      if (m == nm - 1 && it >= ITMAX) atomicOr(status, ST_RATTLE2);
+    }
+  }
+  if (valid) {
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+      r[S * k + 9LL * m + d] = rl[d];
+      p[S * k + 9LL * m + d] = pl[d];
+      f2[S * k + 9LL * m + d] = fl[d];
+    }
+  }
+}
+
+inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+const gb_params &current_params();  // api.cpp
+
+namespace {
+
+// drop-in single-bead calls share one small device workspace
+struct RattleWs {
+  int nm = 0;
+  double *r = nullptr, *rold = nullptr, *p = nullptr, *f = nullptr, *rec = nullptr, *vir = nullptr;
+  double *mass = nullptr;
+  unsigned *status = nullptr;
+  cudaStream_t s = nullptr;
+} g_ws;
+
+RatPar make_rp(const gb_params &P, const double *mass3) {
+  RatPar rp;
+  const double rehh = 2.0 * std::sin(0.5 * P.theta) * P.reoh;
+  rp.rcb[0] = P.reoh * P.reoh;
+  rp.rcb[1] = P.reoh * P.reoh;
+  rp.rcb[2] = rehh * rehh;
+  for (int i = 0; i < 3; ++i) rp.rm[i] = 1.0 / mass3[i];
+  return rp;
+}
+
+#define CK(x)                                             \
+  do {                                                    \
+    cudaError_t e_ = (x);                                 \
+    if (e_ != cudaSuccess) return ctx_check_cuda(e_, #x); \
+  } while (0)
+
+int ws_ensure(int nm) {
+  if (g_ws.nm >= nm && g_ws.r) return GB_OK;
+  for (void *q : {(void *)g_ws.r, (void *)g_ws.rold, (void *)g_ws.p, (void *)g_ws.f, (void *)g_ws.rec,
+                  (void *)g_ws.vir, (void *)g_ws.status})
+    if (q) cudaFree(q);
+  const size_t n = 9 * (size_t)nm;
+  CK(cudaMalloc(&g_ws.r, sizeof(double) * n));
+  CK(cudaMalloc(&g_ws.rold, sizeof(double) * n));
+  CK(cudaMalloc(&g_ws.p, sizeof(double) * n));
+  CK(cudaMalloc(&g_ws.f, sizeof(double) * n));
+  CK(cudaMalloc(&g_ws.rec, sizeof(double) * 8 * (size_t)nm));
+  CK(cudaMalloc(&g_ws.vir, sizeof(double) * 9));
+  CK(cudaMalloc(&g_ws.status, sizeof(unsigned)));
+  CK(cudaMemset(g_ws.status, 0, sizeof(unsigned)));
+  if (!g_ws.s) CK(cudaStreamCreateWithFlags(&g_ws.s, cudaStreamNonBlocking));
+  g_ws.nm = nm;
+  return GB_OK;
+}
+
+int rattle_dropin(int stage, double *r, const double *rold, double *p, int nm, const double *mass,
+                  double dt, double *dvdr, double *vir, int na) {
+  if (na != 3 * nm) return ctx_set_error(GB_E_ARG, "na must be 3*nm");
+  const gb_params &P = current_params();
+  if (3 * nm != P.nctot) return ctx_set_error(GB_E_ARG, "number of bonds inconsistent in shake/rattle routine");
+  int st = ws_ensure(nm);
+  if (st) return st;
+  const size_t n = 9 * (size_t)nm;
+  cudaStream_t s = g_ws.s;
+  CK(cudaMemcpyAsync(g_ws.r, r, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  if (stage == 1) CK(cudaMemcpyAsync(g_ws.rold, rold, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(g_ws.p, p, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(g_ws.f, dvdr, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  RatPar rp = make_rp(P, mass);
+  k_rattle<<<nblk(nm, 128), 128, 0, s>>>(stage, g_ws.r, g_ws.rold, g_ws.p, g_ws.f, nm, 1, dt, rp,
+                                         g_ws.rec, g_ws.status);
+  k_rattle_virial<<<1, 256, 0, s>>>(g_ws.rec, nm, 1, g_ws.vir, 1.0, 0);
+  if (stage == 1) CK(cudaMemcpyAsync(r, g_ws.r, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(p, g_ws.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(dvdr, g_ws.f, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(vir, g_ws.vir, sizeof(double) * 9, cudaMemcpyDeviceToHost, s));
+  unsigned stw = 0;
+  CK(cudaMemcpyAsync(&stw, g_ws.status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (stw) {
+    CK(cudaMemset(g_ws.status, 0, sizeof(unsigned)));
+    return stage == 1 ? ctx_set_error(GB_E_RATTLE1, "max iterations exceeded in rattle stage 1")
+                      : ctx_set_error(GB_E_RATTLE2, "max iterations exceeded in rattle stage 2");
+  }
+  return GB_OK;
+}
+
+}  // namespace
+
+int dev_rattle_setup(int nm, const gb_params &P) {
+  (void)P;
+  if (3 * nm > 5000) return ctx_set_error(GB_E_ARG, "rattle: 3*nm exceeds nbondmax = 5000 (globals.inc:26)");
+  return ws_ensure(nm);
+}
+
+int dev_rattle_s1(double *r, const double *rold, double *p, int nm, const double *mass, double dt,
+                  double *dvdr, double *vir, int na) {
+  return rattle_dropin(1, r, rold, p, nm, mass, dt, dvdr, vir, na);
+}
+
+int dev_rattle_s2(double *r, double *p, int nm, const double *mass, double dt, double *dvdr,
+                  double *vir, int na) {
+  return rattle_dropin(2, r, nullptr, p, nm, mass, dt, dvdr, vir, na);
+}
+
+int term_forces_rigid(gb_context *c);  // step.cpp: forces(r, v, dvdr, nb, ..., 1)
+
+int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) {
+  (void)vir_inout;
+  if (c->P.therm == GB_THERM_PRG || c->P.therm == GB_THERM_PRL)
+    return ctx_set_error(GB_E_UNSUPPORTED, "PRG/PRL thermostat kicks are not on the device path");
+  if (3 * c->nm != c->P.nctot) return ctx_set_error(GB_E_ARG, "number of bonds inconsistent in shake/rattle routine");
+  const int nb = c->nb, nm = c->nm;
+  const long long N = 3LL * c->na * nb;
+  cudaStream_t s = c->stream;
+  double mass3h[3];
+  CK(cudaMemcpy(mass3h, c->mass, sizeof(double) * 3, cudaMemcpyDeviceToHost));
+  RatPar rp = make_rp(c->P, mass3h);
+  const double halfdt = 0.5 * dt, smalldt = dt / (double)nb;
+  double omegan = nb / (beta * 1.0);
+  omegan = omegan * omegan;
+  // p -= dt/2 dvdr (evolve_rigid.f90:132)
+  launch_axpy(s, c->p, c->dvdr, -halfdt, N);
+  const int mpb = nb >= 128 ? 1 : 128 / nb;
+  const size_t smem = sizeof(double) * 9 * (size_t)mpb * nb;
+  k_rig_substeps<<<nblk(nm, mpb), mpb * nb, smem, s>>>(c->r, c->p, c->dvdr2, nm, nb, mpb, smalldt,
+                                                      omegan, rp, c->mass, c->status);
+  // intermolecular forces on all beads (evolve_rigid.f90:174)
+  int st = term_forces_rigid(c);
+  if (st) return st;
+  // p -= dt/2 dvdr; rattle stage 2 with dt, constraint virial (evolve_rigid.f90:181-190)
+  launch_axpy(s, c->p, c->dvdr, -halfdt, N);
+  double *rec = c->g;  // nb*nm*8 <= 3*na*nb doubles
+  k_rattle<<<nblk((long long)nm * nb, 128), 128, 0, s>>>(2, c->r, nullptr, c->p, c->dvdr, nm, nb, dt, rp,
+                                                        rec, c->status);
+  double *vslot = c->acc + (size_t)ACC_INT * ACC_STRIDE;
+  k_rattle_virial<<<nb, 256, 0, s>>>(rec, nm, nb, vslot + 1, 1.0, 1);
+  c->plan.B_int = nb;  // vir_hf = sum_k vir_k / nb (evolve_rigid.f90:198)
+  CK(cudaMemsetAsync(c->dvdr2, 0, sizeof(double) * N, s));
+  c->launches += 6;
+  return GB_OK;
+}

@@ -1,0 +1,577 @@
+// step.cpp -- host orchestration of the device RPMD path.
+//
+// dev_forces      <- forces      (md_forces.f90:1-110)
+// dev_full_forces <- full_forces (md_forces.f90:305-472)
+// dev_evolve_pi   <- evolve_pi   (evolve_pi.f90:1-322)
+// Every kernel is launched on the context's stream; the energies are summed on
+// the device into accumulator slots and turned into the reference's bead-averaged
+// energies and virials by dev_collect after one synchronisation.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "gb_common.h"
+#include "gb_context.h"
+#include "gb_kernels.h"
+
+// from k_recip.cu
+size_t recip_sk_smem(int kmax, int nkxy);
+size_t recip_force_smem(int kmax);
+int recip_sk_chunk();
+void recip_set_attributes(size_t sk_smem, size_t f_smem);
+
+namespace {
+
+const double PI = 3.141592653589793238462643383279502884;
+
+#define CK(x)                                             \
+  do {                                                    \
+    cudaError_t e_ = (x);                                 \
+    if (e_ != cudaSuccess) return ctx_check_cuda(e_, #x); \
+  } while (0)
+
+double *slot(gb_context *c, int s) { return c->acc + (size_t)s * ACC_STRIDE; }
+
+std::vector<double> twiddles(int n) {
+  std::vector<double> t(2 * (size_t)n);
+  for (int m = 0; m < n; ++m) {
+    double a = 2.0 * PI * (double)m / (double)n;
+    t[m] = std::cos(a);
+    t[n + m] = std::sin(a);
+  }
+  return t;
+}
+
+int upload_tw(gb_context *c, double **dst, int n) {
+  std::vector<double> t = twiddles(n);
+  if (*dst) cudaFree(*dst);
+  CK(cudaMalloc(dst, sizeof(double) * t.size()));
+  CK(cudaMemcpyAsync(*dst, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return GB_OK;
+}
+
+// ring_rpmd (md_pathi.f90:190-231) on the host; monod(ic, c, k) at ic + 3*(c + 4*k)
+void ring_rpmd_host(const double *mass3, int nb, double dt, double beta, double *monod) {
+  const double hbar = 1.0;
+  for (int j = 0; j < 3; ++j) {
+    monod[j + 3 * (0 + 4 * 0)] = 1.0;
+    monod[j + 3 * (1 + 4 * 0)] = 0.0;
+    monod[j + 3 * (2 + 4 * 0)] = dt / mass3[j];
+    monod[j + 3 * (3 + 4 * 0)] = 1.0;
+    if (nb > 1) {
+      double betan = beta / (double)nb;
+      double twown = 2.0 / (betan * hbar);
+      double pibyn = std::acos(-1.0) / (double)nb;
+      for (int k = 1; k <= nb / 2; ++k) {
+        double wk = twown * std::sin(k * pibyn);
+        double wt = wk * dt, wm = wk * mass3[j];
+        double cwt = std::cos(wt), swt = std::sin(wt);
+        monod[j + 3 * (0 + 4 * k)] = cwt;
+        monod[j + 3 * (1 + 4 * k)] = -wm * swt;
+        monod[j + 3 * (2 + 4 * k)] = swt / wm;
+        monod[j + 3 * (3 + 4 * k)] = cwt;
+      }
+      for (int k = 1; k <= (nb - 1) / 2; ++k)
+        for (int cc = 0; cc < 4; ++cc) monod[j + 3 * (cc + 4 * (nb - k))] = monod[j + 3 * (cc + 4 * k)];
+    }
+  }
+}
+
+// half-space k vectors with the reference's loop-exit membership
+// (ewald_cubic.f90:292-520), grouped in (kx, ky) columns
+int build_kvectors(gb_context *c) {
+  const int kmax = c->P.kmax;
+  const double rlat = 2.0 * PI;
+  const double rkmax2 = c->P.rkmax * c->P.rkmax;
+  const double b = 0.25 / (c->P.walpha * c->P.walpha);
+  struct Col { int kx, ky, lo, hi; };
+  std::vector<Col> cols;
+  for (int kx = 0; kx <= kmax; ++kx) {
+    const double rkx = rlat * kx;
+    int kz0 = 0;  // ky = 0: kz = 1.. while rkx^2 + rkz^2 <= rkmax2
+    for (int kz = 1; kz <= kmax; ++kz) {
+      double rkz = rlat * kz;
+      if (rkx * rkx + rkz * rkz > rkmax2) break;
+      kz0 = kz;
+    }
+    if (kx > 0) cols.push_back({kx, 0, -kz0, kz0});
+    else if (kz0 > 0) cols.push_back({0, 0, 1, kz0});
+    for (int ky = 1; ky <= kmax; ++ky) {
+      const double rky = rlat * ky;
+      if (rkx * rkx + rky * rky > rkmax2) break;
+      int kzm = 0;
+      for (int kz = 1; kz <= kmax; ++kz) {
+        double rkz = rlat * kz;
+        if (rkx * rkx + rky * rky + rkz * rkz > rkmax2) break;
+        kzm = kz;
+      }
+      cols.push_back({kx, ky, -kzm, kzm});
+      if (kx > 0) cols.push_back({kx, -ky, -kzm, kzm});
+    }
+  }
+  std::stable_sort(cols.begin(), cols.end(), [](const Col &a, const Col &b2) {
+    return (a.hi - a.lo) > (b2.hi - b2.lo);
+  });
+  std::vector<int> kxy(4 * cols.size()), koff(cols.size());
+  std::vector<int> klist;
+  std::vector<double> kw;
+  int nk = 0;
+  for (size_t p = 0; p < cols.size(); ++p) {
+    const Col &cl = cols[p];
+    kxy[4 * p] = cl.kx; kxy[4 * p + 1] = cl.ky; kxy[4 * p + 2] = cl.lo; kxy[4 * p + 3] = cl.hi;
+    koff[p] = nk;
+    for (int kz = cl.lo; kz <= cl.hi; ++kz) {
+      klist.push_back(cl.kx); klist.push_back(cl.ky); klist.push_back(kz); klist.push_back((int)p);
+      double rkx = rlat * cl.kx, rky = rlat * cl.ky, rkz = rlat * kz;
+      double rk2 = rkx * rkx + rky * rky + rkz * rkz;
+      double f = 2.0 * rlat;  // 4 pi: each k stands for k and -k
+      kw.push_back((f / rk2) * std::exp(-b * rk2));
+      ++nk;
+    }
+  }
+  for (void *p : {(void *)c->kxy, (void *)c->kxy_koff, (void *)c->klist, (void *)c->kw})
+    if (p) cudaFree(p);
+  c->nkxy = (int)cols.size();
+  c->nk = nk;
+  CK(cudaMalloc(&c->kxy, sizeof(int) * kxy.size()));
+  CK(cudaMalloc(&c->kxy_koff, sizeof(int) * koff.size()));
+  CK(cudaMalloc(&c->klist, sizeof(int) * klist.size()));
+  CK(cudaMalloc(&c->kw, sizeof(double) * kw.size()));
+  CK(cudaMemcpy(c->kxy, kxy.data(), sizeof(int) * kxy.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->kxy_koff, koff.data(), sizeof(int) * koff.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->klist, klist.data(), sizeof(int) * klist.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->kw, kw.data(), sizeof(double) * kw.size(), cudaMemcpyHostToDevice));
+  // partial structure factors for up to nb configurations
+  const int nchunk = (c->na + recip_sk_chunk() - 1) / recip_sk_chunk();
+  size_t part = sizeof(double) * 2 * (size_t)nk * nchunk * std::max(c->nb, 1);
+  size_t skb = sizeof(double) * 2 * (size_t)nk * std::max(c->nb, 1);
+  if (c->sk_part) cudaFree(c->sk_part);
+  if (c->sk) cudaFree(c->sk);
+  CK(cudaMalloc(&c->sk_part, part));
+  CK(cudaMalloc(&c->sk, skb));
+  c->sk_part_bytes = part;
+  c->sk_bytes = skb;
+  if (c->nkxy > 1024 || recip_sk_smem(kmax, c->nkxy) > 227 * 1024 || recip_force_smem(kmax) > 227 * 1024)
+    return ctx_set_error(GB_E_UNSUPPORTED, "kmax too large for the reciprocal-space kernels");
+  recip_set_attributes(recip_sk_smem(kmax, c->nkxy), recip_force_smem(kmax));
+  c->kmax_alloc = kmax;
+  return GB_OK;
+}
+
+// pair-list storage of at least nconf x npt x cap entries
+int ensure_list(gb_context *c, int nconf, int npt, int cap) {
+  size_t need_idx = sizeof(int) * (size_t)nconf * npt * cap;
+  size_t need_cnt = sizeof(int) * (size_t)nconf * npt;
+  if (need_idx > c->pl_idx_bytes) {
+    if (c->pl.idx) cudaFree(c->pl.idx);
+    c->pl.idx = nullptr;
+    CK(cudaMalloc(&c->pl.idx, need_idx));
+    c->pl_idx_bytes = need_idx;
+  }
+  if (need_cnt > c->pl_cnt_bytes) {
+    if (c->pl.count) cudaFree(c->pl.count);
+    c->pl.count = nullptr;
+    CK(cudaMalloc(&c->pl.count, need_cnt));
+    c->pl_cnt_bytes = need_cnt;
+  }
+  c->pl.nconf = nconf;
+  c->pl.npt = npt;
+  c->pl.cap = cap;
+  return GB_OK;
+}
+
+// partners expected within rc for npt points in volume vol, doubled plus margin
+int list_cap(int npt, double rc, double vol) {
+  double full = (double)npt * (4.0 / 3.0) * PI * rc * rc * rc / vol;
+  int cap = (int)(1.1 * full) + 48;
+  return std::min(cap, std::max(npt, 1));
+}
+
+double boxmin(const gb_context *c) { return std::min(c->box[0], std::min(c->box[1], c->box[2])); }
+double boxmax(const gb_context *c) { return std::max(c->box[0], std::max(c->box[1], c->box[2])); }
+
+// ---- one force term on B configurations ----
+
+int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, int accumulate, int s) {
+  if (!c->P.iamcub) return ctx_set_error(GB_E_UNSUPPORTED, "non-cubic Ewald (ewald_nc) is not on the device path");
+  if (c->P.wm > 0.0 || c->P.wh > 0.0) return ctx_set_error(GB_E_UNSUPPORTED, "smeared-charge Ewald is not on the device path");
+  const int na = c->na;
+  const double L = c->box[0], onboxl = 1.0 / L;
+  launch_msite(c->stream, r, c->rs, na, B, c->P.alpha, onboxl);
+  CK(cudaMemsetAsync(c->g, 0, sizeof(double) * 3 * (size_t)na * B, c->stream));
+  PairGeom g{};
+  g.pos = c->rs;
+  g.cstride = 3LL * na;
+  g.pstride = 3;
+  g.npt = na;
+  g.unit = 1;
+  g.box[0] = g.box[1] = g.box[2] = 1.0;
+  g.onbox[0] = g.onbox[1] = g.onbox[2] = 1.0;
+  g.rcutsq = c->P.wrcut * c->P.wrcut;
+  g.excl_mol = 0;
+  int st = ensure_list(c, B, na, list_cap(na, c->P.wrcut, 1.0));
+  if (st) return st;
+  launch_frac32(c->stream, g, B, c->rs32);
+  launch_build_list(c->stream, g, B, c->rs32, c->pl, c->status);
+  launch_ewald_real(c->stream, c->rs, c->z, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
+  launch_recip_sk(c->stream, c, c->rs, c->z, B);
+  launch_recip_weights(c->stream, c, B, slot(c, s));
+  launch_recip_force(c->stream, c, c->rs, c->z, B, c->g);
+  launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, onboxl * onboxl, sign, accumulate);
+  c->launches += 8;
+  return GB_OK;
+}
+
+int term_lj(gb_context *c, const double *r, int B, double *out, int accumulate, int s) {
+  if (c->P.oo_gam != 0.0) return ctx_set_error(GB_E_UNSUPPORTED, "Buckingham O-O is not on the device path");
+  const int na = c->na, nm = c->nm;
+  if (!accumulate) CK(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)na * B, c->stream));
+  PairGeom g{};
+  g.pstride = 9;
+  g.npt = nm;
+  g.unit = 0;
+  for (int d = 0; d < 3; ++d) {
+    g.box[d] = c->box[d];
+    g.onbox[d] = 1.0 / c->box[d];
+  }
+  g.excl_mol = 0;
+  const double vol = c->box[0] * c->box[1] * c->box[2];
+  int nconf;
+  if (B > 3) {  // centroid neighbour list (md_forces.f90:34-53)
+    launch_centroid(c->stream, r, c->rc, na, B);
+    const double cut = std::min(c->P.rcut, 0.5 * boxmin(c));
+    g.pos = c->rc;
+    g.cstride = 0;
+    g.rcutsq = cut * cut;
+    nconf = 1;
+    int st = ensure_list(c, 1, nm, list_cap(nm, cut, vol));
+    if (st) return st;
+    c->launches += 1;
+  } else {  // lj_basic / lj_cell: every pair within rcut, bead by bead
+    g.pos = r;
+    g.cstride = 3LL * na;
+    g.rcutsq = c->P.rcut * c->P.rcut;
+    nconf = B;
+    int st = ensure_list(c, B, nm, list_cap(nm, c->P.rcut, vol));
+    if (st) return st;
+  }
+  launch_frac32(c->stream, g, nconf, c->rs32);
+  launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
+  launch_lj(c->stream, r, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut, c->box,
+            48.0 * c->P.oo_eps, out, slot(c, s));
+  c->launches += 3;
+  return GB_OK;
+}
+
+int term_tem(gb_context *c, const double *r, int B, double *out, double sign, int accumulate, int s) {
+  if (c->P.wm > 0.0 || c->P.wh > 0.0) return ctx_set_error(GB_E_UNSUPPORTED, "ewc_correction not yet implemented for smeared charges");
+  const int na = c->na;
+  const double sig = c->P.sig;
+  const double alpha = std::fabs(c->P.alpha - 1.0) > 1e-4 ? c->P.alpha : 1.0;
+  const double vol = c->box[0] * c->box[1] * c->box[2];
+  PairGeom g{};
+  g.npt = na;
+  g.unit = 0;
+  g.pstride = 3;
+  for (int d = 0; d < 3; ++d) {
+    g.box[d] = c->box[d];
+    g.onbox[d] = 1.0 / c->box[d];
+  }
+  g.excl_mol = 1;
+  launch_msite(c->stream, r, c->rs, na, B, alpha, 1.0);
+  int nconf;
+  if (B > 1) {  // centroid list, cut sig + 5 bohr (md_forces.f90:69-89) -> ewc_list_tem
+    if (sig > 0.5 * boxmax(c)) return ctx_set_error(GB_E_CUTOFF, "ewc_list : rcut too large");
+    double cut = sig + 5.0;
+    if (cut > 0.5 * boxmin(c)) cut = std::min(cut, 0.5 * boxmin(c));
+    launch_centroid(c->stream, r, c->rc, na, B);
+    g.pos = c->rc;
+    g.cstride = 0;
+    g.rcutsq = cut * cut;
+    nconf = 1;
+    int st = ensure_list(c, 1, na, list_cap(na, cut, vol));
+    if (st) return st;
+    c->launches += 1;
+  } else {  // ewc_basic_tem / ewc_cell_tem on the M-site positions
+    if (3.0 * sig > boxmax(c)) {
+      if (sig > 0.5 * boxmax(c)) return ctx_set_error(GB_E_CUTOFF, "ewc_basic : rcut too large");
+    } else if (sig > 0.5 * boxmin(c)) {
+      return ctx_set_error(GB_E_CUTOFF, "ewc_basic : rcut too large");
+    }
+    g.pos = c->rs;
+    g.cstride = 3LL * na;
+    g.rcutsq = sig * sig;
+    nconf = B;
+    int st = ensure_list(c, B, na, list_cap(na, sig, vol));
+    if (st) return st;
+  }
+  CK(cudaMemsetAsync(c->g, 0, sizeof(double) * 3 * (size_t)na * B, c->stream));
+  launch_frac32(c->stream, g, nconf, c->rs32);
+  launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
+  launch_tem(c->stream, c->rs, c->z, na, B, c->pl, sig, c->box, c->g, slot(c, s));
+  launch_msite_chain(c->stream, c->g, out, na, B, alpha, 1.0, sign, accumulate);
+  c->launches += 5;
+  return GB_OK;
+}
+
+int intra_model(const gb_params &P) {
+  if (P.intra_model == GB_INTRA_SPCFW) return 1;
+  if (P.alp == 0.0) return 0;
+  return 2;
+}
+
+int term_intra(gb_context *c, const double *r, int B, double *out, int accumulate, int s) {
+  if (c->P.intra_model != GB_INTRA_SPCFW && c->P.alp != 0.0 && c->P.alpb != 0.0)
+    return ctx_set_error(GB_E_UNSUPPORTED, "intra_morse is not on the device path");
+  launch_intra(c->stream, r, out, c->na, B, intra_model(c->P), c->P, slot(c, s), accumulate);
+  c->launches += 1;
+  return GB_OK;
+}
+
+// low-frequency forces of full_forces / evolve_pi: contracted terms from rnm,
+// bead-representation terms from r; dvdr = expand + extras, optional kick
+int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, double halfdt) {
+  const int nb = c->nb, na = c->na;
+  const int nbdf1 = c->P.nbdf1, nbdf2 = c->P.nbdf2;
+  const double sig = c->P.sig;
+  const bool con1 = nb > 1 && nbdf1 > 0, con2 = nb > 1 && nbdf2 > 0;
+  int st;
+  if (con1) {
+    if ((nbdf1 - 1) % 2 != 0) return ctx_set_error(GB_E_CONTRACT, "* Beadiabatic factor must be ODD");
+    launch_ring_contract(c->stream, rnm, c->rb1, na, nb, nbdf1, c->tw_c1);
+    if ((st = term_ewald(c, c->rb1, nbdf1, c->fb1, 1.0, 0, ACC_EW))) return st;
+    c->plan.B_ew = nbdf1;
+    if (sig > 0.0) {
+      if ((st = term_tem(c, c->rb1, nbdf1, c->fb1, -1.0, 1, ACC_TEM))) return st;
+      c->plan.B_tem = nbdf1;
+    }
+    c->launches += 1;
+  }
+  if (con2) {
+    if ((nbdf2 - 1) % 2 != 0) return ctx_set_error(GB_E_CONTRACT, "* Beadiabatic factor must be ODD");
+    launch_ring_contract(c->stream, rnm, c->rb2, na, nb, nbdf2, c->tw_c2);
+    if ((st = term_lj(c, c->rb2, nbdf2, c->fb2, 0, ACC_LJ))) return st;
+    c->plan.B_lj = nbdf2;
+    c->launches += 1;
+  }
+  const double *e1 = nullptr, *e2 = nullptr, *e3 = nullptr;
+  if (nb == 1 || nbdf1 <= 0) {
+    if ((st = term_ewald(c, r, nb, c->f_a, 1.0, 0, ACC_EW2))) return st;
+    c->plan.B_ew2 = nb;
+    e1 = c->f_a;
+  } else if (sig > 0.0) {
+    if ((st = term_tem(c, r, nb, c->f_b, 1.0, 0, ACC_TEM2))) return st;
+    c->plan.B_tem2 = nb;
+    e2 = c->f_b;
+  }
+  if (nb == 1 || nbdf2 <= 0) {
+    if ((st = term_lj(c, r, nb, c->f_c, 0, ACC_LJ2))) return st;
+    c->plan.B_lj2 = nb;
+    e3 = c->f_c;
+  }
+  launch_expand_forces(c->stream, c->dvdr, con1 ? c->fb1 : nullptr, nbdf1, c->tw_c1,
+                       con2 ? c->fb2 : nullptr, nbdf2, c->tw_c2, e1, e2, e3, p, halfdt, na, nb,
+                       c->tw_nb);
+  c->launches += 1;
+  return GB_OK;
+}
+
+}  // namespace
+
+int dev_prepare(gb_context *c, double dt, double beta) {
+  int st;
+  if (!c->tw_nb && (st = upload_tw(c, &c->tw_nb, c->nb))) return st;
+  if (c->P.nbdf1 > 0 && c->tw_c1_n != c->P.nbdf1) {
+    if (c->P.nbdf1 > 63 || c->P.nbdf1 > c->nb) return ctx_set_error(GB_E_ARG, "RP contraction beads must not exceed nb (and 63 on the device)");
+    if ((st = upload_tw(c, &c->tw_c1, c->P.nbdf1))) return st;
+    c->tw_c1_n = c->P.nbdf1;
+  }
+  if (c->P.nbdf2 > 0 && c->tw_c2_n != c->P.nbdf2) {
+    if (c->P.nbdf2 > 63 || c->P.nbdf2 > c->nb) return ctx_set_error(GB_E_ARG, "RP contraction beads must not exceed nb (and 63 on the device)");
+    if ((st = upload_tw(c, &c->tw_c2, c->P.nbdf2))) return st;
+    c->tw_c2_n = c->P.nbdf2;
+  }
+  if (c->kmax_alloc != c->P.kmax) {
+    if ((st = build_kvectors(c))) return st;
+  }
+  if (dt > 0.0 && (dt != c->monod_dt || beta != c->monod_beta)) {
+    double mass3[3];
+    CK(cudaMemcpy(mass3, c->mass, sizeof(double) * 3, cudaMemcpyDeviceToHost));
+    std::vector<double> monod(12 * (size_t)c->nb);
+    ring_rpmd_host(mass3, c->nb, dt / (double)c->P.mts, beta, monod.data());
+    CK(cudaMemcpy(c->monod, monod.data(), sizeof(double) * monod.size(), cudaMemcpyHostToDevice));
+    c->monod_dt = dt;
+    c->monod_beta = beta;
+  }
+  return GB_OK;
+}
+
+int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt) {
+  int st;
+  if ((st = dev_prepare(c, 0.0, 0.0))) return st;
+  c->plan = EnergyPlan();
+  CK(cudaMemsetAsync(c->acc, 0, sizeof(double) * ACC_NSLOT * ACC_STRIDE, c->stream));
+  CK(cudaMemsetAsync(out, 0, sizeof(double) * 3 * (size_t)c->na * B, c->stream));
+  if (iopt == 5) {
+    if ((st = term_tem(c, r, B, out, 1.0, 1, ACC_TEM2))) return st;
+    c->plan.B_tem2 = B;
+    return GB_OK;
+  }
+  if (iopt < 0 || iopt > 4) return ctx_set_error(GB_E_UNSUPPORTED, "iopt not on the device path");
+  if (iopt <= 2) {
+    if ((st = term_ewald(c, r, B, out, 1.0, 1, ACC_EW2))) return st;
+    c->plan.B_ew2 = B;
+  }
+  if (iopt == 0 || iopt == 1 || iopt == 3) {
+    if ((st = term_lj(c, r, B, out, 1, ACC_LJ2))) return st;
+    c->plan.B_lj2 = B;
+  }
+  if (iopt == 0 || iopt == 4) {
+    if ((st = term_intra(c, r, B, out, 1, ACC_INT))) return st;
+    c->plan.B_int = B;
+  }
+  return GB_OK;
+}
+
+int dev_full_forces(gb_context *c) {
+  int st;
+  if ((st = dev_prepare(c, 0.0, 0.0))) return st;
+  c->plan = EnergyPlan();
+  const int nb = c->nb, na = c->na;
+  CK(cudaMemsetAsync(c->acc, 0, sizeof(double) * ACC_NSLOT * ACC_STRIDE, c->stream));
+  if ((st = term_intra(c, c->r, nb, c->dvdr2, 0, ACC_INT))) return st;
+  c->plan.B_int = nb;
+  const bool contract = nb > 1 && (c->P.nbdf1 > 0 || c->P.nbdf2 > 0);
+  if (contract) {
+    launch_realft(c->stream, c->r, c->rnm, 3 * na, nb, +1, c->tw_nb);
+    c->launches += 1;
+  }
+  return low_frequency(c, c->rnm, c->r, nullptr, 0.0);
+}
+
+int dev_evolve_pi(gb_context *c, double dt, double beta) {
+  int st;
+  if (c->P.therm == GB_THERM_PRG || c->P.therm == GB_THERM_PRL)
+    return ctx_set_error(GB_E_UNSUPPORTED, "PRG/PRL thermostat kicks are not on the device path");
+  if ((st = dev_prepare(c, dt, beta))) return st;
+  c->plan = EnergyPlan();
+  c->plan.evolve = 1;
+  c->last_beta = beta;
+  const int nb = c->nb, na = c->na, mts = c->P.mts;
+  c->plan.mts = mts;
+  const long long N = 3LL * na * nb;
+  const double dtsmall = dt / (double)mts, halfdtsmall = 0.5 * dtsmall, halfdt = 0.5 * dt;
+  cudaStream_t s = c->stream;
+  CK(cudaMemsetAsync(c->acc, 0, sizeof(double) * ACC_NSLOT * ACC_STRIDE, s));
+  // evolve_pi.f90:82-88
+  launch_axpy(s, c->p, c->dvdr, -halfdt, N);
+  launch_axpy(s, c->p, c->dvdr2, -halfdtsmall, N);
+  launch_realft(s, c->p, c->p, 3 * na, nb, +1, c->tw_nb);
+  launch_realft(s, c->r, c->rnm, 3 * na, nb, +1, c->tw_nb);
+  c->launches += 4;
+  // multiple time steps under the intramolecular force (evolve_pi.f90:93-161)
+  for (int im = 1; im <= mts; ++im) {
+    launch_rotate(s, c->p, c->rnm, c->monod, na, nb);
+    launch_realft(s, c->rnm, c->rst, 3 * na, nb, -1, c->tw_nb);
+    CK(cudaMemsetAsync(slot(c, ACC_INT), 0, sizeof(double), s));  // vint of the last substep
+    if ((st = term_intra(c, c->rst, nb, c->dvdr2, 0, ACC_INT))) return st;
+    launch_virial_ke(s, c->rst, c->dvdr, c->dvdr2, na, nb, slot(c, ACC_KE));
+    c->launches += 3;
+    if (im != mts) {
+      launch_realft(s, c->dvdr2, c->dvdr2, 3 * na, nb, +1, c->tw_nb);
+      launch_axpy(s, c->p, c->dvdr2, -dtsmall, N);
+      c->launches += 2;
+    }
+  }
+  c->plan.B_int = nb;
+  // momenta back to beads; r := rst (evolve_pi.f90:222-228)
+  launch_realft(s, c->p, c->p, 3 * na, nb, -1, c->tw_nb);
+  std::swap(c->r, c->rst);
+  launch_axpy(s, c->p, c->dvdr2, -halfdtsmall, N);
+  c->launches += 2;
+  // low-frequency forces and the closing kick (evolve_pi.f90:194-279)
+  return low_frequency(c, c->rnm, c->r, c->p, halfdt);
+}
+
+// forces(r, v, dvdr, nb, ..., iopt = 1) of evolve_rig_pi (evolve_rigid.f90:174)
+int term_forces_rigid(gb_context *c) {
+  int st;
+  if ((st = dev_prepare(c, 0.0, 0.0))) return st;
+  c->plan = EnergyPlan();
+  CK(cudaMemsetAsync(c->acc, 0, sizeof(double) * ACC_NSLOT * ACC_STRIDE, c->stream));
+  if ((st = term_ewald(c, c->r, c->nb, c->dvdr, 1.0, 0, ACC_EW2))) return st;
+  c->plan.B_ew2 = c->nb;
+  if ((st = term_lj(c, c->r, c->nb, c->dvdr, 1, ACC_LJ2))) return st;
+  c->plan.B_lj2 = c->nb;
+  return GB_OK;
+}
+
+int dev_collect(gb_context *c, int mode, double dt, double beta) {
+  (void)dt;
+  (void)beta;
+  CK(cudaMemcpyAsync(c->h_acc, c->acc, sizeof(double) * ACC_NSLOT * ACC_STRIDE, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(c->h_status, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  unsigned stw = *c->h_status;
+  if (stw) {
+    CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+    if (stw & ST_LIST_OVERFLOW) return ctx_set_error(GB_E_LIST, "neighbour list too small");
+    if (stw & ST_RATTLE1) return ctx_set_error(GB_E_RATTLE1, "max iterations exceeded in rattle stage 1");
+    if (stw & ST_RATTLE2) return ctx_set_error(GB_E_RATTLE2, "max iterations exceeded in rattle stage 2");
+    return ctx_set_error(GB_E_NONFINITE, "device status error");
+  }
+  const double *A = c->h_acc;
+  auto S = [&](int s) { return A + (size_t)s * ACC_STRIDE; };
+  const double L = c->box[0];
+  const double qq = c->qq;
+  const double vself = c->P.walpha / std::sqrt(PI) * qq;
+  const EnergyPlan &pl = c->plan;
+  double vew = 0.0, vlj = 0.0, vint = 0.0;
+  double vir_ew[9] = {0}, vir_lj[9] = {0}, vir_int[9] = {0};
+  auto add_ewald = [&](int s, int B) {
+    if (!B) return;
+    vew += (S(s)[0] - B * vself) / L / B;
+    for (int i = 0; i < 9; ++i) vir_ew[i] += S(s)[1 + i] / L / B;
+  };
+  auto add_tem = [&](int s, int B, double sign) {
+    if (!B) return;
+    vew += sign * S(s)[0] / B;
+    for (int i = 0; i < 9; ++i) vir_ew[i] += sign * S(s)[1 + i] / B;
+  };
+  auto add_lj = [&](int s, int B) {
+    if (!B) return;
+    vlj += 4.0 * c->P.oo_eps * S(s)[0] / B;
+    for (int i = 0; i < 9; ++i) vir_lj[i] += 48.0 * c->P.oo_eps * S(s)[1 + i] / B;
+  };
+  add_ewald(ACC_EW, pl.B_ew);
+  add_tem(ACC_TEM, pl.B_tem, -1.0);
+  add_ewald(ACC_EW2, pl.B_ew2);
+  add_tem(ACC_TEM2, pl.B_tem2, 1.0);
+  add_lj(ACC_LJ, pl.B_lj);
+  add_lj(ACC_LJ2, pl.B_lj2);
+  if (pl.B_int) {
+    vint = S(ACC_INT)[0] / pl.B_int;
+    double div = pl.evolve ? (double)pl.mts : 1.0;
+    for (int i = 0; i < 9; ++i) vir_int[i] = S(ACC_INT)[1 + i] / pl.B_int / div;
+  }
+  c->e_vew = vew;
+  c->e_vlj = vlj;
+  c->e_vint = vint;
+  c->e_v = vew + vlj + vint;
+  for (int i = 0; i < 9; ++i) {
+    c->e_vir_lf[i] = vir_lj[i] + vir_ew[i];
+    c->e_vir_hf[i] = vir_int[i];
+    c->e_vir[i] = c->e_vir_lf[i] + c->e_vir_hf[i];
+  }
+  if (pl.evolve) {
+    const int nb = c->nb;
+    double tq1 = 0.5 * S(ACC_KE)[0] / nb, tq2 = 0.5 * S(ACC_KE)[1] / nb;
+    double tc = 0.5 * (3 * c->na - 3 - c->P.nctot) / c->last_beta;
+    c->e_tv = tc + (tq1 + tq2) / pl.mts;
+  }
+  (void)mode;
+  return GB_OK;
+}

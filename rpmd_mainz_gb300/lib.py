@@ -1,0 +1,252 @@
+"""ctypes bindings of libgbrpmd.so with the reference's call signatures.
+
+The functions below mirror the Fortran routines the library replaces
+(md_forces.f90 `forces` / `full_forces`, evolve_pi.f90 `evolve_pi`,
+md_rattle.f90 `rattle_setup` / `rattle_s1` / `rattle_s2`, evolve_rigid.f90
+`evolve_rig_pi`): same arguments, same meaning, arrays shaped (nb, na, 3) in
+numpy, which is the memory order of the Fortran r(3, na, nb).  A non-zero
+status from the library raises GbError with the library's message, as the
+reference would `stop`.
+
+`load()` fails loudly when the library has not been built; there is no
+fallback implementation.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from .abi import GbParams, STATUS_NAMES
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgbrpmd.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "gbrpmd.h")
+
+_lib = None
+
+D = C.POINTER(C.c_double)
+I = C.POINTER(C.c_int)
+
+
+class GbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gbrpmd error {code} ({STATUS_NAMES.get(code, '?')}): {msg}")
+        self.code = code
+
+
+def header_functions():
+    """Names of every function declared in include/gbrpmd.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbrpmd_\w+)\s*\(", text)))
+
+
+def load(path=None):
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
+    lib.gbrpmd_last_error.restype = C.c_char_p
+    lib.gbrpmd_ran2.restype = C.c_double
+    lib.gbrpmd_ran2.argtypes = [I, D, D]
+    lib.gbrpmd_gaussian.restype = C.c_double
+    lib.gbrpmd_gaussian.argtypes = [I, D]
+    lib.gbrpmd_ctx_stream.restype = C.c_void_p
+    lib.gbrpmd_ctx_stream.argtypes = [C.c_void_p]
+    lib.gbrpmd_ctx_launch_count.restype = C.c_int64
+    lib.gbrpmd_ctx_launch_count.argtypes = [C.c_void_p]
+    lib.gbrpmd_ctx_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, D, D]
+    for name in ["gbrpmd_ctx_destroy", "gbrpmd_ctx_sync"]:
+        getattr(lib, name).argtypes = [C.c_void_p]
+    lib.gbrpmd_ctx_upload.argtypes = [C.c_void_p, D, D, D, D, D]
+    lib.gbrpmd_ctx_download.argtypes = [C.c_void_p, D, D, D, D]
+    lib.gbrpmd_ctx_full_forces.argtypes = [C.c_void_p, D, D, D, D, D]
+    lib.gbrpmd_ctx_evolve.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
+    lib.gbrpmd_ctx_energies.argtypes = [C.c_void_p, D, D, D]
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(D)
+
+
+def _check(st):
+    if st != 0:
+        raise GbError(st, load().gbrpmd_last_error().decode())
+
+
+def _arr(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def init(params: GbParams):
+    _check(load().gbrpmd_init(C.byref(params)))
+
+
+def get_params() -> GbParams:
+    p = GbParams()
+    _check(load().gbrpmd_get_params(C.byref(p)))
+    return p
+
+
+def finalize():
+    _check(load().gbrpmd_finalize())
+
+
+def forces(r, box, z, iopt):
+    """forces(r,v,dvdr,nb,na,boxlxyz,z,virial,iopt) -> (v, dvdr, virial[3,3])."""
+    r = _arr(r)
+    nb, na, _ = r.shape
+    dvdr = np.zeros_like(r)
+    vir = np.zeros(9)
+    v = C.c_double()
+    _check(load().gbrpmd_forces(_ptr(r), C.byref(v), _ptr(dvdr), C.byref(C.c_int(nb)), C.byref(C.c_int(na)),
+                                _ptr(_arr(box)), _ptr(_arr(z)), _ptr(vir), C.byref(C.c_int(iopt))))
+    return v.value, dvdr, vir.reshape(3, 3, order="F")
+
+
+def full_forces(r, box, z):
+    """full_forces(r,na,nb,v,vew,voo,vint,vir,z,boxlxyz,dvdr,dvdr2)."""
+    r = _arr(r)
+    nb, na, _ = r.shape
+    dvdr = np.zeros_like(r)
+    dvdr2 = np.zeros_like(r)
+    vir = np.zeros(9)
+    v, vew, voo, vint = (C.c_double() for _ in range(4))
+    _check(load().gbrpmd_full_forces(_ptr(r), C.byref(C.c_int(na)), C.byref(C.c_int(nb)), C.byref(v),
+                                     C.byref(vew), C.byref(voo), C.byref(vint), _ptr(vir), _ptr(_arr(z)),
+                                     _ptr(_arr(box)), _ptr(dvdr), _ptr(dvdr2)))
+    return dict(v=v.value, vew=vew.value, voo=voo.value, vint=vint.value, dvdr=dvdr, dvdr2=dvdr2,
+                vir=vir.reshape(3, 3, order="F"))
+
+
+class State:
+    """Trajectory arrays the caller owns, as the Fortran host owns p, r, dvdr, dvdr2."""
+
+    def __init__(self, r, p, dvdr, dvdr2, box):
+        self.r = _arr(r).copy()
+        self.p = _arr(p).copy()
+        self.dvdr = _arr(dvdr).copy()
+        self.dvdr2 = _arr(dvdr2).copy()
+        self.box = _arr(box).copy()
+        self.vir = np.zeros(9)
+        self.vir_lf = np.zeros(9)
+
+
+def evolve_pi(state: State, dt, mass, z, beta, irun=0):
+    """evolve_pi(p,r,v,vew,vlj,vint,dvdr,dvdr2,dt,mass,na,nb,boxlxyz,z,beta,vir,vir_lf,irun,nbaro)."""
+    nb, na, _ = state.r.shape
+    v, vew, vlj, vint = (C.c_double() for _ in range(4))
+    _check(load().gbrpmd_evolve_pi(_ptr(state.p), _ptr(state.r), C.byref(v), C.byref(vew), C.byref(vlj),
+                                   C.byref(vint), _ptr(state.dvdr), _ptr(state.dvdr2), C.byref(C.c_double(dt)),
+                                   _ptr(_arr(mass)), C.byref(C.c_int(na)), C.byref(C.c_int(nb)), _ptr(state.box),
+                                   _ptr(_arr(z)), C.byref(C.c_double(beta)), _ptr(state.vir), _ptr(state.vir_lf),
+                                   C.byref(C.c_int(irun)), C.byref(C.c_int(0))))
+    return dict(v=v.value, vew=vew.value, vlj=vlj.value, vint=vint.value)
+
+
+def rattle_setup(nm):
+    _check(load().gbrpmd_rattle_setup(C.byref(C.c_int(nm))))
+
+
+def rattle_s1(r, rold, p, mass, dt, dvdr):
+    """One bead: r, rold, p, dvdr shaped (na, 3); returns vir[3,3] (arrays updated in place)."""
+    na = r.shape[0]
+    vir = np.zeros(9)
+    _check(load().gbrpmd_rattle_s1(_ptr(r), _ptr(_arr(rold)), _ptr(p), C.byref(C.c_int(na // 3)), _ptr(_arr(mass)),
+                                   C.byref(C.c_double(dt)), _ptr(dvdr), _ptr(vir), C.byref(C.c_int(na))))
+    return vir.reshape(3, 3, order="F")
+
+
+def rattle_s2(r, p, mass, dt, dvdr):
+    na = r.shape[0]
+    vir = np.zeros(9)
+    _check(load().gbrpmd_rattle_s2(_ptr(r), _ptr(p), C.byref(C.c_int(na // 3)), _ptr(_arr(mass)),
+                                   C.byref(C.c_double(dt)), _ptr(dvdr), _ptr(vir), C.byref(C.c_int(na))))
+    return vir.reshape(3, 3, order="F")
+
+
+def evolve_rig_pi(state: State, dt, mass, z, beta, irun=0):
+    nb, na, _ = state.r.shape
+    v, v_lf, v_hf = C.c_double(), C.c_double(), C.c_double()
+    _check(load().gbrpmd_evolve_rig_pi(_ptr(state.p), _ptr(state.r), C.byref(v), C.byref(v_lf), C.byref(v_hf),
+                                       _ptr(state.dvdr), _ptr(state.dvdr2), C.byref(C.c_double(dt)),
+                                       _ptr(_arr(mass)), C.byref(C.c_int(na)), C.byref(C.c_int(nb)),
+                                       _ptr(state.box), _ptr(_arr(z)), C.byref(C.c_double(beta)),
+                                       _ptr(state.vir), _ptr(state.vir_lf), C.byref(C.c_int(irun)),
+                                       C.byref(C.c_int(0))))
+    return dict(v=v.value)
+
+
+class Context:
+    """Resident trajectory: state kept in device memory between steps."""
+
+    def __init__(self, na, nb, mass, z):
+        self.na, self.nb = na, nb
+        self.h = C.c_void_p()
+        _check(load().gbrpmd_ctx_create(C.byref(self.h), na, nb, _ptr(_arr(mass)), _ptr(_arr(z))))
+
+    def close(self):
+        if self.h:
+            load().gbrpmd_ctx_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, r=None, p=None, dvdr=None, dvdr2=None, box=None):
+        keep = [None if a is None else _arr(a) for a in (r, p, dvdr, dvdr2, box)]
+        _check(load().gbrpmd_ctx_upload(self.h, *[_ptr(a) for a in keep]))
+        self.sync()
+
+    def download(self):
+        shape = (self.nb, self.na, 3)
+        r, p, f, f2 = (np.zeros(shape) for _ in range(4))
+        _check(load().gbrpmd_ctx_download(self.h, _ptr(r), _ptr(p), _ptr(f), _ptr(f2)))
+        return r, p, f, f2
+
+    def full_forces(self):
+        v, vew, voo, vint = (C.c_double() for _ in range(4))
+        vir = np.zeros(9)
+        _check(load().gbrpmd_ctx_full_forces(self.h, C.byref(v), C.byref(vew), C.byref(voo), C.byref(vint), _ptr(vir)))
+        return dict(v=v.value, vew=vew.value, voo=voo.value, vint=vint.value, vir=vir.reshape(3, 3, order="F"))
+
+    def evolve(self, nsteps, dt, beta):
+        _check(load().gbrpmd_ctx_evolve(self.h, nsteps, dt, beta))
+
+    def sync(self):
+        _check(load().gbrpmd_ctx_sync(self.h))
+
+    def energies(self):
+        out = np.zeros(5)
+        vir = np.zeros(9)
+        vir_lf = np.zeros(9)
+        _check(load().gbrpmd_ctx_energies(self.h, _ptr(out), _ptr(vir), _ptr(vir_lf)))
+        return dict(v=out[0], vew=out[1], vlj=out[2], vint=out[3], tv=out[4], vir=vir.reshape(3, 3, order="F"),
+                    vir_lf=vir_lf.reshape(3, 3, order="F"))
+
+    @property
+    def stream(self):
+        return load().gbrpmd_ctx_stream(self.h)
+
+    @property
+    def launches(self):
+        return load().gbrpmd_ctx_launch_count(self.h)
+
+
+def ran2(idum: C.c_int, rmin=0.0, rmax=1.0):
+    return load().gbrpmd_ran2(C.byref(idum), C.byref(C.c_double(rmin)), C.byref(C.c_double(rmax)))
+
+
+def gaussian(idum: C.c_int, sigma=1.0):
+    return load().gbrpmd_gaussian(C.byref(idum), C.byref(C.c_double(sigma)))
