@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 RPMD step in bead-molecule-steps/s.
+
+Workload (one "step" = one outer evolve_pi step, evolve_pi.f90:1-322):
+q-SPC/Fw water, 4096 H2O on a 16^3 CUB lattice (L = 49.71 A, rho = 0.997
+g/cm^3), nb = 32 beads, T = 298 K, MTS = 5 (dt = 1.25 fs outer, 0.25 fs inner),
+ring-polymer contraction: Ewald on the centroid (nbdf1 = 1), Lennard-Jones on
+5 normal modes (nbdf2 = 5; the reference requires an odd count), intramolecular
+forces on all 32 beads; plain FP64.  Inputs are synthetic: the reference's
+deterministic CUB lattice and momenta drawn from the reference's ran2/gaussian
+stream (sample_rpmd) after an initial full_forces.
+
+value:  nb * nm * K / (sum of the K steps' CUDA-event times), state resident in
+        HBM, L2 flushed (256 MiB write) between steps outside the timed events.
+e2e:    the same metric through the drop-in C-ABI call gbrpmd_evolve_pi with
+        pinned host arrays: p, r, dvdr, dvdr2 copied in and out every step.
+--impl reference: the reference's algorithm on the host CPU (the C++
+        restatement in oracle/, since the Fortran reference has no compiler
+        here), one independent trajectory per host thread.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PARAM = os.path.join(ROOT, "tests", "golden", "params", "param_qspcfw")
+WORKLOADS = {
+    "qspcfw_4096_nb32_mts5_contracted": dict(ncell=(16, 16, 16), nb=32, mts=5, dtfs=1.25, nbdf1=1, nbdf2=5),
+    "qspcfw_216_nb32": dict(ncell=(6, 6, 6), nb=32, mts=1, dtfs=0.5),
+}
+DEFAULT = "qspcfw_4096_nb32_mts5_contracted"
+REGIONS = ["mts_block", "pair_lists", "ewald_real", "recip_sk", "recip_weights", "recip_force", "lj",
+           "tem", "expand_kick", "msite", "rattle"]
+# algorithmic FP64 flops per work unit of a region (declared weights):
+# real-space in-cut pair 60, reciprocal (k, site) 16 split 8 + 8 between the
+# structure-factor and the force pass, LJ pair 45
+FLOPS_PER_UNIT = {"ewald_real": 60.0, "recip_sk": 8.0, "recip_force": 8.0, "lj": 45.0}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_system(name):
+    from rpmd_mainz_gb300 import lib, system
+
+    cfg = WORKLOADS[name]
+    s = system.water_box(PARAM, **cfg)
+    lib.init(s["params"])
+    irun = C.c_int(-4711)
+    s["p"] = system.sample_momenta(s["na"], s["nb"], s["mass"], s["beta"], irun)
+    return s
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(k)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 peak: cuBLAS DGEMM 8192^3 (2 N^3 flops), best of 3."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def read_profile_traffic(region):
+    """DRAM bytes per launch of `region` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == region:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(s, seconds_target=15.0):
+    """The oracle port on the host cores: one trajectory per thread, bounded sample."""
+    from tests import oracle_lib as orc
+
+    orc.set_params(s["params"])
+    ff = orc.full_forces(s["r"], s["box"], s["z"])
+    st = orc.State(s["r"], s["p"], ff["dvdr"], ff["dvdr2"], s["box"])
+    threads = os.cpu_count() or 1
+    t1 = orc.bench_replicas(1, st, s["dt"], s["mass"], s["z"], s["beta"], 1)
+    steps = max(1, min(20, int(seconds_target / max(t1, 1e-3))))
+    wall = orc.bench_replicas(threads, st, s["dt"], s["mass"], s["z"], s["beta"], steps)
+    value = threads * steps * s["nb"] * s["nm"] / wall
+    return {"value": value, "unit": "bead-molecule-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{threads} independent trajectories x {steps} evolve_pi steps of the same workload "
+                      f"(one per host thread, {wall:.1f} s wall); single-thread step {t1:.2f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    s = make_system(args.workload)
+    from tests import oracle_lib as orc
+
+    orc.set_params(s["params"])
+    ff = orc.full_forces(s["r"], s["box"], s["z"])
+    st = orc.State(s["r"], s["p"], ff["dvdr"], ff["dvdr2"], s["box"])
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        orc.bench_replicas(threads, st, s["dt"], s["mass"], s["z"], s["beta"], 1)
+    times = []
+    for _ in range(args.steps):
+        times.append(orc.bench_replicas(threads, st, s["dt"], s["mass"], s["z"], s["beta"], 1))
+    total = sum(times)
+    value = threads * args.steps * s["nb"] * s["nm"] / total
+    out = {
+        "impl": "reference", "metric": "bead-molecule-steps/s", "value": value, "unit": "bead-molecule-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "nm": s["nm"], "nb": s["nb"], "mts": s["params"].mts,
+                   "nbdf1": s["params"].nbdf1, "nbdf2": s["params"].nbdf2, "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": "bead-molecule-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"each step: {threads} host threads advance one independent trajectory by one "
+                                   f"evolve_pi step (C++ restatement of the Fortran reference)"},
+        "e2e": {"value": value, "unit": "bead-molecule-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "p50_ms": 1e3 * statistics.median(times), "p99_ms": 1e3 * float(np.percentile(times, 99)),
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import __graft_entry__ as g
+
+    g.build()
+    from rpmd_mainz_gb300 import lib
+
+    s = make_system(args.workload)
+    na, nb, nm = s["na"], s["nb"], s["nm"]
+    ff = lib.full_forces(s["r"], s["box"], s["z"])
+    ctx = lib.Context(na, nb, s["mass"], s["z"])
+    ctx.upload(r=s["r"], p=s["p"], dvdr=ff["dvdr"], dvdr2=ff["dvdr2"], box=s["box"])
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        ctx.evolve(1, s["dt"], s["beta"])
+    ctx.sync()
+
+    # profiled pass (not timed): per-region CUDA-event times for the roofline
+    lib.load().gbrpmd_ctx_set_profiling(ctx.h, 1)
+    ctx.evolve(1, s["dt"], s["beta"])
+    ctx.sync()
+    R = len(REGIONS)
+    ms, units, cnt = np.zeros(R), np.zeros(R), np.zeros(R, dtype=np.int32)
+    lib.load().gbrpmd_ctx_region_times(ctx.h, lib._ptr(ms), lib._ptr(units), cnt.ctypes.data_as(C.POINTER(C.c_int)),
+                                       C.c_int(R))
+    lib.load().gbrpmd_ctx_set_profiling(ctx.h, 0)
+    regions = {REGIONS[i]: {"ms": float(ms[i]), "launches": int(cnt[i]), "units": float(units[i])}
+               for i in range(R) if cnt[i]}
+
+    # timed region
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    step_ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            ctx.evolve(1, s["dt"], s["beta"])
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    ctx.sync()
+    torch.cuda.synchronize()
+    launches = ctx.launches - launches0
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * args.steps * nb * nm / (total_ms * 1e-3)
+    energies = ctx.energies()
+
+    # e2e through the drop-in C ABI with pinned host buffers
+    shape = (nb, na, 3)
+    r_h, p_h, f_h, f2_h = (torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4))
+    r0, p0, f0, f20 = ctx.download()
+    r_h[:], p_h[:], f_h[:], f2_h[:] = r0, p0, f0, f20
+    st = lib.State.__new__(lib.State)
+    st.r, st.p, st.dvdr, st.dvdr2 = r_h, p_h, f_h, f2_h
+    st.box = s["box"].copy()
+    st.vir, st.vir_lf = np.zeros(9), np.zeros(9)
+    lib.evolve_pi(st, s["dt"], s["mass"], s["z"], s["beta"])  # warm the drop-in context
+    e2e_times = []
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        lib.evolve_pi(st, s["dt"], s["mass"], s["z"], s["beta"])
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = world * nb * nm * len(e2e_times) / sum(e2e_times)
+    nbytes = 4 * r_h.nbytes
+
+    out = {
+        "metric": "bead-molecule-steps/s", "value": value, "unit": "bead-molecule-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (CUB lattice, Maxwell-Boltzmann momenta from the reference's ran2 stream)",
+        "config": {"workload": args.workload, "nm": nm, "nb": nb, "mts": s["params"].mts,
+                   "nbdf1": s["params"].nbdf1, "nbdf2": s["params"].nbdf2, "precision": "fp64",
+                   "l2": "256 MiB flush between steps, outside the timed events",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e_value, "unit": "bead-molecule-steps/s", "h2d_bytes_per_step": int(nbytes),
+                "d2h_bytes_per_step": int(nbytes + 8 * 22),
+                "path": "gbrpmd_evolve_pi drop-in, pinned host p/r/dvdr/dvdr2"},
+        "energies_last_step": {"v": energies["v"], "vew": energies["vew"], "vlj": energies["vlj"],
+                               "vint": energies["vint"]},
+        "regions_ms_one_step": regions,
+    }
+    # roofline of the dominant kernel region (FP64 CUDA-core bound)
+    if rank == 0:
+        peak = fp64_peak_tflops(torch)
+        dom = max((k for k in regions if k in FLOPS_PER_UNIT), key=lambda k: regions[k]["ms"])
+        rr = regions[dom]
+        per_launch_ms = rr["ms"] / rr["launches"]
+        flops_per_launch = FLOPS_PER_UNIT[dom] * rr["units"] / rr["launches"]
+        achieved = flops_per_launch / (per_launch_ms * 1e-3) / 1e12
+        out["roofline"] = {"bound": "fp64", "kernel_region": dom, "achieved": achieved, "peak": peak,
+                           "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom),
+                           "peak_source": "measured in this run: cuBLAS DGEMM 8192^3 (FP64 CUDA-core/tensor "
+                                          "rate; MEASURED_PEAKS.json holds only HBM and BF16)",
+                           "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": rr["units"] / rr["launches"]}
+        out["clocks"] = clk.summary()
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(s)
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

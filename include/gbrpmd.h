@@ -160,6 +160,23 @@ int gbrpmd_evolve_rig_pi(double *p, double *r, double *v, double *v_lf, double *
                          const double *beta, double *vir, double *vir_lf, int *irun,
                          const int *nbaro);
 
+/* ---- host-side set-up, in main.f90's start-up order ---------------------- */
+
+/* replaces setup_box_size for the CUB lattice (setup_options.f90:191-270):
+   box lengths from the unit-cell counts and the density (g/cm^3) */
+int gbrpmd_setup_box_size(const int *ncellxyz, double rho, double wmass, double *boxlxyz,
+                          int *nm);
+/* replaces cubic (setup_positions.f90:94-150) and the bead copy of
+   setup_positions (setup_positions.f90:78-85): r(3, 3*nm, nb) */
+int gbrpmd_cubic_lattice(double *r, int nm, int nb, const double *boxlxyz, const int *ncellxyz,
+                         double theta, double reoh);
+/* replaces setup_ewald (setup_options.f90:104-189): fills wrcut, walpha,
+   rkmax, kmax and iamcub of *params from ecut, iamcub, na and the box */
+int gbrpmd_setup_ewald(int na, const double *boxlxyz, gb_params *params);
+/* replaces sample_rpmd + pshift (module_thermostat.f90:199-264): momenta
+   from the library's gaussian stream, centre-of-mass momentum removed */
+int gbrpmd_sample_rpmd(double *p, int na, int nb, const double *mass, double beta, int *irun);
+
 /* ---- serial random stream (random.f90:1-72) ----------------------------- */
 /* The thermostat kicks inside evolve_pi draw from the reference's global
    ran2/gaussian stream.  The library owns that stream; a Fortran host routes
@@ -198,6 +215,20 @@ int gbrpmd_ctx_energies(gb_context *ctx, double *out5, double *vir, double *vir_
 void *gbrpmd_ctx_stream(gb_context *ctx);
 /* number of kernel launches issued by this context since creation */
 int64_t gbrpmd_ctx_launch_count(gb_context *ctx);
+/* CUDA-event timing of the library's kernel regions on this context (for
+   profiling and roofline reports; adds one synchronisation per pair list) */
+int gbrpmd_ctx_set_profiling(gb_context *ctx, int on);
+/* per region: total milliseconds, work units, launches since the last call;
+   regions: 0 multiple-time-step block, 1 pair lists, 2 real-space Ewald,
+   3 structure factors, 4 k-space weights, 5 k-space forces, 6 Lennard-Jones,
+   7 TEM correction, 8 contraction and kicks, 9 M-site, 10 RATTLE */
+int gbrpmd_ctx_region_times(gb_context *ctx, double *ms, double *units, int *counts, int nregion);
+/* the md_eq step loop (md_eq.f90:182-323) on the device state: nsteps
+   evolve_pi steps, each followed by the Andersen test ran2(irun) < thresh
+   that resamples all momenta (md_eq.f90:311-315) when therm is AND.
+   energies (4 per step: v, vew, vlj, vint) may be NULL. */
+int gbrpmd_run_md_eq(gb_context *ctx, int nsteps, double dt, double beta, double thresh,
+                     int *irun, double *energies);
 
 #ifdef __cplusplus
 }

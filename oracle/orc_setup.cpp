@@ -197,26 +197,48 @@ void hc2r_direct(const double *in, double *x, int n, const Twiddle &t) {
 using cd = std::complex<double>;
 
 // in-place iterative radix-2 complex FFT of length h (power of two);
-// sign = -1 forward (exp(-i...)), +1 backward (unnormalised)
+// sign = -1 forward (exp(-i...)), +1 backward (unnormalised).  Twiddles
+// exp(sign 2 pi i k / h) come from a per-length table.
 void cfft(cd *a, int h, int sign) {
+  static thread_local int tw_h = 0;
+  static thread_local std::vector<cd> tw;
+  if (tw_h != h) {
+    tw.resize(h);
+    const double pi = std::acos(-1.0);
+    for (int k = 0; k < h; ++k) tw[k] = cd(std::cos(2.0 * pi * k / h), std::sin(2.0 * pi * k / h));
+    tw_h = h;
+  }
   for (int i = 1, j = 0; i < h; ++i) {
     int bit = h >> 1;
     for (; j & bit; bit >>= 1) j ^= bit;
     j ^= bit;
     if (i < j) std::swap(a[i], a[j]);
   }
-  const double pi = std::acos(-1.0);
   for (int len = 2; len <= h; len <<= 1) {
+    const int step = h / len;
     for (int i = 0; i < h; i += len) {
       for (int k = 0; k < len / 2; ++k) {
-        double ang = sign * 2.0 * pi * k / len;
-        cd w(std::cos(ang), std::sin(ang));
+        cd w = tw[k * step];
+        if (sign < 0) w = std::conj(w);
         cd u = a[i + k], v = a[i + k + len / 2] * w;
         a[i + k] = u + v;
         a[i + k + len / 2] = u - v;
       }
     }
   }
+}
+
+// exp(+2 pi i k / n), k = 0..n/2, cached per length
+const std::vector<cd> &post_twiddles(int n) {
+  static thread_local int tn = 0;
+  static thread_local std::vector<cd> w;
+  if (tn != n) {
+    w.resize(n / 2 + 1);
+    const double pi = std::acos(-1.0);
+    for (int k = 0; k <= n / 2; ++k) w[k] = cd(std::cos(2.0 * pi * k / n), std::sin(2.0 * pi * k / n));
+    tn = n;
+  }
+  return w;
 }
 
 // R2HC for n = 2h, h a power of two: FFT of the packed sequence
@@ -227,12 +249,11 @@ void r2hc_fft(const double *x, double *out, int n) {
   std::vector<cd> z(h);
   for (int j = 0; j < h; ++j) z[j] = cd(x[2 * j], x[2 * j + 1]);
   cfft(z.data(), h, -1);
-  const double pi = std::acos(-1.0);
+  const std::vector<cd> &wn = post_twiddles(n);
   for (int k = 0; k <= h; ++k) {
     cd zk = z[k % h], zc = std::conj(z[(h - k) % h]);
     cd e = 0.5 * (zk + zc), o = cd(0.0, -0.5) * (zk - zc);
-    double ang = -2.0 * pi * k / n;
-    cd xk = e + cd(std::cos(ang), std::sin(ang)) * o;
+    cd xk = e + std::conj(wn[k]) * o;
     out[k] = xk.real();
     if (k > 0 && k < h) out[n - k] = xk.imag();
   }
@@ -248,11 +269,10 @@ void hc2r_fft(const double *in, double *x, int n) {
     return cd(in[k], in[n - k]);
   };
   std::vector<cd> z(h);
-  const double pi = std::acos(-1.0);
+  const std::vector<cd> &wn = post_twiddles(n);
   for (int k = 0; k < h; ++k) {
     cd xk = X(k), xc = std::conj(X(h - k));
-    double ang = 2.0 * pi * k / n;
-    cd e = 0.5 * (xk + xc), o = 0.5 * cd(std::cos(ang), std::sin(ang)) * (xk - xc);
+    cd e = 0.5 * (xk + xc), o = 0.5 * wn[k] * (xk - xc);
     z[k] = e + cd(0.0, 1.0) * o;
   }
   cfft(z.data(), h, +1);

@@ -94,6 +94,27 @@ int ctx_check_cuda(cudaError_t e, const char *what) {
   return e == cudaErrorMemoryAllocation ? GB_E_NOMEM : GB_E_CUDA;
 }
 
+void prof_begin(gb_context *c, int region) {
+  if (!c->prof) return;
+  (void)region;
+  if (c->ev_next + 2 > c->ev_pool.size()) {
+    for (int i = 0; i < 64; ++i) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      c->ev_pool.push_back(e);
+    }
+  }
+  cudaEventRecord(c->ev_pool[c->ev_next], c->stream);
+}
+
+void prof_end(gb_context *c, int region, double units) {
+  if (!c->prof) return;
+  cudaEvent_t a = c->ev_pool[c->ev_next], b = c->ev_pool[c->ev_next + 1];
+  cudaEventRecord(b, c->stream);
+  c->marks.push_back({region, a, b, units});
+  c->ev_next += 2;
+}
+
 int ctx_alloc(gb_context *c, int na, int nb) {
   int st = check_sizes(na, nb);
   if (st) return st;
@@ -128,6 +149,9 @@ int ctx_alloc(gb_context *c, int na, int nb) {
 
 void ctx_free(gb_context *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  c->ev_pool.clear();
+  if (c->d_count) cudaFree(c->d_count);
   for (void *p : c->allocs) cudaFree(p);
   c->allocs.clear();
   for (void *p : {(void *)c->pl.idx, (void *)c->pl.count, (void *)c->kxy, (void *)c->kxy_koff,
@@ -332,6 +356,34 @@ int gbrpmd_ctx_energies(gb_context *c, double *out5, double *vir, double *vir_lf
 }
 
 void *gbrpmd_ctx_stream(gb_context *c) { return (void *)c->stream; }
+
+int gbrpmd_ctx_set_profiling(gb_context *c, int on) {
+  CK(cudaStreamSynchronize(c->stream));
+  c->prof = on;
+  c->marks.clear();
+  c->ev_next = 0;
+  return GB_OK;
+}
+
+int gbrpmd_ctx_region_times(gb_context *c, double *ms, double *units, int *counts, int nregion) {
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < nregion; ++i) {
+    ms[i] = 0.0;
+    units[i] = 0.0;
+    counts[i] = 0;
+  }
+  for (const auto &m : c->marks) {
+    if (m.region < 0 || m.region >= nregion) continue;
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, m.a, m.b));
+    ms[m.region] += t;
+    units[m.region] += m.units;
+    counts[m.region] += 1;
+  }
+  c->marks.clear();
+  c->ev_next = 0;
+  return GB_OK;
+}
 
 int64_t gbrpmd_ctx_launch_count(gb_context *c) { return c->launches; }
 

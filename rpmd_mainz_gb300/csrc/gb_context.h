@@ -82,7 +82,37 @@ struct gb_context {
 
   int64_t launches = 0;
   std::vector<void *> allocs;
+
+  // optional per-region CUDA-event timing (gbrpmd_ctx_set_profiling)
+  int prof = 0;
+  struct Mark {
+    int region;
+    cudaEvent_t a, b;
+    double units;  // work units of this launch (pairs, k*sites, molecule-beads ...)
+  };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_next = 0;
+  int *d_count = nullptr;  // device scratch for pair counts (profiling only)
 };
+
+// profiled regions
+enum ProfRegion : int {
+  PR_MTS = 0,        // multiple-time-step block (kicks, transforms, rotation, intra, virial_ke)
+  PR_LIST = 1,       // pair-list builds
+  PR_EW_REAL = 2,    // real-space Ewald pairs (units: in-cut pairs)
+  PR_RECIP_SK = 3,   // structure factors (units: k vectors x sites)
+  PR_RECIP_W = 4,    // reduction / weights
+  PR_RECIP_F = 5,    // reciprocal forces (units: k vectors x sites)
+  PR_LJ = 6,         // Lennard-Jones pairs (units: list pairs x beads)
+  PR_TEM = 7,        // TEM correction pairs
+  PR_EXPAND = 8,     // contraction, force expansion, final kick
+  PR_MSITE = 9,      // M-site substitution and chain rule
+  PR_RATTLE = 10,    // rigid substeps and RATTLE
+  PR_NREGION = 11
+};
+void prof_begin(gb_context *c, int region);
+void prof_end(gb_context *c, int region, double units);
 
 // ---- context lifetime and helpers (api.cpp) ----
 int ctx_alloc(gb_context *c, int na, int nb);

@@ -26,6 +26,7 @@ struct PairGeom {
 void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac);
 void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
                        PairList &pl, unsigned *status);
+double list_total(cudaStream_t s, const PairList &pl);  // profiling only (synchronises)
 
 // ---- Ewald, unit box (k_pairs.cu, k_recip.cu) ----
 // rs: M-site substituted positions scaled by 1/L, [B][na][3]

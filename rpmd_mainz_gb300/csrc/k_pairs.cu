@@ -318,9 +318,29 @@ __global__ void k_centroid(const double *r, double *rc, int na, int B) {
   rc[t] = s / (double)B;
 }
 
+__global__ void k_sum_counts(const int *count, long long n, unsigned long long *out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long v = t < n ? (unsigned long long)count[t] : 0ull;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(out, v);
+}
+
 inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
+
+// total entries of a pair list (profiling only: synchronises the stream)
+double list_total(cudaStream_t s, const PairList &pl) {
+  unsigned long long *d = nullptr, h = 0;
+  if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return 0.0;
+  cudaMemsetAsync(d, 0, sizeof(unsigned long long), s);
+  long long n = (long long)pl.nconf * pl.npt;
+  k_sum_counts<<<nblk(n, 256), 256, 0, s>>>(pl.count, n, d);
+  cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  cudaFree(d);
+  return (double)h;
+}
 
 void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac) {
   long long n = (long long)nconf * g.npt;

@@ -348,6 +348,7 @@ int rattle_dropin(int stage, double *r, const double *rold, double *p, int nm, c
   CK(cudaMemcpyAsync(p, g_ws.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(dvdr, g_ws.f, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(vir, g_ws.vir, sizeof(double) * 9, cudaMemcpyDeviceToHost, s));
+  CK(cudaGetLastError());
   unsigned stw = 0;
   CK(cudaMemcpyAsync(&stw, g_ws.status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -412,5 +413,6 @@ int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) 
   c->plan.B_int = nb;  // vir_hf = sum_k vir_k / nb (evolve_rigid.f90:198)
   CK(cudaMemsetAsync(c->dvdr2, 0, sizeof(double) * N, s));
   c->launches += 6;
+  CK(cudaGetLastError());
   return GB_OK;
 }

@@ -217,7 +217,14 @@ size_t recip_sk_smem(int kmax, int nkxy) {
 }
 size_t recip_force_smem(int kmax) { return sizeof(double) * 6 * (kmax + 1) * 128; }
 int recip_sk_chunk() { return SK_CHUNK; }
+// The dynamic shared-memory limit is a per-kernel property of the process, so
+// it is raised once to the largest size any context may request (227 KB).
 void recip_set_attributes(size_t sk_smem, size_t f_smem) {
-  cudaFuncSetAttribute(k_recip_sk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sk_smem);
-  cudaFuncSetAttribute(k_recip_force, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f_smem);
+  (void)sk_smem;
+  (void)f_smem;
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_recip_sk, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  done = true;
 }

@@ -34,6 +34,12 @@ const double PI = 3.141592653589793238462643383279502884;
 
 double *slot(gb_context *c, int s) { return c->acc + (size_t)s * ACC_STRIDE; }
 
+// reports a failed kernel launch (bad configuration, shared-memory limit) at once
+int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GB_OK : ctx_check_cuda(e, "kernel launch");
+}
+
 std::vector<double> twiddles(int n) {
   std::vector<double> t(2 * (size_t)n);
   for (int m = 0; m < n; ++m) {
@@ -200,8 +206,10 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   if (c->P.wm > 0.0 || c->P.wh > 0.0) return ctx_set_error(GB_E_UNSUPPORTED, "smeared-charge Ewald is not on the device path");
   const int na = c->na;
   const double L = c->box[0], onboxl = 1.0 / L;
+  prof_begin(c, PR_MSITE);
   launch_msite(c->stream, r, c->rs, na, B, c->P.alpha, onboxl);
   CK(cudaMemsetAsync(c->g, 0, sizeof(double) * 3 * (size_t)na * B, c->stream));
+  prof_end(c, PR_MSITE, (double)na * B);
   PairGeom g{};
   g.pos = c->rs;
   g.cstride = 3LL * na;
@@ -214,13 +222,27 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   g.excl_mol = 0;
   int st = ensure_list(c, B, na, list_cap(na, c->P.wrcut, 1.0));
   if (st) return st;
+  prof_begin(c, PR_LIST);
   launch_frac32(c->stream, g, B, c->rs32);
   launch_build_list(c->stream, g, B, c->rs32, c->pl, c->status);
+  prof_end(c, PR_LIST, (double)na * B);
+  const double npairs = c->prof ? list_total(c->stream, c->pl) : 0.0;
+  prof_begin(c, PR_EW_REAL);
   launch_ewald_real(c->stream, c->rs, c->z, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
+  prof_end(c, PR_EW_REAL, npairs);
+  const double ksites = (double)c->nk * na * B;
+  prof_begin(c, PR_RECIP_SK);
   launch_recip_sk(c->stream, c, c->rs, c->z, B);
+  prof_end(c, PR_RECIP_SK, ksites);
+  prof_begin(c, PR_RECIP_W);
   launch_recip_weights(c->stream, c, B, slot(c, s));
+  prof_end(c, PR_RECIP_W, (double)c->nk * B);
+  prof_begin(c, PR_RECIP_F);
   launch_recip_force(c->stream, c, c->rs, c->z, B, c->g);
+  prof_end(c, PR_RECIP_F, ksites);
+  prof_begin(c, PR_MSITE);
   launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, onboxl * onboxl, sign, accumulate);
+  prof_end(c, PR_MSITE, (double)na * B);
   c->launches += 8;
   return GB_OK;
 }
@@ -258,10 +280,15 @@ int term_lj(gb_context *c, const double *r, int B, double *out, int accumulate, 
     int st = ensure_list(c, B, nm, list_cap(nm, c->P.rcut, vol));
     if (st) return st;
   }
+  prof_begin(c, PR_LIST);
   launch_frac32(c->stream, g, nconf, c->rs32);
   launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
+  prof_end(c, PR_LIST, (double)nm * nconf);
+  const double npairs = c->prof ? list_total(c->stream, c->pl) * (nconf == 1 ? B : 1) : 0.0;
+  prof_begin(c, PR_LJ);
   launch_lj(c->stream, r, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut, c->box,
             48.0 * c->P.oo_eps, out, slot(c, s));
+  prof_end(c, PR_LJ, npairs);
   c->launches += 3;
   return GB_OK;
 }
@@ -309,9 +336,13 @@ int term_tem(gb_context *c, const double *r, int B, double *out, double sign, in
     if (st) return st;
   }
   CK(cudaMemsetAsync(c->g, 0, sizeof(double) * 3 * (size_t)na * B, c->stream));
+  prof_begin(c, PR_LIST);
   launch_frac32(c->stream, g, nconf, c->rs32);
   launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
+  prof_end(c, PR_LIST, (double)na * nconf);
+  prof_begin(c, PR_TEM);
   launch_tem(c->stream, c->rs, c->z, na, B, c->pl, sig, c->box, c->g, slot(c, s));
+  prof_end(c, PR_TEM, 0.0);
   launch_msite_chain(c->stream, c->g, out, na, B, alpha, 1.0, sign, accumulate);
   c->launches += 5;
   return GB_OK;
@@ -372,9 +403,11 @@ int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, 
     c->plan.B_lj2 = nb;
     e3 = c->f_c;
   }
+  prof_begin(c, PR_EXPAND);
   launch_expand_forces(c->stream, c->dvdr, con1 ? c->fb1 : nullptr, nbdf1, c->tw_c1,
                        con2 ? c->fb2 : nullptr, nbdf2, c->tw_c2, e1, e2, e3, p, halfdt, na, nb,
                        c->tw_nb);
+  prof_end(c, PR_EXPAND, 3.0 * na * nb);
   c->launches += 1;
   return GB_OK;
 }
@@ -418,7 +451,7 @@ int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt) {
   if (iopt == 5) {
     if ((st = term_tem(c, r, B, out, 1.0, 1, ACC_TEM2))) return st;
     c->plan.B_tem2 = B;
-    return GB_OK;
+    return launch_status();
   }
   if (iopt < 0 || iopt > 4) return ctx_set_error(GB_E_UNSUPPORTED, "iopt not on the device path");
   if (iopt <= 2) {
@@ -433,7 +466,7 @@ int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt) {
     if ((st = term_intra(c, r, B, out, 1, ACC_INT))) return st;
     c->plan.B_int = B;
   }
-  return GB_OK;
+  return launch_status();
 }
 
 int dev_full_forces(gb_context *c) {
@@ -449,7 +482,8 @@ int dev_full_forces(gb_context *c) {
     launch_realft(c->stream, c->r, c->rnm, 3 * na, nb, +1, c->tw_nb);
     c->launches += 1;
   }
-  return low_frequency(c, c->rnm, c->r, nullptr, 0.0);
+  if ((st = low_frequency(c, c->rnm, c->r, nullptr, 0.0))) return st;
+  return launch_status();
 }
 
 int dev_evolve_pi(gb_context *c, double dt, double beta) {
@@ -466,6 +500,7 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   const double dtsmall = dt / (double)mts, halfdtsmall = 0.5 * dtsmall, halfdt = 0.5 * dt;
   cudaStream_t s = c->stream;
   CK(cudaMemsetAsync(c->acc, 0, sizeof(double) * ACC_NSLOT * ACC_STRIDE, s));
+  prof_begin(c, PR_MTS);
   // evolve_pi.f90:82-88
   launch_axpy(s, c->p, c->dvdr, -halfdt, N);
   launch_axpy(s, c->p, c->dvdr2, -halfdtsmall, N);
@@ -492,8 +527,10 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   std::swap(c->r, c->rst);
   launch_axpy(s, c->p, c->dvdr2, -halfdtsmall, N);
   c->launches += 2;
+  prof_end(c, PR_MTS, (double)c->nm * nb * mts);
   // low-frequency forces and the closing kick (evolve_pi.f90:194-279)
-  return low_frequency(c, c->rnm, c->r, c->p, halfdt);
+  if ((st = low_frequency(c, c->rnm, c->r, c->p, halfdt))) return st;
+  return launch_status();
 }
 
 // forces(r, v, dvdr, nb, ..., iopt = 1) of evolve_rig_pi (evolve_rigid.f90:174)
@@ -506,7 +543,7 @@ int term_forces_rigid(gb_context *c) {
   c->plan.B_ew2 = c->nb;
   if ((st = term_lj(c, c->r, c->nb, c->dvdr, 1, ACC_LJ2))) return st;
   c->plan.B_lj2 = c->nb;
-  return GB_OK;
+  return launch_status();
 }
 
 int dev_collect(gb_context *c, int mode, double dt, double beta) {
@@ -515,6 +552,7 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
   CK(cudaMemcpyAsync(c->h_acc, c->acc, sizeof(double) * ACC_NSLOT * ACC_STRIDE, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaMemcpyAsync(c->h_status, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  CK(cudaGetLastError());
   unsigned stw = *c->h_status;
   if (stw) {
     CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
