@@ -119,6 +119,22 @@ int gbrpmd_finalize(void);
 int gbrpmd_forces(double *r, double *v, double *dvdr, const int *nb, const int *na,
                   const double *boxlxyz, const double *z, double *virial, const int *iopt);
 
+/* No counterpart in the reference.  Same results as gbrpmd_forces with
+   iopt = 2 (Ewald energy, gradient and virial of nb configurations, host
+   arrays in and out), for callers that cannot let the library allocate device
+   memory: hosts running under a device-memory budget owned by another
+   framework's pool, or code that must not trigger cudaMalloc / cudaFree (and
+   their implicit synchronisation) while its own streams are busy.  All device
+   work uses one 16 MiB array that the library reserves at load time on every
+   GPU that loads it (held until exit); nothing is allocated per call.  Its
+   device address is looked up on the first call made on each device, so make
+   that first call before any stream capture.  Calls share the array: each call
+   clears what must start at zero, and calls that overlap on the GPU race.
+   Limits: na*nb <= 8192 sites, nb <= 64, at most 2048 k vectors and 192
+   pair partners per site (GB_E_NOMEM / GB_E_LIST beyond them). */
+int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, const int *nb, const int *na,
+                               const double *boxlxyz, const double *z, double *virial);
+
 /* replaces subroutine full_forces(r,na,nb,v,vew,voo,vint,vir,z,boxlxyz,dvdr,dvdr2)
    (md_forces.f90:305-472): low-frequency (Ewald + LJ, with ring-polymer
    contraction when nbdf1/nbdf2 > 0) into dvdr, intramolecular into dvdr2. */
