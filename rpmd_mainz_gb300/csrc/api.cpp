@@ -2,6 +2,7 @@
 // device contexts, drop-in entry points and the serial random stream.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -125,6 +126,8 @@ int ctx_alloc(gb_context *c, int na, int nb) {
   c->na = na;
   c->nb = nb;
   c->nm = na / 3;
+  const char *gen = std::getenv("GBRPMD_GENERIC_MTS");
+  c->generic_mts = gen && gen[0] == '1';
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   const size_t N = 3 * (size_t)na * nb, S = 3 * (size_t)na;
   if ((st = dalloc(c, &c->p, N)) || (st = dalloc(c, &c->r, N)) || (st = dalloc(c, &c->dvdr, N)) ||

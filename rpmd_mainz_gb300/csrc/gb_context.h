@@ -31,6 +31,7 @@ struct gb_context {
   EnergyPlan plan;
   double qq = 0.0;  // sum of squared charges (Ewald self term)
   double last_beta = 1.0;  // beta of the last evolve_pi (virial kinetic energy)
+  int generic_mts = 0;     // 1: run the MTS block as separate kernels (GBRPMD_GENERIC_MTS=1)
   cudaStream_t stream = nullptr;
   int device = 0;
   gb_params P{};  // parameters in force for this context (copied at each call)

@@ -25,31 +25,22 @@ GB_HD constexpr int gb_bitrev(int i, int h) {
   return r;
 }
 
-// in-place radix-2 complex FFT of length H on register arrays; N = table length
-// (a multiple of H); inv selects exp(+...) twiddles
-template <int H, int N, bool INV>
-GB_D void gb_cfft(double (&zr)[H], double (&zi)[H], const double *__restrict__ tw) {
-#pragma unroll
-  for (int i = 0; i < H; ++i) {
-    const int j = gb_bitrev(i, H);
-    if (i < j) {
-      double t = zr[i]; zr[i] = zr[j]; zr[j] = t;
-      t = zi[i]; zi[i] = zi[j]; zi[j] = t;
-    }
-  }
-#pragma unroll
-  for (int len = 2; len <= H; len <<= 1) {
-    const int half = len >> 1;
+// one radix-2 stage of butterfly span LEN (template recursion keeps every index
+// a compile-time constant, so the arrays stay in registers)
+template <int H, int N, bool INV, int LEN>
+GB_D void gb_cfft_stage(double (&zr)[H], double (&zi)[H], const double *__restrict__ tw) {
+  if constexpr (LEN <= H) {
+    constexpr int half = LEN / 2;
 #pragma unroll
     for (int k = 0; k < half; ++k) {
       double wr = 1.0, wi = 0.0;
       if (k > 0) {
-        const int m = k * (N / len);
+        const int m = k * (N / LEN);
         wr = tw[m];
         wi = INV ? tw[N + m] : -tw[N + m];
       }
 #pragma unroll
-      for (int i = 0; i < H; i += len) {
+      for (int i = 0; i < H; i += LEN) {
         const int a = i + k, b = a + half;
         double tr, ti;
         if (k == 0) {
@@ -65,7 +56,23 @@ GB_D void gb_cfft(double (&zr)[H], double (&zi)[H], const double *__restrict__ t
         zi[a] = zi[a] + ti;
       }
     }
+    gb_cfft_stage<H, N, INV, 2 * LEN>(zr, zi, tw);
   }
+}
+
+// in-place radix-2 complex FFT of length H on register arrays; N = table length
+// (a multiple of H); INV selects exp(+...) twiddles
+template <int H, int N, bool INV>
+GB_D void gb_cfft(double (&zr)[H], double (&zi)[H], const double *__restrict__ tw) {
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const int j = gb_bitrev(i, H);
+    if (i < j) {
+      double t = zr[i]; zr[i] = zr[j]; zr[j] = t;
+      t = zi[i]; zi[i] = zi[j]; zi[j] = t;
+    }
+  }
+  gb_cfft_stage<H, N, INV, 2>(zr, zi, tw);
 }
 
 // unscaled R2HC of length N (power of two) in registers
@@ -161,5 +168,70 @@ GB_D void gb_hc2r_direct(const double *in, double *x, int n, const double *__res
     }
     if ((n & 1) == 0) s += (j & 1) ? -in[n / 2] : in[n / 2];
     x[j] = s;
+  }
+}
+
+// Accessor forms of the power-of-two transforms: `in(j)` yields input element
+// j, `out(k, v)` receives output element k.  All input elements are read before
+// the first output element is written, so input and output may be the same
+// storage (in-place in registers) and either may live in shared or global
+// memory; with constant indices after unrolling, register arrays stay in
+// registers.
+template <int N, class In, class Out>
+GB_D void gb_r2hc_io(In in, Out out, const double *__restrict__ tw) {
+  if constexpr (N == 1) {
+    out(0, in(0));
+  } else {
+    constexpr int H = N / 2;
+    double zr[H], zi[H];
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      zr[j] = in(2 * j);
+      zi[j] = in(2 * j + 1);
+    }
+    if constexpr (H > 1) gb_cfft<H, N, false>(zr, zi, tw);
+    out(0, zr[0] + zi[0]);
+    out(H, zr[0] - zi[0]);
+#pragma unroll
+    for (int k = 1; k < H; ++k) {
+      const int b = H - k;
+      const double er = 0.5 * (zr[k] + zr[b]), ei = 0.5 * (zi[k] - zi[b]);
+      const double orr = 0.5 * (zi[k] + zi[b]), oi = -0.5 * (zr[k] - zr[b]);
+      const double c = tw[k], s = tw[N + k];
+      out(k, er + c * orr + s * oi);
+      out(N - k, ei + c * oi - s * orr);
+    }
+  }
+}
+
+template <int N, class In, class Out>
+GB_D void gb_hc2r_io(In in, Out out, const double *__restrict__ tw) {
+  if constexpr (N == 1) {
+    out(0, in(0));
+  } else {
+    constexpr int H = N / 2;
+    double zr[H], zi[H];
+    {
+      const double i0 = in(0), ih = in(H);
+      zr[0] = 0.5 * (i0 + ih);
+      zi[0] = 0.5 * (i0 - ih);
+    }
+#pragma unroll
+    for (int k = 1; k < H; ++k) {
+      const double xr = in(k), xi = in(N - k);
+      const double cr = in(H - k), ci = -in(H + k);
+      const double er = 0.5 * (xr + cr), ei = 0.5 * (xi + ci);
+      const double dr = xr - cr, di = xi - ci;
+      const double c = tw[k], s = tw[N + k];
+      const double orr = 0.5 * (c * dr - s * di), oi = 0.5 * (c * di + s * dr);
+      zr[k] = er - oi;
+      zi[k] = ei + orr;
+    }
+    if constexpr (H > 1) gb_cfft<H, N, true>(zr, zi, tw);
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      out(2 * j, 2.0 * zr[j]);
+      out(2 * j + 1, 2.0 * zi[j]);
+    }
   }
 }

@@ -1,0 +1,248 @@
+// k_mts.cu -- the multiple-time-step block of evolve_pi in one kernel (FP64).
+//
+// evolve_pi.f90:82-161 and 222-228: the opening kicks, the forward normal-mode
+// transforms of p and r, mts substeps of {free ring-polymer rotation, back
+// transform of r, intramolecular forces on every bead, virial kinetic-energy
+// partial sums, forward transform of the forces and the momentum kick}, and the
+// closing back transform of p with the last half kick.  None of these couples
+// different molecules, so one block owns whole ring polymers of MPB molecules:
+// each of its 9*MPB threads holds one coordinate row (atom, xyz) of p and r in
+// registers and runs the transforms in registers (gb_fft.cuh); the bead
+// positions and intramolecular forces of a substep pass between the row view
+// and the (molecule, bead) view through shared memory.  HBM traffic per step is
+// one read of p, r, dvdr, dvdr2 (dvdr once more per substep for the estimator)
+// and one write of p, r, rnm, dvdr2.
+#include "gb_common.cuh"
+#include "gb_fft.cuh"
+#include "gb_intra.cuh"
+#include "gb_kernels.h"
+
+namespace {
+
+template <int NB>
+struct MtsCfg {
+  static constexpr int MPB = NB <= 32 ? 32 : 16;  // molecules per block
+  static constexpr int T = 9 * MPB;               // threads: one per coordinate row
+  static constexpr int LD = NB + 1;               // padded bead stride in shared memory
+};
+
+struct MtsArgs {
+  double *p, *r, *rnm, *dvdr2;
+  const double *dvdr;
+  const double *monod;  // monod(ic, c, k) at ic + 3*(c + 4*k)
+  const double *tw;     // twiddles of length nb
+  double *acc_int, *acc_ke;
+  int na, nm, mts, model;
+  double halfdt, dtsmall, halfdtsmall;
+  IntraPar ip;
+};
+
+template <int NB>
+__global__ void __launch_bounds__(MtsCfg<NB>::T, 1) k_mts_fused(MtsArgs a) {
+  using C = MtsCfg<NB>;
+  extern __shared__ double sm[];
+  double *s_rst = sm;                              // [MPB*9][LD]
+  double *s_f2 = s_rst + C::MPB * 9 * C::LD;       // [MPB*9][LD]
+  double *s_mono = s_f2 + C::MPB * 9 * C::LD;      // [12*NB]
+  double *s_tw = s_mono + 12 * NB;                 // [2*NB]
+  double *s_red = s_tw + 2 * NB;                   // [32 warps][18]
+  const int t = threadIdx.x;
+  for (int i = t; i < 12 * NB; i += C::T) s_mono[i] = a.monod[i];
+  for (int i = t; i < 2 * NB; i += C::T) s_tw[i] = a.tw[i];
+
+  // Every thread runs the same instruction stream between barriers: rows past
+  // the last molecule work on a copy of the last molecule and store nothing.
+  const int m0 = blockIdx.x * C::MPB;
+  const int ml = t / 9, lr = t % 9;           // local molecule, row within molecule
+  const int m = m0 + ml;
+  const bool valid = m < a.nm;
+  const int mc = valid ? m : a.nm - 1;        // molecule whose data this row reads
+  const long long S = 3LL * a.na;             // stride between beads
+  const long long row = 9LL * mc + lr;        // global coordinate row
+  const int ic = lr / 3;                      // atom type O, H, H
+  const int xyz = lr % 3;
+
+  double p[NB], x[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    const double pj = a.p[row + S * j] - a.halfdt * a.dvdr[row + S * j];
+    p[j] = pj - a.halfdtsmall * a.dvdr2[row + S * j];
+    x[j] = a.r[row + S * j];
+  }
+  __syncthreads();
+  const double sc = sqrt(1.0 / (double)NB);
+  gb_r2hc_io<NB>([&](int j) { return p[j]; }, [&](int k, double v) { p[k] = sc * v; }, s_tw);
+  gb_r2hc_io<NB>([&](int j) { return x[j]; }, [&](int k, double v) { x[k] = sc * v; }, s_tw);
+
+  double e_last = 0.0, vir[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double q1 = 0.0, q2 = 0.0;
+  for (int im = 1; im <= a.mts; ++im) {
+    {
+      // free ring-polymer rotation (evolve_pi.f90:109-125)
+#pragma unroll
+      for (int k = 0; k < NB; ++k) {
+        const double *mo = s_mono + ic + 12 * k;
+        const double pp = p[k] * mo[0] + x[k] * mo[3];
+        x[k] = p[k] * mo[6] + x[k] * mo[9];
+        p[k] = pp;
+      }
+      // bead positions rst = HC2R(r) (evolve_pi.f90:141-145)
+      double *dst = s_rst + (ml * 9 + lr) * C::LD;
+      gb_hc2r_io<NB>([&](int j) { return x[j]; }, [&](int k, double v) { dst[k] = sc * v; }, s_tw);
+    }
+    __syncthreads();
+    // intramolecular forces per (molecule, bead) (forces(rst, ..., 4)); rows of
+    // molecules past the end hold copies and are left out of the sums
+    double e_sub = 0.0;
+    for (int idx = t; idx < C::MPB * NB; idx += C::T) {
+      const int mm = idx / NB, j = idx % NB;
+      const double w = (m0 + mm < a.nm) ? 1.0 : 0.0;
+      double xm[9], fm[9], vm[9];
+#pragma unroll
+      for (int d = 0; d < 9; ++d) xm[d] = s_rst[(mm * 9 + d) * C::LD + j];
+      e_sub += w * intra_molecule(a.model, xm, fm, vm, a.ip);
+#pragma unroll
+      for (int d = 0; d < 9; ++d) {
+        s_f2[(mm * 9 + d) * C::LD + j] = fm[d];
+        vir[d] += w * vm[d];
+      }
+    }
+    if (im == a.mts) e_last = e_sub;
+    __syncthreads();
+    {
+      // virial_ke partial sums (kinetic.f90:23-40)
+      const double *rs_row = s_rst + (ml * 9 + lr) * C::LD;
+      const double *f2_row = s_f2 + (ml * 9 + lr) * C::LD;
+      double rc = 0.0;
+#pragma unroll
+      for (int j = 0; j < NB; ++j) rc = rc + rs_row[j];
+      rc = rc / (double)NB;
+      const double w = valid ? 1.0 : 0.0;
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const double dr = w * (rs_row[j] - rc);
+        q1 += dr * a.dvdr[row + S * j];
+        q2 += dr * f2_row[j];
+      }
+      if (im != a.mts) {  // FT(dvdr2) and p -= dtsmall dvdr2 (evolve_pi.f90:156-159)
+        const double dts = a.dtsmall;
+        gb_r2hc_io<NB>([&](int j) { return f2_row[j]; },
+                       [&](int k, double v) { p[k] = p[k] - dts * (sc * v); }, s_tw);
+      }
+    }
+    if (im != a.mts) __syncthreads();
+  }
+  {
+    // back to beads: p = HC2R(p); r = rst; p -= halfdtsmall dvdr2 (evolve_pi.f90:222-228)
+    const double *rs_row = s_rst + (ml * 9 + lr) * C::LD;
+    const double *f2_row = s_f2 + (ml * 9 + lr) * C::LD;
+    const double hds = a.halfdtsmall;
+    double *gp = a.p + row;
+    gb_hc2r_io<NB>([&](int j) { return p[j]; },
+                   [&](int k, double v) {
+                     if (valid) gp[S * k] = sc * v - hds * f2_row[k];
+                   }, s_tw);
+    if (valid) {
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        a.r[row + S * j] = rs_row[j];
+        a.rnm[row + S * j] = x[j];
+        a.dvdr2[row + S * j] = f2_row[j];
+      }
+    }
+  }
+  // block sums: [0] last-substep intra energy, [1..9] intra virial summed over
+  // substeps, [10] tq1, [11] tq2, [12..14] tq1 per xyz, [15..17] tq2 per xyz
+  double red[18];
+  red[0] = e_last;
+#pragma unroll
+  for (int d = 0; d < 9; ++d) red[1 + d] = vir[d];
+  red[10] = q1;
+  red[11] = q2;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    red[12 + d] = d == xyz ? q1 : 0.0;
+    red[15 + d] = d == xyz ? q2 : 0.0;
+  }
+  const int lane = t & 31, warp = t >> 5, nw = (C::T + 31) / 32;
+#pragma unroll
+  for (int i = 0; i < 18; ++i) {
+    double v = warp_sum(red[i]);
+    if (lane == 0) s_red[warp * 18 + i] = v;
+  }
+  __syncthreads();
+  if (t < 18) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += s_red[w * 18 + t];
+    if (s != 0.0) {
+      if (t < 10) atomicAdd(a.acc_int + t, s);
+      else if (t < 12) atomicAdd(a.acc_ke + (t - 10), s);
+      else atomicAdd(a.acc_ke + 2 + (t - 12), s);
+    }
+  }
+}
+
+template <int NB>
+size_t mts_smem() {
+  using C = MtsCfg<NB>;
+  return sizeof(double) * (2 * C::MPB * 9 * C::LD + 12 * NB + 2 * NB + 32 * 18);
+}
+
+template <int NB>
+void launch_nb(cudaStream_t s, const MtsArgs &a) {
+  using C = MtsCfg<NB>;
+  static bool attr = false;
+  const size_t smem = mts_smem<NB>();
+  if (!attr) {
+    cudaFuncSetAttribute(k_mts_fused<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  const unsigned grid = (unsigned)((a.nm + C::MPB - 1) / C::MPB);
+  k_mts_fused<NB><<<grid, C::T, smem, s>>>(a);
+}
+
+int intra_model_of(const gb_params &P) {
+  if (P.intra_model == GB_INTRA_SPCFW) return 1;
+  return P.alp == 0.0 ? 0 : 2;
+}
+
+}  // namespace
+
+// Runs the fused block when nb is a power of two up to 64; *used = 0 otherwise.
+void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used) {
+  *used = 0;
+  const int nb = c->nb;
+  if (nb != 2 && nb != 4 && nb != 8 && nb != 16 && nb != 32 && nb != 64) return;
+  MtsArgs a;
+  a.p = c->p;
+  a.r = c->r;
+  a.rnm = c->rnm;
+  a.dvdr2 = c->dvdr2;
+  a.dvdr = c->dvdr;
+  a.monod = c->monod;
+  a.tw = c->tw_nb;
+  a.acc_int = c->acc + (size_t)ACC_INT * ACC_STRIDE;
+  a.acc_ke = c->acc + (size_t)ACC_KE * ACC_STRIDE;
+  a.na = c->na;
+  a.nm = c->nm;
+  a.mts = c->P.mts;
+  a.model = intra_model_of(c->P);
+  a.halfdt = 0.5 * dt;
+  a.dtsmall = dt / (double)c->P.mts;
+  a.halfdtsmall = 0.5 * a.dtsmall;
+  a.ip.reoh = c->P.reoh;
+  a.ip.theta = c->P.theta;
+  a.ip.rehh = 2.0 * sin(0.5 * c->P.theta) * c->P.reoh;
+  a.ip.apot = c->P.apot;
+  a.ip.bpot = c->P.bpot;
+  a.ip.alp = c->P.alp;
+  switch (nb) {
+    case 2: launch_nb<2>(s, a); break;
+    case 4: launch_nb<4>(s, a); break;
+    case 8: launch_nb<8>(s, a); break;
+    case 16: launch_nb<16>(s, a); break;
+    case 32: launch_nb<32>(s, a); break;
+    case 64: launch_nb<64>(s, a); break;
+  }
+  *used = 1;
+}

@@ -52,13 +52,19 @@ GB_D bool exact_pair_in(const PairGeom &g, const double *a, const double *b) {
   return dsq3(dx, dy, dz) < g.rcutsq;
 }
 
-__global__ void __launch_bounds__(LB_T) k_build_list(PairGeom g, const float4 *frac, int *count,
-                                                     int *idx, int cap, float3 len, float thr_lo,
-                                                     float thr_hi, unsigned *status) {
+// Block (i-tile, j-chunk, configuration): each thread tests its point i against
+// a 1024-point chunk of partners staged through shared memory and appends hits
+// with an atomic counter per point, so the order inside a list is arbitrary.
+constexpr int LB_JCHUNK = 1024;
+
+__global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *frac, int *count,
+                                                      int *idx, int cap, float3 len, float thr_lo,
+                                                      float thr_hi, unsigned *status) {
   __shared__ float4 tile[LB_T];
-  const int c = blockIdx.y;
+  const int c = blockIdx.z;
   const int i = blockIdx.x * LB_T + threadIdx.x;
   const int npt = g.npt;
+  const int j0 = blockIdx.y * LB_JCHUNK, j1 = min(npt, j0 + LB_JCHUNK);
   const float4 *fr = frac + (long long)c * npt;
   const double *base = g.pos + c * g.cstride;
   float4 fi = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -70,14 +76,15 @@ __global__ void __launch_bounds__(LB_T) k_build_list(PairGeom g, const float4 *f
     pi[1] = x[1];
     pi[2] = x[2];
   }
-  int n = 0;
+  int *cnt = count + (long long)c * npt + (i < npt ? i : 0);
   int *my = idx + ((long long)c * npt + (i < npt ? i : 0)) * cap;
-  for (int jt = 0; jt < npt; jt += LB_T) {
+  bool over = false;
+  for (int jt = j0; jt < j1; jt += LB_T) {
     const int jl = jt + threadIdx.x;
-    tile[threadIdx.x] = jl < npt ? fr[jl] : make_float4(0.5f, 0.5f, 0.5f, 0.f);
+    tile[threadIdx.x] = jl < j1 ? fr[jl] : make_float4(0.5f, 0.5f, 0.5f, 0.f);
     __syncthreads();
     if (i < npt) {
-      const int jmax = min(LB_T, npt - jt);
+      const int jmax = min(LB_T, j1 - jt);
       for (int jj = 0; jj < jmax; ++jj) {
         const int j = jt + jj;
         if (j == i) continue;
@@ -93,17 +100,15 @@ __global__ void __launch_bounds__(LB_T) k_build_list(PairGeom g, const float4 *f
         bool ok = d2 < thr_lo;
         if (!ok) ok = exact_pair_in(g, pi, base + (long long)j * g.pstride);
         if (ok) {
-          if (n < cap) my[n] = j;
-          ++n;
+          const int slot = atomicAdd(cnt, 1);
+          if (slot < cap) my[slot] = j;
+          else over = true;
         }
       }
     }
     __syncthreads();
   }
-  if (i < npt) {
-    count[(long long)c * npt + i] = min(n, cap);
-    if (n > cap) atomicOr(status, ST_LIST_OVERFLOW);
-  }
+  if (over) atomicOr(status, ST_LIST_OVERFLOW);
 }
 
 // ---- M-site substitution and scaling (md_forces.f90:179-188, ewald_cubic.f90:20-22) ----
@@ -161,7 +166,7 @@ __global__ void __launch_bounds__(128) k_ewald_real(const double *rs, const doub
     double *G = g + (long long)c * na * 3;
     const double xi = R[3 * i], yi = R[3 * i + 1], zi = R[3 * i + 2], qi = q[i];
     const int mi = i / 3;
-    const int n = count[(long long)c * na + i];
+    const int n = min(count[(long long)c * na + i], cap);
     const int *L = idx + ((long long)c * na + i) * cap;
     double fx = 0, fy = 0, fz = 0;
     for (int t = 0; t < n; ++t) {
@@ -214,7 +219,7 @@ __global__ void __launch_bounds__(128) k_lj(const double *r, int na, int npt, in
     const double *R = r + (long long)c * na * 3;
     double *F = out + (long long)c * na * 3;
     const int lc = nconf_list == 1 ? 0 : c;
-    const int n = count[(long long)lc * npt + o];
+    const int n = min(count[(long long)lc * npt + o], cap);
     const int *L = idx + ((long long)lc * npt + o) * cap;
     const double xo = R[9 * o], yo = R[9 * o + 1], zo = R[9 * o + 2];
     double fx = 0, fy = 0, fz = 0;
@@ -266,7 +271,7 @@ __global__ void __launch_bounds__(128) k_tem(const double *rs, const double *q, 
     const double *R = rs + (long long)c * na * 3;
     double *G = g + (long long)c * na * 3;
     const int lc = nconf_list == 1 ? 0 : c;
-    const int n = count[(long long)lc * na + i];
+    const int n = min(count[(long long)lc * na + i], cap);
     const int *L = idx + ((long long)lc * na + i) * cap;
     const double xo = R[3 * i], yo = R[3 * i + 1], zo = R[3 * i + 2], qo = q[i];
     double fx = 0, fy = 0, fz = 0;
@@ -362,8 +367,9 @@ void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float
   // pairs within 4e-6 * lmax^2 of the cut-off go to the exact FP64 test
   const double band = 4e-6 * lmax * lmax;
   const float thr_lo = (float)(g.rcutsq - band), thr_hi = (float)(g.rcutsq + band);
-  dim3 grid(nblk(g.npt, LB_T), nconf);
-  k_build_list<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status);
+  cudaMemsetAsync(pl.count, 0, sizeof(int) * (size_t)nconf * g.npt, s);
+  dim3 grid(nblk(g.npt, LB_T), nblk(g.npt, LB_JCHUNK), nconf);
+  k_build_list2<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status);
 }
 
 void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, double alpha,

@@ -501,6 +501,16 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   cudaStream_t s = c->stream;
   CK(cudaMemsetAsync(c->acc, 0, sizeof(double) * ACC_NSLOT * ACC_STRIDE, s));
   prof_begin(c, PR_MTS);
+  // one fused kernel for power-of-two nb up to 64 (k_mts.cu)
+  int fused = 0;
+  if (!c->generic_mts) launch_fused_mts(s, c, dt, &fused);
+  if (fused) {
+    c->plan.B_int = nb;
+    c->launches += 1;
+    prof_end(c, PR_MTS, (double)c->nm * nb * mts);
+    if ((st = low_frequency(c, c->rnm, c->r, c->p, halfdt))) return st;
+    return launch_status();
+  }
   // evolve_pi.f90:82-88
   launch_axpy(s, c->p, c->dvdr, -halfdt, N);
   launch_axpy(s, c->p, c->dvdr2, -halfdtsmall, N);

@@ -154,6 +154,10 @@ def test_golden_replay_evolve_pi():
     dict(param="param_qspcfw", ncell=(4, 4, 4), nb=8, mts=3, nbdf1=1, nbdf2=3),
     dict(param="param_qspcfw", ncell=(4, 4, 4), nb=8, mts=1),
     dict(param="param_qspcfw", ncell=(4, 4, 4), nb=16, mts=5, nbdf1=1, nbdf2=5, dtfs=1.25),
+    dict(param="param_qspcfw", ncell=(3, 3, 3), nb=32, mts=2, nbdf1=1, nbdf2=3),   # fused MTS, nb = 32
+    dict(param="param_qspcfw", ncell=(3, 3, 3), nb=64, mts=1),                     # fused MTS, nb = 64
+    dict(param="param_qspcfw", ncell=(3, 3, 3), nb=6, mts=2, nbdf1=3, nbdf2=5),    # separate kernels
+    dict(param="param_scott", ncell=(3, 3, 3), nb=4, mts=5, nbdf1=1, nbdf2=3, sig_A=4.5),  # TEM, morse
 ])
 def test_evolve_pi_steps(case):
     s = setup(**case)
