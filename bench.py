@@ -42,9 +42,11 @@ DEFAULT = "qspcfw_4096_nb32_mts5_contracted"
 REGIONS = ["mts_block", "pair_lists", "ewald_real", "recip_sk", "recip_weights", "recip_force", "lj",
            "tem", "expand_kick", "msite", "rattle"]
 # algorithmic FP64 flops per work unit of a region (declared weights):
-# real-space in-cut pair 60, reciprocal (k, site) 16 split 8 + 8 between the
-# structure-factor and the force pass, LJ pair 45
-FLOPS_PER_UNIT = {"ewald_real": 60.0, "recip_sk": 8.0, "recip_force": 8.0, "lj": 45.0}
+# real-space in-cut pair 60; reciprocal (k vector, site) 12 with kz and -kz
+# taken together: 4 in the structure-factor pass (two complex-times-real FMAs
+# per pair of vectors), 8 in the force pass (eight FMAs per pair of vectors);
+# LJ pair 45
+FLOPS_PER_UNIT = {"ewald_real": 60.0, "recip_sk": 4.0, "recip_force": 8.0, "lj": 45.0}
 
 
 def log(*a):

@@ -157,8 +157,8 @@ void ctx_free(gb_context *c) {
   if (c->d_count) cudaFree(c->d_count);
   for (void *p : c->allocs) cudaFree(p);
   c->allocs.clear();
-  for (void *p : {(void *)c->pl.idx, (void *)c->pl.count, (void *)c->kxy, (void *)c->kxy_koff,
-                  (void *)c->klist, (void *)c->kw, (void *)c->sk_part, (void *)c->sk,
+  for (void *p : {(void *)c->pl.idx, (void *)c->pl.count, (void *)c->kcol, (void *)c->kgrp,
+                  (void *)c->kpair, (void *)c->kw, (void *)c->ktab, (void *)c->sk_part, (void *)c->sk,
                   (void *)c->tw_nb, (void *)c->tw_c1, (void *)c->tw_c2})
     if (p) cudaFree(p);
   if (c->h_acc) cudaFreeHost(c->h_acc);

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/gbrpmd.h"
+#include "gb_kvec.h"
 
 // One pair list: for each of `nconf` configurations and each of `npt` points,
 // up to `cap` partner indices; the pair (i, j) is stored once, in the list of
@@ -56,15 +57,18 @@ struct gb_context {
   size_t pl_idx_bytes = 0, pl_cnt_bytes = 0;
 
   // reciprocal space
-  int kmax_alloc = -1;
-  int nkxy = 0, nk = 0;          // (kx,ky) pairs and k vectors of the half space
-  int *kxy = nullptr;            // [nkxy][4]: kx, ky, kz_lo, kz_hi, sorted by kz range
-  int *kxy_koff = nullptr;       // [nkxy] offset of the pair's first k in the k list
-  int4 *klist = nullptr;         // [nk]: kx, ky, kz, pair index
-  double *sk_part = nullptr;     // [nconf][nchunk][nk][2]
-  double *sk = nullptr;          // [nconf][nk][2] weighted structure factors
-  size_t sk_part_bytes = 0, sk_bytes = 0;
-  double *kw = nullptr;          // [nk] weights (f / k^2) exp(-b k^2)
+  int kmax_alloc = -1;           // k tables built for these kmax, rkmax, walpha
+  double k_rkmax = -1.0, k_walpha = -1.0;
+  int ncol = 0, nkp = 0, ngrp = 0;  // (kx,ky) columns, k pairs (kx,ky,+-m), structure-factor items
+  int nk = 0;                   // k vectors of the half space
+  KCol *kcol = nullptr;         // [ncol] columns (gb_kvec.h)
+  int4 *kgrp = nullptr;         // [ngrp] structure-factor work items
+  int4 *kpair = nullptr;        // [nkp] kx, ky, m, kind
+  double *kw = nullptr;         // [nkp] weights (4 pi / k^2) exp(-b k^2)
+  double2 *ktab = nullptr;      // [nconf][na][3][kmax+1] per-site powers e^{i 2 pi m x}
+  double *sk_part = nullptr;    // [nconf][nchunk][nkp][4] chunk partials of P, Q
+  double *sk = nullptr;         // [nconf][nkp][8] force tables
+  size_t ktab_bytes = 0, sk_part_bytes = 0, sk_bytes = 0;
 
   // tables and accumulators
   double *tw_nb = nullptr, *tw_c1 = nullptr, *tw_c2 = nullptr;  // twiddles for nb, nbdf1, nbdf2

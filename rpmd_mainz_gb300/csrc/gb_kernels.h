@@ -5,6 +5,13 @@
 
 #include "gb_context.h"
 
+// reciprocal-space kernel geometry (k_recip.cu)
+int recip_sk_chunk();                // sites per structure-factor block
+int recip_group_len();               // m values per structure-factor work item
+size_t recip_sk_smem(int kmax);      // dynamic shared memory of the passes
+size_t recip_force_smem(int kmax);
+void recip_set_attributes();         // raises the kernels' shared-memory limit once
+
 // Geometry of one pair search.  Point i of configuration c sits at
 // pos[c * cstride + i * pstride + {0,1,2}] (doubles).  `unit` selects the
 // unit-box minimum image dx - nint(dx) (rwald, ewald_cubic.f90:121-126);
@@ -34,6 +41,7 @@ void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, do
                   double scale);
 void launch_ewald_real(cudaStream_t s, const double *rs, const double *q, int na, int B,
                        const PairList &pl, double alpha, double *g, double *acc);
+// structure factors: per-site power tables, then chunk partials (2 launches)
 void launch_recip_sk(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);
 void launch_recip_weights(cudaStream_t s, gb_context *c, int B, double *acc);
 void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B,

@@ -1,0 +1,116 @@
+// gb_kvec.h -- reciprocal-space k-vector tables (host side, no heap use).
+//
+// The half space of k vectors kept by kwald (ewald_cubic.f90:292-520): for
+// every kx >= 0 the (kx, ky) columns with kx^2 + ky^2 (times (2 pi)^2) within
+// rkmax^2, each holding kz = -kzm..kzm (kx = ky = 0: kz = 1..kz0).  Loop exits
+// follow the reference's tests and rounding.
+//
+// The device kernels pair kz with -kz: S(kx, ky, +-m) = P +- i Q with
+// P = sum q e^{i(kx x + ky y)} cos(2 pi m z), Q = ... sin(2 pi m z), so one
+// "k pair" (kx, ky, m) stands for one or two k vectors:
+//   kind 0: m = 0 (one vector), kind 1: m > 0 with both signs, kind 2: the
+//   kx = ky = 0 column, m > 0 with +m only.
+// Tables built here:
+//   KCol  per column: kx, ky, first k pair, m range, and kx, ky as doubles;
+//   kp    per k pair: kx, ky, m, kind;  kw per k pair: (4 pi / k^2) e^{-k^2 b};
+//   grp   structure-factor work items: up to G consecutive m of one column,
+//         full-length items first, then shorter ones by decreasing length.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "../../include/gbrpmd.h"
+
+struct alignas(16) KCol {
+  int kx, ky, koff, mm;  // mm = m_lo | (m_hi << 16)
+  double dkx, dky;
+};
+static_assert(sizeof(KCol) == 32, "KCol layout");
+
+struct KTables {
+  int ncol = 0, nkp = 0, ngrp = 0, nk = 0;  // nk: k vectors (both kz signs counted)
+};
+
+// Fills the caller's arrays (capacities cap_*); returns 0, or 1 when a
+// capacity is exceeded.  G: maximum m values per structure-factor work item.
+inline int gb_build_ktables(const gb_params &P, int G, KCol *col, int cap_col, int4 *kp, double *kw,
+                            int cap_kp, int4 *grp, int cap_grp, KTables *out) {
+  const double PI = 3.141592653589793238462643383279502884;
+  const int kmax = P.kmax;
+  const double rlat = 2.0 * PI;
+  const double rkmax2 = P.rkmax * P.rkmax;
+  const double b = 0.25 / (P.walpha * P.walpha);
+  KTables t;
+  auto add_col = [&](int kx, int ky, int mlo, int mhi) -> bool {
+    if (t.ncol >= cap_col || t.nkp + (mhi - mlo + 1) > cap_kp) return false;
+    KCol &c = col[t.ncol++];
+    c.kx = kx;
+    c.ky = ky;
+    c.koff = t.nkp;
+    c.mm = mlo | (mhi << 16);
+    c.dkx = (double)kx;
+    c.dky = (double)ky;
+    for (int m = mlo; m <= mhi; ++m) {
+      const int kind = (kx == 0 && ky == 0) ? 2 : (m == 0 ? 0 : 1);
+      kp[t.nkp] = make_int4(kx, ky, m, kind);
+      const double rkx = rlat * kx, rky = rlat * ky, rkz = rlat * m;
+      const double rk2 = rkx * rkx + rky * rky + rkz * rkz;
+      kw[t.nkp] = (2.0 * rlat / rk2) * std::exp(-b * rk2);  // 4 pi: k and -k
+      ++t.nkp;
+      t.nk += kind == 1 ? 2 : 1;
+    }
+    return true;
+  };
+  for (int kx = 0; kx <= kmax; ++kx) {
+    const double rkx = rlat * kx;
+    int kz0 = 0;  // ky = 0: kz = 1.. while rkx^2 + rkz^2 <= rkmax2
+    for (int kz = 1; kz <= kmax; ++kz) {
+      const double rkz = rlat * kz;
+      if (rkx * rkx + rkz * rkz > rkmax2) break;
+      kz0 = kz;
+    }
+    if (kx > 0) {
+      if (!add_col(kx, 0, 0, kz0)) return 1;
+    } else if (kz0 > 0) {
+      if (!add_col(0, 0, 1, kz0)) return 1;
+    }
+    for (int ky = 1; ky <= kmax; ++ky) {
+      const double rky = rlat * ky;
+      if (rkx * rkx + rky * rky > rkmax2) break;
+      int kzm = 0;
+      for (int kz = 1; kz <= kmax; ++kz) {
+        const double rkz = rlat * kz;
+        if (rkx * rkx + rky * rky + rkz * rkz > rkmax2) break;
+        kzm = kz;
+      }
+      if (!add_col(kx, ky, 0, kzm)) return 1;
+      if (kx > 0 && !add_col(kx, -ky, 0, kzm)) return 1;
+    }
+  }
+  // work items: full runs of G first, then the remainders by decreasing length
+  auto add_grp = [&](const KCol &c, int m0, int len) -> bool {
+    if (t.ngrp >= cap_grp) return false;
+    grp[t.ngrp++] = make_int4(c.kx | (len << 16), c.ky, m0, c.koff + (m0 - (c.mm & 0xffff)));
+    return true;
+  };
+  for (int i = 0; i < t.ncol; ++i) {
+    const int mlo = col[i].mm & 0xffff, mhi = col[i].mm >> 16;
+    for (int m0 = mlo; m0 + G - 1 <= mhi; m0 += G)
+      if (!add_grp(col[i], m0, G)) return 1;
+  }
+  for (int len = G - 1; len >= 1; --len) {
+    for (int i = 0; i < t.ncol; ++i) {
+      const int mlo = col[i].mm & 0xffff, mhi = col[i].mm >> 16;
+      const int n = mhi - mlo + 1;
+      if (n % G == len && !add_grp(col[i], mlo + (n / G) * G, len)) return 1;
+    }
+  }
+  *out = t;
+  return 0;
+}
+
+// capacities that always suffice for a given kmax
+inline int gb_kcap_col(int kmax) { return (kmax + 1) * (2 * kmax + 1); }
+inline int gb_kcap_kp(int kmax) { return gb_kcap_col(kmax) * (kmax + 1); }

@@ -151,16 +151,24 @@ __global__ void k_msite_chain(const double *g, double *out, int nm, int B, doubl
 }
 
 // ---- real-space Ewald (rwald, ewald_cubic.f90:78-233) in the unit box ----
-__global__ void __launch_bounds__(128) k_ewald_real(const double *rs, const double *q, int na,
-                                                    const int *count, const int *idx, int cap,
-                                                    double alpha, double *g, double *acc) {
-  __shared__ double sh[32 * 10];
+// rwald (ewald_cubic.f90:78-233) on a pair list, FP64.  Per pair one rsqrt
+// gives 1/dr, so that dr, erfc/dr and (sfac e - du)/dr^2 need no sqrt and no
+// division; only t = p/(p + x) of the A&S 7.1.26 erfc approximation divides.
+// The minimum image uses rint: every listed pair has drsq < wrcut^2 <= 1/4, so
+// no component sits at a rounding tie, where rint and Fortran's nint differ.
+// The virial is symmetric (dx dvy = dy dvx up to rounding): six sums, mirrored
+// when the block sums are added.
+__global__ void __launch_bounds__(128) k_ewald_real(const double *__restrict__ rs, const double *__restrict__ q,
+                                                    int na, const int *__restrict__ count,
+                                                    const int *__restrict__ idx, int cap, double alpha,
+                                                    double *g, double *acc) {
+  __shared__ double sh[32 * 7];
   const double p = 3.0525860, a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741,
                a4 = -1.453152027, a5 = 1.061405429;
   const double sfac = -2.0 * alpha / sqrt(acos(-1.0));
   const int c = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // v, vir(1..9) column-major
+  double vals[7] = {0, 0, 0, 0, 0, 0, 0};  // v, xx, xy, xz, yy, yz, zz
   if (i < na) {
     const double *R = rs + (long long)c * na * 3;
     double *G = g + (long long)c * na * 3;
@@ -172,18 +180,18 @@ __global__ void __launch_bounds__(128) k_ewald_real(const double *rs, const doub
     for (int t = 0; t < n; ++t) {
       const int j = L[t];
       double dx = xi - R[3 * j], dy = yi - R[3 * j + 1], dz = zi - R[3 * j + 2];
-      dx -= nint_d(dx);
-      dy -= nint_d(dy);
-      dz -= nint_d(dz);
+      dx -= rint(dx);
+      dy -= rint(dy);
+      dz -= rint(dz);
       const double drsq = dx * dx + dy * dy + dz * dz;
-      const double dr = sqrt(drsq);
-      const double x = alpha * dr;
+      const double inv = rsqrt(drsq);
+      const double x = alpha * (drsq * inv);
       const double e = exp(-x * x);
       const double tt = p / (p + x);
       double erfc = e * tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5))));
       if (mi == j / 3) erfc -= 1.0;
-      const double du = erfc / dr;
-      const double dur = (sfac * e - du) / drsq;
+      const double du = erfc * inv;
+      const double dur = (sfac * e - du) * (inv * inv);
       const double qij = qi * q[j];
       const double dv = qij * du, dvr = qij * dur;
       const double dvx = dvr * dx, dvy = dvr * dy, dvz = dvr * dz;
@@ -194,15 +202,38 @@ __global__ void __launch_bounds__(128) k_ewald_real(const double *rs, const doub
       atomicAdd(G + 3 * j + 1, -dvy);
       atomicAdd(G + 3 * j + 2, -dvz);
       vals[0] += dv;
-      vals[1] += dx * dvx; vals[2] += dy * dvx; vals[3] += dz * dvx;
-      vals[4] += dx * dvy; vals[5] += dy * dvy; vals[6] += dz * dvy;
-      vals[7] += dx * dvz; vals[8] += dy * dvz; vals[9] += dz * dvz;
+      vals[1] += dx * dvx;
+      vals[2] += dy * dvx;
+      vals[3] += dz * dvx;
+      vals[4] += dy * dvy;
+      vals[5] += dz * dvy;
+      vals[6] += dz * dvz;
     }
     atomicAdd(G + 3 * i, fx);
     atomicAdd(G + 3 * i + 1, fy);
     atomicAdd(G + 3 * i + 2, fz);
   }
-  block_sum_atomic<10>(vals, sh, acc);
+  // block sums; slot layout v, vir(1..3, 1..3) column-major
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    const double v = warp_sum(vals[k]);
+    if (lane == 0) sh[warp * 7 + k] = v;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int dst0[7] = {0, 1, 2, 3, 5, 6, 9};  // v, xx, yx, zx, yy, zy, zz
+    constexpr int dst1[7] = {-1, -1, 4, 7, -1, 8, -1};  // mirrored xy, xz, yz
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      double s2 = lane < nw ? sh[lane * 7 + k] : 0.0;
+      s2 = warp_sum(s2);
+      if (lane == 0 && s2 != 0.0) {
+        atomicAdd(acc + dst0[k], s2);
+        if (dst1[k] >= 0) atomicAdd(acc + dst1[k], s2);
+      }
+    }
+  }
 }
 
 // ---- Lennard-Jones O-O (lj_list / lj_basic / lj_cell, ljones.f90) ----

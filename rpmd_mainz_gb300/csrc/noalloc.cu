@@ -32,10 +32,6 @@
 #include "gb_context.h"
 #include "gb_kernels.h"
 
-size_t recip_sk_smem(int kmax, int nkxy);
-size_t recip_force_smem(int kmax);
-int recip_sk_chunk();
-void recip_set_attributes(size_t sk_smem, size_t f_smem);
 const gb_params &current_params();
 int ctx_set_error(int code, const std::string &msg);
 
@@ -54,77 +50,11 @@ __device__ __align__(256) unsigned char g_static_scratch[STATIC_SCRATCH_BYTES];
 unsigned char *g_scratch_ptr[MAX_DEVICES] = {nullptr};
 
 // host-side k tables (fixed size: no heap allocation)
-int h_kxy[4 * MAX_NKXY], h_koff[MAX_NKXY], h_klist[4 * MAX_NK];
+KCol h_col[MAX_NKXY];
+int4 h_kp[MAX_NK], h_grp[MAX_NK];
 double h_kw[MAX_NK];
 
 const double PI = 3.141592653589793238462643383279502884;
-
-// the reference's half-space k vectors (ewald_cubic.f90:292-520), grouped in
-// (kx, ky) columns sorted by kz range; returns GB_OK or an error
-int kvectors(const gb_params &P, int *nkxy, int *nk) {
-  const int kmax = P.kmax;
-  const double rlat = 2.0 * PI, rkmax2 = P.rkmax * P.rkmax, b = 0.25 / (P.walpha * P.walpha);
-  int cols[4 * MAX_NKXY];
-  int nc = 0;
-  auto push = [&](int kx, int ky, int lo, int hi) {
-    if (nc >= MAX_NKXY) return false;
-    cols[4 * nc] = kx; cols[4 * nc + 1] = ky; cols[4 * nc + 2] = lo; cols[4 * nc + 3] = hi;
-    ++nc;
-    return true;
-  };
-  for (int kx = 0; kx <= kmax; ++kx) {
-    const double rkx = rlat * kx;
-    int kz0 = 0;
-    for (int kz = 1; kz <= kmax; ++kz) {
-      double rkz = rlat * kz;
-      if (rkx * rkx + rkz * rkz > rkmax2) break;
-      kz0 = kz;
-    }
-    bool ok = true;
-    if (kx > 0) ok = push(kx, 0, -kz0, kz0);
-    else if (kz0 > 0) ok = push(0, 0, 1, kz0);
-    if (!ok) return ctx_set_error(GB_E_NOMEM, "static Ewald: more than 512 (kx, ky) columns");
-    for (int ky = 1; ky <= kmax; ++ky) {
-      const double rky = rlat * ky;
-      if (rkx * rkx + rky * rky > rkmax2) break;
-      int kzm = 0;
-      for (int kz = 1; kz <= kmax; ++kz) {
-        double rkz = rlat * kz;
-        if (rkx * rkx + rky * rky + rkz * rkz > rkmax2) break;
-        kzm = kz;
-      }
-      if (!push(kx, ky, -kzm, kzm) || (kx > 0 && !push(kx, -ky, -kzm, kzm)))
-        return ctx_set_error(GB_E_NOMEM, "static Ewald: more than 512 (kx, ky) columns");
-    }
-  }
-  // insertion sort by descending kz range (stable)
-  for (int i = 1; i < nc; ++i) {
-    int t[4] = {cols[4 * i], cols[4 * i + 1], cols[4 * i + 2], cols[4 * i + 3]};
-    int j = i - 1;
-    while (j >= 0 && (cols[4 * j + 3] - cols[4 * j + 2]) < (t[3] - t[2])) {
-      for (int d = 0; d < 4; ++d) cols[4 * (j + 1) + d] = cols[4 * j + d];
-      --j;
-    }
-    for (int d = 0; d < 4; ++d) cols[4 * (j + 1) + d] = t[d];
-  }
-  int n = 0;
-  for (int p = 0; p < nc; ++p) {
-    for (int d = 0; d < 4; ++d) h_kxy[4 * p + d] = cols[4 * p + d];
-    h_koff[p] = n;
-    for (int kz = cols[4 * p + 2]; kz <= cols[4 * p + 3]; ++kz) {
-      if (n >= MAX_NK) return ctx_set_error(GB_E_NOMEM, "static Ewald: more than 2048 k vectors");
-      h_klist[4 * n] = cols[4 * p]; h_klist[4 * n + 1] = cols[4 * p + 1];
-      h_klist[4 * n + 2] = kz; h_klist[4 * n + 3] = p;
-      double rkx = rlat * cols[4 * p], rky = rlat * cols[4 * p + 1], rkz = rlat * kz;
-      double rk2 = rkx * rkx + rky * rky + rkz * rkz;
-      h_kw[n] = (2.0 * rlat / rk2) * std::exp(-b * rk2);
-      ++n;
-    }
-  }
-  *nkxy = nc;
-  *nk = n;
-  return GB_OK;
-}
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -159,11 +89,12 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
     SCK(cudaGetSymbolAddress(&p, g_static_scratch));
     g_scratch_ptr[dev] = (unsigned char *)p;
   }
-  int nkxy = 0, nk = 0;
-  int st = kvectors(P, &nkxy, &nk);
-  if (st) return st;
-  if (recip_sk_smem(P.kmax, nkxy) > 227 * 1024 || recip_force_smem(P.kmax) > 227 * 1024)
+  if (P.kmax < 0 || recip_sk_smem(P.kmax) > 227 * 1024 || recip_force_smem(P.kmax) > 227 * 1024)
     return ctx_set_error(GB_E_NOMEM, "static Ewald: kmax too large for the reciprocal-space kernels");
+  KTables kt;
+  if (gb_build_ktables(P, recip_group_len(), h_col, MAX_NKXY, h_kp, h_kw, MAX_NK, h_grp, MAX_NK, &kt) ||
+      kt.nk > MAX_NK)
+    return ctx_set_error(GB_E_NOMEM, "static Ewald: more than 2048 k vectors or 512 (kx, ky) columns");
   const int nchunk = (n + recip_sk_chunk() - 1) / recip_sk_chunk();
   const size_t N = 3 * (size_t)n * B;
   double onepivol = (4.0 / 3.0) * PI * P.wrcut * P.wrcut * P.wrcut;
@@ -184,12 +115,13 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   float4 *d_frac = (float4 *)take(sizeof(float4) * (size_t)n * B);
   int *d_cnt = (int *)take(sizeof(int) * (size_t)n * B);
   int *d_idx = (int *)take(sizeof(int) * (size_t)n * B * cap);
-  int *d_kxy = (int *)take(sizeof(int) * 4 * nkxy);
-  int *d_koff = (int *)take(sizeof(int) * nkxy);
-  int4 *d_klist = (int4 *)take(sizeof(int4) * nk);
-  double *d_kw = (double *)take(sizeof(double) * nk);
-  double *d_skp = (double *)take(sizeof(double) * 2 * (size_t)nk * nchunk * B);
-  double *d_sk = (double *)take(sizeof(double) * 2 * (size_t)nk * B);
+  KCol *d_col = (KCol *)take(sizeof(KCol) * kt.ncol);
+  int4 *d_grp = (int4 *)take(sizeof(int4) * kt.ngrp);
+  int4 *d_kp = (int4 *)take(sizeof(int4) * kt.nkp);
+  double *d_kw = (double *)take(sizeof(double) * kt.nkp);
+  double2 *d_tab = (double2 *)take(sizeof(double2) * 3 * (size_t)(P.kmax + 1) * n * B);
+  double *d_skp = (double *)take(sizeof(double) * 4 * (size_t)kt.nkp * nchunk * B);
+  double *d_sk = (double *)take(sizeof(double) * 8 * (size_t)kt.nkp * B);
   double *d_acc = (double *)take(sizeof(double) * ACC_STRIDE);
   unsigned *d_status = (unsigned *)take(sizeof(unsigned));
   if (off > STATIC_SCRATCH_BYTES) return ctx_set_error(GB_E_NOMEM, "static Ewald: working set exceeds the 16 MiB buffer");
@@ -197,10 +129,10 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   cudaStream_t s = 0;  // legacy default stream: no stream object is created
   SCK(cudaMemcpyAsync(d_r, r, sizeof(double) * N, cudaMemcpyHostToDevice, s));
   SCK(cudaMemcpyAsync(d_z, z, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  SCK(cudaMemcpyAsync(d_kxy, h_kxy, sizeof(int) * 4 * nkxy, cudaMemcpyHostToDevice, s));
-  SCK(cudaMemcpyAsync(d_koff, h_koff, sizeof(int) * nkxy, cudaMemcpyHostToDevice, s));
-  SCK(cudaMemcpyAsync(d_klist, h_klist, sizeof(int) * 4 * nk, cudaMemcpyHostToDevice, s));
-  SCK(cudaMemcpyAsync(d_kw, h_kw, sizeof(double) * nk, cudaMemcpyHostToDevice, s));
+  SCK(cudaMemcpyAsync(d_col, h_col, sizeof(KCol) * kt.ncol, cudaMemcpyHostToDevice, s));
+  SCK(cudaMemcpyAsync(d_grp, h_grp, sizeof(int4) * kt.ngrp, cudaMemcpyHostToDevice, s));
+  SCK(cudaMemcpyAsync(d_kp, h_kp, sizeof(int4) * kt.nkp, cudaMemcpyHostToDevice, s));
+  SCK(cudaMemcpyAsync(d_kw, h_kw, sizeof(double) * kt.nkp, cudaMemcpyHostToDevice, s));
   // cleared every call: gradient accumulator, energy/virial sums, status word
   SCK(cudaMemsetAsync(d_g, 0, sizeof(double) * N, s));
   SCK(cudaMemsetAsync(d_acc, 0, sizeof(double) * ACC_STRIDE, s));
@@ -211,15 +143,18 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   view.nb = B;
   view.nm = n / 3;
   view.P = P;
-  view.nkxy = nkxy;
-  view.nk = nk;
-  view.kxy = d_kxy;
-  view.kxy_koff = d_koff;
-  view.klist = d_klist;
+  view.ncol = kt.ncol;
+  view.nkp = kt.nkp;
+  view.ngrp = kt.ngrp;
+  view.nk = kt.nk;
+  view.kcol = d_col;
+  view.kgrp = d_grp;
+  view.kpair = d_kp;
   view.kw = d_kw;
+  view.ktab = d_tab;
   view.sk_part = d_skp;
   view.sk = d_sk;
-  recip_set_attributes(recip_sk_smem(P.kmax, nkxy), recip_force_smem(P.kmax));
+  recip_set_attributes();
 
   const double L = boxlxyz[0], onboxl = 1.0 / L;
   launch_msite(s, d_r, d_rs, n, B, P.alpha, onboxl);

@@ -16,12 +16,6 @@
 #include "gb_context.h"
 #include "gb_kernels.h"
 
-// from k_recip.cu
-size_t recip_sk_smem(int kmax, int nkxy);
-size_t recip_force_smem(int kmax);
-int recip_sk_chunk();
-void recip_set_attributes(size_t sk_smem, size_t f_smem);
-
 namespace {
 
 const double PI = 3.141592653589793238462643383279502884;
@@ -87,83 +81,52 @@ void ring_rpmd_host(const double *mass3, int nb, double dt, double beta, double 
 }
 
 // half-space k vectors with the reference's loop-exit membership
-// (ewald_cubic.f90:292-520), grouped in (kx, ky) columns
+// (ewald_cubic.f90:292-520) as (kx, ky) columns and +-kz pairs (gb_kvec.h),
+// plus the per-evaluation buffers for up to max(nb, 1) configurations
 int build_kvectors(gb_context *c) {
   const int kmax = c->P.kmax;
-  const double rlat = 2.0 * PI;
-  const double rkmax2 = c->P.rkmax * c->P.rkmax;
-  const double b = 0.25 / (c->P.walpha * c->P.walpha);
-  struct Col { int kx, ky, lo, hi; };
-  std::vector<Col> cols;
-  for (int kx = 0; kx <= kmax; ++kx) {
-    const double rkx = rlat * kx;
-    int kz0 = 0;  // ky = 0: kz = 1.. while rkx^2 + rkz^2 <= rkmax2
-    for (int kz = 1; kz <= kmax; ++kz) {
-      double rkz = rlat * kz;
-      if (rkx * rkx + rkz * rkz > rkmax2) break;
-      kz0 = kz;
-    }
-    if (kx > 0) cols.push_back({kx, 0, -kz0, kz0});
-    else if (kz0 > 0) cols.push_back({0, 0, 1, kz0});
-    for (int ky = 1; ky <= kmax; ++ky) {
-      const double rky = rlat * ky;
-      if (rkx * rkx + rky * rky > rkmax2) break;
-      int kzm = 0;
-      for (int kz = 1; kz <= kmax; ++kz) {
-        double rkz = rlat * kz;
-        if (rkx * rkx + rky * rky + rkz * rkz > rkmax2) break;
-        kzm = kz;
-      }
-      cols.push_back({kx, ky, -kzm, kzm});
-      if (kx > 0) cols.push_back({kx, -ky, -kzm, kzm});
-    }
-  }
-  std::stable_sort(cols.begin(), cols.end(), [](const Col &a, const Col &b2) {
-    return (a.hi - a.lo) > (b2.hi - b2.lo);
-  });
-  std::vector<int> kxy(4 * cols.size()), koff(cols.size());
-  std::vector<int> klist;
-  std::vector<double> kw;
-  int nk = 0;
-  for (size_t p = 0; p < cols.size(); ++p) {
-    const Col &cl = cols[p];
-    kxy[4 * p] = cl.kx; kxy[4 * p + 1] = cl.ky; kxy[4 * p + 2] = cl.lo; kxy[4 * p + 3] = cl.hi;
-    koff[p] = nk;
-    for (int kz = cl.lo; kz <= cl.hi; ++kz) {
-      klist.push_back(cl.kx); klist.push_back(cl.ky); klist.push_back(kz); klist.push_back((int)p);
-      double rkx = rlat * cl.kx, rky = rlat * cl.ky, rkz = rlat * kz;
-      double rk2 = rkx * rkx + rky * rky + rkz * rkz;
-      double f = 2.0 * rlat;  // 4 pi: each k stands for k and -k
-      kw.push_back((f / rk2) * std::exp(-b * rk2));
-      ++nk;
-    }
-  }
-  for (void *p : {(void *)c->kxy, (void *)c->kxy_koff, (void *)c->klist, (void *)c->kw})
-    if (p) cudaFree(p);
-  c->nkxy = (int)cols.size();
-  c->nk = nk;
-  CK(cudaMalloc(&c->kxy, sizeof(int) * kxy.size()));
-  CK(cudaMalloc(&c->kxy_koff, sizeof(int) * koff.size()));
-  CK(cudaMalloc(&c->klist, sizeof(int) * klist.size()));
-  CK(cudaMalloc(&c->kw, sizeof(double) * kw.size()));
-  CK(cudaMemcpy(c->kxy, kxy.data(), sizeof(int) * kxy.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c->kxy_koff, koff.data(), sizeof(int) * koff.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c->klist, klist.data(), sizeof(int) * klist.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c->kw, kw.data(), sizeof(double) * kw.size(), cudaMemcpyHostToDevice));
-  // partial structure factors for up to nb configurations
-  const int nchunk = (c->na + recip_sk_chunk() - 1) / recip_sk_chunk();
-  size_t part = sizeof(double) * 2 * (size_t)nk * nchunk * std::max(c->nb, 1);
-  size_t skb = sizeof(double) * 2 * (size_t)nk * std::max(c->nb, 1);
-  if (c->sk_part) cudaFree(c->sk_part);
-  if (c->sk) cudaFree(c->sk);
-  CK(cudaMalloc(&c->sk_part, part));
-  CK(cudaMalloc(&c->sk, skb));
-  c->sk_part_bytes = part;
-  c->sk_bytes = skb;
-  if (c->nkxy > 1024 || recip_sk_smem(kmax, c->nkxy) > 227 * 1024 || recip_force_smem(kmax) > 227 * 1024)
+  if (kmax < 0 || kmax > 4000) return ctx_set_error(GB_E_ARG, "kmax out of range");
+  if (recip_sk_smem(kmax) > 227 * 1024 || recip_force_smem(kmax) > 227 * 1024)
     return ctx_set_error(GB_E_UNSUPPORTED, "kmax too large for the reciprocal-space kernels");
-  recip_set_attributes(recip_sk_smem(kmax, c->nkxy), recip_force_smem(kmax));
+  const int cap_col = gb_kcap_col(kmax), cap_kp = gb_kcap_kp(kmax);
+  std::vector<KCol> col(cap_col);
+  std::vector<int4> kp(cap_kp), grp(cap_kp);
+  std::vector<double> kw(cap_kp);
+  KTables t;
+  if (gb_build_ktables(c->P, recip_group_len(), col.data(), cap_col, kp.data(), kw.data(), cap_kp, grp.data(),
+                       cap_kp, &t))
+    return ctx_set_error(GB_E_ARG, "k-vector table capacity exceeded");
+  for (void *p : {(void *)c->kcol, (void *)c->kgrp, (void *)c->kpair, (void *)c->kw, (void *)c->ktab,
+                  (void *)c->sk_part, (void *)c->sk})
+    if (p) cudaFree(p);
+  c->kcol = nullptr;
+  c->kgrp = c->kpair = nullptr;
+  c->kw = c->sk_part = c->sk = nullptr;
+  c->ktab = nullptr;
+  c->ncol = t.ncol;
+  c->nkp = t.nkp;
+  c->ngrp = t.ngrp;
+  c->nk = t.nk;
+  const int nc = std::max(c->nb, 1);
+  const int nchunk = (c->na + recip_sk_chunk() - 1) / recip_sk_chunk();
+  c->ktab_bytes = sizeof(double2) * 3 * (size_t)(kmax + 1) * c->na * nc;
+  c->sk_part_bytes = sizeof(double) * 4 * (size_t)std::max(t.nkp, 1) * nchunk * nc;
+  c->sk_bytes = sizeof(double) * 8 * (size_t)std::max(t.nkp, 1) * nc;
+  CK(cudaMalloc(&c->kcol, sizeof(KCol) * std::max(t.ncol, 1)));
+  CK(cudaMalloc(&c->kgrp, sizeof(int4) * std::max(t.ngrp, 1)));
+  CK(cudaMalloc(&c->kpair, sizeof(int4) * std::max(t.nkp, 1)));
+  CK(cudaMalloc(&c->kw, sizeof(double) * std::max(t.nkp, 1)));
+  CK(cudaMalloc(&c->ktab, c->ktab_bytes));
+  CK(cudaMalloc(&c->sk_part, c->sk_part_bytes));
+  CK(cudaMalloc(&c->sk, c->sk_bytes));
+  CK(cudaMemcpy(c->kcol, col.data(), sizeof(KCol) * t.ncol, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->kgrp, grp.data(), sizeof(int4) * t.ngrp, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->kpair, kp.data(), sizeof(int4) * t.nkp, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->kw, kw.data(), sizeof(double) * t.nkp, cudaMemcpyHostToDevice));
+  recip_set_attributes();
   c->kmax_alloc = kmax;
+  c->k_rkmax = c->P.rkmax;
+  c->k_walpha = c->P.walpha;
   return GB_OK;
 }
 
@@ -236,14 +199,14 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   prof_end(c, PR_RECIP_SK, ksites);
   prof_begin(c, PR_RECIP_W);
   launch_recip_weights(c->stream, c, B, slot(c, s));
-  prof_end(c, PR_RECIP_W, (double)c->nk * B);
+  prof_end(c, PR_RECIP_W, (double)c->nkp * B);
   prof_begin(c, PR_RECIP_F);
   launch_recip_force(c->stream, c, c->rs, c->z, B, c->g);
   prof_end(c, PR_RECIP_F, ksites);
   prof_begin(c, PR_MSITE);
   launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, onboxl * onboxl, sign, accumulate);
   prof_end(c, PR_MSITE, (double)na * B);
-  c->launches += 8;
+  c->launches += 9;
   return GB_OK;
 }
 
@@ -427,7 +390,7 @@ int dev_prepare(gb_context *c, double dt, double beta) {
     if ((st = upload_tw(c, &c->tw_c2, c->P.nbdf2))) return st;
     c->tw_c2_n = c->P.nbdf2;
   }
-  if (c->kmax_alloc != c->P.kmax) {
+  if (c->kmax_alloc != c->P.kmax || c->k_rkmax != c->P.rkmax || c->k_walpha != c->P.walpha) {
     if ((st = build_kvectors(c))) return st;
   }
   if (dt > 0.0 && (dt != c->monod_dt || beta != c->monod_beta)) {
