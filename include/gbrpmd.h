@@ -239,6 +239,16 @@ int gbrpmd_ctx_set_profiling(gb_context *ctx, int on);
    3 structure factors, 4 k-space weights, 5 k-space forces, 6 Lennard-Jones,
    7 TEM correction, 8 contraction and kicks, 9 M-site, 10 RATTLE */
 int gbrpmd_ctx_region_times(gb_context *ctx, double *ms, double *units, int *counts, int nregion);
+/* Pair-list skin (no counterpart in the reference, which rebuilds its cell
+   lists at every call): each list of the context (real-space Ewald, LJ, TEM)
+   keeps a superset at cut-off * (1 + fraction), rebuilt on the device only
+   when a point has moved by more than half the skin since its last rebuild, and
+   filters it into the exact pair set at every use, so results do not depend on
+   the fraction.  Default 0.1 (environment GBRPMD_LIST_SKIN); 0 rebuilds every
+   list at every use. */
+int gbrpmd_ctx_set_list_skin(gb_context *ctx, double fraction);
+/* rebuilds of the three skin lists since the context was created (synchronises) */
+int gbrpmd_ctx_list_rebuilds(gb_context *ctx, unsigned *counts3);
 /* the md_eq step loop (md_eq.f90:182-323) on the device state: nsteps
    evolve_pi steps, each followed by the Andersen test ran2(irun) < thresh
    that resamples all momenta (md_eq.f90:311-315) when therm is AND.

@@ -1,5 +1,6 @@
 // api.cpp -- C ABI of the library (include/gbrpmd.h): parameter store,
 // device contexts, drop-in entry points and the serial random stream.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -128,6 +129,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
   c->nm = na / 3;
   const char *gen = std::getenv("GBRPMD_GENERIC_MTS");
   c->generic_mts = gen && gen[0] == '1';
+  if (const char *sk = std::getenv("GBRPMD_LIST_SKIN")) c->list_skin = std::max(0.0, std::atof(sk));
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   const size_t N = 3 * (size_t)na * nb, S = 3 * (size_t)na;
   if ((st = dalloc(c, &c->p, N)) || (st = dalloc(c, &c->r, N)) || (st = dalloc(c, &c->dvdr, N)) ||
@@ -161,6 +163,9 @@ void ctx_free(gb_context *c) {
                   (void *)c->kpair, (void *)c->kw, (void *)c->ktab, (void *)c->sk_part, (void *)c->sk,
                   (void *)c->tw_nb, (void *)c->tw_c1, (void *)c->tw_c2})
     if (p) cudaFree(p);
+  for (SkinList &L : c->sl)
+    for (void *p : {(void *)L.pl.idx, (void *)L.pl.count, (void *)L.ref, (void *)L.flag, (void *)L.rebuilds})
+      if (p) cudaFree(p);
   if (c->h_acc) cudaFreeHost(c->h_acc);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -365,6 +370,24 @@ int gbrpmd_ctx_set_profiling(gb_context *c, int on) {
   c->prof = on;
   c->marks.clear();
   c->ev_next = 0;
+  return GB_OK;
+}
+
+int gbrpmd_ctx_set_list_skin(gb_context *c, double fraction) {
+  if (!c) return ctx_set_error(GB_E_ARG, "null context");
+  if (!(fraction >= 0.0) || fraction > 1.0) return ctx_set_error(GB_E_ARG, "list skin fraction must be in [0, 1]");
+  c->list_skin = fraction;
+  for (SkinList &L : c->sl) L.valid = false;
+  return GB_OK;
+}
+
+int gbrpmd_ctx_list_rebuilds(gb_context *c, unsigned *counts3) {
+  if (!c || !counts3) return ctx_set_error(GB_E_ARG, "null argument");
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < LIST_N; ++i) {
+    counts3[i] = 0;
+    if (c->sl[i].rebuilds) CK(cudaMemcpy(&counts3[i], c->sl[i].rebuilds, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  }
   return GB_OK;
 }
 

@@ -22,6 +22,23 @@ struct PairList {
 
 // Which accumulator slots the last evaluation filled and with how many
 // configurations, so that the bead-averaged energies can be formed.
+// A pair list kept at cut-off + skin and rebuilt only when some point has moved
+// more than skin/2 since its last rebuild (the decision is taken on the device);
+// every use filters it into the exact list of pairs within the cut-off.
+struct SkinList {
+  PairList pl;                   // superset: pairs within cut-off + skin at the last rebuild
+  size_t idx_bytes = 0, cnt_bytes = 0;
+  double *ref = nullptr;         // [nconf][npt][3] positions at the last rebuild
+  size_t ref_bytes = 0;
+  unsigned *flag = nullptr;      // device word: nonzero = rebuild at this use
+  unsigned *rebuilds = nullptr;  // device counter of rebuilds
+  bool valid = false;            // storage and key match the last use
+  int nconf = 0, npt = 0, unit = 0, excl = 0;
+  long long pstride = 0, cstride = 0;
+  double cutsq = 0.0, skin = 0.0, box[3] = {0, 0, 0};
+};
+enum { LIST_EW = 0, LIST_LJ = 1, LIST_TEM = 2, LIST_N = 3 };
+
 struct EnergyPlan {
   int B_ew = 0, B_tem = 0, B_lj = 0, B_ew2 = 0, B_tem2 = 0, B_lj2 = 0, B_int = 0;
   int evolve = 0, mts = 1;
@@ -53,8 +70,10 @@ struct gb_context {
   double *rs = nullptr;    // site positions scratch [nb][na][3]
   float4 *rs32 = nullptr;  // FP32 fractional coordinates for list prefilters [nb][na]
   double *rc = nullptr;    // centroid scratch [na][3]
-  PairList pl;             // shared pair-list storage (re-sized on demand)
+  PairList pl;             // exact pair list of the current term (re-sized on demand)
   size_t pl_idx_bytes = 0, pl_cnt_bytes = 0;
+  SkinList sl[LIST_N];     // per-term skin lists (Ewald real space, LJ, TEM)
+  double list_skin = 0.1;  // skin as a fraction of the cut-off; 0: full rebuild at every use
 
   // reciprocal space
   int kmax_alloc = -1;           // k tables built for these kmax, rkmax, walpha

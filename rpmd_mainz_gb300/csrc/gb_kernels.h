@@ -31,8 +31,18 @@ struct PairGeom {
 
 // ---- pair lists (k_pairs.cu) ----
 void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac);
+// every pair within g.rcutsq; with a gate word, only when *gate != 0 (counts
+// are then zeroed on the device, so the decision needs no host round trip)
 void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
-                       PairList &pl, unsigned *status);
+                       PairList &pl, unsigned *status, const unsigned *gate = nullptr);
+// skin lists: displacement test against the rebuild positions, position save
+// on a rebuild, and the filter from the superset to the exact list
+void launch_skin_check(cudaStream_t s, const PairGeom &g, int nconf, const double *ref, double lim2,
+                       unsigned *flag);
+void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref, const unsigned *flag,
+                      unsigned *rebuilds);
+void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
+                        const PairList &skin, PairList &pl, unsigned *status);
 double list_total(cudaStream_t s, const PairList &pl);  // profiling only (synchronises)
 
 // ---- Ewald, unit box (k_pairs.cu, k_recip.cu) ----

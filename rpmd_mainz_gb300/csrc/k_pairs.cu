@@ -59,8 +59,9 @@ constexpr int LB_JCHUNK = 1024;
 
 __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *frac, int *count,
                                                       int *idx, int cap, float3 len, float thr_lo,
-                                                      float thr_hi, unsigned *status) {
+                                                      float thr_hi, unsigned *status, const unsigned *gate) {
   __shared__ float4 tile[LB_T];
+  if (gate && *gate == 0u) return;  // skin list still valid: nothing to rebuild
   const int c = blockIdx.z;
   const int i = blockIdx.x * LB_T + threadIdx.x;
   const int npt = g.npt;
@@ -109,6 +110,86 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
     __syncthreads();
   }
   if (over) atomicOr(status, ST_LIST_OVERFLOW);
+}
+
+// ---- skin lists ----
+// flag |= 1 when a point of any configuration has moved by more than sqrt(lim2)
+// since ref was taken (ref: [nconf][npt][3])
+__global__ void k_skin_check(PairGeom g, int nconf, const double *ref, double lim2, unsigned *flag) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool moved = false;
+  if (t < (long long)nconf * g.npt) {
+    const int c = (int)(t / g.npt), i = (int)(t % g.npt);
+    const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
+    const double *r0 = ref + 3 * t;
+    const double dx = x[0] - r0[0], dy = x[1] - r0[1], dz = x[2] - r0[2];
+    moved = !(dx * dx + dy * dy + dz * dz <= lim2);  // NaN counts as moved
+  }
+  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+// on a rebuild: zero the superset list's counts
+__global__ void k_skin_zero(int *count, long long n, const unsigned *flag) {
+  if (*flag == 0u) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) count[t] = 0;
+}
+
+// on a rebuild: remember the positions it was made from
+__global__ void k_skin_save(PairGeom g, int nconf, double *ref, const unsigned *flag, unsigned *rebuilds) {
+  if (*flag == 0u) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) atomicAdd(rebuilds, 1u);
+  if (t >= (long long)nconf * g.npt) return;
+  const int c = (int)(t / g.npt), i = (int)(t % g.npt);
+  const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
+  ref[3 * t] = x[0];
+  ref[3 * t + 1] = x[1];
+  ref[3 * t + 2] = x[2];
+}
+
+// exact list from the superset: one warp per (configuration, point); the same
+// FP32 prefilter and reference-rounded FP64 band test as the full build, lanes
+// append in list order through a ballot
+__global__ void __launch_bounds__(128) k_list_filter(PairGeom g, int nconf, const float4 *frac,
+                                                     const int *scount, const int *sidx, int scap,
+                                                     int *count, int *idx, int cap, float3 len,
+                                                     float thr_lo, float thr_hi, unsigned *status) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= (long long)nconf * g.npt) return;
+  const int c = (int)(w / g.npt), i = (int)(w % g.npt);
+  const float4 *fr = frac + (long long)c * g.npt;
+  const double *base = g.pos + c * g.cstride;
+  const float4 fi = fr[i];
+  const double *pi = base + (long long)i * g.pstride;
+  const int n = min(scount[w], scap);
+  const int *L = sidx + w * scap;
+  int *out = idx + w * cap;
+  int written = 0;
+  for (int t0 = 0; t0 < n; t0 += 32) {
+    const int t = t0 + lane;
+    int j = 0;
+    bool ok = false;
+    if (t < n) {
+      j = L[t];
+      const float4 fj = fr[j];
+      float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
+      dx = (dx - rintf(dx)) * len.x;
+      dy = (dy - rintf(dy)) * len.y;
+      dz = (dz - rintf(dz)) * len.z;
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 < thr_hi) ok = d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    const int pos = written + __popc(m & ((1u << lane) - 1u));
+    if (ok && pos < cap) out[pos] = j;
+    written += __popc(m);
+  }
+  if (lane == 0) {
+    count[w] = min(written, cap);
+    if (written > cap) atomicOr(status, ST_LIST_OVERFLOW);
+  }
 }
 
 // ---- M-site substitution and scaling (md_forces.f90:179-188, ewald_cubic.f90:20-22) ----
@@ -383,24 +464,56 @@ void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac) {
   k_frac32<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac);
 }
 
-void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
-                       PairList &pl, unsigned *status) {
-  float3 len;
+// FP32 thresholds around rcutsq: below lo accept, at or above hi reject,
+// between: exact FP64 test
+void list_thresholds(const PairGeom &g, float3 *len, float *lo, float *hi) {
   double lmax;
   if (g.unit) {
-    len = make_float3(1.f, 1.f, 1.f);
+    *len = make_float3(1.f, 1.f, 1.f);
     lmax = 1.0;
   } else {
-    len = make_float3((float)g.box[0], (float)g.box[1], (float)g.box[2]);
+    *len = make_float3((float)g.box[0], (float)g.box[1], (float)g.box[2]);
     lmax = fmax(g.box[0], fmax(g.box[1], g.box[2]));
   }
   // FP32 error of d^2 is below 1e-6 * lmax^2 for wrapped fractional coordinates;
   // pairs within 4e-6 * lmax^2 of the cut-off go to the exact FP64 test
   const double band = 4e-6 * lmax * lmax;
-  const float thr_lo = (float)(g.rcutsq - band), thr_hi = (float)(g.rcutsq + band);
-  cudaMemsetAsync(pl.count, 0, sizeof(int) * (size_t)nconf * g.npt, s);
+  *lo = (float)(g.rcutsq - band);
+  *hi = (float)(g.rcutsq + band);
+}
+
+void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
+                       PairList &pl, unsigned *status, const unsigned *gate) {
+  float3 len;
+  float thr_lo, thr_hi;
+  list_thresholds(g, &len, &thr_lo, &thr_hi);
+  const long long ncount = (long long)nconf * g.npt;
+  if (gate) k_skin_zero<<<nblk(ncount, 256), 256, 0, s>>>(pl.count, ncount, gate);
+  else cudaMemsetAsync(pl.count, 0, sizeof(int) * (size_t)ncount, s);
   dim3 grid(nblk(g.npt, LB_T), nblk(g.npt, LB_JCHUNK), nconf);
-  k_build_list2<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status);
+  k_build_list2<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status, gate);
+}
+
+void launch_skin_check(cudaStream_t s, const PairGeom &g, int nconf, const double *ref, double lim2,
+                       unsigned *flag) {
+  const long long n = (long long)nconf * g.npt;
+  k_skin_check<<<nblk(n, 256), 256, 0, s>>>(g, nconf, ref, lim2, flag);
+}
+
+void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref, const unsigned *flag,
+                      unsigned *rebuilds) {
+  const long long n = (long long)nconf * g.npt;
+  k_skin_save<<<nblk(n, 256), 256, 0, s>>>(g, nconf, ref, flag, rebuilds);
+}
+
+void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
+                        const PairList &skin, PairList &pl, unsigned *status) {
+  float3 len;
+  float thr_lo, thr_hi;
+  list_thresholds(g, &len, &thr_lo, &thr_hi);
+  const long long nw = (long long)nconf * g.npt;
+  k_list_filter<<<nblk(nw * 32, 128), 128, 0, s>>>(g, nconf, frac, skin.count, skin.idx, skin.cap, pl.count,
+                                                   pl.idx, pl.cap, len, thr_lo, thr_hi, status);
 }
 
 void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, double alpha,

@@ -159,6 +159,88 @@ int list_cap(int npt, double rc, double vol) {
   return std::min(cap, std::max(npt, 1));
 }
 
+// c->pl = every pair within g.rcutsq (rounded as the reference rounds it) for
+// nconf configurations of g, through skin list `which`: its superset at
+// cut-off + skin is rebuilt on the device only when a point has moved by more
+// than skin/2 since the last rebuild, then filtered into the exact list.
+// Returns the number of launches through *nl.
+int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut, double vol, int *nl) {
+  int st = ensure_list(c, nconf, g.npt, list_cap(g.npt, cut, vol));
+  if (st) return st;
+  launch_frac32(c->stream, g, nconf, c->rs32);
+  if (c->list_skin <= 0.0) {
+    launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
+    *nl = 2;
+    return GB_OK;
+  }
+  SkinList &S = c->sl[which];
+  const double skin = c->list_skin * cut, scut = cut + skin;
+  bool same = S.valid && S.nconf == nconf && S.npt == g.npt && S.unit == g.unit && S.excl == g.excl_mol &&
+              S.pstride == g.pstride && S.cstride == g.cstride && S.cutsq == g.rcutsq && S.skin == skin;
+  for (int d = 0; d < 3; ++d) same = same && S.box[d] == g.box[d];
+  if (!same) {
+    S.valid = false;
+    const int cap = list_cap(g.npt, scut, vol);
+    const size_t need_idx = sizeof(int) * (size_t)nconf * g.npt * cap;
+    const size_t need_cnt = sizeof(int) * (size_t)nconf * g.npt;
+    const size_t need_ref = sizeof(double) * 3 * (size_t)nconf * g.npt;
+    if (need_idx > S.idx_bytes) {
+      if (S.pl.idx) cudaFree(S.pl.idx);
+      S.pl.idx = nullptr;
+      S.idx_bytes = 0;
+      CK(cudaMalloc(&S.pl.idx, need_idx));
+      S.idx_bytes = need_idx;
+    }
+    if (need_cnt > S.cnt_bytes) {
+      if (S.pl.count) cudaFree(S.pl.count);
+      S.pl.count = nullptr;
+      S.cnt_bytes = 0;
+      CK(cudaMalloc(&S.pl.count, need_cnt));
+      S.cnt_bytes = need_cnt;
+    }
+    if (need_ref > S.ref_bytes) {
+      if (S.ref) cudaFree(S.ref);
+      S.ref = nullptr;
+      S.ref_bytes = 0;
+      CK(cudaMalloc(&S.ref, need_ref));
+      S.ref_bytes = need_ref;
+    }
+    if (!S.flag) CK(cudaMalloc(&S.flag, sizeof(unsigned)));
+    if (!S.rebuilds) {
+      CK(cudaMalloc(&S.rebuilds, sizeof(unsigned)));
+      CK(cudaMemsetAsync(S.rebuilds, 0, sizeof(unsigned), c->stream));
+    }
+    S.pl.nconf = nconf;
+    S.pl.npt = g.npt;
+    S.pl.cap = cap;
+  }
+  CK(cudaMemsetAsync(S.flag, same ? 0 : 1, sizeof(unsigned), c->stream));
+  int n = 1;
+  if (same) {  // rebuild when a point moved by more than skin/2 (a hair less, for rounding)
+    const double lim = 0.5 * skin * (1.0 - 1e-9);
+    launch_skin_check(c->stream, g, nconf, S.ref, lim * lim, S.flag);
+    n += 1;
+  }
+  PairGeom gs = g;
+  gs.rcutsq = scut * scut;
+  launch_build_list(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag);
+  launch_skin_save(c->stream, g, nconf, S.ref, S.flag, S.rebuilds);
+  launch_list_filter(c->stream, g, nconf, c->rs32, S.pl, c->pl, c->status);
+  n += 4;
+  S.valid = true;
+  S.nconf = nconf;
+  S.npt = g.npt;
+  S.unit = g.unit;
+  S.excl = g.excl_mol;
+  S.pstride = g.pstride;
+  S.cstride = g.cstride;
+  S.cutsq = g.rcutsq;
+  S.skin = skin;
+  for (int d = 0; d < 3; ++d) S.box[d] = g.box[d];
+  *nl = n;
+  return GB_OK;
+}
+
 double boxmin(const gb_context *c) { return std::min(c->box[0], std::min(c->box[1], c->box[2])); }
 double boxmax(const gb_context *c) { return std::max(c->box[0], std::max(c->box[1], c->box[2])); }
 
@@ -183,12 +265,12 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   g.onbox[0] = g.onbox[1] = g.onbox[2] = 1.0;
   g.rcutsq = c->P.wrcut * c->P.wrcut;
   g.excl_mol = 0;
-  int st = ensure_list(c, B, na, list_cap(na, c->P.wrcut, 1.0));
-  if (st) return st;
+  int nl = 0;
   prof_begin(c, PR_LIST);
-  launch_frac32(c->stream, g, B, c->rs32);
-  launch_build_list(c->stream, g, B, c->rs32, c->pl, c->status);
+  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, 1.0, &nl);
+  if (st) return st;
   prof_end(c, PR_LIST, (double)na * B);
+  c->launches += nl;
   const double npairs = c->prof ? list_total(c->stream, c->pl) : 0.0;
   prof_begin(c, PR_EW_REAL);
   launch_ewald_real(c->stream, c->rs, c->z, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
@@ -206,7 +288,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   prof_begin(c, PR_MSITE);
   launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, onboxl * onboxl, sign, accumulate);
   prof_end(c, PR_MSITE, (double)na * B);
-  c->launches += 9;
+  c->launches += 7;
   return GB_OK;
 }
 
@@ -225,6 +307,7 @@ int term_lj(gb_context *c, const double *r, int B, double *out, int accumulate, 
   g.excl_mol = 0;
   const double vol = c->box[0] * c->box[1] * c->box[2];
   int nconf;
+  double lcut;
   if (B > 3) {  // centroid neighbour list (md_forces.f90:34-53)
     launch_centroid(c->stream, r, c->rc, na, B);
     const double cut = std::min(c->P.rcut, 0.5 * boxmin(c));
@@ -232,27 +315,27 @@ int term_lj(gb_context *c, const double *r, int B, double *out, int accumulate, 
     g.cstride = 0;
     g.rcutsq = cut * cut;
     nconf = 1;
-    int st = ensure_list(c, 1, nm, list_cap(nm, cut, vol));
-    if (st) return st;
+    lcut = cut;
     c->launches += 1;
   } else {  // lj_basic / lj_cell: every pair within rcut, bead by bead
     g.pos = r;
     g.cstride = 3LL * na;
     g.rcutsq = c->P.rcut * c->P.rcut;
     nconf = B;
-    int st = ensure_list(c, B, nm, list_cap(nm, c->P.rcut, vol));
-    if (st) return st;
+    lcut = c->P.rcut;
   }
+  int nl = 0;
   prof_begin(c, PR_LIST);
-  launch_frac32(c->stream, g, nconf, c->rs32);
-  launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
+  int st = make_list(c, LIST_LJ, g, nconf, lcut, vol, &nl);
+  if (st) return st;
   prof_end(c, PR_LIST, (double)nm * nconf);
+  c->launches += nl;
   const double npairs = c->prof ? list_total(c->stream, c->pl) * (nconf == 1 ? B : 1) : 0.0;
   prof_begin(c, PR_LJ);
   launch_lj(c->stream, r, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut, c->box,
             48.0 * c->P.oo_eps, out, slot(c, s));
   prof_end(c, PR_LJ, npairs);
-  c->launches += 3;
+  c->launches += 1;
   return GB_OK;
 }
 
@@ -273,6 +356,7 @@ int term_tem(gb_context *c, const double *r, int B, double *out, double sign, in
   g.excl_mol = 1;
   launch_msite(c->stream, r, c->rs, na, B, alpha, 1.0);
   int nconf;
+  double lcut;
   if (B > 1) {  // centroid list, cut sig + 5 bohr (md_forces.f90:69-89) -> ewc_list_tem
     if (sig > 0.5 * boxmax(c)) return ctx_set_error(GB_E_CUTOFF, "ewc_list : rcut too large");
     double cut = sig + 5.0;
@@ -282,8 +366,7 @@ int term_tem(gb_context *c, const double *r, int B, double *out, double sign, in
     g.cstride = 0;
     g.rcutsq = cut * cut;
     nconf = 1;
-    int st = ensure_list(c, 1, na, list_cap(na, cut, vol));
-    if (st) return st;
+    lcut = cut;
     c->launches += 1;
   } else {  // ewc_basic_tem / ewc_cell_tem on the M-site positions
     if (3.0 * sig > boxmax(c)) {
@@ -295,19 +378,20 @@ int term_tem(gb_context *c, const double *r, int B, double *out, double sign, in
     g.cstride = 3LL * na;
     g.rcutsq = sig * sig;
     nconf = B;
-    int st = ensure_list(c, B, na, list_cap(na, sig, vol));
-    if (st) return st;
+    lcut = sig;
   }
   CK(cudaMemsetAsync(c->g, 0, sizeof(double) * 3 * (size_t)na * B, c->stream));
+  int nl = 0;
   prof_begin(c, PR_LIST);
-  launch_frac32(c->stream, g, nconf, c->rs32);
-  launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
+  int st = make_list(c, LIST_TEM, g, nconf, lcut, vol, &nl);
+  if (st) return st;
   prof_end(c, PR_LIST, (double)na * nconf);
+  c->launches += nl;
   prof_begin(c, PR_TEM);
   launch_tem(c->stream, c->rs, c->z, na, B, c->pl, sig, c->box, c->g, slot(c, s));
   prof_end(c, PR_TEM, 0.0);
   launch_msite_chain(c->stream, c->g, out, na, B, alpha, 1.0, sign, accumulate);
-  c->launches += 5;
+  c->launches += 3;
   return GB_OK;
 }
 
@@ -529,6 +613,7 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
   unsigned stw = *c->h_status;
   if (stw) {
     CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+    for (SkinList &L : c->sl) L.valid = false;  // a list may have overflowed: rebuild at next use
     if (stw & ST_LIST_OVERFLOW) return ctx_set_error(GB_E_LIST, "neighbour list too small");
     if (stw & ST_RATTLE1) return ctx_set_error(GB_E_RATTLE1, "max iterations exceeded in rattle stage 1");
     if (stw & ST_RATTLE2) return ctx_set_error(GB_E_RATTLE2, "max iterations exceeded in rattle stage 2");

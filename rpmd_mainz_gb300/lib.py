@@ -67,6 +67,8 @@ def load(path=None):
     lib.gbrpmd_ctx_full_forces.argtypes = [C.c_void_p, D, D, D, D, D]
     lib.gbrpmd_ctx_evolve.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
     lib.gbrpmd_ctx_energies.argtypes = [C.c_void_p, D, D, D]
+    lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
+    lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
     _lib = lib
     return lib
 
@@ -242,6 +244,16 @@ class Context:
     @property
     def launches(self):
         return load().gbrpmd_ctx_launch_count(self.h)
+
+    def set_list_skin(self, fraction):
+        """Pair-list skin as a fraction of each cut-off (0: rebuild at every use)."""
+        _check(load().gbrpmd_ctx_set_list_skin(self.h, C.c_double(fraction)))
+
+    def list_rebuilds(self):
+        """Rebuilds of the (Ewald, LJ, TEM) skin lists since creation."""
+        out = (C.c_uint * 3)()
+        _check(load().gbrpmd_ctx_list_rebuilds(self.h, out))
+        return tuple(out)
 
 
 def ran2(idum: C.c_int, rmin=0.0, rmax=1.0):

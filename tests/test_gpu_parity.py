@@ -198,6 +198,62 @@ def test_resident_context_matches_dropin():
     ctx.close()
 
 
+SKIN_CASES = [
+    dict(param="param_qspcfw", ncell=(5, 5, 5), nb=8, mts=2, nbdf1=1, nbdf2=5),  # centroid LJ list
+    dict(param="param_scott", ncell=(4, 4, 4), nb=2, mts=5, nbdf1=1, nbdf2=1, sig_A=4.5),  # TEM, per-bead LJ
+]
+
+
+@pytest.mark.parametrize("case", SKIN_CASES)
+def test_skin_lists_match_oracle(case):
+    """Twelve steps with reused skin lists equal the oracle, which builds every
+    list from scratch; the Ewald list must have been reused at least once."""
+    s = setup(**case)
+    r = systems.perturbed(s, seed=70)
+    ff = orc.full_forces(r, s["box"], s["z"])
+    rng = np.random.default_rng(71)
+    p = rng.normal(size=r.shape) * np.sqrt(s["mass"][None, :, None] / (s["beta"] / s["nb"]))
+    nsteps = 12
+    ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+    ctx.set_list_skin(0.1)
+    ctx.upload(r=r, p=p, dvdr=ff["dvdr"], dvdr2=ff["dvdr2"], box=s["box"])
+    ctx.evolve(nsteps, s["dt"], s["beta"])
+    ctx.sync()
+    rr, pp, f1, f2 = ctx.download()
+    rebuilds = ctx.list_rebuilds()
+    ctx.close()
+    ref = orc.State(r, p, ff["dvdr"], ff["dvdr2"], s["box"])
+    g = orc.Rng(1)
+    for _ in range(nsteps):
+        orc.evolve_pi(ref, s["dt"], s["mass"], s["z"], s["beta"], g)
+    assert rel(rr, ref.r) < TOL and rel(pp, ref.p) < TOL
+    assert rel(f1, ref.dvdr) < TOL and rel(f2, ref.dvdr2) < TOL
+    assert 1 <= rebuilds[0] < nsteps, rebuilds
+
+
+@pytest.mark.parametrize("case", SKIN_CASES)
+def test_skin_fraction_does_not_change_results(case):
+    """No skin (full rebuild at every use), a thin skin (frequent rebuilds) and
+    a thick one give the same trajectory up to summation order."""
+    s = setup(**case)
+    r = systems.perturbed(s, seed=72)
+    ff = orc.full_forces(r, s["box"], s["z"])
+    rng = np.random.default_rng(73)
+    p = rng.normal(size=r.shape) * np.sqrt(s["mass"][None, :, None] / (s["beta"] / s["nb"]))
+    out = []
+    for frac in (0.0, 0.003, 0.3):
+        ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+        ctx.set_list_skin(frac)
+        ctx.upload(r=r, p=p, dvdr=ff["dvdr"], dvdr2=ff["dvdr2"], box=s["box"])
+        ctx.evolve(8, s["dt"], s["beta"])
+        ctx.sync()
+        out.append(ctx.download())
+        ctx.close()
+    for other in out[1:]:
+        for a, b in zip(other, out[0]):
+            assert rel(a, b) < 1e-12
+
+
 def rigid_system(nb=4):
     s = setup(param="param_tip05_rigid", ncell=(4, 4, 4), nb=nb)
     lib.rattle_setup(s["nm"])
