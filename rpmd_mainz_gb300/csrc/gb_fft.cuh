@@ -33,9 +33,9 @@ GB_D void gb_cfft_stage(double (&zr)[H], double (&zi)[H], const double *__restri
     constexpr int half = LEN / 2;
 #pragma unroll
     for (int k = 0; k < half; ++k) {
+      const int m = k * (N / LEN);
       double wr = 1.0, wi = 0.0;
-      if (k > 0) {
-        const int m = k * (N / LEN);
+      if (k > 0 && 4 * m != N) {
         wr = tw[m];
         wi = INV ? tw[N + m] : -tw[N + m];
       }
@@ -46,6 +46,9 @@ GB_D void gb_cfft_stage(double (&zr)[H], double (&zi)[H], const double *__restri
         if (k == 0) {
           tr = zr[b];
           ti = zi[b];
+        } else if (4 * m == N) {  // w = -i (forward) or +i (inverse): no multiplication
+          tr = INV ? -zi[b] : zi[b];
+          ti = INV ? zr[b] : -zr[b];
         } else {
           tr = zr[b] * wr - zi[b] * wi;
           ti = zr[b] * wi + zi[b] * wr;
@@ -171,16 +174,23 @@ GB_D void gb_hc2r_direct(const double *in, double *x, int n, const double *__res
   }
 }
 
-// Accessor forms of the power-of-two transforms: `in(j)` yields input element
-// j, `out(k, v)` receives output element k.  All input elements are read before
-// the first output element is written, so input and output may be the same
-// storage (in-place in registers) and either may live in shared or global
-// memory; with constant indices after unrolling, register arrays stay in
-// registers.
+// Scaled accessor forms of the power-of-two transforms, as the propagator uses
+// them: `in(j)` yields input element j, `out(k, v)` receives output element k
+// already multiplied by the scale sc.  All inputs are read before the first
+// output is written, so input and output may share storage; with constant
+// indices after unrolling, register arrays stay in registers.
+//
+// The half-complex split treats k and H - k together (their twiddles are
+// (c, s) and (-c, s)), which halves its arithmetic; the scale is folded into
+// pre-scaled twiddle tables:
+//   twf[m] = (sc / 2) cos(2 pi m / n), twf[n + m] = (sc / 2) sin(...)  (forward)
+//   twi[m] = sc cos(2 pi m / n),       twi[n + m] = sc sin(...)        (inverse)
+// tw is the unscaled table of the complex FFT.
 template <int N, class In, class Out>
-GB_D void gb_r2hc_io(In in, Out out, const double *__restrict__ tw) {
+GB_D void gb_r2hc_s(In in, Out out, const double *__restrict__ tw, const double *__restrict__ twf) {
+  const double sc = twf[0] + twf[0];
   if constexpr (N == 1) {
-    out(0, in(0));
+    out(0, sc * in(0));
   } else {
     constexpr int H = N / 2;
     double zr[H], zi[H];
@@ -190,48 +200,65 @@ GB_D void gb_r2hc_io(In in, Out out, const double *__restrict__ tw) {
       zi[j] = in(2 * j + 1);
     }
     if constexpr (H > 1) gb_cfft<H, N, false>(zr, zi, tw);
-    out(0, zr[0] + zi[0]);
-    out(H, zr[0] - zi[0]);
+    out(0, sc * (zr[0] + zi[0]));
+    out(H, sc * (zr[0] - zi[0]));
 #pragma unroll
-    for (int k = 1; k < H; ++k) {
+    for (int k = 1; 2 * k < H; ++k) {
       const int b = H - k;
-      const double er = 0.5 * (zr[k] + zr[b]), ei = 0.5 * (zi[k] - zi[b]);
-      const double orr = 0.5 * (zi[k] + zi[b]), oi = -0.5 * (zr[k] - zr[b]);
-      const double c = tw[k], s = tw[N + k];
-      out(k, er + c * orr + s * oi);
-      out(N - k, ei + c * oi - s * orr);
+      const double P = zr[k] + zr[b], Q = zi[k] + zi[b];
+      const double R = zr[k] - zr[b], D = zi[k] - zi[b];
+      const double hc = twf[k], hs = twf[N + k];
+      const double hP = twf[0] * P, hD = twf[0] * D;
+      const double T1 = hc * Q - hs * R, T2 = hc * R + hs * Q;
+      out(k, hP + T1);
+      out(b, hP - T1);
+      out(N - k, hD - T2);
+      out(N - b, -hD - T2);
+    }
+    if constexpr (H % 2 == 0) {  // k = H/2 = n/4: cos = 0, sin = 1
+      out(H / 2, sc * zr[H / 2]);
+      out(N - H / 2, -sc * zi[H / 2]);
     }
   }
 }
 
 template <int N, class In, class Out>
-GB_D void gb_hc2r_io(In in, Out out, const double *__restrict__ tw) {
+GB_D void gb_hc2r_s(In in, Out out, const double *__restrict__ tw, const double *__restrict__ twi) {
+  const double sc = twi[0];
   if constexpr (N == 1) {
-    out(0, in(0));
+    out(0, sc * in(0));
   } else {
     constexpr int H = N / 2;
     double zr[H], zi[H];
     {
       const double i0 = in(0), ih = in(H);
-      zr[0] = 0.5 * (i0 + ih);
-      zi[0] = 0.5 * (i0 - ih);
+      zr[0] = sc * (i0 + ih);
+      zi[0] = sc * (i0 - ih);
     }
 #pragma unroll
-    for (int k = 1; k < H; ++k) {
-      const double xr = in(k), xi = in(N - k);
-      const double cr = in(H - k), ci = -in(H + k);
-      const double er = 0.5 * (xr + cr), ei = 0.5 * (xi + ci);
+    for (int k = 1; 2 * k < H; ++k) {
+      const int b = H - k;
+      // X_k = in(k) + i in(N-k), conj(X_{H-k}) = in(H-k) - i in(H+k)
+      const double xr = in(k), xi = in(N - k), cr = in(b), ci = -in(H + k);
+      const double A = sc * (xr + cr), B = sc * (xi + ci);
       const double dr = xr - cr, di = xi - ci;
-      const double c = tw[k], s = tw[N + k];
-      const double orr = 0.5 * (c * dr - s * di), oi = 0.5 * (c * di + s * dr);
-      zr[k] = er - oi;
-      zi[k] = ei + orr;
+      const double c = twi[k], s = twi[N + k];
+      const double U = c * di + s * dr, V = c * dr - s * di;
+      zr[k] = A - U;
+      zr[b] = A + U;
+      zi[k] = B + V;
+      zi[b] = V - B;
+    }
+    if constexpr (H % 2 == 0) {  // k = H/2: cos = 0, sin = 1
+      const double xr = in(H / 2), xi = in(N - H / 2);
+      zr[H / 2] = 2.0 * sc * xr;
+      zi[H / 2] = -2.0 * sc * xi;
     }
     if constexpr (H > 1) gb_cfft<H, N, true>(zr, zi, tw);
 #pragma unroll
     for (int j = 0; j < H; ++j) {
-      out(2 * j, 2.0 * zr[j]);
-      out(2 * j + 1, 2.0 * zi[j]);
+      out(2 * j, zr[j]);
+      out(2 * j + 1, zi[j]);
     }
   }
 }

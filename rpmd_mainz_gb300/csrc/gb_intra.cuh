@@ -22,8 +22,9 @@ GB_D double intra_molecule(int model, const double *x, double *f, double *vir, c
   const double dr1sq = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;
   const double dr2sq = dx2 * dx2 + dy2 * dy2 + dz2 * dz2;
   const double dr3sq = dx3 * dx3 + dy3 * dy3 + dz3 * dz3;
-  const double dr1a = sqrt(dr1sq), dr2a = sqrt(dr2sq), dr3a = sqrt(dr3sq);
-  const double i1 = 1.0 / dr1a, i2 = 1.0 / dr2a, i3 = 1.0 / dr3a;
+  // one rsqrt per bond instead of a square root and a division
+  const double i1 = rsqrt(dr1sq), i2 = rsqrt(dr2sq), i3 = rsqrt(dr3sq);
+  const double dr1a = dr1sq * i1, dr2a = dr2sq * i2, dr3a = dr3sq * i3;
   const double dr1 = dr1a - ip.reoh, dr2 = dr2a - ip.reoh;
   double v, dvdr1, dvdr2, dvdr3;
   if (model == 0) {
@@ -91,15 +92,13 @@ GB_D double intra_molecule(int model, const double *x, double *f, double *vir, c
     vir[7] = vir[5] = dy1 * dvdz1 + dy2 * dvdz2 + dy3 * dvdz3;
     vir[8] = dz1 * dvdz1 + dz2 * dvdz2 + dz3 * dvdz3;
   } else {
-    // vir(a,b) = sum over the three bonds of d_a * dvd_b (intra_harmonic.f90:86-94)
+    // vir(a,b) = sum over the three bonds of d_a * dvd_b (intra_harmonic.f90:86-94);
+    // dvd_b is parallel to d, so vir(a,b) = vir(b,a) up to rounding: six sums
     vir[0] = dx1 * dvdx1 + dx2 * dvdx2 + dx3 * dvdx3;
-    vir[1] = dy1 * dvdx1 + dy2 * dvdx2 + dy3 * dvdx3;
-    vir[2] = dz1 * dvdx1 + dz2 * dvdx2 + dz3 * dvdx3;
-    vir[3] = dx1 * dvdy1 + dx2 * dvdy2 + dx3 * dvdy3;
+    vir[3] = vir[1] = dy1 * dvdx1 + dy2 * dvdx2 + dy3 * dvdx3;
+    vir[6] = vir[2] = dz1 * dvdx1 + dz2 * dvdx2 + dz3 * dvdx3;
     vir[4] = dy1 * dvdy1 + dy2 * dvdy2 + dy3 * dvdy3;
-    vir[5] = dz1 * dvdy1 + dz2 * dvdy2 + dz3 * dvdy3;
-    vir[6] = dx1 * dvdz1 + dx2 * dvdz2 + dx3 * dvdz3;
-    vir[7] = dy1 * dvdz1 + dy2 * dvdz2 + dy3 * dvdz3;
+    vir[7] = vir[5] = dz1 * dvdy1 + dz2 * dvdy2 + dz3 * dvdy3;
     vir[8] = dz1 * dvdz1 + dz2 * dvdz2 + dz3 * dvdz3;
   }
   return v;

@@ -17,13 +17,21 @@
 #include "gb_intra.cuh"
 #include "gb_kernels.h"
 
+#include <algorithm>
+
 namespace {
 
+// A block owns mpb molecules (chosen at launch so that the grid is one wave
+// over the SMs, at most MPB_MAX) and runs 9 * mpb threads, one per coordinate
+// row, rounded up to whole warps; the extra lanes of the last warp carry rows
+// of no molecule and store nothing.
+// At most 8 warps (28 molecules, 252 rows) keep two warps per SM sub-partition,
+// which leaves 255 registers per thread for the register-resident rows.
 template <int NB>
 struct MtsCfg {
-  static constexpr int MPB = NB <= 32 ? 32 : 16;  // molecules per block
-  static constexpr int T = 9 * MPB;               // threads: one per coordinate row
-  static constexpr int LD = NB + 1;               // padded bead stride in shared memory
+  static constexpr int MPB_MAX = NB <= 32 ? 28 : 14;
+  static constexpr int T_MAX = (9 * MPB_MAX + 31) / 32 * 32;
+  static constexpr int LD = NB + 1;  // padded bead stride in shared memory
 };
 
 struct MtsArgs {
@@ -32,30 +40,42 @@ struct MtsArgs {
   const double *monod;  // monod(ic, c, k) at ic + 3*(c + 4*k)
   const double *tw;     // twiddles of length nb
   double *acc_int, *acc_ke;
-  int na, nm, mts, model;
+  int na, nm, mts, model, mpb;
   double halfdt, dtsmall, halfdtsmall;
   IntraPar ip;
 };
 
 template <int NB>
-__global__ void __launch_bounds__(MtsCfg<NB>::T, 1) k_mts_fused(MtsArgs a) {
+__global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_fused(MtsArgs a) {
   using C = MtsCfg<NB>;
   extern __shared__ double sm[];
-  double *s_rst = sm;                              // [MPB*9][LD]
-  double *s_f2 = s_rst + C::MPB * 9 * C::LD;       // [MPB*9][LD]
-  double *s_mono = s_f2 + C::MPB * 9 * C::LD;      // [12*NB]
-  double *s_tw = s_mono + 12 * NB;                 // [2*NB]
-  double *s_red = s_tw + 2 * NB;                   // [32 warps][18]
+  const int T = blockDim.x;
+  const int nrow = (T + 8) / 9 * 9;                // rows with shared-memory slots
+  double *s_rst = sm;                              // [nrow][LD]
+  double *s_f2 = s_rst + nrow * C::LD;             // [nrow][LD]
+  double *s_mono = s_f2 + nrow * C::LD;            // [12*NB]
+  double *s_tw = s_mono + 12 * NB;                 // [2*NB] cos, sin
+  double *s_twf = s_tw + 2 * NB;                   // [2*NB] scaled by sqrt(1/nb) / 2 (forward)
+  double *s_twi = s_twf + 2 * NB;                  // [2*NB] scaled by sqrt(1/nb) (inverse)
+  double *s_red = s_twi + 2 * NB;                  // [32 warps][18]
   const int t = threadIdx.x;
-  for (int i = t; i < 12 * NB; i += C::T) s_mono[i] = a.monod[i];
-  for (int i = t; i < 2 * NB; i += C::T) s_tw[i] = a.tw[i];
+  const double sc = sqrt(1.0 / (double)NB);
+  for (int i = t; i < 12 * NB; i += T) s_mono[i] = a.monod[i];
+  for (int i = t; i < 2 * NB; i += T) {
+    const double w = a.tw[i];
+    s_tw[i] = w;
+    s_twf[i] = (0.5 * sc) * w;
+    s_twi[i] = sc * w;
+  }
 
   // Every thread runs the same instruction stream between barriers: rows past
-  // the last molecule work on a copy of the last molecule and store nothing.
-  const int m0 = blockIdx.x * C::MPB;
+  // the last molecule (or past the block's mpb) work on a copy of the last
+  // molecule and store nothing.
+  const int mpb = a.mpb;
+  const int m0 = blockIdx.x * mpb;
   const int ml = t / 9, lr = t % 9;           // local molecule, row within molecule
   const int m = m0 + ml;
-  const bool valid = m < a.nm;
+  const bool valid = ml < mpb && m < a.nm;
   const int mc = valid ? m : a.nm - 1;        // molecule whose data this row reads
   const long long S = 3LL * a.na;             // stride between beads
   const long long row = 9LL * mc + lr;        // global coordinate row
@@ -70,9 +90,8 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T, 1) k_mts_fused(MtsArgs a) {
     x[j] = a.r[row + S * j];
   }
   __syncthreads();
-  const double sc = sqrt(1.0 / (double)NB);
-  gb_r2hc_io<NB>([&](int j) { return p[j]; }, [&](int k, double v) { p[k] = sc * v; }, s_tw);
-  gb_r2hc_io<NB>([&](int j) { return x[j]; }, [&](int k, double v) { x[k] = sc * v; }, s_tw);
+  gb_r2hc_s<NB>([&](int j) { return p[j]; }, [&](int k, double v) { p[k] = v; }, s_tw, s_twf);
+  gb_r2hc_s<NB>([&](int j) { return x[j]; }, [&](int k, double v) { x[k] = v; }, s_tw, s_twf);
 
   double e_last = 0.0, vir[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   double q1 = 0.0, q2 = 0.0;
@@ -88,13 +107,13 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T, 1) k_mts_fused(MtsArgs a) {
       }
       // bead positions rst = HC2R(r) (evolve_pi.f90:141-145)
       double *dst = s_rst + (ml * 9 + lr) * C::LD;
-      gb_hc2r_io<NB>([&](int j) { return x[j]; }, [&](int k, double v) { dst[k] = sc * v; }, s_tw);
+      gb_hc2r_s<NB>([&](int j) { return x[j]; }, [&](int k, double v) { dst[k] = v; }, s_tw, s_twi);
     }
     __syncthreads();
     // intramolecular forces per (molecule, bead) (forces(rst, ..., 4)); rows of
     // molecules past the end hold copies and are left out of the sums
     double e_sub = 0.0;
-    for (int idx = t; idx < C::MPB * NB; idx += C::T) {
+    for (int idx = t; idx < mpb * NB; idx += T) {
       const int mm = idx / NB, j = idx % NB;
       const double w = (m0 + mm < a.nm) ? 1.0 : 0.0;
       double xm[9], fm[9], vm[9];
@@ -117,17 +136,18 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T, 1) k_mts_fused(MtsArgs a) {
 #pragma unroll
       for (int j = 0; j < NB; ++j) rc = rc + rs_row[j];
       rc = rc / (double)NB;
-      const double w = valid ? 1.0 : 0.0;
+      if (valid) {  // rows of no molecule have no intramolecular forces in s_f2
 #pragma unroll
-      for (int j = 0; j < NB; ++j) {
-        const double dr = w * (rs_row[j] - rc);
-        q1 += dr * a.dvdr[row + S * j];
-        q2 += dr * f2_row[j];
+        for (int j = 0; j < NB; ++j) {
+          const double dr = rs_row[j] - rc;
+          q1 += dr * a.dvdr[row + S * j];
+          q2 += dr * f2_row[j];
+        }
       }
       if (im != a.mts) {  // FT(dvdr2) and p -= dtsmall dvdr2 (evolve_pi.f90:156-159)
         const double dts = a.dtsmall;
-        gb_r2hc_io<NB>([&](int j) { return f2_row[j]; },
-                       [&](int k, double v) { p[k] = p[k] - dts * (sc * v); }, s_tw);
+        gb_r2hc_s<NB>([&](int j) { return f2_row[j]; }, [&](int k, double v) { p[k] = p[k] - dts * v; },
+                      s_tw, s_twf);
       }
     }
     if (im != a.mts) __syncthreads();
@@ -138,10 +158,10 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T, 1) k_mts_fused(MtsArgs a) {
     const double *f2_row = s_f2 + (ml * 9 + lr) * C::LD;
     const double hds = a.halfdtsmall;
     double *gp = a.p + row;
-    gb_hc2r_io<NB>([&](int j) { return p[j]; },
-                   [&](int k, double v) {
-                     if (valid) gp[S * k] = sc * v - hds * f2_row[k];
-                   }, s_tw);
+    gb_hc2r_s<NB>([&](int j) { return p[j]; },
+                  [&](int k, double v) {
+                    if (valid) gp[S * k] = v - hds * f2_row[k];
+                  }, s_tw, s_twi);
     if (valid) {
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
@@ -164,7 +184,7 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T, 1) k_mts_fused(MtsArgs a) {
     red[12 + d] = d == xyz ? q1 : 0.0;
     red[15 + d] = d == xyz ? q2 : 0.0;
   }
-  const int lane = t & 31, warp = t >> 5, nw = (C::T + 31) / 32;
+  const int lane = t & 31, warp = t >> 5, nw = (T + 31) / 32;
 #pragma unroll
   for (int i = 0; i < 18; ++i) {
     double v = warp_sum(red[i]);
@@ -183,22 +203,28 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T, 1) k_mts_fused(MtsArgs a) {
 }
 
 template <int NB>
-size_t mts_smem() {
+size_t mts_smem(int T) {
   using C = MtsCfg<NB>;
-  return sizeof(double) * (2 * C::MPB * 9 * C::LD + 12 * NB + 2 * NB + 32 * 18);
+  const int nrow = (T + 8) / 9 * 9;
+  return sizeof(double) * (2 * nrow * C::LD + 12 * NB + 6 * NB + 32 * 18);
 }
 
 template <int NB>
-void launch_nb(cudaStream_t s, const MtsArgs &a) {
+void launch_nb(cudaStream_t s, MtsArgs a) {
   using C = MtsCfg<NB>;
   static bool attr = false;
-  const size_t smem = mts_smem<NB>();
-  if (!attr) {
-    cudaFuncSetAttribute(k_mts_fused<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (!attr) {  // the largest request of any launch
+    cudaFuncSetAttribute(k_mts_fused<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mts_smem<NB>(C::T_MAX));
     attr = true;
   }
-  const unsigned grid = (unsigned)((a.nm + C::MPB - 1) / C::MPB);
-  k_mts_fused<NB><<<grid, C::T, smem, s>>>(a);
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // one wave of blocks over the SMs when the molecules fit, else MPB_MAX per block
+  a.mpb = std::max(1, std::min(C::MPB_MAX, (a.nm + nsm - 1) / std::max(nsm, 1)));
+  const int T = (9 * a.mpb + 31) / 32 * 32;
+  const unsigned grid = (unsigned)((a.nm + a.mpb - 1) / a.mpb);
+  k_mts_fused<NB><<<grid, T, mts_smem<NB>(T), s>>>(a);
 }
 
 int intra_model_of(const gb_params &P) {

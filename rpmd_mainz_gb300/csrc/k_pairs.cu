@@ -239,26 +239,67 @@ __global__ void k_msite_chain(const double *g, double *out, int nm, int B, doubl
 // no component sits at a rounding tie, where rint and Fortran's nint differ.
 // The virial is symmetric (dx dvy = dy dvx up to rounding): six sums, mirrored
 // when the block sums are added.
-__global__ void __launch_bounds__(128) k_ewald_real(const double *__restrict__ rs, const double *__restrict__ q,
-                                                    int na, const int *__restrict__ count,
-                                                    const int *__restrict__ idx, int cap, double alpha,
-                                                    double *g, double *acc) {
+//
+// PAIR_NP adjacent lanes share one site's list (entries sub, sub + NP, ...),
+// so that the grid holds enough warps to fill every SM; the site's own force
+// is reduced over its lanes with shuffles before one atomic add.
+constexpr int PAIR_NP = 8;
+constexpr int PAIR_T = 64;
+
+template <int NP>
+GB_D double group_sum(double v) {
+#pragma unroll
+  for (int o = NP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block sums of (v, xx, yx, zx, yy, zy, zz) into an accumulator slot laid out
+// as v, vir(1..3, 1..3) column-major, the symmetric entries mirrored
+GB_D void block_sum_sym7(double (&vals)[7], double *sh, double *acc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    const double v = warp_sum(vals[k]);
+    if (lane == 0) sh[warp * 7 + k] = v;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int dst0[7] = {0, 1, 2, 3, 5, 6, 9};       // v, xx, yx, zx, yy, zy, zz
+    constexpr int dst1[7] = {-1, -1, 4, 7, -1, 8, -1};   // mirrored xy, xz, yz
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      double s2 = lane < nw ? sh[lane * 7 + k] : 0.0;
+      s2 = warp_sum(s2);
+      if (lane == 0 && s2 != 0.0) {
+        atomicAdd(acc + dst0[k], s2);
+        if (dst1[k] >= 0) atomicAdd(acc + dst1[k], s2);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(PAIR_T) k_ewald_real(const double *__restrict__ rs, const double *__restrict__ q,
+                                                       int na, const int *__restrict__ count,
+                                                       const int *__restrict__ idx, int cap, double alpha,
+                                                       double *g, double *acc) {
   __shared__ double sh[32 * 7];
   const double p = 3.0525860, a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741,
                a4 = -1.453152027, a5 = 1.061405429;
   const double sfac = -2.0 * alpha / sqrt(acos(-1.0));
   const int c = blockIdx.y;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double vals[7] = {0, 0, 0, 0, 0, 0, 0};  // v, xx, xy, xz, yy, yz, zz
-  if (i < na) {
-    const double *R = rs + (long long)c * na * 3;
-    double *G = g + (long long)c * na * 3;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(tid / PAIR_NP), sub = (int)(tid % PAIR_NP);
+  const bool active = i < na;
+  double vals[7] = {0, 0, 0, 0, 0, 0, 0};  // v, xx, yx, zx, yy, zy, zz
+  double fx = 0, fy = 0, fz = 0;
+  const double *R = rs + (long long)c * na * 3;
+  double *G = g + (long long)c * na * 3;
+  if (active) {
     const double xi = R[3 * i], yi = R[3 * i + 1], zi = R[3 * i + 2], qi = q[i];
     const int mi = i / 3;
     const int n = min(count[(long long)c * na + i], cap);
     const int *L = idx + ((long long)c * na + i) * cap;
-    double fx = 0, fy = 0, fz = 0;
-    for (int t = 0; t < n; ++t) {
+    for (int t = sub; t < n; t += PAIR_NP) {
       const int j = L[t];
       double dx = xi - R[3 * j], dy = yi - R[3 * j + 1], dz = zi - R[3 * j + 2];
       dx -= rint(dx);
@@ -290,52 +331,41 @@ __global__ void __launch_bounds__(128) k_ewald_real(const double *__restrict__ r
       vals[5] += dz * dvy;
       vals[6] += dz * dvz;
     }
+  }
+  fx = group_sum<PAIR_NP>(fx);
+  fy = group_sum<PAIR_NP>(fy);
+  fz = group_sum<PAIR_NP>(fz);
+  if (active && sub == 0) {
     atomicAdd(G + 3 * i, fx);
     atomicAdd(G + 3 * i + 1, fy);
     atomicAdd(G + 3 * i + 2, fz);
   }
-  // block sums; slot layout v, vir(1..3, 1..3) column-major
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int k = 0; k < 7; ++k) {
-    const double v = warp_sum(vals[k]);
-    if (lane == 0) sh[warp * 7 + k] = v;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    constexpr int dst0[7] = {0, 1, 2, 3, 5, 6, 9};  // v, xx, yx, zx, yy, zy, zz
-    constexpr int dst1[7] = {-1, -1, 4, 7, -1, 8, -1};  // mirrored xy, xz, yz
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-      double s2 = lane < nw ? sh[lane * 7 + k] : 0.0;
-      s2 = warp_sum(s2);
-      if (lane == 0 && s2 != 0.0) {
-        atomicAdd(acc + dst0[k], s2);
-        if (dst1[k] >= 0) atomicAdd(acc + dst1[k], s2);
-      }
-    }
-  }
+  block_sum_sym7(vals, sh, acc);
 }
 
 // ---- Lennard-Jones O-O (lj_list / lj_basic / lj_cell, ljones.f90) ----
 // points are the oxygens; bead test with the same rounding as the reference
-__global__ void __launch_bounds__(128) k_lj(const double *r, int na, int npt, int nconf_list,
-                                            const int *count, const int *idx, int cap,
-                                            double sigsq, double rcutsq, double3 box, double3 onbox,
-                                            double dscale, double *out, double *acc) {
+constexpr int LJ_NP = 4;
+
+__global__ void __launch_bounds__(PAIR_T) k_lj(const double *r, int na, int npt, int nconf_list,
+                                               const int *count, const int *idx, int cap,
+                                               double sigsq, double rcutsq, double3 box, double3 onbox,
+                                               double dscale, double *out, double *acc) {
   __shared__ double sh[32 * 10];
   const int c = blockIdx.y;
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int o = (int)(tid / LJ_NP), sub = (int)(tid % LJ_NP);
+  const bool active = o < npt;
   double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  if (o < npt) {
-    const double *R = r + (long long)c * na * 3;
-    double *F = out + (long long)c * na * 3;
+  double fx = 0, fy = 0, fz = 0;
+  const double *R = r + (long long)c * na * 3;
+  double *F = out + (long long)c * na * 3;
+  if (active) {
     const int lc = nconf_list == 1 ? 0 : c;
     const int n = min(count[(long long)lc * npt + o], cap);
     const int *L = idx + ((long long)lc * npt + o) * cap;
     const double xo = R[9 * o], yo = R[9 * o + 1], zo = R[9 * o + 2];
-    double fx = 0, fy = 0, fz = 0;
-    for (int t = 0; t < n; ++t) {
+    for (int t = sub; t < n; t += LJ_NP) {
       const int j = L[t];
       double dx = __dsub_rn(R[9 * j], xo), dy = __dsub_rn(R[9 * j + 1], yo), dz = __dsub_rn(R[9 * j + 2], zo);
       dx = __dsub_rn(dx, __dmul_rn(box.x, nint_d(__dmul_rn(onbox.x, dx))));
@@ -362,6 +392,11 @@ __global__ void __launch_bounds__(128) k_lj(const double *r, int na, int npt, in
         vals[7] -= dx * dfz; vals[8] -= dy * dfz; vals[9] -= dz * dfz;
       }
     }
+  }
+  fx = group_sum<LJ_NP>(fx);
+  fy = group_sum<LJ_NP>(fy);
+  fz = group_sum<LJ_NP>(fz);
+  if (active && sub == 0) {
     atomicAdd(F + 9 * o, dscale * fx);
     atomicAdd(F + 9 * o + 1, dscale * fy);
     atomicAdd(F + 9 * o + 2, dscale * fz);
@@ -533,17 +568,17 @@ void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, in
 
 void launch_ewald_real(cudaStream_t s, const double *rs, const double *q, int na, int B,
                        const PairList &pl, double alpha, double *g, double *acc) {
-  dim3 grid(nblk(na, 128), B);
-  k_ewald_real<<<grid, 128, 0, s>>>(rs, q, na, pl.count, pl.idx, pl.cap, alpha, g, acc);
+  dim3 grid(nblk((long long)na * PAIR_NP, PAIR_T), B);
+  k_ewald_real<<<grid, PAIR_T, 0, s>>>(rs, q, na, pl.count, pl.idx, pl.cap, alpha, g, acc);
 }
 
 void launch_lj(cudaStream_t s, const double *r, int na, int B, const PairList &pl, double sigsq,
                double rcutsq, const double *box, double dscale, double *out, double *acc) {
   int npt = na / 3;
-  dim3 grid(nblk(npt, 128), B);
+  dim3 grid(nblk((long long)npt * LJ_NP, PAIR_T), B);
   double3 bx = make_double3(box[0], box[1], box[2]);
   double3 ob = make_double3(1.0 / box[0], 1.0 / box[1], 1.0 / box[2]);
-  k_lj<<<grid, 128, 0, s>>>(r, na, npt, pl.nconf, pl.count, pl.idx, pl.cap, sigsq, rcutsq, bx, ob,
+  k_lj<<<grid, PAIR_T, 0, s>>>(r, na, npt, pl.nconf, pl.count, pl.idx, pl.cap, sigsq, rcutsq, bx, ob,
                             dscale, out, acc);
 }
 
