@@ -6,10 +6,15 @@ q-SPC/Fw water, 4096 H2O on a 16^3 CUB lattice (L = 49.71 A, rho = 0.997
 g/cm^3), nb = 32 beads, T = 298 K, MTS = 5 (dt = 1.25 fs outer, 0.25 fs inner),
 ring-polymer contraction: Ewald on the centroid (nbdf1 = 1), Lennard-Jones on
 5 normal modes (nbdf2 = 5; the reference requires an odd count), intramolecular
-forces on all 32 beads; plain FP64.  Inputs are synthetic: the reference's
-deterministic CUB lattice and momenta drawn from the reference's ran2/gaussian
-stream (sample_rpmd) after an initial full_forces.
+forces on all 32 beads.  Inputs are synthetic: the reference's deterministic
+CUB lattice and momenta drawn from the reference's ran2/gaussian stream
+(sample_rpmd) after an initial full_forces.
 
+--precision mixed (default): FP32 pair / reciprocal / transform arithmetic with
+        compensated sums, FP64 state, propagator, energies and virials; the
+        plain-FP64 arm is timed in the same run ("fp64_arm", "mixed_over_fp64")
+        and the force error against it is reported ("error_vs_fp64").
+--precision fp64: the plain-FP64 path alone.
 value:  nb * nm * K / (sum of the K steps' CUDA-event times), state resident in
         HBM, L2 flushed (256 MiB write) between steps outside the timed events.
 e2e:    the same metric through the drop-in C-ABI call gbrpmd_evolve_pi with
@@ -137,6 +142,28 @@ def fp64_peak_tflops(torch):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def fp32_peak_tflops(torch):
+    """Measured FP32 CUDA-core peak: cuBLAS SGEMM 8192^3 with TF32 off, best of 3."""
+    n = 8192
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(n, n, dtype=torch.float32, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float32, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    torch.backends.cuda.matmul.allow_tf32 = old
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
 def read_profile_traffic(region):
     """DRAM bytes per launch of `region` from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
@@ -202,34 +229,18 @@ def run_reference(args, rank, world):
     return 0
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
-    ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    args = ap.parse_args()
-    args.warmup = max(args.warmup, 3)
-    rank, world, local = dist_env()
-    if args.impl == "reference":
-        return run_reference(args, rank, world)
-
-    import torch
-
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
-    import __graft_entry__ as g
-
-    g.build()
+def set_precision(s, prec):
     from rpmd_mainz_gb300 import lib
 
-    s = make_system(args.workload)
+    s["params"].precision = prec
+    lib.init(s["params"])
+
+
+def measure(args, s, prec, torch, world, local):
+    """One arm on the resident context: profiled pass, timed steps, e2e drop-in."""
+    from rpmd_mainz_gb300 import lib
+
+    set_precision(s, prec)
     na, nb, nm = s["na"], s["nb"], s["nm"]
     ff = lib.full_forces(s["r"], s["box"], s["z"])
     ctx = lib.Context(na, nb, s["mass"], s["z"])
@@ -303,45 +314,121 @@ def main():
         e2e_times.append(time.perf_counter() - t0)
     e2e_value = world * nb * nm * len(e2e_times) / sum(e2e_times)
     nbytes = 4 * r_h.nbytes
+    ctx.close()
+    del flush
+    return dict(value=value, total_ms=total_ms, step_ms=step_ms, launches=launches, rebuilds=rebuilds,
+                energies=energies, regions=regions, clocks=clk.summary(), e2e_value=e2e_value, e2e_bytes=nbytes)
 
+
+def force_error(s):
+    """Relative RMS force error (total and low-frequency) and energy error of the
+    mixed path against the FP64 path on the workload's starting snapshot."""
+    from rpmd_mainz_gb300 import lib
+
+    out = []
+    for prec in (0, 1):
+        set_precision(s, prec)
+        out.append(lib.full_forces(s["r"], s["box"], s["z"]))
+    f64, fmx = out
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    return {"force_rel_rms": rel(fmx["dvdr"] + fmx["dvdr2"], f64["dvdr"] + f64["dvdr2"]),
+            "lowfreq_force_rel_rms": rel(fmx["dvdr"], f64["dvdr"]),
+            "energy_rel": abs(fmx["v"] - f64["v"]) / abs(f64["v"]),
+            "virial_rel": rel(fmx["vir"], f64["vir"]), "bound": 1e-5}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-arm", action="store_true", help="skip the plain-FP64 comparison arm")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import __graft_entry__ as g
+
+    g.build()
+
+    s = make_system(args.workload)
+    prec = 1 if args.precision == "mixed" else 0
+    m = measure(args, s, prec, torch, world, local)
+    fp64 = None
+    if prec == 1 and not args.no_fp64_arm:
+        f = measure(args, s, 0, torch, world, local)
+        fp64 = {"value": f["value"], "ms_per_step": f["total_ms"] / args.steps,
+                "p50_ms": float(np.median(f["step_ms"])), "p99_ms": float(np.percentile(f["step_ms"], 99)),
+                "regions_ms_one_step": {k: v["ms"] for k, v in f["regions"].items()}}
+    err = force_error(s) if prec == 1 else None
+    regions = m["regions"]
     out = {
-        "metric": "bead-molecule-steps/s", "value": value, "unit": "bead-molecule-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "metric": "bead-molecule-steps/s", "value": m["value"], "unit": "bead-molecule-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["total_ms"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 mixed" if prec == 1 else "f64",
         "data": "synthetic (CUB lattice, Maxwell-Boltzmann momenta from the reference's ran2 stream)",
-        "config": {"workload": args.workload, "nm": nm, "nb": nb, "mts": s["params"].mts,
-                   "nbdf1": s["params"].nbdf1, "nbdf2": s["params"].nbdf2, "precision": "fp64",
+        "config": {"workload": args.workload, "nm": s["nm"], "nb": s["nb"], "mts": s["params"].mts,
+                   "nbdf1": s["params"].nbdf1, "nbdf2": s["params"].nbdf2, "precision": args.precision,
                    "l2": "256 MiB flush between steps, outside the timed events",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
-        "gpu_launches": int(launches),
-        "list_rebuilds": {"ewald": rebuilds[0], "lj": rebuilds[1], "tem": rebuilds[2],
+        "p50_ms": float(np.median(m["step_ms"])), "p99_ms": float(np.percentile(m["step_ms"], 99)),
+        "gpu_launches": int(m["launches"]),
+        "list_rebuilds": {"ewald": m["rebuilds"][0], "lj": m["rebuilds"][1], "tem": m["rebuilds"][2],
                           "skin": "0.1 of each cut-off; exact pair sets filtered from the skin list every step"},
-        "e2e": {"value": e2e_value, "unit": "bead-molecule-steps/s", "h2d_bytes_per_step": int(nbytes),
-                "d2h_bytes_per_step": int(nbytes + 8 * 22),
+        "e2e": {"value": m["e2e_value"], "unit": "bead-molecule-steps/s", "h2d_bytes_per_step": int(m["e2e_bytes"]),
+                "d2h_bytes_per_step": int(m["e2e_bytes"] + 8 * 22),
                 "path": "gbrpmd_evolve_pi drop-in, pinned host p/r/dvdr/dvdr2"},
-        "energies_last_step": {"v": energies["v"], "vew": energies["vew"], "vlj": energies["vlj"],
-                               "vint": energies["vint"]},
+        "energies_last_step": {k: m["energies"][k] for k in ("v", "vew", "vlj", "vint")},
         "regions_ms_one_step": regions,
     }
-    # roofline of the dominant kernel region (FP64 CUDA-core bound)
+    if fp64 is not None:
+        out["fp64_arm"] = fp64
+        out["mixed_over_fp64"] = m["value"] / fp64["value"]
+    if err is not None:
+        out["error_vs_fp64"] = err
     if rank == 0:
-        peak = fp64_peak_tflops(torch)
+        # roofline of the dominant kernel region
         dom = max((k for k in regions if k in FLOPS_PER_UNIT), key=lambda k: regions[k]["ms"])
         rr = regions[dom]
         per_launch_ms = rr["ms"] / rr["launches"]
         flops_per_launch = FLOPS_PER_UNIT[dom] * rr["units"] / rr["launches"]
         achieved = flops_per_launch / (per_launch_ms * 1e-3) / 1e12
-        out["roofline"] = {"bound": "fp64", "kernel_region": dom, "achieved": achieved, "peak": peak,
-                           "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom),
-                           "peak_source": "measured in this run: cuBLAS DGEMM 8192^3 (FP64 CUDA-core/tensor "
-                                          "rate; MEASURED_PEAKS.json holds only HBM and BF16)",
-                           "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": rr["units"] / rr["launches"]}
-        out["clocks"] = clk.summary()
+        if prec == 0:
+            peak = fp64_peak_tflops(torch)
+            out["roofline"] = {"bound": "fp64", "kernel_region": dom, "achieved": achieved, "peak": peak,
+                               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom),
+                               "peak_source": "measured in this run: cuBLAS DGEMM 8192^3 (FP64 rate; "
+                                              "MEASURED_PEAKS.json holds only HBM and BF16)",
+                               "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": rr["units"] / rr["launches"]}
+        else:
+            peak = fp32_peak_tflops(torch)
+            out["roofline"] = {"bound": "fp32", "kernel_region": dom, "achieved": achieved, "peak": peak,
+                               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom),
+                               "peak_source": "measured in this run: cuBLAS SGEMM 8192^3 without TF32 (FP32 "
+                                              "CUDA-core rate; MEASURED_PEAKS.json holds only HBM and BF16)",
+                               "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": rr["units"] / rr["launches"]}
+        out["clocks"] = m["clocks"]
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(s)
         print(json.dumps(out), flush=True)
-    ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

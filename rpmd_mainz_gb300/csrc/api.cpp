@@ -73,6 +73,9 @@ int set_charges(gb_context *c, const double *z) {
   double qq = 0.0;
   for (int i = 0; i < c->na; ++i) qq = qq + z[i] * z[i];
   c->qq = qq;
+  c->h_z32.resize(c->na);
+  for (int i = 0; i < c->na; ++i) c->h_z32[i] = (float)z[i];
+  CK(cudaMemcpyAsync(c->z32, c->h_z32.data(), sizeof(float) * c->na, cudaMemcpyHostToDevice, c->stream));
   return upload(c, c->z, z, (size_t)c->na);
 }
 
@@ -138,7 +141,9 @@ int ctx_alloc(gb_context *c, int na, int nb) {
       (st = dalloc(c, &c->f_a, N)) || (st = dalloc(c, &c->f_b, N)) || (st = dalloc(c, &c->f_c, N)) ||
       (st = dalloc(c, &c->rb1, N)) || (st = dalloc(c, &c->fb1, N)) || (st = dalloc(c, &c->rb2, N)) ||
       (st = dalloc(c, &c->fb2, N)) || (st = dalloc(c, &c->g, N)) || (st = dalloc(c, &c->rs, N)) ||
-      (st = dalloc(c, &c->rs32, (size_t)na * nb)) || (st = dalloc(c, &c->rc, S)) ||
+      (st = dalloc(c, &c->rs32, (size_t)na * nb)) || (st = dalloc(c, &c->lo32, (size_t)na * nb)) ||
+      (st = dalloc(c, &c->hi32, (size_t)na * nb / 3)) || (st = dalloc(c, &c->olo32, (size_t)na * nb / 3)) ||
+      (st = dalloc(c, &c->z32, (size_t)na)) || (st = dalloc(c, &c->rc, S)) ||
       (st = dalloc(c, &c->monod, 12 * (size_t)nb)) ||
       (st = dalloc(c, &c->acc, (size_t)ACC_NSLOT * ACC_STRIDE)) || (st = dalloc(c, &c->status, 1)))
     return st;
@@ -177,6 +182,8 @@ extern "C" {
 int gbrpmd_init(const gb_params *params) {
   if (!params) return ctx_set_error(GB_E_ARG, "null params");
   if (params->mts < 1) return ctx_set_error(GB_E_ARG, "mts must be >= 1");
+  if (params->precision != GB_PREC_FP64 && params->precision != GB_PREC_MIXED)
+    return ctx_set_error(GB_E_ARG, "precision must be GB_PREC_FP64 or GB_PREC_MIXED");
   g_params = *params;
   g_init = true;
   return GB_OK;

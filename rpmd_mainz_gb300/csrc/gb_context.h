@@ -33,7 +33,7 @@ struct SkinList {
   unsigned *flag = nullptr;      // device word: nonzero = rebuild at this use
   unsigned *rebuilds = nullptr;  // device counter of rebuilds
   bool valid = false;            // storage and key match the last use
-  int nconf = 0, npt = 0, unit = 0, excl = 0;
+  int nconf = 0, npt = 0, unit = 0, excl = 0, full = 0;
   long long pstride = 0, cstride = 0;
   double cutsq = 0.0, skin = 0.0, box[3] = {0, 0, 0};
 };
@@ -69,6 +69,11 @@ struct gb_context {
   double *g = nullptr;     // unit-box gradient scratch [nb][na][3]
   double *rs = nullptr;    // site positions scratch [nb][na][3]
   float4 *rs32 = nullptr;  // FP32 fractional coordinates for list prefilters [nb][na]
+  float4 *lo32 = nullptr;  // their FP32 remainders (mixed precision) [nb][na]
+  float4 *hi32 = nullptr;  // bead oxygen coordinates for the FP32 LJ kernel [nb][nm]
+  float4 *olo32 = nullptr; // and their remainders [nb][nm]
+  float *z32 = nullptr;    // charges in FP32 [na]
+  std::vector<float> h_z32;
   double *rc = nullptr;    // centroid scratch [na][3]
   PairList pl;             // exact pair list of the current term (re-sized on demand)
   size_t pl_idx_bytes = 0, pl_cnt_bytes = 0;

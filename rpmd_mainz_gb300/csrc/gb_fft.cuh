@@ -27,14 +27,14 @@ GB_HD constexpr int gb_bitrev(int i, int h) {
 
 // one radix-2 stage of butterfly span LEN (template recursion keeps every index
 // a compile-time constant, so the arrays stay in registers)
-template <int H, int N, bool INV, int LEN>
-GB_D void gb_cfft_stage(double (&zr)[H], double (&zi)[H], const double *__restrict__ tw) {
+template <int H, int N, bool INV, int LEN, typename R>
+GB_D void gb_cfft_stage(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw) {
   if constexpr (LEN <= H) {
     constexpr int half = LEN / 2;
 #pragma unroll
     for (int k = 0; k < half; ++k) {
       const int m = k * (N / LEN);
-      double wr = 1.0, wi = 0.0;
+      R wr = (R)1, wi = (R)0;
       if (k > 0 && 4 * m != N) {
         wr = tw[m];
         wi = INV ? tw[N + m] : -tw[N + m];
@@ -42,7 +42,7 @@ GB_D void gb_cfft_stage(double (&zr)[H], double (&zi)[H], const double *__restri
 #pragma unroll
       for (int i = 0; i < H; i += LEN) {
         const int a = i + k, b = a + half;
-        double tr, ti;
+        R tr, ti;
         if (k == 0) {
           tr = zr[b];
           ti = zi[b];
@@ -59,23 +59,23 @@ GB_D void gb_cfft_stage(double (&zr)[H], double (&zi)[H], const double *__restri
         zi[a] = zi[a] + ti;
       }
     }
-    gb_cfft_stage<H, N, INV, 2 * LEN>(zr, zi, tw);
+    gb_cfft_stage<H, N, INV, 2 * LEN, R>(zr, zi, tw);
   }
 }
 
 // in-place radix-2 complex FFT of length H on register arrays; N = table length
 // (a multiple of H); INV selects exp(+...) twiddles
-template <int H, int N, bool INV>
-GB_D void gb_cfft(double (&zr)[H], double (&zi)[H], const double *__restrict__ tw) {
+template <int H, int N, bool INV, typename R>
+GB_D void gb_cfft(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw) {
 #pragma unroll
   for (int i = 0; i < H; ++i) {
     const int j = gb_bitrev(i, H);
     if (i < j) {
-      double t = zr[i]; zr[i] = zr[j]; zr[j] = t;
+      R t = zr[i]; zr[i] = zr[j]; zr[j] = t;
       t = zi[i]; zi[i] = zi[j]; zi[j] = t;
     }
   }
-  gb_cfft_stage<H, N, INV, 2>(zr, zi, tw);
+  gb_cfft_stage<H, N, INV, 2, R>(zr, zi, tw);
 }
 
 // unscaled R2HC of length N (power of two) in registers
@@ -186,30 +186,30 @@ GB_D void gb_hc2r_direct(const double *in, double *x, int n, const double *__res
 //   twf[m] = (sc / 2) cos(2 pi m / n), twf[n + m] = (sc / 2) sin(...)  (forward)
 //   twi[m] = sc cos(2 pi m / n),       twi[n + m] = sc sin(...)        (inverse)
 // tw is the unscaled table of the complex FFT.
-template <int N, class In, class Out>
-GB_D void gb_r2hc_s(In in, Out out, const double *__restrict__ tw, const double *__restrict__ twf) {
-  const double sc = twf[0] + twf[0];
+template <int N, typename R = double, class In, class Out>
+GB_D void gb_r2hc_s(In in, Out out, const R *__restrict__ tw, const R *__restrict__ twf) {
+  const R sc = twf[0] + twf[0];
   if constexpr (N == 1) {
     out(0, sc * in(0));
   } else {
     constexpr int H = N / 2;
-    double zr[H], zi[H];
+    R zr[H], zi[H];
 #pragma unroll
     for (int j = 0; j < H; ++j) {
       zr[j] = in(2 * j);
       zi[j] = in(2 * j + 1);
     }
-    if constexpr (H > 1) gb_cfft<H, N, false>(zr, zi, tw);
+    if constexpr (H > 1) gb_cfft<H, N, false, R>(zr, zi, tw);
     out(0, sc * (zr[0] + zi[0]));
     out(H, sc * (zr[0] - zi[0]));
 #pragma unroll
     for (int k = 1; 2 * k < H; ++k) {
       const int b = H - k;
-      const double P = zr[k] + zr[b], Q = zi[k] + zi[b];
-      const double R = zr[k] - zr[b], D = zi[k] - zi[b];
-      const double hc = twf[k], hs = twf[N + k];
-      const double hP = twf[0] * P, hD = twf[0] * D;
-      const double T1 = hc * Q - hs * R, T2 = hc * R + hs * Q;
+      const R P = zr[k] + zr[b], Q = zi[k] + zi[b];
+      const R Rd = zr[k] - zr[b], D = zi[k] - zi[b];
+      const R hc = twf[k], hs = twf[N + k];
+      const R hP = twf[0] * P, hD = twf[0] * D;
+      const R T1 = hc * Q - hs * Rd, T2 = hc * Rd + hs * Q;
       out(k, hP + T1);
       out(b, hP - T1);
       out(N - k, hD - T2);
@@ -222,16 +222,16 @@ GB_D void gb_r2hc_s(In in, Out out, const double *__restrict__ tw, const double 
   }
 }
 
-template <int N, class In, class Out>
-GB_D void gb_hc2r_s(In in, Out out, const double *__restrict__ tw, const double *__restrict__ twi) {
-  const double sc = twi[0];
+template <int N, typename R = double, class In, class Out>
+GB_D void gb_hc2r_s(In in, Out out, const R *__restrict__ tw, const R *__restrict__ twi) {
+  const R sc = twi[0];
   if constexpr (N == 1) {
     out(0, sc * in(0));
   } else {
     constexpr int H = N / 2;
-    double zr[H], zi[H];
+    R zr[H], zi[H];
     {
-      const double i0 = in(0), ih = in(H);
+      const R i0 = in(0), ih = in(H);
       zr[0] = sc * (i0 + ih);
       zi[0] = sc * (i0 - ih);
     }
@@ -239,22 +239,22 @@ GB_D void gb_hc2r_s(In in, Out out, const double *__restrict__ tw, const double 
     for (int k = 1; 2 * k < H; ++k) {
       const int b = H - k;
       // X_k = in(k) + i in(N-k), conj(X_{H-k}) = in(H-k) - i in(H+k)
-      const double xr = in(k), xi = in(N - k), cr = in(b), ci = -in(H + k);
-      const double A = sc * (xr + cr), B = sc * (xi + ci);
-      const double dr = xr - cr, di = xi - ci;
-      const double c = twi[k], s = twi[N + k];
-      const double U = c * di + s * dr, V = c * dr - s * di;
+      const R xr = in(k), xi = in(N - k), cr = in(b), ci = -in(H + k);
+      const R A = sc * (xr + cr), B = sc * (xi + ci);
+      const R dr = xr - cr, di = xi - ci;
+      const R c = twi[k], s = twi[N + k];
+      const R U = c * di + s * dr, V = c * dr - s * di;
       zr[k] = A - U;
       zr[b] = A + U;
       zi[k] = B + V;
       zi[b] = V - B;
     }
     if constexpr (H % 2 == 0) {  // k = H/2: cos = 0, sin = 1
-      const double xr = in(H / 2), xi = in(N - H / 2);
-      zr[H / 2] = 2.0 * sc * xr;
-      zi[H / 2] = -2.0 * sc * xi;
+      const R xr = in(H / 2), xi = in(N - H / 2);
+      zr[H / 2] = (R)2 * sc * xr;
+      zi[H / 2] = (R)-2 * sc * xi;
     }
-    if constexpr (H > 1) gb_cfft<H, N, true>(zr, zi, tw);
+    if constexpr (H > 1) gb_cfft<H, N, true, R>(zr, zi, tw);
 #pragma unroll
     for (int j = 0; j < H; ++j) {
       out(2 * j, zr[j]);

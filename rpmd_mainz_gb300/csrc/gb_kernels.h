@@ -27,10 +27,11 @@ struct PairGeom {
   double box[3], onbox[3];
   double rcutsq;
   int excl_mol;  // skip pairs with i/3 == j/3 (same molecule; TEM correction)
+  int full;      // 1: store each pair in both lists (no parity halving)
 };
 
 // ---- pair lists (k_pairs.cu) ----
-void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac);
+void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo = nullptr);
 // every pair within g.rcutsq; with a gate word, only when *gate != 0 (counts
 // are then zeroed on the device, so the decision needs no host round trip)
 void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
@@ -56,6 +57,15 @@ void launch_recip_sk(cudaStream_t s, gb_context *c, const double *rs, const doub
 void launch_recip_weights(cudaStream_t s, gb_context *c, int B, double *acc);
 void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B,
                         double *g);
+// ---- mixed precision (k_mixed.cu): FP32 arithmetic, full lists, hi/lo positions ----
+void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, const float *q, int na, int B,
+                          const PairList &pl, double alpha, double *g, double *acc);
+void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
+                  double sigsq, double rcutsq, const double *box, double dscale, double *out, double *acc);
+void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);
+void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc);
+void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g);
+void recip_set_attributes_mx();
 // out[b] = sign * chain_rule(scale * g[b]) (+= when accumulate)
 void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, int B, double alpha,
                         double scale, double sign, int accumulate);

@@ -1,0 +1,465 @@
+// k_mixed.cu -- FP32 force kernels of the mixed-precision path.
+//
+// Same pair sets and formulas as the FP64 kernels (k_pairs.cu, k_recip.cu),
+// with the per-pair and per-(k, site) arithmetic in FP32:
+//  * positions enter as two FP32 numbers per wrapped fractional coordinate
+//    (hi + lo, k_frac32), so a minimum-image displacement
+//    (hi_i - hi_j - rint(hi_i - hi_j)) + (lo_i - lo_j) keeps ~1e-14 of the box;
+//  * pair kernels walk full lists (each pair from both ends), so every point's
+//    force is summed by its own lanes and no atomics are needed;
+//  * force and energy sums are compensated (Kahan) FP32 per thread, virials
+//    plain FP32 per thread; all of them FP64 across threads;
+//  * the reciprocal-space power tables come from the FP64 recurrence rounded
+//    to FP32; structure-factor partials are FP32 over 32 sites and FP64 over
+//    chunks; energy, virial and the k-space totals stay FP64.
+#include "gb_common.cuh"
+#include "gb_kernels.h"
+
+namespace {
+
+constexpr int MX_T = 64;     // threads per block of the pair kernels
+constexpr int MX_NP = 8;     // lanes per site in the real-space kernel
+constexpr int MX_LJ_NP = 4;  // lanes per oxygen in the LJ kernel
+
+GB_D void kadd(float &s, float &c, float v) {  // Kahan-compensated s += v
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+template <int NP>
+GB_D double group_sum_d(double v) {
+#pragma unroll
+  for (int o = NP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// minimum-image difference of two hi/lo fractional coordinates
+GB_D float dmin(float hi_a, float lo_a, float hi_b, float lo_b) {
+  const float d = hi_a - hi_b;
+  return (d - rintf(d)) + (lo_a - lo_b);
+}
+
+// block sums of (v, xx, yx, zx, yy, zy, zz) into v, vir(1..3, 1..3) column-major
+GB_D void block_sum_sym7_mx(double (&vals)[7], double *sh, double *acc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    const double v = warp_sum(vals[k]);
+    if (lane == 0) sh[warp * 7 + k] = v;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int dst0[7] = {0, 1, 2, 3, 5, 6, 9};
+    constexpr int dst1[7] = {-1, -1, 4, 7, -1, 8, -1};
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      double s2 = lane < nw ? sh[lane * 7 + k] : 0.0;
+      s2 = warp_sum(s2);
+      if (lane == 0 && s2 != 0.0) {
+        atomicAdd(acc + dst0[k], s2);
+        if (dst1[k] >= 0) atomicAdd(acc + dst1[k], s2);
+      }
+    }
+  }
+}
+
+// rwald (ewald_cubic.f90:78-233) in FP32 over a full list; g += gradient
+// (single writer per site), energy and virial halved for the double count
+__global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                                                        const float *__restrict__ q, int na,
+                                                        const int *__restrict__ count, const int *__restrict__ idx,
+                                                        int cap, float alpha, double *g, double *acc) {
+  __shared__ double sh[32 * 7];
+  const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
+              a4 = -1.453152027f, a5 = 1.061405429f;
+  const float sfac = (float)(-2.0 / sqrt(acos(-1.0))) * alpha;
+  const int c = blockIdx.y;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(tid / MX_NP), sub = (int)(tid % MX_NP);
+  const bool active = i < na;
+  const float4 *H = hi + (long long)c * na, *Lo = lo + (long long)c * na;
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  float ev = 0.f, evc = 0.f, vxx = 0.f, vyx = 0.f, vzx = 0.f, vyy = 0.f, vzy = 0.f, vzz = 0.f;
+  if (active) {
+    const float4 hi_i = H[i], lo_i = Lo[i];
+    const float qi = q[i];
+    const int mi = i / 3;
+    const int n = min(count[(long long)c * na + i], cap);
+    const int *L = idx + ((long long)c * na + i) * cap;
+    for (int t = sub; t < n; t += MX_NP) {
+      const int j = L[t];
+      const float4 hj = H[j], lj = Lo[j];
+      const float dx = dmin(hi_i.x, lo_i.x, hj.x, lj.x);
+      const float dy = dmin(hi_i.y, lo_i.y, hj.y, lj.y);
+      const float dz = dmin(hi_i.z, lo_i.z, hj.z, lj.z);
+      const float drsq = dx * dx + dy * dy + dz * dz;
+      const float inv = rsqrtf(drsq);
+      const float x = alpha * (drsq * inv);
+      const float e = expf(-x * x);
+      const float tt = __fdividef(p, p + x);
+      float erfc = e * tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5))));
+      if (mi == j / 3) erfc -= 1.0f;
+      const float du = erfc * inv;
+      const float dur = (sfac * e - du) * (inv * inv);
+      const float qij = qi * q[j];
+      const float dvr = qij * dur;
+      const float fx = dvr * dx, fy = dvr * dy, fz = dvr * dz;
+      kadd(sx, cx, fx);
+      kadd(sy, cy, fy);
+      kadd(sz, cz, fz);
+      kadd(ev, evc, qij * du);
+      vxx += dx * fx;
+      vyx += dy * fx;
+      vzx += dz * fx;
+      vyy += dy * fy;
+      vzy += dz * fy;
+      vzz += dz * fz;
+    }
+  }
+  const double fx = group_sum_d<MX_NP>((double)sx - (double)cx);
+  const double fy = group_sum_d<MX_NP>((double)sy - (double)cy);
+  const double fz = group_sum_d<MX_NP>((double)sz - (double)cz);
+  if (active && sub == 0) {
+    double *G = g + ((long long)c * na + i) * 3;
+    G[0] += fx;
+    G[1] += fy;
+    G[2] += fz;
+  }
+  double vals[7] = {0.5 * ((double)ev - (double)evc), 0.5 * vxx, 0.5 * vyx, 0.5 * vzx, 0.5 * vyy, 0.5 * vzy, 0.5 * vzz};
+  block_sum_sym7_mx(vals, sh, acc);
+}
+
+// lj_list / lj_basic (ljones.f90) in FP32 over a full oxygen list; bead pairs
+// beyond rcut are skipped as in the reference; out += dscale * gradient
+__global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo, int na,
+                                                int npt, int nconf_list, const int *__restrict__ count,
+                                                const int *__restrict__ idx, int cap, float sigsq, float rcutsq,
+                                                float3 box, double dscale, double *out, double *acc) {
+  __shared__ double sh[32 * 10];
+  const int c = blockIdx.y;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int o = (int)(tid / MX_LJ_NP), sub = (int)(tid % MX_LJ_NP);
+  const bool active = o < npt;
+  const float4 *H = hi + (long long)c * npt, *Lo = lo + (long long)c * npt;
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  float vsum = 0.f, vcmp = 0.f, w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (active) {
+    const int lc = nconf_list == 1 ? 0 : c;
+    const int n = min(count[(long long)lc * npt + o], cap);
+    const int *L = idx + ((long long)lc * npt + o) * cap;
+    const float4 hi_o = H[o], lo_o = Lo[o];
+    for (int t = sub; t < n; t += MX_LJ_NP) {
+      const int j = L[t];
+      const float4 hj = H[j], lj = Lo[j];
+      // j - o, as the reference orients it
+      const float dx = dmin(hj.x, lj.x, hi_o.x, lo_o.x) * box.x;
+      const float dy = dmin(hj.y, lj.y, hi_o.y, lo_o.y) * box.y;
+      const float dz = dmin(hj.z, lj.z, hi_o.z, lo_o.z) * box.z;
+      const float drsq = dx * dx + dy * dy + dz * dz;
+      if (drsq < rcutsq) {
+        const float onr2 = __fdividef(1.0f, drsq);
+        const float sr2 = sigsq * onr2;
+        const float sr6 = sr2 * sr2 * sr2;
+        const float fij = sr6 * (sr6 - 0.5f) * onr2;
+        const float fx = fij * dx, fy = fij * dy, fz = fij * dz;
+        kadd(sx, cx, fx);
+        kadd(sy, cy, fy);
+        kadd(sz, cz, fz);
+        kadd(vsum, vcmp, sr6 * (sr6 - 1.0f));
+        w[0] -= dx * fx; w[1] -= dy * fx; w[2] -= dz * fx;
+        w[3] -= dx * fy; w[4] -= dy * fy; w[5] -= dz * fy;
+        w[6] -= dx * fz; w[7] -= dy * fz; w[8] -= dz * fz;
+      }
+    }
+  }
+  const double fx = group_sum_d<MX_LJ_NP>((double)sx - (double)cx);
+  const double fy = group_sum_d<MX_LJ_NP>((double)sy - (double)cy);
+  const double fz = group_sum_d<MX_LJ_NP>((double)sz - (double)cz);
+  if (active && sub == 0) {
+    double *F = out + (long long)c * na * 3 + 9LL * o;
+    F[0] += dscale * fx;
+    F[1] += dscale * fy;
+    F[2] += dscale * fz;
+  }
+  double vals[10];
+  vals[0] = 0.5 * ((double)vsum - (double)vcmp);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) vals[1 + k] = 0.5 * w[k];
+  block_sum_atomic<10>(vals, sh, acc);
+}
+
+// ---- reciprocal space (kwald, ewald_cubic.f90:235-533), FP32 ----
+constexpr int MSK_CHUNK = 32;
+constexpr int MSK_G = 8;
+constexpr int MSK_T = 128;
+constexpr int MF_T = 64;
+constexpr int SIGN32 = (int)0x80000000u;
+
+GB_D float flipf(float v, int mask) { return __int_as_float(__float_as_int(v) ^ mask); }
+
+// FP64 recurrence (ewald_cubic.f90:254-286) rounded to FP32
+__global__ void k_recip_tables_mx(const double *rs, const double *q, int na, int B, int kmax, float2 *tab) {
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= 3LL * na * B) return;
+  const int ax = (int)(w % 3);
+  const int s = (int)((w / 3) % na);
+  const double arg = 2.0 * acos(-1.0) * rs[w];
+  double sn, cs;
+  sincos(arg, &sn, &cs);
+  double pr = ax == 0 ? q[s] : 1.0, pi = 0.0;
+  float2 *t = tab + w * (kmax + 1);
+  t[0] = make_float2((float)pr, 0.f);
+  for (int k = 1; k <= kmax; ++k) {
+    const double nr = cs * pr - sn * pi;
+    const double ni = sn * pr + cs * pi;
+    pr = nr;
+    pi = ni;
+    t[k] = make_float2((float)pr, (float)pi);
+  }
+}
+
+__global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na, int kmax, int ngrp,
+                                                       const int4 *grp, int nkp, int nchunk, float4 *sk_part) {
+  extern __shared__ float2 stf[];  // [MSK_CHUNK][3][K1]
+  const int K1 = kmax + 1, K3 = 3 * K1;
+  const int c = blockIdx.z, chunk = blockIdx.y;
+  const int s0 = chunk * MSK_CHUNK, ns = min(MSK_CHUNK, na - s0);
+  const float2 *src = tab + ((long long)c * na + s0) * K3;
+  for (int w = threadIdx.x; w < ns * K3; w += MSK_T) stf[w] = src[w];
+  __syncthreads();
+  const int gi = blockIdx.x * MSK_T + threadIdx.x;
+  if (gi >= ngrp) return;
+  const int4 gr = __ldg(grp + gi);
+  const int kx = gr.x & 0xffff, len = gr.x >> 16, ky = gr.y, m0 = gr.z;
+  const int aky = abs(ky);
+  const int ymask = ky < 0 ? SIGN32 : 0;
+  float pr[MSK_G], pi[MSK_G], qr[MSK_G], qi[MSK_G];
+#pragma unroll
+  for (int g = 0; g < MSK_G; ++g) pr[g] = pi[g] = qr[g] = qi[g] = 0.f;
+  for (int s = 0; s < ns; ++s) {
+    const float2 *S = stf + s * K3;
+    const float2 X = S[kx], Y = S[K1 + aky];
+    const float yi = flipf(Y.y, ymask);
+    const float cr = fmaf(X.x, Y.x, -X.y * yi);
+    const float ci = fmaf(X.x, yi, X.y * Y.x);
+    const float2 *Z = S + 2 * K1 + m0;
+#pragma unroll
+    for (int g = 0; g < MSK_G; ++g) {
+      if (g < len) {
+        const float2 z = Z[g];
+        pr[g] = fmaf(cr, z.x, pr[g]);
+        pi[g] = fmaf(ci, z.x, pi[g]);
+        qr[g] = fmaf(cr, z.y, qr[g]);
+        qi[g] = fmaf(ci, z.y, qi[g]);
+      }
+    }
+  }
+  float4 *out = sk_part + ((long long)c * nchunk + chunk) * nkp + gr.w;
+#pragma unroll
+  for (int g = 0; g < MSK_G; ++g)
+    if (g < len) out[g] = make_float4(pr[g], pi[g], qr[g], qi[g]);
+}
+
+// FP64 sums of the chunk partials, energy and virial; FP32 force tables
+__global__ void __launch_bounds__(256) k_recip_weights_mx(const float4 *sk_part, int nchunk, int nkp,
+                                                          const int4 *kpair, const double *kw, double bfac,
+                                                          float4 *sk, double *acc) {
+  __shared__ double part[4][8][32];
+  __shared__ double sh[8 * 10];
+  const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
+  const int c = blockIdx.y;
+  const int k = blockIdx.x * 32 + lane;
+  double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  if (k < nkp) {
+    for (int ch = slice; ch < nchunk; ch += 8) {
+      const float4 p = sk_part[((long long)c * nchunk + ch) * nkp + k];
+      a0 += p.x;
+      a1 += p.y;
+      a2 += p.z;
+      a3 += p.w;
+    }
+  }
+  part[0][slice][lane] = a0;
+  part[1][slice][lane] = a1;
+  part[2][slice][lane] = a2;
+  part[3][slice][lane] = a3;
+  __syncthreads();
+  double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (slice == 0 && k < nkp) {
+    double Pr = 0, Pi = 0, Qr = 0, Qi = 0;
+    for (int j = 0; j < 8; ++j) {
+      Pr += part[0][j][lane];
+      Pi += part[1][j][lane];
+      Qr += part[2][j][lane];
+      Qi += part[3][j][lane];
+    }
+    const int4 kv = kpair[k];
+    const double rlat = 2.0 * acos(-1.0);
+    const double rk[3] = {rlat * kv.x, rlat * kv.y, rlat * kv.z};
+    const double rk2 = rk[0] * rk[0] + rk[1] * rk[1] + rk[2] * rk[2];
+    const double w = kw[k];
+    double et, Ar, Ai, Dr, Di;
+    if (kv.w == 1) {
+      et = 2.0 * w * (Pr * Pr + Pi * Pi + Qr * Qr + Qi * Qi);
+      Ar = 4.0 * w * Pr;
+      Ai = 4.0 * w * Pi;
+      Dr = -4.0 * w * Qi;
+      Di = 4.0 * w * Qr;
+    } else if (kv.w == 2) {
+      const double sr = Pr - Qi, si = Pi + Qr;
+      et = w * (sr * sr + si * si);
+      Ar = Dr = 2.0 * w * sr;
+      Ai = Di = 2.0 * w * si;
+    } else {
+      et = w * (Pr * Pr + Pi * Pi);
+      Ar = 2.0 * w * Pr;
+      Ai = 2.0 * w * Pi;
+      Dr = Di = 0.0;
+    }
+    const double term = 2.0 * (1.0 / rk2 + bfac);
+    vals[0] = et;
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        vals[1 + a + 3 * b] = et * (term * fabs(rk[a]) * fabs(rk[b]) - (a == b ? 1.0 : 0.0));
+    const double m = (double)kv.z;
+    float4 *o = sk + ((long long)c * nkp + k) * 2;
+    o[0] = make_float4((float)Ar, (float)-Ai, (float)Dr, (float)Di);
+    o[1] = make_float4((float)(m * Dr), (float)(m * Ai), (float)(-m * Di), (float)(m * Ar));
+  }
+  block_sum_atomic<10>(vals, sh, acc);
+}
+
+__global__ void __launch_bounds__(MF_T) k_recip_force_mx(const float2 *__restrict__ tab, int na, int kmax, int ncol,
+                                                         const KCol *__restrict__ cols, int nkp,
+                                                         const float4 *__restrict__ sk, double *g) {
+  extern __shared__ float2 stf[];  // [3][K1][MF_T]
+  const int K1 = kmax + 1, K3 = 3 * K1;
+  const int c = blockIdx.z, t = threadIdx.x;
+  const int i0 = blockIdx.x * MF_T, i = i0 + t;
+  for (int w = t; w < K3 * MF_T; w += MF_T) {
+    const int e = w / MF_T, sl = w % MF_T;
+    const int si = min(i0 + sl, na - 1);
+    stf[w] = tab[((long long)c * na + si) * K3 + e];
+  }
+  const long long kp_lo = (long long)blockIdx.y * nkp / gridDim.y;
+  const long long kp_hi = (long long)(blockIdx.y + 1) * nkp / gridDim.y;
+  auto first_col = [&](long long kp) {
+    int lo = 0, hi = ncol;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(&cols[mid].koff) < kp) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo;
+  };
+  const int col0 = first_col(kp_lo), col1 = first_col(kp_hi);
+  __syncthreads();
+  const float4 *T = sk + (long long)c * nkp * 2;
+  float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
+  for (int col = col0; col < col1; ++col) {
+    const int4 ci4 = __ldg(reinterpret_cast<const int4 *>(cols + col));
+    const int kx = ci4.x, ky = ci4.y, koff = ci4.z, mlo = ci4.w & 0xffff, mhi = ci4.w >> 16;
+    const float2 X = stf[kx * MF_T + t], Y = stf[(K1 + abs(ky)) * MF_T + t];
+    const float yi = flipf(Y.y, ky < 0 ? SIGN32 : 0);
+    const float cr = fmaf(X.x, Y.x, -X.y * yi);
+    const float ci = fmaf(X.x, yi, X.y * Y.x);
+    const float4 *Tp = T + 2LL * (koff - mlo);
+    const float2 *Z = stf + 2 * K1 * MF_T + t;
+    float ur = 0.f, ui = 0.f, vr = 0.f, vi = 0.f;
+    for (int m = mlo; m <= mhi; ++m) {
+      const float2 z = Z[m * MF_T];
+      const float4 t0 = Tp[2 * m], t1 = Tp[2 * m + 1];
+      ur = fmaf(z.x, t0.x, fmaf(z.y, t0.w, ur));
+      ui = fmaf(z.x, t0.y, fmaf(z.y, t0.z, ui));
+      vr = fmaf(z.x, t1.x, fmaf(z.y, t1.y, vr));
+      vi = fmaf(z.x, t1.z, fmaf(z.y, t1.w, vi));
+    }
+    const float ts = -fmaf(cr, ui, ci * ur);
+    kadd(sx, ex, (float)kx * ts);
+    kadd(sy, ey, (float)ky * ts);
+    kadd(sz, ez, -fmaf(cr, vi, ci * vr));
+  }
+  if (i < na && col1 > col0) {
+    const double rlat = 2.0 * acos(-1.0);
+    double *G = g + ((long long)c * na + i) * 3;
+    atomicAdd(G, rlat * ((double)sx - (double)ex));
+    atomicAdd(G + 1, rlat * ((double)sy - (double)ey));
+    atomicAdd(G + 2, rlat * ((double)sz - (double)ez));
+  }
+}
+
+inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+int sm_count_mx() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 1;
+  return n;
+}
+
+}  // namespace
+
+void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, const float *q, int na, int B,
+                          const PairList &pl, double alpha, double *g, double *acc) {
+  dim3 grid(nblk((long long)na * MX_NP, MX_T), B);
+  k_ewald_real_mx<<<grid, MX_T, 0, s>>>(hi, lo, q, na, pl.count, pl.idx, pl.cap, (float)alpha, g, acc);
+}
+
+void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
+                  double sigsq, double rcutsq, const double *box, double dscale, double *out, double *acc) {
+  const int npt = na / 3;
+  dim3 grid(nblk((long long)npt * MX_LJ_NP, MX_T), B);
+  const float3 bx = make_float3((float)box[0], (float)box[1], (float)box[2]);
+  k_lj_mx<<<grid, MX_T, 0, s>>>(hi, lo, na, npt, pl.nconf, pl.count, pl.idx, pl.cap, (float)sigsq, (float)rcutsq,
+                                bx, dscale, out, acc);
+}
+
+size_t recip_sk_smem_mx(int kmax) { return sizeof(float2) * MSK_CHUNK * 3 * (kmax + 1); }
+size_t recip_force_smem_mx(int kmax) { return sizeof(float2) * 3 * (kmax + 1) * MF_T; }
+
+// partial sums need nconf * nchunk * nkp float4 (half of the FP64 layout)
+void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B) {
+  if (c->nkp == 0) return;
+  const int kmax = c->P.kmax;
+  const long long nw = 3LL * c->na * B;
+  float2 *tab = reinterpret_cast<float2 *>(c->ktab);
+  k_recip_tables_mx<<<nblk(nw, 128), 128, 0, s>>>(rs, q, c->na, B, kmax, tab);
+  const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
+  dim3 grid(nblk(c->ngrp, MSK_T), nchunk, B);
+  k_recip_sk_mx<<<grid, MSK_T, recip_sk_smem_mx(kmax), s>>>(tab, c->na, kmax, c->ngrp, c->kgrp, c->nkp, nchunk,
+                                                            reinterpret_cast<float4 *>(c->sk_part));
+}
+
+void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc) {
+  if (c->nkp == 0) return;
+  const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
+  const double bfac = 0.25 / (c->P.walpha * c->P.walpha);
+  dim3 grid(nblk(c->nkp, 32), B);
+  k_recip_weights_mx<<<grid, 256, 0, s>>>(reinterpret_cast<const float4 *>(c->sk_part), nchunk, c->nkp, c->kpair,
+                                          c->kw, bfac, reinterpret_cast<float4 *>(c->sk), acc);
+}
+
+void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
+  if (c->nkp == 0) return;
+  const int kmax = c->P.kmax;
+  const unsigned bx = nblk(c->na, MF_T);
+  const long long want = 8LL * sm_count_mx();
+  int nseg = (int)((want + (long long)bx * B - 1) / ((long long)bx * B));
+  nseg = std::max(1, std::min(16, std::min(nseg, c->ncol)));
+  dim3 grid(bx, nseg, B);
+  k_recip_force_mx<<<grid, MF_T, recip_force_smem_mx(kmax), s>>>(reinterpret_cast<const float2 *>(c->ktab), c->na,
+                                                                 kmax, c->ncol, c->kcol, c->nkp,
+                                                                 reinterpret_cast<const float4 *>(c->sk), g);
+}
+
+void recip_set_attributes_mx() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_recip_sk_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  done = true;
+}

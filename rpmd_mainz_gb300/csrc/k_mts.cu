@@ -202,6 +202,204 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_fused(MtsArgs a) {
   }
 }
 
+// Mixed precision (same structure as k_mts_fused): the normal-mode state, the
+// free ring-polymer rotation (its coefficients) and the kicks stay FP64; every
+// transform runs in FP32 on deviations -- the centroid mode is the FP64 bead
+// sum, the other modes come from an FP32 transform of x_j - x_0 -- and the
+// intramolecular forces run in FP32 on positions taken relative to the
+// molecule's oxygen centroid, so that FP32 holds them to ~1e-7 bohr.
+template <int NB>
+__global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
+  using C = MtsCfg<NB>;
+  extern __shared__ double sm[];
+  const int T = blockDim.x;
+  const int nrow = (T + 8) / 9 * 9;
+  const int nf = (3 * nrow * C::LD + 1) & ~1;      // float slots, rounded to whole doubles
+  float *s_dev = reinterpret_cast<float *>(sm);    // [nrow][LD] x_j - (oxygen centroid)
+  float *s_f2 = s_dev + nrow * C::LD;              // [nrow][LD] intramolecular forces
+  float *s_dvf = s_f2 + nrow * C::LD;              // [nrow][LD] dvdr for the estimator
+  double *s_cen = sm + nf / 2;                     // [nrow] row centroids
+  double *s_mono = s_cen + nrow;                   // [12*NB]
+  double *s_red = s_mono + 12 * NB;                // [32 warps][18]
+  float *s_tw = reinterpret_cast<float *>(s_red + 32 * 18);  // [2*NB] cos, sin
+  float *s_twf = s_tw + 2 * NB;                    // scaled by sqrt(1/nb) / 2
+  float *s_twi = s_twf + 2 * NB;                   // scaled by sqrt(1/nb)
+  const int t = threadIdx.x;
+  const double sc = sqrt(1.0 / (double)NB);
+  for (int i = t; i < 12 * NB; i += T) s_mono[i] = a.monod[i];
+  for (int i = t; i < 2 * NB; i += T) {
+    const double w = a.tw[i];
+    s_tw[i] = (float)w;
+    s_twf[i] = (float)((0.5 * sc) * w);
+    s_twi[i] = (float)(sc * w);
+  }
+  const int mpb = a.mpb;
+  const int m0 = blockIdx.x * mpb;
+  const int ml = t / 9, lr = t % 9;
+  const int m = m0 + ml;
+  const bool valid = ml < mpb && m < a.nm;
+  const int mc = valid ? m : a.nm - 1;
+  const long long S = 3LL * a.na;
+  const long long row = 9LL * mc + lr;
+  const int ic = lr / 3;
+  const int xyz = lr % 3;
+  const int orow = ml * 9 + xyz;                   // oxygen row of the same coordinate
+  float *dv_row = s_dvf + t * C::LD;
+
+  double pm[NB], xm[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    const double dv = a.dvdr[row + S * j];
+    const double pj = a.p[row + S * j] - a.halfdt * dv;
+    pm[j] = pj - a.halfdtsmall * a.dvdr2[row + S * j];
+    xm[j] = a.r[row + S * j];
+    dv_row[j] = (float)dv;
+  }
+  __syncthreads();
+  // forward transforms: mode 0 = sc * (FP64 bead sum), modes k >= 1 from the
+  // FP32 transform of the deviations from bead 0
+  auto to_modes = [&](double (&v)[NB]) {
+    double sum = 0.0;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) sum += v[j];
+    const double v0 = v[0];
+    float d[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) d[j] = (float)(v[j] - v0);
+    gb_r2hc_s<NB, float>([&](int j) { return d[j]; },
+                         [&](int k, float val) {
+                           if (k > 0) v[k] = (double)val;
+                         },
+                         s_tw, s_twf);
+    v[0] = sc * sum;
+  };
+  to_modes(pm);
+  to_modes(xm);
+
+  double e_last = 0.0, q1 = 0.0, q2 = 0.0;
+  float vir[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float off = 0.f;  // this row's centroid minus its oxygen's centroid
+  for (int im = 1; im <= a.mts; ++im) {
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {  // free ring-polymer rotation, FP64 (evolve_pi.f90:109-125)
+      const double *mo = s_mono + ic + 12 * k;
+      const double pp = pm[k] * mo[0] + xm[k] * mo[3];
+      xm[k] = pm[k] * mo[6] + xm[k] * mo[9];
+      pm[k] = pp;
+    }
+    const double cen = sc * xm[0];
+    s_cen[t] = cen;
+    __syncthreads();
+    off = (float)(cen - s_cen[orow]);
+    {  // bead positions relative to the oxygen centroid (evolve_pi.f90:141-145)
+      float xf[NB];
+#pragma unroll
+      for (int k = 0; k < NB; ++k) xf[k] = k ? (float)xm[k] : 0.f;
+      float *dst = s_dev + t * C::LD;
+      gb_hc2r_s<NB, float>([&](int j) { return xf[j]; }, [&](int k, float v) { dst[k] = off + v; }, s_tw, s_twi);
+    }
+    __syncthreads();
+    double e_sub = 0.0;
+    for (int idx = t; idx < mpb * NB; idx += T) {
+      const int mm = idx / NB, j = idx % NB;
+      const bool w = m0 + mm < a.nm;
+      float xr[9], fm[9], vm[9];
+#pragma unroll
+      for (int d = 0; d < 9; ++d) xr[d] = s_dev[(mm * 9 + d) * C::LD + j];
+      const float e = intra_molecule_t<float>(a.model, xr, fm, vm, a.ip);
+#pragma unroll
+      for (int d = 0; d < 9; ++d) s_f2[(mm * 9 + d) * C::LD + j] = fm[d];
+      if (w) {
+        e_sub += (double)e;
+#pragma unroll
+        for (int d = 0; d < 9; ++d) vir[d] += vm[d];
+      }
+    }
+    if (im == a.mts) e_last = e_sub;
+    __syncthreads();
+    {
+      const float *dev_row = s_dev + t * C::LD;
+      const float *f2_row = s_f2 + t * C::LD;
+      if (valid) {  // virial_ke partial sums (kinetic.f90:23-40) about the bead centroid
+        float a1 = 0.f, a2 = 0.f;
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+          const float dr = dev_row[j] - off;
+          a1 += dr * dv_row[j];
+          a2 += dr * f2_row[j];
+        }
+        q1 += (double)a1;
+        q2 += (double)a2;
+      }
+      if (im != a.mts) {  // FT(dvdr2) and p -= dtsmall dvdr2 (evolve_pi.f90:156-159)
+        const double dts = a.dtsmall;
+        gb_r2hc_s<NB, float>([&](int j) { return f2_row[j]; },
+                             [&](int k, float v) { pm[k] = pm[k] - dts * (double)v; }, s_tw, s_twf);
+      }
+    }
+    if (im != a.mts) __syncthreads();
+  }
+  {
+    // back to beads: p = HC2R(p); r = rst; p -= halfdtsmall dvdr2 (evolve_pi.f90:222-228)
+    const float *dev_row = s_dev + t * C::LD;
+    const float *f2_row = s_f2 + t * C::LD;
+    const double hds = a.halfdtsmall;
+    const double pc = sc * pm[0], cen = sc * xm[0];
+    float pf[NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) pf[k] = k ? (float)pm[k] : 0.f;
+    double *gp = a.p + row;
+    gb_hc2r_s<NB, float>([&](int j) { return pf[j]; },
+                         [&](int k, float v) {
+                           if (valid) gp[S * k] = pc + (double)v - hds * (double)f2_row[k];
+                         },
+                         s_tw, s_twi);
+    if (valid) {
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        a.r[row + S * j] = cen + (double)(dev_row[j] - off);
+        a.rnm[row + S * j] = xm[j];
+        a.dvdr2[row + S * j] = (double)f2_row[j];
+      }
+    }
+  }
+  double red[18];
+  red[0] = e_last;
+#pragma unroll
+  for (int d = 0; d < 9; ++d) red[1 + d] = (double)vir[d];
+  red[10] = q1;
+  red[11] = q2;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    red[12 + d] = d == xyz ? q1 : 0.0;
+    red[15 + d] = d == xyz ? q2 : 0.0;
+  }
+  const int lane = t & 31, warp = t >> 5, nw = (T + 31) / 32;
+#pragma unroll
+  for (int i = 0; i < 18; ++i) {
+    double v = warp_sum(red[i]);
+    if (lane == 0) s_red[warp * 18 + i] = v;
+  }
+  __syncthreads();
+  if (t < 18) {
+    double s2 = 0.0;
+    for (int w = 0; w < nw; ++w) s2 += s_red[w * 18 + t];
+    if (s2 != 0.0) {
+      if (t < 10) atomicAdd(a.acc_int + t, s2);
+      else if (t < 12) atomicAdd(a.acc_ke + (t - 10), s2);
+      else atomicAdd(a.acc_ke + 2 + (t - 12), s2);
+    }
+  }
+}
+
+template <int NB>
+size_t mts_smem_mixed(int T) {
+  using C = MtsCfg<NB>;
+  const int nrow = (T + 8) / 9 * 9;
+  const int nf = (3 * nrow * C::LD + 1) & ~1;
+  return sizeof(float) * nf + sizeof(double) * (nrow + 12 * NB + 32 * 18) + sizeof(float) * 6 * NB;
+}
+
 template <int NB>
 size_t mts_smem(int T) {
   using C = MtsCfg<NB>;
@@ -210,11 +408,13 @@ size_t mts_smem(int T) {
 }
 
 template <int NB>
-void launch_nb(cudaStream_t s, MtsArgs a) {
+void launch_nb(cudaStream_t s, MtsArgs a, bool mixed) {
   using C = MtsCfg<NB>;
   static bool attr = false;
   if (!attr) {  // the largest request of any launch
     cudaFuncSetAttribute(k_mts_fused<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mts_smem<NB>(C::T_MAX));
+    cudaFuncSetAttribute(k_mts_mixed<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)mts_smem_mixed<NB>(C::T_MAX));
     attr = true;
   }
   int dev = 0, nsm = 1;
@@ -224,7 +424,8 @@ void launch_nb(cudaStream_t s, MtsArgs a) {
   a.mpb = std::max(1, std::min(C::MPB_MAX, (a.nm + nsm - 1) / std::max(nsm, 1)));
   const int T = (9 * a.mpb + 31) / 32 * 32;
   const unsigned grid = (unsigned)((a.nm + a.mpb - 1) / a.mpb);
-  k_mts_fused<NB><<<grid, T, mts_smem<NB>(T), s>>>(a);
+  if (mixed) k_mts_mixed<NB><<<grid, T, mts_smem_mixed<NB>(T), s>>>(a);
+  else k_mts_fused<NB><<<grid, T, mts_smem<NB>(T), s>>>(a);
 }
 
 int intra_model_of(const gb_params &P) {
@@ -262,13 +463,14 @@ void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used) {
   a.ip.apot = c->P.apot;
   a.ip.bpot = c->P.bpot;
   a.ip.alp = c->P.alp;
+  const bool mixed = c->P.precision == GB_PREC_MIXED;
   switch (nb) {
-    case 2: launch_nb<2>(s, a); break;
-    case 4: launch_nb<4>(s, a); break;
-    case 8: launch_nb<8>(s, a); break;
-    case 16: launch_nb<16>(s, a); break;
-    case 32: launch_nb<32>(s, a); break;
-    case 64: launch_nb<64>(s, a); break;
+    case 2: launch_nb<2>(s, a, mixed); break;
+    case 4: launch_nb<4>(s, a, mixed); break;
+    case 8: launch_nb<8>(s, a, mixed); break;
+    case 16: launch_nb<16>(s, a, mixed); break;
+    case 32: launch_nb<32>(s, a, mixed); break;
+    case 64: launch_nb<64>(s, a, mixed); break;
   }
   *used = 1;
 }

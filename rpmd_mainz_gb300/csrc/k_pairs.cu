@@ -8,11 +8,12 @@
 // whose FP64 test, rounded exactly like the reference's
 // dx*dx + dy*dy + dz*dz < rcut*rcut, decides the pairs inside a narrow band
 // around the cut-off.  Each pair is stored once, in the list of i when
-// (i < j) == ((i + j) odd), which halves the lists and balances their lengths.
+// (i < j) == ((i + j) odd), which halves the lists and balances their lengths;
+// full lists (PairGeom::full, for the FP32 kernels) store it in both.
 //
-// Pair forces.  One thread per (configuration, point) walks its list, keeps the
-// point's own force in registers and scatters the partner's force with FP64
-// atomics; energy and virial are reduced per block and added to an
+// Pair forces (FP64).  A few lanes per (configuration, point) walk its half
+// list, keep the point's own force in registers and scatter the partner's force
+// with FP64 atomics; energy and virial are reduced per block and added to an
 // accumulator slot.
 #include "gb_common.cuh"
 #include "gb_kernels.h"
@@ -21,20 +22,26 @@ namespace {
 
 constexpr int LB_T = 128;
 
-__global__ void k_frac32(PairGeom g, int nconf, float4 *frac) {
+// wrapped fractional coordinates u in [0, 1) as FP32 (frac); with lo, also the
+// remainder u - frac as a second FP32, so that frac + lo carries u to ~1e-14
+__global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nconf * g.npt) return;
   int c = (int)(t / g.npt), i = (int)(t % g.npt);
   const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
-  float f[3];
+  float f[3], e[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     double u = g.unit ? x[d] : x[d] * g.onbox[d];
     u -= floor(u);
-    float uf = (float)u;
+    const float uf = (float)u;
+    // remainder against the rounded value, before 1.0f wraps to 0: hi + lo is
+    // then u or u - 1, both the same point of the periodic box
+    e[d] = (float)(u - (double)uf);
     f[d] = uf >= 1.0f ? 0.0f : uf;
   }
   frac[t] = make_float4(f[0], f[1], f[2], 0.0f);
+  if (lo) lo[t] = make_float4(e[0], e[1], e[2], 0.0f);
 }
 
 // exact FP64 minimum-image test, rounded as the reference rounds it
@@ -89,7 +96,7 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
       for (int jj = 0; jj < jmax; ++jj) {
         const int j = jt + jj;
         if (j == i) continue;
-        if ((i < j) != (((i + j) & 1) != 0)) continue;
+        if (!g.full && (i < j) != (((i + j) & 1) != 0)) continue;
         if (g.excl_mol && (i / 3) == (j / 3)) continue;
         const float4 fj = tile[jj];
         float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
@@ -494,9 +501,9 @@ double list_total(cudaStream_t s, const PairList &pl) {
   return (double)h;
 }
 
-void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac) {
+void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo) {
   long long n = (long long)nconf * g.npt;
-  k_frac32<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac);
+  k_frac32<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo);
 }
 
 // FP32 thresholds around rcutsq: below lo accept, at or above hi reject,

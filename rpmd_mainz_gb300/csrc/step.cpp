@@ -164,10 +164,11 @@ int list_cap(int npt, double rc, double vol) {
 // cut-off + skin is rebuilt on the device only when a point has moved by more
 // than skin/2 since the last rebuild, then filtered into the exact list.
 // Returns the number of launches through *nl.
-int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut, double vol, int *nl) {
+int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut, double vol, int *nl,
+              float4 *lo = nullptr) {
   int st = ensure_list(c, nconf, g.npt, list_cap(g.npt, cut, vol));
   if (st) return st;
-  launch_frac32(c->stream, g, nconf, c->rs32);
+  launch_frac32(c->stream, g, nconf, c->rs32, lo);
   if (c->list_skin <= 0.0) {
     launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
     *nl = 2;
@@ -176,6 +177,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   SkinList &S = c->sl[which];
   const double skin = c->list_skin * cut, scut = cut + skin;
   bool same = S.valid && S.nconf == nconf && S.npt == g.npt && S.unit == g.unit && S.excl == g.excl_mol &&
+              S.full == g.full &&
               S.pstride == g.pstride && S.cstride == g.cstride && S.cutsq == g.rcutsq && S.skin == skin;
   for (int d = 0; d < 3; ++d) same = same && S.box[d] == g.box[d];
   if (!same) {
@@ -232,6 +234,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   S.npt = g.npt;
   S.unit = g.unit;
   S.excl = g.excl_mol;
+  S.full = g.full;
   S.pstride = g.pstride;
   S.cstride = g.cstride;
   S.cutsq = g.rcutsq;
@@ -265,26 +268,45 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   g.onbox[0] = g.onbox[1] = g.onbox[2] = 1.0;
   g.rcutsq = c->P.wrcut * c->P.wrcut;
   g.excl_mol = 0;
+  const bool mixed = c->P.precision == GB_PREC_MIXED;
+  g.full = mixed ? 1 : 0;  // the FP32 kernel walks full lists
   int nl = 0;
   prof_begin(c, PR_LIST);
-  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, 1.0, &nl);
+  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, 1.0, &nl, mixed ? c->lo32 : nullptr);
   if (st) return st;
   prof_end(c, PR_LIST, (double)na * B);
   c->launches += nl;
-  const double npairs = c->prof ? list_total(c->stream, c->pl) : 0.0;
-  prof_begin(c, PR_EW_REAL);
-  launch_ewald_real(c->stream, c->rs, c->z, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
-  prof_end(c, PR_EW_REAL, npairs);
+  // in-cut pairs (each once)
+  const double npairs = c->prof ? list_total(c->stream, c->pl) * (mixed ? 0.5 : 1.0) : 0.0;
   const double ksites = (double)c->nk * na * B;
-  prof_begin(c, PR_RECIP_SK);
-  launch_recip_sk(c->stream, c, c->rs, c->z, B);
-  prof_end(c, PR_RECIP_SK, ksites);
-  prof_begin(c, PR_RECIP_W);
-  launch_recip_weights(c->stream, c, B, slot(c, s));
-  prof_end(c, PR_RECIP_W, (double)c->nkp * B);
-  prof_begin(c, PR_RECIP_F);
-  launch_recip_force(c->stream, c, c->rs, c->z, B, c->g);
-  prof_end(c, PR_RECIP_F, ksites);
+  if (mixed) {
+    recip_set_attributes_mx();
+    prof_begin(c, PR_EW_REAL);
+    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, c->z32, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
+    prof_end(c, PR_EW_REAL, npairs);
+    prof_begin(c, PR_RECIP_SK);
+    launch_recip_sk_mx(c->stream, c, c->rs, c->z, B);
+    prof_end(c, PR_RECIP_SK, ksites);
+    prof_begin(c, PR_RECIP_W);
+    launch_recip_weights_mx(c->stream, c, B, slot(c, s));
+    prof_end(c, PR_RECIP_W, (double)c->nkp * B);
+    prof_begin(c, PR_RECIP_F);
+    launch_recip_force_mx(c->stream, c, B, c->g);
+    prof_end(c, PR_RECIP_F, ksites);
+  } else {
+    prof_begin(c, PR_EW_REAL);
+    launch_ewald_real(c->stream, c->rs, c->z, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
+    prof_end(c, PR_EW_REAL, npairs);
+    prof_begin(c, PR_RECIP_SK);
+    launch_recip_sk(c->stream, c, c->rs, c->z, B);
+    prof_end(c, PR_RECIP_SK, ksites);
+    prof_begin(c, PR_RECIP_W);
+    launch_recip_weights(c->stream, c, B, slot(c, s));
+    prof_end(c, PR_RECIP_W, (double)c->nkp * B);
+    prof_begin(c, PR_RECIP_F);
+    launch_recip_force(c->stream, c, c->rs, c->z, B, c->g);
+    prof_end(c, PR_RECIP_F, ksites);
+  }
   prof_begin(c, PR_MSITE);
   launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, onboxl * onboxl, sign, accumulate);
   prof_end(c, PR_MSITE, (double)na * B);
@@ -324,16 +346,29 @@ int term_lj(gb_context *c, const double *r, int B, double *out, int accumulate, 
     nconf = B;
     lcut = c->P.rcut;
   }
+  const bool mixed = c->P.precision == GB_PREC_MIXED;
+  g.full = mixed ? 1 : 0;
   int nl = 0;
   prof_begin(c, PR_LIST);
   int st = make_list(c, LIST_LJ, g, nconf, lcut, vol, &nl);
   if (st) return st;
   prof_end(c, PR_LIST, (double)nm * nconf);
   c->launches += nl;
-  const double npairs = c->prof ? list_total(c->stream, c->pl) * (nconf == 1 ? B : 1) : 0.0;
+  const double npairs =
+      c->prof ? list_total(c->stream, c->pl) * (nconf == 1 ? B : 1) * (mixed ? 0.5 : 1.0) : 0.0;
   prof_begin(c, PR_LJ);
-  launch_lj(c->stream, r, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut, c->box,
-            48.0 * c->P.oo_eps, out, slot(c, s));
+  if (mixed) {
+    PairGeom go = g;  // the bead oxygens of every configuration, as hi/lo FP32
+    go.pos = r;
+    go.cstride = 3LL * na;
+    launch_frac32(c->stream, go, B, c->hi32, c->olo32);
+    launch_lj_mx(c->stream, c->hi32, c->olo32, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut,
+                 c->box, 48.0 * c->P.oo_eps, out, slot(c, s));
+    c->launches += 1;
+  } else {
+    launch_lj(c->stream, r, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut, c->box,
+              48.0 * c->P.oo_eps, out, slot(c, s));
+  }
   prof_end(c, PR_LJ, npairs);
   c->launches += 1;
   return GB_OK;
