@@ -249,6 +249,11 @@ int gbrpmd_ctx_region_times(gb_context *ctx, double *ms, double *units, int *cou
 int gbrpmd_ctx_set_list_skin(gb_context *ctx, double fraction);
 /* rebuilds of the three skin lists since the context was created (synchronises) */
 int gbrpmd_ctx_list_rebuilds(gb_context *ctx, unsigned *counts3);
+/* CUDA-graph replay of gbrpmd_ctx_evolve / gbrpmd_evolve_pi steps (no counterpart
+   in the reference): on by default (environment GBRPMD_GRAPHS=0 turns it off);
+   the second step with unchanged parameters, dt, beta and box is captured and
+   later steps replay it.  Results do not depend on the setting. */
+int gbrpmd_ctx_set_graphs(gb_context *ctx, int on);
 /* the md_eq step loop (md_eq.f90:182-323) on the device state: nsteps
    evolve_pi steps, each followed by the Andersen test ran2(irun) < thresh
    that resamples all momenta (md_eq.f90:311-315) when therm is AND.

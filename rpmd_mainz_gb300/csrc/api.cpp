@@ -73,9 +73,6 @@ int set_charges(gb_context *c, const double *z) {
   double qq = 0.0;
   for (int i = 0; i < c->na; ++i) qq = qq + z[i] * z[i];
   c->qq = qq;
-  c->h_z32.resize(c->na);
-  for (int i = 0; i < c->na; ++i) c->h_z32[i] = (float)z[i];
-  CK(cudaMemcpyAsync(c->z32, c->h_z32.data(), sizeof(float) * c->na, cudaMemcpyHostToDevice, c->stream));
   return upload(c, c->z, z, (size_t)c->na);
 }
 
@@ -133,6 +130,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
   const char *gen = std::getenv("GBRPMD_GENERIC_MTS");
   c->generic_mts = gen && gen[0] == '1';
   if (const char *sk = std::getenv("GBRPMD_LIST_SKIN")) c->list_skin = std::max(0.0, std::atof(sk));
+  if (const char *gr = std::getenv("GBRPMD_GRAPHS")) c->use_graphs = gr[0] != '0';
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   const size_t N = 3 * (size_t)na * nb, S = 3 * (size_t)na;
   if ((st = dalloc(c, &c->p, N)) || (st = dalloc(c, &c->r, N)) || (st = dalloc(c, &c->dvdr, N)) ||
@@ -143,7 +141,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
       (st = dalloc(c, &c->fb2, N)) || (st = dalloc(c, &c->g, N)) || (st = dalloc(c, &c->rs, N)) ||
       (st = dalloc(c, &c->rs32, (size_t)na * nb)) || (st = dalloc(c, &c->lo32, (size_t)na * nb)) ||
       (st = dalloc(c, &c->hi32, (size_t)na * nb / 3)) || (st = dalloc(c, &c->olo32, (size_t)na * nb / 3)) ||
-      (st = dalloc(c, &c->z32, (size_t)na)) || (st = dalloc(c, &c->rc, S)) ||
+      (st = dalloc(c, &c->rc, S)) ||
       (st = dalloc(c, &c->monod, 12 * (size_t)nb)) ||
       (st = dalloc(c, &c->acc, (size_t)ACC_NSLOT * ACC_STRIDE)) || (st = dalloc(c, &c->status, 1)))
     return st;
@@ -159,6 +157,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
 
 void ctx_free(gb_context *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
+  dev_graph_reset(c);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   c->ev_pool.clear();
   if (c->d_count) cudaFree(c->d_count);
@@ -263,7 +262,7 @@ int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj, 
   if (c->monod_dt > 0.0) {  // masses may have changed: rebuild the monodromy table
     c->monod_dt = -1.0;
   }
-  if ((st = dev_evolve_pi(c, *dt, *beta))) return st;
+  if ((st = dev_step(c, *dt, *beta))) return st;
   if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
       (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N)))
     return st;
@@ -347,7 +346,7 @@ int gbrpmd_ctx_full_forces(gb_context *c, double *v, double *vew, double *voo, d
 int gbrpmd_ctx_evolve(gb_context *c, int nsteps, double dt, double beta) {
   c->P = g_params;
   for (int s = 0; s < nsteps; ++s) {
-    int st = dev_evolve_pi(c, dt, beta);
+    int st = dev_step(c, dt, beta);
     if (st) return st;
   }
   return GB_OK;
@@ -374,6 +373,7 @@ void *gbrpmd_ctx_stream(gb_context *c) { return (void *)c->stream; }
 
 int gbrpmd_ctx_set_profiling(gb_context *c, int on) {
   CK(cudaStreamSynchronize(c->stream));
+  dev_graph_reset(c);
   c->prof = on;
   c->marks.clear();
   c->ev_next = 0;
@@ -385,6 +385,15 @@ int gbrpmd_ctx_set_list_skin(gb_context *c, double fraction) {
   if (!(fraction >= 0.0) || fraction > 1.0) return ctx_set_error(GB_E_ARG, "list skin fraction must be in [0, 1]");
   c->list_skin = fraction;
   for (SkinList &L : c->sl) L.valid = false;
+  dev_graph_reset(c);
+  return GB_OK;
+}
+
+int gbrpmd_ctx_set_graphs(gb_context *c, int on) {
+  if (!c) return ctx_set_error(GB_E_ARG, "null context");
+  CK(cudaStreamSynchronize(c->stream));
+  dev_graph_reset(c);
+  c->use_graphs = on ? 1 : 0;
   return GB_OK;
 }
 

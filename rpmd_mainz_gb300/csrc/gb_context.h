@@ -72,8 +72,6 @@ struct gb_context {
   float4 *lo32 = nullptr;  // their FP32 remainders (mixed precision) [nb][na]
   float4 *hi32 = nullptr;  // bead oxygen coordinates for the FP32 LJ kernel [nb][nm]
   float4 *olo32 = nullptr; // and their remainders [nb][nm]
-  float *z32 = nullptr;    // charges in FP32 [na]
-  std::vector<float> h_z32;
   double *rc = nullptr;    // centroid scratch [na][3]
   PairList pl;             // exact pair list of the current term (re-sized on demand)
   size_t pl_idx_bytes = 0, pl_cnt_bytes = 0;
@@ -111,6 +109,19 @@ struct gb_context {
 
   int64_t launches = 0;
   std::vector<void *> allocs;
+
+  // the evolve step as a CUDA graph (dev_step): captured on the second step
+  // with an unchanged key, replayed while the key holds
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    bool valid = false;
+    int seen = 0;            // consecutive plain steps run with this key
+    double dt = 0, beta = 0, box[3] = {0, 0, 0};
+    gb_params P{};
+    int64_t launches = 0;    // kernels per replay
+    EnergyPlan plan;
+  } graph;
+  int use_graphs = 1;        // GBRPMD_GRAPHS=0 turns replay off
 
   // optional per-region CUDA-event timing (gbrpmd_ctx_set_profiling)
   int prof = 0;
@@ -153,5 +164,8 @@ int ctx_check_cuda(cudaError_t e, const char *what);
 int dev_prepare(gb_context *c, double dt, double beta);  // twiddles, monodromy, k lists
 int dev_full_forces(gb_context *c);                      // dvdr, dvdr2 from r
 int dev_evolve_pi(gb_context *c, double dt, double beta);
+// one evolve_pi step, replayed from a captured CUDA graph when it can be
+int dev_step(gb_context *c, double dt, double beta);
+void dev_graph_reset(gb_context *c);
 int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt);  // drop-in `forces`
 int dev_collect(gb_context *c, int mode, double dt, double beta);  // sync, read accumulators

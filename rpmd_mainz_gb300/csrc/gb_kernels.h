@@ -31,7 +31,10 @@ struct PairGeom {
 };
 
 // ---- pair lists (k_pairs.cu) ----
-void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo = nullptr);
+// wrapped fractional coordinates; optional remainders lo and per-point values
+// q (stored in frac.w)
+void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo = nullptr,
+                   const double *q = nullptr);
 // every pair within g.rcutsq; with a gate word, only when *gate != 0 (counts
 // are then zeroed on the device, so the decision needs no host round trip)
 void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
@@ -58,8 +61,9 @@ void launch_recip_weights(cudaStream_t s, gb_context *c, int B, double *acc);
 void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B,
                         double *g);
 // ---- mixed precision (k_mixed.cu): FP32 arithmetic, full lists, hi/lo positions ----
-void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, const float *q, int na, int B,
-                          const PairList &pl, double alpha, double *g, double *acc);
+// hi.w carries the site charge (launch_frac32 with q)
+void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
+                          double alpha, double *g, double *acc);
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
                   double sigsq, double rcutsq, const double *box, double dscale, double *out, double *acc);
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);
@@ -98,9 +102,9 @@ void launch_copy(cudaStream_t s, double *dst, const double *src, long long n);
 void launch_ring_contract(cudaStream_t s, const double *rnm, double *rb, int na, int nb, int nbc,
                           const double *tw_c);
 // dvdr (bead rep) = HC2R_nb( expand(fb1) + expand(fb2) ) [+ bead-rep extras], then
-// p -= halfdt * dvdr when p != nullptr
+// p -= halfdt * dvdr when p != nullptr; mixed: the expansion dot products in FP32
 void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int nbc1,
                           const double *tw_c1, const double *fb2, int nbc2, const double *tw_c2,
                           const double *e1, const double *e2, const double *e3, double *p,
-                          double halfdt, int na, int nb, const double *tw_nb);
+                          double halfdt, int na, int nb, const double *tw_nb, bool mixed);
 void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used);

@@ -66,11 +66,14 @@ GB_D void block_sum_sym7_mx(double (&vals)[7], double *sh, double *acc) {
 }
 
 // rwald (ewald_cubic.f90:78-233) in FP32 over a full list; g += gradient
-// (single writer per site), energy and virial halved for the double count
+// (single writer per site), energy and virial halved for the double count.
+// The charge rides in hi.w.  Each lane takes every NP-th partner, four at a
+// time with their indices and positions loaded before any arithmetic, so that
+// four gathers are in flight per lane.
 __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
-                                                        const float *__restrict__ q, int na,
-                                                        const int *__restrict__ count, const int *__restrict__ idx,
-                                                        int cap, float alpha, double *g, double *acc) {
+                                                        int na, const int *__restrict__ count,
+                                                        const int *__restrict__ idx, int cap, float alpha, double *g,
+                                                        double *acc) {
   __shared__ double sh[32 * 7];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
@@ -84,13 +87,11 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
   float ev = 0.f, evc = 0.f, vxx = 0.f, vyx = 0.f, vzx = 0.f, vyy = 0.f, vzy = 0.f, vzz = 0.f;
   if (active) {
     const float4 hi_i = H[i], lo_i = Lo[i];
-    const float qi = q[i];
+    const float qi = hi_i.w;
     const int mi = i / 3;
     const int n = min(count[(long long)c * na + i], cap);
     const int *L = idx + ((long long)c * na + i) * cap;
-    for (int t = sub; t < n; t += MX_NP) {
-      const int j = L[t];
-      const float4 hj = H[j], lj = Lo[j];
+    auto pair = [&](int j, const float4 &hj, const float4 &lj) {
       const float dx = dmin(hi_i.x, lo_i.x, hj.x, lj.x);
       const float dy = dmin(hi_i.y, lo_i.y, hj.y, lj.y);
       const float dz = dmin(hi_i.z, lo_i.z, hj.z, lj.z);
@@ -103,7 +104,7 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
       if (mi == j / 3) erfc -= 1.0f;
       const float du = erfc * inv;
       const float dur = (sfac * e - du) * (inv * inv);
-      const float qij = qi * q[j];
+      const float qij = qi * hj.w;
       const float dvr = qij * dur;
       const float fx = dvr * dx, fy = dvr * dy, fz = dvr * dz;
       kadd(sx, cx, fx);
@@ -116,6 +117,20 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
       vyy += dy * fy;
       vzy += dz * fy;
       vzz += dz * fz;
+    };
+    int t = sub;
+    for (; t + 3 * MX_NP < n; t += 4 * MX_NP) {
+      const int j0 = L[t], j1 = L[t + MX_NP], j2 = L[t + 2 * MX_NP], j3 = L[t + 3 * MX_NP];
+      const float4 h0 = H[j0], h1 = H[j1], h2 = H[j2], h3 = H[j3];
+      const float4 l0 = Lo[j0], l1 = Lo[j1], l2 = Lo[j2], l3 = Lo[j3];
+      pair(j0, h0, l0);
+      pair(j1, h1, l1);
+      pair(j2, h2, l2);
+      pair(j3, h3, l3);
+    }
+    for (; t < n; t += MX_NP) {
+      const int j = L[t];
+      pair(j, H[j], Lo[j]);
     }
   }
   const double fx = group_sum_d<MX_NP>((double)sx - (double)cx);
@@ -150,9 +165,7 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
     const int n = min(count[(long long)lc * npt + o], cap);
     const int *L = idx + ((long long)lc * npt + o) * cap;
     const float4 hi_o = H[o], lo_o = Lo[o];
-    for (int t = sub; t < n; t += MX_LJ_NP) {
-      const int j = L[t];
-      const float4 hj = H[j], lj = Lo[j];
+    auto pair = [&](const float4 &hj, const float4 &lj) {
       // j - o, as the reference orients it
       const float dx = dmin(hj.x, lj.x, hi_o.x, lo_o.x) * box.x;
       const float dy = dmin(hj.y, lj.y, hi_o.y, lo_o.y) * box.y;
@@ -172,6 +185,20 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
         w[3] -= dx * fy; w[4] -= dy * fy; w[5] -= dz * fy;
         w[6] -= dx * fz; w[7] -= dy * fz; w[8] -= dz * fz;
       }
+    };
+    int t = sub;
+    for (; t + 3 * MX_LJ_NP < n; t += 4 * MX_LJ_NP) {
+      const int j0 = L[t], j1 = L[t + MX_LJ_NP], j2 = L[t + 2 * MX_LJ_NP], j3 = L[t + 3 * MX_LJ_NP];
+      const float4 h0 = H[j0], h1 = H[j1], h2 = H[j2], h3 = H[j3];
+      const float4 l0 = Lo[j0], l1 = Lo[j1], l2 = Lo[j2], l3 = Lo[j3];
+      pair(h0, l0);
+      pair(h1, l1);
+      pair(h2, l2);
+      pair(h3, l3);
+    }
+    for (; t < n; t += MX_LJ_NP) {
+      const int j = L[t];
+      pair(H[j], Lo[j]);
     }
   }
   const double fx = group_sum_d<MX_LJ_NP>((double)sx - (double)cx);
@@ -194,7 +221,8 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
 constexpr int MSK_CHUNK = 32;
 constexpr int MSK_G = 8;
 constexpr int MSK_T = 128;
-constexpr int MF_T = 64;
+constexpr int MF_S = 32;  // sites per force block
+constexpr int MF_G = 8;   // column shares (warps) per force block
 constexpr int SIGN32 = (int)0x80000000u;
 
 GB_D float flipf(float v, int mask) { return __int_as_float(__float_as_int(v) ^ mask); }
@@ -263,17 +291,19 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
 }
 
 // FP64 sums of the chunk partials, energy and virial; FP32 force tables
-__global__ void __launch_bounds__(256) k_recip_weights_mx(const float4 *sk_part, int nchunk, int nkp,
-                                                          const int4 *kpair, const double *kw, double bfac,
-                                                          float4 *sk, double *acc) {
-  __shared__ double part[4][8][32];
-  __shared__ double sh[8 * 10];
+constexpr int MW_SL = 16;  // chunk slices per k pair in the weights kernel
+
+__global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *sk_part, int nchunk, int nkp,
+                                                                const int4 *kpair, const double *kw, double bfac,
+                                                                float4 *sk, double *acc) {
+  __shared__ double part[4][MW_SL][32];
+  __shared__ double sh[MW_SL * 10];
   const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
   const int c = blockIdx.y;
   const int k = blockIdx.x * 32 + lane;
   double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
   if (k < nkp) {
-    for (int ch = slice; ch < nchunk; ch += 8) {
+    for (int ch = slice; ch < nchunk; ch += MW_SL) {
       const float4 p = sk_part[((long long)c * nchunk + ch) * nkp + k];
       a0 += p.x;
       a1 += p.y;
@@ -289,7 +319,7 @@ __global__ void __launch_bounds__(256) k_recip_weights_mx(const float4 *sk_part,
   double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (slice == 0 && k < nkp) {
     double Pr = 0, Pi = 0, Qr = 0, Qi = 0;
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < MW_SL; ++j) {
       Pr += part[0][j][lane];
       Pi += part[1][j][lane];
       Qr += part[2][j][lane];
@@ -333,20 +363,25 @@ __global__ void __launch_bounds__(256) k_recip_weights_mx(const float4 *sk_part,
   block_sum_atomic<10>(vals, sh, acc);
 }
 
-__global__ void __launch_bounds__(MF_T) k_recip_force_mx(const float2 *__restrict__ tab, int na, int kmax, int ncol,
-                                                         const KCol *__restrict__ cols, int nkp,
-                                                         const float4 *__restrict__ sk, double *g) {
-  extern __shared__ float2 stf[];  // [3][K1][MF_T]
+// one block per 32 sites: its site tables are loaded into shared memory once,
+// and each of its MF_G warps takes a share of the columns (by k-pair count);
+// the warps' per-site sums are added in FP64 in a fixed order
+__global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__restrict__ tab, int na, int kmax,
+                                                              int ncol, const KCol *__restrict__ cols, int nkp,
+                                                              const float4 *__restrict__ sk, double *g) {
+  extern __shared__ float2 stf[];  // [3][K1][MF_S], then [MF_G][MF_S][3] double sums
   const int K1 = kmax + 1, K3 = 3 * K1;
-  const int c = blockIdx.z, t = threadIdx.x;
-  const int i0 = blockIdx.x * MF_T, i = i0 + t;
-  for (int w = t; w < K3 * MF_T; w += MF_T) {
-    const int e = w / MF_T, sl = w % MF_T;
-    const int si = min(i0 + sl, na - 1);
+  const int c = blockIdx.y;
+  const int t = threadIdx.x, sl = t % MF_S, wg = t / MF_S;
+  const int i0 = blockIdx.x * MF_S, i = i0 + sl;
+  for (int w = t; w < K3 * MF_S; w += MF_S * MF_G) {
+    const int e = w / MF_S, s2 = w % MF_S;
+    const int si = min(i0 + s2, na - 1);
     stf[w] = tab[((long long)c * na + si) * K3 + e];
   }
-  const long long kp_lo = (long long)blockIdx.y * nkp / gridDim.y;
-  const long long kp_hi = (long long)(blockIdx.y + 1) * nkp / gridDim.y;
+  double *red = reinterpret_cast<double *>(stf + ((K3 * MF_S + 1) & ~1));
+  const long long kp_lo = (long long)wg * nkp / MF_G;
+  const long long kp_hi = (long long)(wg + 1) * nkp / MF_G;
   auto first_col = [&](long long kp) {
     int lo = 0, hi = ncol;
     while (lo < hi) {
@@ -363,16 +398,17 @@ __global__ void __launch_bounds__(MF_T) k_recip_force_mx(const float2 *__restric
   for (int col = col0; col < col1; ++col) {
     const int4 ci4 = __ldg(reinterpret_cast<const int4 *>(cols + col));
     const int kx = ci4.x, ky = ci4.y, koff = ci4.z, mlo = ci4.w & 0xffff, mhi = ci4.w >> 16;
-    const float2 X = stf[kx * MF_T + t], Y = stf[(K1 + abs(ky)) * MF_T + t];
+    const float2 X = stf[kx * MF_S + sl], Y = stf[(K1 + abs(ky)) * MF_S + sl];
     const float yi = flipf(Y.y, ky < 0 ? SIGN32 : 0);
     const float cr = fmaf(X.x, Y.x, -X.y * yi);
     const float ci = fmaf(X.x, yi, X.y * Y.x);
     const float4 *Tp = T + 2LL * (koff - mlo);
-    const float2 *Z = stf + 2 * K1 * MF_T + t;
+    const float2 *Z = stf + 2 * K1 * MF_S + sl;
     float ur = 0.f, ui = 0.f, vr = 0.f, vi = 0.f;
+#pragma unroll 4
     for (int m = mlo; m <= mhi; ++m) {
-      const float2 z = Z[m * MF_T];
-      const float4 t0 = Tp[2 * m], t1 = Tp[2 * m + 1];
+      const float2 z = Z[m * MF_S];
+      const float4 t0 = __ldg(Tp + 2 * m), t1 = __ldg(Tp + 2 * m + 1);
       ur = fmaf(z.x, t0.x, fmaf(z.y, t0.w, ur));
       ui = fmaf(z.x, t0.y, fmaf(z.y, t0.z, ui));
       vr = fmaf(z.x, t1.x, fmaf(z.y, t1.y, vr));
@@ -383,12 +419,15 @@ __global__ void __launch_bounds__(MF_T) k_recip_force_mx(const float2 *__restric
     kadd(sy, ey, (float)ky * ts);
     kadd(sz, ez, -fmaf(cr, vi, ci * vr));
   }
-  if (i < na && col1 > col0) {
-    const double rlat = 2.0 * acos(-1.0);
-    double *G = g + ((long long)c * na + i) * 3;
-    atomicAdd(G, rlat * ((double)sx - (double)ex));
-    atomicAdd(G + 1, rlat * ((double)sy - (double)ey));
-    atomicAdd(G + 2, rlat * ((double)sz - (double)ez));
+  red[(wg * MF_S + sl) * 3] = (double)sx - (double)ex;
+  red[(wg * MF_S + sl) * 3 + 1] = (double)sy - (double)ey;
+  red[(wg * MF_S + sl) * 3 + 2] = (double)sz - (double)ez;
+  __syncthreads();
+  if (t < 3 * MF_S) {
+    const int s2 = t / 3, d = t % 3;
+    double f = 0.0;
+    for (int w = 0; w < MF_G; ++w) f += red[(w * MF_S + s2) * 3 + d];
+    if (i0 + s2 < na) g[((long long)c * na + i0 + s2) * 3 + d] += 2.0 * acos(-1.0) * f;
   }
 }
 
@@ -403,10 +442,10 @@ int sm_count_mx() {
 
 }  // namespace
 
-void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, const float *q, int na, int B,
-                          const PairList &pl, double alpha, double *g, double *acc) {
+void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
+                          double alpha, double *g, double *acc) {
   dim3 grid(nblk((long long)na * MX_NP, MX_T), B);
-  k_ewald_real_mx<<<grid, MX_T, 0, s>>>(hi, lo, q, na, pl.count, pl.idx, pl.cap, (float)alpha, g, acc);
+  k_ewald_real_mx<<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, g, acc);
 }
 
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
@@ -419,7 +458,9 @@ void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, in
 }
 
 size_t recip_sk_smem_mx(int kmax) { return sizeof(float2) * MSK_CHUNK * 3 * (kmax + 1); }
-size_t recip_force_smem_mx(int kmax) { return sizeof(float2) * 3 * (kmax + 1) * MF_T; }
+size_t recip_force_smem_mx(int kmax) {
+  return sizeof(float2) * ((3 * (kmax + 1) * MF_S + 1) & ~1) + sizeof(double) * MF_G * MF_S * 3;
+}
 
 // partial sums need nconf * nchunk * nkp float4 (half of the FP64 layout)
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B) {
@@ -439,21 +480,17 @@ void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc) 
   const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
   const double bfac = 0.25 / (c->P.walpha * c->P.walpha);
   dim3 grid(nblk(c->nkp, 32), B);
-  k_recip_weights_mx<<<grid, 256, 0, s>>>(reinterpret_cast<const float4 *>(c->sk_part), nchunk, c->nkp, c->kpair,
+  k_recip_weights_mx<<<grid, 32 * MW_SL, 0, s>>>(reinterpret_cast<const float4 *>(c->sk_part), nchunk, c->nkp, c->kpair,
                                           c->kw, bfac, reinterpret_cast<float4 *>(c->sk), acc);
 }
 
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
   if (c->nkp == 0) return;
   const int kmax = c->P.kmax;
-  const unsigned bx = nblk(c->na, MF_T);
-  const long long want = 8LL * sm_count_mx();
-  int nseg = (int)((want + (long long)bx * B - 1) / ((long long)bx * B));
-  nseg = std::max(1, std::min(16, std::min(nseg, c->ncol)));
-  dim3 grid(bx, nseg, B);
-  k_recip_force_mx<<<grid, MF_T, recip_force_smem_mx(kmax), s>>>(reinterpret_cast<const float2 *>(c->ktab), c->na,
-                                                                 kmax, c->ncol, c->kcol, c->nkp,
-                                                                 reinterpret_cast<const float4 *>(c->sk), g);
+  dim3 grid(nblk(c->na, MF_S), B);
+  k_recip_force_mx<<<grid, MF_S * MF_G, recip_force_smem_mx(kmax), s>>>(
+      reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
+      reinterpret_cast<const float4 *>(c->sk), g);
 }
 
 void recip_set_attributes_mx() {

@@ -131,6 +131,74 @@ __global__ void k_expand_forces(double *dvdr, const double *fb1, int nbc1, const
   }
 }
 
+// The same expansion for contracted rings of at most 2*HM+1 beads: the
+// contracted forces of a row are reduced to NQ = 2*HM+1 mode coefficients
+// (force_contract, evolve_pi.f90:377-403), and each bead's value is the dot
+// product with a per-bead table E[j] = sqrt(1/nb) (1, 2 cos(2 pi jk/nb),
+// -2 sin(2 pi jk/nb), k = 1..HM) held in shared memory.  R = float runs the
+// dot product in FP32 (mixed precision); the kick stays FP64.
+template <int HM, typename R>
+__global__ void k_expand_table(double *dvdr, const double *fb1, int nbc1, const double *tw_c1, const double *fb2,
+                               int nbc2, const double *tw_c2, const double *e1, const double *e2, const double *e3,
+                               double *p, double halfdt, int na, int nb, const double *tw_nb) {
+  constexpr int NQ = 2 * HM + 1;
+  extern __shared__ double smx[];
+  R *E = reinterpret_cast<R *>(smx);  // [nb][NQ]
+  const double sc = sqrt(1.0 / (double)nb);
+  for (int w = threadIdx.x; w < nb * NQ; w += blockDim.x) {
+    const int j = w / NQ, q = w % NQ;
+    double v = sc;
+    if (q > 0) {
+      const int k = (q + 1) / 2, m = (j * k) % nb;
+      v = (q & 1) ? 2.0 * sc * tw_nb[m] : -2.0 * sc * tw_nb[nb + m];
+    }
+    E[w] = (R)v;
+  }
+  __syncthreads();
+  const long long S = 3LL * na;
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= S) return;
+  double cf[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) cf[q] = 0.0;
+  const double *fbs[2] = {fb1, fb2};
+  const int nbcs[2] = {nbc1, nbc2};
+  const double *tws[2] = {tw_c1, tw_c2};
+  bool any = false;
+  for (int t = 0; t < 2; ++t) {
+    if (!fbs[t]) continue;
+    any = true;
+    const int nbc = nbcs[t], h = (nbc - 1) / 2;
+    double tmp[NQ + 1], hc[NQ + 1];  // nbc <= 2 HM + 2
+    for (int j = 0; j < nbc; ++j) tmp[j] = fbs[t][row + S * j];
+    gb_r2hc_direct(tmp, hc, nbc, tws[t]);
+    const double s1 = sqrt(1.0 / (double)nbc), s2 = sqrt((double)nb / (double)nbc);
+    cf[0] += s2 * (s1 * hc[0]);
+#pragma unroll
+    for (int k = 1; k <= HM; ++k) {
+      if (k <= h) {
+        cf[2 * k - 1] += s2 * (s1 * hc[k]);
+        cf[2 * k] += s2 * (s1 * hc[nbc - k]);
+      }
+    }
+  }
+  R cr[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) cr[q] = (R)cf[q];
+  for (int j = 0; j < nb; ++j) {
+    R s = (R)0;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) s += cr[q] * E[j * NQ + q];
+    double v = any ? (double)s : 0.0;
+    const long long o = row + S * j;
+    if (e1) v += e1[o];
+    if (e2) v += e2[o];
+    if (e3) v += e3[o];
+    dvdr[o] = v;
+    if (p) p[o] = p[o] - halfdt * v;
+  }
+}
+
 // intramolecular forces on B configurations (potenl_opt iopt = 4 path)
 __global__ void __launch_bounds__(128) k_intra(const double *r, double *out, int nm, int B, int model,
                                                IntraPar ip, double *acc, int accumulate) {
@@ -221,10 +289,38 @@ void launch_ring_contract(cudaStream_t s, const double *rnm, double *rb, int na,
   k_ring_contract<<<nblk(n, 128), 128, 0, s>>>(rnm, rb, na, nb, nbc, tw_c);
 }
 
+template <int HM>
+void launch_expand_hm(cudaStream_t s, bool mixed, double *dvdr, const double *fb1, int nbc1, const double *tw_c1,
+                      const double *fb2, int nbc2, const double *tw_c2, const double *e1, const double *e2,
+                      const double *e3, double *p, double halfdt, int na, int nb, const double *tw_nb) {
+  const long long n = 3LL * na;
+  const size_t smem = sizeof(double) * nb * (2 * HM + 1);
+  if (mixed)
+    k_expand_table<HM, float><<<nblk(n, 128), 128, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3,
+                                                              p, halfdt, na, nb, tw_nb);
+  else
+    k_expand_table<HM, double><<<nblk(n, 128), 128, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3,
+                                                               p, halfdt, na, nb, tw_nb);
+}
+
 void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int nbc1,
                           const double *tw_c1, const double *fb2, int nbc2, const double *tw_c2,
                           const double *e1, const double *e2, const double *e3, double *p,
-                          double halfdt, int na, int nb, const double *tw_nb) {
+                          double halfdt, int na, int nb, const double *tw_nb, bool mixed) {
+  int nbc = 1;
+  if (fb1) nbc = max(nbc, nbc1);
+  if (fb2) nbc = max(nbc, nbc2);
+  const int h = (nbc - 1) / 2;
+  // modes beyond nb/2 do not exist; the table form needs HM <= nb/2 and 2HM+1 <= nb
+  if (2 * h + 1 <= nb && h <= 4) {
+    switch (h) {
+      case 0: launch_expand_hm<0>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
+      case 1: launch_expand_hm<1>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
+      case 2: launch_expand_hm<2>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
+      case 3: launch_expand_hm<3>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
+      case 4: launch_expand_hm<4>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
+    }
+  }
   long long n = 3LL * na;
   k_expand_forces<<<nblk(n, 64), 64, 0, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p,
                                              halfdt, na, nb, tw_nb);

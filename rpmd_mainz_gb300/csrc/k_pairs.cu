@@ -24,7 +24,7 @@ constexpr int LB_T = 128;
 
 // wrapped fractional coordinates u in [0, 1) as FP32 (frac); with lo, also the
 // remainder u - frac as a second FP32, so that frac + lo carries u to ~1e-14
-__global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo) {
+__global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nconf * g.npt) return;
   int c = (int)(t / g.npt), i = (int)(t % g.npt);
@@ -40,7 +40,7 @@ __global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo) {
     e[d] = (float)(u - (double)uf);
     f[d] = uf >= 1.0f ? 0.0f : uf;
   }
-  frac[t] = make_float4(f[0], f[1], f[2], 0.0f);
+  frac[t] = make_float4(f[0], f[1], f[2], q ? (float)q[i] : 0.0f);
   if (lo) lo[t] = make_float4(e[0], e[1], e[2], 0.0f);
 }
 
@@ -501,9 +501,9 @@ double list_total(cudaStream_t s, const PairList &pl) {
   return (double)h;
 }
 
-void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo) {
+void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q) {
   long long n = (long long)nconf * g.npt;
-  k_frac32<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo);
+  k_frac32<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q);
 }
 
 // FP32 thresholds around rcutsq: below lo accept, at or above hi reject,

@@ -165,10 +165,10 @@ int list_cap(int npt, double rc, double vol) {
 // than skin/2 since the last rebuild, then filtered into the exact list.
 // Returns the number of launches through *nl.
 int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut, double vol, int *nl,
-              float4 *lo = nullptr) {
+              float4 *lo = nullptr, const double *q = nullptr) {
   int st = ensure_list(c, nconf, g.npt, list_cap(g.npt, cut, vol));
   if (st) return st;
-  launch_frac32(c->stream, g, nconf, c->rs32, lo);
+  launch_frac32(c->stream, g, nconf, c->rs32, lo, q);
   if (c->list_skin <= 0.0) {
     launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
     *nl = 2;
@@ -272,7 +272,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   g.full = mixed ? 1 : 0;  // the FP32 kernel walks full lists
   int nl = 0;
   prof_begin(c, PR_LIST);
-  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, 1.0, &nl, mixed ? c->lo32 : nullptr);
+  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, 1.0, &nl, mixed ? c->lo32 : nullptr, mixed ? c->z : nullptr);
   if (st) return st;
   prof_end(c, PR_LIST, (double)na * B);
   c->launches += nl;
@@ -282,7 +282,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   if (mixed) {
     recip_set_attributes_mx();
     prof_begin(c, PR_EW_REAL);
-    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, c->z32, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
+    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
     prof_end(c, PR_EW_REAL, npairs);
     prof_begin(c, PR_RECIP_SK);
     launch_recip_sk_mx(c->stream, c, c->rs, c->z, B);
@@ -488,7 +488,7 @@ int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, 
   prof_begin(c, PR_EXPAND);
   launch_expand_forces(c->stream, c->dvdr, con1 ? c->fb1 : nullptr, nbdf1, c->tw_c1,
                        con2 ? c->fb2 : nullptr, nbdf2, c->tw_c2, e1, e2, e3, p, halfdt, na, nb,
-                       c->tw_nb);
+                       c->tw_nb, c->P.precision == GB_PREC_MIXED);
   prof_end(c, PR_EXPAND, 3.0 * na * nb);
   c->launches += 1;
   return GB_OK;
@@ -525,6 +525,7 @@ int dev_prepare(gb_context *c, double dt, double beta) {
 }
 
 int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt) {
+  dev_graph_reset(c);  // other list configurations: a captured step would be stale
   int st;
   if ((st = dev_prepare(c, 0.0, 0.0))) return st;
   c->plan = EnergyPlan();
@@ -552,6 +553,7 @@ int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt) {
 }
 
 int dev_full_forces(gb_context *c) {
+  dev_graph_reset(c);  // other list configurations: a captured step would be stale
   int st;
   if ((st = dev_prepare(c, 0.0, 0.0))) return st;
   c->plan = EnergyPlan();
@@ -625,8 +627,72 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   return launch_status();
 }
 
+void dev_graph_reset(gb_context *c) {
+  if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
+  c->graph.exec = nullptr;
+  c->graph.valid = false;
+  c->graph.seen = 0;
+}
+
+// The fused step makes all of its decisions on the device (skin-list rebuilds
+// included) and no host synchronisation, so once the parameters, dt, beta and
+// box are unchanged the host side of a step repeats exactly: the second such
+// step is captured into a graph and later steps replay it.  Anything that
+// changes the key (or a device status error, which invalidates the skin
+// lists) drops the graph.
+int dev_step(gb_context *c, double dt, double beta) {
+  auto &G = c->graph;
+  const bool eligible = c->use_graphs && !c->prof && !c->generic_mts &&
+                        (c->nb == 2 || c->nb == 4 || c->nb == 8 || c->nb == 16 || c->nb == 32 || c->nb == 64) &&
+                        c->P.therm != GB_THERM_PRG && c->P.therm != GB_THERM_PRL;
+  const bool same = eligible && G.dt == dt && G.beta == beta && G.box[0] == c->box[0] && G.box[1] == c->box[1] &&
+                    G.box[2] == c->box[2] && std::memcmp(&G.P, &c->P, sizeof(gb_params)) == 0;
+  if (!same) {
+    dev_graph_reset(c);
+    G.dt = dt;
+    G.beta = beta;
+    for (int d = 0; d < 3; ++d) G.box[d] = c->box[d];
+    G.P = c->P;
+  }
+  if (same && G.valid) {
+    CK(cudaGraphLaunch(G.exec, c->stream));
+    c->launches += G.launches;
+    c->plan = G.plan;
+    c->last_beta = beta;
+    return GB_OK;
+  }
+  if (!eligible || G.seen < 1) {  // plain step; the next one with this key is captured
+    int st = dev_evolve_pi(c, dt, beta);
+    if (st) return st;
+    if (eligible) G.seen += 1;
+    return GB_OK;
+  }
+  const int64_t l0 = c->launches;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int st = dev_evolve_pi(c, dt, beta);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+  if (st) {
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+  }
+  if (e != cudaSuccess) return ctx_check_cuda(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&G.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    G.exec = nullptr;
+    return ctx_check_cuda(e, "cudaGraphInstantiate");
+  }
+  G.valid = true;
+  G.launches = c->launches - l0;
+  G.plan = c->plan;
+  CK(cudaGraphLaunch(G.exec, c->stream));  // the captured step has not run yet
+  return GB_OK;
+}
+
 // forces(r, v, dvdr, nb, ..., iopt = 1) of evolve_rig_pi (evolve_rigid.f90:174)
 int term_forces_rigid(gb_context *c) {
+  dev_graph_reset(c);  // other list configurations: a captured step would be stale
   int st;
   if ((st = dev_prepare(c, 0.0, 0.0))) return st;
   c->plan = EnergyPlan();
@@ -649,6 +715,7 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
   if (stw) {
     CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
     for (SkinList &L : c->sl) L.valid = false;  // a list may have overflowed: rebuild at next use
+    dev_graph_reset(c);
     if (stw & ST_LIST_OVERFLOW) return ctx_set_error(GB_E_LIST, "neighbour list too small");
     if (stw & ST_RATTLE1) return ctx_set_error(GB_E_RATTLE1, "max iterations exceeded in rattle stage 1");
     if (stw & ST_RATTLE2) return ctx_set_error(GB_E_RATTLE2, "max iterations exceeded in rattle stage 2");

@@ -69,6 +69,7 @@ def load(path=None):
     lib.gbrpmd_ctx_energies.argtypes = [C.c_void_p, D, D, D]
     lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
     lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
+    lib.gbrpmd_ctx_set_graphs.argtypes = [C.c_void_p, C.c_int]
     _lib = lib
     return lib
 
@@ -248,6 +249,10 @@ class Context:
     def set_list_skin(self, fraction):
         """Pair-list skin as a fraction of each cut-off (0: rebuild at every use)."""
         _check(load().gbrpmd_ctx_set_list_skin(self.h, C.c_double(fraction)))
+
+    def set_graphs(self, on):
+        """CUDA-graph replay of evolve steps (on by default)."""
+        _check(load().gbrpmd_ctx_set_graphs(self.h, 1 if on else 0))
 
     def list_rebuilds(self):
         """Rebuilds of the (Ewald, LJ, TEM) skin lists since creation."""

@@ -254,6 +254,39 @@ def test_skin_fraction_does_not_change_results(case):
             assert rel(a, b) < 1e-12
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_replay_matches_plain_steps(precision):
+    """Steps replayed from a captured CUDA graph, with a full_forces call in
+    between (which drops the graph), equal the same steps launched one by one."""
+    s = setup(param="param_qspcfw", ncell=(5, 5, 5), nb=8, mts=2, nbdf1=1, nbdf2=5)
+    prm = s["params"]
+    prm.precision = precision
+    lib.init(prm)
+    r = systems.perturbed(s, seed=80)
+    ff = lib.full_forces(r, s["box"], s["z"])
+    rng = np.random.default_rng(81)
+    p = rng.normal(size=r.shape) * np.sqrt(s["mass"][None, :, None] / (s["beta"] / s["nb"]))
+    out = []
+    for graphs in (False, True):
+        ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+        ctx.set_graphs(graphs)
+        ctx.upload(r=r, p=p, dvdr=ff["dvdr"], dvdr2=ff["dvdr2"], box=s["box"])
+        ctx.evolve(5, s["dt"], s["beta"])
+        ctx.full_forces()
+        ctx.evolve(6, s["dt"], s["beta"])
+        ctx.sync()
+        out.append((ctx.download(), ctx.energies(), ctx.launches))
+        ctx.close()
+    prm.precision = 0
+    lib.init(prm)
+    (a, ea, la), (b, eb, lb) = out
+    for x, y in zip(a, b):
+        assert rel(x, y) < 1e-12
+    for k in ("v", "vew", "vlj", "vint", "tv"):
+        assert erel(eb[k], ea[k]) < 1e-11
+    assert la == lb
+
+
 def rigid_system(nb=4):
     s = setup(param="param_tip05_rigid", ncell=(4, 4, 4), nb=nb)
     lib.rattle_setup(s["nm"])
