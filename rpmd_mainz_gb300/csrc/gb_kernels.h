@@ -63,7 +63,7 @@ void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const d
 // ---- mixed precision (k_mixed.cu): FP32 arithmetic, full lists, hi/lo positions ----
 // hi.w carries the site charge (launch_frac32 with q)
 void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double *g, double *acc);
+                          double alpha, double rcutsq, double *g, double *acc);
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
                   double sigsq, double rcutsq, const double *box, double dscale, double *out, double *acc);
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);

@@ -6,7 +6,9 @@
 //    (hi + lo, k_frac32), so a minimum-image displacement
 //    (hi_i - hi_j - rint(hi_i - hi_j)) + (lo_i - lo_j) keeps ~1e-14 of the box;
 //  * pair kernels walk full lists (each pair from both ends), so every point's
-//    force is summed by its own lanes and no atomics are needed;
+//    force is summed by its own lanes and no atomics are needed; the
+//    real-space kernel walks the skin list itself and drops pairs beyond the
+//    cut-off with its FP32 distance (no per-step exact filter);
 //  * force and energy sums are compensated (Kahan) FP32 per thread, virials
 //    plain FP32 per thread; all of them FP64 across threads;
 //  * the reciprocal-space power tables come from the FP64 recurrence rounded
@@ -18,7 +20,7 @@
 namespace {
 
 constexpr int MX_T = 64;     // threads per block of the pair kernels
-constexpr int MX_NP = 8;     // lanes per site in the real-space kernel
+constexpr int MX_NP = 16;    // lanes per site in the real-space kernel
 constexpr int MX_LJ_NP = 4;  // lanes per oxygen in the LJ kernel
 
 GB_D void kadd(float &s, float &c, float v) {  // Kahan-compensated s += v
@@ -39,6 +41,39 @@ GB_D double group_sum_d(double v) {
 GB_D float dmin(float hi_a, float lo_a, float hi_b, float lo_b) {
   const float d = hi_a - hi_b;
   return (d - rintf(d)) + (lo_a - lo_b);
+}
+
+GB_D float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block sums into acc[0] (energy: FP64 across lanes) and acc[1..NV-1]
+// (virial entries: FP32 within a warp, FP64 across warps); dst[k] < 0 skips
+template <int NV>
+GB_D void block_sum_mx(double e, const float (&v)[NV - 1], double *sh, double *acc, const int (&dst)[NV],
+                       const int (&dst2)[NV]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const double ew = warp_sum(e);
+  if (lane == 0) sh[warp * NV] = ew;
+#pragma unroll
+  for (int k = 1; k < NV; ++k) {
+    const float w = warp_sum_f(v[k - 1]);
+    if (lane == 0) sh[warp * NV + k] = (double)w;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s2 = lane < nw ? sh[lane * NV + k] : 0.0;
+      s2 = warp_sum(s2);
+      if (lane == 0 && s2 != 0.0) {
+        atomicAdd(acc + dst[k], s2);
+        if (dst2[k] >= 0) atomicAdd(acc + dst2[k], s2);
+      }
+    }
+  }
 }
 
 // block sums of (v, xx, yx, zx, yy, zy, zz) into v, vir(1..3, 1..3) column-major
@@ -72,8 +107,8 @@ GB_D void block_sum_sym7_mx(double (&vals)[7], double *sh, double *acc) {
 // four gathers are in flight per lane.
 __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                                                         int na, const int *__restrict__ count,
-                                                        const int *__restrict__ idx, int cap, float alpha, double *g,
-                                                        double *acc) {
+                                                        const int *__restrict__ idx, int cap, float alpha,
+                                                        float rcutsq, double *g, double *acc) {
   __shared__ double sh[32 * 7];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
@@ -96,6 +131,7 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
       const float dy = dmin(hi_i.y, lo_i.y, hj.y, lj.y);
       const float dz = dmin(hi_i.z, lo_i.z, hj.z, lj.z);
       const float drsq = dx * dx + dy * dy + dz * dz;
+      if (!(drsq < rcutsq)) return;  // skin-list entry beyond the cut-off
       const float inv = rsqrtf(drsq);
       const float x = alpha * (drsq * inv);
       const float e = expf(-x * x);
@@ -142,8 +178,10 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
     G[1] += fy;
     G[2] += fz;
   }
-  double vals[7] = {0.5 * ((double)ev - (double)evc), 0.5 * vxx, 0.5 * vyx, 0.5 * vzx, 0.5 * vyy, 0.5 * vzy, 0.5 * vzz};
-  block_sum_sym7_mx(vals, sh, acc);
+  const float vir6[6] = {0.5f * vxx, 0.5f * vyx, 0.5f * vzx, 0.5f * vyy, 0.5f * vzy, 0.5f * vzz};
+  constexpr int dst[7] = {0, 1, 2, 3, 5, 6, 9};       // v, xx, yx, zx, yy, zy, zz
+  constexpr int dst2[7] = {-1, -1, 4, 7, -1, 8, -1};  // mirrored xy, xz, yz
+  block_sum_mx<7>(0.5 * ((double)ev - (double)evc), vir6, sh, acc, dst, dst2);
 }
 
 // lj_list / lj_basic (ljones.f90) in FP32 over a full oxygen list; bead pairs
@@ -210,15 +248,16 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
     F[1] += dscale * fy;
     F[2] += dscale * fz;
   }
-  double vals[10];
-  vals[0] = 0.5 * ((double)vsum - (double)vcmp);
+  float vir9[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) vals[1 + k] = 0.5 * w[k];
-  block_sum_atomic<10>(vals, sh, acc);
+  for (int k = 0; k < 9; ++k) vir9[k] = 0.5f * w[k];
+  constexpr int dst[10] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9};
+  constexpr int dst2[10] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  block_sum_mx<10>(0.5 * ((double)vsum - (double)vcmp), vir9, sh, acc, dst, dst2);
 }
 
 // ---- reciprocal space (kwald, ewald_cubic.f90:235-533), FP32 ----
-constexpr int MSK_CHUNK = 32;
+constexpr int MSK_CHUNK = 128;  // sites per structure-factor block (FP32 partial sums)
 constexpr int MSK_G = 8;
 constexpr int MSK_T = 128;
 constexpr int MF_S = 32;  // sites per force block
@@ -443,9 +482,9 @@ int sm_count_mx() {
 }  // namespace
 
 void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double *g, double *acc) {
+                          double alpha, double rcutsq, double *g, double *acc) {
   dim3 grid(nblk((long long)na * MX_NP, MX_T), B);
-  k_ewald_real_mx<<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, g, acc);
+  k_ewald_real_mx<<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, (float)rcutsq, g, acc);
 }
 
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,

@@ -202,12 +202,17 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_fused(MtsArgs a) {
   }
 }
 
-// Mixed precision (same structure as k_mts_fused): the normal-mode state, the
-// free ring-polymer rotation (its coefficients) and the kicks stay FP64; every
-// transform runs in FP32 on deviations -- the centroid mode is the FP64 bead
-// sum, the other modes come from an FP32 transform of x_j - x_0 -- and the
-// intramolecular forces run in FP32 on positions taken relative to the
-// molecule's oxygen centroid, so that FP32 holds them to ~1e-7 bohr.
+// Mixed precision (same structure as k_mts_fused).  The centroid mode of p and
+// r stays FP64 (its bead sums, its free step and its kicks); the other normal
+// modes live in FP32 registers.  Their free ring-polymer rotation uses each
+// FP64 coefficient split into FP32 hi + lo, so that the rotation keeps its
+// unit determinant to ~1e-14 (a coefficient rounded to FP32 alone would make
+// the mode amplitudes grow or shrink steadily); the products and the states
+// round to FP32, which is noise.  Every transform runs in FP32 on deviations:
+// the centroid mode is the FP64 bead sum, the other modes come from an FP32
+// transform of x_j - x_0.  The intramolecular forces run in FP32 on positions
+// taken relative to the molecule's oxygen centroid, so that FP32 holds them to
+// ~1e-7 bohr.
 template <int NB>
 __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
   using C = MtsCfg<NB>;
@@ -219,14 +224,22 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
   float *s_f2 = s_dev + nrow * C::LD;              // [nrow][LD] intramolecular forces
   float *s_dvf = s_f2 + nrow * C::LD;              // [nrow][LD] dvdr for the estimator
   double *s_cen = sm + nf / 2;                     // [nrow] row centroids
-  double *s_mono = s_cen + nrow;                   // [12*NB]
-  double *s_red = s_mono + 12 * NB;                // [32 warps][18]
-  float *s_tw = reinterpret_cast<float *>(s_red + 32 * 18);  // [2*NB] cos, sin
+  double *s_mono = s_cen + nrow;                   // [12] monodromy of the centroid mode
+  double *s_red = s_mono + 12;                     // [32 warps][18]
+  float *s_mh = reinterpret_cast<float *>(s_red + 32 * 18);  // [12*NB] coefficients, hi
+  float *s_ml = s_mh + 12 * NB;                    // [12*NB] and lo parts
+  float *s_tw = s_ml + 12 * NB;                    // [2*NB] cos, sin
   float *s_twf = s_tw + 2 * NB;                    // scaled by sqrt(1/nb) / 2
   float *s_twi = s_twf + 2 * NB;                   // scaled by sqrt(1/nb)
   const int t = threadIdx.x;
   const double sc = sqrt(1.0 / (double)NB);
-  for (int i = t; i < 12 * NB; i += T) s_mono[i] = a.monod[i];
+  for (int i = t; i < 12 * NB; i += T) {
+    const double w = a.monod[i];
+    const float h = (float)w;
+    s_mh[i] = h;
+    s_ml[i] = (float)(w - (double)h);
+    if (i < 12) s_mono[i] = w;
+  }
   for (int i = t; i < 2 * NB; i += T) {
     const double w = a.tw[i];
     s_tw[i] = (float)w;
@@ -246,57 +259,62 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
   const int orow = ml * 9 + xyz;                   // oxygen row of the same coordinate
   float *dv_row = s_dvf + t * C::LD;
 
-  double pm[NB], xm[NB];
+  // kicks in FP64, then the modes: mode 0 = sc * (FP64 bead sum), modes k >= 1
+  // from the FP32 transform of the deviations from bead 0
+  double p0, x0;
+  float pf[NB], xf[NB];
+  {
+    double v[NB];
+    auto to_modes = [&](float (&out)[NB]) {
+      double sum = 0.0;
 #pragma unroll
-  for (int j = 0; j < NB; ++j) {
-    const double dv = a.dvdr[row + S * j];
-    const double pj = a.p[row + S * j] - a.halfdt * dv;
-    pm[j] = pj - a.halfdtsmall * a.dvdr2[row + S * j];
-    xm[j] = a.r[row + S * j];
-    dv_row[j] = (float)dv;
+      for (int j = 0; j < NB; ++j) sum += v[j];
+      const double v0 = v[0];
+      float d[NB];
+#pragma unroll
+      for (int j = 0; j < NB; ++j) d[j] = (float)(v[j] - v0);
+      gb_r2hc_s<NB, float>([&](int j) { return d[j]; }, [&](int k, float val) { out[k] = val; }, s_tw, s_twf);
+      return sc * sum;
+    };
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const double dv = a.dvdr[row + S * j];
+      const double pj = a.p[row + S * j] - a.halfdt * dv;
+      v[j] = pj - a.halfdtsmall * a.dvdr2[row + S * j];
+      dv_row[j] = (float)dv;
+    }
+    __syncthreads();  // the shared tables are written
+    p0 = to_modes(pf);
+#pragma unroll
+    for (int j = 0; j < NB; ++j) v[j] = a.r[row + S * j];
+    x0 = to_modes(xf);
   }
-  __syncthreads();
-  // forward transforms: mode 0 = sc * (FP64 bead sum), modes k >= 1 from the
-  // FP32 transform of the deviations from bead 0
-  auto to_modes = [&](double (&v)[NB]) {
-    double sum = 0.0;
-#pragma unroll
-    for (int j = 0; j < NB; ++j) sum += v[j];
-    const double v0 = v[0];
-    float d[NB];
-#pragma unroll
-    for (int j = 0; j < NB; ++j) d[j] = (float)(v[j] - v0);
-    gb_r2hc_s<NB, float>([&](int j) { return d[j]; },
-                         [&](int k, float val) {
-                           if (k > 0) v[k] = (double)val;
-                         },
-                         s_tw, s_twf);
-    v[0] = sc * sum;
-  };
-  to_modes(pm);
-  to_modes(xm);
 
   double e_last = 0.0, q1 = 0.0, q2 = 0.0;
   float vir[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float off = 0.f;  // this row's centroid minus its oxygen's centroid
   for (int im = 1; im <= a.mts; ++im) {
+    {  // free ring-polymer rotation (evolve_pi.f90:109-125)
+      const double *mo = s_mono + ic;
+      const double pp = p0 * mo[0] + x0 * mo[3];
+      x0 = p0 * mo[6] + x0 * mo[9];
+      p0 = pp;
 #pragma unroll
-    for (int k = 0; k < NB; ++k) {  // free ring-polymer rotation, FP64 (evolve_pi.f90:109-125)
-      const double *mo = s_mono + ic + 12 * k;
-      const double pp = pm[k] * mo[0] + xm[k] * mo[3];
-      xm[k] = pm[k] * mo[6] + xm[k] * mo[9];
-      pm[k] = pp;
+      for (int k = 1; k < NB; ++k) {
+        const float *h = s_mh + ic + 12 * k, *l = s_ml + ic + 12 * k;
+        const float pk = pf[k], xk = xf[k];
+        pf[k] = fmaf(pk, h[0], fmaf(xk, h[3], fmaf(pk, l[0], xk * l[3])));
+        xf[k] = fmaf(pk, h[6], fmaf(xk, h[9], fmaf(pk, l[6], xk * l[9])));
+      }
     }
-    const double cen = sc * xm[0];
+    const double cen = sc * x0;
     s_cen[t] = cen;
     __syncthreads();
     off = (float)(cen - s_cen[orow]);
     {  // bead positions relative to the oxygen centroid (evolve_pi.f90:141-145)
-      float xf[NB];
-#pragma unroll
-      for (int k = 0; k < NB; ++k) xf[k] = k ? (float)xm[k] : 0.f;
       float *dst = s_dev + t * C::LD;
-      gb_hc2r_s<NB, float>([&](int j) { return xf[j]; }, [&](int k, float v) { dst[k] = off + v; }, s_tw, s_twi);
+      gb_hc2r_s<NB, float>([&](int j) { return j ? xf[j] : 0.f; }, [&](int k, float v) { dst[k] = off + v; }, s_tw,
+                           s_twi);
     }
     __syncthreads();
     double e_sub = 0.0;
@@ -332,9 +350,15 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
         q2 += (double)a2;
       }
       if (im != a.mts) {  // FT(dvdr2) and p -= dtsmall dvdr2 (evolve_pi.f90:156-159)
-        const double dts = a.dtsmall;
+        const float dtsf = (float)a.dtsmall;
+        float f0 = 0.f;
         gb_r2hc_s<NB, float>([&](int j) { return f2_row[j]; },
-                             [&](int k, float v) { pm[k] = pm[k] - dts * (double)v; }, s_tw, s_twf);
+                             [&](int k, float v) {
+                               if (k) pf[k] = fmaf(-dtsf, v, pf[k]);
+                               else f0 = v;
+                             },
+                             s_tw, s_twf);
+        p0 = p0 - a.dtsmall * (double)f0;
       }
     }
     if (im != a.mts) __syncthreads();
@@ -343,22 +367,19 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
     // back to beads: p = HC2R(p); r = rst; p -= halfdtsmall dvdr2 (evolve_pi.f90:222-228)
     const float *dev_row = s_dev + t * C::LD;
     const float *f2_row = s_f2 + t * C::LD;
-    const double hds = a.halfdtsmall;
-    const double pc = sc * pm[0], cen = sc * xm[0];
-    float pf[NB];
-#pragma unroll
-    for (int k = 0; k < NB; ++k) pf[k] = k ? (float)pm[k] : 0.f;
+    const float hds = (float)a.halfdtsmall;
+    const double pc = sc * p0, cen = sc * x0;
     double *gp = a.p + row;
-    gb_hc2r_s<NB, float>([&](int j) { return pf[j]; },
+    gb_hc2r_s<NB, float>([&](int j) { return j ? pf[j] : 0.f; },
                          [&](int k, float v) {
-                           if (valid) gp[S * k] = pc + (double)v - hds * (double)f2_row[k];
+                           if (valid) gp[S * k] = pc + (double)fmaf(-hds, f2_row[k], v);
                          },
                          s_tw, s_twi);
     if (valid) {
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
         a.r[row + S * j] = cen + (double)(dev_row[j] - off);
-        a.rnm[row + S * j] = xm[j];
+        a.rnm[row + S * j] = j ? (double)xf[j] : x0;
         a.dvdr2[row + S * j] = (double)f2_row[j];
       }
     }
@@ -397,7 +418,7 @@ size_t mts_smem_mixed(int T) {
   using C = MtsCfg<NB>;
   const int nrow = (T + 8) / 9 * 9;
   const int nf = (3 * nrow * C::LD + 1) & ~1;
-  return sizeof(float) * nf + sizeof(double) * (nrow + 12 * NB + 32 * 18) + sizeof(float) * 6 * NB;
+  return sizeof(float) * nf + sizeof(double) * (nrow + 12 + 32 * 18) + sizeof(float) * (24 * NB + 6 * NB);
 }
 
 template <int NB>

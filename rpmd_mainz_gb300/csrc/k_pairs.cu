@@ -60,8 +60,9 @@ GB_D bool exact_pair_in(const PairGeom &g, const double *a, const double *b) {
 }
 
 // Block (i-tile, j-chunk, configuration): each thread tests its point i against
-// a 1024-point chunk of partners staged through shared memory and appends hits
-// with an atomic counter per point, so the order inside a list is arbitrary.
+// a 1024-point chunk of partners staged through shared memory, reserves slots
+// for its hits with one atomic add per (point, chunk) and writes them, so the
+// order of the chunks inside a list is arbitrary.
 constexpr int LB_JCHUNK = 1024;
 
 __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *frac, int *count,
@@ -86,37 +87,45 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
   }
   int *cnt = count + (long long)c * npt + (i < npt ? i : 0);
   int *my = idx + ((long long)c * npt + (i < npt ? i : 0)) * cap;
-  bool over = false;
-  for (int jt = j0; jt < j1; jt += LB_T) {
-    const int jl = jt + threadIdx.x;
-    tile[threadIdx.x] = jl < j1 ? fr[jl] : make_float4(0.5f, 0.5f, 0.5f, 0.f);
-    __syncthreads();
-    if (i < npt) {
-      const int jmax = min(LB_T, j1 - jt);
-      for (int jj = 0; jj < jmax; ++jj) {
-        const int j = jt + jj;
-        if (j == i) continue;
-        if (!g.full && (i < j) != (((i + j) & 1) != 0)) continue;
-        if (g.excl_mol && (i / 3) == (j / 3)) continue;
-        const float4 fj = tile[jj];
-        float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
-        dx = (dx - rintf(dx)) * len.x;
-        dy = (dy - rintf(dy)) * len.y;
-        dz = (dz - rintf(dz)) * len.z;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        if (d2 >= thr_hi) continue;
-        bool ok = d2 < thr_lo;
-        if (!ok) ok = exact_pair_in(g, pi, base + (long long)j * g.pstride);
-        if (ok) {
-          const int slot = atomicAdd(cnt, 1);
-          if (slot < cap) my[slot] = j;
-          else over = true;
+  // two passes over the chunk: count this point's partners, reserve their
+  // slots with one atomic add, then test again and write them
+  int nfound = 0, slot = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1 && i < npt && nfound > 0) slot = atomicAdd(cnt, nfound);
+    for (int jt = j0; jt < j1; jt += LB_T) {
+      const int jl = jt + threadIdx.x;
+      tile[threadIdx.x] = jl < j1 ? fr[jl] : make_float4(0.5f, 0.5f, 0.5f, 0.f);
+      __syncthreads();
+      if (i < npt && (pass == 0 || nfound > 0)) {
+        const int jmax = min(LB_T, j1 - jt);
+        for (int jj = 0; jj < jmax; ++jj) {
+          const int j = jt + jj;
+          if (j == i) continue;
+          if (!g.full && (i < j) != (((i + j) & 1) != 0)) continue;
+          if (g.excl_mol && (i / 3) == (j / 3)) continue;
+          const float4 fj = tile[jj];
+          float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
+          dx = (dx - rintf(dx)) * len.x;
+          dy = (dy - rintf(dy)) * len.y;
+          dz = (dz - rintf(dz)) * len.z;
+          const float d2 = dx * dx + dy * dy + dz * dz;
+          if (d2 >= thr_hi) continue;
+          bool ok = d2 < thr_lo;
+          if (!ok) ok = exact_pair_in(g, pi, base + (long long)j * g.pstride);
+          if (ok) {
+            if (pass == 0) {
+              ++nfound;
+            } else {
+              if (slot < cap) my[slot] = j;
+              ++slot;
+            }
+          }
         }
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
-  if (over) atomicOr(status, ST_LIST_OVERFLOW);
+  if (i < npt && nfound > 0 && slot > cap) atomicOr(status, ST_LIST_OVERFLOW);
 }
 
 // ---- skin lists ----

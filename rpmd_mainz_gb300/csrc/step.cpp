@@ -164,8 +164,11 @@ int list_cap(int npt, double rc, double vol) {
 // cut-off + skin is rebuilt on the device only when a point has moved by more
 // than skin/2 since the last rebuild, then filtered into the exact list.
 // Returns the number of launches through *nl.
+// With superset = true the filter is skipped and *use points at the skin list
+// itself (a consumer that tests the cut-off on its own); else *use = &c->pl.
 int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut, double vol, int *nl,
-              float4 *lo = nullptr, const double *q = nullptr) {
+              float4 *lo = nullptr, const double *q = nullptr, bool superset = false, PairList **use = nullptr) {
+  if (use) *use = &c->pl;
   int st = ensure_list(c, nconf, g.npt, list_cap(g.npt, cut, vol));
   if (st) return st;
   launch_frac32(c->stream, g, nconf, c->rs32, lo, q);
@@ -227,8 +230,15 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   gs.rcutsq = scut * scut;
   launch_build_list(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag);
   launch_skin_save(c->stream, g, nconf, S.ref, S.flag, S.rebuilds);
-  launch_list_filter(c->stream, g, nconf, c->rs32, S.pl, c->pl, c->status);
-  n += 4;
+  n += 3;
+  if (superset && use) {
+    *use = &S.pl;
+    // profiling counts in-cut pairs: the exact list is made for the count only
+    if (c->prof) launch_list_filter(c->stream, g, nconf, c->rs32, S.pl, c->pl, c->status);
+  } else {
+    launch_list_filter(c->stream, g, nconf, c->rs32, S.pl, c->pl, c->status);
+    n += 1;
+  }
   S.valid = true;
   S.nconf = nconf;
   S.npt = g.npt;
@@ -272,17 +282,20 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   g.full = mixed ? 1 : 0;  // the FP32 kernel walks full lists
   int nl = 0;
   prof_begin(c, PR_LIST);
-  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, 1.0, &nl, mixed ? c->lo32 : nullptr, mixed ? c->z : nullptr);
+  PairList *pl = nullptr;  // mixed: the skin list itself, cut-off tested in the FP32 kernel
+  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, 1.0, &nl, mixed ? c->lo32 : nullptr, mixed ? c->z : nullptr,
+                     mixed, &pl);
   if (st) return st;
   prof_end(c, PR_LIST, (double)na * B);
   c->launches += nl;
-  // in-cut pairs (each once)
+  // in-cut pairs, each once (profiling fills c->pl with the exact list)
   const double npairs = c->prof ? list_total(c->stream, c->pl) * (mixed ? 0.5 : 1.0) : 0.0;
   const double ksites = (double)c->nk * na * B;
   if (mixed) {
     recip_set_attributes_mx();
     prof_begin(c, PR_EW_REAL);
-    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
+    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, c->g,
+                         slot(c, s));
     prof_end(c, PR_EW_REAL, npairs);
     prof_begin(c, PR_RECIP_SK);
     launch_recip_sk_mx(c->stream, c, c->rs, c->z, B);
