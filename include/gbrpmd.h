@@ -254,6 +254,29 @@ int gbrpmd_ctx_list_rebuilds(gb_context *ctx, unsigned *counts3);
    the second step with unchanged parameters, dt, beta and box is captured and
    later steps replay it.  Results do not depend on the setting. */
 int gbrpmd_ctx_set_graphs(gb_context *ctx, int on);
+/* Parameters owned by one context (instead of the set given to gbrpmd_init),
+   as batch replicas of different boxes and Ewald set-ups need them. */
+int gbrpmd_ctx_set_params(gb_context *ctx, const gb_params *params);
+
+/* ---- batched replicas (no counterpart in the reference, which runs one
+   trajectory per process; batch.cpp) ----
+   A batch advances resident contexts of any molecule and bead counts together:
+   each step is one CUDA graph with one branch per replica (captured on the
+   second step after a membership change, replayed afterwards).  Every replica
+   keeps its own parameters (gbrpmd_ctx_set_params), dt, beta and, with
+   thresh > 0, its own Andersen test (md_eq.f90:311-315) on ran2 stream irun.
+   Call gbrpmd_batch_sync before reading a replica (gbrpmd_ctx_sync,
+   gbrpmd_ctx_download); queue no other work on a replica while it is in a batch. */
+typedef struct gb_batch gb_batch;
+int gbrpmd_batch_create(gb_batch **batch);
+int gbrpmd_batch_destroy(gb_batch *batch);
+int gbrpmd_batch_add(gb_batch *batch, gb_context *ctx, double dt, double beta, double thresh, int irun);
+int gbrpmd_batch_remove(gb_batch *batch, gb_context *ctx);
+int gbrpmd_batch_size(gb_batch *batch);
+int gbrpmd_batch_step(gb_batch *batch, int nsteps);
+int gbrpmd_batch_sync(gb_batch *batch);
+void *gbrpmd_batch_stream(gb_batch *batch);
+
 /* the md_eq step loop (md_eq.f90:182-323) on the device state: nsteps
    evolve_pi steps, each followed by the Andersen test ran2(irun) < thresh
    that resamples all momenta (md_eq.f90:311-315) when therm is AND.

@@ -330,7 +330,7 @@ int gbrpmd_ctx_download(gb_context *c, double *r, double *p, double *dvdr, doubl
 
 int gbrpmd_ctx_full_forces(gb_context *c, double *v, double *vew, double *voo, double *vint,
                            double *vir) {
-  c->P = g_params;
+  if (!c->own_params) c->P = g_params;
   int st = dev_full_forces(c);
   if (st) return st;
   if ((st = dev_collect(c, 0, 0.0, 1.0))) return st;
@@ -344,7 +344,7 @@ int gbrpmd_ctx_full_forces(gb_context *c, double *v, double *vew, double *voo, d
 }
 
 int gbrpmd_ctx_evolve(gb_context *c, int nsteps, double dt, double beta) {
-  c->P = g_params;
+  if (!c->own_params) c->P = g_params;
   for (int s = 0; s < nsteps; ++s) {
     int st = dev_step(c, dt, beta);
     if (st) return st;
@@ -386,6 +386,17 @@ int gbrpmd_ctx_set_list_skin(gb_context *c, double fraction) {
   c->list_skin = fraction;
   for (SkinList &L : c->sl) L.valid = false;
   dev_graph_reset(c);
+  return GB_OK;
+}
+
+int gbrpmd_ctx_set_params(gb_context *c, const gb_params *params) {
+  if (!c || !params) return ctx_set_error(GB_E_ARG, "null argument");
+  if (params->mts < 1) return ctx_set_error(GB_E_ARG, "mts must be >= 1");
+  if (params->precision != GB_PREC_FP64 && params->precision != GB_PREC_MIXED)
+    return ctx_set_error(GB_E_ARG, "precision must be GB_PREC_FP64 or GB_PREC_MIXED");
+  CK(cudaStreamSynchronize(c->stream));
+  c->P = *params;
+  c->own_params = 1;
   return GB_OK;
 }
 

@@ -53,6 +53,7 @@ struct gb_context {
   cudaStream_t stream = nullptr;
   int device = 0;
   gb_params P{};  // parameters in force for this context (copied at each call)
+  int own_params = 0;  // 1: P was set for this context (gbrpmd_ctx_set_params) and stays
 
   // trajectory state, layout r(3,na,nb)
   double *p = nullptr, *r = nullptr, *dvdr = nullptr, *dvdr2 = nullptr;

@@ -60,20 +60,23 @@ GB_D bool exact_pair_in(const PairGeom &g, const double *a, const double *b) {
 }
 
 // Block (i-tile, j-chunk, configuration): each thread tests its point i against
-// a 1024-point chunk of partners staged through shared memory, reserves slots
-// for its hits with one atomic add per (point, chunk) and writes them, so the
-// order of the chunks inside a list is arbitrary.
-constexpr int LB_JCHUNK = 1024;
+// a chunk of partners staged through shared memory.  Hits go to a 32-entry
+// staging row per thread in shared memory; a full row (and the rest at the end
+// of the chunk) reserves its slots in the point's list with one atomic add and
+// is copied out, so the order of the flushed groups inside a list is arbitrary.
+constexpr int LB_STAGE = 32;
 
 __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *frac, int *count,
                                                       int *idx, int cap, float3 len, float thr_lo,
-                                                      float thr_hi, unsigned *status, const unsigned *gate) {
+                                                      float thr_hi, unsigned *status, const unsigned *gate,
+                                                      int jchunk) {
   __shared__ float4 tile[LB_T];
+  __shared__ int stage[LB_T][LB_STAGE + 1];
   if (gate && *gate == 0u) return;  // skin list still valid: nothing to rebuild
   const int c = blockIdx.z;
   const int i = blockIdx.x * LB_T + threadIdx.x;
   const int npt = g.npt;
-  const int j0 = blockIdx.y * LB_JCHUNK, j1 = min(npt, j0 + LB_JCHUNK);
+  const int j0 = blockIdx.y * jchunk, j1 = min(npt, j0 + jchunk);
   const float4 *fr = frac + (long long)c * npt;
   const double *base = g.pos + c * g.cstride;
   float4 fi = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -87,45 +90,47 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
   }
   int *cnt = count + (long long)c * npt + (i < npt ? i : 0);
   int *my = idx + ((long long)c * npt + (i < npt ? i : 0)) * cap;
-  // two passes over the chunk: count this point's partners, reserve their
-  // slots with one atomic add, then test again and write them
-  int nfound = 0, slot = 0;
-  for (int pass = 0; pass < 2; ++pass) {
-    if (pass == 1 && i < npt && nfound > 0) slot = atomicAdd(cnt, nfound);
-    for (int jt = j0; jt < j1; jt += LB_T) {
-      const int jl = jt + threadIdx.x;
-      tile[threadIdx.x] = jl < j1 ? fr[jl] : make_float4(0.5f, 0.5f, 0.5f, 0.f);
-      __syncthreads();
-      if (i < npt && (pass == 0 || nfound > 0)) {
-        const int jmax = min(LB_T, j1 - jt);
-        for (int jj = 0; jj < jmax; ++jj) {
-          const int j = jt + jj;
-          if (j == i) continue;
-          if (!g.full && (i < j) != (((i + j) & 1) != 0)) continue;
-          if (g.excl_mol && (i / 3) == (j / 3)) continue;
-          const float4 fj = tile[jj];
-          float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
-          dx = (dx - rintf(dx)) * len.x;
-          dy = (dy - rintf(dy)) * len.y;
-          dz = (dz - rintf(dz)) * len.z;
-          const float d2 = dx * dx + dy * dy + dz * dz;
-          if (d2 >= thr_hi) continue;
-          bool ok = d2 < thr_lo;
-          if (!ok) ok = exact_pair_in(g, pi, base + (long long)j * g.pstride);
-          if (ok) {
-            if (pass == 0) {
-              ++nfound;
-            } else {
-              if (slot < cap) my[slot] = j;
-              ++slot;
-            }
-          }
+  int *st = stage[threadIdx.x];
+  int nst = 0;
+  bool over = false;
+  auto flush = [&]() {
+    const int slot = atomicAdd(cnt, nst);
+    for (int k = 0; k < nst; ++k) {
+      if (slot + k < cap) my[slot + k] = st[k];
+      else over = true;
+    }
+    nst = 0;
+  };
+  for (int jt = j0; jt < j1; jt += LB_T) {
+    const int jl = jt + threadIdx.x;
+    tile[threadIdx.x] = jl < j1 ? fr[jl] : make_float4(0.5f, 0.5f, 0.5f, 0.f);
+    __syncthreads();
+    if (i < npt) {
+      const int jmax = min(LB_T, j1 - jt);
+      for (int jj = 0; jj < jmax; ++jj) {
+        const int j = jt + jj;
+        if (j == i) continue;
+        if (!g.full && (i < j) != (((i + j) & 1) != 0)) continue;
+        if (g.excl_mol && (i / 3) == (j / 3)) continue;
+        const float4 fj = tile[jj];
+        float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
+        dx = (dx - rintf(dx)) * len.x;
+        dy = (dy - rintf(dy)) * len.y;
+        dz = (dz - rintf(dz)) * len.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 >= thr_hi) continue;
+        bool ok = d2 < thr_lo;
+        if (!ok) ok = exact_pair_in(g, pi, base + (long long)j * g.pstride);
+        if (ok) {
+          st[nst++] = j;
+          if (nst == LB_STAGE) flush();
         }
       }
-      __syncthreads();
     }
+    __syncthreads();
   }
-  if (i < npt && nfound > 0 && slot > cap) atomicOr(status, ST_LIST_OVERFLOW);
+  if (i < npt && nst > 0) flush();
+  if (over) atomicOr(status, ST_LIST_OVERFLOW);
 }
 
 // ---- skin lists ----
@@ -541,8 +546,16 @@ void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float
   const long long ncount = (long long)nconf * g.npt;
   if (gate) k_skin_zero<<<nblk(ncount, 256), 256, 0, s>>>(pl.count, ncount, gate);
   else cudaMemsetAsync(pl.count, 0, sizeof(int) * (size_t)ncount, s);
-  dim3 grid(nblk(g.npt, LB_T), nblk(g.npt, LB_JCHUNK), nconf);
-  k_build_list2<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status, gate);
+  // partner chunks of 1024 points, halved until the grid has ~4 blocks per SM
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int jchunk = 1024;
+  const long long bi = (long long)nblk(g.npt, LB_T) * nconf;
+  while (jchunk > LB_T && bi * (long long)nblk(g.npt, jchunk) < 4LL * nsm) jchunk /= 2;
+  dim3 grid(nblk(g.npt, LB_T), nblk(g.npt, jchunk), nconf);
+  k_build_list2<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status, gate,
+                                      jchunk);
 }
 
 void launch_skin_check(cudaStream_t s, const PairGeom &g, int nconf, const double *ref, double lim2,

@@ -127,8 +127,8 @@ int gbrpmd_sample_rpmd(double *p, int na, int nb, const double *mass, double bet
 // step).  Momenta for a collision are drawn on the host and uploaded.
 int gbrpmd_run_md_eq(gb_context *c, int nsteps, double dt, double beta, double thresh, int *irun,
                      double *energies) {
-  const gb_params &P = current_params();
-  c->P = P;
+  if (!c->own_params) c->P = current_params();
+  const gb_params &P = c->P;
   std::vector<double> hmass, hp;
   if (P.therm == GB_THERM_AND) {
     hmass.resize(c->na);

@@ -70,6 +70,18 @@ def load(path=None):
     lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
     lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
     lib.gbrpmd_ctx_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_ctx_set_params.argtypes = [C.c_void_p, C.c_void_p]
+    lib.gbrpmd_run_md_eq.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int),
+                                     C.c_void_p]
+    lib.gbrpmd_batch_create.argtypes = [C.POINTER(C.c_void_p)]
+    lib.gbrpmd_batch_destroy.argtypes = [C.c_void_p]
+    lib.gbrpmd_batch_add.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int]
+    lib.gbrpmd_batch_remove.argtypes = [C.c_void_p, C.c_void_p]
+    lib.gbrpmd_batch_size.argtypes = [C.c_void_p]
+    lib.gbrpmd_batch_step.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_batch_sync.argtypes = [C.c_void_p]
+    lib.gbrpmd_batch_stream.restype = C.c_void_p
+    lib.gbrpmd_batch_stream.argtypes = [C.c_void_p]
     _lib = lib
     return lib
 
@@ -250,6 +262,17 @@ class Context:
         """Pair-list skin as a fraction of each cut-off (0: rebuild at every use)."""
         _check(load().gbrpmd_ctx_set_list_skin(self.h, C.c_double(fraction)))
 
+    def set_params(self, params):
+        """Parameters owned by this context (a batch replica needs them)."""
+        _check(load().gbrpmd_ctx_set_params(self.h, C.byref(params)))
+
+    def run_md_eq(self, nsteps, dt, beta, thresh, irun: C.c_int, energies=False):
+        """md_eq step loop with the Andersen test; irun is advanced in place."""
+        e = np.zeros(4 * nsteps) if energies else None
+        _check(load().gbrpmd_run_md_eq(self.h, nsteps, dt, beta, thresh, C.byref(irun),
+                                       None if e is None else _ptr(e)))
+        return None if e is None else e.reshape(nsteps, 4)
+
     def set_graphs(self, on):
         """CUDA-graph replay of evolve steps (on by default)."""
         _check(load().gbrpmd_ctx_set_graphs(self.h, 1 if on else 0))
@@ -267,3 +290,44 @@ def ran2(idum: C.c_int, rmin=0.0, rmax=1.0):
 
 def gaussian(idum: C.c_int, sigma=1.0):
     return load().gbrpmd_gaussian(C.byref(idum), C.byref(C.c_double(sigma)))
+
+
+class Batch:
+    """Resident contexts advanced together, one CUDA-graph launch per step."""
+
+    def __init__(self):
+        self.h = C.c_void_p()
+        self.members = []
+        _check(load().gbrpmd_batch_create(C.byref(self.h)))
+
+    def add(self, ctx, dt, beta, thresh=0.0, irun=0):
+        _check(load().gbrpmd_batch_add(self.h, ctx.h, dt, beta, thresh, irun))
+        self.members.append(ctx)
+
+    def remove(self, ctx):
+        _check(load().gbrpmd_batch_remove(self.h, ctx.h))
+        self.members.remove(ctx)
+
+    def step(self, nsteps=1):
+        _check(load().gbrpmd_batch_step(self.h, nsteps))
+
+    def sync(self):
+        _check(load().gbrpmd_batch_sync(self.h))
+
+    @property
+    def stream(self):
+        return load().gbrpmd_batch_stream(self.h)
+
+    def __len__(self):
+        return load().gbrpmd_batch_size(self.h)
+
+    def close(self):
+        if self.h:
+            load().gbrpmd_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
