@@ -164,16 +164,16 @@ def fp32_peak_tflops(torch):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def read_profile_traffic(region):
+def read_profile_traffic(region, precision):
     """DRAM bytes per launch of `region` from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
         parts = line.split()
-        if len(parts) >= 2 and parts[0] == region:
+        if len(parts) >= 3 and not line.startswith("#") and parts[0] == region and parts[1] == precision:
             try:
-                return float(parts[1])
+                return float(parts[2])
             except ValueError:
                 return None
     return None
@@ -416,14 +416,14 @@ def main():
         if prec == 0:
             peak = fp64_peak_tflops(torch)
             out["roofline"] = {"bound": "fp64", "kernel_region": dom, "achieved": achieved, "peak": peak,
-                               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom),
+                               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom, "fp64"),
                                "peak_source": "measured in this run: cuBLAS DGEMM 8192^3 (FP64 rate; "
                                               "MEASURED_PEAKS.json holds only HBM and BF16)",
                                "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": rr["units"] / rr["launches"]}
         else:
             peak = fp32_peak_tflops(torch)
             out["roofline"] = {"bound": "fp32", "kernel_region": dom, "achieved": achieved, "peak": peak,
-                               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom),
+                               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom, "mixed"),
                                "peak_source": "measured in this run: cuBLAS SGEMM 8192^3 without TF32 (FP32 "
                                               "CUDA-core rate; MEASURED_PEAKS.json holds only HBM and BF16)",
                                "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": rr["units"] / rr["launches"]}

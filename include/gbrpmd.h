@@ -26,6 +26,7 @@
 #ifndef GBRPMD_H
 #define GBRPMD_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -276,6 +277,35 @@ int gbrpmd_batch_size(gb_batch *batch);
 int gbrpmd_batch_step(gb_batch *batch, int nsteps);
 int gbrpmd_batch_sync(gb_batch *batch);
 void *gbrpmd_batch_stream(gb_batch *batch);
+
+/* Device memory: what a context holds now, and what one of (na, nb) with
+   these parameters will hold once it has stepped (the server's admission test). */
+size_t gbrpmd_ctx_device_bytes(gb_context *ctx);
+size_t gbrpmd_estimate_device_bytes(int na, int nb, const gb_params *params);
+
+/* ---- serving loop (no counterpart in the reference; server.cpp) ----
+   Continuous batching of independent trajectory requests.  A request brings
+   its system (na, nb, parameters, masses, charges, box), its starting state in
+   host arrays the caller keeps valid until the request is polled (final r, p,
+   dvdr, dvdr2 are written back into them; dvdr/dvdr2 may both be NULL, then
+   full_forces supplies the starting forces), nsteps evolve_pi steps, dt, beta
+   and an optional Andersen test.  gbrpmd_server_tick admits queued requests in
+   arrival order while a slot is free and the estimated device footprint fits
+   the byte budget, advances all resident trajectories by up to `steps` steps
+   in one batch, and retires finished ones.  gbrpmd_server_poll returns
+   finished requests with status, seconds from submission to admission and to
+   completion, and last-step energies (v, vew, vlj, vint, tv). */
+typedef struct gb_server gb_server;
+int gbrpmd_server_create(gb_server **server, size_t budget_bytes, int max_slots);
+int gbrpmd_server_destroy(gb_server *server);
+int gbrpmd_server_submit(gb_server *server, int na, int nb, const gb_params *params, const double *mass,
+                         const double *z, const double *boxlxyz, double *r, double *p, double *dvdr,
+                         double *dvdr2, int forces_given, int nsteps, double dt, double beta, double thresh,
+                         int irun, int64_t *id);
+int gbrpmd_server_tick(gb_server *server, int steps);
+int gbrpmd_server_counts(gb_server *server, int *queued, int *active, int *finished, size_t *bytes_in_use);
+int gbrpmd_server_poll(gb_server *server, int max, int64_t *ids, int *status, double *t_admit,
+                       double *t_done, double *energies5, int *n);
 
 /* the md_eq step loop (md_eq.f90:182-323) on the device state: nsteps
    evolve_pi steps, each followed by the Andersen test ran2(irun) < thresh

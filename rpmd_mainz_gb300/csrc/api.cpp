@@ -12,6 +12,7 @@
 
 #include "gb_common.h"
 #include "gb_context.h"
+#include "gb_rng.h"
 
 namespace {
 
@@ -30,6 +31,7 @@ template <typename T>
 int dalloc(gb_context *c, T **p, size_t n) {
   CK(cudaMalloc((void **)p, sizeof(T) * (n ? n : 1)));
   c->allocs.push_back((void *)*p);
+  c->alloc_bytes += sizeof(T) * (n ? n : 1);
   return GB_OK;
 }
 
@@ -400,6 +402,12 @@ int gbrpmd_ctx_set_params(gb_context *c, const gb_params *params) {
   return GB_OK;
 }
 
+size_t gbrpmd_ctx_device_bytes(gb_context *c) { return c ? ctx_device_bytes(c) : 0; }
+
+size_t gbrpmd_estimate_device_bytes(int na, int nb, const gb_params *params) {
+  return params ? dev_estimate_bytes(na, nb, *params) : 0;
+}
+
 int gbrpmd_ctx_set_graphs(gb_context *c, int on) {
   if (!c) return ctx_set_error(GB_E_ARG, "null context");
   CK(cudaStreamSynchronize(c->stream));
@@ -440,63 +448,12 @@ int gbrpmd_ctx_region_times(gb_context *c, double *ms, double *units, int *count
 
 int64_t gbrpmd_ctx_launch_count(gb_context *c) { return c->launches; }
 
-// ---- serial random stream (random.f90:1-72) ----
-static struct {
-  int iv[32] = {0};
-  int iy = 0;
-  int idum2 = 123456789;
-  int iset = 0;
-  double gset = 0.0;
-} g_rng;
+// ---- serial random stream (random.f90:1-72), one process-wide state ----
+RngState g_rng;
 
-double gbrpmd_ran2(int *idum, const double *rmin, const double *rmax) {
-  const int im1 = 2147483563, im2 = 2147483399, imm1 = im1 - 1;
-  const int ia1 = 40014, ia2 = 40692, iq1 = 53668, iq2 = 52774, ir1 = 12211, ir2 = 3791;
-  const int ntab = 32, ndiv = 1 + imm1 / ntab;
-  const double am = 1.0 / im1, eps = 1.2e-7, rnmx = 1.0 - eps;
-  int k, j;
-  if (*idum <= 0) {
-    *idum = (-*idum) > 1 ? -*idum : 1;
-    g_rng.idum2 = *idum;
-    for (j = ntab + 8; j >= 1; --j) {
-      k = *idum / iq1;
-      *idum = ia1 * (*idum - k * iq1) - k * ir1;
-      if (*idum < 0) *idum += im1;
-      if (j <= ntab) g_rng.iv[j - 1] = *idum;
-    }
-    g_rng.iy = g_rng.iv[0];
-  }
-  k = *idum / iq1;
-  *idum = ia1 * (*idum - k * iq1) - k * ir1;
-  if (*idum < 0) *idum += im1;
-  k = g_rng.idum2 / iq2;
-  g_rng.idum2 = ia2 * (g_rng.idum2 - k * iq2) - k * ir2;
-  if (g_rng.idum2 < 0) g_rng.idum2 += im2;
-  j = 1 + g_rng.iy / ndiv;
-  g_rng.iy = g_rng.iv[j - 1] - g_rng.idum2;
-  g_rng.iv[j - 1] = *idum;
-  if (g_rng.iy < 1) g_rng.iy += imm1;
-  double u = am * g_rng.iy;
-  return ((*rmax - *rmin) * (u < rnmx ? u : rnmx)) + *rmin;
-}
+double gbrpmd_ran2(int *idum, const double *rmin, const double *rmax) { return rng_ran2(g_rng, idum, *rmin, *rmax); }
 
-double gbrpmd_gaussian(int *idum, const double *sigma) {
-  const double zero = 0.0, one = 1.0;
-  if (g_rng.iset == 0) {
-    double v1, v2, rsq;
-    do {
-      v1 = 2.0 * gbrpmd_ran2(idum, &zero, &one) - 1.0;
-      v2 = 2.0 * gbrpmd_ran2(idum, &zero, &one) - 1.0;
-      rsq = v1 * v1 + v2 * v2;
-    } while (rsq >= 1.0 || rsq == 0.0);
-    double fac = std::sqrt(-2.0 * std::log(rsq) / rsq);
-    g_rng.gset = v1 * fac;
-    g_rng.iset = 1;
-    return *sigma * v2 * fac;
-  }
-  g_rng.iset = 0;
-  return *sigma * g_rng.gset;
-}
+double gbrpmd_gaussian(int *idum, const double *sigma) { return rng_gaussian(g_rng, idum, *sigma); }
 
 }  // extern "C"
 

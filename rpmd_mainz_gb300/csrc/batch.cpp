@@ -11,8 +11,10 @@
 // performs any lazy set-up); the next one is captured; later steps replay.
 //
 // The Andersen test of md_eq (md_eq.f90:311-315) stays on the host: after each
-// step, every replica with thresh > 0 draws ran2 from its own stream and, on a
-// collision, momenta from sample_rpmd are copied in on the batch stream.
+// step, every replica with thresh > 0 draws ran2 from its own stream (its own
+// saved generator state, so that it is the stream the replica would draw
+// alone) and, on a collision, momenta from sample_rpmd are copied in on the
+// batch stream.
 //
 // Work runs on the batch stream: call gbrpmd_batch_sync before using a
 // replica's context directly (gbrpmd_ctx_sync, gbrpmd_ctx_download), and do
@@ -25,6 +27,7 @@
 
 #include "gb_common.h"
 #include "gb_context.h"
+#include "gb_rng.h"
 
 int ctx_set_error(int code, const std::string &msg);
 int ctx_check_cuda(cudaError_t e, const char *what);
@@ -35,6 +38,7 @@ struct gb_batch {
     double dt = 0, beta = 0, thresh = 0;
     int irun = 0;
     std::vector<double> hmass, hp;
+    RngState rng;  // this replica's ran2 / gaussian state
     cudaEvent_t join = nullptr;
     int64_t launches = 0;  // this replica's kernels in the captured step
     EnergyPlan plan;       // and its accumulator plan
@@ -77,13 +81,11 @@ int run_branches(gb_batch *b) {
 }
 
 int andersen(gb_batch *b) {
-  const double zero = 0.0, one = 1.0;
   for (auto &r : b->reps) {
     if (!(r.thresh > 0.0)) continue;
-    if (gbrpmd_ran2(&r.irun, &zero, &one) < r.thresh) {
+    if (rng_ran2(r.rng, &r.irun, 0.0, 1.0) < r.thresh) {
       r.hp.resize(3 * (size_t)r.c->na * r.c->nb);
-      int st = gbrpmd_sample_rpmd(r.hp.data(), r.c->na, r.c->nb, r.hmass.data(), r.beta, &r.irun);
-      if (st) return st;
+      rng_sample_rpmd(r.rng, r.hp.data(), r.c->na, r.c->nb, r.hmass.data(), r.beta, &r.irun);
       BCK(cudaMemcpyAsync(r.c->p, r.hp.data(), sizeof(double) * r.hp.size(), cudaMemcpyHostToDevice, b->s0));
       BCK(cudaStreamSynchronize(b->s0));  // hp is reused at the next collision
     }

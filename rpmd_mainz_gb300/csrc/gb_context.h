@@ -110,7 +110,7 @@ struct gb_context {
 
   int64_t launches = 0;
   std::vector<void *> allocs;
-
+  size_t alloc_bytes = 0;  // bytes of `allocs`
   // the evolve step as a CUDA graph (dev_step): captured on the second step
   // with an unchanged key, replayed while the key holds
   struct StepGraph {
@@ -167,6 +167,8 @@ int dev_full_forces(gb_context *c);                      // dvdr, dvdr2 from r
 int dev_evolve_pi(gb_context *c, double dt, double beta);
 // one evolve_pi step, replayed from a captured CUDA graph when it can be
 int dev_step(gb_context *c, double dt, double beta);
+size_t dev_estimate_bytes(int na, int nb, const gb_params &P);
+size_t ctx_device_bytes(const gb_context *c);  // device bytes the context holds now
 void dev_graph_reset(gb_context *c);
 int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt);  // drop-in `forces`
 int dev_collect(gb_context *c, int mode, double dt, double beta);  // sync, read accumulators

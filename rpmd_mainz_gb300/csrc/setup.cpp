@@ -13,9 +13,10 @@
 
 #include "gb_common.h"
 #include "gb_context.h"
+#include "gb_rng.h"
 
 extern "C" double gbrpmd_ran2(int *idum, const double *rmin, const double *rmax);
-extern "C" double gbrpmd_gaussian(int *idum, const double *sigma);
+extern RngState g_rng;  // api.cpp
 const gb_params &current_params();
 
 extern "C" {
@@ -90,34 +91,7 @@ int gbrpmd_setup_ewald(int na, const double *boxlxyz, gb_params *P) {
 }
 
 int gbrpmd_sample_rpmd(double *p, int na, int nb, const double *mass, double beta, int *irun) {
-  const double betan = beta / (double)nb;
-  for (int k = 0; k < nb; ++k)
-    for (int j = 0; j < na; ++j)
-      for (int l = 0; l < 3; ++l) {
-        double sigma = std::sqrt(mass[j] / betan);
-        p[l + 3 * ((size_t)j + (size_t)na * k)] = gbrpmd_gaussian(irun, &sigma);
-      }
-  // pshift
-  double vx = 0.0, vy = 0.0, vz = 0.0, totmass = 0.0;
-  for (int j = 0; j < na; ++j) totmass = totmass + mass[j];
-  totmass = (double)nb * totmass;
-  for (int k = 0; k < nb; ++k)
-    for (int j = 0; j < na; ++j) {
-      const double *q = p + 3 * ((size_t)j + (size_t)na * k);
-      vx = vx + q[0];
-      vy = vy + q[1];
-      vz = vz + q[2];
-    }
-  vx = vx / totmass;
-  vy = vy / totmass;
-  vz = vz / totmass;
-  for (int k = 0; k < nb; ++k)
-    for (int j = 0; j < na; ++j) {
-      double *q = p + 3 * ((size_t)j + (size_t)na * k);
-      q[0] = q[0] - mass[j] * vx;
-      q[1] = q[1] - mass[j] * vy;
-      q[2] = q[2] - mass[j] * vz;
-    }
+  rng_sample_rpmd(g_rng, p, na, nb, mass, beta, irun);
   return GB_OK;
 }
 

@@ -786,3 +786,51 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
   (void)mode;
   return GB_OK;
 }
+
+// Device bytes a context of (na, nb) with parameters P holds once it has run
+// evolve_pi: the arrays of ctx_alloc, the k-space tables (build_kvectors) and
+// the exact and skin pair lists of the Ewald, LJ and TEM terms (make_list, skin
+// 0.1), plus a tenth for allocation granularity and small tables.  Used to admit
+// batch replicas by memory footprint before anything is allocated.
+size_t dev_estimate_bytes(int na, int nb, const gb_params &P) {
+  const size_t N = 3 * (size_t)na * nb, nm = na / 3;
+  size_t b = sizeof(double) * (15 * N + 5 * (size_t)na + 12 * (size_t)nb + ACC_NSLOT * ACC_STRIDE);
+  b += sizeof(float4) * (2 * (size_t)na * nb + 2 * nm * nb);
+  const int kmax = std::max(P.kmax, 0);
+  const int cap_col = gb_kcap_col(kmax), cap_kp = gb_kcap_kp(kmax);
+  std::vector<KCol> col(cap_col);
+  std::vector<int4> kp(cap_kp), grp(cap_kp);
+  std::vector<double> kw(cap_kp);
+  KTables t;
+  if (!gb_build_ktables(P, recip_group_len(), col.data(), cap_col, kp.data(), kw.data(), cap_kp, grp.data(),
+                        cap_kp, &t)) {
+    const size_t nc = std::max(nb, 1), nchunk = (na + recip_sk_chunk() - 1) / recip_sk_chunk();
+    b += sizeof(double2) * 3 * (size_t)(kmax + 1) * na * nc;
+    b += sizeof(double) * (4 * (size_t)std::max(t.nkp, 1) * nchunk + 8 * (size_t)t.nkp) * nc;
+    b += sizeof(KCol) * t.ncol + sizeof(int4) * (t.ngrp + t.nkp) + sizeof(double) * t.nkp;
+  }
+  // pair lists: one exact list sized for the largest term, one skin list per term
+  size_t exact = 0;
+  auto lists = [&](size_t nconf, int npt, double cut, double vol) {
+    const size_t cap = list_cap(npt, cut, vol), scap = list_cap(npt, 1.1 * cut, vol);
+    exact = std::max(exact, sizeof(int) * nconf * npt * (cap + 1));
+    return sizeof(int) * nconf * npt * (scap + 1) + sizeof(double) * 3 * nconf * npt;
+  };
+  // the LJ and TEM cut-offs are in bohr: the box holds nm molecules at the
+  // density of liquid water, 29.9 A^3 each
+  const double vol = (double)nm * 29.9 / (0.5291772108 * 0.5291772108 * 0.5291772108);
+  const size_t bew = (nb > 1 && P.nbdf1 > 0) ? P.nbdf1 : nb;
+  const size_t blj = (nb > 1 && P.nbdf2 > 0) ? P.nbdf2 : nb;
+  b += lists(bew, na, P.wrcut, 1.0);
+  b += lists(blj > 3 ? 1 : blj, (int)nm, P.rcut, vol);
+  if (P.sig > 0.0) b += lists(1, na, P.sig + 5.0, vol);
+  b += exact;
+  return b + b / 10;
+}
+
+size_t ctx_device_bytes(const gb_context *c) {
+  size_t b = c->alloc_bytes + c->ktab_bytes + c->sk_part_bytes + c->sk_bytes + c->pl_idx_bytes + c->pl_cnt_bytes;
+  b += sizeof(KCol) * c->ncol + sizeof(int4) * (c->ngrp + c->nkp) + sizeof(double) * c->nkp;
+  for (const SkinList &L : c->sl) b += L.idx_bytes + L.cnt_bytes + L.ref_bytes;
+  return b;
+}

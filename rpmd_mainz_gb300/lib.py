@@ -82,6 +82,19 @@ def load(path=None):
     lib.gbrpmd_batch_sync.argtypes = [C.c_void_p]
     lib.gbrpmd_batch_stream.restype = C.c_void_p
     lib.gbrpmd_batch_stream.argtypes = [C.c_void_p]
+    lib.gbrpmd_ctx_device_bytes.restype = C.c_size_t
+    lib.gbrpmd_ctx_device_bytes.argtypes = [C.c_void_p]
+    lib.gbrpmd_estimate_device_bytes.restype = C.c_size_t
+    lib.gbrpmd_estimate_device_bytes.argtypes = [C.c_int, C.c_int, C.c_void_p]
+    lib.gbrpmd_server_create.argtypes = [C.POINTER(C.c_void_p), C.c_size_t, C.c_int]
+    lib.gbrpmd_server_destroy.argtypes = [C.c_void_p]
+    lib.gbrpmd_server_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, D, D, D, D, D, D, D, C.c_int,
+                                         C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_int64)]
+    lib.gbrpmd_server_tick.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_server_counts.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_size_t)]
+    lib.gbrpmd_server_poll.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int), D, D, D,
+                                       C.POINTER(C.c_int)]
     _lib = lib
     return lib
 
@@ -273,6 +286,10 @@ class Context:
                                        None if e is None else _ptr(e)))
         return None if e is None else e.reshape(nsteps, 4)
 
+    @property
+    def device_bytes(self):
+        return load().gbrpmd_ctx_device_bytes(self.h)
+
     def set_graphs(self, on):
         """CUDA-graph replay of evolve steps (on by default)."""
         _check(load().gbrpmd_ctx_set_graphs(self.h, 1 if on else 0))
@@ -324,6 +341,70 @@ class Batch:
     def close(self):
         if self.h:
             load().gbrpmd_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def estimate_device_bytes(na, nb, params):
+    return load().gbrpmd_estimate_device_bytes(na, nb, C.byref(params))
+
+
+class Server:
+    """Continuous batching of trajectory requests with resident device state."""
+
+    def __init__(self, budget_bytes, max_slots):
+        self.h = C.c_void_p()
+        self.keep = {}
+        _check(load().gbrpmd_server_create(C.byref(self.h), int(budget_bytes), int(max_slots)))
+
+    def submit(self, system, r, p, nsteps, dvdr=None, dvdr2=None, thresh=0.0, irun=0, params=None,
+               dt=None, beta=None):
+        """Queue a trajectory.  r, p (and dvdr, dvdr2; without them the server
+        computes the starting forces) are copied; poll() hands back the final state."""
+        s = system
+        prm = params if params is not None else s["params"]
+        given = dvdr is not None
+        arrs = dict(r=_arr(r).copy(), p=_arr(p).copy(), mass=_arr(s["mass"]), z=_arr(s["z"]), box=_arr(s["box"]),
+                    dvdr=_arr(dvdr).copy() if given else np.zeros_like(_arr(r)),
+                    dvdr2=_arr(dvdr2).copy() if given else np.zeros_like(_arr(r)), params=prm)
+        rid = C.c_int64()
+        _check(load().gbrpmd_server_submit(self.h, s["na"], s["nb"], C.byref(prm), _ptr(arrs["mass"]), _ptr(arrs["z"]),
+                                           _ptr(arrs["box"]), _ptr(arrs["r"]), _ptr(arrs["p"]), _ptr(arrs["dvdr"]),
+                                           _ptr(arrs["dvdr2"]), 1 if given else 0, int(nsteps),
+                                           s["dt"] if dt is None else dt, s["beta"] if beta is None else beta,
+                                           thresh, irun, C.byref(rid)))
+        self.keep[rid.value] = arrs
+        return rid.value
+
+    def tick(self, steps=1):
+        _check(load().gbrpmd_server_tick(self.h, int(steps)))
+
+    def counts(self):
+        q, a, f, b = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+        _check(load().gbrpmd_server_counts(self.h, C.byref(q), C.byref(a), C.byref(f), C.byref(b)))
+        return dict(queued=q.value, active=a.value, finished=f.value, bytes=b.value)
+
+    def poll(self, max_n=1024):
+        ids = (C.c_int64 * max_n)()
+        st = (C.c_int * max_n)()
+        ta, td, en = np.zeros(max_n), np.zeros(max_n), np.zeros(5 * max_n)
+        n = C.c_int()
+        _check(load().gbrpmd_server_poll(self.h, max_n, ids, st, _ptr(ta), _ptr(td), _ptr(en), C.byref(n)))
+        out = []
+        for i in range(n.value):
+            arrs = self.keep.pop(ids[i])
+            out.append(dict(id=ids[i], status=st[i], t_admit=ta[i], t_done=td[i], energies=en[5 * i:5 * i + 5].copy(),
+                            r=arrs["r"], p=arrs["p"], dvdr=arrs["dvdr"], dvdr2=arrs["dvdr2"]))
+        return out
+
+    def close(self):
+        if self.h:
+            load().gbrpmd_server_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

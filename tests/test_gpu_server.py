@@ -1,0 +1,127 @@
+"""Serving loop (gbrpmd_server_*): continuous batching of trajectory requests.
+
+Requests arrive while others run, are admitted by their estimated device
+footprint, share batch steps, and leave when done.  Each served result must
+equal the same request run alone on its own context: 1e-11 relative for FP64
+requests, 1e-6 for mixed-precision ones (the order of FP32 sums follows the
+pair-list order, which varies between runs).
+"""
+import numpy as np
+import pytest
+
+from rpmd_mainz_gb300 import lib
+
+from . import systems
+
+pytestmark = pytest.mark.gpu
+
+REQUESTS = [
+    (dict(param="param_qspcfw", ncell=(4, 4, 4), nb=8, mts=1, dtfs=0.5, temp=250.0), 9),
+    (dict(param="param_qspcfw", ncell=(3, 3, 3), nb=16, mts=5, dtfs=1.25, nbdf1=1, nbdf2=5, temp=320.0), 4),
+    (dict(param="param_qspcfw", ncell=(5, 5, 5), nb=4, mts=2, dtfs=1.0, temp=300.0), 7),
+    (dict(param="param_qspcfw", ncell=(4, 4, 4), nb=32, mts=1, dtfs=0.5, temp=280.0, precision=1), 5),
+    (dict(param="param_qspcfw", ncell=(3, 3, 3), nb=8, mts=1, dtfs=0.5, temp=350.0), 6),
+]
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    yield
+    lib.finalize()
+
+
+def request_state(case, seed):
+    s = systems.build(**case)
+    lib.init(s["params"])
+    r = systems.perturbed(s, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    p = rng.normal(size=r.shape) * np.sqrt(s["mass"][None, :, None] / (s["beta"] / s["nb"]))
+    return s, r, p
+
+
+def run_alone(s, r, p, nsteps):
+    ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+    ctx.set_params(s["params"])
+    ctx.upload(r=r, p=p, box=s["box"])
+    ctx.full_forces()
+    ctx.evolve(nsteps, s["dt"], s["beta"])
+    ctx.sync()
+    out = ctx.download()
+    ctx.close()
+    return out
+
+
+def test_served_results_equal_alone():
+    reqs = [(case, n) + request_state(case, 500 + 7 * i) for i, (case, n) in enumerate(REQUESTS)]
+    alone = [run_alone(s, r, p, n) for case, n, s, r, p in reqs]
+    srv = lib.Server(budget_bytes=8 << 30, max_slots=3)
+    ids = {}
+    arrivals = {0: [0, 1], 2: [2], 3: [3, 4]}  # tick -> requests arriving
+    finished = {}
+    tick = 0
+    while len(finished) < len(reqs):
+        for k in arrivals.get(tick, []):
+            case, n, s, r, p = reqs[k]
+            ids[srv.submit(s, r, p, n)] = k
+        c = srv.counts()
+        assert c["active"] <= 3
+        srv.tick(2)
+        for res in srv.poll():
+            assert res["status"] == 0
+            finished[ids[res["id"]]] = res
+        tick += 1
+        assert tick < 100
+    for k, res in finished.items():
+        tol = 1e-6 if reqs[k][0].get("precision", 0) else 1e-11
+        for got, want in zip((res["r"], res["p"], res["dvdr"], res["dvdr2"]), alone[k]):
+            assert rel(got, want) < tol, k
+        assert res["t_done"] >= res["t_admit"] >= 0.0
+    srv.close()
+
+
+def test_admission_respects_memory_budget():
+    case = dict(param="param_qspcfw", ncell=(4, 4, 4), nb=8, mts=1, dtfs=0.5)
+    s, r, p = request_state(case, 600)
+    need = lib.estimate_device_bytes(s["na"], s["nb"], s["params"])
+    srv = lib.Server(budget_bytes=2 * need + need // 2, max_slots=8)  # room for two at a time
+    for _ in range(5):
+        srv.submit(s, r, p, 3)
+    done = 0
+    peak = 0
+    for _ in range(50):
+        srv.tick(1)
+        c = srv.counts()
+        peak = max(peak, c["active"])
+        assert c["active"] <= 2 and c["bytes"] <= 2 * need + need // 2
+        done += len(srv.poll())
+        if done == 5:
+            break
+    assert done == 5 and peak == 2
+    srv.close()
+
+
+@pytest.mark.parametrize("case", [
+    dict(param="param_qspcfw", ncell=(8, 8, 8), nb=16, mts=1, dtfs=0.5),
+    dict(param="param_qspcfw", ncell=(8, 8, 8), nb=32, mts=5, dtfs=1.25, nbdf1=1, nbdf2=5),
+])
+def test_footprint_estimate(case):
+    """The admission estimate covers what a context allocates by its second
+    step and overshoots it by less than a factor 1.6."""
+    s, r, p = request_state(case, 700)
+    est = lib.estimate_device_bytes(s["na"], s["nb"], s["params"])
+    ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+    ctx.set_params(s["params"])
+    ctx.upload(r=r, p=p, box=s["box"])
+    ctx.full_forces()
+    ctx.evolve(2, s["dt"], s["beta"])
+    ctx.sync()
+    used = ctx.device_bytes
+    ctx.close()
+    assert used <= est <= 1.6 * used, (used, est)
