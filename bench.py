@@ -44,6 +44,8 @@ WORKLOADS = {
     "qspcfw_216_nb32": dict(ncell=(6, 6, 6), nb=32, mts=1, dtfs=0.5),
 }
 DEFAULT = "qspcfw_4096_nb32_mts5_contracted"
+# multi-trajectory workloads (rpmd_mainz_gb300/workloads.py)
+BATCH_WORKLOADS = ("replicas_256", "served_stream")
 REGIONS = ["mts_block", "pair_lists", "ewald_real", "recip_sk", "recip_weights", "recip_force", "lj",
            "tem", "expand_kick", "msite", "rattle"]
 # algorithmic FP64 flops per work unit of a region (declared weights):
@@ -342,13 +344,163 @@ def force_error(s):
             "virial_rel": rel(fmx["vir"], f64["vir"]), "bound": 1e-5}
 
 
+def run_replicas(args, torch):
+    """256 independent NVT replicas (molecules in {64, 216, 343, 512}, nb in
+    {8, 16, 32, 64}, T in [250, 350] K, Andersen thresh 0.01, dt 0.5 fs): the
+    mixed-precision batch (one CUDA-graph launch per step for all replicas)
+    against the plain-FP64 contexts stepped in a loop (each on its own stream,
+    all synchronised once per step)."""
+    from rpmd_mainz_gb300 import lib, workloads
+
+    reps = workloads.replica_set(n=args.replicas, precision=1)
+    lib.init(reps[0]["params"])
+    work = sum(s["nb"] * s["nm"] for s in reps)
+
+    def contexts(prec):
+        out = []
+        for s in reps:
+            prm = s["params"].copy()
+            prm.precision = prec
+            ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+            ctx.set_params(prm)
+            ctx.upload(r=s["r"], p=s["p"], box=s["box"])
+            ctx.full_forces()
+            out.append(ctx)
+        return out
+
+    # mixed-precision batch
+    ctxs = contexts(1)
+    batch = lib.Batch()
+    for i, (s, ctx) in enumerate(zip(reps, ctxs)):
+        batch.add(ctx, s["dt"], s["beta"], 0.01, -(5000 + i))
+    stream = torch.cuda.ExternalStream(batch.stream)
+    batch.step(args.warmup)
+    batch.sync()
+    step_ms = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            batch.step(1)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    batch.sync()
+    value = args.steps * work / (sum(step_ms) * 1e-3)
+    evolved = [c.download()[0] for c in ctxs[:8]]  # configurations for the force-error check
+    batch.close()
+    for c in ctxs:
+        c.close()
+    # plain-FP64 loop over the same replicas
+    ctxs = contexts(0)
+    for c, s in zip(ctxs, reps):
+        c.evolve(args.warmup, s["dt"], s["beta"])
+    for c in ctxs:
+        c.sync()
+    loop_ms = []
+    for _ in range(max(2, args.steps // 4)):
+        t0 = time.perf_counter()
+        for c, s in zip(ctxs, reps):
+            c.evolve(1, s["dt"], s["beta"])
+        for c in ctxs:
+            c.sync()
+        loop_ms.append(1e3 * (time.perf_counter() - t0))
+    fp64_value = len(loop_ms) * work / (sum(loop_ms) * 1e-3)
+    for c in ctxs:
+        c.close()
+    # force error of the mixed path on the first eight replicas' evolved
+    # configurations (the starting lattices are symmetric: forces nearly cancel)
+    errs = []
+    for s, r in zip(reps[:8], evolved):
+        out = []
+        for prec in (0, 1):
+            prm = s["params"].copy()
+            prm.precision = prec
+            lib.init(prm)
+            out.append(lib.full_forces(r, s["box"], s["z"]))
+        f64, fmx = out
+        tot64 = f64["dvdr"] + f64["dvdr2"]
+        errs.append(float(np.linalg.norm(fmx["dvdr"] + fmx["dvdr2"] - tot64) / np.linalg.norm(tot64)))
+    return {
+        "metric": "bead-molecule-steps/s", "value": value, "unit": "bead-molecule-steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 mixed",
+        "data": "synthetic (CUB lattices, momenta from the reference's ran2 stream, seeded per replica)",
+        "config": {"workload": "replicas_256", "replicas": len(reps), "bead_molecules_per_step": work,
+                   "sizes": "nm in {64,216,343,512}, nb in {8,16,32,64}, T in [250,350] K",
+                   "l2": "inputs larger than L2 in aggregate", "parallelism": "one batch, one graph per step"},
+        "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
+        "fp64_loop": {"value": fp64_value, "ms_per_step": float(np.mean(loop_ms))},
+        "batched_mixed_over_fp64_loop": value / fp64_value,
+        "error_vs_fp64": {"force_rel_rms_max_of_8": max(errs), "bound": 1e-5,
+                          "on": "the first 8 replicas after the timed steps"},
+        "clocks": clk.summary(),
+    }
+
+
+def run_served(args, torch):
+    """Poisson arrivals (mean 50 per second) of trajectory requests of mixed
+    sizes (64-1728 molecules, nb 4-64), each `--request-steps` evolve_pi steps,
+    served by the continuous-batching loop under a device-memory budget."""
+    from rpmd_mainz_gb300 import lib, workloads
+
+    stream = workloads.request_stream(n=args.requests, nsteps=args.request_steps)
+    lib.init(stream[0][1]["params"])
+    work = sum(s["nb"] * s["nm"] * n for _, s, n in stream)
+    srv = lib.Server(budget_bytes=args.budget_gb << 30, max_slots=args.slots)
+    t0 = time.perf_counter()
+    nxt = 0
+    done = []
+    shape = {}
+    with ClockSampler(0) as clk:
+        while len(done) < len(stream):
+            now = time.perf_counter() - t0
+            while nxt < len(stream) and stream[nxt][0] <= now:
+                _, s, n = stream[nxt]
+                shape[srv.submit(s, s["r"], s["p"], n)] = (s["nm"], s["nb"])
+                nxt += 1
+            c = srv.counts()
+            if c["active"] == 0 and c["queued"] == 0:
+                time.sleep(max(0.0, min(0.01, stream[nxt][0] - now)) if nxt < len(stream) else 0.0)
+                continue
+            srv.tick(args.tick_steps)
+            for res in srv.poll():
+                if res["status"] != 0:
+                    raise RuntimeError(f"request {res['id']} (nm, nb = {shape[res['id']]}) ended with status "
+                                       f"{res['status']}: {lib.last_error()}")
+                done.append(res)
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = np.array([d["t_done"] for d in done])
+    wait = np.array([d["t_admit"] for d in done])
+    return {
+        "metric": "bead-molecule-steps/s", "value": work / wall, "unit": "bead-molecule-steps/s", "n_gpus": 1,
+        "steps": args.request_steps, "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 mixed", "data": "synthetic request stream (seeded Poisson arrivals, CUB lattices)",
+        "config": {"workload": "served_stream", "requests": len(stream), "arrival_rate_per_s": 50.0,
+                   "steps_per_request": args.request_steps, "tick_steps": args.tick_steps, "slots": args.slots,
+                   "budget_gib": args.budget_gb, "sizes": "nm in 64..1728 (cubic lattices), nb in {4,8,16,32,64}"},
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "queue_wait_p50": float(np.percentile(wait, 50)), "queue_wait_p99": float(np.percentile(wait, 99))},
+        "wall_s": wall, "clocks": clk.summary(),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS) + list(BATCH_WORKLOADS))
+    ap.add_argument("--replicas", type=int, default=256)
+    ap.add_argument("--requests", type=int, default=60)
+    ap.add_argument("--request-steps", type=int, default=100)
+    ap.add_argument("--tick-steps", type=int, default=10)
+    ap.add_argument("--slots", type=int, default=32)
+    ap.add_argument("--budget-gb", type=int, default=64)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -369,6 +521,12 @@ def main():
     import __graft_entry__ as g
 
     g.build()
+
+    if args.workload in BATCH_WORKLOADS:
+        if rank == 0:
+            out = run_replicas(args, torch) if args.workload == "replicas_256" else run_served(args, torch)
+            print(json.dumps(out), flush=True)
+        return 0
 
     s = make_system(args.workload)
     prec = 1 if args.precision == "mixed" else 0

@@ -250,6 +250,9 @@ int gbrpmd_ctx_region_times(gb_context *ctx, double *ms, double *units, int *cou
 int gbrpmd_ctx_set_list_skin(gb_context *ctx, double fraction);
 /* rebuilds of the three skin lists since the context was created (synchronises) */
 int gbrpmd_ctx_list_rebuilds(gb_context *ctx, unsigned *counts3);
+/* diagnostics (synchronises): longest list and capacity of the Ewald, LJ and
+   TEM skin lists and of the exact list last built, as 4 (max, cap) pairs */
+int gbrpmd_ctx_list_occupancy(gb_context *ctx, int *out8);
 /* CUDA-graph replay of gbrpmd_ctx_evolve / gbrpmd_evolve_pi steps (no counterpart
    in the reference): on by default (environment GBRPMD_GRAPHS=0 turns it off);
    the second step with unchanged parameters, dt, beta and box is captured and

@@ -13,6 +13,7 @@
 #include "gb_common.h"
 #include "gb_context.h"
 #include "gb_rng.h"
+#include "gb_kernels.h"
 
 namespace {
 
@@ -408,6 +409,18 @@ size_t gbrpmd_estimate_device_bytes(int na, int nb, const gb_params *params) {
   return params ? dev_estimate_bytes(na, nb, *params) : 0;
 }
 
+int gbrpmd_ctx_list_occupancy(gb_context *c, int *out8) {
+  if (!c || !out8) return ctx_set_error(GB_E_ARG, "null argument");
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < LIST_N; ++i) {
+    out8[2 * i] = list_max(c->stream, c->sl[i].pl);
+    out8[2 * i + 1] = c->sl[i].pl.cap;
+  }
+  out8[6] = list_max(c->stream, c->pl);
+  out8[7] = c->pl.cap;
+  return GB_OK;
+}
+
 int gbrpmd_ctx_set_graphs(gb_context *c, int on) {
   if (!c) return ctx_set_error(GB_E_ARG, "null context");
   CK(cudaStreamSynchronize(c->stream));
@@ -421,7 +434,10 @@ int gbrpmd_ctx_list_rebuilds(gb_context *c, unsigned *counts3) {
   CK(cudaStreamSynchronize(c->stream));
   for (int i = 0; i < LIST_N; ++i) {
     counts3[i] = 0;
-    if (c->sl[i].rebuilds) CK(cudaMemcpy(&counts3[i], c->sl[i].rebuilds, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (c->sl[i].rebuilds) {
+      CK(cudaMemcpyAsync(&counts3[i], c->sl[i].rebuilds, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    }
   }
   return GB_OK;
 }

@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -50,6 +51,7 @@ struct gb_batch {
   bool valid = false;
   int seen = 0;
   int64_t steps = 0;
+  bool graphs = true;  // GBRPMD_BATCH_GRAPHS=0: every step as ordinary launches
 };
 
 namespace {
@@ -105,6 +107,7 @@ int gbrpmd_batch_create(gb_batch **out) {
     delete b;
     return ctx_set_error(GB_E_CUDA, "batch stream or event creation failed");
   }
+  if (const char *e = std::getenv("GBRPMD_BATCH_GRAPHS")) b->graphs = e[0] != '0';
   *out = b;
   return GB_OK;
 }
@@ -136,7 +139,8 @@ int gbrpmd_batch_add(gb_batch *b, gb_context *c, double dt, double beta, double 
   r.irun = irun;
   if (thresh > 0.0) {
     r.hmass.resize(c->na);
-    BCK(cudaMemcpy(r.hmass.data(), c->mass, sizeof(double) * c->na, cudaMemcpyDeviceToHost));
+    BCK(cudaMemcpyAsync(r.hmass.data(), c->mass, sizeof(double) * c->na, cudaMemcpyDeviceToHost, c->stream));
+    BCK(cudaStreamSynchronize(c->stream));
   }
   BCK(cudaEventCreateWithFlags(&r.join, cudaEventDisableTiming));
   b->reps.push_back(std::move(r));
@@ -174,7 +178,7 @@ int gbrpmd_batch_step(gb_batch *b, int nsteps) {
         r.c->launches += r.launches;
         r.c->plan = r.plan;
       }
-    } else if (b->seen < 1) {
+    } else if (b->seen < 1 || !b->graphs) {
       int st = run_branches(b);
       if (st) return st;
       b->seen += 1;

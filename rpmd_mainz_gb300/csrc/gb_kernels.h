@@ -48,6 +48,7 @@ void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref,
 void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
                         const PairList &skin, PairList &pl, unsigned *status);
 double list_total(cudaStream_t s, const PairList &pl);  // profiling only (synchronises)
+int list_max(cudaStream_t s, const PairList &pl);       // diagnostics only (synchronises)
 
 // ---- Ewald, unit box (k_pairs.cu, k_recip.cu) ----
 // rs: M-site substituted positions scaled by 1/L, [B][na][3]

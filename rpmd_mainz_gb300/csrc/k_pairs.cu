@@ -498,9 +498,30 @@ __global__ void k_sum_counts(const int *count, long long n, unsigned long long *
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(out, v);
 }
 
+__global__ void k_max_count(const int *count, long long n, int *out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int v = t < n ? count[t] : 0;
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(out, v);
+}
+
 inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
+
+// longest list (diagnostics only: synchronises the stream)
+int list_max(cudaStream_t s, const PairList &pl) {
+  if (!pl.count || pl.nconf <= 0 || pl.npt <= 0) return 0;
+  int *d = nullptr, h = 0;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return -1;
+  cudaMemsetAsync(d, 0, sizeof(int), s);
+  long long n = (long long)pl.nconf * pl.npt;
+  k_max_count<<<nblk(n, 256), 256, 0, s>>>(pl.count, n, d);
+  cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  cudaFree(d);
+  return h;
+}
 
 // total entries of a pair list (profiling only: synchronises the stream)
 double list_total(cudaStream_t s, const PairList &pl) {

@@ -321,8 +321,8 @@ int ws_ensure(int nm) {
   CK(cudaMalloc(&g_ws.rec, sizeof(double) * 8 * (size_t)nm));
   CK(cudaMalloc(&g_ws.vir, sizeof(double) * 9));
   CK(cudaMalloc(&g_ws.status, sizeof(unsigned)));
-  CK(cudaMemset(g_ws.status, 0, sizeof(unsigned)));
   if (!g_ws.s) CK(cudaStreamCreateWithFlags(&g_ws.s, cudaStreamNonBlocking));
+  CK(cudaMemsetAsync(g_ws.status, 0, sizeof(unsigned), g_ws.s));
   g_ws.nm = nm;
   return GB_OK;
 }
@@ -353,7 +353,7 @@ int rattle_dropin(int stage, double *r, const double *rold, double *p, int nm, c
   CK(cudaMemcpyAsync(&stw, g_ws.status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (stw) {
-    CK(cudaMemset(g_ws.status, 0, sizeof(unsigned)));
+    CK(cudaMemsetAsync(g_ws.status, 0, sizeof(unsigned), g_ws.s));
     return stage == 1 ? ctx_set_error(GB_E_RATTLE1, "max iterations exceeded in rattle stage 1")
                       : ctx_set_error(GB_E_RATTLE2, "max iterations exceeded in rattle stage 2");
   }
@@ -389,7 +389,8 @@ int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) 
   const long long N = 3LL * c->na * nb;
   cudaStream_t s = c->stream;
   double mass3h[3];
-  CK(cudaMemcpy(mass3h, c->mass, sizeof(double) * 3, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(mass3h, c->mass, sizeof(double) * 3, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   RatPar rp = make_rp(c->P, mass3h);
   const double halfdt = 0.5 * dt, smalldt = dt / (double)nb;
   double omegan = nb / (beta * 1.0);

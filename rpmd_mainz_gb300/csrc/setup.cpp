@@ -106,7 +106,8 @@ int gbrpmd_run_md_eq(gb_context *c, int nsteps, double dt, double beta, double t
   std::vector<double> hmass, hp;
   if (P.therm == GB_THERM_AND) {
     hmass.resize(c->na);
-    if (cudaMemcpy(hmass.data(), c->mass, sizeof(double) * c->na, cudaMemcpyDeviceToHost) != cudaSuccess)
+    if (cudaMemcpyAsync(hmass.data(), c->mass, sizeof(double) * c->na, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
       return ctx_set_error(GB_E_CUDA, "mass download failed");
   }
   const double zero = 0.0, one = 1.0;

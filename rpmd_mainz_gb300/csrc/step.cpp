@@ -119,10 +119,14 @@ int build_kvectors(gb_context *c) {
   CK(cudaMalloc(&c->ktab, c->ktab_bytes));
   CK(cudaMalloc(&c->sk_part, c->sk_part_bytes));
   CK(cudaMalloc(&c->sk, c->sk_bytes));
-  CK(cudaMemcpy(c->kcol, col.data(), sizeof(KCol) * t.ncol, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c->kgrp, grp.data(), sizeof(int4) * t.ngrp, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c->kpair, kp.data(), sizeof(int4) * t.nkp, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c->kw, kw.data(), sizeof(double) * t.nkp, cudaMemcpyHostToDevice));
+  // set-up copies go on the context's (non-blocking) stream and complete before
+  // return: a plain cudaMemcpy from pageable memory may return before its DMA
+  // lands and is not ordered with that stream's kernels
+  CK(cudaMemcpyAsync(c->kcol, col.data(), sizeof(KCol) * t.ncol, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->kgrp, grp.data(), sizeof(int4) * t.ngrp, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->kpair, kp.data(), sizeof(int4) * t.nkp, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->kw, kw.data(), sizeof(double) * t.nkp, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   recip_set_attributes();
   c->kmax_alloc = kmax;
   c->k_rkmax = c->P.rkmax;
@@ -527,10 +531,12 @@ int dev_prepare(gb_context *c, double dt, double beta) {
   }
   if (dt > 0.0 && (dt != c->monod_dt || beta != c->monod_beta)) {
     double mass3[3];
-    CK(cudaMemcpy(mass3, c->mass, sizeof(double) * 3, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(mass3, c->mass, sizeof(double) * 3, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     std::vector<double> monod(12 * (size_t)c->nb);
     ring_rpmd_host(mass3, c->nb, dt / (double)c->P.mts, beta, monod.data());
-    CK(cudaMemcpy(c->monod, monod.data(), sizeof(double) * monod.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(c->monod, monod.data(), sizeof(double) * monod.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));  // monod is a local vector
     c->monod_dt = dt;
     c->monod_beta = beta;
   }

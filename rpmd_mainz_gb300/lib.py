@@ -70,6 +70,7 @@ def load(path=None):
     lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
     lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
     lib.gbrpmd_ctx_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_ctx_list_occupancy.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     lib.gbrpmd_ctx_set_params.argtypes = [C.c_void_p, C.c_void_p]
     lib.gbrpmd_run_md_eq.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int),
                                      C.c_void_p]
@@ -122,6 +123,11 @@ def get_params() -> GbParams:
     p = GbParams()
     _check(load().gbrpmd_get_params(C.byref(p)))
     return p
+
+
+def last_error():
+    """Message of the library's last error."""
+    return load().gbrpmd_last_error().decode()
 
 
 def finalize():
@@ -289,6 +295,12 @@ class Context:
     @property
     def device_bytes(self):
         return load().gbrpmd_ctx_device_bytes(self.h)
+
+    def list_occupancy(self):
+        """(max, cap) of the Ewald, LJ and TEM skin lists and of the exact list."""
+        out = (C.c_int * 8)()
+        _check(load().gbrpmd_ctx_list_occupancy(self.h, out))
+        return {k: (out[2 * i], out[2 * i + 1]) for i, k in enumerate(("ewald", "lj", "tem", "exact"))}
 
     def set_graphs(self, on):
         """CUDA-graph replay of evolve steps (on by default)."""

@@ -1,0 +1,58 @@
+"""Synthetic multi-trajectory workloads: replica sets and request streams.
+
+Each system is a q-SPC/Fw water box on the reference's CUB lattice at
+0.997 g/cm^3 (main.f90 set-up through `system.water_box`), with momenta drawn
+from the reference's ran2/gaussian stream seeded per system.  Only cubic
+lattices are used: the device Ewald sum is the cubic one, so molecule counts
+that need an anisotropic lattice (128 = 8 x 4 x 4) are left out.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import system
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PARAM_QSPCFW = os.path.join(os.path.dirname(HERE), "tests", "golden", "params", "param_qspcfw")
+
+CUBIC_CELLS = {64: 4, 216: 6, 343: 7, 512: 8, 729: 9, 1000: 10, 1331: 11, 1728: 12}
+
+
+def _box(nm, nb, temp, precision, seed, dtfs=0.5, mts=1, param=PARAM_QSPCFW):
+    n = CUBIC_CELLS[nm]
+    s = system.water_box(param, ncell=(n, n, n), nb=nb, temp=temp, dtfs=dtfs, mts=mts, precision=precision)
+    irun = C.c_int(-(1 + seed))
+    s["p"] = system.sample_momenta(s["na"], s["nb"], s["mass"], s["beta"], irun)
+    s["seed"] = seed
+    s["temp"] = temp
+    return s
+
+
+def replica_set(n=256, seed=2026, precision=1, sizes=(64, 216, 343, 512), beads=(8, 16, 32, 64),
+                temps=(250.0, 350.0)):
+    """n independent NVT replicas: molecule count, bead count and temperature
+    drawn uniformly per replica from a seeded generator."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nm = int(rng.choice(sizes))
+        nb = int(rng.choice(beads))
+        temp = float(rng.uniform(*temps))
+        out.append(_box(nm, nb, temp, precision, seed=1000 * seed + i))
+    return out
+
+
+def request_stream(n=60, rate=50.0, seed=7, precision=1, sizes=(64, 216, 343, 512, 729, 1000, 1331, 1728),
+                   beads=(4, 8, 16, 32, 64), nsteps=100, temp=298.0):
+    """n trajectory requests with Poisson arrivals (mean `rate` per second):
+    [(arrival_seconds, system, nsteps)], sizes and bead counts drawn per request."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += float(rng.exponential(1.0 / rate))
+        nm = int(rng.choice(sizes))
+        nb = int(rng.choice(beads))
+        out.append((t, _box(nm, nb, temp, precision, seed=100000 + 1000 * seed + i), nsteps))
+    return out
