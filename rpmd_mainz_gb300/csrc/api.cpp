@@ -71,6 +71,21 @@ int download(gb_context *c, double *dst, const double *src, size_t n) {
   return GB_OK;
 }
 
+// masses to the device; a change of the O, H, H masses marks the monodromy
+// table stale (dev_prepare rebuilds it before the next step, never inside a
+// captured one)
+int set_masses(gb_context *c, const double *mass) {
+  if (!mass) return GB_OK;
+  const int n = std::min(3, c->na);
+  bool same = true;
+  for (int i = 0; i < n; ++i) same = same && c->h_mass3[i] == mass[i];
+  if (!same) {
+    for (int i = 0; i < n; ++i) c->h_mass3[i] = mass[i];
+    c->mass_version += 1;
+  }
+  return upload(c, c->mass, mass, (size_t)c->na);
+}
+
 int set_charges(gb_context *c, const double *z) {
   if (!z) return GB_OK;
   double qq = 0.0;
@@ -259,12 +274,8 @@ int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj, 
   const size_t N = 3 * (size_t)(*na) * (*nb);
   std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
   if ((st = upload(c, c->p, p, N)) || (st = upload(c, c->r, r, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||
-      (st = upload(c, c->dvdr2, dvdr2, N)) || (st = upload(c, c->mass, mass, (size_t)*na)) ||
-      (st = set_charges(c, z)))
+      (st = upload(c, c->dvdr2, dvdr2, N)) || (st = set_masses(c, mass)) || (st = set_charges(c, z)))
     return st;
-  if (c->monod_dt > 0.0) {  // masses may have changed: rebuild the monodromy table
-    c->monod_dt = -1.0;
-  }
   if ((st = dev_step(c, *dt, *beta))) return st;
   if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
       (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N)))
@@ -293,7 +304,7 @@ int gbrpmd_ctx_create(gb_context **ctx, int na, int nb, const double *mass, cons
     return st;
   }
   c->P = g_params;
-  if ((st = upload(c, c->mass, mass, (size_t)na)) || (st = set_charges(c, z))) {
+  if ((st = set_masses(c, mass)) || (st = set_charges(c, z))) {
     ctx_free(c);
     delete c;
     return st;
@@ -515,7 +526,7 @@ int gbrpmd_evolve_rig_pi(double *p, double *r, double *v, double *v_lf, double *
   const size_t N = 3 * (size_t)(*na) * (*nb);
   std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
   if ((st = upload(c, c->p, p, N)) || (st = upload(c, c->r, r, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||
-      (st = upload(c, c->dvdr2, dvdr2, N)) || (st = upload(c, c->mass, mass, (size_t)*na)) ||
+      (st = upload(c, c->dvdr2, dvdr2, N)) || (st = set_masses(c, mass)) ||
       (st = set_charges(c, z)))
     return st;
   if ((st = dev_evolve_rig_pi(c, *dt, *beta, vir))) return st;

@@ -184,7 +184,11 @@ int gbrpmd_batch_step(gb_batch *b, int nsteps) {
       b->seen += 1;
     } else {
       std::vector<int64_t> l0;
-      for (auto &r : b->reps) l0.push_back(r.c->launches);
+      for (auto &r : b->reps) {
+        int sp = dev_prepare(r.c, r.dt, r.beta);  // set-up copies synchronise: never inside the capture
+        if (sp) return sp;
+        l0.push_back(r.c->launches);
+      }
       BCK(cudaStreamBeginCapture(b->s0, cudaStreamCaptureModeThreadLocal));
       int st = run_branches(b);
       cudaGraph_t g = nullptr;

@@ -97,7 +97,10 @@ struct gb_context {
   double *tw_nb = nullptr, *tw_c1 = nullptr, *tw_c2 = nullptr;  // twiddles for nb, nbdf1, nbdf2
   int tw_c1_n = 0, tw_c2_n = 0;
   double *monod = nullptr;  // [nb][4][3]
-  double monod_dt = -1.0, monod_beta = -1.0;
+  double monod_dt = -1.0, monod_beta = -1.0;  // monodromy built for these dt, beta,
+  int monod_mts = -1, monod_mass_version = -1;  // mts and masses
+  double h_mass3[3] = {0, 0, 0};  // host copy of the O, H, H masses (ring_rpmd needs only these)
+  int mass_version = 0;           // bumped when uploaded masses differ
   double *acc = nullptr;    // ACC_NSLOT * ACC_STRIDE
   unsigned *status = nullptr;
   double *h_acc = nullptr;  // pinned host mirror

@@ -388,10 +388,7 @@ int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) 
   const int nb = c->nb, nm = c->nm;
   const long long N = 3LL * c->na * nb;
   cudaStream_t s = c->stream;
-  double mass3h[3];
-  CK(cudaMemcpyAsync(mass3h, c->mass, sizeof(double) * 3, cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  RatPar rp = make_rp(c->P, mass3h);
+  RatPar rp = make_rp(c->P, c->h_mass3);
   const double halfdt = 0.5 * dt, smalldt = dt / (double)nb;
   double omegan = nb / (beta * 1.0);
   omegan = omegan * omegan;

@@ -529,16 +529,16 @@ int dev_prepare(gb_context *c, double dt, double beta) {
   if (c->kmax_alloc != c->P.kmax || c->k_rkmax != c->P.rkmax || c->k_walpha != c->P.walpha) {
     if ((st = build_kvectors(c))) return st;
   }
-  if (dt > 0.0 && (dt != c->monod_dt || beta != c->monod_beta)) {
-    double mass3[3];
-    CK(cudaMemcpyAsync(mass3, c->mass, sizeof(double) * 3, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+  if (dt > 0.0 && (dt != c->monod_dt || beta != c->monod_beta || c->P.mts != c->monod_mts ||
+                   c->mass_version != c->monod_mass_version)) {
     std::vector<double> monod(12 * (size_t)c->nb);
-    ring_rpmd_host(mass3, c->nb, dt / (double)c->P.mts, beta, monod.data());
+    ring_rpmd_host(c->h_mass3, c->nb, dt / (double)c->P.mts, beta, monod.data());
     CK(cudaMemcpyAsync(c->monod, monod.data(), sizeof(double) * monod.size(), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));  // monod is a local vector
     c->monod_dt = dt;
     c->monod_beta = beta;
+    c->monod_mts = c->P.mts;
+    c->monod_mass_version = c->mass_version;
   }
   return GB_OK;
 }
@@ -686,6 +686,8 @@ int dev_step(gb_context *c, double dt, double beta) {
     if (eligible) G.seen += 1;
     return GB_OK;
   }
+  int sp = dev_prepare(c, dt, beta);  // set-up copies synchronise: never inside the capture
+  if (sp) return sp;
   const int64_t l0 = c->launches;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int st = dev_evolve_pi(c, dt, beta);

@@ -280,10 +280,13 @@ def test_graph_replay_matches_plain_steps(precision):
     prm.precision = 0
     lib.init(prm)
     (a, ea, la), (b, eb, lb) = out
+    # FP64: only the order of atomic additions differs; mixed: the pair-list
+    # order (atomic group appends) also reorders FP32 sums, at their rounding level
+    tol = 1e-12 if precision == 0 else 1e-6
     for x, y in zip(a, b):
-        assert rel(x, y) < 1e-12
+        assert rel(x, y) < tol
     for k in ("v", "vew", "vlj", "vint", "tv"):
-        assert erel(eb[k], ea[k]) < 1e-11
+        assert erel(eb[k], ea[k]) < 10 * tol
     assert la == lb
 
 
