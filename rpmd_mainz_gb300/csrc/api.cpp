@@ -182,7 +182,7 @@ void ctx_free(gb_context *c) {
   for (void *p : c->allocs) cudaFree(p);
   c->allocs.clear();
   for (void *p : {(void *)c->pl.idx, (void *)c->pl.count, (void *)c->kcol, (void *)c->kgrp,
-                  (void *)c->kpair, (void *)c->kw, (void *)c->ktab, (void *)c->sk_part, (void *)c->sk,
+                  (void *)c->kpair, (void *)c->kw, (void *)c->kvir, (void *)c->ktab, (void *)c->sk_part, (void *)c->sk,
                   (void *)c->tw_nb, (void *)c->tw_c1, (void *)c->tw_c2})
     if (p) cudaFree(p);
   for (SkinList &L : c->sl)

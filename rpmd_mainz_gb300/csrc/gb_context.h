@@ -88,6 +88,7 @@ struct gb_context {
   int4 *kgrp = nullptr;         // [ngrp] structure-factor work items
   int4 *kpair = nullptr;        // [nkp] kx, ky, m, kind
   double *kw = nullptr;         // [nkp] weights (4 pi / k^2) exp(-b k^2)
+  double *kvir = nullptr;       // [nkp][9] virial factors (gb_kvir_table)
   double2 *ktab = nullptr;      // [nconf][na][3][kmax+1] per-site powers e^{i 2 pi m x}
   double *sk_part = nullptr;    // [nconf][nchunk][nkp][4] chunk partials of P, Q
   double *sk = nullptr;         // [nconf][nkp][8] force tables

@@ -114,3 +114,19 @@ inline int gb_build_ktables(const gb_params &P, int G, KCol *col, int cap_col, i
 // capacities that always suffice for a given kmax
 inline int gb_kcap_col(int kmax) { return (kmax + 1) * (2 * kmax + 1); }
 inline int gb_kcap_kp(int kmax) { return gb_kcap_col(kmax) * (kmax + 1); }
+
+// Per k pair the virial factors term |rk_a| |rk_b| - delta_ab with
+// term = 2 (1/rk^2 + 1/(4 alpha^2)) and rk = 2 pi (kx, ky, m), column-major
+// (a + 3 b) -- the reference's |k_a| |k_b| form (ewald_cubic.f90:488-503).
+inline void gb_kvir_table(const int4 *kp, int nkp, double walpha, double *out) {
+  const double rlat = 2.0 * 3.141592653589793238462643383279502884;
+  const double bfac = 0.25 / (walpha * walpha);
+  for (int k = 0; k < nkp; ++k) {
+    const double rk[3] = {rlat * kp[k].x, rlat * kp[k].y, rlat * kp[k].z};
+    const double rk2 = rk[0] * rk[0] + rk[1] * rk[1] + rk[2] * rk[2];
+    const double term = 2.0 * (1.0 / rk2 + bfac);
+    for (int b = 0; b < 3; ++b)
+      for (int a = 0; a < 3; ++a)
+        out[9 * (size_t)k + a + 3 * b] = term * std::fabs(rk[a]) * std::fabs(rk[b]) - (a == b ? 1.0 : 0.0);
+  }
+}

@@ -31,7 +31,7 @@ GB_D void kadd(float &s, float &c, float v) {  // Kahan-compensated s += v
 }
 
 template <int NP>
-GB_D double group_sum_d(double v) {
+GB_D float group_sum_f(float v) {
 #pragma unroll
   for (int o = NP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -169,14 +169,15 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
       pair(j, H[j], Lo[j]);
     }
   }
-  const double fx = group_sum_d<MX_NP>((double)sx - (double)cx);
-  const double fy = group_sum_d<MX_NP>((double)sy - (double)cy);
-  const double fz = group_sum_d<MX_NP>((double)sz - (double)cz);
+  // each lane's compensated sum, then FP32 across the site's lanes
+  const float fx = group_sum_f<MX_NP>(sx - cx);
+  const float fy = group_sum_f<MX_NP>(sy - cy);
+  const float fz = group_sum_f<MX_NP>(sz - cz);
   if (active && sub == 0) {
     double *G = g + ((long long)c * na + i) * 3;
-    G[0] += fx;
-    G[1] += fy;
-    G[2] += fz;
+    G[0] += (double)fx;
+    G[1] += (double)fy;
+    G[2] += (double)fz;
   }
   const float vir6[6] = {0.5f * vxx, 0.5f * vyx, 0.5f * vzx, 0.5f * vyy, 0.5f * vzy, 0.5f * vzz};
   constexpr int dst[7] = {0, 1, 2, 3, 5, 6, 9};       // v, xx, yx, zx, yy, zy, zz
@@ -239,14 +240,14 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
       pair(H[j], Lo[j]);
     }
   }
-  const double fx = group_sum_d<MX_LJ_NP>((double)sx - (double)cx);
-  const double fy = group_sum_d<MX_LJ_NP>((double)sy - (double)cy);
-  const double fz = group_sum_d<MX_LJ_NP>((double)sz - (double)cz);
+  const float fx = group_sum_f<MX_LJ_NP>(sx - cx);
+  const float fy = group_sum_f<MX_LJ_NP>(sy - cy);
+  const float fz = group_sum_f<MX_LJ_NP>(sz - cz);
   if (active && sub == 0) {
     double *F = out + (long long)c * na * 3 + 9LL * o;
-    F[0] += dscale * fx;
-    F[1] += dscale * fy;
-    F[2] += dscale * fz;
+    F[0] += dscale * (double)fx;
+    F[1] += dscale * (double)fy;
+    F[2] += dscale * (double)fz;
   }
   float vir9[9];
 #pragma unroll
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
 constexpr int MW_SL = 16;  // chunk slices per k pair in the weights kernel
 
 __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *sk_part, int nchunk, int nkp,
-                                                                const int4 *kpair, const double *kw, double bfac,
+                                                                const int4 *kpair, const double *kw, const double *kvir,
                                                                 float4 *sk, double *acc) {
   __shared__ double part[4][MW_SL][32];
   __shared__ double sh[MW_SL * 10];
@@ -365,9 +366,6 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
       Qi += part[3][j][lane];
     }
     const int4 kv = kpair[k];
-    const double rlat = 2.0 * acos(-1.0);
-    const double rk[3] = {rlat * kv.x, rlat * kv.y, rlat * kv.z};
-    const double rk2 = rk[0] * rk[0] + rk[1] * rk[1] + rk[2] * rk[2];
     const double w = kw[k];
     double et, Ar, Ai, Dr, Di;
     if (kv.w == 1) {
@@ -387,13 +385,14 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
       Ai = 2.0 * w * Pi;
       Dr = Di = 0.0;
     }
-    const double term = 2.0 * (1.0 / rk2 + bfac);
     vals[0] = et;
+    // the reference combines the (+-ky, +-kz) partners into one energy and
+    // multiplies it by term * rk_a * rk_b with rk_y, rk_z >= 0, so its
+    // off-diagonal virial uses |k_a| |k_b| (ewald_cubic.f90:488-503); the
+    // factors come from gb_kvir_table
+    const double *kv9 = kvir + 9LL * k;
 #pragma unroll
-    for (int b = 0; b < 3; ++b)
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        vals[1 + a + 3 * b] = et * (term * fabs(rk[a]) * fabs(rk[b]) - (a == b ? 1.0 : 0.0));
+    for (int e = 0; e < 9; ++e) vals[1 + e] = et * kv9[e];
     const double m = (double)kv.z;
     float4 *o = sk + ((long long)c * nkp + k) * 2;
     o[0] = make_float4((float)Ar, (float)-Ai, (float)Dr, (float)Di);
@@ -405,10 +404,16 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
 // one block per 32 sites: its site tables are loaded into shared memory once,
 // and each of its MF_G warps takes a share of the columns (by k-pair count);
 // the warps' per-site sums are added in FP64 in a fixed order
+// STAGED: the whole k-pair table (8 floats per pair) is copied to shared
+// memory first, so that the inner loop reads it with shared-memory broadcasts
+template <bool STAGED>
 __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__restrict__ tab, int na, int kmax,
                                                               int ncol, const KCol *__restrict__ cols, int nkp,
                                                               const float4 *__restrict__ sk, double *g) {
-  extern __shared__ float2 stf[];  // [3][K1][MF_S], then [MF_G][MF_S][3] double sums
+  // [3][K1][MF_S] float2 site tables, [MF_G][MF_S][3] double sums, then
+  // (STAGED) the k-pair table [nkp][2] float4
+  extern __shared__ float4 smf[];
+  float2 *stf = reinterpret_cast<float2 *>(smf);
   const int K1 = kmax + 1, K3 = 3 * K1;
   const int c = blockIdx.y;
   const int t = threadIdx.x, sl = t % MF_S, wg = t / MF_S;
@@ -418,7 +423,13 @@ __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__
     const int si = min(i0 + s2, na - 1);
     stf[w] = tab[((long long)c * na + si) * K3 + e];
   }
-  double *red = reinterpret_cast<double *>(stf + ((K3 * MF_S + 1) & ~1));
+  const int tab_f4 = (K3 * MF_S + 1) / 2;                       // float4 slots of the site tables
+  double *red = reinterpret_cast<double *>(smf + tab_f4);       // MF_G * MF_S * 3 doubles
+  float4 *sT = smf + tab_f4 + (MF_G * MF_S * 3 + 1) / 2;        // [nkp][2]
+  if (STAGED) {
+    const float4 *src = sk + (long long)c * nkp * 2;
+    for (int w = t; w < 2 * nkp; w += MF_S * MF_G) sT[w] = src[w];
+  }
   const long long kp_lo = (long long)wg * nkp / MF_G;
   const long long kp_hi = (long long)(wg + 1) * nkp / MF_G;
   auto first_col = [&](long long kp) {
@@ -432,7 +443,7 @@ __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__
   };
   const int col0 = first_col(kp_lo), col1 = first_col(kp_hi);
   __syncthreads();
-  const float4 *T = sk + (long long)c * nkp * 2;
+  const float4 *T = STAGED ? sT : sk + (long long)c * nkp * 2;
   float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
   for (int col = col0; col < col1; ++col) {
     const int4 ci4 = __ldg(reinterpret_cast<const int4 *>(cols + col));
@@ -447,7 +458,14 @@ __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__
 #pragma unroll 4
     for (int m = mlo; m <= mhi; ++m) {
       const float2 z = Z[m * MF_S];
-      const float4 t0 = __ldg(Tp + 2 * m), t1 = __ldg(Tp + 2 * m + 1);
+      float4 t0, t1;
+      if (STAGED) {
+        t0 = Tp[2 * m];
+        t1 = Tp[2 * m + 1];
+      } else {
+        t0 = __ldg(Tp + 2 * m);
+        t1 = __ldg(Tp + 2 * m + 1);
+      }
       ur = fmaf(z.x, t0.x, fmaf(z.y, t0.w, ur));
       ui = fmaf(z.x, t0.y, fmaf(z.y, t0.z, ui));
       vr = fmaf(z.x, t1.x, fmaf(z.y, t1.y, vr));
@@ -497,8 +515,8 @@ void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, in
 }
 
 size_t recip_sk_smem_mx(int kmax) { return sizeof(float2) * MSK_CHUNK * 3 * (kmax + 1); }
-size_t recip_force_smem_mx(int kmax) {
-  return sizeof(float2) * ((3 * (kmax + 1) * MF_S + 1) & ~1) + sizeof(double) * MF_G * MF_S * 3;
+size_t recip_force_smem_mx(int kmax, int nkp_staged) {
+  return sizeof(float4) * ((3 * (kmax + 1) * MF_S + 1) / 2 + (MF_G * MF_S * 3 + 1) / 2 + 2 * (size_t)nkp_staged);
 }
 
 // partial sums need nconf * nchunk * nkp float4 (half of the FP64 layout)
@@ -517,25 +535,31 @@ void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const d
 void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc) {
   if (c->nkp == 0) return;
   const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
-  const double bfac = 0.25 / (c->P.walpha * c->P.walpha);
   dim3 grid(nblk(c->nkp, 32), B);
   k_recip_weights_mx<<<grid, 32 * MW_SL, 0, s>>>(reinterpret_cast<const float4 *>(c->sk_part), nchunk, c->nkp, c->kpair,
-                                          c->kw, bfac, reinterpret_cast<float4 *>(c->sk), acc);
+                                          c->kw, c->kvir, reinterpret_cast<float4 *>(c->sk), acc);
 }
 
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
   if (c->nkp == 0) return;
   const int kmax = c->P.kmax;
   dim3 grid(nblk(c->na, MF_S), B);
-  k_recip_force_mx<<<grid, MF_S * MF_G, recip_force_smem_mx(kmax), s>>>(
-      reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
-      reinterpret_cast<const float4 *>(c->sk), g);
+  const size_t staged = recip_force_smem_mx(kmax, c->nkp);
+  if (staged <= 160 * 1024)
+    k_recip_force_mx<true><<<grid, MF_S * MF_G, staged, s>>>(
+        reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
+        reinterpret_cast<const float4 *>(c->sk), g);
+  else
+    k_recip_force_mx<false><<<grid, MF_S * MF_G, recip_force_smem_mx(kmax, 0), s>>>(
+        reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
+        reinterpret_cast<const float4 *>(c->sk), g);
 }
 
 void recip_set_attributes_mx() {
   static bool done = false;
   if (done) return;
   cudaFuncSetAttribute(k_recip_sk_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   done = true;
 }

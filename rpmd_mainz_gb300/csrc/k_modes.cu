@@ -185,6 +185,7 @@ __global__ void k_expand_table(double *dvdr, const double *fb1, int nbc1, const 
   R cr[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) cr[q] = (R)cf[q];
+#pragma unroll 8
   for (int j = 0; j < nb; ++j) {
     R s = (R)0;
 #pragma unroll

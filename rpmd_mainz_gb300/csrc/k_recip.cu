@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(SK_T) k_recip_sk(const double2 *tab, int na, i
 // one block: 32 k pairs x 8 chunk slices; energy, virial and force tables
 // (ewald_cubic.f90:308-328, 355-380, 408-440, 482-517)
 __global__ void __launch_bounds__(256) k_recip_weights(const double4_32a *sk_part, int nchunk, int nkp,
-                                                       const int4 *kpair, const double *kw, double bfac,
+                                                       const int4 *kpair, const double *kw, const double *kvir,
                                                        double4_32a *sk, double *acc) {
   __shared__ double4_32a part[8][32];
   __shared__ double sh[8 * 10];
@@ -137,9 +137,6 @@ __global__ void __launch_bounds__(256) k_recip_weights(const double4_32a *sk_par
       Qi += part[j][lane].w;
     }
     const int4 kv = kpair[k];
-    const double rlat = 2.0 * acos(-1.0);
-    const double rk[3] = {rlat * kv.x, rlat * kv.y, rlat * kv.z};
-    const double rk2 = rk[0] * rk[0] + rk[1] * rk[1] + rk[2] * rk[2];
     const double w = kw[k];
     double et, Ar, Ai, Dr, Di;
     if (kv.w == 1) {  // S(+-m) = P +- iQ
@@ -159,16 +156,14 @@ __global__ void __launch_bounds__(256) k_recip_weights(const double4_32a *sk_par
       Ai = 2.0 * w * Pi;
       Dr = Di = 0.0;
     }
-    const double term = 2.0 * (1.0 / rk2 + bfac);
     vals[0] = et;
     // the reference combines the (+-ky, +-kz) partners into one energy and
     // multiplies it by term * rk_a * rk_b with rk_y, rk_z >= 0, so its
-    // off-diagonal virial uses |k_a| |k_b| (ewald_cubic.f90:488-503)
+    // off-diagonal virial uses |k_a| |k_b| (ewald_cubic.f90:488-503); the
+    // factors come from gb_kvir_table
+    const double *kv9 = kvir + 9LL * k;
 #pragma unroll
-    for (int b = 0; b < 3; ++b)
-#pragma unroll
-      for (int a2 = 0; a2 < 3; ++a2)
-        vals[1 + a2 + 3 * b] = et * (term * fabs(rk[a2]) * fabs(rk[b]) - (a2 == b ? 1.0 : 0.0));
+    for (int e = 0; e < 9; ++e) vals[1 + e] = et * kv9[e];
     const double m = (double)kv.z;
     double4_32a *o = sk + ((long long)c * nkp + k) * 2;
     o[0] = make_double4_32a(Ar, -Ai, Dr, Di);
@@ -270,9 +265,8 @@ void launch_recip_sk(cudaStream_t s, gb_context *c, const double *rs, const doub
 void launch_recip_weights(cudaStream_t s, gb_context *c, int B, double *acc) {
   if (c->nkp == 0) return;
   const int nchunk = (c->na + SK_CHUNK - 1) / SK_CHUNK;
-  const double bfac = 0.25 / (c->P.walpha * c->P.walpha);
   dim3 grid(nblk(c->nkp, 32), B);
-  k_recip_weights<<<grid, 256, 0, s>>>((const double4_32a *)c->sk_part, nchunk, c->nkp, c->kpair, c->kw, bfac,
+  k_recip_weights<<<grid, 256, 0, s>>>((const double4_32a *)c->sk_part, nchunk, c->nkp, c->kpair, c->kw, c->kvir,
                                        (double4_32a *)c->sk, acc);
 }
 

@@ -52,7 +52,7 @@ unsigned char *g_scratch_ptr[MAX_DEVICES] = {nullptr};
 // host-side k tables (fixed size: no heap allocation)
 KCol h_col[MAX_NKXY];
 int4 h_kp[MAX_NK], h_grp[MAX_NK];
-double h_kw[MAX_NK];
+double h_kw[MAX_NK], h_kvir[9 * MAX_NK];
 
 const double PI = 3.141592653589793238462643383279502884;
 
@@ -119,6 +119,7 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   int4 *d_grp = (int4 *)take(sizeof(int4) * kt.ngrp);
   int4 *d_kp = (int4 *)take(sizeof(int4) * kt.nkp);
   double *d_kw = (double *)take(sizeof(double) * kt.nkp);
+  double *d_kvir = (double *)take(sizeof(double) * 9 * kt.nkp);
   double2 *d_tab = (double2 *)take(sizeof(double2) * 3 * (size_t)(P.kmax + 1) * n * B);
   double *d_skp = (double *)take(sizeof(double) * 4 * (size_t)kt.nkp * nchunk * B);
   double *d_sk = (double *)take(sizeof(double) * 8 * (size_t)kt.nkp * B);
@@ -133,6 +134,8 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   SCK(cudaMemcpyAsync(d_grp, h_grp, sizeof(int4) * kt.ngrp, cudaMemcpyHostToDevice, s));
   SCK(cudaMemcpyAsync(d_kp, h_kp, sizeof(int4) * kt.nkp, cudaMemcpyHostToDevice, s));
   SCK(cudaMemcpyAsync(d_kw, h_kw, sizeof(double) * kt.nkp, cudaMemcpyHostToDevice, s));
+  gb_kvir_table(h_kp, kt.nkp, P.walpha, h_kvir);
+  SCK(cudaMemcpyAsync(d_kvir, h_kvir, sizeof(double) * 9 * kt.nkp, cudaMemcpyHostToDevice, s));
   // cleared every call: gradient accumulator, energy/virial sums, status word
   SCK(cudaMemsetAsync(d_g, 0, sizeof(double) * N, s));
   SCK(cudaMemsetAsync(d_acc, 0, sizeof(double) * ACC_STRIDE, s));
@@ -151,6 +154,7 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   view.kgrp = d_grp;
   view.kpair = d_kp;
   view.kw = d_kw;
+  view.kvir = d_kvir;
   view.ktab = d_tab;
   view.sk_part = d_skp;
   view.sk = d_sk;

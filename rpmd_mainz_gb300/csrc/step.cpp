@@ -96,12 +96,12 @@ int build_kvectors(gb_context *c) {
   if (gb_build_ktables(c->P, recip_group_len(), col.data(), cap_col, kp.data(), kw.data(), cap_kp, grp.data(),
                        cap_kp, &t))
     return ctx_set_error(GB_E_ARG, "k-vector table capacity exceeded");
-  for (void *p : {(void *)c->kcol, (void *)c->kgrp, (void *)c->kpair, (void *)c->kw, (void *)c->ktab,
-                  (void *)c->sk_part, (void *)c->sk})
+  for (void *p : {(void *)c->kcol, (void *)c->kgrp, (void *)c->kpair, (void *)c->kw, (void *)c->kvir,
+                  (void *)c->ktab, (void *)c->sk_part, (void *)c->sk})
     if (p) cudaFree(p);
   c->kcol = nullptr;
   c->kgrp = c->kpair = nullptr;
-  c->kw = c->sk_part = c->sk = nullptr;
+  c->kw = c->kvir = c->sk_part = c->sk = nullptr;
   c->ktab = nullptr;
   c->ncol = t.ncol;
   c->nkp = t.nkp;
@@ -116,6 +116,9 @@ int build_kvectors(gb_context *c) {
   CK(cudaMalloc(&c->kgrp, sizeof(int4) * std::max(t.ngrp, 1)));
   CK(cudaMalloc(&c->kpair, sizeof(int4) * std::max(t.nkp, 1)));
   CK(cudaMalloc(&c->kw, sizeof(double) * std::max(t.nkp, 1)));
+  CK(cudaMalloc(&c->kvir, sizeof(double) * 9 * std::max(t.nkp, 1)));
+  std::vector<double> kvir(9 * (size_t)std::max(t.nkp, 1));
+  gb_kvir_table(kp.data(), t.nkp, c->P.walpha, kvir.data());
   CK(cudaMalloc(&c->ktab, c->ktab_bytes));
   CK(cudaMalloc(&c->sk_part, c->sk_part_bytes));
   CK(cudaMalloc(&c->sk, c->sk_bytes));
@@ -126,6 +129,7 @@ int build_kvectors(gb_context *c) {
   CK(cudaMemcpyAsync(c->kgrp, grp.data(), sizeof(int4) * t.ngrp, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->kpair, kp.data(), sizeof(int4) * t.nkp, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->kw, kw.data(), sizeof(double) * t.nkp, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->kvir, kvir.data(), sizeof(double) * 9 * t.nkp, cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   recip_set_attributes();
   c->kmax_alloc = kmax;
@@ -838,7 +842,7 @@ size_t dev_estimate_bytes(int na, int nb, const gb_params &P) {
 
 size_t ctx_device_bytes(const gb_context *c) {
   size_t b = c->alloc_bytes + c->ktab_bytes + c->sk_part_bytes + c->sk_bytes + c->pl_idx_bytes + c->pl_cnt_bytes;
-  b += sizeof(KCol) * c->ncol + sizeof(int4) * (c->ngrp + c->nkp) + sizeof(double) * c->nkp;
+  b += sizeof(KCol) * c->ncol + sizeof(int4) * (c->ngrp + c->nkp) + sizeof(double) * 10 * c->nkp;
   for (const SkinList &L : c->sl) b += L.idx_bytes + L.cnt_bytes + L.ref_bytes;
   return b;
 }
