@@ -45,7 +45,7 @@ WORKLOADS = {
 }
 DEFAULT = "qspcfw_4096_nb32_mts5_contracted"
 # multi-trajectory workloads (rpmd_mainz_gb300/workloads.py)
-BATCH_WORKLOADS = ("replicas_256", "served_stream")
+BATCH_WORKLOADS = ("replicas_256", "served_stream", "qspcfw_216_nb32_nve")
 REGIONS = ["mts_block", "pair_lists", "ewald_real", "recip_sk", "recip_weights", "recip_force", "lj",
            "tem", "expand_kick", "msite", "rattle"]
 # algorithmic FP64 flops per work unit of a region (declared weights):
@@ -440,6 +440,106 @@ def run_replicas(args, torch):
     }
 
 
+def run_nve(args, torch):
+    """Mixed precision on the 216-molecule, nb = 32 system (dt 0.5 fs, every
+    bead, no contraction): the force / energy / virial error against the FP64
+    path on 20 seeded snapshots (an FP64 Andersen NVT run from the lattice,
+    one snapshot every 50 steps, thresh = 1/sqrt(1000) as md_eq sets it for
+    ttaufs = 0), then `--nve-ps` of NVE (no thermostat) from the last snapshot
+    with both paths, sampling the conserved RPMD energy nb*v + tk + vrp
+    (md_eq.f90:274) every 100 steps; drift = least-squares slope."""
+    from rpmd_mainz_gb300 import lib, system
+
+    s = system.water_box(PARAM, ncell=(6, 6, 6), nb=32, mts=1, dtfs=0.5)
+    irun = C.c_int(-4711)
+    s["p"] = system.sample_momenta(s["na"], s["nb"], s["mass"], s["beta"], irun)
+    na, nm, nb, dt, beta = s["na"], s["nm"], s["nb"], s["dt"], s["beta"]
+
+    def params(prec, therm):
+        prm = s["params"].copy()
+        prm.precision = prec
+        prm.therm = therm
+        return prm
+
+    lib.init(params(0, 1))
+    ctx = lib.Context(na, nb, s["mass"], s["z"])
+    ctx.set_params(params(0, 1))
+    ctx.upload(r=s["r"], p=s["p"], box=s["box"])
+    ctx.full_forces()
+    seed = C.c_int(-2026)
+    snaps = []
+    for _ in range(20):
+        ctx.run_md_eq(50, dt, beta, 1.0 / np.sqrt(1000.0), seed)
+        snaps.append(ctx.download())
+    ctx.close()
+    per_bead, energy, virial, total = [], [], [], []
+    for r, _, _, _ in snaps:
+        out = []
+        for prec in (0, 1):
+            lib.init(params(prec, 0))
+            out.append(lib.full_forces(r, s["box"], s["z"]))
+        f64, fmx = out
+        F64, Fmx = f64["dvdr"] + f64["dvdr2"], fmx["dvdr"] + fmx["dvdr2"]
+        per_bead.append(float(max(np.linalg.norm(Fmx[k] - F64[k]) / np.linalg.norm(F64[k]) for k in range(nb))))
+        total.append(float(np.linalg.norm(Fmx - F64) / np.linalg.norm(F64)))
+        energy.append(abs(fmx["v"] - f64["v"]) / abs(f64["v"]))
+        virial.append(float(np.linalg.norm(fmx["vir"] - f64["vir"]) / np.linalg.norm(f64["vir"])))
+
+    r0, p0 = snaps[-1][0], snaps[-1][1]
+    nsteps = int(round(args.nve_ps * 1000.0 / 0.5))
+    block = 100
+    arms = {}
+    for name, prec in (("mixed", 1), ("fp64", 0)):
+        lib.init(params(prec, 0))
+        c = lib.Context(na, nb, s["mass"], s["z"])
+        c.set_params(params(prec, 0))
+        c.upload(r=r0, p=p0, box=s["box"])
+        c.full_forces()
+        stream = torch.cuda.ExternalStream(c.stream)
+        e_t, e_h, ms = [0.0], [c.estimators(beta)["econs"]], 0.0
+        launches0 = c.launches
+        with ClockSampler(0) as clk:
+            for b in range(nsteps // block):
+                with torch.cuda.stream(stream):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                c.evolve(block, dt, beta)
+                with torch.cuda.stream(stream):
+                    e1.record(stream)
+                e1.synchronize()
+                ms += e0.elapsed_time(e1)
+                e_t.append((b + 1) * block * 0.5e-3)  # ps
+                e_h.append(c.estimators(beta)["econs"])
+        c.sync()
+        t = np.array(e_t) * 1e-3  # ns
+        e = np.array(e_h) * 2625.49963 / nm  # kJ/mol per molecule
+        slope, icpt = np.polyfit(t, e, 1)
+        arms[name] = {"value": nsteps * nb * nm / (ms * 1e-3), "ms_per_step": ms / nsteps,
+                      "drift_kjmol_per_ns_per_molecule": float(slope),
+                      "fluctuation_rms_kjmol_per_molecule": float(np.std(e - (slope * t + icpt))),
+                      "econs_first_last_kjmol_per_molecule": [float(e[0]), float(e[-1])],
+                      "gpu_launches": int(c.launches - launches0 - (nsteps // block)), "clocks": clk.summary()}
+        c.close()
+    mx = arms["mixed"]
+    return {
+        "metric": "bead-molecule-steps/s", "value": mx["value"], "unit": "bead-molecule-steps/s", "n_gpus": 1,
+        "steps": nsteps, "warmup": 0, "ms_per_step": mx["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 mixed",
+        "data": "synthetic (CUB lattice, momenta from the reference's ran2 stream, FP64 Andersen NVT snapshots)",
+        "config": {"workload": "qspcfw_216_nb32_nve", "nm": nm, "nb": nb, "dt_fs": 0.5, "nve_ps": args.nve_ps,
+                   "snapshots": len(snaps), "l2": "state smaller than L2 (resident NVE run, no flush)",
+                   "parallelism": "single GPU"},
+        "gpu_launches": mx["gpu_launches"],
+        "error_vs_fp64": {"snapshots": len(snaps), "force_rel_rms_per_bead_max": max(per_bead),
+                          "force_rel_rms_per_bead_median": float(np.median(per_bead)),
+                          "force_rel_rms_total_max": max(total), "energy_rel_max": max(energy),
+                          "virial_rel_max": max(virial), "bound": 1e-5},
+        "nve": {"mixed": mx, "fp64": arms["fp64"]},
+        "mixed_over_fp64": mx["value"] / arms["fp64"]["value"],
+        "clocks": mx["clocks"],
+    }
+
+
 def run_served(args, torch):
     """Poisson arrivals (mean 50 per second) of trajectory requests of mixed
     sizes (64-1728 molecules, nb 4-64), each `--request-steps` evolve_pi steps,
@@ -501,6 +601,7 @@ def main():
     ap.add_argument("--tick-steps", type=int, default=10)
     ap.add_argument("--slots", type=int, default=32)
     ap.add_argument("--budget-gb", type=int, default=64)
+    ap.add_argument("--nve-ps", type=float, default=10.0, help="NVE length of the qspcfw_216_nb32_nve workload")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -524,7 +625,8 @@ def main():
 
     if args.workload in BATCH_WORKLOADS:
         if rank == 0:
-            out = run_replicas(args, torch) if args.workload == "replicas_256" else run_served(args, torch)
+            runner = {"replicas_256": run_replicas, "served_stream": run_served, "qspcfw_216_nb32_nve": run_nve}
+            out = runner[args.workload](args, torch)
             print(json.dumps(out), flush=True)
         return 0
 

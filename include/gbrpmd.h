@@ -228,6 +228,20 @@ int gbrpmd_ctx_sync(gb_context *ctx);
 /* energies and virials of the last step: out[0..4] = v, vew, vlj, vint, tv;
    vir[9], vir_lf[9] column-major */
 int gbrpmd_ctx_energies(gb_context *ctx, double *out5, double *vir, double *vir_lf);
+/* The estimators md_eq prints at an output step (md_eq.f90:190-299), from the
+   resident state left by the last evolve (bead representation) and the
+   energies / virial of that evaluation; synchronises.  out[16]:
+     0 tk     kinetic_rpmd (kinetic.f90:248-265)
+     1 vrp    ring-polymer spring energy, omega_n = nb / (beta hbar) (md_eq.f90:252-270)
+     2 nb*v + tk + vrp   the conserved RPMD energy (md_eq.f90:274, not divided by na)
+     3 temperature in K (md_eq.f90:272)
+     4 tv, 5..7 tvxyz    virial_ke (kinetic.f90:1-54)
+     8 pressure in hartree/bohr^3 with the LJ tail (md_pressure.f90:1-56)
+     9..11 dipx, dipy, dipz, 12 dip2, 13 dipm   dipole (md_tools.f90:75-128)
+     14 density in g/cm^3 (md_eq.f90:196-198), 15 v (bead-averaged potential)
+   rcm [nm][3] (optional): center_water (md_tools.f90:367-390); mdip [nm][3]
+   (optional): bead-averaged molecular dipoles (m_dipole). */
+int gbrpmd_ctx_estimators(gb_context *ctx, double beta, double *out16, double *rcm, double *mdip);
 /* the CUDA stream (cudaStream_t) the context launches on */
 void *gbrpmd_ctx_stream(gb_context *ctx);
 /* number of kernel launches issued by this context since creation */

@@ -94,6 +94,11 @@ void force_contract(double *dvdr, double *dvdr_c, int na, int nb, int nb_c);
 void virial_ke(const double *r, const double *dvdr, const double *dvdr2, double &tv,
                double tvxyz[3], double &tq1, double &tq2, double beta, int na, int nb);
 void kinetic_rpmd(const double *p, int na, double &tk, const double *mass, int nb);
+// md_eq's output block (md_eq.f90:190-299): out[16] in the order of
+// gbrpmd_ctx_estimators; rcm, mdip [nm][3] optional
+void md_eq_estimators(const double *r, const double *p, const double *dvdr, const double *dvdr2,
+                      const double *mass, const double *z, int na, int nb, double beta, double v,
+                      const double vir[9], const double box[3], double out[16], double *rcm, double *mdip);
 void sample_rpmd(double *p, int na, int nb, const double *mass, double beta, Rng &g,
                  int &irun);
 void pshift(double *p, const double *mass, int na, int nb);

@@ -79,6 +79,11 @@ void orc_virial_ke(const double *r, const double *dvdr, const double *dvdr2, dou
 void orc_kinetic_rpmd(const double *p, int na, double *tk, const double *mass, int nb) {
   kinetic_rpmd(p, na, *tk, mass, nb);
 }
+void orc_md_eq_estimators(const double *r, const double *p, const double *dvdr, const double *dvdr2,
+                          const double *mass, const double *z, int na, int nb, double beta, double v,
+                          const double *vir, const double *box, double *out, double *rcm, double *mdip) {
+  md_eq_estimators(r, p, dvdr, dvdr2, mass, z, na, nb, beta, v, vir, box, out, rcm, mdip);
+}
 void orc_sample_rpmd(double *p, int na, int nb, const double *mass, double beta, void *g,
                      int *irun) {
   sample_rpmd(p, na, nb, mass, beta, *(Rng *)g, *irun);

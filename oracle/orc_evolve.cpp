@@ -106,6 +106,98 @@ void kinetic_rpmd(const double *p, int na, double &tk, const double *mass, int n
     }
 }
 
+// The estimators md_eq writes at an output step, each restated from its routine:
+// spring energy md_eq.f90:252-270, temperature md_eq.f90:272, virial_ke
+// kinetic.f90:1-54, pressure + pres_lj_tail md_pressure.f90:1-56, dipole
+// md_tools.f90:75-128, center_water md_tools.f90:367-390, density md_eq.f90:196-198.
+void md_eq_estimators(const double *r, const double *p, const double *dvdr, const double *dvdr2,
+                      const double *mass, const double *z, int na, int nb, double beta, double v,
+                      const double vir[9], const double box[3], double out[16], double *rcm, double *mdip) {
+  const int nm = na / 3;
+  const double toK = 3.157733e+5, hbar = 1.0, tokgcm3 = 6.147323129e-3;
+  double tk;
+  kinetic_rpmd(p, na, tk, mass, nb);
+  double vrp = 0.0;
+  const double omegan = (double)nb / (beta * hbar);
+  if (nb > 0) {
+    for (int i = 0; i < na; ++i)
+      for (int k = 1; k <= nb; ++k) {
+        int k1 = k, k2 = k == 1 ? nb : k - 1;
+        const double *a = r + 3 * ((size_t)i + (size_t)na * (k1 - 1));
+        const double *b = r + 3 * ((size_t)i + (size_t)na * (k2 - 1));
+        double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+        double dist = (dx * dx + dy * dy + dz * dz);
+        vrp = vrp + 0.5 * mass[i] * (omegan * omegan) * dist;
+      }
+  }
+  double temp = toK * (2.0 * tk / ((double)(3 * na - P.nctot - 3) * (double)nb)) / (double)nb;
+  double tv, tvxyz[3], tq1, tq2;
+  virial_ke(r, dvdr, dvdr2, tv, tvxyz, tq1, tq2, beta, na, nb);
+  // pressure
+  double w = vir[0] + vir[4] + vir[8];
+  w = -w / 3.0;
+  double vol = box[0] * box[1] * box[2];
+  double pres = (2.0 * tv / 3.0 + w) / vol;
+  double ptail = 0.0;
+  if (P.oo_gam == 0.0) {
+    double pi = std::acos(-1.0);
+    double rho = (double)nm / vol;
+    double prefac = (16.0 * pi * (rho * rho) * P.oo_eps * (P.oo_sig * P.oo_sig * P.oo_sig)) / 3.0;
+    ptail = prefac * ((2.0 / 3.0) * std::pow(P.oo_sig / P.rcut, 9) - std::pow(P.oo_sig / P.rcut, 3));
+  }
+  pres = pres + ptail;
+  // dipole
+  double alpha2 = 0.5 * (1.0 - P.alpha);
+  double dipx = 0.0, dipy = 0.0, dipz = 0.0, dipm = 0.0;
+  std::vector<double> md(3 * (size_t)nm, 0.0);
+  for (int k = 0; k < nb; ++k)
+    for (int j = 0; j < na; j += 3) {
+      double fac1 = (z[j + 1] + alpha2 * z[j]);
+      double fac2 = (z[j + 2] + alpha2 * z[j]);
+      const double *ro = r + 3 * ((size_t)j + (size_t)na * k);
+      double d[3];
+      for (int x = 0; x < 3; ++x) d[x] = P.alpha * z[j] * ro[x] + fac1 * ro[3 + x] + fac2 * ro[6 + x];
+      dipx = dipx + d[0];
+      dipy = dipy + d[1];
+      dipz = dipz + d[2];
+      for (int x = 0; x < 3; ++x) md[3 * (size_t)(j / 3) + x] += d[x];
+      dipm = dipm + std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    }
+  dipm = dipm / (double)(nb * nm);
+  dipx = dipx / (double)nb;
+  dipy = dipy / (double)nb;
+  dipz = dipz / (double)nb;
+  if (mdip)
+    for (size_t i = 0; i < md.size(); ++i) mdip[i] = md[i] / nb;
+  // center_water: p(9, nm, nb) view of r
+  if (rcm) {
+    double wt = 1.0 / (double)nb;
+    for (int j = 0; j < nm; ++j) {
+      double pc[3] = {0, 0, 0};
+      for (int k = 0; k < nb; ++k) {
+        const double *q = r + 9 * ((size_t)j) + 3 * (size_t)na * k;
+        for (int x = 0; x < 3; ++x) pc[x] = pc[x] + q[x] + q[3 + x] + q[6 + x];
+      }
+      for (int x = 0; x < 3; ++x) rcm[3 * (size_t)j + x] = pc[x] * wt;
+    }
+  }
+  double wmass = mass[0] + mass[1] + mass[2];
+  out[0] = tk;
+  out[1] = vrp;
+  out[2] = nb * v + tk + vrp;
+  out[3] = temp;
+  out[4] = tv;
+  for (int x = 0; x < 3; ++x) out[5 + x] = tvxyz[x];
+  out[8] = pres;
+  out[9] = dipx;
+  out[10] = dipy;
+  out[11] = dipz;
+  out[12] = dipx * dipx + dipy * dipy + dipz * dipz;
+  out[13] = dipm;
+  out[14] = tokgcm3 * (wmass * (double)nm / vol);
+  out[15] = v;
+}
+
 // pshift (module_thermostat.f90:229-264)
 void pshift(double *p, const double *mass, int na, int nb) {
   double vx = 0.0, vy = 0.0, vz = 0.0, totmass = 0.0;

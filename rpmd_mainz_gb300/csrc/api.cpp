@@ -385,6 +385,58 @@ int gbrpmd_ctx_energies(gb_context *c, double *out5, double *vir, double *vir_lf
 
 void *gbrpmd_ctx_stream(gb_context *c) { return (void *)c->stream; }
 
+// md_eq's output block (md_eq.f90:190-299) on the resident state; see gbrpmd.h
+int gbrpmd_ctx_estimators(gb_context *c, double beta, double *out, double *rcm, double *mdip) {
+  if (!c || !out) return ctx_set_error(GB_E_ARG, "null argument");
+  if (!(beta > 0.0)) return ctx_set_error(GB_E_ARG, "beta must be positive");
+  if (!c->own_params) c->P = g_params;
+  const int na = c->na, nb = c->nb, nm = na / 3;
+  int st;
+  if (!c->est && (st = dalloc(c, &c->est, 16 + 6 * (size_t)nm))) return st;
+  double *d_rcm = rcm ? c->est + 16 : nullptr, *d_mdip = mdip ? c->est + 16 + 3 * (size_t)nm : nullptr;
+  CK(cudaMemsetAsync(c->est, 0, sizeof(double) * 16, c->stream));
+  launch_estimators(c->stream, c->r, c->p, c->dvdr, c->dvdr2, c->mass, c->z, na, nb, c->P.alpha, c->est, d_rcm,
+                    d_mdip);
+  ++c->launches;
+  CK(cudaGetLastError());
+  double a[16];
+  CK(cudaMemcpyAsync(a, c->est, sizeof(double) * 16, cudaMemcpyDeviceToHost, c->stream));
+  if (rcm) CK(cudaMemcpyAsync(rcm, d_rcm, sizeof(double) * 3 * nm, cudaMemcpyDeviceToHost, c->stream));
+  if (mdip) CK(cudaMemcpyAsync(mdip, d_mdip, sizeof(double) * 3 * nm, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const gb_params &P = c->P;
+  const double tk = a[0];                                      // kinetic_rpmd
+  const double omegan = (double)nb / (beta * GB_HBAR);         // md_eq.f90:254
+  const double vrp = 0.5 * omegan * omegan * a[1];
+  const double temp = GB_TO_K * (2.0 * tk / ((double)(3 * na - P.nctot - 3) * (double)nb)) / (double)nb;
+  const double tc = 0.5 * (double)(3 * na - 3 - P.nctot) / beta;  // virial_ke: nc = 3 (kinetic.f90:42-47)
+  const double tv = tc + 0.5 * a[2] / nb + 0.5 * a[3] / nb;
+  const double vol = c->box[0] * c->box[1] * c->box[2];
+  // pressure (md_pressure.f90:1-30) from the virial of the last evaluation and pres_lj_tail (32-56)
+  const double w = -(c->e_vir[0] + c->e_vir[4] + c->e_vir[8]) / 3.0;
+  double pres = (2.0 * tv / 3.0 + w) / vol;
+  if (P.oo_gam == 0.0) {
+    const double rho = (double)nm / vol, sr = P.oo_sig / P.rcut;
+    const double pi = std::acos(-1.0);
+    const double prefac = (16.0 * pi * (rho * rho) * P.oo_eps * (P.oo_sig * P.oo_sig * P.oo_sig)) / 3.0;
+    pres += prefac * ((2.0 / 3.0) * std::pow(sr, 9) - std::pow(sr, 3));
+  }
+  const double dip[3] = {a[10] / nb, a[11] / nb, a[12] / nb};
+  out[0] = tk;
+  out[1] = vrp;
+  out[2] = nb * c->e_v + tk + vrp;  // md_eq.f90:274 (times na)
+  out[3] = temp;
+  out[4] = tv;
+  for (int x = 0; x < 3; ++x) out[5 + x] = tc / 3.0 + 0.5 * a[4 + x] / nb + 0.5 * a[7 + x] / nb;
+  out[8] = pres;
+  for (int x = 0; x < 3; ++x) out[9 + x] = dip[x];
+  out[12] = dip[0] * dip[0] + dip[1] * dip[1] + dip[2] * dip[2];
+  out[13] = a[13] / ((double)nb * nm);
+  out[14] = GB_TO_KGCM3 * ((c->h_mass3[0] + c->h_mass3[1] + c->h_mass3[2]) * (double)nm / vol);  // md_eq.f90:196-198
+  out[15] = c->e_v;
+  return GB_OK;
+}
+
 int gbrpmd_ctx_set_profiling(gb_context *c, int on) {
   CK(cudaStreamSynchronize(c->stream));
   dev_graph_reset(c);

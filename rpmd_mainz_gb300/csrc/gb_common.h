@@ -22,6 +22,13 @@ enum AccSlot : int {
 };
 #define ACC_STRIDE 16
 
+// unit conversions of globals.inc:10-21 (CODATA values the reference uses)
+#define GB_TO_K 3.157733e+5        // hartree -> kelvin
+#define GB_TO_KJMOL 2625.49963     // hartree -> kJ/mol
+#define GB_TO_BAR 2.9421e+8        // hartree/bohr^3 -> bar
+#define GB_TO_KGCM3 6.147323129e-3 // electron masses per bohr^3 -> g/cm^3
+#define GB_HBAR 1.0
+
 // device status word bits (reported by gbrpmd_ctx_sync)
 #define ST_LIST_OVERFLOW 1u
 #define ST_NONFINITE 2u

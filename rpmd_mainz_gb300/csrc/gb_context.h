@@ -103,6 +103,7 @@ struct gb_context {
   double h_mass3[3] = {0, 0, 0};  // host copy of the O, H, H masses (ring_rpmd needs only these)
   int mass_version = 0;           // bumped when uploaded masses differ
   double *acc = nullptr;    // ACC_NSLOT * ACC_STRIDE
+  double *est = nullptr;    // estimator sums [16] and per-molecule outputs [2][nm][3] (lazy)
   unsigned *status = nullptr;
   double *h_acc = nullptr;  // pinned host mirror
   unsigned *h_status = nullptr;

@@ -93,6 +93,10 @@ void launch_intra(cudaStream_t s, const double *r, double *out, int na, int B, i
                   const gb_params &P, double *acc, int accumulate);
 void launch_virial_ke(cudaStream_t s, const double *r, const double *dvdr, const double *dvdr2,
                       int na, int nb, double *acc);
+// md_eq's output-step estimators (k_est.cu): acc[14] sums, optional rcm / mdip [nm][3]
+void launch_estimators(cudaStream_t s, const double *r, const double *p, const double *dvdr, const double *dvdr2,
+                       const double *mass, const double *z, int na, int nb, double alpha, double *acc, double *rcm,
+                       double *mdip);
 
 // ---- normal modes (k_modes.cu) ----
 void launch_realft(cudaStream_t s, const double *in, double *out, int m, int n, int mode,

@@ -67,6 +67,7 @@ def load(path=None):
     lib.gbrpmd_ctx_full_forces.argtypes = [C.c_void_p, D, D, D, D, D]
     lib.gbrpmd_ctx_evolve.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
     lib.gbrpmd_ctx_energies.argtypes = [C.c_void_p, D, D, D]
+    lib.gbrpmd_ctx_estimators.argtypes = [C.c_void_p, C.c_double, D, D, D]
     lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
     lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
     lib.gbrpmd_ctx_set_graphs.argtypes = [C.c_void_p, C.c_int]
@@ -268,6 +269,24 @@ class Context:
         _check(load().gbrpmd_ctx_energies(self.h, _ptr(out), _ptr(vir), _ptr(vir_lf)))
         return dict(v=out[0], vew=out[1], vlj=out[2], vint=out[3], tv=out[4], vir=vir.reshape(3, 3, order="F"),
                     vir_lf=vir_lf.reshape(3, 3, order="F"))
+
+    ESTIMATORS = ("tk", "vrp", "econs", "temp", "tv", "tvx", "tvy", "tvz", "pres", "dipx", "dipy", "dipz", "dip2",
+                  "dipm", "den", "v")
+
+    def estimators(self, beta, centroids=False, dipoles=False):
+        """md_eq's output-step estimators on the resident state (gbrpmd_ctx_estimators):
+        a dict of ESTIMATORS, plus 'rcm' / 'mdip' arrays (nm, 3) when asked."""
+        nm = self.na // 3
+        out = np.zeros(16)
+        rcm = np.zeros((nm, 3)) if centroids else None
+        mdip = np.zeros((nm, 3)) if dipoles else None
+        _check(load().gbrpmd_ctx_estimators(self.h, C.c_double(beta), _ptr(out), _ptr(rcm), _ptr(mdip)))
+        d = dict(zip(self.ESTIMATORS, out.tolist()))
+        if centroids:
+            d["rcm"] = rcm
+        if dipoles:
+            d["mdip"] = mdip
+        return d
 
     @property
     def stream(self):

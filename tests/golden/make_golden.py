@@ -13,6 +13,11 @@ Writes
                            box, and the initial CUB lattice vmd_start.xyz
   gentest_kat.json         the set-up values and initial energy printed in
                            `output`
+  gentest_eq.npz           eq.xyz (print_structure restart file, io.f90:1-17:
+                           the bead positions in bohr and the box after the
+                           1000 NPT equilibration steps) and the last lines of
+                           E_eq.out, virial_ke_eq.out and V_eq.out (md_eq.f90:
+                           274-277), printed at the same step
 Frames are written every pb = 20 steps of the two 2*nt = 250-step NVE
 trajectories of md_dynamics.f90 (trajectory(), lines 517-546): file frames
 0..11 belong to trajectory 1, 12..23 to trajectory 2.
@@ -69,6 +74,20 @@ def main(ref):
     data["start_box"] = sbox[0]
     data["frames"] = np.array(FRAMES)
     np.savez_compressed(os.path.join(HERE, "gentest_frames.npz"), **data)
+
+    with open(os.path.join(cmp_dir, "eq.xyz")) as f:
+        tok = f.read().split()
+    nm, na, nb = (int(t) for t in tok[:3])
+    box = np.array([float(t) for t in tok[3:6]])
+    r = np.array([float(t) for t in tok[6:6 + 3 * na * nb]]).reshape(nb, na, 3)
+
+    def last_line(name):
+        with open(os.path.join(cmp_dir, name)) as f:
+            return np.array([float(t) for t in f.read().split("\n")[-2].split()])
+
+    np.savez_compressed(os.path.join(HERE, "gentest_eq.npz"), r=r, box=box, nm=nm, na=na, nb=nb,
+                        E_eq=last_line("E_eq.out"), virial_ke_eq=last_line("virial_ke_eq.out"),
+                        V_eq=last_line("V_eq.out"))
 
     out = open(os.path.join(cmp_dir, "output")).read()
 

@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(ORACLE_DIR, "_build", "liborc.so")
 TOA = 0.5291772108
 TOFS = 41.341373
 KBOLTZ_MAIN = 3.166829e-6  # main.f90:168 literal
+TOKJMOL = 2625.49963  # globals.inc:18
 
 _lib = None
 
@@ -179,6 +180,25 @@ def virial_ke(r, dvdr, dvdr2, beta):
                          _ptr(np.ascontiguousarray(dvdr2)), C.byref(tv), _ptr(tvxyz), C.byref(tq1), C.byref(tq2),
                          C.c_double(beta), C.c_int(na), C.c_int(nb))
     return tv.value, tvxyz, tq1.value, tq2.value
+
+
+ESTIMATORS = ("tk", "vrp", "econs", "temp", "tv", "tvx", "tvy", "tvz", "pres", "dipx", "dipy", "dipz", "dip2",
+              "dipm", "den", "v")
+
+
+def estimators(r, p, dvdr, dvdr2, mass, z, beta, v, vir, box):
+    """md_eq's output-step estimators (orc md_eq_estimators); vir column-major 3x3."""
+    nb, na, _ = r.shape
+    nm = na // 3
+    out, rcm, mdip = np.zeros(16), np.zeros((nm, 3)), np.zeros((nm, 3))
+    load().orc_md_eq_estimators(_ptr(np.ascontiguousarray(r)), _ptr(np.ascontiguousarray(p)),
+                                _ptr(np.ascontiguousarray(dvdr)), _ptr(np.ascontiguousarray(dvdr2)),
+                                _ptr(np.asarray(mass, float)), _ptr(np.asarray(z, float)), C.c_int(na), C.c_int(nb),
+                                C.c_double(beta), C.c_double(v), _ptr(np.asfortranarray(vir).ravel(order="F").copy()),
+                                _ptr(np.asarray(box, float)), _ptr(out), _ptr(rcm), _ptr(mdip))
+    d = dict(zip(ESTIMATORS, out.tolist()))
+    d["rcm"], d["mdip"] = rcm, mdip
+    return d
 
 
 def rattle_setup(nm):

@@ -100,3 +100,26 @@ def test_evolve_pi_replay(fa, fb):
     F = -(st.dvdr + st.dvdr2)
     Fref = np.stack([GOLD["frc1"][fb], GOLD["frc2"][fb]])
     assert np.linalg.norm(F - Fref) / np.linalg.norm(Fref) < 1e-11
+
+
+EQ = np.load(os.path.join(systems.GOLDEN, "gentest_eq.npz"))
+
+
+def test_md_eq_estimators_at_eq_restart():
+    # eq.xyz is the state after md_eq's last step; E_eq.out, V_eq.out and
+    # virial_ke_eq.out print that step's estimators (md_eq.f90:190-277) from
+    # the positions and the forces of the same evaluation.  The momenta are not
+    # in the file, so tk and the conserved energy are left out here.
+    s = gentest_system()
+    r, box = EQ["r"], EQ["box"]
+    na, nm, nb = s["na"], s["nm"], s["nb"]
+    ff = orc.full_forces(r, box, s["z"])
+    assert ff["status"] == 0
+    est = orc.estimators(r, np.zeros_like(r), ff["dvdr"], ff["dvdr2"], s["mass"], s["z"], s["beta"], ff["v"],
+                         ff["vir"], box)
+    E, V, TV = EQ["E_eq"], EQ["V_eq"], EQ["virial_ke_eq"]
+    assert abs(est["vrp"] / na - E[2]) <= 5e-9                      # f13.8
+    assert abs(nb * est["v"] / na - E[3]) <= 5e-9
+    assert abs(est["v"] - V[1]) <= 5e-7                             # f14.6
+    assert abs(orc.TOKJMOL * est["v"] / na - V[2]) <= 5e-7
+    assert abs(orc.TOKJMOL * est["tv"] / nm - TV[1]) <= 1e-13 * abs(TV[1])  # list-directed, full precision
