@@ -450,7 +450,7 @@ def run_nve(args, torch):
     (md_eq.f90:274) every 100 steps; drift = least-squares slope."""
     from rpmd_mainz_gb300 import lib, system
 
-    s = system.water_box(PARAM, ncell=(6, 6, 6), nb=32, mts=1, dtfs=0.5)
+    s = system.water_box(PARAM, ncell=(6, 6, 6), nb=32, mts=1, dtfs=args.nve_dtfs)
     irun = C.c_int(-4711)
     s["p"] = system.sample_momenta(s["na"], s["nb"], s["mass"], s["beta"], irun)
     na, nm, nb, dt, beta = s["na"], s["nm"], s["nb"], s["dt"], s["beta"]
@@ -486,7 +486,7 @@ def run_nve(args, torch):
         virial.append(float(np.linalg.norm(fmx["vir"] - f64["vir"]) / np.linalg.norm(f64["vir"])))
 
     r0, p0 = snaps[-1][0], snaps[-1][1]
-    nsteps = int(round(args.nve_ps * 1000.0 / 0.5))
+    nsteps = int(round(args.nve_ps * 1000.0 / args.nve_dtfs))
     block = 100
     arms = {}
     for name, prec in (("mixed", 1), ("fp64", 0)):
@@ -508,14 +508,16 @@ def run_nve(args, torch):
                     e1.record(stream)
                 e1.synchronize()
                 ms += e0.elapsed_time(e1)
-                e_t.append((b + 1) * block * 0.5e-3)  # ps
+                e_t.append((b + 1) * block * args.nve_dtfs * 1e-3)  # ps
                 e_h.append(c.estimators(beta)["econs"])
         c.sync()
         t = np.array(e_t) * 1e-3  # ns
         e = np.array(e_h) * 2625.49963 / nm  # kJ/mol per molecule
         slope, icpt = np.polyfit(t, e, 1)
+        e_ref = abs(float(e[0]))
         arms[name] = {"value": nsteps * nb * nm / (ms * 1e-3), "ms_per_step": ms / nsteps,
                       "drift_kjmol_per_ns_per_molecule": float(slope),
+                      "drift_relative_per_ns": float(slope) / e_ref,
                       "fluctuation_rms_kjmol_per_molecule": float(np.std(e - (slope * t + icpt))),
                       "econs_first_last_kjmol_per_molecule": [float(e[0]), float(e[-1])],
                       "gpu_launches": int(c.launches - launches0 - (nsteps // block)), "clocks": clk.summary()}
@@ -526,7 +528,7 @@ def run_nve(args, torch):
         "steps": nsteps, "warmup": 0, "ms_per_step": mx["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 mixed",
         "data": "synthetic (CUB lattice, momenta from the reference's ran2 stream, FP64 Andersen NVT snapshots)",
-        "config": {"workload": "qspcfw_216_nb32_nve", "nm": nm, "nb": nb, "dt_fs": 0.5, "nve_ps": args.nve_ps,
+        "config": {"workload": "qspcfw_216_nb32_nve", "nm": nm, "nb": nb, "dt_fs": args.nve_dtfs, "nve_ps": args.nve_ps,
                    "snapshots": len(snaps), "l2": "state smaller than L2 (resident NVE run, no flush)",
                    "parallelism": "single GPU"},
         "gpu_launches": mx["gpu_launches"],
@@ -602,6 +604,7 @@ def main():
     ap.add_argument("--slots", type=int, default=32)
     ap.add_argument("--budget-gb", type=int, default=64)
     ap.add_argument("--nve-ps", type=float, default=10.0, help="NVE length of the qspcfw_216_nb32_nve workload")
+    ap.add_argument("--nve-dtfs", type=float, default=0.5, help="time step (fs) of the qspcfw_216_nb32_nve workload")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -25,19 +25,38 @@ GB_HD constexpr int gb_bitrev(int i, int h) {
   return r;
 }
 
+GB_D float gb_fma(float a, float b, float c) { return fmaf(a, b, c); }
+GB_D double gb_fma(double a, double b, double c) { return fma(a, b, c); }
+
+// Table products.  With SPLIT each table value is the pair hi + lo (hi the
+// value rounded to R, lo the rounding remainder), and a product v * x is formed
+// as fma(hi, x, lo * x): the table then carries ~2x the precision of R, so a
+// forward and an inverse transform compose to the identity up to the rounding
+// of the data alone (which is unbiased), instead of up to a fixed error of the
+// rounded twiddles that repeats in every round trip.
+template <bool SPLIT, typename R>
+GB_D R gb_tmul(const R *__restrict__ hi, const R *__restrict__ lo, int i, R x) {
+  if constexpr (SPLIT) return gb_fma(hi[i], x, lo[i] * x);
+  else return hi[i] * x;
+}
+
 // one radix-2 stage of butterfly span LEN (template recursion keeps every index
 // a compile-time constant, so the arrays stay in registers)
-template <int H, int N, bool INV, int LEN, typename R>
-GB_D void gb_cfft_stage(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw) {
+template <int H, int N, bool INV, int LEN, typename R, bool SPLIT>
+GB_D void gb_cfft_stage(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw, const R *__restrict__ twl) {
   if constexpr (LEN <= H) {
     constexpr int half = LEN / 2;
 #pragma unroll
     for (int k = 0; k < half; ++k) {
       const int m = k * (N / LEN);
-      R wr = (R)1, wi = (R)0;
+      R wr = (R)1, wi = (R)0, wrl = (R)0, wil = (R)0;
       if (k > 0 && 4 * m != N) {
         wr = tw[m];
         wi = INV ? tw[N + m] : -tw[N + m];
+        if constexpr (SPLIT) {
+          wrl = twl[m];
+          wil = INV ? twl[N + m] : -twl[N + m];
+        }
       }
 #pragma unroll
       for (int i = 0; i < H; i += LEN) {
@@ -49,6 +68,9 @@ GB_D void gb_cfft_stage(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw) {
         } else if (4 * m == N) {  // w = -i (forward) or +i (inverse): no multiplication
           tr = INV ? -zi[b] : zi[b];
           ti = INV ? zr[b] : -zr[b];
+        } else if constexpr (SPLIT) {
+          tr = gb_fma(zr[b], wr, gb_fma(-zi[b], wi, zr[b] * wrl - zi[b] * wil));
+          ti = gb_fma(zr[b], wi, gb_fma(zi[b], wr, zr[b] * wil + zi[b] * wrl));
         } else {
           tr = zr[b] * wr - zi[b] * wi;
           ti = zr[b] * wi + zi[b] * wr;
@@ -59,14 +81,14 @@ GB_D void gb_cfft_stage(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw) {
         zi[a] = zi[a] + ti;
       }
     }
-    gb_cfft_stage<H, N, INV, 2 * LEN, R>(zr, zi, tw);
+    gb_cfft_stage<H, N, INV, 2 * LEN, R, SPLIT>(zr, zi, tw, twl);
   }
 }
 
 // in-place radix-2 complex FFT of length H on register arrays; N = table length
-// (a multiple of H); INV selects exp(+...) twiddles
-template <int H, int N, bool INV, typename R>
-GB_D void gb_cfft(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw) {
+// (a multiple of H); INV selects exp(+...) twiddles; twl: the lo parts (SPLIT)
+template <int H, int N, bool INV, typename R, bool SPLIT = false>
+GB_D void gb_cfft(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw, const R *__restrict__ twl = nullptr) {
 #pragma unroll
   for (int i = 0; i < H; ++i) {
     const int j = gb_bitrev(i, H);
@@ -75,7 +97,7 @@ GB_D void gb_cfft(R (&zr)[H], R (&zi)[H], const R *__restrict__ tw) {
       t = zi[i]; zi[i] = zi[j]; zi[j] = t;
     }
   }
-  gb_cfft_stage<H, N, INV, 2, R>(zr, zi, tw);
+  gb_cfft_stage<H, N, INV, 2, R, SPLIT>(zr, zi, tw, twl);
 }
 
 // unscaled R2HC of length N (power of two) in registers
@@ -91,7 +113,7 @@ GB_D void gb_r2hc(const double (&x)[N], double (&out)[N], const double *__restri
       zr[j] = x[2 * j];
       zi[j] = x[2 * j + 1];
     }
-    if constexpr (H > 1) gb_cfft<H, N, false>(zr, zi, tw);
+    if constexpr (H > 1) gb_cfft<H, N, false, double>(zr, zi, tw);
     out[0] = zr[0] + zi[0];
     out[H] = zr[0] - zi[0];
 #pragma unroll
@@ -127,7 +149,7 @@ GB_D void gb_hc2r(const double (&in)[N], double (&x)[N], const double *__restric
       zr[k] = er - oi;
       zi[k] = ei + orr;
     }
-    if constexpr (H > 1) gb_cfft<H, N, true>(zr, zi, tw);
+    if constexpr (H > 1) gb_cfft<H, N, true, double>(zr, zi, tw);
 #pragma unroll
     for (int j = 0; j < H; ++j) {
       x[2 * j] = 2.0 * zr[j];
@@ -185,12 +207,15 @@ GB_D void gb_hc2r_direct(const double *in, double *x, int n, const double *__res
 // pre-scaled twiddle tables:
 //   twf[m] = (sc / 2) cos(2 pi m / n), twf[n + m] = (sc / 2) sin(...)  (forward)
 //   twi[m] = sc cos(2 pi m / n),       twi[n + m] = sc sin(...)        (inverse)
-// tw is the unscaled table of the complex FFT.
-template <int N, typename R = double, class In, class Out>
-GB_D void gb_r2hc_s(In in, Out out, const R *__restrict__ tw, const R *__restrict__ twf) {
-  const R sc = twf[0] + twf[0];
+// tw is the unscaled table of the complex FFT.  SPLIT: tw_l / twf_l / twi_l
+// hold the lo parts of the three tables (gb_tmul).
+template <int N, typename R = double, bool SPLIT = false, class In, class Out>
+GB_D void gb_r2hc_s(In in, Out out, const R *__restrict__ tw, const R *__restrict__ twf,
+                    const R *__restrict__ tw_l = nullptr, const R *__restrict__ twf_l = nullptr) {
+  // sc = 2 twf[0] (exact doubling of both parts)
+  auto scm = [&](R x) { return (R)2 * gb_tmul<SPLIT, R>(twf, twf_l, 0, x); };
   if constexpr (N == 1) {
-    out(0, sc * in(0));
+    out(0, scm(in(0)));
   } else {
     constexpr int H = N / 2;
     R zr[H], zi[H];
@@ -199,51 +224,68 @@ GB_D void gb_r2hc_s(In in, Out out, const R *__restrict__ tw, const R *__restric
       zr[j] = in(2 * j);
       zi[j] = in(2 * j + 1);
     }
-    if constexpr (H > 1) gb_cfft<H, N, false, R>(zr, zi, tw);
-    out(0, sc * (zr[0] + zi[0]));
-    out(H, sc * (zr[0] - zi[0]));
+    if constexpr (H > 1) gb_cfft<H, N, false, R, SPLIT>(zr, zi, tw, tw_l);
+    out(0, scm(zr[0] + zi[0]));
+    out(H, scm(zr[0] - zi[0]));
 #pragma unroll
     for (int k = 1; 2 * k < H; ++k) {
       const int b = H - k;
       const R P = zr[k] + zr[b], Q = zi[k] + zi[b];
       const R Rd = zr[k] - zr[b], D = zi[k] - zi[b];
-      const R hc = twf[k], hs = twf[N + k];
-      const R hP = twf[0] * P, hD = twf[0] * D;
-      const R T1 = hc * Q - hs * Rd, T2 = hc * Rd + hs * Q;
+      const R hP = gb_tmul<SPLIT, R>(twf, twf_l, 0, P), hD = gb_tmul<SPLIT, R>(twf, twf_l, 0, D);
+      R T1, T2;
+      if constexpr (SPLIT) {
+        const R hc = twf[k], hs = twf[N + k], hcl = twf_l[k], hsl = twf_l[N + k];
+        T1 = gb_fma(hc, Q, gb_fma(-hs, Rd, hcl * Q - hsl * Rd));
+        T2 = gb_fma(hc, Rd, gb_fma(hs, Q, hcl * Rd + hsl * Q));
+      } else {
+        const R hc = twf[k], hs = twf[N + k];
+        T1 = hc * Q - hs * Rd;
+        T2 = hc * Rd + hs * Q;
+      }
       out(k, hP + T1);
       out(b, hP - T1);
       out(N - k, hD - T2);
       out(N - b, -hD - T2);
     }
     if constexpr (H % 2 == 0) {  // k = H/2 = n/4: cos = 0, sin = 1
-      out(H / 2, sc * zr[H / 2]);
-      out(N - H / 2, -sc * zi[H / 2]);
+      out(H / 2, scm(zr[H / 2]));
+      out(N - H / 2, -scm(zi[H / 2]));
     }
   }
 }
 
-template <int N, typename R = double, class In, class Out>
-GB_D void gb_hc2r_s(In in, Out out, const R *__restrict__ tw, const R *__restrict__ twi) {
-  const R sc = twi[0];
+template <int N, typename R = double, bool SPLIT = false, class In, class Out>
+GB_D void gb_hc2r_s(In in, Out out, const R *__restrict__ tw, const R *__restrict__ twi,
+                    const R *__restrict__ tw_l = nullptr, const R *__restrict__ twi_l = nullptr) {
+  auto scm = [&](R x) { return gb_tmul<SPLIT, R>(twi, twi_l, 0, x); };  // sc = twi[0]
   if constexpr (N == 1) {
-    out(0, sc * in(0));
+    out(0, scm(in(0)));
   } else {
     constexpr int H = N / 2;
     R zr[H], zi[H];
     {
       const R i0 = in(0), ih = in(H);
-      zr[0] = sc * (i0 + ih);
-      zi[0] = sc * (i0 - ih);
+      zr[0] = scm(i0 + ih);
+      zi[0] = scm(i0 - ih);
     }
 #pragma unroll
     for (int k = 1; 2 * k < H; ++k) {
       const int b = H - k;
       // X_k = in(k) + i in(N-k), conj(X_{H-k}) = in(H-k) - i in(H+k)
       const R xr = in(k), xi = in(N - k), cr = in(b), ci = -in(H + k);
-      const R A = sc * (xr + cr), B = sc * (xi + ci);
+      const R A = scm(xr + cr), B = scm(xi + ci);
       const R dr = xr - cr, di = xi - ci;
-      const R c = twi[k], s = twi[N + k];
-      const R U = c * di + s * dr, V = c * dr - s * di;
+      R U, V;
+      if constexpr (SPLIT) {
+        const R c = twi[k], s = twi[N + k], cl = twi_l[k], sl = twi_l[N + k];
+        U = gb_fma(c, di, gb_fma(s, dr, cl * di + sl * dr));
+        V = gb_fma(c, dr, gb_fma(-s, di, cl * dr - sl * di));
+      } else {
+        const R c = twi[k], s = twi[N + k];
+        U = c * di + s * dr;
+        V = c * dr - s * di;
+      }
       zr[k] = A - U;
       zr[b] = A + U;
       zi[k] = B + V;
@@ -251,10 +293,10 @@ GB_D void gb_hc2r_s(In in, Out out, const R *__restrict__ tw, const R *__restric
     }
     if constexpr (H % 2 == 0) {  // k = H/2: cos = 0, sin = 1
       const R xr = in(H / 2), xi = in(N - H / 2);
-      zr[H / 2] = (R)2 * sc * xr;
-      zi[H / 2] = (R)-2 * sc * xi;
+      zr[H / 2] = (R)2 * scm(xr);
+      zi[H / 2] = (R)-2 * scm(xi);
     }
-    if constexpr (H > 1) gb_cfft<H, N, true, R>(zr, zi, tw);
+    if constexpr (H > 1) gb_cfft<H, N, true, R, SPLIT>(zr, zi, tw, tw_l);
 #pragma unroll
     for (int j = 0; j < H; ++j) {
       out(2 * j, zr[j]);

@@ -231,6 +231,9 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
   float *s_tw = s_ml + 12 * NB;                    // [2*NB] cos, sin
   float *s_twf = s_tw + 2 * NB;                    // scaled by sqrt(1/nb) / 2
   float *s_twi = s_twf + 2 * NB;                   // scaled by sqrt(1/nb)
+  float *s_tw_l = s_twi + 2 * NB;                  // lo parts of the three tables
+  float *s_twf_l = s_tw_l + 2 * NB;
+  float *s_twi_l = s_twf_l + 2 * NB;
   const int t = threadIdx.x;
   const double sc = sqrt(1.0 / (double)NB);
   for (int i = t; i < 12 * NB; i += T) {
@@ -241,10 +244,13 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
     if (i < 12) s_mono[i] = w;
   }
   for (int i = t; i < 2 * NB; i += T) {
-    const double w = a.tw[i];
+    const double w = a.tw[i], wf = (0.5 * sc) * w, wi = sc * w;
     s_tw[i] = (float)w;
-    s_twf[i] = (float)((0.5 * sc) * w);
-    s_twi[i] = (float)(sc * w);
+    s_twf[i] = (float)wf;
+    s_twi[i] = (float)wi;
+    s_tw_l[i] = (float)(w - (double)s_tw[i]);
+    s_twf_l[i] = (float)(wf - (double)s_twf[i]);
+    s_twi_l[i] = (float)(wi - (double)s_twi[i]);
   }
   const int mpb = a.mpb;
   const int m0 = blockIdx.x * mpb;
@@ -273,7 +279,10 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
       float d[NB];
 #pragma unroll
       for (int j = 0; j < NB; ++j) d[j] = (float)(v[j] - v0);
-      gb_r2hc_s<NB, float>([&](int j) { return d[j]; }, [&](int k, float val) { out[k] = val; }, s_tw, s_twf);
+      // the state's round trip (this forward transform, the inverse at the end
+      // of the step) uses split tables: no systematic gain per step
+      gb_r2hc_s<NB, float, true>([&](int j) { return d[j]; }, [&](int k, float val) { out[k] = val; }, s_tw, s_twf,
+                                 s_tw_l, s_twf_l);
       return sc * sum;
     };
 #pragma unroll
@@ -313,8 +322,19 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
     off = (float)(cen - s_cen[orow]);
     {  // bead positions relative to the oxygen centroid (evolve_pi.f90:141-145)
       float *dst = s_dev + t * C::LD;
-      gb_hc2r_s<NB, float>([&](int j) { return j ? xf[j] : 0.f; }, [&](int k, float v) { dst[k] = off + v; }, s_tw,
-                           s_twi);
+      if (im == a.mts) {  // the last substep's positions are the new state: split tables,
+                          // and r = centroid + deviation without the offset's rounding
+        double *gr = a.r + row;
+        gb_hc2r_s<NB, float, true>([&](int j) { return j ? xf[j] : 0.f; },
+                                   [&](int k, float v) {
+                                     dst[k] = off + v;
+                                     if (valid) gr[S * k] = cen + (double)v;
+                                   },
+                                   s_tw, s_twi, s_tw_l, s_twi_l);
+      } else {
+        gb_hc2r_s<NB, float>([&](int j) { return j ? xf[j] : 0.f; }, [&](int k, float v) { dst[k] = off + v; },
+                             s_tw, s_twi);
+      }
     }
     __syncthreads();
     double e_sub = 0.0;
@@ -364,21 +384,20 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
     if (im != a.mts) __syncthreads();
   }
   {
-    // back to beads: p = HC2R(p); r = rst; p -= halfdtsmall dvdr2 (evolve_pi.f90:222-228)
-    const float *dev_row = s_dev + t * C::LD;
+    // back to beads: p = HC2R(p); r = rst (written in the last substep);
+    // p -= halfdtsmall dvdr2 (evolve_pi.f90:222-228)
     const float *f2_row = s_f2 + t * C::LD;
     const float hds = (float)a.halfdtsmall;
-    const double pc = sc * p0, cen = sc * x0;
+    const double pc = sc * p0;
     double *gp = a.p + row;
-    gb_hc2r_s<NB, float>([&](int j) { return j ? pf[j] : 0.f; },
-                         [&](int k, float v) {
-                           if (valid) gp[S * k] = pc + (double)fmaf(-hds, f2_row[k], v);
-                         },
-                         s_tw, s_twi);
+    gb_hc2r_s<NB, float, true>([&](int j) { return j ? pf[j] : 0.f; },
+                               [&](int k, float v) {
+                                 if (valid) gp[S * k] = pc + (double)fmaf(-hds, f2_row[k], v);
+                               },
+                               s_tw, s_twi, s_tw_l, s_twi_l);
     if (valid) {
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
-        a.r[row + S * j] = cen + (double)(dev_row[j] - off);
         a.rnm[row + S * j] = j ? (double)xf[j] : x0;
         a.dvdr2[row + S * j] = (double)f2_row[j];
       }
@@ -418,7 +437,7 @@ size_t mts_smem_mixed(int T) {
   using C = MtsCfg<NB>;
   const int nrow = (T + 8) / 9 * 9;
   const int nf = (3 * nrow * C::LD + 1) & ~1;
-  return sizeof(float) * nf + sizeof(double) * (nrow + 12 + 32 * 18) + sizeof(float) * (24 * NB + 6 * NB);
+  return sizeof(float) * nf + sizeof(double) * (nrow + 12 + 32 * 18) + sizeof(float) * (24 * NB + 12 * NB);
 }
 
 template <int NB>

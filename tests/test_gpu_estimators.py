@@ -87,3 +87,35 @@ def test_estimators_at_reference_restart():
     assert abs(nb * est["v"] / na - E[3]) <= 5e-9
     assert abs(est["v"] - V[1]) <= 5e-7
     assert abs(orc.TOKJMOL * est["tv"] / nm - TV[1]) <= 1e-12 * abs(TV[1])
+
+
+def test_mixed_conserved_energy_tracks_fp64():
+    # NVE (no thermostat), 216 H2O, nb = 8, dt 0.5 fs: the conserved RPMD
+    # energy nb*v + tk + vrp of the mixed path stays with the FP64 path's over
+    # 400 steps (both trajectories start from the same state); bound 2e-6 of
+    # the conserved energy.  Before the normal-mode transforms of the state
+    # used split twiddle tables, the FP32 round trip shrank the bead deviations
+    # by a fixed ~3e-8 per step and the difference grew linearly to 2e-5.
+    s = systems.build(param="param_qspcfw", ncell=(6, 6, 6), nb=8, therm="NON")
+    r = systems.perturbed(s, seed=9)
+    p = orc.sample_rpmd(s["na"], s["nb"], s["mass"], s["beta"], orc.Rng(21))
+    series = {}
+    for prec in (0, 1):
+        prm = s["params"].copy()
+        prm.precision = prec
+        lib.init(prm)
+        ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+        try:
+            ctx.set_params(prm)
+            ctx.upload(r=r, p=p, box=s["box"])
+            ctx.full_forces()
+            e = [ctx.estimators(s["beta"])["econs"]]
+            for _ in range(8):
+                ctx.evolve(50, s["dt"], s["beta"])
+                e.append(ctx.estimators(s["beta"])["econs"])
+        finally:
+            ctx.close()
+        series[prec] = np.array(e)
+    e64, emx = series[0], series[1]
+    scale = np.abs(e64).max()
+    assert np.abs(emx - e64).max() <= 2e-6 * scale, (emx - e64) / scale
