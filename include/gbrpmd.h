@@ -53,6 +53,12 @@ extern "C" {
 #define GB_THERM_PRG 2  /* global Parrinello kick inside evolve_pi (evolve_pi.f90:73) */
 #define GB_THERM_PRL 3  /* local Langevin kick inside evolve_pi  (evolve_pi.f90:75) */
 
+/* barostat selector (module barostat, `baro`, module_barostat.f90:5), used when
+   evolve_pi is called with nbaro = 1 (md_eq.f90:55-58: ens = 'NPT') */
+#define GB_BARO_NONE 0
+#define GB_BARO_BER 1   /* Berendsen, beren_baro (module_barostat.f90:88-129), cubic boxes */
+#define GB_BARO_MCI 2   /* Monte Carlo volume moves (mc_baro): not on the device path  */
+
 /* intramolecular model selector */
 #define GB_INTRA_REFERENCE 0 /* potenl_opt dispatch (md_forces.f90:254-263)         */
 #define GB_INTRA_SPCFW 1     /* intra_spcfw (intra_spcfw.f90), commented out in ref */
@@ -88,12 +94,13 @@ typedef struct gb_params {
   /* module thermostat: therm, ttau  (module_thermostat.f90:3-4) */
   int32_t therm;
   double ttau;
-  /* module barostat: taub, patm (module_barostat.f90:3-5); the barostat
-     itself is not part of the device path, these are carried for callers */
+  /* module barostat: taub, patm (module_barostat.f90:3-5), in atomic units
+     as main.f90:166,263 converts them (taub = tofs * taufs, patm = pres / tobar) */
   double taub, patm;
   /* selectors of this library */
   int32_t intra_model; /* GB_INTRA_* */
   int32_t precision;   /* GB_PREC_*  */
+  int32_t baro;        /* GB_BARO_*: module barostat's `baro` */
 } gb_params;
 
 /* ---- set-up --------------------------------------------------------------- */

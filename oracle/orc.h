@@ -94,6 +94,14 @@ void force_contract(double *dvdr, double *dvdr_c, int na, int nb, int nb_c);
 void virial_ke(const double *r, const double *dvdr, const double *dvdr2, double &tv,
                double tvxyz[3], double &tq1, double &tq2, double beta, int na, int nb);
 void kinetic_rpmd(const double *p, int na, double &tk, const double *mass, int nb);
+double pressure(const double vir[9], double tv, int na, const double box[3]);
+void beren_baro(const double vir[9], double tv, double dt, double *r, double box[3], int na, int nb);
+// md_eq's step loops (md_eq.f90:55-323) without file output: for ens != NVT
+// the nq-step NVT pre-equilibration, then ne steps with nbaro = npt; per step
+// the values md_eq prints (see orc_md_eq)
+Status md_eq(double *p, double *r, double *dvdr, double *dvdr2, double dt, const double *mass, int na, int nb,
+             double box[3], const double *z, double beta, int ne, int npre_eq, int npt, double ttaufs, Rng &g,
+             int &irun, double *pre_out, double *eq_out);
 // md_eq's output block (md_eq.f90:190-299): out[16] in the order of
 // gbrpmd_ctx_estimators; rcm, mdip [nm][3] optional
 void md_eq_estimators(const double *r, const double *p, const double *dvdr, const double *dvdr2,

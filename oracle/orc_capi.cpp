@@ -143,6 +143,13 @@ int orc_run_steps(double *p, double *r, double *dvdr, double *dvdr2, double dt, 
   return GB_OK;
 }
 
+int orc_md_eq(double *p, double *r, double *dvdr, double *dvdr2, double dt, const double *mass, int na, int nb,
+              double *box, const double *z, double beta, int ne, int npre_eq, int npt, double ttaufs, void *g,
+              int *irun, double *pre_out, double *eq_out) {
+  return md_eq(p, r, dvdr, dvdr2, dt, mass, na, nb, box, z, beta, ne, npre_eq, npt, ttaufs, *(Rng *)g, *irun,
+               pre_out, eq_out);
+}
+
 // ---- throughput of independent replicas on host threads ----
 // Runs `nthreads` copies of the same trajectory state, each on its own thread
 // for nsteps evolve_pi steps (no thermostat collisions), and returns the wall

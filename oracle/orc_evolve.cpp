@@ -5,6 +5,7 @@
 // module_thermostat.f90 (sample_rpmd, pshift, parinello_therm,
 // parinello_therm_loc), md_rattle.f90 and evolve_rigid.f90 (evolve_rig_pi,
 // bead_forces).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -285,6 +286,50 @@ void parinello_therm_loc(double *p, const double *mass, double tau, int na, int 
     }
 }
 
+// pressure (md_pressure.f90:1-30) with pres_lj_tail (md_pressure.f90:32-56)
+double pressure(const double vir[9], double tv, int na, const double box[3]) {
+  double w = vir[0] + vir[4] + vir[8];
+  w = -w / 3.0;
+  double vol = box[0] * box[1] * box[2];
+  double pres = (2.0 * tv / 3.0 + w) / vol;
+  double ptail = 0.0;
+  if (P.oo_gam == 0.0) {
+    int nm = na / 3;
+    double pi = std::acos(-1.0);
+    double rho = (double)nm / vol;
+    double prefac = (16.0 * pi * (rho * rho) * P.oo_eps * (P.oo_sig * P.oo_sig * P.oo_sig)) / 3.0;
+    ptail = prefac * ((2.0 / 3.0) * std::pow(P.oo_sig / P.rcut, 9) - std::pow(P.oo_sig / P.rcut, 3));
+  }
+  return pres + ptail;
+}
+
+// beren_baro (module_barostat.f90:88-129): isotropic Berendsen scaling of the
+// box and of each water's center_water vector (md_tools.f90:367-390)
+void beren_baro(const double vir[9], double tv, double dt, double *r, double box[3], int na, int nb) {
+  double pres = pressure(vir, tv, na, box);
+  int nm = na / 3;
+  double compi = 13531.0;
+  double bstat = compi / (3.0 * P.taub);
+  double scale = std::fabs(1.0 - (dt * bstat) * (P.patm - pres));
+  for (int d = 0; d < 3; ++d) box[d] = scale * box[d];
+  std::vector<double> rcm(3 * (size_t)nm, 0.0);
+  double wt = 1.0 / (double)nb;
+  for (int j = 0; j < nm; ++j) {
+    double pc[3] = {0, 0, 0};
+    for (int k = 0; k < nb; ++k) {
+      const double *q = r + 9 * (size_t)j + 3 * (size_t)na * k;
+      for (int x = 0; x < 3; ++x) pc[x] = pc[x] + q[x] + q[3 + x] + q[6 + x];
+    }
+    for (int x = 0; x < 3; ++x) rcm[3 * (size_t)j + x] = pc[x] * wt;
+  }
+  for (int i = 0; i < nm; ++i)
+    for (int k = 0; k < nb; ++k)
+      for (int a = 0; a < 3; ++a) {
+        double *q = r + 3 * ((size_t)(3 * i + a) + (size_t)na * k);
+        for (int x = 0; x < 3; ++x) q[x] = q[x] + rcm[3 * (size_t)i + x] * (scale - 1.0);
+      }
+}
+
 // evolve_pi (evolve_pi.f90:1-322), type = 'RPMD'
 Status evolve_pi(double *p, double *r, double &v, double &vew, double &vlj, double &vint,
                  double *dvdr, double *dvdr2, double dt, const double *mass, int na, int nb,
@@ -347,7 +392,12 @@ Status evolve_pi(double *p, double *r, double &v, double &vew, double &vlj, doub
   for (int i = 0; i < 9; ++i) vir[i] = vir_lf[i] + vir_hf[i];
   if (tv_out) *tv_out = tv;
 
-  if (nbaro == 1) return GB_E_UNSUPPORTED;  // beren_driver / mc_baro (module_barostat.f90)
+  if (nbaro == 1) {  // evolve_pi.f90:176-189: beren_driver on the bead positions rst
+    if (P.baro != GB_BARO_BER || !P.iamcub) return GB_E_UNSUPPORTED;  // mc_baro, beren_baro_nc
+    beren_baro(vir, tv, dt, rst.data(), box, na, nb);
+    std::memcpy(r, rst.data(), sizeof(double) * N);
+    realft(r, 3 * na, nb, +1);
+  }
 
   const int nbdf1 = P.nbdf1, nbdf2 = P.nbdf2;
   if (nbdf1 > 0) {
@@ -628,6 +678,105 @@ Status evolve_rig_pi(const Rattle &rt, double *p, double *r, double &v, double &
   if (nbaro == 1) return GB_E_UNSUPPORTED;
   v_lf = v;
   v_hf = 0.0;
+  return GB_OK;
+}
+
+// ring-polymer spring energy as md_eq computes it (md_eq.f90:119-136, 252-270)
+static double spring_energy(const double *r, const double *mass, int na, int nb, double beta) {
+  const double hbar = 1.0;
+  double vrp = 0.0;
+  double omegan = (double)nb / (beta * hbar);
+  if (nb > 0)
+    for (int i = 0; i < na; ++i)
+      for (int k = 1; k <= nb; ++k) {
+        int k1 = k, k2 = k == 1 ? nb : k - 1;
+        const double *a = r + 3 * ((size_t)i + (size_t)na * (k1 - 1));
+        const double *b = r + 3 * ((size_t)i + (size_t)na * (k2 - 1));
+        double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+        double dist = (dx * dx + dy * dy + dz * dz);
+        vrp = vrp + 0.5 * mass[i] * (omegan * omegan) * dist;
+      }
+  return vrp;
+}
+
+// md_eq (md_eq.f90:55-323), the Andersen collisions included (therm = AND).
+// pre_out[5 per pre-equilibration step]: tps, (nb v + tk + vrp)/na, vrp/na,
+//   nb v/na, tk/na  (E_pre_eq.out, md_eq.f90:139-140)
+// eq_out[12 per step]: the same five (E_eq.out), temperature (temp_eq.out),
+//   tv tokjmol / nm (virial_ke_eq.out), v and tokjmol v / na (V_eq.out),
+//   pressure in bar (pressure_eq.out), density (density_eq.out), box length
+Status md_eq(double *p, double *r, double *dvdr, double *dvdr2, double dt, const double *mass, int na, int nb,
+             double box[3], const double *z, double beta, int ne, int npre_eq, int npt, double ttaufs, Rng &g,
+             int &irun, double *pre_out, double *eq_out) {
+  const double toK = 3.157733e+5, toKjmol = 2625.49963, tobar = 2.9421e+8, tokgcm3 = 6.147323129e-3,
+               tofs = 41.341373;
+  int nbaro = npt ? 1 : 0;
+  double vir[9] = {0}, vir_lf[9] = {0};
+  double v, v1, v2, v3, tv, tk;
+  const int nm = na / 3;
+  double dtfs = dt / tofs;
+  double thresh;
+  if (!npt) {
+    if (ttaufs > 0.0 && P.therm == GB_THERM_AND) thresh = dtfs / ttaufs;
+    else thresh = std::max(0.01, 1.0 / std::sqrt((double)ne));
+  } else {
+    thresh = 0.01;
+  }
+  Status st;
+  if (npt) {  // quick NVT pre-equilibration (md_eq.f90:93-157)
+    int nq = std::min(20000, ne / 10);
+    if (npre_eq != 0) nq = npre_eq;
+    for (int jq = 1; jq <= nq; ++jq) {
+      st = evolve_pi(p, r, v, v1, v2, v3, dvdr, dvdr2, dt, mass, na, nb, box, z, beta, vir, vir_lf, g, irun, 0,
+                     nullptr);
+      if (st) return st;
+      double tps = 1.0e-3 * jq * dtfs;
+      kinetic_rpmd(p, na, tk, mass, nb);
+      double vrp = spring_energy(r, mass, na, nb, beta);
+      if (pre_out) {
+        double *o = pre_out + 5 * (size_t)(jq - 1);
+        o[0] = tps;
+        o[1] = (nb * v + tk + vrp) / na;
+        o[2] = vrp / na;
+        o[3] = (nb * v) / na;
+        o[4] = tk / na;
+      }
+      if (P.therm == GB_THERM_AND)
+        if (ran2(g, irun, 0.0, 1.0) < thresh) sample_rpmd(p, na, nb, mass, beta, g, irun);
+    }
+  }
+  for (int je = 1; je <= ne; ++je) {  // md_eq.f90:181-318, jout = 1
+    st = evolve_pi(p, r, v, v1, v2, v3, dvdr, dvdr2, dt, mass, na, nb, box, z, beta, vir, vir_lf, g, irun, nbaro,
+                   nullptr);
+    if (st) return st;
+    double tps = 1.0e-3 * je * dtfs;
+    double tvxyz[3], tq1, tq2;
+    virial_ke(r, dvdr, dvdr2, tv, tvxyz, tq1, tq2, beta, na, nb);
+    double pres = pressure(vir, tv, na, box);
+    double vol = box[0] * box[1] * box[2];
+    double wmass = mass[0] + mass[1] + mass[2];
+    double den = tokgcm3 * (wmass * (double)nm / vol);
+    kinetic_rpmd(p, na, tk, mass, nb);
+    double vrp = spring_energy(r, mass, na, nb, beta);
+    double temp = toK * (2.0 * tk / ((double)(3 * na - P.nctot - 3) * (double)nb)) / (double)nb;
+    if (eq_out) {
+      double *o = eq_out + 12 * (size_t)(je - 1);
+      o[0] = tps;
+      o[1] = (nb * v + tk + vrp) / na;
+      o[2] = vrp / na;
+      o[3] = (nb * v) / na;
+      o[4] = tk / na;
+      o[5] = temp;
+      o[6] = tv * toKjmol / (double)nm;
+      o[7] = v;
+      o[8] = toKjmol * (v / na);
+      o[9] = pres * tobar;
+      o[10] = den;
+      o[11] = box[0];
+    }
+    if (P.therm == GB_THERM_AND)
+      if (ran2(g, irun, 0.0, 1.0) < thresh) sample_rpmd(p, na, nb, mass, beta, g, irun);
+  }
   return GB_OK;
 }
 

@@ -23,6 +23,10 @@ GB_THERM_AND = 1
 GB_THERM_PRG = 2
 GB_THERM_PRL = 3
 
+GB_BARO_NONE = 0
+GB_BARO_BER = 1
+GB_BARO_MCI = 2
+
 GB_INTRA_REFERENCE = 0
 GB_INTRA_SPCFW = 1
 
@@ -58,6 +62,7 @@ class GbParams(C.Structure):
         ("taub", C.c_double), ("patm", C.c_double),
         ("intra_model", C.c_int32),
         ("precision", C.c_int32),
+        ("baro", C.c_int32),
     ]
 
     def copy(self):

@@ -18,6 +18,10 @@ Writes
                            1000 NPT equilibration steps) and the last lines of
                            E_eq.out, virial_ke_eq.out and V_eq.out (md_eq.f90:
                            274-277), printed at the same step
+  gentest_md_eq.npz        the md_eq series of the same run: E_pre_eq.out (the
+                           100-step NVT pre-equilibration) and E_eq.out,
+                           temp_eq.out, virial_ke_eq.out, V_eq.out,
+                           pressure_eq.out, density_eq.out (1000 NPT steps)
 Frames are written every pb = 20 steps of the two 2*nt = 250-step NVE
 trajectories of md_dynamics.f90 (trajectory(), lines 517-546): file frames
 0..11 belong to trajectory 1, 12..23 to trajectory 2.
@@ -88,6 +92,15 @@ def main(ref):
     np.savez_compressed(os.path.join(HERE, "gentest_eq.npz"), r=r, box=box, nm=nm, na=na, nb=nb,
                         E_eq=last_line("E_eq.out"), virial_ke_eq=last_line("virial_ke_eq.out"),
                         V_eq=last_line("V_eq.out"))
+
+    def table(name):
+        with open(os.path.join(cmp_dir, name)) as f:
+            return np.array([[float(t) for t in ln.split()] for ln in f if ln.strip()])
+
+    np.savez_compressed(os.path.join(HERE, "gentest_md_eq.npz"),
+                        **{n.replace(".out", ""): table(n) for n in ("E_pre_eq.out", "E_eq.out", "temp_eq.out",
+                                                                      "virial_ke_eq.out", "V_eq.out",
+                                                                      "pressure_eq.out", "density_eq.out")})
 
     out = open(os.path.join(cmp_dir, "output")).read()
 

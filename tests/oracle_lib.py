@@ -20,6 +20,7 @@ TOA = 0.5291772108
 TOFS = 41.341373
 KBOLTZ_MAIN = 3.166829e-6  # main.f90:168 literal
 TOKJMOL = 2625.49963  # globals.inc:18
+TOBAR = 2.9421e+8  # globals.inc:19
 
 _lib = None
 
@@ -163,6 +164,19 @@ def run_steps(state: State, dt, mass, z, beta, nsteps, thresh, rng: Rng):
                               _ptr(np.asarray(z, float)), C.c_double(beta), C.c_int(nsteps), C.c_double(thresh),
                               rng.buf, C.byref(rng.irun), _ptr(state.vir_lf), _ptr(en))
     return st, en
+
+
+def md_eq(state: State, dt, mass, z, beta, ne, npt, rng: Rng, npre_eq=0, ttaufs=0.0):
+    """md_eq's loops (orc md_eq); returns (status, pre[nq, 5], eq[ne, 12])."""
+    nb, na, _ = state.r.shape
+    nq = (npre_eq or min(20000, ne // 10)) if npt else 0
+    pre, eq = np.zeros((max(nq, 1), 5)), np.zeros((ne, 12))
+    st = load().orc_md_eq(_ptr(state.p), _ptr(state.r), _ptr(state.dvdr), _ptr(state.dvdr2), C.c_double(dt),
+                          _ptr(np.asarray(mass, float)), C.c_int(na), C.c_int(nb), _ptr(state.box),
+                          _ptr(np.asarray(z, float)), C.c_double(beta), C.c_int(ne), C.c_int(npre_eq),
+                          C.c_int(1 if npt else 0), C.c_double(ttaufs), rng.buf, C.byref(rng.irun), _ptr(pre),
+                          _ptr(eq))
+    return st, pre[:nq], eq
 
 
 def sample_rpmd(na, nb, mass, beta, rng: Rng):

@@ -22,6 +22,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 PARAMS = os.path.join(GOLDEN, "params")
 
 THERM = {"AND": GB_THERM_AND, "NON": GB_THERM_NONE, "PRG": GB_THERM_PRG, "PRL": GB_THERM_PRL}
+BARO = {"NON": 0, "BER": 1, "MCI": 2}
 
 
 def read_param(name):
@@ -30,7 +31,7 @@ def read_param(name):
 
 def build(param="param_qspcfw", ncell=(6, 6, 6), nb=32, temp=298.0, rho=0.997, rcut_A=9.0, dtfs=0.5,
           mts=1, nbdf1=0, nbdf2=0, sig_A=0.0, therm="AND", ttaufs=0.0, ecut=0.0, intra_model=0,
-          precision=0):
+          precision=0, baro="NON", taufs=0.0, pres_bar=1.0):
     prm = read_param(param) if isinstance(param, str) else dict(param)
     P = GbParams()
     P.oo_eps = prm["oo_eps"]
@@ -58,6 +59,10 @@ def build(param="param_qspcfw", ncell=(6, 6, 6), nb=32, temp=298.0, rho=0.997, r
     P.ttau = 41.341373 * ttaufs
     P.intra_model = intra_model
     P.precision = precision
+    # module barostat (main.f90:166, 259-270): patm = pres / tobar, taub = tofs * taufs
+    P.baro = BARO[baro]
+    P.taub = orc.TOFS * taufs
+    P.patm = pres_bar / orc.TOBAR
     rigid = prm["apot"] == 0.0 and prm["bpot"] == 0.0
     beta = 1.0 / (orc.KBOLTZ_MAIN * temp)
     dt = orc.TOFS * dtfs

@@ -23,7 +23,7 @@ def gentest_system():
     return systems.build(param="param_scott", ncell=INP["ncellxyz"], nb=INP["nb"], temp=INP["temp"],
                          rho=INP["rho"], rcut_A=INP["rcut"], dtfs=INP["dtfs"], mts=INP["mts"],
                          nbdf1=INP["nbdf1"], nbdf2=INP["nbdf2"], sig_A=INP["sig"], therm=INP["therm"],
-                         ttaufs=INP["ttaufs"])
+                         ttaufs=INP["ttaufs"], baro=INP["baro"], taufs=INP["taufs"], pres_bar=INP["pres"])
 
 
 def frame_state(s, fi):
@@ -123,3 +123,39 @@ def test_md_eq_estimators_at_eq_restart():
     assert abs(est["v"] - V[1]) <= 5e-7                             # f14.6
     assert abs(orc.TOKJMOL * est["v"] / na - V[2]) <= 5e-7
     assert abs(orc.TOKJMOL * est["tv"] / nm - TV[1]) <= 1e-13 * abs(TV[1])  # list-directed, full precision
+
+
+MDEQ = np.load(os.path.join(systems.GOLDEN, "gentest_md_eq.npz"))
+
+
+def gentest_start():
+    """main.f90's start of the gentest run: the CUB lattice, one gaussian drawn
+    at the seeding (main.f90:298-299), full_forces, then sample (main.f90:785-788)."""
+    s = gentest_system()
+    rng = orc.Rng(INP["irun"])
+    rng.gaussian(1.0)
+    ff = orc.full_forces(s["r"], s["box"], s["z"])
+    p = orc.sample_rpmd(s["na"], s["nb"], s["mass"], s["beta"], rng)
+    return s, rng, orc.State(s["r"], p, ff["dvdr"], ff["dvdr2"], s["box"].copy())
+
+
+def test_md_eq_replays_gentest_equilibration():
+    # The whole equilibration of the reference's regression run, replayed from
+    # the lattice with the reference's random stream: 100 NVT pre-equilibration
+    # steps and 1000 NPT steps (Berendsen barostat inside evolve_pi, Andersen
+    # collisions in md_eq), against every series md_eq printed and eq.xyz.
+    s, rng, st = gentest_start()
+    status, pre, eq = orc.md_eq(st, s["dt"], s["mass"], s["z"], s["beta"], INP["ne"], True, rng)
+    assert status == 0
+    assert np.abs(pre - MDEQ["E_pre_eq"]).max() <= 5.01e-9                        # f13.8
+    assert np.abs(eq[:, 1:5] - MDEQ["E_eq"][:, 1:5]).max() <= 5.01e-9             # f13.8
+    assert np.abs(eq[:, 7:9] - MDEQ["V_eq"][:, 1:3]).max() <= 5.01e-7             # f14.6
+    for col, name in ((5, "temp_eq"), (6, "virial_ke_eq")):                       # full precision
+        ref = MDEQ[name][:, 1]
+        assert (np.abs(eq[:, col] - ref) / np.abs(ref)).max() <= 1e-11, name
+    every10 = np.arange(9, INP["ne"], 10)
+    pr = MDEQ["pressure_eq"][:, 1]
+    assert np.abs(eq[every10, 9] - pr).max() <= 1e-10 * np.abs(pr).max()
+    assert np.abs(eq[every10, 10] - MDEQ["density_eq"][:, 1]).max() <= 1e-13
+    assert np.abs(st.box - EQ["box"]).max() <= 1e-12
+    assert np.abs(st.r - EQ["r"]).max() <= 1e-9                                   # bohr
