@@ -152,8 +152,10 @@ int gbrpmd_full_forces(double *r, const int *na, const int *nb, double *v, doubl
 
 /* replaces subroutine evolve_pi(p,r,v,vew,vlj,vint,dvdr,dvdr2,dt,mass,na,nb,
    boxlxyz,z,beta,vir,vir_lf,irun,nbaro)  (evolve_pi.f90:1-322): one outer
-   multiple-time-step RPMD step in the normal-mode representation.
-   nbaro must be 0 (barostats are outside the device path). */
+   multiple-time-step RPMD step in the normal-mode representation, with the
+   PRG / PRL thermostat kicks (drawing the process-wide random stream with irun)
+   and, for nbaro = 1, the Berendsen barostat (baro = GB_BARO_BER, cubic box),
+   which scales boxlxyz in place and reads vir_lf as the previous call left it. */
 int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj,
                      double *vint, double *dvdr, double *dvdr2, const double *dt,
                      const double *mass, const int *na, const int *nb, double *boxlxyz,
@@ -177,7 +179,8 @@ int gbrpmd_rattle_s2(double *r, double *p, const int *nm, const double *mass,
 
 /* replaces subroutine evolve_rig_pi(p,r,v,v_lf,v_hf,dvdr,dvdr2,dt,mass,na,nb,
    boxlxyz,z,beta,vir,vir_lf,irun,nbaro)  (evolve_rigid.f90:100-224): rigid
-   ring-polymer step with primitive bead springs and RATTLE. nbaro must be 0. */
+   ring-polymer step with primitive bead springs and RATTLE, with the PRG / PRL
+   thermostat kicks.  nbaro must be 0 (its barostat is not on the device path). */
 int gbrpmd_evolve_rig_pi(double *p, double *r, double *v, double *v_lf, double *v_hf,
                          double *dvdr, double *dvdr2, const double *dt, const double *mass,
                          const int *na, const int *nb, double *boxlxyz, const double *z,
@@ -235,6 +238,21 @@ int gbrpmd_ctx_sync(gb_context *ctx);
 /* energies and virials of the last step: out[0..4] = v, vew, vlj, vint, tv;
    vir[9], vir_lf[9] column-major */
 int gbrpmd_ctx_energies(gb_context *ctx, double *out5, double *vir, double *vir_lf);
+/* Random stream owned by the context (no counterpart in the reference, whose
+   stream is process-wide): the PRG / PRL thermostat kicks of
+   gbrpmd_ctx_evolve draw from a fresh ran2 / gaussian state seeded with idum
+   (negative to initialise, as ran2 requires).  The drop-in entry points and
+   gbrpmd_run_md_eq draw the process-wide stream with the caller's irun. */
+int gbrpmd_ctx_set_rng(gb_context *ctx, int idum);
+/* evolve_pi's nbaro for gbrpmd_ctx_evolve / gbrpmd_run_md_eq on this context
+   (md_eq.f90:55-58: 1 when ens = 'NPT'): the Berendsen barostat scales the box
+   and the water centroids inside every step (one synchronisation per step). */
+int gbrpmd_ctx_set_nbaro(gb_context *ctx, int nbaro);
+/* the context's current box (changed by the barostat) */
+int gbrpmd_ctx_box(gb_context *ctx, double *box3);
+/* Resets the process-wide ran2 / gaussian state (shuffle table, second
+   generator, cached gaussian) to the state the reference has at program start. */
+void gbrpmd_rng_reset(void);
 /* The estimators md_eq prints at an output step (md_eq.f90:190-299), from the
    resident state left by the last evolve (bead representation) and the
    energies / virial of that evaluation; synchronises.  out[16]:

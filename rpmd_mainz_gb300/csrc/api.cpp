@@ -15,6 +15,8 @@
 #include "gb_rng.h"
 #include "gb_kernels.h"
 
+RngState g_rng;  // the process-wide random stream (random.f90's saved state)
+
 namespace {
 
 gb_params g_params;
@@ -190,6 +192,10 @@ void ctx_free(gb_context *c) {
       if (p) cudaFree(p);
   if (c->h_acc) cudaFreeHost(c->h_acc);
   if (c->h_status) cudaFreeHost(c->h_status);
+  if (c->h_gauss) cudaFreeHost(c->h_gauss);
+  if (c->d_gauss) cudaFree(c->d_gauss);
+  if (c->d_therm) cudaFree(c->d_therm);
+  if (c->gauss_ev) cudaEventDestroy(c->gauss_ev);
   if (c->stream) cudaStreamDestroy(c->stream);
   c->stream = nullptr;
 }
@@ -266,17 +272,23 @@ int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj, 
                      const int *na, const int *nb, double *boxlxyz, const double *z,
                      const double *beta, double *vir, double *vir_lf, int *irun,
                      const int *nbaro) {
-  (void)irun;
-  if (*nbaro != 0) return ctx_set_error(GB_E_UNSUPPORTED, "barostats are not on the device path (nbaro must be 0)");
   gb_context *c;
   int st = dropin_ctx(*na, *nb, &c);
   if (st) return st;
   const size_t N = 3 * (size_t)(*na) * (*nb);
   std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
+  std::memcpy(c->vir_lf_in, vir_lf, sizeof(double) * 9);  // the barostat reads the previous call's vir_lf
+  c->nbaro = *nbaro;
+  c->th_rng = &g_rng;  // thermostat kicks draw the process-wide stream with the caller's irun
+  c->th_idum = irun;
   if ((st = upload(c, c->p, p, N)) || (st = upload(c, c->r, r, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||
       (st = upload(c, c->dvdr2, dvdr2, N)) || (st = set_masses(c, mass)) || (st = set_charges(c, z)))
     return st;
-  if ((st = dev_step(c, *dt, *beta))) return st;
+  st = dev_step(c, *dt, *beta);
+  c->th_rng = nullptr;
+  c->th_idum = nullptr;
+  if (st) return st;
+  std::memcpy(boxlxyz, c->box, sizeof(double) * 3);  // scaled by the barostat
   if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
       (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N)))
     return st;
@@ -359,12 +371,44 @@ int gbrpmd_ctx_full_forces(gb_context *c, double *v, double *vew, double *voo, d
 
 int gbrpmd_ctx_evolve(gb_context *c, int nsteps, double dt, double beta) {
   if (!c->own_params) c->P = g_params;
-  for (int s = 0; s < nsteps; ++s) {
-    int st = dev_step(c, dt, beta);
-    if (st) return st;
+  if (c->has_own_rng) {
+    c->th_rng = &c->own_rng;
+    c->th_idum = &c->own_idum;
   }
+  int st = GB_OK;
+  for (int s = 0; s < nsteps && !st; ++s) {
+    st = dev_step(c, dt, beta);
+    // with a barostat each step needs the last one's vir_lf on the host
+    if (!st && c->nbaro) st = dev_collect(c, 1, dt, beta);
+  }
+  c->th_rng = nullptr;
+  c->th_idum = nullptr;
+  return st;
+}
+
+int gbrpmd_ctx_set_rng(gb_context *c, int idum) {
+  if (!c) return ctx_set_error(GB_E_ARG, "null context");
+  c->own_rng = RngState();
+  c->own_idum = idum;
+  c->has_own_rng = true;
   return GB_OK;
 }
+
+int gbrpmd_ctx_set_nbaro(gb_context *c, int nbaro) {
+  if (!c) return ctx_set_error(GB_E_ARG, "null context");
+  if (nbaro != 0 && nbaro != 1) return ctx_set_error(GB_E_ARG, "nbaro must be 0 or 1");
+  c->nbaro = nbaro;
+  dev_graph_reset(c);
+  return GB_OK;
+}
+
+int gbrpmd_ctx_box(gb_context *c, double *box3) {
+  if (!c || !box3) return ctx_set_error(GB_E_ARG, "null argument");
+  for (int d = 0; d < 3; ++d) box3[d] = c->box[d];
+  return GB_OK;
+}
+
+void gbrpmd_rng_reset(void) { g_rng = RngState(); }
 
 int gbrpmd_ctx_sync(gb_context *c) { return dev_collect(c, 1, 0.0, c->last_beta); }
 
@@ -528,7 +572,6 @@ int gbrpmd_ctx_region_times(gb_context *c, double *ms, double *units, int *count
 int64_t gbrpmd_ctx_launch_count(gb_context *c) { return c->launches; }
 
 // ---- serial random stream (random.f90:1-72), one process-wide state ----
-RngState g_rng;
 
 double gbrpmd_ran2(int *idum, const double *rmin, const double *rmax) { return rng_ran2(g_rng, idum, *rmin, *rmax); }
 
@@ -570,18 +613,22 @@ int gbrpmd_evolve_rig_pi(double *p, double *r, double *v, double *v_lf, double *
                          double *dvdr2, const double *dt, const double *mass, const int *na,
                          const int *nb, double *boxlxyz, const double *z, const double *beta,
                          double *vir, double *vir_lf, int *irun, const int *nbaro) {
-  (void)irun;
-  if (*nbaro != 0) return ctx_set_error(GB_E_UNSUPPORTED, "barostats are not on the device path (nbaro must be 0)");
   gb_context *c;
   int st = dropin_ctx(*na, *nb, &c);
   if (st) return st;
   const size_t N = 3 * (size_t)(*na) * (*nb);
   std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
+  c->nbaro = *nbaro;
   if ((st = upload(c, c->p, p, N)) || (st = upload(c, c->r, r, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||
       (st = upload(c, c->dvdr2, dvdr2, N)) || (st = set_masses(c, mass)) ||
       (st = set_charges(c, z)))
     return st;
-  if ((st = dev_evolve_rig_pi(c, *dt, *beta, vir))) return st;
+  c->th_rng = &g_rng;
+  c->th_idum = irun;
+  st = dev_evolve_rig_pi(c, *dt, *beta, vir);
+  c->th_rng = nullptr;
+  c->th_idum = nullptr;
+  if (st) return st;
   if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
       (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N)))
     return st;

@@ -9,6 +9,7 @@
 
 #include "../../include/gbrpmd.h"
 #include "gb_kvec.h"
+#include "gb_rng.h"
 
 // One pair list: for each of `nconf` configurations and each of `npt` points,
 // up to `cap` partner indices; the pair (i, j) is stored once, in the list of
@@ -104,6 +105,19 @@ struct gb_context {
   int mass_version = 0;           // bumped when uploaded masses differ
   double *acc = nullptr;    // ACC_NSLOT * ACC_STRIDE
   double *est = nullptr;    // estimator sums [16] and per-molecule outputs [2][nm][3] (lazy)
+
+  // thermostat kicks and barostat inside evolve_pi
+  int nbaro = 0;                  // evolve_pi's nbaro (md_eq.f90:55-58: 1 for ens = 'NPT')
+  RngState *th_rng = nullptr;     // the random stream the PRG / PRL kicks draw from,
+  int *th_idum = nullptr;         // set by the caller of each step
+  RngState own_rng;               // a stream owned by the context (gbrpmd_ctx_set_rng)
+  int own_idum = 0;
+  bool has_own_rng = false;
+  double *d_gauss = nullptr;      // [3 na nb] gaussians of one PRL kick (device)
+  double *h_gauss = nullptr;      // pinned staging of the same
+  cudaEvent_t gauss_ev = nullptr; // the staging buffer's last copy
+  bool gauss_pending = false;
+  double *d_therm = nullptr;      // [4] device scratch (PRG kinetic energy)
   unsigned *status = nullptr;
   double *h_acc = nullptr;  // pinned host mirror
   unsigned *h_status = nullptr;
@@ -170,6 +184,8 @@ int ctx_check_cuda(cudaError_t e, const char *what);
 int dev_prepare(gb_context *c, double dt, double beta);  // twiddles, monodromy, k lists
 int dev_full_forces(gb_context *c);                      // dvdr, dvdr2 from r
 int dev_evolve_pi(gb_context *c, double dt, double beta);
+// a PRG / PRL thermostat kick on the bead momenta (no-op for other thermostats)
+int therm_kick(gb_context *c, double dtk, double beta);
 // one evolve_pi step, replayed from a captured CUDA graph when it can be
 int dev_step(gb_context *c, double dt, double beta);
 size_t dev_estimate_bytes(int na, int nb, const gb_params &P);

@@ -93,6 +93,13 @@ void launch_intra(cudaStream_t s, const double *r, double *out, int na, int B, i
                   const gb_params &P, double *acc, int accumulate);
 void launch_virial_ke(cudaStream_t s, const double *r, const double *dvdr, const double *dvdr2,
                       int na, int nb, double *acc);
+// thermostat kicks and Berendsen shift inside evolve_pi (k_therm.cu)
+void launch_prl(cudaStream_t s, double *p, const double *mass, const double *g, int na, int nb, double c1, double c2,
+                double betan);
+void launch_kinetic(cudaStream_t s, const double *p, const double *mass, int na, int nb, double *out);
+void launch_prg_scale(cudaStream_t s, double *p, int na, int nb, const double *kt, double c, double ktav, double ndof,
+                      double snfm1, double ranno);
+void launch_baro_shift(cudaStream_t s, double *r, double *rnm, int na, int nb, double sm1);
 // md_eq's output-step estimators (k_est.cu): acc[14] sums, optional rcm / mdip [nm][3]
 void launch_estimators(cudaStream_t s, const double *r, const double *p, const double *dvdr, const double *dvdr2,
                        const double *mass, const double *z, int na, int nb, double alpha, double *acc, double *rcm,

@@ -382,8 +382,7 @@ int term_forces_rigid(gb_context *c);  // step.cpp: forces(r, v, dvdr, nb, ..., 
 
 int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) {
   (void)vir_inout;
-  if (c->P.therm == GB_THERM_PRG || c->P.therm == GB_THERM_PRL)
-    return ctx_set_error(GB_E_UNSUPPORTED, "PRG/PRL thermostat kicks are not on the device path");
+  if (c->nbaro) return ctx_set_error(GB_E_UNSUPPORTED, "barostats of evolve_rig_pi are not on the device path");
   if (3 * c->nm != c->P.nctot) return ctx_set_error(GB_E_ARG, "number of bonds inconsistent in shake/rattle routine");
   const int nb = c->nb, nm = c->nm;
   const long long N = 3LL * c->na * nb;
@@ -392,15 +391,16 @@ int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) 
   const double halfdt = 0.5 * dt, smalldt = dt / (double)nb;
   double omegan = nb / (beta * 1.0);
   omegan = omegan * omegan;
-  // p -= dt/2 dvdr (evolve_rigid.f90:132)
+  // thermostat kick with halfdt (evolve_rigid.f90:124-128), then p -= dt/2 dvdr (132)
+  int st = therm_kick(c, halfdt, beta);
+  if (st) return st;
   launch_axpy(s, c->p, c->dvdr, -halfdt, N);
   const int mpb = nb >= 128 ? 1 : 128 / nb;
   const size_t smem = sizeof(double) * 9 * (size_t)mpb * nb;
   k_rig_substeps<<<nblk(nm, mpb), mpb * nb, smem, s>>>(c->r, c->p, c->dvdr2, nm, nb, mpb, smalldt,
                                                       omegan, rp, c->mass, c->status);
   // intermolecular forces on all beads (evolve_rigid.f90:174)
-  int st = term_forces_rigid(c);
-  if (st) return st;
+  if ((st = term_forces_rigid(c))) return st;
   // p -= dt/2 dvdr; rattle stage 2 with dt, constraint virial (evolve_rigid.f90:181-190)
   launch_axpy(s, c->p, c->dvdr, -halfdt, N);
   double *rec = c->g;  // nb*nm*8 <= 3*na*nb doubles
@@ -411,6 +411,7 @@ int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) 
   c->plan.B_int = nb;  // vir_hf = sum_k vir_k / nb (evolve_rigid.f90:198)
   CK(cudaMemsetAsync(c->dvdr2, 0, sizeof(double) * N, s));
   c->launches += 6;
+  if ((st = therm_kick(c, halfdt, beta))) return st;  // evolve_rigid.f90:192-196
   CK(cudaGetLastError());
   return GB_OK;
 }

@@ -1,0 +1,104 @@
+// k_therm.cu -- the thermostat kicks and the Berendsen box scaling that
+// evolve_pi applies inside one step (evolve_pi.f90:72-80, 172-189, 281-290).
+//
+// Both thermostats act on the momenta in the bead representation, r(3,na,nb)
+// order.  The random numbers are the reference's serial gaussian stream, drawn
+// on the host in the order the reference draws them and passed in.
+#include <algorithm>
+
+#include "gb_common.cuh"
+#include "gb_kernels.h"
+
+namespace {
+
+inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// parinello_therm_loc (module_thermostat.f90:56-82):
+//   p = c1 p + c2 sqrt(m_j / betan) g,  g in the order bead, atom, xyz
+// (products and the sum rounded separately, as the reference computes them)
+__global__ void __launch_bounds__(256) k_prl(double *__restrict__ p, const double *__restrict__ mass,
+                                             const double *__restrict__ g, long long N, int na, double c1,
+                                             double c2, double betan) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int j = (int)((i / 3) % na);
+  const double c3 = __dmul_rn(c2, sqrt(mass[j] / betan));
+  p[i] = __dadd_rn(__dmul_rn(c1, p[i]), __dmul_rn(c3, g[i]));
+}
+
+// kinetic energy sum p^2 / (2 m) of parinello_therm (module_thermostat.f90:28-35)
+__global__ void __launch_bounds__(256) k_kinetic(const double *__restrict__ p, const double *__restrict__ mass,
+                                                 long long N, int na, double *out) {
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)((i / 3) % na);
+    v[0] += p[i] * p[i] / (2.0 * mass[j]);
+  }
+  block_sum_atomic<1>(v, sh, out);
+}
+
+// parinello_therm's rescaling (module_thermostat.f90:37-51); every thread forms
+// the same alpha from the device kinetic energy *kt
+__global__ void __launch_bounds__(256) k_prg_scale(double *__restrict__ p, long long N, const double *__restrict__ kt,
+                                                   double c, double ktav, double ndof, double snfm1, double ranno) {
+  const double ransq = ranno * ranno;
+  const double fac = (1.0 - c) * ktav / (ndof * kt[0]);
+  const double t1 = __dmul_rn(fac, snfm1 + ransq);  // no contraction into the sum below
+  const double t2 = __dmul_rn(2.0 * ranno, sqrt(c * fac));
+  double alpha = sqrt(c + t1 + t2);
+  const double plusmin = ranno + sqrt(c / fac);
+  alpha = plusmin >= 0.0 ? fabs(alpha) : -fabs(alpha);  // Fortran sign(alpha, plusmin)
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+    p[i] = alpha * p[i];
+}
+
+// beren_baro's molecule shift (module_barostat.f90:111-126): every atom of water
+// m on every bead moves by rcm_m (scale - 1), rcm = center_water
+// (md_tools.f90:367-390: the bead average of the sum of the three atoms'
+// positions).  The shift is the same on every bead, so in the normal-mode
+// positions rnm (when given) only the centroid row changes, by sqrt(nb) times it.
+__global__ void __launch_bounds__(128) k_baro_shift(double *__restrict__ r, double *__restrict__ rnm, int nm, int nb,
+                                                    double sm1, double sqnb) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 3 * nm) return;
+  const int m = idx / 3, x = idx % 3;
+  const long long S = 9LL * nm;
+  const long long o = 9LL * m + x;
+  double pc = 0.0;
+  for (int k = 0; k < nb; ++k) pc = pc + r[o + S * k] + r[o + 3 + S * k] + r[o + 6 + S * k];
+  pc = pc * (1.0 / (double)nb);
+  const double d = __dmul_rn(pc, sm1);
+  for (int k = 0; k < nb; ++k)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) r[o + 3 * a + S * k] = r[o + 3 * a + S * k] + d;
+  if (rnm)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) rnm[o + 3 * a] = rnm[o + 3 * a] + __dmul_rn(sqnb, d);
+}
+
+}  // namespace
+
+void launch_prl(cudaStream_t s, double *p, const double *mass, const double *g, int na, int nb, double c1, double c2,
+                double betan) {
+  const long long N = 3LL * na * nb;
+  k_prl<<<nblk(N, 256), 256, 0, s>>>(p, mass, g, N, na, c1, c2, betan);
+}
+
+void launch_kinetic(cudaStream_t s, const double *p, const double *mass, int na, int nb, double *out) {
+  const long long N = 3LL * na * nb;
+  const unsigned grid = std::min<unsigned>(nblk(N, 256), 1024u);
+  k_kinetic<<<grid, 256, 0, s>>>(p, mass, N, na, out);
+}
+
+void launch_prg_scale(cudaStream_t s, double *p, int na, int nb, const double *kt, double c, double ktav, double ndof,
+                      double snfm1, double ranno) {
+  const long long N = 3LL * na * nb;
+  const unsigned grid = std::min<unsigned>(nblk(N, 256), 4096u);
+  k_prg_scale<<<grid, 256, 0, s>>>(p, N, kt, c, ktav, ndof, snfm1, ranno);
+}
+
+void launch_baro_shift(cudaStream_t s, double *r, double *rnm, int na, int nb, double sm1) {
+  const int nm = na / 3;
+  k_baro_shift<<<nblk(3LL * nm, 128), 128, 0, s>>>(r, rnm, nm, nb, sm1, sqrt((double)nb));
+}

@@ -111,11 +111,23 @@ int gbrpmd_run_md_eq(gb_context *c, int nsteps, double dt, double beta, double t
       return ctx_set_error(GB_E_CUDA, "mass download failed");
   }
   const double zero = 0.0, one = 1.0;
+  c->th_rng = &g_rng;  // PRG / PRL kicks draw the same stream as the collisions
+  c->th_idum = irun;
+  struct Clear {
+    gb_context *c;
+    ~Clear() {
+      c->th_rng = nullptr;
+      c->th_idum = nullptr;
+    }
+  } clear{c};
   for (int s = 0; s < nsteps; ++s) {
     int st = dev_evolve_pi(c, dt, beta);
     if (st) return st;
-    if (energies) {
+    // energies, and with a barostat the vir_lf the next step reads, need the
+    // step's accumulators; the last step is always collected
+    if (energies || c->nbaro || s == nsteps - 1)
       if ((st = dev_collect(c, 1, dt, beta))) return st;
+    if (energies) {
       energies[4 * s + 0] = c->e_v;
       energies[4 * s + 1] = c->e_vew;
       energies[4 * s + 2] = c->e_vlj;

@@ -593,10 +593,100 @@ int dev_full_forces(gb_context *c) {
   return launch_status();
 }
 
+// One thermostat kick of evolve_pi (evolve_pi.f90:72-80, 281-290) on the bead
+// momenta: parinello_therm (PRG, global rescaling) or parinello_therm_loc (PRL,
+// local Langevin), drawing the reference's gaussian stream c->th_rng / th_idum
+// on the host in the reference's order.  dtk: the time step the reference
+// passes (halfdt for PRG, dt for PRL in evolve_pi; halfdt for both in
+// evolve_rig_pi).
+int therm_kick(gb_context *c, double dtk, double beta) {
+  const gb_params &P = c->P;
+  if (P.therm != GB_THERM_PRG && P.therm != GB_THERM_PRL) return GB_OK;
+  if (!c->th_rng || !c->th_idum)
+    return ctx_set_error(GB_E_ARG, "PRG/PRL thermostat: no random stream (gbrpmd_ctx_set_rng)");
+  const int na = c->na, nb = c->nb;
+  const size_t N = 3 * (size_t)na * nb;
+  const double betan = beta / (double)nb;
+  RngState &g = *c->th_rng;
+  int *idum = c->th_idum;
+  if (!c->d_therm) CK(cudaMalloc(&c->d_therm, sizeof(double) * 4));
+  if (P.therm == GB_THERM_PRL) {  // module_thermostat.f90:56-82
+    const double gamma = 1.0 / (2.0 * P.ttau);
+    const double c1 = std::exp(-0.5 * gamma * dtk);
+    const double c2 = std::sqrt(1.0 - c1 * c1);
+    if (!c->d_gauss) {
+      CK(cudaMalloc(&c->d_gauss, sizeof(double) * N));
+      CK(cudaMallocHost(&c->h_gauss, sizeof(double) * N));
+      CK(cudaEventCreateWithFlags(&c->gauss_ev, cudaEventDisableTiming));
+    }
+    if (c->gauss_pending) CK(cudaEventSynchronize(c->gauss_ev));  // staging buffer free again
+    for (size_t i = 0; i < N; ++i) c->h_gauss[i] = rng_gaussian(g, idum, 1.0);
+    CK(cudaMemcpyAsync(c->d_gauss, c->h_gauss, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaEventRecord(c->gauss_ev, c->stream));
+    c->gauss_pending = true;
+    launch_prl(c->stream, c->p, c->mass, c->d_gauss, na, nb, c1, c2, betan);
+    c->launches += 1;
+    return GB_OK;
+  }
+  // parinello_therm (module_thermostat.f90:6-54)
+  const int ndof = (int)(3 * na * (double)nb - P.nctot - 3);
+  (void)rng_gaussian(g, idum, 1.0);  // rt: drawn, not used
+  const double ktav = (double)ndof / (2.0 * betan);
+  double snfm1 = 0.0;
+  for (int i = 1; i <= ndof - 1; ++i) {
+    const double ranno = rng_gaussian(g, idum, 1.0);
+    snfm1 = snfm1 + ranno * ranno;
+  }
+  CK(cudaMemsetAsync(c->d_therm, 0, sizeof(double), c->stream));
+  launch_kinetic(c->stream, c->p, c->mass, na, nb, c->d_therm);
+  const double ranno = rng_gaussian(g, idum, 1.0);
+  const double cc = std::exp(-dtk / P.ttau);
+  launch_prg_scale(c->stream, c->p, na, nb, c->d_therm, cc, ktav, (double)ndof, snfm1, ranno);
+  c->launches += 2;
+  return GB_OK;
+}
+
+// Berendsen barostat of evolve_pi with nbaro = 1 (evolve_pi.f90:163-189):
+// pressure from this step's MTS-averaged virial kinetic energy and virial
+// (the previous call's vir_lf plus this step's high-frequency virial), box and
+// water centroids scaled (beren_baro, module_barostat.f90:88-129).  Needs the
+// step's accumulators on the host: one synchronisation.
+int barostat(gb_context *c, double dt) {
+  const gb_params &P = c->P;
+  if (P.baro != GB_BARO_BER)
+    return ctx_set_error(GB_E_UNSUPPORTED, "only the Berendsen barostat (baro = BER) is on the device path");
+  if (!P.iamcub) return ctx_set_error(GB_E_UNSUPPORTED, "beren_baro_nc (non-cubic boxes) is not on the device path");
+  CK(cudaMemcpyAsync(c->h_acc, c->acc, sizeof(double) * ACC_NSLOT * ACC_STRIDE, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const double *A = c->h_acc;
+  const int na = c->na, nb = c->nb, mts = P.mts, nm = na / 3;
+  double vir[9];
+  for (int i = 0; i < 9; ++i)
+    vir[i] = c->vir_lf_in[i] + A[(size_t)ACC_INT * ACC_STRIDE + 1 + i] / nb / (double)mts;
+  const double tq1 = 0.5 * A[(size_t)ACC_KE * ACC_STRIDE + 0] / nb, tq2 = 0.5 * A[(size_t)ACC_KE * ACC_STRIDE + 1] / nb;
+  const double tc = 0.5 * (3 * na - 3 - P.nctot) / c->last_beta;
+  const double tv = tc + (tq1 + tq2) / mts;
+  // pressure (md_pressure.f90:1-56)
+  double w = vir[0] + vir[4] + vir[8];
+  w = -w / 3.0;
+  const double vol = c->box[0] * c->box[1] * c->box[2];
+  double pres = (2.0 * tv / 3.0 + w) / vol;
+  if (P.oo_gam == 0.0) {
+    const double pi = std::acos(-1.0), rho = (double)nm / vol;
+    const double prefac = (16.0 * pi * (rho * rho) * P.oo_eps * (P.oo_sig * P.oo_sig * P.oo_sig)) / 3.0;
+    pres = pres + prefac * ((2.0 / 3.0) * std::pow(P.oo_sig / P.rcut, 9) - std::pow(P.oo_sig / P.rcut, 3));
+  }
+  const double compi = 13531.0, bstat = compi / (3.0 * P.taub);
+  const double scale = std::fabs(1.0 - (dt * bstat) * (P.patm - pres));
+  for (int d = 0; d < 3; ++d) c->box[d] = scale * c->box[d];
+  launch_baro_shift(c->stream, c->r, nb > 1 ? c->rnm : nullptr, na, nb, scale - 1.0);
+  c->launches += 1;
+  return GB_OK;
+}
+
 int dev_evolve_pi(gb_context *c, double dt, double beta) {
   int st;
-  if (c->P.therm == GB_THERM_PRG || c->P.therm == GB_THERM_PRL)
-    return ctx_set_error(GB_E_UNSUPPORTED, "PRG/PRL thermostat kicks are not on the device path");
+  if (c->nbaro && c->graph.valid) dev_graph_reset(c);
   if ((st = dev_prepare(c, dt, beta))) return st;
   c->plan = EnergyPlan();
   c->plan.evolve = 1;
@@ -606,6 +696,8 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   const long long N = 3LL * na * nb;
   const double dtsmall = dt / (double)mts, halfdtsmall = 0.5 * dtsmall, halfdt = 0.5 * dt;
   cudaStream_t s = c->stream;
+  const double dt_therm = c->P.therm == GB_THERM_PRG ? halfdt : dt;  // evolve_pi.f90:73-77
+  if ((st = therm_kick(c, dt_therm, beta))) return st;
   CK(cudaMemsetAsync(c->acc, 0, sizeof(double) * ACC_NSLOT * ACC_STRIDE, s));
   prof_begin(c, PR_MTS);
   // one fused kernel for power-of-two nb up to 64 (k_mts.cu)
@@ -615,7 +707,9 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
     c->plan.B_int = nb;
     c->launches += 1;
     prof_end(c, PR_MTS, (double)c->nm * nb * mts);
+    if (c->nbaro && (st = barostat(c, dt))) return st;
     if ((st = low_frequency(c, c->rnm, c->r, c->p, halfdt))) return st;
+    if ((st = therm_kick(c, dt_therm, beta))) return st;
     return launch_status();
   }
   // evolve_pi.f90:82-88
@@ -645,8 +739,10 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   launch_axpy(s, c->p, c->dvdr2, -halfdtsmall, N);
   c->launches += 2;
   prof_end(c, PR_MTS, (double)c->nm * nb * mts);
+  if (c->nbaro && (st = barostat(c, dt))) return st;
   // low-frequency forces and the closing kick (evolve_pi.f90:194-279)
   if ((st = low_frequency(c, c->rnm, c->r, c->p, halfdt))) return st;
+  if ((st = therm_kick(c, dt_therm, beta))) return st;
   return launch_status();
 }
 
@@ -667,7 +763,7 @@ int dev_step(gb_context *c, double dt, double beta) {
   auto &G = c->graph;
   const bool eligible = c->use_graphs && !c->prof && !c->generic_mts &&
                         (c->nb == 2 || c->nb == 4 || c->nb == 8 || c->nb == 16 || c->nb == 32 || c->nb == 64) &&
-                        c->P.therm != GB_THERM_PRG && c->P.therm != GB_THERM_PRL;
+                        c->P.therm != GB_THERM_PRG && c->P.therm != GB_THERM_PRL && !c->nbaro;
   const bool same = eligible && G.dt == dt && G.beta == beta && G.box[0] == c->box[0] && G.box[1] == c->box[1] &&
                     G.box[2] == c->box[2] && std::memcmp(&G.P, &c->P, sizeof(gb_params)) == 0;
   if (!same) {
@@ -790,6 +886,8 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
     c->e_vir[i] = c->e_vir_lf[i] + c->e_vir_hf[i];
   }
   if (pl.evolve) {
+    // evolve_pi's vir_lf output is the next call's vir_lf input (the barostat reads it)
+    for (int i = 0; i < 9; ++i) c->vir_lf_in[i] = c->e_vir_lf[i];
     const int nb = c->nb;
     double tq1 = 0.5 * S(ACC_KE)[0] / nb, tq2 = 0.5 * S(ACC_KE)[1] / nb;
     double tc = 0.5 * (3 * c->na - 3 - c->P.nctot) / c->last_beta;

@@ -68,6 +68,10 @@ def load(path=None):
     lib.gbrpmd_ctx_evolve.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
     lib.gbrpmd_ctx_energies.argtypes = [C.c_void_p, D, D, D]
     lib.gbrpmd_ctx_estimators.argtypes = [C.c_void_p, C.c_double, D, D, D]
+    lib.gbrpmd_ctx_set_rng.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_ctx_set_nbaro.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_ctx_box.argtypes = [C.c_void_p, D]
+    lib.gbrpmd_rng_reset.restype = None
     lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
     lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
     lib.gbrpmd_ctx_set_graphs.argtypes = [C.c_void_p, C.c_int]
@@ -126,6 +130,11 @@ def get_params() -> GbParams:
     return p
 
 
+def rng_reset():
+    """Process-wide ran2 / gaussian state back to the reference's start-up state."""
+    load().gbrpmd_rng_reset()
+
+
 def last_error():
     """Message of the library's last error."""
     return load().gbrpmd_last_error().decode()
@@ -175,15 +184,18 @@ class State:
         self.vir_lf = np.zeros(9)
 
 
-def evolve_pi(state: State, dt, mass, z, beta, irun=0):
-    """evolve_pi(p,r,v,vew,vlj,vint,dvdr,dvdr2,dt,mass,na,nb,boxlxyz,z,beta,vir,vir_lf,irun,nbaro)."""
+def evolve_pi(state: State, dt, mass, z, beta, irun=0, nbaro=0):
+    """evolve_pi(p,r,v,vew,vlj,vint,dvdr,dvdr2,dt,mass,na,nb,boxlxyz,z,beta,vir,vir_lf,irun,nbaro).
+    irun: an int, or a ctypes c_int that the thermostat draws advance in place;
+    state.box is scaled in place by the barostat (nbaro = 1)."""
     nb, na, _ = state.r.shape
     v, vew, vlj, vint = (C.c_double() for _ in range(4))
+    idum = irun if isinstance(irun, C.c_int) else C.c_int(irun)
     _check(load().gbrpmd_evolve_pi(_ptr(state.p), _ptr(state.r), C.byref(v), C.byref(vew), C.byref(vlj),
                                    C.byref(vint), _ptr(state.dvdr), _ptr(state.dvdr2), C.byref(C.c_double(dt)),
                                    _ptr(_arr(mass)), C.byref(C.c_int(na)), C.byref(C.c_int(nb)), _ptr(state.box),
                                    _ptr(_arr(z)), C.byref(C.c_double(beta)), _ptr(state.vir), _ptr(state.vir_lf),
-                                   C.byref(C.c_int(irun)), C.byref(C.c_int(0))))
+                                   C.byref(idum), C.byref(C.c_int(nbaro))))
     return dict(v=v.value, vew=vew.value, vlj=vlj.value, vint=vint.value)
 
 
@@ -269,6 +281,20 @@ class Context:
         _check(load().gbrpmd_ctx_energies(self.h, _ptr(out), _ptr(vir), _ptr(vir_lf)))
         return dict(v=out[0], vew=out[1], vlj=out[2], vint=out[3], tv=out[4], vir=vir.reshape(3, 3, order="F"),
                     vir_lf=vir_lf.reshape(3, 3, order="F"))
+
+    def set_rng(self, idum):
+        """Context-owned random stream for the PRG / PRL kicks of evolve()."""
+        _check(load().gbrpmd_ctx_set_rng(self.h, int(idum)))
+
+    def set_nbaro(self, nbaro):
+        """evolve_pi's nbaro for evolve() / run_md_eq() (1: Berendsen barostat)."""
+        _check(load().gbrpmd_ctx_set_nbaro(self.h, int(nbaro)))
+
+    @property
+    def box(self):
+        b = np.zeros(3)
+        _check(load().gbrpmd_ctx_box(self.h, _ptr(b)))
+        return b
 
     ESTIMATORS = ("tk", "vrp", "econs", "temp", "tv", "tvx", "tvy", "tvz", "pres", "dipx", "dipy", "dipz", "dip2",
                   "dipm", "den", "v")

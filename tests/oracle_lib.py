@@ -145,14 +145,14 @@ class State:
         return s
 
 
-def evolve_pi(state: State, dt, mass, z, beta, rng: Rng):
+def evolve_pi(state: State, dt, mass, z, beta, rng: Rng, nbaro=0):
     nb, na, _ = state.r.shape
     v, vew, vlj, vint, tv = (C.c_double(0.0) for _ in range(5))
     st = load().orc_evolve_pi(_ptr(state.p), _ptr(state.r), C.byref(v), C.byref(vew), C.byref(vlj),
                               C.byref(vint), _ptr(state.dvdr), _ptr(state.dvdr2), C.c_double(dt),
                               _ptr(np.asarray(mass, float)), C.c_int(na), C.c_int(nb), _ptr(state.box),
                               _ptr(np.asarray(z, float)), C.c_double(beta), _ptr(state.vir),
-                              _ptr(state.vir_lf), rng.buf, C.byref(rng.irun), C.c_int(0), C.byref(tv))
+                              _ptr(state.vir_lf), rng.buf, C.byref(rng.irun), C.c_int(nbaro), C.byref(tv))
     return dict(status=st, v=v.value, vew=vew.value, vlj=vlj.value, vint=vint.value, tv=tv.value)
 
 

@@ -1,0 +1,128 @@
+"""The thermostat kicks and the barostat inside evolve_pi on the device,
+through the drop-in C ABI, against the oracle: PRL (parinello_therm_loc) and
+PRG (parinello_therm) kicks drawing the reference's random stream, and the
+Berendsen barostat (nbaro = 1); then the reference's own gentest equilibration
+(100 NVT + 1000 NPT steps, Andersen collisions, md_eq.f90) replayed on the
+device from the lattice against every series the reference printed.
+
+Tolerance: 1e-10 relative (L2) for positions, momenta and forces and for the
+box after the steps, as for the other plain-FP64 parity tests.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from rpmd_mainz_gb300 import lib
+
+from . import oracle_lib as orc
+from . import systems
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    yield
+    lib.finalize()
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(b)
+
+
+def run_both(s, nsteps, nbaro=0, seed=31):
+    lib.init(s["params"])
+    r = systems.perturbed(s, seed=3)
+    p = orc.sample_rpmd(s["na"], s["nb"], s["mass"], s["beta"], orc.Rng(11))
+    ff = orc.full_forces(r, s["box"], s["z"])
+    ref = orc.State(r, p, ff["dvdr"], ff["dvdr2"], s["box"].copy())
+    dev = lib.State(r, p, ff["dvdr"], ff["dvdr2"], s["box"].copy())
+    rng = orc.Rng(seed)
+    lib.rng_reset()
+    irun = C.c_int(-seed)
+    for _ in range(nsteps):
+        assert orc.evolve_pi(ref, s["dt"], s["mass"], s["z"], s["beta"], rng, nbaro=nbaro)["status"] == 0
+        lib.evolve_pi(dev, s["dt"], s["mass"], s["z"], s["beta"], irun=irun, nbaro=nbaro)
+    assert irun.value == rng.irun.value  # the same number of draws
+    return ref, dev
+
+
+@pytest.mark.parametrize("therm", ["PRL", "PRG"])
+@pytest.mark.parametrize("case", [dict(ncell=(4, 4, 4), nb=8),
+                                  dict(ncell=(4, 4, 4), nb=16, mts=5, dtfs=1.25, nbdf1=1, nbdf2=3)])
+def test_thermostat_kicks_match_oracle(therm, case):
+    s = systems.build(param="param_qspcfw", therm=therm, ttaufs=100.0, **case)
+    ref, dev = run_both(s, 4)
+    assert rel(dev.p, ref.p) < TOL
+    assert rel(dev.r, ref.r) < TOL
+    assert rel(dev.dvdr + dev.dvdr2, ref.dvdr + ref.dvdr2) < TOL
+
+
+@pytest.mark.parametrize("case", [dict(ncell=(4, 4, 4), nb=8), dict(ncell=(5, 5, 5), nb=4, mts=5, dtfs=1.25,
+                                                                     nbdf1=1, nbdf2=3)])
+def test_berendsen_barostat_matches_oracle(case):
+    s = systems.build(param="param_qspcfw", therm="NON", baro="BER", taufs=200.0, **case)
+    ref, dev = run_both(s, 4, nbaro=1)
+    assert abs(ref.box[0] - s["box"][0]) > 1e-9  # the box moved
+    assert np.abs(dev.box - ref.box).max() <= TOL * ref.box[0]
+    assert rel(dev.r, ref.r) < TOL
+    assert rel(dev.p, ref.p) < TOL
+    assert rel(dev.dvdr + dev.dvdr2, ref.dvdr + ref.dvdr2) < TOL
+
+
+def test_device_replays_gentest_equilibration():
+    # main.f90:298-299 seeding, full_forces, sample, then md_eq (100 NVT steps,
+    # then 1000 NPT steps with the Berendsen barostat), all on the device
+    from .test_oracle_golden import EQ, INP, MDEQ, gentest_system
+
+    s = gentest_system()
+    lib.init(s["params"])
+    na, nm, nb = s["na"], s["nm"], s["nb"]
+    lib.rng_reset()
+    irun = C.c_int(-INP["irun"])
+    lib.gaussian(irun, 1.0)
+    ctx = lib.Context(na, nb, s["mass"], s["z"])
+    try:
+        ctx.upload(r=s["r"], box=s["box"])
+        ctx.full_forces()
+        from rpmd_mainz_gb300 import system
+
+        ctx.upload(p=system.sample_momenta(na, nb, s["mass"], s["beta"], irun))
+
+        def md_eq_step():  # evolve, the printed estimators, then the collision test (md_eq.f90:186-315)
+            ctx.evolve(1, s["dt"], s["beta"])
+            ctx.sync()
+            e = ctx.estimators(s["beta"])
+            e["box"] = ctx.box[0]
+            if lib.ran2(irun) < 0.01:  # thresh for ens = NPT
+                ctx.upload(p=system.sample_momenta(na, nb, s["mass"], s["beta"], irun))
+            return e
+
+        pre = [md_eq_step() for _ in range(100)]  # NVT pre-equilibration
+        ctx.set_nbaro(1)
+        eq = [md_eq_step() for _ in range(INP["ne"])]
+        r_end = ctx.download()[0]
+    finally:
+        ctx.close()
+    E = np.array([[(nb * e["v"] + e["tk"] + e["vrp"]) / na, e["vrp"] / na, nb * e["v"] / na, e["tk"] / na]
+                  for e in pre])
+    assert np.abs(E - MDEQ["E_pre_eq"][:, 1:5]).max() <= 5.01e-9
+    E = np.array([[(nb * e["v"] + e["tk"] + e["vrp"]) / na, e["vrp"] / na, nb * e["v"] / na, e["tk"] / na]
+                  for e in eq])
+    assert np.abs(E - MDEQ["E_eq"][:, 1:5]).max() <= 5.01e-9
+    temp = np.array([e["temp"] for e in eq])
+    tv = np.array([orc.TOKJMOL * e["tv"] / nm for e in eq])
+    assert (np.abs(temp - MDEQ["temp_eq"][:, 1]) / MDEQ["temp_eq"][:, 1]).max() <= 1e-10
+    assert (np.abs(tv - MDEQ["virial_ke_eq"][:, 1]) / np.abs(MDEQ["virial_ke_eq"][:, 1])).max() <= 1e-10
+    pres = np.array([orc.TOBAR * e["pres"] for e in eq])[9::10]
+    assert np.abs(pres - MDEQ["pressure_eq"][:, 1]).max() <= 1e-9 * np.abs(MDEQ["pressure_eq"][:, 1]).max()
+    den = np.array([e["den"] for e in eq])[9::10]
+    assert np.abs(den - MDEQ["density_eq"][:, 1]).max() <= 1e-12
+    assert abs(eq[-1]["box"] - EQ["box"][0]) <= 1e-11
+    assert np.abs(r_end - EQ["r"]).max() <= 1e-8
