@@ -544,8 +544,9 @@ def run_nve(args, torch):
 
 def run_served(args, torch):
     """Poisson arrivals (mean 50 per second) of trajectory requests of mixed
-    sizes (64-1728 molecules, nb 4-64), each `--request-steps` evolve_pi steps,
-    served by the continuous-batching loop under a device-memory budget."""
+    sizes (64-1728 molecules, nb 4-64), half of them rigid TIP4P/2005 water
+    (evolve_rig_pi with RATTLE), each `--request-steps` steps, served by the
+    continuous-batching loop under a device-memory budget."""
     from rpmd_mainz_gb300 import lib, workloads
 
     stream = workloads.request_stream(n=args.requests, nsteps=args.request_steps)
@@ -555,13 +556,15 @@ def run_served(args, torch):
     t0 = time.perf_counter()
     nxt = 0
     done = []
-    shape = {}
+    shape, sidx = {}, {}
     with ClockSampler(0) as clk:
         while len(done) < len(stream):
             now = time.perf_counter() - t0
             while nxt < len(stream) and stream[nxt][0] <= now:
                 _, s, n = stream[nxt]
-                shape[srv.submit(s, s["r"], s["p"], n)] = (s["nm"], s["nb"])
+                rid = srv.submit(s, s["r"], s["p"], n)
+                shape[rid] = (s["nm"], s["nb"])
+                sidx[rid] = nxt
                 nxt += 1
             c = srv.counts()
             if c["active"] == 0 and c["queued"] == 0:
@@ -577,13 +580,35 @@ def run_served(args, torch):
     srv.close()
     lat = np.array([d["t_done"] for d in done])
     wait = np.array([d["t_admit"] for d in done])
+    # force error of the mixed path on served final states: up to three rigid
+    # and three flexible requests
+    by_id = {d["id"]: d for d in done}
+    ids = sorted(by_id)
+    rigid_ids = [i for i in ids if stream[sidx[i]][1]["rigid"]][:3]
+    flex_ids = [i for i in ids if not stream[sidx[i]][1]["rigid"]][:3]
+    errs = {}
+    for i in rigid_ids + flex_ids:
+        s = stream[sidx[i]][1]
+        out = []
+        for prec in (0, 1):
+            prm = s["params"].copy()
+            prm.precision = prec
+            lib.init(prm)
+            out.append(lib.full_forces(by_id[i]["r"], s["box"], s["z"]))
+        f64, fmx = out
+        t64 = f64["dvdr"] + f64["dvdr2"]
+        errs[i] = float(np.linalg.norm(fmx["dvdr"] + fmx["dvdr2"] - t64) / np.linalg.norm(t64))
     return {
         "metric": "bead-molecule-steps/s", "value": work / wall, "unit": "bead-molecule-steps/s", "n_gpus": 1,
         "steps": args.request_steps, "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64 mixed", "data": "synthetic request stream (seeded Poisson arrivals, CUB lattices)",
         "config": {"workload": "served_stream", "requests": len(stream), "arrival_rate_per_s": 50.0,
                    "steps_per_request": args.request_steps, "tick_steps": args.tick_steps, "slots": args.slots,
-                   "budget_gib": args.budget_gb, "sizes": "nm in 64..1728 (cubic lattices), nb in {4,8,16,32,64}"},
+                   "budget_gib": args.budget_gb, "sizes": "nm in 64..1728 (cubic lattices), nb in {4,8,16,32,64}",
+                   "rigid_requests": int(sum(1 for _, s, _ in stream if s["rigid"])),
+                   "models": "flexible q-SPC/Fw (evolve_pi) and rigid TIP4P/2005 (evolve_rig_pi, RATTLE)"},
+        "error_vs_fp64": {"force_rel_rms_max": max(errs.values()) if errs else None, "bound": 1e-5,
+                          "on": f"final states of {len(rigid_ids)} rigid and {len(flex_ids)} flexible requests"},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "queue_wait_p50": float(np.percentile(wait, 50)), "queue_wait_p99": float(np.percentile(wait, 99))},
         "wall_s": wall, "clocks": clk.summary(),

@@ -585,7 +585,6 @@ int dev_rattle_s1(double *r, const double *rold, double *p, int nm, const double
                   double *dvdr, double *vir, int na);
 int dev_rattle_s2(double *r, double *p, int nm, const double *mass, double dt, double *dvdr,
                   double *vir, int na);
-int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout);
 
 extern "C" {
 

@@ -74,7 +74,7 @@ int run_branches(gb_batch *b) {
   BCK(cudaEventRecord(b->fork, b->s0));
   for (auto &r : b->reps) {
     BCK(cudaStreamWaitEvent(r.c->stream, b->fork, 0));
-    int st = dev_evolve_pi(r.c, r.dt, r.beta);
+    int st = dev_evolve_step(r.c, r.dt, r.beta);  // evolve_pi, or evolve_rig_pi for rigid water
     if (st) return st;
     BCK(cudaEventRecord(r.join, r.c->stream));
     BCK(cudaStreamWaitEvent(b->s0, r.join, 0));
@@ -127,6 +127,9 @@ int gbrpmd_batch_destroy(gb_batch *b) {
 int gbrpmd_batch_add(gb_batch *b, gb_context *c, double dt, double beta, double thresh, int irun) {
   if (!b || !c) return ctx_set_error(GB_E_ARG, "null argument");
   if (!c->own_params) return ctx_set_error(GB_E_ARG, "a batch replica needs its own parameters (gbrpmd_ctx_set_params)");
+  if (c->nbaro) return ctx_set_error(GB_E_UNSUPPORTED, "a batch replica cannot run a barostat (it synchronises each step)");
+  if (c->P.therm == GB_THERM_PRG || c->P.therm == GB_THERM_PRL)
+    return ctx_set_error(GB_E_UNSUPPORTED, "a batch replica cannot run PRG/PRL kicks (host-drawn stream each step)");
   for (auto &r : b->reps)
     if (r.c == c) return ctx_set_error(GB_E_ARG, "context already in the batch");
   BCK(cudaStreamSynchronize(b->s0));
@@ -187,6 +190,7 @@ int gbrpmd_batch_step(gb_batch *b, int nsteps) {
       for (auto &r : b->reps) {
         int sp = dev_prepare(r.c, r.dt, r.beta);  // set-up copies synchronise: never inside the capture
         if (sp) return sp;
+        dev_graph_reset(r.c);  // nor a graph destruction
         l0.push_back(r.c->launches);
       }
       BCK(cudaStreamBeginCapture(b->s0, cudaStreamCaptureModeThreadLocal));

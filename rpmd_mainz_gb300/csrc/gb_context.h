@@ -186,6 +186,12 @@ int dev_full_forces(gb_context *c);                      // dvdr, dvdr2 from r
 int dev_evolve_pi(gb_context *c, double dt, double beta);
 // a PRG / PRL thermostat kick on the bead momenta (no-op for other thermostats)
 int therm_kick(gb_context *c, double dtk, double beta);
+// evolve_rig_pi (k_rattle.cu); vir_inout unused on the device
+int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout);
+// rigid water: no intramolecular potential (main.f90:151-159, iamrigid)
+inline bool ctx_rigid(const gb_context *c) { return c->P.apot == 0.0 && c->P.bpot == 0.0; }
+// one step of the context's integrator: evolve_rig_pi for rigid water, else evolve_pi
+int dev_evolve_step(gb_context *c, double dt, double beta);
 // one evolve_pi step, replayed from a captured CUDA graph when it can be
 int dev_step(gb_context *c, double dt, double beta);
 size_t dev_estimate_bytes(int na, int nb, const gb_params &P);

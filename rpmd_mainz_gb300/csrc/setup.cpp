@@ -121,7 +121,7 @@ int gbrpmd_run_md_eq(gb_context *c, int nsteps, double dt, double beta, double t
     }
   } clear{c};
   for (int s = 0; s < nsteps; ++s) {
-    int st = dev_evolve_pi(c, dt, beta);
+    int st = dev_evolve_step(c, dt, beta);
     if (st) return st;
     // energies, and with a barostat the vir_lf the next step reads, need the
     // step's accumulators; the last step is always collected

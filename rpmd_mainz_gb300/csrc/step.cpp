@@ -746,6 +746,14 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   return launch_status();
 }
 
+int dev_evolve_step(gb_context *c, double dt, double beta) {
+  if (ctx_rigid(c)) {
+    c->last_beta = beta;
+    return dev_evolve_rig_pi(c, dt, beta, nullptr);
+  }
+  return dev_evolve_pi(c, dt, beta);
+}
+
 void dev_graph_reset(gb_context *c) {
   if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
   c->graph.exec = nullptr;
@@ -761,6 +769,7 @@ void dev_graph_reset(gb_context *c) {
 // lists) drops the graph.
 int dev_step(gb_context *c, double dt, double beta) {
   auto &G = c->graph;
+  if (ctx_rigid(c)) return dev_evolve_step(c, dt, beta);  // its force call drops step graphs
   const bool eligible = c->use_graphs && !c->prof && !c->generic_mts &&
                         (c->nb == 2 || c->nb == 4 || c->nb == 8 || c->nb == 16 || c->nb == 32 || c->nb == 64) &&
                         c->P.therm != GB_THERM_PRG && c->P.therm != GB_THERM_PRL && !c->nbaro;

@@ -15,6 +15,8 @@ from . import system
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PARAM_QSPCFW = os.path.join(os.path.dirname(HERE), "tests", "golden", "params", "param_qspcfw")
+# rigid 4-site TIP4P/2005 water (O-H 0.9572 A, HOH 104.52 deg, M-site 0.1546 A, qH 0.5897 e)
+PARAM_TIP05 = os.path.join(os.path.dirname(HERE), "tests", "golden", "params", "param_tip05_rigid")
 
 CUBIC_CELLS = {64: 4, 216: 6, 343: 7, 512: 8, 729: 9, 1000: 10, 1331: 11, 1728: 12}
 
@@ -44,9 +46,12 @@ def replica_set(n=256, seed=2026, precision=1, sizes=(64, 216, 343, 512), beads=
 
 
 def request_stream(n=60, rate=50.0, seed=7, precision=1, sizes=(64, 216, 343, 512, 729, 1000, 1331, 1728),
-                   beads=(4, 8, 16, 32, 64), nsteps=100, temp=298.0):
+                   beads=(4, 8, 16, 32, 64), nsteps=100, temp=298.0, rigid_fraction=0.5):
     """n trajectory requests with Poisson arrivals (mean `rate` per second):
-    [(arrival_seconds, system, nsteps)], sizes and bead counts drawn per request."""
+    [(arrival_seconds, system, nsteps)], sizes and bead counts drawn per
+    request; a `rigid_fraction` of them are rigid TIP4P/2005 water (RATTLE,
+    at most 1666 molecules as the reference's bond table allows), the rest
+    flexible q-SPC/Fw."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
@@ -54,5 +59,7 @@ def request_stream(n=60, rate=50.0, seed=7, precision=1, sizes=(64, 216, 343, 51
         t += float(rng.exponential(1.0 / rate))
         nm = int(rng.choice(sizes))
         nb = int(rng.choice(beads))
-        out.append((t, _box(nm, nb, temp, precision, seed=100000 + 1000 * seed + i), nsteps))
+        rigid = bool(rng.random() < rigid_fraction) and nm <= 1666
+        out.append((t, _box(nm, nb, temp, precision, seed=100000 + 1000 * seed + i,
+                            param=PARAM_TIP05 if rigid else PARAM_QSPCFW), nsteps))
     return out

@@ -27,6 +27,8 @@ REPLICAS = [
     dict(param="param_qspcfw", ncell=(5, 5, 5), nb=4, mts=2, dtfs=1.0, temp=300.0),
     dict(param="param_qspcfw", ncell=(3, 3, 3), nb=16, mts=5, dtfs=1.25, nbdf1=1, nbdf2=5, temp=350.0),
     dict(param="param_qspcfw", ncell=(4, 4, 4), nb=32, mts=1, dtfs=0.5, temp=298.0, precision=1),
+    # rigid 4-site water (evolve_rig_pi with RATTLE) beside the flexible replicas
+    dict(param="param_tip05_rigid", ncell=(3, 3, 3), nb=4, mts=1, dtfs=0.5, temp=300.0),
 ]
 
 
@@ -46,7 +48,8 @@ def built():
 def make_replica(case, seed):
     s = systems.build(**case)
     lib.init(s["params"])
-    r = systems.perturbed(s, seed=seed)
+    # rigid water starts on its lattice, where the bond constraints hold
+    r = s["r"].copy() if s["rigid"] else systems.perturbed(s, seed=seed)
     ff = lib.full_forces(r, s["box"], s["z"])
     rng = np.random.default_rng(seed + 1)
     p = rng.normal(size=r.shape) * np.sqrt(s["mass"][None, :, None] / (s["beta"] / s["nb"]))

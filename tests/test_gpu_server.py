@@ -21,6 +21,7 @@ REQUESTS = [
     (dict(param="param_qspcfw", ncell=(5, 5, 5), nb=4, mts=2, dtfs=1.0, temp=300.0), 7),
     (dict(param="param_qspcfw", ncell=(4, 4, 4), nb=32, mts=1, dtfs=0.5, temp=280.0, precision=1), 5),
     (dict(param="param_qspcfw", ncell=(3, 3, 3), nb=8, mts=1, dtfs=0.5, temp=350.0), 6),
+    (dict(param="param_tip05_rigid", ncell=(3, 3, 3), nb=4, mts=1, dtfs=0.5, temp=300.0), 5),  # rigid, RATTLE
 ]
 
 
@@ -40,7 +41,7 @@ def built():
 def request_state(case, seed):
     s = systems.build(**case)
     lib.init(s["params"])
-    r = systems.perturbed(s, seed=seed)
+    r = s["r"].copy() if s["rigid"] else systems.perturbed(s, seed=seed)
     rng = np.random.default_rng(seed + 1)
     p = rng.normal(size=r.shape) * np.sqrt(s["mass"][None, :, None] / (s["beta"] / s["nb"]))
     return s, r, p
@@ -63,7 +64,7 @@ def test_served_results_equal_alone():
     alone = [run_alone(s, r, p, n) for case, n, s, r, p in reqs]
     srv = lib.Server(budget_bytes=8 << 30, max_slots=3)
     ids = {}
-    arrivals = {0: [0, 1], 2: [2], 3: [3, 4]}  # tick -> requests arriving
+    arrivals = {0: [0, 1], 2: [2], 3: [3, 4], 4: [5]}  # tick -> requests arriving
     finished = {}
     tick = 0
     while len(finished) < len(reqs):
