@@ -33,6 +33,7 @@ constexpr double RTOL = 1e-6;
 struct RatPar {
   double rcb[3];  // squared constrained lengths: reoh^2, reoh^2, rehh^2
   double rm[3];   // 1/mass of O, H1, H2
+  double g2[3];   // 1 / ((rm1 + rm2) rcb) per bond (stage-2 multiplier)
 };
 
 // bond b of a molecule: atoms (ii, jj)
@@ -41,14 +42,32 @@ GB_D void bond_atoms(int b, int &ii, int &jj) {
   jj = b == 0 ? 1 : 2;
 }
 
-// one molecule, stage 1; returns sweeps used; rec[0..4] = v11, v12, v22, v33, v23
-// sums, rec[5] = last gdx*dz term, rec[6] = 1 if any correction
+// One molecule, stage 1; returns the sweeps used; rec[0..4] = v11, v12, v22,
+// v33, v23 sums, rec[5] = the last correction's gdx*dz term, rec[6] = 1 if any
+// correction.  The sweeps follow the reference's order and tests.  Every
+// correction of bond b moves p, dvdr and the virial along the same vector (the
+// bond at the start, rold), so the sweeps update r and sum gamma per bond, and
+// p, dvdr and the virial sums take the summed gamma once at the end: the
+// reference's sums, reassociated.  FP64 divisions cost ~10 FP64 operations on
+// this GPU: those by dt become products with 1/dt.  Both change results by
+// rounding only.
 GB_D int rattle1_mol(double *r, const double *rold, double *p, double *f, double dt,
                      const RatPar &rp, double *rec) {
+  const double idt = 1.0 / dt;
+  double ov[3][3], gsum[3] = {0.0, 0.0, 0.0}, glast = 0.0;
+  int blast = -1;
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    int ii, jj;
+    bond_atoms(b, ii, jj);
+#pragma unroll
+    for (int x = 0; x < 3; ++x) ov[b][x] = rold[3 * jj + x] - rold[3 * ii + x];
+  }
   bool done = false;
   int it = 0;
   while (!done && it < ITMAX) {
     done = true;
+#pragma unroll
     for (int b = 0; b < 3; ++b) {
       int ii, jj;
       bond_atoms(b, ii, jj);
@@ -57,70 +76,113 @@ GB_D int rattle1_mol(double *r, const double *rold, double *p, double *f, double
       const double diff = rp.rcb[b] - d2;
       if (fabs(diff) > rp.rcb[b] * RTOL) {
         const double rm1 = rp.rm[jj], rm2 = rp.rm[ii];
-        const double dx2 = rold[3 * jj] - rold[3 * ii], dy2 = rold[3 * jj + 1] - rold[3 * ii + 1],
-                     dz2 = rold[3 * jj + 2] - rold[3 * ii + 2];
-        const double dot = dx1 * dx2 + dy1 * dy2 + dz1 * dz2;
+        const double dot = dx1 * ov[b][0] + dy1 * ov[b][1] + dz1 * ov[b][2];
         const double gamma = diff / (2.0 * (rm1 + rm2) * dot);
-        double gdx = gamma * dx2, gdy = gamma * dy2, gdz = gamma * dz2;
-        r[3 * jj] += rm1 * gdx; r[3 * jj + 1] += rm1 * gdy; r[3 * jj + 2] += rm1 * gdz;
-        r[3 * ii] -= rm2 * gdx; r[3 * ii + 1] -= rm2 * gdy; r[3 * ii + 2] -= rm2 * gdz;
-        gdx = gdx / dt; gdy = gdy / dt; gdz = gdz / dt;
-        p[3 * jj] += gdx; p[3 * jj + 1] += gdy; p[3 * jj + 2] += gdz;
-        p[3 * ii] -= gdx; p[3 * ii + 1] -= gdy; p[3 * ii + 2] -= gdz;
-        gdx = 2.0 * gdx; gdy = 2.0 * gdy; gdz = 2.0 * gdz;
-        rec[0] -= gdx * dx2;
-        rec[1] -= gdx * dy2;
-        rec[5] = gdx * dz2;
-        rec[6] = 1.0;
-        rec[4] -= gdy * dz2;
-        rec[2] -= gdy * dy2;
-        rec[3] -= gdz * dz2;
-        f[3 * jj] += gdx; f[3 * jj + 1] += gdy; f[3 * jj + 2] += gdz;
-        f[3 * ii] -= gdx; f[3 * ii + 1] -= gdy; f[3 * ii + 2] -= gdz;
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          const double g = gamma * ov[b][x];
+          r[3 * jj + x] += rm1 * g;
+          r[3 * ii + x] -= rm2 * g;
+        }
+        gsum[b] += gamma;
+        glast = gamma;
+        blast = b;
         done = false;
       }
     }
     ++it;
   }
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    if (gsum[b] == 0.0) continue;
+    int ii, jj;
+    bond_atoms(b, ii, jj);
+    const double g = gsum[b] * idt;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      p[3 * jj + x] += g * ov[b][x];
+      p[3 * ii + x] -= g * ov[b][x];
+      f[3 * jj + x] += 2.0 * g * ov[b][x];
+      f[3 * ii + x] -= 2.0 * g * ov[b][x];
+    }
+    const double g2 = 2.0 * g;
+    rec[0] -= g2 * ov[b][0] * ov[b][0];
+    rec[1] -= g2 * ov[b][0] * ov[b][1];
+    rec[2] -= g2 * ov[b][1] * ov[b][1];
+    rec[3] -= g2 * ov[b][2] * ov[b][2];
+    rec[4] -= g2 * ov[b][1] * ov[b][2];
+  }
+  if (blast >= 0) {
+    rec[5] = (2.0 * glast * idt * ov[blast][0]) * ov[blast][2];
+    rec[6] = 1.0;
+  }
   return it;
 }
 
-// one molecule, stage 2 (velocity constraints)
+// One molecule, stage 2 (velocity constraints).  r does not change here, so
+// the bond vectors are fixed and only p must follow every correction; dvdr and
+// the virial sums take the summed gamma per bond at the end (as in stage 1).
 GB_D int rattle2_mol(const double *r, double *p, double *f, double dt, const RatPar &rp,
                      double *rec) {
-  const double halfdt = 0.5 * dt;
+  const double ihalfdt = 2.0 / dt;
+  double bv[3][3], gsum[3] = {0.0, 0.0, 0.0}, glast = 0.0;
+  int blast = -1;
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    int ii, jj;
+    bond_atoms(b, ii, jj);
+#pragma unroll
+    for (int x = 0; x < 3; ++x) bv[b][x] = r[3 * jj + x] - r[3 * ii + x];
+  }
   bool done = false;
   int it = 0;
   while (!done && it <= ITMAX) {
     done = true;
+#pragma unroll
     for (int b = 0; b < 3; ++b) {
       int ii, jj;
       bond_atoms(b, ii, jj);
-      const double dx1 = r[3 * jj] - r[3 * ii], dy1 = r[3 * jj + 1] - r[3 * ii + 1], dz1 = r[3 * jj + 2] - r[3 * ii + 2];
       const double rm1 = rp.rm[jj], rm2 = rp.rm[ii];
       const double dvx1 = p[3 * jj] * rm1 - p[3 * ii] * rm2;
       const double dvy1 = p[3 * jj + 1] * rm1 - p[3 * ii + 1] * rm2;
       const double dvz1 = p[3 * jj + 2] * rm1 - p[3 * ii + 2] * rm2;
-      const double dot = dx1 * dvx1 + dy1 * dvy1 + dz1 * dvz1;
-      const double gamma = -dot / ((rm1 + rm2) * rp.rcb[b]);
+      const double dot = bv[b][0] * dvx1 + bv[b][1] * dvy1 + bv[b][2] * dvz1;
+      const double gamma = -dot * rp.g2[b];
       if (fabs(gamma) > RTOL) {
-        double gdx = gamma * dx1, gdy = gamma * dy1, gdz = gamma * dz1;
-        p[3 * jj] += gdx; p[3 * jj + 1] += gdy; p[3 * jj + 2] += gdz;
-        p[3 * ii] -= gdx; p[3 * ii + 1] -= gdy; p[3 * ii + 2] -= gdz;
-        gdx = gdx / halfdt; gdy = gdy / halfdt; gdz = gdz / halfdt;
-        rec[0] -= gdx * dx1;
-        rec[1] -= gdx * dy1;
-        rec[5] = gdx * dz1;
-        rec[6] = 1.0;
-        rec[4] -= gdy * dz1;
-        rec[2] -= gdy * dy1;
-        rec[3] -= gdz * dz1;
-        f[3 * jj] += gdx; f[3 * jj + 1] += gdy; f[3 * jj + 2] += gdz;
-        f[3 * ii] -= gdx; f[3 * ii + 1] -= gdy; f[3 * ii + 2] -= gdz;
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          const double g = gamma * bv[b][x];
+          p[3 * jj + x] += g;
+          p[3 * ii + x] -= g;
+        }
+        gsum[b] += gamma;
+        glast = gamma;
+        blast = b;
         done = false;
       }
     }
     ++it;
+  }
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    if (gsum[b] == 0.0) continue;
+    int ii, jj;
+    bond_atoms(b, ii, jj);
+    const double g = gsum[b] * ihalfdt;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      f[3 * jj + x] += g * bv[b][x];
+      f[3 * ii + x] -= g * bv[b][x];
+    }
+    rec[0] -= g * bv[b][0] * bv[b][0];
+    rec[1] -= g * bv[b][0] * bv[b][1];
+    rec[2] -= g * bv[b][1] * bv[b][1];
+    rec[3] -= g * bv[b][2] * bv[b][2];
+    rec[4] -= g * bv[b][1] * bv[b][2];
+  }
+  if (blast >= 0) {
+    rec[5] = (glast * ihalfdt * bv[blast][0]) * bv[blast][2];
+    rec[6] = 1.0;
   }
   return it;
 }
@@ -216,6 +278,7 @@ __global__ void k_rig_substeps(double *r, double *p, double *f2, int nm, int nb,
   const int m = blockIdx.x * mpb + ml;
   const bool valid = ml < mpb && m < nm;
   const double halfsmalldt = 0.5 * smalldt;
+  const double sdm[3] = {smalldt / mass3[0], smalldt / mass3[1], smalldt / mass3[2]};
   double rl[9], pl[9], fl[9], ro[9], rec[8];
   const long long S = 9LL * nm;  // doubles per bead
   if (valid) {
@@ -248,7 +311,7 @@ __global__ void k_rig_substeps(double *r, double *p, double *f2, int nm, int nb,
       for (int d = 0; d < 9; ++d) {
         ro[d] = rl[d];
         pl[d] = pl[d] - halfsmalldt * fl[d];
-        rl[d] = rl[d] + pl[d] * smalldt / mass3[d / 3];
+        rl[d] = rl[d] + pl[d] * sdm[d / 3];
       }
 #pragma unroll
       for (int d = 0; d < 8; ++d) rec[d] = 0.0;
@@ -299,6 +362,10 @@ RatPar make_rp(const gb_params &P, const double *mass3) {
   rp.rcb[1] = P.reoh * P.reoh;
   rp.rcb[2] = rehh * rehh;
   for (int i = 0; i < 3; ++i) rp.rm[i] = 1.0 / mass3[i];
+  for (int b = 0; b < 3; ++b) {
+    const int ii = b == 2 ? 1 : 0, jj = b == 0 ? 1 : 2;  // bond_atoms
+    rp.g2[b] = 1.0 / ((rp.rm[jj] + rp.rm[ii]) * rp.rcb[b]);
+  }
   return rp;
 }
 
@@ -395,17 +462,23 @@ int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) 
   int st = therm_kick(c, halfdt, beta);
   if (st) return st;
   launch_axpy(s, c->p, c->dvdr, -halfdt, N);
-  const int mpb = nb >= 128 ? 1 : 128 / nb;
+  // whole warps, but as many blocks as the molecules allow: the substeps are
+  // FP64-bound, so every SM should hold some of them
+  const int mpb = nb >= 32 ? 1 : (32 + nb - 1) / nb;
   const size_t smem = sizeof(double) * 9 * (size_t)mpb * nb;
+  prof_begin(c, PR_RATTLE);
   k_rig_substeps<<<nblk(nm, mpb), mpb * nb, smem, s>>>(c->r, c->p, c->dvdr2, nm, nb, mpb, smalldt,
                                                       omegan, rp, c->mass, c->status);
+  prof_end(c, PR_RATTLE, (double)nm * nb * nb);
   // intermolecular forces on all beads (evolve_rigid.f90:174)
   if ((st = term_forces_rigid(c))) return st;
   // p -= dt/2 dvdr; rattle stage 2 with dt, constraint virial (evolve_rigid.f90:181-190)
   launch_axpy(s, c->p, c->dvdr, -halfdt, N);
   double *rec = c->g;  // nb*nm*8 <= 3*na*nb doubles
+  prof_begin(c, PR_RATTLE);
   k_rattle<<<nblk((long long)nm * nb, 128), 128, 0, s>>>(2, c->r, nullptr, c->p, c->dvdr, nm, nb, dt, rp,
                                                         rec, c->status);
+  prof_end(c, PR_RATTLE, (double)nm * nb);
   double *vslot = c->acc + (size_t)ACC_INT * ACC_STRIDE;
   k_rattle_virial<<<nb, 256, 0, s>>>(rec, nm, nb, vslot + 1, 1.0, 1);
   c->plan.B_int = nb;  // vir_hf = sum_k vir_k / nb (evolve_rigid.f90:198)
