@@ -467,6 +467,212 @@ void kwald(int n, const double *q, const double *r, double &v, double vir[9], do
 }
 
 // ===========================================================================
+// Ewald sum, non-cubic box (ewald_noncubic.f90)
+// ===========================================================================
+// one real-space pair of rwald_basic / rwald_cell (ewald_noncubic.f90:103-152,
+// 271-308), i, j 1-based, minimum image per side
+inline void rwald_nc_pair(int i, int j, const int *mol, const double *q, const double *r, double &v,
+                          double vir[9], double *dvdr, double rcutsq, double alpha, double sfac,
+                          const double box[3], const double onbox[3]) {
+  const double p = 3.0525860, a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741,
+               a4 = -1.453152027, a5 = 1.061405429;
+  double dx = X(r, 0, i - 1) - X(r, 0, j - 1);
+  double dy = X(r, 1, i - 1) - X(r, 1, j - 1);
+  double dz = X(r, 2, i - 1) - X(r, 2, j - 1);
+  dx = dx - box[0] * nint(dx * onbox[0]);
+  dy = dy - box[1] * nint(dy * onbox[1]);
+  dz = dz - box[2] * nint(dz * onbox[2]);
+  double drsq = dx * dx + dy * dy + dz * dz;
+  if (drsq < rcutsq) {
+    double dr = std::sqrt(drsq);
+    double x = alpha * dr;
+    double e = std::exp(-x * x);
+    double t = p / (p + x);
+    double erfc = e * t * (a1 + t * (a2 + t * (a3 + t * (a4 + t * a5))));
+    if (mol[i - 1] == mol[j - 1]) erfc = erfc - 1.0;
+    double du = erfc / dr;
+    double dur = (sfac * e - du) / drsq;
+    double qij = q[i - 1] * q[j - 1];
+    double dv = qij * du;
+    double dvr = qij * dur;
+    double dvx = dvr * dx, dvy = dvr * dy, dvz = dvr * dz;
+    v = v + dv;
+    X(dvdr, 0, i - 1) += dvx; X(dvdr, 1, i - 1) += dvy; X(dvdr, 2, i - 1) += dvz;
+    X(dvdr, 0, j - 1) -= dvx; X(dvdr, 1, j - 1) -= dvy; X(dvdr, 2, j - 1) -= dvz;
+    M33(vir, 0, 0) += dx * dvx; M33(vir, 0, 1) += dx * dvy; M33(vir, 0, 2) += dx * dvz;
+    M33(vir, 1, 0) += dy * dvx; M33(vir, 1, 1) += dy * dvy; M33(vir, 1, 2) += dy * dvz;
+    M33(vir, 2, 0) += dz * dvx; M33(vir, 2, 1) += dz * dvy; M33(vir, 2, 2) += dz * dvz;
+  }
+}
+
+// rwald_basic (ewald_noncubic.f90:204-273) and rwald_cell (ewald_noncubic.f90:56-202)
+void rwald_nc(int n, const int *mol, const double *q, const double *r, double &v, double vir[9],
+              double *dvdr, double rcut, double alpha, const double box[3], bool cells) {
+  const double pi = std::acos(-1.0);
+  double rfac = alpha / std::sqrt(pi);
+  double sfac = -2.0 * rfac;
+  double rcutsq = rcut * rcut;
+  const double onbox[3] = {1.0 / box[0], 1.0 / box[1], 1.0 / box[2]};
+  if (!cells) {
+    for (int i = 1; i <= n; ++i)
+      for (int j = 1; j <= i - 1; ++j) rwald_nc_pair(i, j, mol, q, r, v, vir, dvdr, rcutsq, alpha, sfac, box, onbox);
+    return;
+  }
+  CellNC c;
+  cell_setup(box, rcut, c);
+  std::vector<int> list;
+  cell_list(r, list, c, n, box, 1);
+  for (int iz = 1; iz <= c.ncell[2]; ++iz)
+    for (int iy = 1; iy <= c.ncell[1]; ++iy)
+      for (int ix = 1; ix <= c.ncell[0]; ++ix) {
+        int i = c.L(ix, iy, iz);
+        while (i > 0) {
+          int j = list[i];
+          while (j > 0) {
+            rwald_nc_pair(i, j, mol, q, r, v, vir, dvdr, rcutsq, alpha, sfac, box, onbox);
+            j = list[j];
+          }
+          i = list[i];
+        }
+      }
+  for (int k = 1; k <= c.nn; ++k) {
+    int incx = c.ink[3 * (k - 1)], incy = c.ink[3 * (k - 1) + 1], incz = c.ink[3 * (k - 1) + 2];
+    for (int iz = 1; iz <= c.ncell[2]; ++iz) {
+      int jz = c.Mz(iz, incz);
+      for (int iy = 1; iy <= c.ncell[1]; ++iy) {
+        int jy = c.My(iy, incy);
+        for (int ix = 1; ix <= c.ncell[0]; ++ix) {
+          int jx = c.Mx(ix, incx);
+          int i = c.L(ix, iy, iz);
+          while (i > 0) {
+            int j = c.L(jx, jy, jz);
+            while (j > 0) {
+              rwald_nc_pair(i, j, mol, q, r, v, vir, dvdr, rcutsq, alpha, sfac, box, onbox);
+              j = list[j];
+            }
+            i = list[i];
+          }
+        }
+      }
+    }
+  }
+}
+
+// kwald_nc (ewald_noncubic.f90:275-460): every k with kx >= 0, |ky|, |kz| <= kmax
+// and 0 < |k|^2 < rkmax2; weight 2 pi / V at kx = 0, 4 pi / V beyond
+void kwald_nc(const double *r, const double *z, int n, double &v, double vir[9], double *dvdr,
+              double alpha, double rkmax2, int kmax, const double box[3]) {
+  const double pi = std::acos(-1.0);
+  double rfac = alpha / std::sqrt(pi);
+  double twopi = 2.0 * pi;
+  double xbox = box[0], ybox = box[1], zbox = box[2];
+  double xlat = twopi / xbox, ylat = twopi / ybox, zlat = twopi / zbox;
+  const int K = kmax, W = 2 * kmax + 1;
+  std::vector<double> ckx((size_t)n * (K + 1)), skx((size_t)n * (K + 1)), cky((size_t)n * W), sky((size_t)n * W),
+      ckz((size_t)n * W), skz((size_t)n * W), cxy(n), sxy(n), dsdr(6 * (size_t)n);
+  auto IX = [&](int i, int k) { return (size_t)i + (size_t)n * k; };          // (i, 0:kmax)
+  auto IY = [&](int i, int k) { return (size_t)i + (size_t)n * (k + K); };    // (i, -kmax:kmax)
+  for (int i = 0; i < n; ++i) {
+    ckx[IX(i, 0)] = z[i];
+    skx[IX(i, 0)] = 0.0;
+    double xi = xlat * X(r, 0, i);
+    double c = std::cos(xi), s = std::sin(xi);
+    for (int kx = 1; kx <= K; ++kx) {
+      ckx[IX(i, kx)] = c * ckx[IX(i, kx - 1)] - s * skx[IX(i, kx - 1)];
+      skx[IX(i, kx)] = s * ckx[IX(i, kx - 1)] + c * skx[IX(i, kx - 1)];
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    cky[IY(i, 0)] = 1.0;
+    sky[IY(i, 0)] = 0.0;
+    double yi = ylat * X(r, 1, i);
+    double c = std::cos(yi), s = std::sin(yi);
+    for (int ky = 1; ky <= K; ++ky) {
+      cky[IY(i, ky)] = c * cky[IY(i, ky - 1)] - s * sky[IY(i, ky - 1)];
+      sky[IY(i, ky)] = s * cky[IY(i, ky - 1)] + c * sky[IY(i, ky - 1)];
+      cky[IY(i, -ky)] = cky[IY(i, ky)];
+      sky[IY(i, -ky)] = -sky[IY(i, ky)];
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    ckz[IY(i, 0)] = 1.0;
+    skz[IY(i, 0)] = 0.0;
+    double zi = zlat * X(r, 2, i);
+    double c = std::cos(zi), s = std::sin(zi);
+    for (int kz = 1; kz <= K; ++kz) {
+      ckz[IY(i, kz)] = c * ckz[IY(i, kz - 1)] - s * skz[IY(i, kz - 1)];
+      skz[IY(i, kz)] = s * ckz[IY(i, kz - 1)] + c * skz[IY(i, kz - 1)];
+      ckz[IY(i, -kz)] = ckz[IY(i, kz)];
+      skz[IY(i, -kz)] = -skz[IY(i, kz)];
+    }
+  }
+  double b = 0.25 / (alpha * alpha);
+  double f = twopi / (xbox * ybox * zbox);
+  for (int kx = 0; kx <= K; ++kx) {
+    if (kx == 1) f = 2.0 * f;
+    double rkx = xlat * kx;
+    for (int ky = -K; ky <= K; ++ky) {
+      double rky = ylat * ky;
+      for (int i = 0; i < n; ++i) {
+        cxy[i] = ckx[IX(i, kx)] * cky[IY(i, ky)] - skx[IX(i, kx)] * sky[IY(i, ky)];
+        sxy[i] = ckx[IX(i, kx)] * sky[IY(i, ky)] + skx[IX(i, kx)] * cky[IY(i, ky)];
+      }
+      for (int kz = -K; kz <= K; ++kz) {
+        double rkz = zlat * kz;
+        double rk2 = rkx * rkx + rky * rky + rkz * rkz;
+        if (rk2 < rkmax2 && rk2 != 0.0) {
+          double sr = 0.0, si = 0.0;
+          for (int i = 0; i < n; ++i) {
+            double tr = cxy[i] * ckz[IY(i, kz)] - sxy[i] * skz[IY(i, kz)];
+            double ti = cxy[i] * skz[IY(i, kz)] + sxy[i] * ckz[IY(i, kz)];
+            sr = sr + tr;
+            si = si + ti;
+            dsdr[6 * i + 0] = -rkx * ti;
+            dsdr[6 * i + 1] = rkx * tr;
+            dsdr[6 * i + 2] = -rky * ti;
+            dsdr[6 * i + 3] = rky * tr;
+            dsdr[6 * i + 4] = -rkz * ti;
+            dsdr[6 * i + 5] = rkz * tr;
+          }
+          double w = (f / rk2) * std::exp(-b * rk2);
+          double et = w * (sr * sr + si * si);
+          v = v + et;
+          w = 2.0 * w;
+          sr = w * sr;
+          si = w * si;
+          for (int i = 0; i < n; ++i) {
+            X(dvdr, 0, i) += sr * dsdr[6 * i + 0] + si * dsdr[6 * i + 1];
+            X(dvdr, 1, i) += sr * dsdr[6 * i + 2] + si * dsdr[6 * i + 3];
+            X(dvdr, 2, i) += sr * dsdr[6 * i + 4] + si * dsdr[6 * i + 5];
+          }
+          double term = 2.0 * (1.0 / rk2 + b);
+          double xx = et * (term * rkx * rkx - 1.0), xy = et * (term * rkx * rky), xz = et * (term * rkx * rkz);
+          double yy = et * (term * rky * rky - 1.0), yz = et * (term * rky * rkz), zz = et * (term * rkz * rkz - 1.0);
+          M33(vir, 0, 0) += xx; M33(vir, 0, 1) += xy; M33(vir, 0, 2) += xz;
+          M33(vir, 1, 0) += xy; M33(vir, 1, 1) += yy; M33(vir, 1, 2) += yz;
+          M33(vir, 2, 0) += xz; M33(vir, 2, 1) += yz; M33(vir, 2, 2) += zz;
+        }
+      }
+    }
+  }
+  double vs = 0.0;
+  for (int i = 0; i < n; ++i) vs = vs + z[i] * z[i];
+  vs = rfac * vs;
+  v = v - vs;
+}
+
+// ewald_nc (ewald_noncubic.f90:1-54), point charges: rwald_basic when
+// 3 wrcut > the longest side, else rwald_cell; then kwald_nc
+void ewald_nc(int n, const int *mol, const double *q, const double *r, double &v, double vir[9],
+              double *dvdr, const double box[3]) {
+  v = 0.0;
+  zero9(vir);
+  double boxmax = std::max(box[0], std::max(box[1], box[2]));
+  rwald_nc(n, mol, q, r, v, vir, dvdr, P.wrcut, P.walpha, box, !(3.0 * P.wrcut > boxmax));
+  kwald_nc(r, q, n, v, vir, dvdr, P.walpha, P.rkmax * P.rkmax, P.kmax, box);
+}
+
+// ===========================================================================
 // neighbour lists (neigh_list.f90); list/point are 1-based like the Fortran:
 // point has na+3 entries at indices 1..na+3, list has maxnab*na entries at
 // indices 1..maxnab*na; index 0 of each array is unused.
@@ -1112,7 +1318,7 @@ Status potenl_opt(double *r, double &v, double *dvdr, double vir[9], int na, int
   int nm = na / 3;
   if (3 * nm != na) return GB_E_ARG;
   if (iopt <= 2) {
-    if (!P.iamcub) return GB_E_UNSUPPORTED;  // ewald_nc (ewald_noncubic.f90)
+    if (P.wm > 0.0 || P.wh > 0.0) return GB_E_UNSUPPORTED;  // rwald_smeared (ewald_smeared.f90)
     double alpha = P.alpha;
     double alpha2 = 0.5 * (1.0 - alpha);
     std::vector<int> mol(na);
@@ -1124,7 +1330,8 @@ Status potenl_opt(double *r, double &v, double *dvdr, double vir[9], int na, int
         X(r, j, i) = alpha * X(r, j, i) + alpha2 * (X(r, j, i + 1) + X(r, j, i + 2));
       }
     double vew, vir_ew[9];
-    ewald_cubic(na, mol.data(), z, r, vew, vir_ew, dvdr, box[0]);
+    if (P.iamcub) ewald_cubic(na, mol.data(), z, r, vew, vir_ew, dvdr, box[0]);
+    else ewald_nc(na, mol.data(), z, r, vew, vir_ew, dvdr, box);  // md_forces.f90:192-197
     v = v + vew;
     for (int i = 0; i < 9; ++i) vir[i] += vir_ew[i];
     for (int j = 0, ic = 0; j < na; j += 3, ++ic)
