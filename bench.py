@@ -345,7 +345,7 @@ def force_error(s):
 
 
 def run_replicas(args, torch):
-    """256 independent NVT replicas (molecules in {64, 216, 343, 512}, nb in
+    """256 independent NVT replicas (molecules in {64, 128, 216, 343, 512}, nb in
     {8, 16, 32, 64}, T in [250, 350] K, Andersen thresh 0.01, dt 0.5 fs): the
     mixed-precision batch (one CUDA-graph launch per step for all replicas)
     against the plain-FP64 contexts stepped in a loop (each on its own stream,
@@ -429,7 +429,7 @@ def run_replicas(args, torch):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 mixed",
         "data": "synthetic (CUB lattices, momenta from the reference's ran2 stream, seeded per replica)",
         "config": {"workload": "replicas_256", "replicas": len(reps), "bead_molecules_per_step": work,
-                   "sizes": "nm in {64,216,343,512}, nb in {8,16,32,64}, T in [250,350] K",
+                   "sizes": "nm in {64,128 (8x4x4 non-cubic box),216,343,512}, nb in {8,16,32,64}, T in [250,350] K",
                    "l2": "inputs larger than L2 in aggregate", "parallelism": "one batch, one graph per step"},
         "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
         "fp64_loop": {"value": fp64_value, "ms_per_step": float(np.mean(loop_ms))},

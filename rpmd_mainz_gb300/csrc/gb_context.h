@@ -81,15 +81,17 @@ struct gb_context {
   double list_skin = 0.1;  // skin as a fraction of the cut-off; 0: full rebuild at every use
 
   // reciprocal space
-  int kmax_alloc = -1;           // k tables built for these kmax, rkmax, walpha
+  int kmax_alloc = -1;           // k tables built for these kmax, rkmax, walpha,
   double k_rkmax = -1.0, k_walpha = -1.0;
+  int k_iamcub = -1;              // box kind
+  double k_box[3] = {0, 0, 0};    // and (non-cubic tables) box
   int ncol = 0, nkp = 0, ngrp = 0;  // (kx,ky) columns, k pairs (kx,ky,+-m), structure-factor items
   int nk = 0;                   // k vectors of the half space
   KCol *kcol = nullptr;         // [ncol] columns (gb_kvec.h)
   int4 *kgrp = nullptr;         // [ngrp] structure-factor work items
   int4 *kpair = nullptr;        // [nkp] kx, ky, m, kind
   double *kw = nullptr;         // [nkp] weights (4 pi / k^2) exp(-b k^2)
-  double *kvir = nullptr;       // [nkp][9] virial factors (gb_kvir_table)
+  double *kvir = nullptr;       // [nkp][GB_KVIR] virial factors (gb_kvec.h)
   double2 *ktab = nullptr;      // [nconf][na][3][kmax+1] per-site powers e^{i 2 pi m x}
   double *sk_part = nullptr;    // [nconf][nchunk][nkp][4] chunk partials of P, Q
   double *sk = nullptr;         // [nconf][nkp][8] force tables

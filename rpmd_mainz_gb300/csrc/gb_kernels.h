@@ -11,6 +11,7 @@ int recip_group_len();               // m values per structure-factor work item
 size_t recip_sk_smem(int kmax);      // dynamic shared memory of the passes
 size_t recip_force_smem(int kmax);
 void recip_set_attributes();         // raises the kernels' shared-memory limit once
+double3 recip_lat(const gb_context *c);  // k per integer index along each axis
 
 // Geometry of one pair search.  Point i of configuration c sits at
 // pos[c * cstride + i * pstride + {0,1,2}] (doubles).  `unit` selects the
@@ -54,8 +55,9 @@ int list_max(cudaStream_t s, const PairList &pl);       // diagnostics only (syn
 // rs: M-site substituted positions scaled by 1/L, [B][na][3]
 void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, double alpha,
                   double scale);
+// box: nullptr for unit-box positions (cubic sum), else the box in bohr (non-cubic)
 void launch_ewald_real(cudaStream_t s, const double *rs, const double *q, int na, int B,
-                       const PairList &pl, double alpha, double *g, double *acc);
+                       const PairList &pl, double alpha, const double *box, double *g, double *acc);
 // structure factors: per-site power tables, then chunk partials (2 launches)
 void launch_recip_sk(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);
 void launch_recip_weights(cudaStream_t s, gb_context *c, int B, double *acc);
@@ -63,8 +65,9 @@ void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const d
                         double *g);
 // ---- mixed precision (k_mixed.cu): FP32 arithmetic, full lists, hi/lo positions ----
 // hi.w carries the site charge (launch_frac32 with q)
+// box: side lengths of the fractional coordinates (1, 1, 1 for the cubic sum)
 void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double rcutsq, double *g, double *acc);
+                          double alpha, double rcutsq, const double *box, double *g, double *acc);
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
                   double sigsq, double rcutsq, const double *box, double dscale, double *out, double *acc);
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);

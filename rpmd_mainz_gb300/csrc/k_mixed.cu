@@ -105,10 +105,13 @@ GB_D void block_sum_sym7_mx(double (&vals)[7], double *sh, double *acc) {
 // The charge rides in hi.w.  Each lane takes every NP-th partner, four at a
 // time with their indices and positions loaded before any arithmetic, so that
 // four gathers are in flight per lane.
+// bx: side lengths that turn fractional differences into distances (1 in the
+// unit box of the cubic sum; the box in bohr for the non-cubic one,
+// rwald_basic / rwald_cell of ewald_noncubic.f90)
 __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                                                         int na, const int *__restrict__ count,
                                                         const int *__restrict__ idx, int cap, float alpha,
-                                                        float rcutsq, double *g, double *acc) {
+                                                        float rcutsq, float3 bx, double *g, double *acc) {
   __shared__ double sh[32 * 7];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
@@ -127,9 +130,9 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
     const int n = min(count[(long long)c * na + i], cap);
     const int *L = idx + ((long long)c * na + i) * cap;
     auto pair = [&](int j, const float4 &hj, const float4 &lj) {
-      const float dx = dmin(hi_i.x, lo_i.x, hj.x, lj.x);
-      const float dy = dmin(hi_i.y, lo_i.y, hj.y, lj.y);
-      const float dz = dmin(hi_i.z, lo_i.z, hj.z, lj.z);
+      const float dx = bx.x * dmin(hi_i.x, lo_i.x, hj.x, lj.x);
+      const float dy = bx.y * dmin(hi_i.y, lo_i.y, hj.y, lj.y);
+      const float dz = bx.z * dmin(hi_i.z, lo_i.z, hj.z, lj.z);
       const float drsq = dx * dx + dy * dy + dz * dz;
       if (!(drsq < rcutsq)) return;  // skin-list entry beyond the cut-off
       const float inv = rsqrtf(drsq);
@@ -267,13 +270,15 @@ constexpr int SIGN32 = (int)0x80000000u;
 
 GB_D float flipf(float v, int mask) { return __int_as_float(__float_as_int(v) ^ mask); }
 
-// FP64 recurrence (ewald_cubic.f90:254-286) rounded to FP32
-__global__ void k_recip_tables_mx(const double *rs, const double *q, int na, int B, int kmax, float2 *tab) {
+// FP64 recurrence (ewald_cubic.f90:254-286, ewald_noncubic.f90:296-336)
+// rounded to FP32; lat as in k_recip_tables
+__global__ void k_recip_tables_mx(const double *rs, const double *q, int na, int B, int kmax, double3 lat,
+                                  float2 *tab) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= 3LL * na * B) return;
   const int ax = (int)(w % 3);
   const int s = (int)((w / 3) % na);
-  const double arg = 2.0 * acos(-1.0) * rs[w];
+  const double arg = (ax == 0 ? lat.x : ax == 1 ? lat.y : lat.z) * rs[w];
   double sn, cs;
   sincos(arg, &sn, &cs);
   double pr = ax == 0 ? q[s] : 1.0, pi = 0.0;
@@ -367,9 +372,10 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
     }
     const int4 kv = kpair[k];
     const double w = kw[k];
-    double et, Ar, Ai, Dr, Di;
+    double et, ed = 0.0, Ar, Ai, Dr, Di;  // ed: et(+m) - et(-m)
     if (kv.w == 1) {
       et = 2.0 * w * (Pr * Pr + Pi * Pi + Qr * Qr + Qi * Qi);
+      ed = 4.0 * w * (Pi * Qr - Pr * Qi);
       Ar = 4.0 * w * Pr;
       Ai = 4.0 * w * Pi;
       Dr = -4.0 * w * Qi;
@@ -386,13 +392,15 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
       Dr = Di = 0.0;
     }
     vals[0] = et;
-    // the reference combines the (+-ky, +-kz) partners into one energy and
-    // multiplies it by term * rk_a * rk_b with rk_y, rk_z >= 0, so its
-    // off-diagonal virial uses |k_a| |k_b| (ewald_cubic.f90:488-503); the
-    // factors come from gb_kvir_table
-    const double *kv9 = kvir + 9LL * k;
+    // virial factors (gb_kvec.h): [0..8] on the summed energy, [9], [10] on
+    // the difference for xz, yz (non-cubic sum only)
+    const double *kf = kvir + (long long)GB_KVIR * k;
 #pragma unroll
-    for (int e = 0; e < 9; ++e) vals[1 + e] = et * kv9[e];
+    for (int e = 0; e < 9; ++e) vals[1 + e] = et * kf[e];
+    vals[1 + 6] += ed * kf[9];
+    vals[1 + 2] += ed * kf[9];
+    vals[1 + 7] += ed * kf[10];
+    vals[1 + 5] += ed * kf[10];
     const double m = (double)kv.z;
     float4 *o = sk + ((long long)c * nkp + k) * 2;
     o[0] = make_float4((float)Ar, (float)-Ai, (float)Dr, (float)Di);
@@ -409,7 +417,7 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
 template <bool STAGED>
 __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__restrict__ tab, int na, int kmax,
                                                               int ncol, const KCol *__restrict__ cols, int nkp,
-                                                              const float4 *__restrict__ sk, double *g) {
+                                                              const float4 *__restrict__ sk, double3 lat, double *g) {
   // [3][K1][MF_S] float2 site tables, [MF_G][MF_S][3] double sums, then
   // (STAGED) the k-pair table [nkp][2] float4
   extern __shared__ float4 smf[];
@@ -484,7 +492,7 @@ __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__
     const int s2 = t / 3, d = t % 3;
     double f = 0.0;
     for (int w = 0; w < MF_G; ++w) f += red[(w * MF_S + s2) * 3 + d];
-    if (i0 + s2 < na) g[((long long)c * na + i0 + s2) * 3 + d] += 2.0 * acos(-1.0) * f;
+    if (i0 + s2 < na) g[((long long)c * na + i0 + s2) * 3 + d] += (d == 0 ? lat.x : d == 1 ? lat.y : lat.z) * f;
   }
 }
 
@@ -500,9 +508,11 @@ int sm_count_mx() {
 }  // namespace
 
 void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double rcutsq, double *g, double *acc) {
+                          double alpha, double rcutsq, const double *box, double *g, double *acc) {
   dim3 grid(nblk((long long)na * MX_NP, MX_T), B);
-  k_ewald_real_mx<<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, (float)rcutsq, g, acc);
+  const float3 bx = make_float3((float)box[0], (float)box[1], (float)box[2]);
+  k_ewald_real_mx<<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, (float)rcutsq, bx, g,
+                                        acc);
 }
 
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
@@ -525,7 +535,7 @@ void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const d
   const int kmax = c->P.kmax;
   const long long nw = 3LL * c->na * B;
   float2 *tab = reinterpret_cast<float2 *>(c->ktab);
-  k_recip_tables_mx<<<nblk(nw, 128), 128, 0, s>>>(rs, q, c->na, B, kmax, tab);
+  k_recip_tables_mx<<<nblk(nw, 128), 128, 0, s>>>(rs, q, c->na, B, kmax, recip_lat(c), tab);
   const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
   dim3 grid(nblk(c->ngrp, MSK_T), nchunk, B);
   k_recip_sk_mx<<<grid, MSK_T, recip_sk_smem_mx(kmax), s>>>(tab, c->na, kmax, c->ngrp, c->kgrp, c->nkp, nchunk,
@@ -548,11 +558,11 @@ void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
   if (staged <= 160 * 1024)
     k_recip_force_mx<true><<<grid, MF_S * MF_G, staged, s>>>(
         reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
-        reinterpret_cast<const float4 *>(c->sk), g);
+        reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
   else
     k_recip_force_mx<false><<<grid, MF_S * MF_G, recip_force_smem_mx(kmax, 0), s>>>(
         reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
-        reinterpret_cast<const float4 *>(c->sk), g);
+        reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
 }
 
 void recip_set_attributes_mx() {

@@ -299,10 +299,13 @@ GB_D void block_sum_sym7(double (&vals)[7], double *sh, double *acc) {
   }
 }
 
+// NC: positions in bohr in a non-cubic box (rwald_basic / rwald_cell,
+// ewald_noncubic.f90:56-273): minimum image dx - L nint(dx / L) per side
+template <bool NC>
 __global__ void __launch_bounds__(PAIR_T) k_ewald_real(const double *__restrict__ rs, const double *__restrict__ q,
                                                        int na, const int *__restrict__ count,
                                                        const int *__restrict__ idx, int cap, double alpha,
-                                                       double *g, double *acc) {
+                                                       double3 box, double3 onbox, double *g, double *acc) {
   __shared__ double sh[32 * 7];
   const double p = 3.0525860, a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741,
                a4 = -1.453152027, a5 = 1.061405429;
@@ -323,9 +326,15 @@ __global__ void __launch_bounds__(PAIR_T) k_ewald_real(const double *__restrict_
     for (int t = sub; t < n; t += PAIR_NP) {
       const int j = L[t];
       double dx = xi - R[3 * j], dy = yi - R[3 * j + 1], dz = zi - R[3 * j + 2];
-      dx -= rint(dx);
-      dy -= rint(dy);
-      dz -= rint(dz);
+      if (NC) {
+        dx -= box.x * rint(dx * onbox.x);
+        dy -= box.y * rint(dy * onbox.y);
+        dz -= box.z * rint(dz * onbox.z);
+      } else {
+        dx -= rint(dx);
+        dy -= rint(dy);
+        dz -= rint(dz);
+      }
       const double drsq = dx * dx + dy * dy + dz * dz;
       const double inv = rsqrt(drsq);
       const double x = alpha * (drsq * inv);
@@ -617,9 +626,16 @@ void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, in
 }
 
 void launch_ewald_real(cudaStream_t s, const double *rs, const double *q, int na, int B,
-                       const PairList &pl, double alpha, double *g, double *acc) {
+                       const PairList &pl, double alpha, const double *box, double *g, double *acc) {
   dim3 grid(nblk((long long)na * PAIR_NP, PAIR_T), B);
-  k_ewald_real<<<grid, PAIR_T, 0, s>>>(rs, q, na, pl.count, pl.idx, pl.cap, alpha, g, acc);
+  if (box) {
+    const double3 bx = make_double3(box[0], box[1], box[2]);
+    const double3 ob = make_double3(1.0 / box[0], 1.0 / box[1], 1.0 / box[2]);
+    k_ewald_real<true><<<grid, PAIR_T, 0, s>>>(rs, q, na, pl.count, pl.idx, pl.cap, alpha, bx, ob, g, acc);
+  } else {
+    const double3 one = make_double3(1.0, 1.0, 1.0);
+    k_ewald_real<false><<<grid, PAIR_T, 0, s>>>(rs, q, na, pl.count, pl.idx, pl.cap, alpha, one, one, g, acc);
+  }
 }
 
 void launch_lj(cudaStream_t s, const double *r, int na, int B, const PairList &pl, double sigsq,

@@ -40,14 +40,17 @@ constexpr long long SIGN = (long long)0x8000000000000000ULL;
 // flips the sign of v when mask is the sign bit (integer pipe, no FP64 op)
 GB_D double flip(double v, long long mask) { return __longlong_as_double(__double_as_longlong(v) ^ mask); }
 
-// per (conf, site, axis): powers e^{i 2 pi m x}, m = 0..kmax, by the
-// reference's recurrence (ewald_cubic.f90:254-286); the x table carries the charge
-__global__ void k_recip_tables(const double *rs, const double *q, int na, int B, int kmax, double2 *tab) {
+// per (conf, site, axis): powers e^{i lat m x}, m = 0..kmax, by the
+// reference's recurrence (ewald_cubic.f90:254-286, ewald_noncubic.f90:296-336);
+// lat = 2 pi in the unit box, 2 pi / L_axis for positions in bohr (non-cubic);
+// the x table carries the charge
+__global__ void k_recip_tables(const double *rs, const double *q, int na, int B, int kmax, double3 lat,
+                               double2 *tab) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= 3LL * na * B) return;
   const int ax = (int)(w % 3);
   const int s = (int)((w / 3) % na);
-  const double arg = 2.0 * acos(-1.0) * rs[w];
+  const double arg = (ax == 0 ? lat.x : ax == 1 ? lat.y : lat.z) * rs[w];
   double sn, cs;
   sincos(arg, &sn, &cs);
   double pr = ax == 0 ? q[s] : 1.0, pi = 0.0;
@@ -138,9 +141,10 @@ __global__ void __launch_bounds__(256) k_recip_weights(const double4_32a *sk_par
     }
     const int4 kv = kpair[k];
     const double w = kw[k];
-    double et, Ar, Ai, Dr, Di;
+    double et, ed = 0.0, Ar, Ai, Dr, Di;  // ed: et(+m) - et(-m)
     if (kv.w == 1) {  // S(+-m) = P +- iQ
       et = 2.0 * w * (Pr * Pr + Pi * Pi + Qr * Qr + Qi * Qi);
+      ed = 4.0 * w * (Pi * Qr - Pr * Qi);
       Ar = 4.0 * w * Pr;
       Ai = 4.0 * w * Pi;
       Dr = -4.0 * w * Qi;
@@ -157,13 +161,16 @@ __global__ void __launch_bounds__(256) k_recip_weights(const double4_32a *sk_par
       Dr = Di = 0.0;
     }
     vals[0] = et;
-    // the reference combines the (+-ky, +-kz) partners into one energy and
-    // multiplies it by term * rk_a * rk_b with rk_y, rk_z >= 0, so its
-    // off-diagonal virial uses |k_a| |k_b| (ewald_cubic.f90:488-503); the
-    // factors come from gb_kvir_table
-    const double *kv9 = kvir + 9LL * k;
+    // virial factors (gb_kvec.h): [0..8] on the summed energy, [9], [10] on the
+    // difference for xz, yz (non-cubic sum; zero in the cubic one, whose
+    // reference virial uses |k_a| |k_b|, ewald_cubic.f90:488-503)
+    const double *kf = kvir + (long long)GB_KVIR * k;
 #pragma unroll
-    for (int e = 0; e < 9; ++e) vals[1 + e] = et * kv9[e];
+    for (int e = 0; e < 9; ++e) vals[1 + e] = et * kf[e];
+    vals[1 + 6] += ed * kf[9];
+    vals[1 + 2] += ed * kf[9];
+    vals[1 + 7] += ed * kf[10];
+    vals[1 + 5] += ed * kf[10];
     const double m = (double)kv.z;
     double4_32a *o = sk + ((long long)c * nkp + k) * 2;
     o[0] = make_double4_32a(Ar, -Ai, Dr, Di);
@@ -176,7 +183,7 @@ __global__ void __launch_bounds__(256) k_recip_weights(const double4_32a *sk_par
 // whose first k pair lies in this block's share [seg nkp / nseg, (seg+1) nkp / nseg)
 __global__ void __launch_bounds__(F_T) k_recip_force(const double2 *__restrict__ tab, int na, int kmax,
                                                      int ncol, const KCol *__restrict__ cols, int nkp,
-                                                     const double4_32a *__restrict__ sk, double *g) {
+                                                     const double4_32a *__restrict__ sk, double3 lat, double *g) {
   extern __shared__ double2 st[];  // [3][K1][F_T]
   const int K1 = kmax + 1, K3 = 3 * K1;
   const int c = blockIdx.z, t = threadIdx.x;
@@ -227,11 +234,10 @@ __global__ void __launch_bounds__(F_T) k_recip_force(const double2 *__restrict__
     fz = fz - fma(cr, vi, ci * vr);
   }
   if (i < na && col1 > col0) {
-    const double rlat = 2.0 * acos(-1.0);
     double *G = g + ((long long)c * na + i) * 3;
-    atomicAdd(G, rlat * fx);
-    atomicAdd(G + 1, rlat * fy);
-    atomicAdd(G + 2, rlat * fz);
+    atomicAdd(G, lat.x * fx);
+    atomicAdd(G + 1, lat.y * fy);
+    atomicAdd(G + 2, lat.z * fz);
   }
 }
 
@@ -246,6 +252,13 @@ int sm_count() {
 
 }  // namespace
 
+// 2 pi per axis for unit-box positions (cubic sum), 2 pi / L_axis for bohr (non-cubic)
+double3 recip_lat(const gb_context *c) {
+  const double twopi = 2.0 * acos(-1.0);
+  if (c->P.iamcub) return make_double3(twopi, twopi, twopi);
+  return make_double3(twopi / c->box[0], twopi / c->box[1], twopi / c->box[2]);
+}
+
 int recip_sk_chunk() { return SK_CHUNK; }
 int recip_group_len() { return SK_G; }
 size_t recip_sk_smem(int kmax) { return sizeof(double2) * SK_CHUNK * 3 * (kmax + 1); }
@@ -255,7 +268,7 @@ void launch_recip_sk(cudaStream_t s, gb_context *c, const double *rs, const doub
   if (c->nkp == 0) return;  // no k vector inside rkmax
   const int kmax = c->P.kmax;
   const long long nw = 3LL * c->na * B;
-  k_recip_tables<<<nblk(nw, 128), 128, 0, s>>>(rs, q, c->na, B, kmax, c->ktab);
+  k_recip_tables<<<nblk(nw, 128), 128, 0, s>>>(rs, q, c->na, B, kmax, recip_lat(c), c->ktab);
   const int nchunk = (c->na + SK_CHUNK - 1) / SK_CHUNK;
   dim3 grid(nblk(c->ngrp, SK_T), nchunk, B);
   k_recip_sk<<<grid, SK_T, recip_sk_smem(kmax), s>>>(c->ktab, c->na, kmax, c->ngrp, c->kgrp, c->nkp, nchunk,
@@ -283,7 +296,7 @@ void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const d
   nseg = std::max(1, std::min(16, std::min(nseg, c->ncol)));
   dim3 grid(bx, nseg, B);
   k_recip_force<<<grid, F_T, recip_force_smem(kmax), s>>>(c->ktab, c->na, kmax, c->ncol, c->kcol, c->nkp,
-                                                          (const double4_32a *)c->sk, g);
+                                                          (const double4_32a *)c->sk, recip_lat(c), g);
 }
 
 // The dynamic shared-memory limit is a per-kernel property of the process, so

@@ -52,7 +52,7 @@ unsigned char *g_scratch_ptr[MAX_DEVICES] = {nullptr};
 // host-side k tables (fixed size: no heap allocation)
 KCol h_col[MAX_NKXY];
 int4 h_kp[MAX_NK], h_grp[MAX_NK];
-double h_kw[MAX_NK], h_kvir[9 * MAX_NK];
+double h_kw[MAX_NK], h_kvir[GB_KVIR * MAX_NK];
 
 const double PI = 3.141592653589793238462643383279502884;
 
@@ -119,7 +119,7 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   int4 *d_grp = (int4 *)take(sizeof(int4) * kt.ngrp);
   int4 *d_kp = (int4 *)take(sizeof(int4) * kt.nkp);
   double *d_kw = (double *)take(sizeof(double) * kt.nkp);
-  double *d_kvir = (double *)take(sizeof(double) * 9 * kt.nkp);
+  double *d_kvir = (double *)take(sizeof(double) * GB_KVIR * kt.nkp);
   double2 *d_tab = (double2 *)take(sizeof(double2) * 3 * (size_t)(P.kmax + 1) * n * B);
   double *d_skp = (double *)take(sizeof(double) * 4 * (size_t)kt.nkp * nchunk * B);
   double *d_sk = (double *)take(sizeof(double) * 8 * (size_t)kt.nkp * B);
@@ -135,7 +135,7 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   SCK(cudaMemcpyAsync(d_kp, h_kp, sizeof(int4) * kt.nkp, cudaMemcpyHostToDevice, s));
   SCK(cudaMemcpyAsync(d_kw, h_kw, sizeof(double) * kt.nkp, cudaMemcpyHostToDevice, s));
   gb_kvir_table(h_kp, kt.nkp, P.walpha, h_kvir);
-  SCK(cudaMemcpyAsync(d_kvir, h_kvir, sizeof(double) * 9 * kt.nkp, cudaMemcpyHostToDevice, s));
+  SCK(cudaMemcpyAsync(d_kvir, h_kvir, sizeof(double) * GB_KVIR * kt.nkp, cudaMemcpyHostToDevice, s));
   // cleared every call: gradient accumulator, energy/virial sums, status word
   SCK(cudaMemsetAsync(d_g, 0, sizeof(double) * N, s));
   SCK(cudaMemsetAsync(d_acc, 0, sizeof(double) * ACC_STRIDE, s));
@@ -180,7 +180,7 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   pl.idx = d_idx;
   launch_frac32(s, g, B, d_frac);
   launch_build_list(s, g, B, d_frac, pl, d_status);
-  launch_ewald_real(s, d_rs, d_z, n, B, pl, P.walpha, d_g, d_acc);
+  launch_ewald_real(s, d_rs, d_z, n, B, pl, P.walpha, nullptr, d_g, d_acc);
   launch_recip_sk(s, &view, d_rs, d_z, B);
   launch_recip_weights(s, &view, B, d_acc);
   launch_recip_force(s, &view, d_rs, d_z, B, d_g);

@@ -93,9 +93,12 @@ int build_kvectors(gb_context *c) {
   std::vector<int4> kp(cap_kp), grp(cap_kp);
   std::vector<double> kw(cap_kp);
   KTables t;
-  if (gb_build_ktables(c->P, recip_group_len(), col.data(), cap_col, kp.data(), kw.data(), cap_kp, grp.data(),
-                       cap_kp, &t))
-    return ctx_set_error(GB_E_ARG, "k-vector table capacity exceeded");
+  const bool cub = c->P.iamcub != 0;
+  const int bad = cub ? gb_build_ktables(c->P, recip_group_len(), col.data(), cap_col, kp.data(), kw.data(), cap_kp,
+                                         grp.data(), cap_kp, &t)
+                      : gb_build_ktables_nc(c->P, c->box, recip_group_len(), col.data(), cap_col, kp.data(), kw.data(),
+                                            cap_kp, grp.data(), cap_kp, &t);
+  if (bad) return ctx_set_error(GB_E_ARG, "k-vector table capacity exceeded");
   for (void *p : {(void *)c->kcol, (void *)c->kgrp, (void *)c->kpair, (void *)c->kw, (void *)c->kvir,
                   (void *)c->ktab, (void *)c->sk_part, (void *)c->sk})
     if (p) cudaFree(p);
@@ -116,9 +119,10 @@ int build_kvectors(gb_context *c) {
   CK(cudaMalloc(&c->kgrp, sizeof(int4) * std::max(t.ngrp, 1)));
   CK(cudaMalloc(&c->kpair, sizeof(int4) * std::max(t.nkp, 1)));
   CK(cudaMalloc(&c->kw, sizeof(double) * std::max(t.nkp, 1)));
-  CK(cudaMalloc(&c->kvir, sizeof(double) * 9 * std::max(t.nkp, 1)));
-  std::vector<double> kvir(9 * (size_t)std::max(t.nkp, 1));
-  gb_kvir_table(kp.data(), t.nkp, c->P.walpha, kvir.data());
+  CK(cudaMalloc(&c->kvir, sizeof(double) * GB_KVIR * std::max(t.nkp, 1)));
+  std::vector<double> kvir(GB_KVIR * (size_t)std::max(t.nkp, 1));
+  if (cub) gb_kvir_table(kp.data(), t.nkp, c->P.walpha, kvir.data());
+  else gb_kvir_table_nc(kp.data(), t.nkp, c->P.walpha, c->box, kvir.data());
   CK(cudaMalloc(&c->ktab, c->ktab_bytes));
   CK(cudaMalloc(&c->sk_part, c->sk_part_bytes));
   CK(cudaMalloc(&c->sk, c->sk_bytes));
@@ -129,12 +133,14 @@ int build_kvectors(gb_context *c) {
   CK(cudaMemcpyAsync(c->kgrp, grp.data(), sizeof(int4) * t.ngrp, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->kpair, kp.data(), sizeof(int4) * t.nkp, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->kw, kw.data(), sizeof(double) * t.nkp, cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemcpyAsync(c->kvir, kvir.data(), sizeof(double) * 9 * t.nkp, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->kvir, kvir.data(), sizeof(double) * GB_KVIR * t.nkp, cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   recip_set_attributes();
   c->kmax_alloc = kmax;
   c->k_rkmax = c->P.rkmax;
   c->k_walpha = c->P.walpha;
+  c->k_iamcub = c->P.iamcub;
+  for (int d = 0; d < 3; ++d) c->k_box[d] = c->box[d];
   return GB_OK;
 }
 
@@ -267,13 +273,20 @@ double boxmax(const gb_context *c) { return std::max(c->box[0], std::max(c->box[
 
 // ---- one force term on B configurations ----
 
+// Ewald sum of B configurations (potenl_opt's M-site substitution and chain
+// rule, md_forces.f90:186-213).  Cubic boxes (ewald_cubic.f90:1-76): positions
+// scaled to the unit box, energy and gradient scaled back by 1/L and 1/L^2.
+// Non-cubic boxes (ewald_nc, ewald_noncubic.f90:1-54): positions, cut-off and
+// k vectors in bohr, no scaling; the same pair, structure-factor, weight and
+// force kernels run with per-axis factors.
 int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, int accumulate, int s) {
-  if (!c->P.iamcub) return ctx_set_error(GB_E_UNSUPPORTED, "non-cubic Ewald (ewald_nc) is not on the device path");
   if (c->P.wm > 0.0 || c->P.wh > 0.0) return ctx_set_error(GB_E_UNSUPPORTED, "smeared-charge Ewald is not on the device path");
   const int na = c->na;
+  const bool cub = c->P.iamcub != 0;
   const double L = c->box[0], onboxl = 1.0 / L;
+  const double pscale = cub ? onboxl : 1.0, gscale = cub ? onboxl * onboxl : 1.0;
   prof_begin(c, PR_MSITE);
-  launch_msite(c->stream, r, c->rs, na, B, c->P.alpha, onboxl);
+  launch_msite(c->stream, r, c->rs, na, B, c->P.alpha, pscale);
   CK(cudaMemsetAsync(c->g, 0, sizeof(double) * 3 * (size_t)na * B, c->stream));
   prof_end(c, PR_MSITE, (double)na * B);
   PairGeom g{};
@@ -281,9 +294,11 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   g.cstride = 3LL * na;
   g.pstride = 3;
   g.npt = na;
-  g.unit = 1;
-  g.box[0] = g.box[1] = g.box[2] = 1.0;
-  g.onbox[0] = g.onbox[1] = g.onbox[2] = 1.0;
+  g.unit = cub ? 1 : 0;
+  for (int d = 0; d < 3; ++d) {
+    g.box[d] = cub ? 1.0 : c->box[d];
+    g.onbox[d] = cub ? 1.0 : 1.0 / c->box[d];
+  }
   g.rcutsq = c->P.wrcut * c->P.wrcut;
   g.excl_mol = 0;
   const bool mixed = c->P.precision == GB_PREC_MIXED;
@@ -291,7 +306,8 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   int nl = 0;
   prof_begin(c, PR_LIST);
   PairList *pl = nullptr;  // mixed: the skin list itself, cut-off tested in the FP32 kernel
-  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, 1.0, &nl, mixed ? c->lo32 : nullptr, mixed ? c->z : nullptr,
+  const double vol = cub ? 1.0 : c->box[0] * c->box[1] * c->box[2];
+  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, vol, &nl, mixed ? c->lo32 : nullptr, mixed ? c->z : nullptr,
                      mixed, &pl);
   if (st) return st;
   prof_end(c, PR_LIST, (double)na * B);
@@ -302,7 +318,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   if (mixed) {
     recip_set_attributes_mx();
     prof_begin(c, PR_EW_REAL);
-    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, c->g,
+    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box, c->g,
                          slot(c, s));
     prof_end(c, PR_EW_REAL, npairs);
     prof_begin(c, PR_RECIP_SK);
@@ -316,7 +332,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
     prof_end(c, PR_RECIP_F, ksites);
   } else {
     prof_begin(c, PR_EW_REAL);
-    launch_ewald_real(c->stream, c->rs, c->z, na, B, c->pl, c->P.walpha, c->g, slot(c, s));
+    launch_ewald_real(c->stream, c->rs, c->z, na, B, c->pl, c->P.walpha, cub ? nullptr : c->box, c->g, slot(c, s));
     prof_end(c, PR_EW_REAL, npairs);
     prof_begin(c, PR_RECIP_SK);
     launch_recip_sk(c->stream, c, c->rs, c->z, B);
@@ -329,7 +345,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
     prof_end(c, PR_RECIP_F, ksites);
   }
   prof_begin(c, PR_MSITE);
-  launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, onboxl * onboxl, sign, accumulate);
+  launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, gscale, sign, accumulate);
   prof_end(c, PR_MSITE, (double)na * B);
   c->launches += 7;
   return GB_OK;
@@ -530,7 +546,10 @@ int dev_prepare(gb_context *c, double dt, double beta) {
     if ((st = upload_tw(c, &c->tw_c2, c->P.nbdf2))) return st;
     c->tw_c2_n = c->P.nbdf2;
   }
-  if (c->kmax_alloc != c->P.kmax || c->k_rkmax != c->P.rkmax || c->k_walpha != c->P.walpha) {
+  // the non-cubic tables depend on the box as well (k vectors in bohr^-1)
+  const bool kbox = !c->P.iamcub && (c->k_box[0] != c->box[0] || c->k_box[1] != c->box[1] || c->k_box[2] != c->box[2]);
+  if (c->kmax_alloc != c->P.kmax || c->k_rkmax != c->P.rkmax || c->k_walpha != c->P.walpha ||
+      c->k_iamcub != c->P.iamcub || kbox) {
     if ((st = build_kvectors(c))) return st;
   }
   if (dt > 0.0 && (dt != c->monod_dt || beta != c->monod_beta || c->P.mts != c->monod_mts ||
@@ -859,10 +878,11 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
   const EnergyPlan &pl = c->plan;
   double vew = 0.0, vlj = 0.0, vint = 0.0;
   double vir_ew[9] = {0}, vir_lj[9] = {0}, vir_int[9] = {0};
+  const double Le = c->P.iamcub ? L : 1.0;  // the cubic sum runs in the unit box
   auto add_ewald = [&](int s, int B) {
     if (!B) return;
-    vew += (S(s)[0] - B * vself) / L / B;
-    for (int i = 0; i < 9; ++i) vir_ew[i] += S(s)[1 + i] / L / B;
+    vew += (S(s)[0] - B * vself) / Le / B;
+    for (int i = 0; i < 9; ++i) vir_ew[i] += S(s)[1 + i] / Le / B;
   };
   auto add_tem = [&](int s, int B, double sign) {
     if (!B) return;

@@ -2,9 +2,8 @@
 
 Each system is a q-SPC/Fw water box on the reference's CUB lattice at
 0.997 g/cm^3 (main.f90 set-up through `system.water_box`), with momenta drawn
-from the reference's ran2/gaussian stream seeded per system.  Only cubic
-lattices are used: the device Ewald sum is the cubic one, so molecule counts
-that need an anisotropic lattice (128 = 8 x 4 x 4) are left out.
+from the reference's ran2/gaussian stream seeded per system.  128 molecules
+sit on the 8 x 4 x 4 lattice of a non-cubic box (the non-cubic Ewald sum).
 """
 import ctypes as C
 import os
@@ -18,12 +17,14 @@ PARAM_QSPCFW = os.path.join(os.path.dirname(HERE), "tests", "golden", "params", 
 # rigid 4-site TIP4P/2005 water (O-H 0.9572 A, HOH 104.52 deg, M-site 0.1546 A, qH 0.5897 e)
 PARAM_TIP05 = os.path.join(os.path.dirname(HERE), "tests", "golden", "params", "param_tip05_rigid")
 
-CUBIC_CELLS = {64: 4, 216: 6, 343: 7, 512: 8, 729: 9, 1000: 10, 1331: 11, 1728: 12}
+# CUB lattice cells per molecule count; 128 molecules need the anisotropic
+# 8 x 4 x 4 lattice (a non-cubic box, ewald_nc)
+CELLS = {64: (4, 4, 4), 128: (8, 4, 4), 216: (6, 6, 6), 343: (7, 7, 7), 512: (8, 8, 8), 729: (9, 9, 9),
+         1000: (10, 10, 10), 1331: (11, 11, 11), 1728: (12, 12, 12)}
 
 
 def _box(nm, nb, temp, precision, seed, dtfs=0.5, mts=1, param=PARAM_QSPCFW):
-    n = CUBIC_CELLS[nm]
-    s = system.water_box(param, ncell=(n, n, n), nb=nb, temp=temp, dtfs=dtfs, mts=mts, precision=precision)
+    s = system.water_box(param, ncell=CELLS[nm], nb=nb, temp=temp, dtfs=dtfs, mts=mts, precision=precision)
     irun = C.c_int(-(1 + seed))
     s["p"] = system.sample_momenta(s["na"], s["nb"], s["mass"], s["beta"], irun)
     s["seed"] = seed
@@ -31,7 +32,7 @@ def _box(nm, nb, temp, precision, seed, dtfs=0.5, mts=1, param=PARAM_QSPCFW):
     return s
 
 
-def replica_set(n=256, seed=2026, precision=1, sizes=(64, 216, 343, 512), beads=(8, 16, 32, 64),
+def replica_set(n=256, seed=2026, precision=1, sizes=(64, 128, 216, 343, 512), beads=(8, 16, 32, 64),
                 temps=(250.0, 350.0)):
     """n independent NVT replicas: molecule count, bead count and temperature
     drawn uniformly per replica from a seeded generator."""
