@@ -119,7 +119,7 @@ def test_noncubic_replica_in_batch(precision):
     want = alone.download()
     alone.close()
     c = fresh()
-    other = setup(param="param_qspcfw", ncell=(4, 4, 4), nb=4, precision=precision)  # a cubic neighbour
+    other = systems.build(param="param_qspcfw", ncell=(4, 4, 4), nb=4, precision=precision)  # a cubic neighbour
     o = lib.Context(other["na"], other["nb"], other["mass"], other["z"])
     o.set_params(other["params"])
     o.upload(r=other["r"], box=other["box"])
