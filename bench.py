@@ -374,6 +374,16 @@ def run_replicas(args, torch):
     for i, (s, ctx) in enumerate(zip(reps, ctxs)):
         batch.add(ctx, s["dt"], s["beta"], 0.01, -(5000 + i))
     stream = torch.cuda.ExternalStream(batch.stream)
+    # launch shapes per distinct replica shape (gbrpmd_batch_autotune), before the timed steps
+    t_tune = time.perf_counter()
+    lib.autotune_reset()
+    batch.autotune(steps=5)
+    t_tune = time.perf_counter() - t_tune
+    shapes = {}
+    for s, ctx in zip(reps, ctxs):
+        ch = ctx.autotune(s["dt"], s["beta"], steps=5)  # cached: returns the choice
+        key = f"nm{s['nm']}_nb{s['nb']}"
+        shapes[key] = f"ew_np={ch['ew_np']} lj_np={ch['lj_np']} mts_mpb={ch['mts_mpb']} skin={ch['skin']}"
     batch.step(args.warmup)
     batch.sync()
     step_ms = []
@@ -432,6 +442,7 @@ def run_replicas(args, torch):
                    "sizes": "nm in {64,128 (8x4x4 non-cubic box),216,343,512}, nb in {8,16,32,64}, T in [250,350] K",
                    "l2": "inputs larger than L2 in aggregate", "parallelism": "one batch, one graph per step"},
         "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
+        "autotune": {"seconds": t_tune, "distinct_shapes": len(shapes), "choices": shapes},
         "fp64_loop": {"value": fp64_value, "ms_per_step": float(np.mean(loop_ms))},
         "batched_mixed_over_fp64_loop": value / fp64_value,
         "error_vs_fp64": {"force_rel_rms_max_of_8": max(errs), "bound": 1e-5,

@@ -238,6 +238,19 @@ int gbrpmd_ctx_sync(gb_context *ctx);
 /* energies and virials of the last step: out[0..4] = v, vew, vlj, vint, tv;
    vir[9], vir_lf[9] column-major */
 int gbrpmd_ctx_energies(gb_context *ctx, double *out5, double *vir, double *vir_lf);
+/* Autotuner (no counterpart in the reference): times `steps` evolve_pi steps
+   of (dt, beta) on this context per candidate launch shape -- lanes per site
+   of the FP32 real-space Ewald kernel, lanes per oxygen of the FP32 LJ kernel,
+   molecules per block of the fused MTS kernel, pair-list skin -- one
+   parameter at a time, keeps the fastest, and leaves the trajectory state as
+   it found it.  Shapes are cached per (atoms, beads, precision, MTS,
+   contraction, box kind, model) for the process.  Results change only by the
+   order of floating-point sums.  out4 (optional): the chosen lanes (Ewald),
+   lanes (LJ), molecules per MTS block (0: one wave over the SMs), skin.
+   Rigid, barostat and PRG/PRL contexts keep the defaults. */
+int gbrpmd_ctx_autotune(gb_context *ctx, double dt, double beta, int steps, double *out4);
+/* forgets the cached shapes */
+void gbrpmd_autotune_reset(void);
 /* Random stream owned by the context (no counterpart in the reference, whose
    stream is process-wide): the PRG / PRL thermostat kicks of
    gbrpmd_ctx_evolve draw from a fresh ran2 / gaussian state seeded with idum
@@ -318,6 +331,8 @@ int gbrpmd_batch_remove(gb_batch *batch, gb_context *ctx);
 int gbrpmd_batch_size(gb_batch *batch);
 int gbrpmd_batch_step(gb_batch *batch, int nsteps);
 int gbrpmd_batch_sync(gb_batch *batch);
+/* gbrpmd_ctx_autotune on every replica (each distinct shape timed once) */
+int gbrpmd_batch_autotune(gb_batch *batch, int steps);
 void *gbrpmd_batch_stream(gb_batch *batch);
 
 /* Device memory: what a context holds now, and what one of (na, nb) with

@@ -223,6 +223,21 @@ int gbrpmd_batch_step(gb_batch *b, int nsteps) {
   return GB_OK;
 }
 
+int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double *out4);  // tune.cpp
+
+// launch shapes of every replica (gbrpmd_ctx_autotune; shapes seen before
+// come from the process-wide cache), then a fresh capture at the next step
+int gbrpmd_batch_autotune(gb_batch *b, int steps) {
+  if (!b) return ctx_set_error(GB_E_ARG, "null batch");
+  BCK(cudaStreamSynchronize(b->s0));
+  for (auto &r : b->reps) {
+    int st = gbrpmd_ctx_autotune(r.c, r.dt, r.beta, steps, nullptr);
+    if (st) return st;
+  }
+  drop_graph(b);
+  return GB_OK;
+}
+
 int gbrpmd_batch_sync(gb_batch *b) {
   if (!b) return ctx_set_error(GB_E_ARG, "null batch");
   BCK(cudaStreamSynchronize(b->s0));

@@ -144,6 +144,14 @@ struct gb_context {
     EnergyPlan plan;
   } graph;
   int use_graphs = 1;        // GBRPMD_GRAPHS=0 turns replay off
+  // launch shapes chosen by gbrpmd_ctx_autotune (tune.cpp); results depend on
+  // them only through the order of floating-point sums
+  struct Tune {
+    int ew_np = 16;   // lanes per site, FP32 real-space Ewald (8, 16, 32)
+    int lj_np = 4;    // lanes per oxygen, FP32 LJ (2, 4, 8)
+    int mts_mpb = 0;  // molecules per block of the MTS kernel (0: one wave over the SMs)
+    int done = 0;
+  } tune;
 
   // optional per-region CUDA-event timing (gbrpmd_ctx_set_profiling)
   int prof = 0;

@@ -65,11 +65,12 @@ void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const d
                         double *g);
 // ---- mixed precision (k_mixed.cu): FP32 arithmetic, full lists, hi/lo positions ----
 // hi.w carries the site charge (launch_frac32 with q)
-// box: side lengths of the fractional coordinates (1, 1, 1 for the cubic sum)
+// box: side lengths of the fractional coordinates (1, 1, 1 for the cubic sum);
+// np: lanes per site (8, 16, 32) / per oxygen (2, 4, 8)
 void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double rcutsq, const double *box, double *g, double *acc);
+                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc);
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                  double sigsq, double rcutsq, const double *box, double dscale, double *out, double *acc);
+                  double sigsq, double rcutsq, const double *box, double dscale, int np, double *out, double *acc);
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);
 void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc);
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g);

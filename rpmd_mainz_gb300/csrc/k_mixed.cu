@@ -14,14 +14,17 @@
 //  * the reciprocal-space power tables come from the FP64 recurrence rounded
 //    to FP32; structure-factor partials are FP32 over 32 sites and FP64 over
 //    chunks; energy, virial and the k-space totals stay FP64.
+#include <type_traits>
+
 #include "gb_common.cuh"
 #include "gb_kernels.h"
 
 namespace {
 
 constexpr int MX_T = 64;     // threads per block of the pair kernels
-constexpr int MX_NP = 16;    // lanes per site in the real-space kernel
-constexpr int MX_LJ_NP = 4;  // lanes per oxygen in the LJ kernel
+// lanes per site (real-space Ewald: 8, 16 or 32, default 16) and per oxygen
+// (LJ: 2, 4 or 8, default 4) are template parameters; the launchers take them
+// from the context's tuning (gbrpmd_ctx_autotune)
 
 GB_D void kadd(float &s, float &c, float v) {  // Kahan-compensated s += v
   const float y = v - c;
@@ -108,6 +111,7 @@ GB_D void block_sum_sym7_mx(double (&vals)[7], double *sh, double *acc) {
 // bx: side lengths that turn fractional differences into distances (1 in the
 // unit box of the cubic sum; the box in bohr for the non-cubic one,
 // rwald_basic / rwald_cell of ewald_noncubic.f90)
+template <int NP>
 __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                                                         int na, const int *__restrict__ count,
                                                         const int *__restrict__ idx, int cap, float alpha,
@@ -118,7 +122,7 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
   const float sfac = (float)(-2.0 / sqrt(acos(-1.0))) * alpha;
   const int c = blockIdx.y;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = (int)(tid / MX_NP), sub = (int)(tid % MX_NP);
+  const int i = (int)(tid / NP), sub = (int)(tid % NP);
   const bool active = i < na;
   const float4 *H = hi + (long long)c * na, *Lo = lo + (long long)c * na;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
@@ -158,8 +162,8 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
       vzz += dz * fz;
     };
     int t = sub;
-    for (; t + 3 * MX_NP < n; t += 4 * MX_NP) {
-      const int j0 = L[t], j1 = L[t + MX_NP], j2 = L[t + 2 * MX_NP], j3 = L[t + 3 * MX_NP];
+    for (; t + 3 * NP < n; t += 4 * NP) {
+      const int j0 = L[t], j1 = L[t + NP], j2 = L[t + 2 * NP], j3 = L[t + 3 * NP];
       const float4 h0 = H[j0], h1 = H[j1], h2 = H[j2], h3 = H[j3];
       const float4 l0 = Lo[j0], l1 = Lo[j1], l2 = Lo[j2], l3 = Lo[j3];
       pair(j0, h0, l0);
@@ -167,15 +171,15 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
       pair(j2, h2, l2);
       pair(j3, h3, l3);
     }
-    for (; t < n; t += MX_NP) {
+    for (; t < n; t += NP) {
       const int j = L[t];
       pair(j, H[j], Lo[j]);
     }
   }
   // each lane's compensated sum, then FP32 across the site's lanes
-  const float fx = group_sum_f<MX_NP>(sx - cx);
-  const float fy = group_sum_f<MX_NP>(sy - cy);
-  const float fz = group_sum_f<MX_NP>(sz - cz);
+  const float fx = group_sum_f<NP>(sx - cx);
+  const float fy = group_sum_f<NP>(sy - cy);
+  const float fz = group_sum_f<NP>(sz - cz);
   if (active && sub == 0) {
     double *G = g + ((long long)c * na + i) * 3;
     G[0] += (double)fx;
@@ -190,6 +194,7 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
 
 // lj_list / lj_basic (ljones.f90) in FP32 over a full oxygen list; bead pairs
 // beyond rcut are skipped as in the reference; out += dscale * gradient
+template <int NP>
 __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo, int na,
                                                 int npt, int nconf_list, const int *__restrict__ count,
                                                 const int *__restrict__ idx, int cap, float sigsq, float rcutsq,
@@ -197,7 +202,7 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
   __shared__ double sh[32 * 10];
   const int c = blockIdx.y;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int o = (int)(tid / MX_LJ_NP), sub = (int)(tid % MX_LJ_NP);
+  const int o = (int)(tid / NP), sub = (int)(tid % NP);
   const bool active = o < npt;
   const float4 *H = hi + (long long)c * npt, *Lo = lo + (long long)c * npt;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
@@ -229,8 +234,8 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
       }
     };
     int t = sub;
-    for (; t + 3 * MX_LJ_NP < n; t += 4 * MX_LJ_NP) {
-      const int j0 = L[t], j1 = L[t + MX_LJ_NP], j2 = L[t + 2 * MX_LJ_NP], j3 = L[t + 3 * MX_LJ_NP];
+    for (; t + 3 * NP < n; t += 4 * NP) {
+      const int j0 = L[t], j1 = L[t + NP], j2 = L[t + 2 * NP], j3 = L[t + 3 * NP];
       const float4 h0 = H[j0], h1 = H[j1], h2 = H[j2], h3 = H[j3];
       const float4 l0 = Lo[j0], l1 = Lo[j1], l2 = Lo[j2], l3 = Lo[j3];
       pair(h0, l0);
@@ -238,14 +243,14 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
       pair(h2, l2);
       pair(h3, l3);
     }
-    for (; t < n; t += MX_LJ_NP) {
+    for (; t < n; t += NP) {
       const int j = L[t];
       pair(H[j], Lo[j]);
     }
   }
-  const float fx = group_sum_f<MX_LJ_NP>(sx - cx);
-  const float fy = group_sum_f<MX_LJ_NP>(sy - cy);
-  const float fz = group_sum_f<MX_LJ_NP>(sz - cz);
+  const float fx = group_sum_f<NP>(sx - cx);
+  const float fy = group_sum_f<NP>(sy - cy);
+  const float fz = group_sum_f<NP>(sz - cz);
   if (active && sub == 0) {
     double *F = out + (long long)c * na * 3 + 9LL * o;
     F[0] += dscale * (double)fx;
@@ -508,20 +513,32 @@ int sm_count_mx() {
 }  // namespace
 
 void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double rcutsq, const double *box, double *g, double *acc) {
-  dim3 grid(nblk((long long)na * MX_NP, MX_T), B);
+                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc) {
   const float3 bx = make_float3((float)box[0], (float)box[1], (float)box[2]);
-  k_ewald_real_mx<<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, (float)rcutsq, bx, g,
-                                        acc);
+  auto go = [&](auto NPc) {
+    constexpr int NP = decltype(NPc)::value;
+    dim3 grid(nblk((long long)na * NP, MX_T), B);
+    k_ewald_real_mx<NP><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, (float)rcutsq, bx,
+                                              g, acc);
+  };
+  if (np == 8) go(std::integral_constant<int, 8>());
+  else if (np == 32) go(std::integral_constant<int, 32>());
+  else go(std::integral_constant<int, 16>());
 }
 
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                  double sigsq, double rcutsq, const double *box, double dscale, double *out, double *acc) {
+                  double sigsq, double rcutsq, const double *box, double dscale, int np, double *out, double *acc) {
   const int npt = na / 3;
-  dim3 grid(nblk((long long)npt * MX_LJ_NP, MX_T), B);
   const float3 bx = make_float3((float)box[0], (float)box[1], (float)box[2]);
-  k_lj_mx<<<grid, MX_T, 0, s>>>(hi, lo, na, npt, pl.nconf, pl.count, pl.idx, pl.cap, (float)sigsq, (float)rcutsq,
-                                bx, dscale, out, acc);
+  auto go = [&](auto NPc) {
+    constexpr int NP = decltype(NPc)::value;
+    dim3 grid(nblk((long long)npt * NP, MX_T), B);
+    k_lj_mx<NP><<<grid, MX_T, 0, s>>>(hi, lo, na, npt, pl.nconf, pl.count, pl.idx, pl.cap, (float)sigsq,
+                                      (float)rcutsq, bx, dscale, out, acc);
+  };
+  if (np == 2) go(std::integral_constant<int, 2>());
+  else if (np == 8) go(std::integral_constant<int, 8>());
+  else go(std::integral_constant<int, 4>());
 }
 
 size_t recip_sk_smem_mx(int kmax) { return sizeof(float2) * MSK_CHUNK * 3 * (kmax + 1); }

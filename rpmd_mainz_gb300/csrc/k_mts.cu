@@ -460,8 +460,10 @@ void launch_nb(cudaStream_t s, MtsArgs a, bool mixed) {
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  // one wave of blocks over the SMs when the molecules fit, else MPB_MAX per block
-  a.mpb = std::max(1, std::min(C::MPB_MAX, (a.nm + nsm - 1) / std::max(nsm, 1)));
+  // one wave of blocks over the SMs when the molecules fit, else MPB_MAX per
+  // block; a tuned count (gbrpmd_ctx_autotune) overrides it
+  a.mpb = a.mpb > 0 ? std::min(C::MPB_MAX, a.mpb)
+                    : std::max(1, std::min(C::MPB_MAX, (a.nm + nsm - 1) / std::max(nsm, 1)));
   const int T = (9 * a.mpb + 31) / 32 * 32;
   const unsigned grid = (unsigned)((a.nm + a.mpb - 1) / a.mpb);
   if (mixed) k_mts_mixed<NB><<<grid, T, mts_smem_mixed<NB>(T), s>>>(a);
@@ -481,6 +483,7 @@ void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used) {
   const int nb = c->nb;
   if (nb != 2 && nb != 4 && nb != 8 && nb != 16 && nb != 32 && nb != 64) return;
   MtsArgs a;
+  a.mpb = c->tune.mts_mpb;  // 0: chosen in launch_nb
   a.p = c->p;
   a.r = c->r;
   a.rnm = c->rnm;

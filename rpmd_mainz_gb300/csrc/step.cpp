@@ -318,7 +318,8 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   if (mixed) {
     recip_set_attributes_mx();
     prof_begin(c, PR_EW_REAL);
-    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box, c->g,
+    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
+                         c->tune.ew_np, c->g,
                          slot(c, s));
     prof_end(c, PR_EW_REAL, npairs);
     prof_begin(c, PR_RECIP_SK);
@@ -400,7 +401,7 @@ int term_lj(gb_context *c, const double *r, int B, double *out, int accumulate, 
     go.cstride = 3LL * na;
     launch_frac32(c->stream, go, B, c->hi32, c->olo32);
     launch_lj_mx(c->stream, c->hi32, c->olo32, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut,
-                 c->box, 48.0 * c->P.oo_eps, out, slot(c, s));
+                 c->box, 48.0 * c->P.oo_eps, c->tune.lj_np, out, slot(c, s));
     c->launches += 1;
   } else {
     launch_lj(c->stream, r, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut, c->box,

@@ -72,6 +72,9 @@ def load(path=None):
     lib.gbrpmd_ctx_set_nbaro.argtypes = [C.c_void_p, C.c_int]
     lib.gbrpmd_ctx_box.argtypes = [C.c_void_p, D]
     lib.gbrpmd_rng_reset.restype = None
+    lib.gbrpmd_ctx_autotune.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int, D]
+    lib.gbrpmd_autotune_reset.restype = None
+    lib.gbrpmd_batch_autotune.argtypes = [C.c_void_p, C.c_int]
     lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
     lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
     lib.gbrpmd_ctx_set_graphs.argtypes = [C.c_void_p, C.c_int]
@@ -128,6 +131,11 @@ def get_params() -> GbParams:
     p = GbParams()
     _check(load().gbrpmd_get_params(C.byref(p)))
     return p
+
+
+def autotune_reset():
+    """Forget the autotuner's cached shapes."""
+    load().gbrpmd_autotune_reset()
 
 
 def rng_reset():
@@ -282,6 +290,12 @@ class Context:
         return dict(v=out[0], vew=out[1], vlj=out[2], vint=out[3], tv=out[4], vir=vir.reshape(3, 3, order="F"),
                     vir_lf=vir_lf.reshape(3, 3, order="F"))
 
+    def autotune(self, dt, beta, steps=10):
+        """Launch shapes timed on this context (gbrpmd_ctx_autotune); returns the choice."""
+        out = np.zeros(4)
+        _check(load().gbrpmd_ctx_autotune(self.h, C.c_double(dt), C.c_double(beta), int(steps), _ptr(out)))
+        return dict(ew_np=int(out[0]), lj_np=int(out[1]), mts_mpb=int(out[2]), skin=float(out[3]))
+
     def set_rng(self, idum):
         """Context-owned random stream for the PRG / PRL kicks of evolve()."""
         _check(load().gbrpmd_ctx_set_rng(self.h, int(idum)))
@@ -381,6 +395,10 @@ class Batch:
     def remove(self, ctx):
         _check(load().gbrpmd_batch_remove(self.h, ctx.h))
         self.members.remove(ctx)
+
+    def autotune(self, steps=10):
+        """gbrpmd_batch_autotune: launch shapes of every replica (cached per shape)."""
+        _check(load().gbrpmd_batch_autotune(self.h, int(steps)))
 
     def step(self, nsteps=1):
         _check(load().gbrpmd_batch_step(self.h, nsteps))
