@@ -403,8 +403,10 @@ def run_replicas(args, torch):
     batch.close()
     for c in ctxs:
         c.close()
-    # plain-FP64 loop over the same replicas
+    # plain-FP64 loop over the same replicas, tuned the same way
     ctxs = contexts(0)
+    for c, s in zip(ctxs, reps):
+        c.autotune(s["dt"], s["beta"], steps=3)
     for c, s in zip(ctxs, reps):
         c.evolve(args.warmup, s["dt"], s["beta"])
     for c in ctxs:
