@@ -250,6 +250,10 @@ def measure(args, s, prec, torch, world, local):
     stream = torch.cuda.ExternalStream(ctx.stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
+    # launch shapes for this system (gbrpmd_ctx_autotune), outside the timed region
+    t_tune = time.perf_counter()
+    tune = ctx.autotune(s["dt"], s["beta"], steps=5) if not args.no_autotune else None
+    t_tune = time.perf_counter() - t_tune
     for _ in range(args.warmup):
         ctx.evolve(1, s["dt"], s["beta"])
     ctx.sync()
@@ -321,7 +325,8 @@ def measure(args, s, prec, torch, world, local):
     ctx.close()
     del flush
     return dict(value=value, total_ms=total_ms, step_ms=step_ms, launches=launches, rebuilds=rebuilds,
-                energies=energies, regions=regions, clocks=clk.summary(), e2e_value=e2e_value, e2e_bytes=nbytes)
+                energies=energies, regions=regions, clocks=clk.summary(), e2e_value=e2e_value, e2e_bytes=nbytes,
+                tune=tune, tune_s=t_tune)
 
 
 def force_error(s):
@@ -647,6 +652,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true", help="skip the plain-FP64 comparison arm")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of tuned ones")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -677,7 +683,7 @@ def main():
     fp64 = None
     if prec == 1 and not args.no_fp64_arm:
         f = measure(args, s, 0, torch, world, local)
-        fp64 = {"value": f["value"], "ms_per_step": f["total_ms"] / args.steps,
+        fp64 = {"value": f["value"], "ms_per_step": f["total_ms"] / args.steps, "autotune": f["tune"],
                 "p50_ms": float(np.median(f["step_ms"])), "p99_ms": float(np.percentile(f["step_ms"], 99)),
                 "regions_ms_one_step": {k: v["ms"] for k, v in f["regions"].items()}}
     err = force_error(s) if prec == 1 else None
@@ -700,6 +706,8 @@ def main():
                 "d2h_bytes_per_step": int(m["e2e_bytes"] + 8 * 22),
                 "path": "gbrpmd_evolve_pi drop-in, pinned host p/r/dvdr/dvdr2"},
         "energies_last_step": {k: m["energies"][k] for k in ("v", "vew", "vlj", "vint")},
+        "autotune": {"choice": m["tune"], "seconds": m["tune_s"],
+                     "note": "gbrpmd_ctx_autotune before the warm-up; the drop-in e2e context takes the cached shape"},
         "regions_ms_one_step": regions,
     }
     if fp64 is not None:

@@ -279,6 +279,7 @@ int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj, 
   std::memcpy(c->box, boxlxyz, sizeof(double) * 3);
   std::memcpy(c->vir_lf_in, vir_lf, sizeof(double) * 9);  // the barostat reads the previous call's vir_lf
   c->nbaro = *nbaro;
+  tune_apply_cached(c);  // launch shapes of an autotuned context of the same shape
   c->th_rng = &g_rng;  // thermostat kicks draw the process-wide stream with the caller's irun
   c->th_idum = irun;
   if ((st = upload(c, c->p, p, N)) || (st = upload(c, c->r, r, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||

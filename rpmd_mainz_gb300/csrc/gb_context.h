@@ -194,6 +194,8 @@ int ctx_check_cuda(cudaError_t e, const char *what);
 int dev_prepare(gb_context *c, double dt, double beta);  // twiddles, monodromy, k lists
 int dev_full_forces(gb_context *c);                      // dvdr, dvdr2 from r
 int dev_evolve_pi(gb_context *c, double dt, double beta);
+// applies a shape the autotuner cached for c's key, if any (tune.cpp)
+void tune_apply_cached(gb_context *c);
 // a PRG / PRL thermostat kick on the bead momenta (no-op for other thermostats)
 int therm_kick(gb_context *c, double dtk, double beta);
 // evolve_rig_pi (k_rattle.cu); vir_inout unused on the device

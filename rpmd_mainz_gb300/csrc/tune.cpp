@@ -116,6 +116,15 @@ int trial(gb_context *c, const Saved &S, const Shape &shape, double dt, double b
 
 }  // namespace
 
+// the cached shape of c's key, if one was tuned (drop-in contexts take it)
+void tune_apply_cached(gb_context *c) {
+  if (c->tune.done || g_cache.empty()) return;
+  auto it = g_cache.find(key_of(c));
+  if (it == g_cache.end()) return;
+  apply(c, it->second);
+  c->tune.done = 1;
+}
+
 extern "C" {
 
 // Chooses the launch shapes of `ctx` for steps of (dt, beta) by timing
