@@ -103,6 +103,24 @@ typedef struct gb_params {
   int32_t baro;        /* GB_BARO_*: module barostat's `baro` */
 } gb_params;
 
+/* ---- on-disk formats (io.f90), host only ------------------------------------ */
+
+/* print_structure (io.f90:1-17): "nm na nb", box, r(:,:,:); append != 0 appends */
+int gbrpmd_write_structure(const char *path, int append, const double *r, const double *box, int nm, int na,
+                           int nb);
+/* reads a print_structure restart file (list-directed: any layout); with r
+   NULL only nm, na, nb and box, so that r (3 na nb doubles) can be sized */
+int gbrpmd_read_structure(const char *path, int *nm, int *na, int *nb, double *box, double *r);
+/* one xyz frame of print_vmd_full / _forces / _vels (bead = 0: bead average)
+   or print_vmd_bead / _forces / _vels (bead = 1..nb), io.f90:310-770.
+   kind 0: positions a = r (Angstrom, oxygens moved into the box unless
+   reftraj != 0); 1: forces -(a + a2), a = dvdr, a2 = dvdr2; 2: velocities
+   a / mass, a = p.  isotope 0 H2O, 1 D2O, 2 HDO. */
+int gbrpmd_write_vmd(const char *path, int append, int kind, int bead, const double *a, const double *a2,
+                     const double *mass, const double *box, int na, int nb, int isotope, int reftraj);
+/* frame `frame` (0-based) of a print_vmd_* file: box and the atom lines' numbers as printed */
+int gbrpmd_read_vmd(const char *path, int frame, int na, double *box, double *xyz);
+
 /* ---- set-up --------------------------------------------------------------- */
 
 /* Stores the hidden inputs; call once after setup_ewald (main.f90:631) and

@@ -72,6 +72,11 @@ def load(path=None):
     lib.gbrpmd_ctx_set_nbaro.argtypes = [C.c_void_p, C.c_int]
     lib.gbrpmd_ctx_box.argtypes = [C.c_void_p, D]
     lib.gbrpmd_rng_reset.restype = None
+    lib.gbrpmd_write_structure.argtypes = [C.c_char_p, C.c_int, D, D, C.c_int, C.c_int, C.c_int]
+    lib.gbrpmd_read_structure.argtypes = [C.c_char_p, I, I, I, D, D]
+    lib.gbrpmd_write_vmd.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, D, D, D, D, C.c_int, C.c_int, C.c_int,
+                                     C.c_int]
+    lib.gbrpmd_read_vmd.argtypes = [C.c_char_p, C.c_int, C.c_int, D, D]
     lib.gbrpmd_ctx_autotune.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int, D]
     lib.gbrpmd_autotune_reset.restype = None
     lib.gbrpmd_batch_autotune.argtypes = [C.c_void_p, C.c_int]
@@ -131,6 +136,44 @@ def get_params() -> GbParams:
     p = GbParams()
     _check(load().gbrpmd_get_params(C.byref(p)))
     return p
+
+
+def write_structure(path, r, box, append=False):
+    """print_structure (io.f90:1-17) of r (nb, na, 3) and the box."""
+    r = _arr(r)
+    nb, na, _ = r.shape
+    _check(load().gbrpmd_write_structure(str(path).encode(), int(append), _ptr(r), _ptr(_arr(box)), na // 3, na, nb))
+
+
+def read_structure(path):
+    """A print_structure restart file: (r (nb, na, 3), box)."""
+    nm, na, nb = C.c_int(), C.c_int(), C.c_int()
+    box = np.zeros(3)
+    _check(load().gbrpmd_read_structure(str(path).encode(), C.byref(nm), C.byref(na), C.byref(nb), _ptr(box), None))
+    r = np.zeros((nb.value, na.value, 3))
+    _check(load().gbrpmd_read_structure(str(path).encode(), C.byref(nm), C.byref(na), C.byref(nb), _ptr(box),
+                                        _ptr(r)))
+    return r, box
+
+
+VMD_KIND = {"xyz": 0, "frc": 1, "vel": 2}
+
+
+def write_vmd(path, kind, a, box, a2=None, mass=None, bead=0, append=False, isotope=0, reftraj=False):
+    """One frame of print_vmd_full* (bead 0) or print_vmd_bead* (bead 1..nb);
+    kind "xyz" (a = r), "frc" (a = dvdr, a2 = dvdr2) or "vel" (a = p, with mass)."""
+    a = _arr(a)
+    nb, na, _ = a.shape
+    _check(load().gbrpmd_write_vmd(str(path).encode(), int(append), VMD_KIND[kind], int(bead), _ptr(a),
+                                   _ptr(None if a2 is None else _arr(a2)), _ptr(None if mass is None else _arr(mass)),
+                                   _ptr(_arr(box)), na, nb, int(isotope), int(reftraj)))
+
+
+def read_vmd(path, na, frame=0):
+    """Frame `frame` of a print_vmd_* file: (numbers (na, 3) as printed, box as printed)."""
+    box, xyz = np.zeros(3), np.zeros((na, 3))
+    _check(load().gbrpmd_read_vmd(str(path).encode(), int(frame), int(na), _ptr(box), _ptr(xyz)))
+    return xyz, box
 
 
 def autotune_reset():

@@ -18,6 +18,7 @@ Writes
                            1000 NPT equilibration steps) and the last lines of
                            E_eq.out, virial_ke_eq.out and V_eq.out (md_eq.f90:
                            274-277), printed at the same step
+  gentest_eq.xyz           eq.xyz itself, for the restart-file reader
   gentest_md_eq.npz        the md_eq series of the same run: E_pre_eq.out (the
                            100-step NVT pre-equilibration) and E_eq.out,
                            temp_eq.out, virial_ke_eq.out, V_eq.out,
@@ -79,6 +80,7 @@ def main(ref):
     data["frames"] = np.array(FRAMES)
     np.savez_compressed(os.path.join(HERE, "gentest_frames.npz"), **data)
 
+    shutil.copyfile(os.path.join(cmp_dir, "eq.xyz"), os.path.join(HERE, "gentest_eq.xyz"))  # restart file, as written
     with open(os.path.join(cmp_dir, "eq.xyz")) as f:
         tok = f.read().split()
     nm, na, nb = (int(t) for t in tok[:3])
