@@ -275,6 +275,19 @@ void gbrpmd_autotune_reset(void);
    (negative to initialise, as ran2 requires).  The drop-in entry points and
    gbrpmd_run_md_eq draw the process-wide stream with the caller's irun. */
 int gbrpmd_ctx_set_rng(gb_context *ctx, int idum);
+/* Source of the PRG / PRL kicks' random numbers on this context (no counterpart
+   in the reference):
+     GB_RNG_REFERENCE  the reference's ran2 / gaussian sequence, drawn on the
+                       host in the reference's order (default; a 4096-water,
+                       32-bead PRL step then needs ~0.8 M host draws),
+     GB_RNG_DEVICE     independent N(0, 1) deviates of a counter-based
+                       generator (Philox4x32-10) drawn on the device from
+                       `seed` and a device kick counter: no host work, the
+                       steps replay from CUDA graphs and may join batches.
+   The thermostat is the same; only the numbers differ. */
+#define GB_RNG_REFERENCE 0
+#define GB_RNG_DEVICE 1
+int gbrpmd_ctx_set_rng_mode(gb_context *ctx, int mode, uint64_t seed);
 /* evolve_pi's nbaro for gbrpmd_ctx_evolve / gbrpmd_run_md_eq on this context
    (md_eq.f90:55-58: 1 when ens = 'NPT'): the Berendsen barostat scales the box
    and the water centroids inside every step (one synchronisation per step). */

@@ -195,6 +195,7 @@ void ctx_free(gb_context *c) {
   if (c->h_gauss) cudaFreeHost(c->h_gauss);
   if (c->d_gauss) cudaFree(c->d_gauss);
   if (c->d_therm) cudaFree(c->d_therm);
+  if (c->d_rngctr) cudaFree(c->d_rngctr);
   if (c->gauss_ev) cudaEventDestroy(c->gauss_ev);
   if (c->stream) cudaStreamDestroy(c->stream);
   c->stream = nullptr;
@@ -392,6 +393,22 @@ int gbrpmd_ctx_set_rng(gb_context *c, int idum) {
   c->own_rng = RngState();
   c->own_idum = idum;
   c->has_own_rng = true;
+  return GB_OK;
+}
+
+int gbrpmd_ctx_set_rng_mode(gb_context *c, int mode, uint64_t seed) {
+  if (!c) return ctx_set_error(GB_E_ARG, "null context");
+  if (mode != GB_RNG_REFERENCE && mode != GB_RNG_DEVICE) return ctx_set_error(GB_E_ARG, "unknown random-stream mode");
+  CK(cudaStreamSynchronize(c->stream));
+  if (mode == GB_RNG_DEVICE) {
+    if (!c->d_rngctr) CK(cudaMalloc(&c->d_rngctr, sizeof(unsigned long long)));
+    if (!c->d_therm) CK(cudaMalloc(&c->d_therm, sizeof(double) * 4));
+    CK(cudaMemsetAsync(c->d_rngctr, 0, sizeof(unsigned long long), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  c->rng_mode = mode;
+  c->rng_seed = seed;
+  dev_graph_reset(c);
   return GB_OK;
 }
 

@@ -128,8 +128,9 @@ int gbrpmd_batch_add(gb_batch *b, gb_context *c, double dt, double beta, double 
   if (!b || !c) return ctx_set_error(GB_E_ARG, "null argument");
   if (!c->own_params) return ctx_set_error(GB_E_ARG, "a batch replica needs its own parameters (gbrpmd_ctx_set_params)");
   if (c->nbaro) return ctx_set_error(GB_E_UNSUPPORTED, "a batch replica cannot run a barostat (it synchronises each step)");
-  if (c->P.therm == GB_THERM_PRG || c->P.therm == GB_THERM_PRL)
-    return ctx_set_error(GB_E_UNSUPPORTED, "a batch replica cannot run PRG/PRL kicks (host-drawn stream each step)");
+  if ((c->P.therm == GB_THERM_PRG || c->P.therm == GB_THERM_PRL) && c->rng_mode != GB_RNG_DEVICE)
+    return ctx_set_error(GB_E_UNSUPPORTED,
+                         "a batch replica with PRG/PRL kicks needs the device random stream (gbrpmd_ctx_set_rng_mode)");
   for (auto &r : b->reps)
     if (r.c == c) return ctx_set_error(GB_E_ARG, "context already in the batch");
   BCK(cudaStreamSynchronize(b->s0));

@@ -119,7 +119,10 @@ struct gb_context {
   double *h_gauss = nullptr;      // pinned staging of the same
   cudaEvent_t gauss_ev = nullptr; // the staging buffer's last copy
   bool gauss_pending = false;
-  double *d_therm = nullptr;      // [4] device scratch (PRG kinetic energy)
+  double *d_therm = nullptr;      // [4] device scratch (PRG kinetic energy, device draws)
+  int rng_mode = GB_RNG_REFERENCE;  // GB_RNG_DEVICE: the kicks draw Philox normals on the device
+  unsigned long long rng_seed = 0;
+  unsigned long long *d_rngctr = nullptr;  // device kick counter of the device stream
   unsigned *status = nullptr;
   double *h_acc = nullptr;  // pinned host mirror
   unsigned *h_status = nullptr;

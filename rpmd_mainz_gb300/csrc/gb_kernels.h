@@ -102,7 +102,13 @@ void launch_prl(cudaStream_t s, double *p, const double *mass, const double *g, 
                 double betan);
 void launch_kinetic(cudaStream_t s, const double *p, const double *mass, int na, int nb, double *out);
 void launch_prg_scale(cudaStream_t s, double *p, int na, int nb, const double *kt, double c, double ktav, double ndof,
-                      double snfm1, double ranno);
+                      double snfm1, double ranno, int dev_draws);
+// device random stream (Philox4x32-10): kicks numbered by the device counter *ctr
+void launch_prl_dev(cudaStream_t s, double *p, const double *mass, int na, int nb, double c1, double c2, double betan,
+                    const unsigned long long *ctr, unsigned long long seed);
+void launch_prg_draw(cudaStream_t s, long long ndof, const unsigned long long *ctr, unsigned long long seed,
+                     double *aux);
+void launch_ctr_next(cudaStream_t s, unsigned long long *ctr);
 void launch_baro_shift(cudaStream_t s, double *r, double *rnm, int na, int nb, double sm1);
 // md_eq's output-step estimators (k_est.cu): acc[14] sums, optional rcm / mdip [nm][3]
 void launch_estimators(cudaStream_t s, const double *r, const double *p, const double *dvdr, const double *dvdr2,

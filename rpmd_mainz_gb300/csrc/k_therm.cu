@@ -13,6 +13,69 @@ namespace {
 
 inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// ---- device random stream (gbrpmd_ctx_set_rng_mode, GB_RNG_DEVICE) ----
+// Philox4x32-10, the counter-based generator of Salmon, Moraes, Dror and Shaw
+// ("Parallel random numbers: as easy as 1, 2, 3", SC 2011): ten rounds of two
+// 32 x 32 -> 64-bit multiplies on a 128-bit counter, the 64-bit key bumped by
+// the golden-ratio Weyl constants between rounds.  Counter (element, kick);
+// one normal deviate per element by the Box-Muller transform of the first two
+// 32-bit outputs.  Statistically a stream of independent N(0, 1) numbers, not
+// the reference's ran2 / gaussian sequence.
+struct U4 {
+  unsigned x, y, z, w;
+};
+
+GB_D U4 philox(U4 c, unsigned k0, unsigned k1) {
+  const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const unsigned hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+GB_D double philox_normal(unsigned long long elem, unsigned long long kick, unsigned long long seed) {
+  const U4 o = philox(U4{(unsigned)elem, (unsigned)(elem >> 32), (unsigned)kick, (unsigned)(kick >> 32)},
+                      (unsigned)seed, (unsigned)(seed >> 32));
+  // u1 in (0, 1], u2 in [0, 1) from 53-bit combinations of the outputs
+  const double u1 = ((double)(((unsigned long long)o.x << 21) ^ (o.y >> 11)) + 1.0) * 0x1p-53;
+  const double u2 = (double)(((unsigned long long)o.z << 21) ^ (o.w >> 11)) * 0x1p-53;
+  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+// PRL kick with device normals: kick number *ctr
+__global__ void __launch_bounds__(256) k_prl_dev(double *__restrict__ p, const double *__restrict__ mass, long long N,
+                                                 int na, double c1, double c2, double betan,
+                                                 const unsigned long long *ctr, unsigned long long seed) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int j = (int)((i / 3) % na);
+  const double c3 = __dmul_rn(c2, sqrt(mass[j] / betan));
+  const double g = philox_normal((unsigned long long)i, *ctr, seed);
+  p[i] = __dadd_rn(__dmul_rn(c1, p[i]), __dmul_rn(c3, g));
+}
+
+// PRG deviates on the device: aux[1] = sum of n - 1 squared normals (chi-square
+// with n - 1 degrees of freedom), aux[2] = one more normal (ranno)
+__global__ void __launch_bounds__(256) k_prg_draw(long long n, const unsigned long long *ctr,
+                                                  unsigned long long seed, double *aux) {
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n - 1;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double g = philox_normal((unsigned long long)i, *ctr, seed);
+    v[0] += g * g;
+  }
+  block_sum_atomic<1>(v, sh, aux + 1);
+  if (blockIdx.x == 0 && threadIdx.x == 0) aux[2] = philox_normal((unsigned long long)(n - 1), *ctr, seed);
+}
+
+__global__ void k_ctr_next(unsigned long long *ctr) { *ctr += 1; }
+
 // parinello_therm_loc (module_thermostat.f90:56-82):
 //   p = c1 p + c2 sqrt(m_j / betan) g,  g in the order bead, atom, xyz
 // (products and the sum rounded separately, as the reference computes them)
@@ -41,7 +104,12 @@ __global__ void __launch_bounds__(256) k_kinetic(const double *__restrict__ p, c
 // parinello_therm's rescaling (module_thermostat.f90:37-51); every thread forms
 // the same alpha from the device kinetic energy *kt
 __global__ void __launch_bounds__(256) k_prg_scale(double *__restrict__ p, long long N, const double *__restrict__ kt,
-                                                   double c, double ktav, double ndof, double snfm1, double ranno) {
+                                                   double c, double ktav, double ndof, double snfm1, double ranno,
+                                                   int dev_draws) {
+  if (dev_draws) {  // snfm1 and ranno drawn on the device (k_prg_draw)
+    snfm1 = kt[1];
+    ranno = kt[2];
+  }
   const double ransq = ranno * ranno;
   const double fac = (1.0 - c) * ktav / (ndof * kt[0]);
   const double t1 = __dmul_rn(fac, snfm1 + ransq);  // no contraction into the sum below
@@ -92,11 +160,25 @@ void launch_kinetic(cudaStream_t s, const double *p, const double *mass, int na,
 }
 
 void launch_prg_scale(cudaStream_t s, double *p, int na, int nb, const double *kt, double c, double ktav, double ndof,
-                      double snfm1, double ranno) {
+                      double snfm1, double ranno, int dev_draws) {
   const long long N = 3LL * na * nb;
   const unsigned grid = std::min<unsigned>(nblk(N, 256), 4096u);
-  k_prg_scale<<<grid, 256, 0, s>>>(p, N, kt, c, ktav, ndof, snfm1, ranno);
+  k_prg_scale<<<grid, 256, 0, s>>>(p, N, kt, c, ktav, ndof, snfm1, ranno, dev_draws);
 }
+
+void launch_prl_dev(cudaStream_t s, double *p, const double *mass, int na, int nb, double c1, double c2, double betan,
+                    const unsigned long long *ctr, unsigned long long seed) {
+  const long long N = 3LL * na * nb;
+  k_prl_dev<<<nblk(N, 256), 256, 0, s>>>(p, mass, N, na, c1, c2, betan, ctr, seed);
+}
+
+void launch_prg_draw(cudaStream_t s, long long ndof, const unsigned long long *ctr, unsigned long long seed,
+                     double *aux) {
+  const unsigned grid = std::max(1u, std::min<unsigned>(nblk(ndof, 256), 1024u));
+  k_prg_draw<<<grid, 256, 0, s>>>(ndof, ctr, seed, aux);
+}
+
+void launch_ctr_next(cudaStream_t s, unsigned long long *ctr) { k_ctr_next<<<1, 1, 0, s>>>(ctr); }
 
 void launch_baro_shift(cudaStream_t s, double *r, double *rnm, int na, int nb, double sm1) {
   const int nm = na / 3;

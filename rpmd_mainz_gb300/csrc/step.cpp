@@ -622,11 +622,30 @@ int dev_full_forces(gb_context *c) {
 int therm_kick(gb_context *c, double dtk, double beta) {
   const gb_params &P = c->P;
   if (P.therm != GB_THERM_PRG && P.therm != GB_THERM_PRL) return GB_OK;
-  if (!c->th_rng || !c->th_idum)
-    return ctx_set_error(GB_E_ARG, "PRG/PRL thermostat: no random stream (gbrpmd_ctx_set_rng)");
   const int na = c->na, nb = c->nb;
   const size_t N = 3 * (size_t)na * nb;
   const double betan = beta / (double)nb;
+  if (c->rng_mode == GB_RNG_DEVICE) {  // device stream: no host work, graph-capturable
+    if (P.therm == GB_THERM_PRL) {
+      const double gamma = 1.0 / (2.0 * P.ttau);
+      const double c1 = std::exp(-0.5 * gamma * dtk), c2 = std::sqrt(1.0 - c1 * c1);
+      launch_prl_dev(c->stream, c->p, c->mass, na, nb, c1, c2, betan, c->d_rngctr, c->rng_seed);
+      c->launches += 1;
+    } else {
+      const long long ndof = (long long)(3 * na * (double)nb - P.nctot - 3);
+      CK(cudaMemsetAsync(c->d_therm, 0, sizeof(double) * 2, c->stream));
+      launch_kinetic(c->stream, c->p, c->mass, na, nb, c->d_therm);
+      launch_prg_draw(c->stream, ndof, c->d_rngctr, c->rng_seed, c->d_therm);
+      launch_prg_scale(c->stream, c->p, na, nb, c->d_therm, std::exp(-dtk / P.ttau), (double)ndof / (2.0 * betan),
+                       (double)ndof, 0.0, 0.0, 1);
+      c->launches += 3;
+    }
+    launch_ctr_next(c->stream, c->d_rngctr);
+    c->launches += 1;
+    return GB_OK;
+  }
+  if (!c->th_rng || !c->th_idum)
+    return ctx_set_error(GB_E_ARG, "PRG/PRL thermostat: no random stream (gbrpmd_ctx_set_rng)");
   RngState &g = *c->th_rng;
   int *idum = c->th_idum;
   if (!c->d_therm) CK(cudaMalloc(&c->d_therm, sizeof(double) * 4));
@@ -661,7 +680,7 @@ int therm_kick(gb_context *c, double dtk, double beta) {
   launch_kinetic(c->stream, c->p, c->mass, na, nb, c->d_therm);
   const double ranno = rng_gaussian(g, idum, 1.0);
   const double cc = std::exp(-dtk / P.ttau);
-  launch_prg_scale(c->stream, c->p, na, nb, c->d_therm, cc, ktav, (double)ndof, snfm1, ranno);
+  launch_prg_scale(c->stream, c->p, na, nb, c->d_therm, cc, ktav, (double)ndof, snfm1, ranno, 0);
   c->launches += 2;
   return GB_OK;
 }
@@ -792,7 +811,8 @@ int dev_step(gb_context *c, double dt, double beta) {
   if (ctx_rigid(c)) return dev_evolve_step(c, dt, beta);  // its force call drops step graphs
   const bool eligible = c->use_graphs && !c->prof && !c->generic_mts &&
                         (c->nb == 2 || c->nb == 4 || c->nb == 8 || c->nb == 16 || c->nb == 32 || c->nb == 64) &&
-                        c->P.therm != GB_THERM_PRG && c->P.therm != GB_THERM_PRL && !c->nbaro;
+                        (c->rng_mode == GB_RNG_DEVICE || (c->P.therm != GB_THERM_PRG && c->P.therm != GB_THERM_PRL)) &&
+                        !c->nbaro;
   const bool same = eligible && G.dt == dt && G.beta == beta && G.box[0] == c->box[0] && G.box[1] == c->box[1] &&
                     G.box[2] == c->box[2] && std::memcmp(&G.P, &c->P, sizeof(gb_params)) == 0;
   if (!same) {

@@ -52,6 +52,7 @@ struct Saved {
   double *dev = nullptr;
   size_t n = 0;
   double e[5], vir[9], vir_lf[9], vir_hf[9], vir_lf_in[9], box[3];
+  unsigned long long ctr = 0;  // the device random stream's kick counter
 };
 
 int save(gb_context *c, Saved &S) {
@@ -66,6 +67,10 @@ int save(gb_context *c, Saved &S) {
   std::memcpy(S.vir_hf, c->e_vir_hf, sizeof S.vir_hf);
   std::memcpy(S.vir_lf_in, c->vir_lf_in, sizeof S.vir_lf_in);
   std::memcpy(S.box, c->box, sizeof S.box);
+  if (c->d_rngctr) {
+    TCK(cudaMemcpyAsync(&S.ctr, c->d_rngctr, sizeof S.ctr, cudaMemcpyDeviceToHost, c->stream));
+    TCK(cudaStreamSynchronize(c->stream));
+  }
   return GB_OK;
 }
 
@@ -73,6 +78,7 @@ int restore(gb_context *c, const Saved &S) {
   double *dst[4] = {c->r, c->p, c->dvdr, c->dvdr2};
   for (int i = 0; i < 4; ++i)
     TCK(cudaMemcpyAsync(dst[i], S.dev + i * S.n, sizeof(double) * S.n, cudaMemcpyDeviceToDevice, c->stream));
+  if (c->d_rngctr) TCK(cudaMemcpyAsync(c->d_rngctr, &S.ctr, sizeof S.ctr, cudaMemcpyHostToDevice, c->stream));
   TCK(cudaStreamSynchronize(c->stream));
   c->e_v = S.e[0], c->e_vew = S.e[1], c->e_vlj = S.e[2], c->e_vint = S.e[3], c->e_tv = S.e[4];
   std::memcpy(c->e_vir, S.vir, sizeof S.vir);
@@ -135,7 +141,8 @@ int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double
   if (!c) return ctx_set_error(GB_E_ARG, "null context");
   if (steps < 1) return ctx_set_error(GB_E_ARG, "steps must be >= 1");
   const gb_params &P = c->P;
-  const bool tunable = !ctx_rigid(c) && !c->nbaro && P.therm != GB_THERM_PRG && P.therm != GB_THERM_PRL;
+  const bool tunable = !ctx_rigid(c) && !c->nbaro &&
+                       (c->rng_mode == GB_RNG_DEVICE || (P.therm != GB_THERM_PRG && P.therm != GB_THERM_PRL));
   auto report = [&]() {
     if (out4) {
       out4[0] = c->tune.ew_np;

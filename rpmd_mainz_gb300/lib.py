@@ -69,6 +69,7 @@ def load(path=None):
     lib.gbrpmd_ctx_energies.argtypes = [C.c_void_p, D, D, D]
     lib.gbrpmd_ctx_estimators.argtypes = [C.c_void_p, C.c_double, D, D, D]
     lib.gbrpmd_ctx_set_rng.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_ctx_set_rng_mode.argtypes = [C.c_void_p, C.c_int, C.c_uint64]
     lib.gbrpmd_ctx_set_nbaro.argtypes = [C.c_void_p, C.c_int]
     lib.gbrpmd_ctx_box.argtypes = [C.c_void_p, D]
     lib.gbrpmd_rng_reset.restype = None
@@ -342,6 +343,11 @@ class Context:
     def set_rng(self, idum):
         """Context-owned random stream for the PRG / PRL kicks of evolve()."""
         _check(load().gbrpmd_ctx_set_rng(self.h, int(idum)))
+
+    def set_rng_mode(self, mode, seed=0):
+        """Random numbers of the PRG / PRL kicks: "reference" (host ran2 / gaussian)
+        or "device" (Philox4x32-10 on the device, seeded)."""
+        _check(load().gbrpmd_ctx_set_rng_mode(self.h, {"reference": 0, "device": 1}[mode], int(seed)))
 
     def set_nbaro(self, nbaro):
         """evolve_pi's nbaro for evolve() / run_md_eq() (1: Berendsen barostat)."""

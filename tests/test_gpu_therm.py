@@ -126,3 +126,61 @@ def test_device_replays_gentest_equilibration():
     assert np.abs(den - MDEQ["density_eq"][:, 1]).max() <= 1e-12
     assert abs(eq[-1]["box"] - EQ["box"][0]) <= 1e-11
     assert np.abs(r_end - EQ["r"]).max() <= 1e-8
+
+
+@pytest.mark.parametrize("therm", ["PRL", "PRG"])
+@pytest.mark.parametrize("mode", ["device", "reference"])
+def test_thermostat_reaches_temperature(therm, mode):
+    # strong coupling (ttau 10 fs) from cold momenta: the kinetic temperature
+    # of md_eq (md_eq.f90:272) settles at the target within its fluctuation
+    s = systems.build(param="param_qspcfw", ncell=(6, 6, 6), nb=8, temp=298.0, therm=therm, ttaufs=10.0)
+    lib.init(s["params"])
+    ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+    try:
+        ctx.set_params(s["params"])
+        ctx.upload(r=s["r"], p=np.zeros_like(s["r"]), box=s["box"])
+        ctx.full_forces()
+        if mode == "device":
+            ctx.set_rng_mode("device", seed=123)
+        else:
+            ctx.set_rng(-77)
+        temps = []
+        for step in range(400):
+            ctx.evolve(1, s["dt"], s["beta"])
+            if step >= 200:
+                ctx.sync()
+                temps.append(ctx.estimators(s["beta"])["temp"])
+    finally:
+        ctx.close()
+    assert abs(np.mean(temps) - 298.0) < 0.03 * 298.0, np.mean(temps)
+    assert np.std(temps) < 0.1 * 298.0
+
+
+def test_device_stream_replica_in_batch_equals_alone():
+    s = systems.build(param="param_qspcfw", ncell=(4, 4, 4), nb=8, therm="PRL", ttaufs=50.0)
+    lib.init(s["params"])
+    r = systems.perturbed(s, seed=70)
+
+    def run(batched):
+        ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+        ctx.set_params(s["params"])
+        ctx.upload(r=r, p=np.zeros_like(r), box=s["box"])
+        ctx.full_forces()
+        ctx.set_rng_mode("device", seed=9)
+        if batched:
+            b = lib.Batch()
+            b.add(ctx, s["dt"], s["beta"])
+            b.step(6)
+            b.sync()
+            b.close()
+        else:
+            ctx.evolve(6, s["dt"], s["beta"])
+            ctx.sync()
+        out = ctx.download()
+        ctx.close()
+        return out
+
+    alone, inbatch = run(False), run(True)
+    assert np.abs(alone[1]).max() > 0.0  # the kicks heated the cold start
+    for a, b in zip(inbatch, alone):
+        assert rel(a, b) < 1e-11
