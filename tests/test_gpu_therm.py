@@ -131,14 +131,16 @@ def test_device_replays_gentest_equilibration():
 @pytest.mark.parametrize("therm", ["PRL", "PRG"])
 @pytest.mark.parametrize("mode", ["device", "reference"])
 def test_thermostat_reaches_temperature(therm, mode):
-    # strong coupling (ttau 10 fs) from cold momenta: the kinetic temperature
-    # of md_eq (md_eq.f90:272) settles at the target within its fluctuation
+    # strong coupling (ttau 10 fs) from cold momenta (a tenth of the thermal
+    # scale; PRG rescales, so it cannot start from zero): the kinetic
+    # temperature of md_eq (md_eq.f90:272) settles at the target
     s = systems.build(param="param_qspcfw", ncell=(6, 6, 6), nb=8, temp=298.0, therm=therm, ttaufs=10.0)
     lib.init(s["params"])
+    p0 = 0.1 * orc.sample_rpmd(s["na"], s["nb"], s["mass"], s["beta"], orc.Rng(8))
     ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
     try:
         ctx.set_params(s["params"])
-        ctx.upload(r=s["r"], p=np.zeros_like(s["r"]), box=s["box"])
+        ctx.upload(r=s["r"], p=p0, box=s["box"])
         ctx.full_forces()
         if mode == "device":
             ctx.set_rng_mode("device", seed=123)
