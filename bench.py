@@ -562,7 +562,7 @@ def run_nve(args, torch):
 
 def run_served(args, torch):
     """Poisson arrivals (mean 50 per second) of trajectory requests of mixed
-    sizes (64-1728 molecules, nb 4-64), half of them rigid TIP4P/2005 water
+    sizes (64-2048 molecules, nb 4-64), half of them rigid TIP4P/2005 water
     (evolve_rig_pi with RATTLE), each `--request-steps` steps, served by the
     continuous-batching loop under a device-memory budget."""
     from rpmd_mainz_gb300 import lib, workloads
@@ -622,7 +622,7 @@ def run_served(args, torch):
         "dtype": "f32+f64 mixed", "data": "synthetic request stream (seeded Poisson arrivals, CUB lattices)",
         "config": {"workload": "served_stream", "requests": len(stream), "arrival_rate_per_s": 50.0,
                    "steps_per_request": args.request_steps, "tick_steps": args.tick_steps, "slots": args.slots,
-                   "budget_gib": args.budget_gb, "sizes": "nm in 64..1728 (cubic lattices), nb in {4,8,16,32,64}",
+                   "budget_gib": args.budget_gb, "sizes": "nm in 64..2048 (CUB lattices; 2048 on 16x16x8, a non-cubic box), nb in {4,8,16,32,64}",
                    "rigid_requests": int(sum(1 for _, s, _ in stream if s["rigid"])),
                    "models": "flexible q-SPC/Fw (evolve_pi) and rigid TIP4P/2005 (evolve_rig_pi, RATTLE)"},
         "error_vs_fp64": {"force_rel_rms_max": max(errs.values()) if errs else None, "bound": 1e-5,

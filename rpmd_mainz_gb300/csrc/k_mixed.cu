@@ -341,8 +341,10 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
 }
 
 // FP64 sums of the chunk partials, energy and virial; FP32 force tables
-constexpr int MW_SL = 16;  // chunk slices per k pair in the weights kernel
+// chunk slices per k pair in the weights kernel (SL warps per block): 16 for
+// many chunks, fewer when the configuration has few sites (idle warps otherwise)
 
+template <int MW_SL>
 __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *sk_part, int nchunk, int nkp,
                                                                 const int4 *kpair, const double *kw, const double *kvir,
                                                                 float4 *sk, double *acc) {
@@ -563,8 +565,14 @@ void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc) 
   if (c->nkp == 0) return;
   const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
   dim3 grid(nblk(c->nkp, 32), B);
-  k_recip_weights_mx<<<grid, 32 * MW_SL, 0, s>>>(reinterpret_cast<const float4 *>(c->sk_part), nchunk, c->nkp, c->kpair,
-                                          c->kw, c->kvir, reinterpret_cast<float4 *>(c->sk), acc);
+  auto go = [&](auto SLc) {
+    constexpr int SL = decltype(SLc)::value;
+    k_recip_weights_mx<SL><<<grid, 32 * SL, 0, s>>>(reinterpret_cast<const float4 *>(c->sk_part), nchunk, c->nkp,
+                                                    c->kpair, c->kw, c->kvir, reinterpret_cast<float4 *>(c->sk), acc);
+  };
+  if (nchunk <= 4) go(std::integral_constant<int, 4>());
+  else if (nchunk <= 8) go(std::integral_constant<int, 8>());
+  else go(std::integral_constant<int, 16>());
 }
 
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {

@@ -20,7 +20,7 @@ PARAM_TIP05 = os.path.join(os.path.dirname(HERE), "tests", "golden", "params", "
 # CUB lattice cells per molecule count; 128 molecules need the anisotropic
 # 8 x 4 x 4 lattice (a non-cubic box, ewald_nc)
 CELLS = {64: (4, 4, 4), 128: (8, 4, 4), 216: (6, 6, 6), 343: (7, 7, 7), 512: (8, 8, 8), 729: (9, 9, 9),
-         1000: (10, 10, 10), 1331: (11, 11, 11), 1728: (12, 12, 12)}
+         1000: (10, 10, 10), 1331: (11, 11, 11), 1728: (12, 12, 12), 2048: (16, 16, 8)}
 
 
 def _box(nm, nb, temp, precision, seed, dtfs=0.5, mts=1, param=PARAM_QSPCFW):
@@ -46,7 +46,7 @@ def replica_set(n=256, seed=2026, precision=1, sizes=(64, 128, 216, 343, 512), b
     return out
 
 
-def request_stream(n=60, rate=50.0, seed=7, precision=1, sizes=(64, 216, 343, 512, 729, 1000, 1331, 1728),
+def request_stream(n=60, rate=50.0, seed=7, precision=1, sizes=(64, 216, 343, 512, 729, 1000, 1331, 1728, 2048),
                    beads=(4, 8, 16, 32, 64), nsteps=100, temp=298.0, rigid_fraction=0.5):
     """n trajectory requests with Poisson arrivals (mean `rate` per second):
     [(arrival_seconds, system, nsteps)], sizes and bead counts drawn per
