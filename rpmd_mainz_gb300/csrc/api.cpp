@@ -197,6 +197,8 @@ void ctx_free(gb_context *c) {
   if (c->d_therm) cudaFree(c->d_therm);
   if (c->d_rngctr) cudaFree(c->d_rngctr);
   if (c->gauss_ev) cudaEventDestroy(c->gauss_ev);
+  if (c->mid_ev) cudaEventDestroy(c->mid_ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   c->stream = nullptr;
 }
@@ -281,20 +283,34 @@ int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj, 
   std::memcpy(c->vir_lf_in, vir_lf, sizeof(double) * 9);  // the barostat reads the previous call's vir_lf
   c->nbaro = *nbaro;
   tune_apply_cached(c);  // launch shapes of an autotuned context of the same shape
+  if (!c->mid_ev) {
+    CK(cudaEventCreateWithFlags(&c->mid_ev, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  }
+  c->want_mid = 1;
   c->th_rng = &g_rng;  // thermostat kicks draw the process-wide stream with the caller's irun
   c->th_idum = irun;
   if ((st = upload(c, c->p, p, N)) || (st = upload(c, c->r, r, N)) || (st = upload(c, c->dvdr, dvdr, N)) ||
       (st = upload(c, c->dvdr2, dvdr2, N)) || (st = set_masses(c, mass)) || (st = set_charges(c, z)))
     return st;
+  c->mid_recorded = false;
   st = dev_step(c, *dt, *beta);
   c->th_rng = nullptr;
   c->th_idum = nullptr;
   if (st) return st;
   std::memcpy(boxlxyz, c->box, sizeof(double) * 3);  // scaled by the barostat
-  if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
-      (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N)))
+  if (c->mid_recorded) {  // r and dvdr2 leave while the low-frequency forces compute
+    CK(cudaStreamWaitEvent(c->copy_stream, c->mid_ev, 0));
+    CK(cudaMemcpyAsync(r, c->r, sizeof(double) * N, cudaMemcpyDeviceToHost, c->copy_stream));
+    CK(cudaMemcpyAsync(dvdr2, c->dvdr2, sizeof(double) * N, cudaMemcpyDeviceToHost, c->copy_stream));
+    if ((st = download(c, p, c->p, N)) || (st = download(c, dvdr, c->dvdr, N))) return st;
+  } else if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
+             (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N))) {
     return st;
-  if ((st = dev_collect(c, 1, *dt, *beta))) return st;
+  }
+  st = dev_collect(c, 1, *dt, *beta);
+  if (c->mid_recorded) CK(cudaStreamSynchronize(c->copy_stream));
+  if (st) return st;
   *v = c->e_v;
   *vew = c->e_vew;
   *vlj = c->e_vlj;

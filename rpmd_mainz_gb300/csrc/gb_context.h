@@ -145,7 +145,15 @@ struct gb_context {
     gb_params P{};
     int64_t launches = 0;    // kernels per replay
     EnergyPlan plan;
+    bool mid = false;        // the replay records mid_ev
   } graph;
+  // drop-in calls: an event after the MTS block (r and dvdr2 final), recorded
+  // into the step (and its graph), so that their copies back to the host run on
+  // copy_stream while the low-frequency forces still compute
+  int want_mid = 0;
+  bool mid_recorded = false;
+  cudaEvent_t mid_ev = nullptr;
+  cudaStream_t copy_stream = nullptr;
   int use_graphs = 1;        // GBRPMD_GRAPHS=0 turns replay off
   // launch shapes chosen by gbrpmd_ctx_autotune (tune.cpp); results depend on
   // them only through the order of floating-point sums

@@ -723,8 +723,17 @@ int barostat(gb_context *c, double dt) {
   return GB_OK;
 }
 
+// r and dvdr2 are final once the MTS block (and the barostat) ran
+int mark_mid(gb_context *c) {
+  if (!c->want_mid || !c->mid_ev) return GB_OK;
+  CK(cudaEventRecordWithFlags(c->mid_ev, c->stream, cudaEventRecordExternal));
+  c->mid_recorded = true;
+  return GB_OK;
+}
+
 int dev_evolve_pi(gb_context *c, double dt, double beta) {
   int st;
+  c->mid_recorded = false;
   if (c->nbaro && c->graph.valid) dev_graph_reset(c);
   if ((st = dev_prepare(c, dt, beta))) return st;
   c->plan = EnergyPlan();
@@ -747,6 +756,7 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
     c->launches += 1;
     prof_end(c, PR_MTS, (double)c->nm * nb * mts);
     if (c->nbaro && (st = barostat(c, dt))) return st;
+    if ((st = mark_mid(c))) return st;
     if ((st = low_frequency(c, c->rnm, c->r, c->p, halfdt))) return st;
     if ((st = therm_kick(c, dt_therm, beta))) return st;
     return launch_status();
@@ -779,6 +789,7 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   c->launches += 2;
   prof_end(c, PR_MTS, (double)c->nm * nb * mts);
   if (c->nbaro && (st = barostat(c, dt))) return st;
+  if ((st = mark_mid(c))) return st;
   // low-frequency forces and the closing kick (evolve_pi.f90:194-279)
   if ((st = low_frequency(c, c->rnm, c->r, c->p, halfdt))) return st;
   if ((st = therm_kick(c, dt_therm, beta))) return st;
@@ -827,6 +838,7 @@ int dev_step(gb_context *c, double dt, double beta) {
     c->launches += G.launches;
     c->plan = G.plan;
     c->last_beta = beta;
+    c->mid_recorded = G.mid;
     return GB_OK;
   }
   if (!eligible || G.seen < 1) {  // plain step; the next one with this key is captured
@@ -856,6 +868,7 @@ int dev_step(gb_context *c, double dt, double beta) {
   G.valid = true;
   G.launches = c->launches - l0;
   G.plan = c->plan;
+  G.mid = c->mid_recorded;
   CK(cudaGraphLaunch(G.exec, c->stream));  // the captured step has not run yet
   return GB_OK;
 }
