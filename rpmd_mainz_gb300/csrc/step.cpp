@@ -726,7 +726,11 @@ int barostat(gb_context *c, double dt) {
 // r and dvdr2 are final once the MTS block (and the barostat) ran
 int mark_mid(gb_context *c) {
   if (!c->want_mid || !c->mid_ev) return GB_OK;
-  CK(cudaEventRecordWithFlags(c->mid_ev, c->stream, cudaEventRecordExternal));
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(c->stream, &cap));
+  // inside a capture the record becomes an external event node of the graph
+  if (cap == cudaStreamCaptureStatusActive) CK(cudaEventRecordWithFlags(c->mid_ev, c->stream, cudaEventRecordExternal));
+  else CK(cudaEventRecord(c->mid_ev, c->stream));
   c->mid_recorded = true;
   return GB_OK;
 }
