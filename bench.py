@@ -68,6 +68,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, torch):
+    """The slowest rank's value on every rank (all-reduce MAX on the process
+    group's device: CUDA for NCCL, host for gloo); x itself when world is 1."""
+    if world <= 1:
+        return float(x)
+    dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank_step, steps, world, total_ms):
+    """Whole-job throughput: every rank's units over the slowest rank's time
+    (replicas only: each rank advances its own trajectory, weak scaling)."""
+    return world * steps * units_per_rank_step / (total_ms * 1e-3)
+
+
 def make_system(name):
     from rpmd_mainz_gb300 import lib, system
 
@@ -297,12 +314,10 @@ def measure(args, s, prec, torch, world, local):
     launches = ctx.launches - launches0
     rebuilds = [b - a for a, b in zip(rebuilds0, ctx.list_rebuilds())]
     total_ms = float(sum(step_ms))
+    total_ms = max_over_ranks(total_ms, world, torch)
     if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
         torch.distributed.barrier()
-    value = world * args.steps * nb * nm / (total_ms * 1e-3)
+    value = job_value(nb * nm, args.steps, world, total_ms)
     energies = ctx.energies()
 
     # e2e through the drop-in C ABI with pinned host buffers
