@@ -137,13 +137,24 @@ __global__ void k_expand_forces(double *dvdr, const double *fb1, int nbc1, const
 // product with a per-bead table E[j] = sqrt(1/nb) (1, 2 cos(2 pi jk/nb),
 // -2 sin(2 pi jk/nb), k = 1..HM) held in shared memory.  R = float runs the
 // dot product in FP32 (mixed precision); the kick stays FP64.
+// A block takes XR coordinate rows: XR threads reduce the rows' contracted
+// forces to coefficients (shared memory), then all XT threads expand them, four
+// threads per row each over a quarter of the beads, consecutive rows in
+// consecutive lanes so that every bead plane is written coalesced.
+// sc[t] = (sqrt(1/nbc_t), sqrt(nb/nbc_t)) of the two contracted terms.
+constexpr int XR = 32;
+constexpr int XT = 4 * XR;
+
 template <int HM, typename R>
-__global__ void k_expand_table(double *dvdr, const double *fb1, int nbc1, const double *tw_c1, const double *fb2,
-                               int nbc2, const double *tw_c2, const double *e1, const double *e2, const double *e3,
-                               double *p, double halfdt, int na, int nb, const double *tw_nb) {
+__global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double *fb1, int nbc1, const double *tw_c1,
+                                                     const double *fb2, int nbc2, const double *tw_c2,
+                                                     const double *e1, const double *e2, const double *e3, double *p,
+                                                     double halfdt, int na, int nb, const double *tw_nb,
+                                                     double2 sc1, double2 sc2) {
   constexpr int NQ = 2 * HM + 1;
   extern __shared__ double smx[];
   R *E = reinterpret_cast<R *>(smx);  // [nb][NQ]
+  R *CF = E + nb * NQ;                // [XR][NQ]
   const double sc = sqrt(1.0 / (double)nb);
   for (int w = threadIdx.x; w < nb * NQ; w += blockDim.x) {
     const int j = w / NQ, q = w % NQ;
@@ -154,39 +165,44 @@ __global__ void k_expand_table(double *dvdr, const double *fb1, int nbc1, const 
     }
     E[w] = (R)v;
   }
-  __syncthreads();
   const long long S = 3LL * na;
-  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= S) return;
-  double cf[NQ];
+  const bool any = fb1 || fb2;
+  const int lr = threadIdx.x % XR, grp = threadIdx.x / XR;
+  const long long row = (long long)blockIdx.x * XR + lr;
+  if (grp == 0 && row < S) {
+    double cf[NQ];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) cf[q] = 0.0;
-  const double *fbs[2] = {fb1, fb2};
-  const int nbcs[2] = {nbc1, nbc2};
-  const double *tws[2] = {tw_c1, tw_c2};
-  bool any = false;
-  for (int t = 0; t < 2; ++t) {
-    if (!fbs[t]) continue;
-    any = true;
-    const int nbc = nbcs[t], h = (nbc - 1) / 2;
-    double tmp[NQ + 1], hc[NQ + 1];  // nbc <= 2 HM + 2
-    for (int j = 0; j < nbc; ++j) tmp[j] = fbs[t][row + S * j];
-    gb_r2hc_direct(tmp, hc, nbc, tws[t]);
-    const double s1 = sqrt(1.0 / (double)nbc), s2 = sqrt((double)nb / (double)nbc);
-    cf[0] += s2 * (s1 * hc[0]);
+    for (int q = 0; q < NQ; ++q) cf[q] = 0.0;
+    const double *fbs[2] = {fb1, fb2};
+    const int nbcs[2] = {nbc1, nbc2};
+    const double *tws[2] = {tw_c1, tw_c2};
+    const double2 scs[2] = {sc1, sc2};
+    for (int t = 0; t < 2; ++t) {
+      if (!fbs[t]) continue;
+      const int nbc = nbcs[t], h = (nbc - 1) / 2;
+      double tmp[NQ + 1], hc[NQ + 1];  // nbc <= 2 HM + 2
+      for (int j = 0; j < nbc; ++j) tmp[j] = fbs[t][row + S * j];
+      gb_r2hc_direct(tmp, hc, nbc, tws[t]);
+      const double s1 = scs[t].x, s2 = scs[t].y;
+      cf[0] += s2 * (s1 * hc[0]);
 #pragma unroll
-    for (int k = 1; k <= HM; ++k) {
-      if (k <= h) {
-        cf[2 * k - 1] += s2 * (s1 * hc[k]);
-        cf[2 * k] += s2 * (s1 * hc[nbc - k]);
+      for (int k = 1; k <= HM; ++k) {
+        if (k <= h) {
+          cf[2 * k - 1] += s2 * (s1 * hc[k]);
+          cf[2 * k] += s2 * (s1 * hc[nbc - k]);
+        }
       }
     }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) CF[lr * NQ + q] = (R)cf[q];
   }
+  __syncthreads();
+  if (row >= S) return;
   R cr[NQ];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) cr[q] = (R)cf[q];
-#pragma unroll 8
-  for (int j = 0; j < nb; ++j) {
+  for (int q = 0; q < NQ; ++q) cr[q] = CF[lr * NQ + q];
+  const int j0 = grp * nb / 4, j1 = (grp + 1) * nb / 4;
+  for (int j = j0; j < j1; ++j) {
     R s = (R)0;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) s += cr[q] * E[j * NQ + q];
@@ -295,13 +311,17 @@ void launch_expand_hm(cudaStream_t s, bool mixed, double *dvdr, const double *fb
                       const double *fb2, int nbc2, const double *tw_c2, const double *e1, const double *e2,
                       const double *e3, double *p, double halfdt, int na, int nb, const double *tw_nb) {
   const long long n = 3LL * na;
-  const size_t smem = sizeof(double) * nb * (2 * HM + 1);
+  const size_t smem = sizeof(double) * (nb + XR) * (2 * HM + 1);
+  auto scale = [&](int nbc) {  // sqrt(1/nbc), sqrt(nb/nbc) of a contraction (force_contract)
+    return nbc > 0 ? make_double2(sqrt(1.0 / (double)nbc), sqrt((double)nb / (double)nbc)) : make_double2(0.0, 0.0);
+  };
+  const double2 sc1 = scale(fb1 ? nbc1 : 0), sc2 = scale(fb2 ? nbc2 : 0);
   if (mixed)
-    k_expand_table<HM, float><<<nblk(n, 128), 128, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3,
-                                                              p, halfdt, na, nb, tw_nb);
+    k_expand_table<HM, float><<<nblk(n, XR), XT, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p,
+                                                            halfdt, na, nb, tw_nb, sc1, sc2);
   else
-    k_expand_table<HM, double><<<nblk(n, 128), 128, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3,
-                                                               p, halfdt, na, nb, tw_nb);
+    k_expand_table<HM, double><<<nblk(n, XR), XT, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3,
+                                                             p, halfdt, na, nb, tw_nb, sc1, sc2);
 }
 
 void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int nbc1,
