@@ -161,6 +161,7 @@ struct gb_context {
     int ew_np = 16;   // lanes per site, FP32 real-space Ewald (8, 16, 32)
     int lj_np = 4;    // lanes per oxygen, FP32 LJ (2, 4, 8)
     int mts_mpb = 0;  // molecules per block of the MTS kernel (0: one wave over the SMs)
+    int rf_g = 8;     // column shares (warps) per block, FP32 k-space force kernel (8, 16)
     int done = 0;
   } tune;
 

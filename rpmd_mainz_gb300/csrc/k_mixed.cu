@@ -270,7 +270,7 @@ constexpr int MSK_CHUNK = 128;  // sites per structure-factor block (FP32 partia
 constexpr int MSK_G = 8;
 constexpr int MSK_T = 128;
 constexpr int MF_S = 32;  // sites per force block
-constexpr int MF_G = 8;   // column shares (warps) per force block
+constexpr int MF_GMAX = 16;  // column shares (warps) per force block: 8 or 16 (tuned)
 constexpr int SIGN32 = (int)0x80000000u;
 
 GB_D float flipf(float v, int mask) { return __int_as_float(__float_as_int(v) ^ mask); }
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
 // the warps' per-site sums are added in FP64 in a fixed order
 // STAGED: the whole k-pair table (8 floats per pair) is copied to shared
 // memory first, so that the inner loop reads it with shared-memory broadcasts
-template <bool STAGED>
+template <bool STAGED, int MF_G>
 __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__restrict__ tab, int na, int kmax,
                                                               int ncol, const KCol *__restrict__ cols, int nkp,
                                                               const float4 *__restrict__ sk, double3 lat, double *g) {
@@ -545,7 +545,7 @@ void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, in
 
 size_t recip_sk_smem_mx(int kmax) { return sizeof(float2) * MSK_CHUNK * 3 * (kmax + 1); }
 size_t recip_force_smem_mx(int kmax, int nkp_staged) {
-  return sizeof(float4) * ((3 * (kmax + 1) * MF_S + 1) / 2 + (MF_G * MF_S * 3 + 1) / 2 + 2 * (size_t)nkp_staged);
+  return sizeof(float4) * ((3 * (kmax + 1) * MF_S + 1) / 2 + (MF_GMAX * MF_S * 3 + 1) / 2 + 2 * (size_t)nkp_staged);
 }
 
 // partial sums need nconf * nchunk * nkp float4 (half of the FP64 layout)
@@ -580,21 +580,28 @@ void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
   const int kmax = c->P.kmax;
   dim3 grid(nblk(c->na, MF_S), B);
   const size_t staged = recip_force_smem_mx(kmax, c->nkp);
-  if (staged <= 160 * 1024)
-    k_recip_force_mx<true><<<grid, MF_S * MF_G, staged, s>>>(
-        reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
-        reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
-  else
-    k_recip_force_mx<false><<<grid, MF_S * MF_G, recip_force_smem_mx(kmax, 0), s>>>(
-        reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
-        reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
+  auto go = [&](auto Gc) {
+    constexpr int G = decltype(Gc)::value;
+    if (staged <= 160 * 1024)
+      k_recip_force_mx<true, G><<<grid, MF_S * G, staged, s>>>(
+          reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
+          reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
+    else
+      k_recip_force_mx<false, G><<<grid, MF_S * G, recip_force_smem_mx(kmax, 0), s>>>(
+          reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
+          reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
+  };
+  if (c->tune.rf_g == 16) go(std::integral_constant<int, 16>());
+  else go(std::integral_constant<int, 8>());
 }
 
 void recip_set_attributes_mx() {
   static bool done = false;
   if (done) return;
   cudaFuncSetAttribute(k_recip_sk_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   done = true;
 }

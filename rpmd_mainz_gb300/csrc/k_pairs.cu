@@ -66,6 +66,10 @@ GB_D bool exact_pair_in(const PairGeom &g, const double *a, const double *b) {
 // is copied out, so the order of the flushed groups inside a list is arbitrary.
 constexpr int LB_STAGE = 32;
 
+// FULL: store every pair in both lists (else the parity rule above); EXCL:
+// skip pairs of the same molecule.  Four partners at a time: their FP32
+// distances first, then the rare near pairs one by one.
+template <bool FULL, bool EXCL>
 __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *frac, int *count,
                                                       int *idx, int cap, float3 len, float thr_lo,
                                                       float thr_hi, unsigned *status, const unsigned *gate,
@@ -101,30 +105,40 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
     }
     nst = 0;
   };
+  auto dist2 = [&](const float4 &fj) {
+    float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
+    dx = (dx - rintf(dx)) * len.x;
+    dy = (dy - rintf(dy)) * len.y;
+    dz = (dz - rintf(dz)) * len.z;
+    return dx * dx + dy * dy + dz * dz;
+  };
+  auto near = [&](int j, float d2) {  // d2 < thr_hi
+    if (j == i) return;
+    if (!FULL && (i < j) != (((i + j) & 1) != 0)) return;
+    if (EXCL && (i / 3) == (j / 3)) return;
+    if (d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride)) {
+      st[nst++] = j;
+      if (nst == LB_STAGE) flush();
+    }
+  };
   for (int jt = j0; jt < j1; jt += LB_T) {
     const int jl = jt + threadIdx.x;
     tile[threadIdx.x] = jl < j1 ? fr[jl] : make_float4(0.5f, 0.5f, 0.5f, 0.f);
     __syncthreads();
     if (i < npt) {
       const int jmax = min(LB_T, j1 - jt);
-      for (int jj = 0; jj < jmax; ++jj) {
-        const int j = jt + jj;
-        if (j == i) continue;
-        if (!g.full && (i < j) != (((i + j) & 1) != 0)) continue;
-        if (g.excl_mol && (i / 3) == (j / 3)) continue;
-        const float4 fj = tile[jj];
-        float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
-        dx = (dx - rintf(dx)) * len.x;
-        dy = (dy - rintf(dy)) * len.y;
-        dz = (dz - rintf(dz)) * len.z;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        if (d2 >= thr_hi) continue;
-        bool ok = d2 < thr_lo;
-        if (!ok) ok = exact_pair_in(g, pi, base + (long long)j * g.pstride);
-        if (ok) {
-          st[nst++] = j;
-          if (nst == LB_STAGE) flush();
-        }
+      int jj = 0;
+      for (; jj + 4 <= jmax; jj += 4) {
+        float d2[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) d2[u] = dist2(tile[jj + u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (d2[u] < thr_hi) near(jt + jj + u, d2[u]);
+      }
+      for (; jj < jmax; ++jj) {
+        const float d2 = dist2(tile[jj]);
+        if (d2 < thr_hi) near(jt + jj, d2);
       }
     }
     __syncthreads();
@@ -584,8 +598,16 @@ void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float
   const long long bi = (long long)nblk(g.npt, LB_T) * nconf;
   while (jchunk > LB_T && bi * (long long)nblk(g.npt, jchunk) < 4LL * nsm) jchunk /= 2;
   dim3 grid(nblk(g.npt, LB_T), nblk(g.npt, jchunk), nconf);
-  k_build_list2<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status, gate,
-                                      jchunk);
+  auto go = [&](auto kern) {
+    kern<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status, gate, jchunk);
+  };
+  if (g.full) {
+    if (g.excl_mol) go(k_build_list2<true, true>);
+    else go(k_build_list2<true, false>);
+  } else {
+    if (g.excl_mol) go(k_build_list2<false, true>);
+    else go(k_build_list2<false, false>);
+  }
 }
 
 void launch_skin_check(cudaStream_t s, const PairGeom &g, int nconf, const double *ref, double lim2,

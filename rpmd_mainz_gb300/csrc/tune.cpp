@@ -6,7 +6,8 @@
 // LJ kernels (more lanes give more warps for small systems, fewer lanes less
 // reduction work for large ones), the molecules per block of the fused MTS
 // kernel (occupancy against the one-wave grid), and the pair-list skin (larger
-// lists against fewer rebuilds).  gbrpmd_ctx_autotune times evolve_pi steps of
+// lists against fewer rebuilds), the warps that share a block's sites in the
+// FP32 k-space force kernel.  gbrpmd_ctx_autotune times evolve_pi steps of
 // the context itself with candidate shapes, one parameter at a time from the
 // defaults (coordinate descent), restores the trajectory state after every
 // trial and keeps the fastest shape.  Results are cached for the process per
@@ -135,20 +136,22 @@ extern "C" {
 
 // Chooses the launch shapes of `ctx` for steps of (dt, beta) by timing
 // `steps` evolve_pi steps per candidate; the trajectory state is the same
-// afterwards.  out4 (optional): lanes per site (Ewald), lanes per oxygen (LJ),
-// molecules per MTS block (0: one wave over the SMs), skin fraction.
-int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double *out4) {
+// afterwards.  out5 (optional): lanes per site (Ewald), lanes per oxygen (LJ),
+// molecules per MTS block (0: one wave over the SMs), skin fraction, warps per
+// k-space force block.
+int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double *out5) {
   if (!c) return ctx_set_error(GB_E_ARG, "null context");
   if (steps < 1) return ctx_set_error(GB_E_ARG, "steps must be >= 1");
   const gb_params &P = c->P;
   const bool tunable = !ctx_rigid(c) && !c->nbaro &&
                        (c->rng_mode == GB_RNG_DEVICE || (P.therm != GB_THERM_PRG && P.therm != GB_THERM_PRL));
   auto report = [&]() {
-    if (out4) {
-      out4[0] = c->tune.ew_np;
-      out4[1] = c->tune.lj_np;
-      out4[2] = c->tune.mts_mpb;
-      out4[3] = c->list_skin;
+    if (out5) {
+      out5[0] = c->tune.ew_np;
+      out5[1] = c->tune.lj_np;
+      out5[2] = c->tune.mts_mpb;
+      out5[3] = c->list_skin;
+      out5[4] = c->tune.rf_g;
     }
     return GB_OK;
   };
@@ -190,6 +193,11 @@ int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double
     for (int np : {2, 8}) {
       Shape cand = best;
       cand.tune.lj_np = np;
+      probe(cand);
+    }
+    {
+      Shape cand = best;
+      cand.tune.rf_g = 16;
       probe(cand);
     }
   }
