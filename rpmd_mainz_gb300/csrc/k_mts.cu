@@ -214,7 +214,9 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_fused(MtsArgs a) {
 // taken relative to the molecule's oxygen centroid, so that FP32 holds them to
 // ~1e-7 bohr.
 template <int NB>
-__global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_mixed(MtsArgs a) {
+// Two blocks per SM: the FP32 modes need about half the registers of the FP64
+// kernel, so 128 per thread (a few spilled at nb = 64) give twice the warps.
+__global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
   using C = MtsCfg<NB>;
   extern __shared__ double sm[];
   const int T = blockDim.x;
@@ -460,10 +462,11 @@ void launch_nb(cudaStream_t s, MtsArgs a, bool mixed) {
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  // one wave of blocks over the SMs when the molecules fit, else MPB_MAX per
-  // block; a tuned count (gbrpmd_ctx_autotune) overrides it
-  a.mpb = a.mpb > 0 ? std::min(C::MPB_MAX, a.mpb)
-                    : std::max(1, std::min(C::MPB_MAX, (a.nm + nsm - 1) / std::max(nsm, 1)));
+  // one wave of blocks over the SMs when the molecules fit (two blocks per SM
+  // for the mixed kernel), else MPB_MAX per block; a tuned count
+  // (gbrpmd_ctx_autotune) overrides it
+  const int wave = std::max(nsm, 1) * (mixed ? 2 : 1);
+  a.mpb = a.mpb > 0 ? std::min(C::MPB_MAX, a.mpb) : std::max(1, std::min(C::MPB_MAX, (a.nm + wave - 1) / wave));
   const int T = (9 * a.mpb + 31) / 32 * 32;
   const unsigned grid = (unsigned)((a.nm + a.mpb - 1) / a.mpb);
   if (mixed) k_mts_mixed<NB><<<grid, T, mts_smem_mixed<NB>(T), s>>>(a);
