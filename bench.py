@@ -403,8 +403,8 @@ def run_replicas(args, torch):
     for s, ctx in zip(reps, ctxs):
         ch = ctx.autotune(s["dt"], s["beta"], steps=5)  # cached: returns the choice
         key = f"nm{s['nm']}_nb{s['nb']}"
-        shapes[key] = (f"ew_np={ch['ew_np']} lj_np={ch['lj_np']} rf_g={ch['rf_g']} mts_mpb={ch['mts_mpb']} "
-                       f"skin={ch['skin']}")
+        shapes[key] = (f"ew_np={ch['ew_np']} lj_np={ch['lj_np']} rf_g={ch['rf_g']} rf_ns={ch['rf_ns']} "
+                       f"mts_mpb={ch['mts_mpb']} skin={ch['skin']}")
     batch.step(args.warmup)
     batch.sync()
     step_ms = []

@@ -259,16 +259,17 @@ int gbrpmd_ctx_energies(gb_context *ctx, double *out5, double *vir, double *vir_
 /* Autotuner (no counterpart in the reference): times `steps` evolve_pi steps
    of (dt, beta) on this context per candidate launch shape -- lanes per site
    of the FP32 real-space Ewald kernel, lanes per oxygen of the FP32 LJ kernel,
-   warps per block of the FP32 k-space force kernel, molecules per block of
+   warps per block and sites per lane of the FP32 k-space force kernel,
+   molecules per block of
    the fused MTS kernel, pair-list skin -- one
    parameter at a time, keeps the fastest, and leaves the trajectory state as
    it found it.  Shapes are cached per (atoms, beads, precision, MTS,
    contraction, box kind, model) for the process.  Results change only by the
-   order of floating-point sums.  out5 (optional): the chosen lanes (Ewald),
+   order of floating-point sums.  out6 (optional): the chosen lanes (Ewald),
    lanes (LJ), molecules per MTS block (0: one wave over the SMs), skin, warps
-   per k-space force block.
+   per k-space force block, sites per lane of the k-space force kernel.
    Rigid, barostat and PRG/PRL contexts keep the defaults. */
-int gbrpmd_ctx_autotune(gb_context *ctx, double dt, double beta, int steps, double *out5);
+int gbrpmd_ctx_autotune(gb_context *ctx, double dt, double beta, int steps, double *out6);
 /* forgets the cached shapes */
 void gbrpmd_autotune_reset(void);
 /* Random stream owned by the context (no counterpart in the reference, whose

@@ -224,7 +224,7 @@ int gbrpmd_batch_step(gb_batch *b, int nsteps) {
   return GB_OK;
 }
 
-int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double *out5);  // tune.cpp
+int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double *out6);  // tune.cpp
 
 // launch shapes of every replica (gbrpmd_ctx_autotune; shapes seen before
 // come from the process-wide cache), then a fresh capture at the next step

@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
 constexpr int MSK_CHUNK = 128;  // sites per structure-factor block (FP32 partial sums)
 constexpr int MSK_G = 8;
 constexpr int MSK_T = 128;
-constexpr int MF_S = 32;  // sites per force block
+constexpr int MF_S = 32;  // sites per lane group of the force block (one warp's lanes; the kernel assumes 32)
 constexpr int MF_GMAX = 16;  // column shares (warps) per force block: 8 or 16 (tuned)
 constexpr int SIGN32 = (int)0x80000000u;
 
@@ -421,29 +421,34 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
 // the warps' per-site sums are added in FP64 in a fixed order
 // STAGED: the whole k-pair table (8 floats per pair) is copied to shared
 // memory first, so that the inner loop reads it with shared-memory broadcasts
-template <bool STAGED, int MF_G>
-__global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__restrict__ tab, int na, int kmax,
-                                                              int ncol, const KCol *__restrict__ cols, int nkp,
-                                                              const float4 *__restrict__ sk, double3 lat, double *g) {
-  // [3][K1][MF_S] float2 site tables, [MF_G][MF_S][3] double sums, then
+// NS sites per lane (block of 32 NS sites): every k-pair table entry loaded
+// from shared memory serves NS sites
+template <bool STAGED, int MF_G, int NS>
+__global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__restrict__ tab, int na,
+                                                                       int kmax, int ncol,
+                                                                       const KCol *__restrict__ cols, int nkp,
+                                                                       const float4 *__restrict__ sk, double3 lat,
+                                                                       double *g) {
+  constexpr int BS = MF_S * NS;  // sites per block
+  // [3][K1][BS] float2 site tables, [MF_G][BS][3] double sums, then
   // (STAGED) the k-pair table [nkp][2] float4
   extern __shared__ float4 smf[];
   float2 *stf = reinterpret_cast<float2 *>(smf);
   const int K1 = kmax + 1, K3 = 3 * K1;
   const int c = blockIdx.y;
-  const int t = threadIdx.x, sl = t % MF_S, wg = t / MF_S;
-  const int i0 = blockIdx.x * MF_S, i = i0 + sl;
-  for (int w = t; w < K3 * MF_S; w += MF_S * MF_G) {
-    const int e = w / MF_S, s2 = w % MF_S;
+  const int t = threadIdx.x, sl = t % 32, wg = t / 32;
+  const int i0 = blockIdx.x * BS;
+  for (int w = t; w < K3 * BS; w += 32 * MF_G) {
+    const int e = w / BS, s2 = w % BS;
     const int si = min(i0 + s2, na - 1);
     stf[w] = tab[((long long)c * na + si) * K3 + e];
   }
-  const int tab_f4 = (K3 * MF_S + 1) / 2;                       // float4 slots of the site tables
-  double *red = reinterpret_cast<double *>(smf + tab_f4);       // MF_G * MF_S * 3 doubles
-  float4 *sT = smf + tab_f4 + (MF_G * MF_S * 3 + 1) / 2;        // [nkp][2]
+  const int tab_f4 = (K3 * BS + 1) / 2;                       // float4 slots of the site tables
+  double *red = reinterpret_cast<double *>(smf + tab_f4);     // MF_G * BS * 3 doubles
+  float4 *sT = smf + tab_f4 + (MF_G * BS * 3 + 1) / 2;        // [nkp][2]
   if (STAGED) {
     const float4 *src = sk + (long long)c * nkp * 2;
-    for (int w = t; w < 2 * nkp; w += MF_S * MF_G) sT[w] = src[w];
+    for (int w = t; w < 2 * nkp; w += 32 * MF_G) sT[w] = src[w];
   }
   const long long kp_lo = (long long)wg * nkp / MF_G;
   const long long kp_hi = (long long)(wg + 1) * nkp / MF_G;
@@ -459,20 +464,26 @@ __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__
   const int col0 = first_col(kp_lo), col1 = first_col(kp_hi);
   __syncthreads();
   const float4 *T = STAGED ? sT : sk + (long long)c * nkp * 2;
-  float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
+  float sx[NS], sy[NS], sz[NS], ex[NS], ey[NS], ez[NS];
+#pragma unroll
+  for (int u = 0; u < NS; ++u) sx[u] = sy[u] = sz[u] = ex[u] = ey[u] = ez[u] = 0.f;
   for (int col = col0; col < col1; ++col) {
     const int4 ci4 = __ldg(reinterpret_cast<const int4 *>(cols + col));
     const int kx = ci4.x, ky = ci4.y, koff = ci4.z, mlo = ci4.w & 0xffff, mhi = ci4.w >> 16;
-    const float2 X = stf[kx * MF_S + sl], Y = stf[(K1 + abs(ky)) * MF_S + sl];
-    const float yi = flipf(Y.y, ky < 0 ? SIGN32 : 0);
-    const float cr = fmaf(X.x, Y.x, -X.y * yi);
-    const float ci = fmaf(X.x, yi, X.y * Y.x);
+    float cr[NS], ci[NS], ur[NS], ui[NS], vr[NS], vi[NS];
+#pragma unroll
+    for (int u = 0; u < NS; ++u) {
+      const int so = sl + 32 * u;
+      const float2 X = stf[kx * BS + so], Y = stf[(K1 + abs(ky)) * BS + so];
+      const float yi = flipf(Y.y, ky < 0 ? SIGN32 : 0);
+      cr[u] = fmaf(X.x, Y.x, -X.y * yi);
+      ci[u] = fmaf(X.x, yi, X.y * Y.x);
+      ur[u] = ui[u] = vr[u] = vi[u] = 0.f;
+    }
     const float4 *Tp = T + 2LL * (koff - mlo);
-    const float2 *Z = stf + 2 * K1 * MF_S + sl;
-    float ur = 0.f, ui = 0.f, vr = 0.f, vi = 0.f;
+    const float2 *Z = stf + 2 * K1 * BS + sl;
 #pragma unroll 4
     for (int m = mlo; m <= mhi; ++m) {
-      const float2 z = Z[m * MF_S];
       float4 t0, t1;
       if (STAGED) {
         t0 = Tp[2 * m];
@@ -481,24 +492,35 @@ __global__ void __launch_bounds__(MF_S * MF_G) k_recip_force_mx(const float2 *__
         t0 = __ldg(Tp + 2 * m);
         t1 = __ldg(Tp + 2 * m + 1);
       }
-      ur = fmaf(z.x, t0.x, fmaf(z.y, t0.w, ur));
-      ui = fmaf(z.x, t0.y, fmaf(z.y, t0.z, ui));
-      vr = fmaf(z.x, t1.x, fmaf(z.y, t1.y, vr));
-      vi = fmaf(z.x, t1.z, fmaf(z.y, t1.w, vi));
+#pragma unroll
+      for (int u = 0; u < NS; ++u) {
+        const float2 z = Z[m * BS + 32 * u];
+        ur[u] = fmaf(z.x, t0.x, fmaf(z.y, t0.w, ur[u]));
+        ui[u] = fmaf(z.x, t0.y, fmaf(z.y, t0.z, ui[u]));
+        vr[u] = fmaf(z.x, t1.x, fmaf(z.y, t1.y, vr[u]));
+        vi[u] = fmaf(z.x, t1.z, fmaf(z.y, t1.w, vi[u]));
+      }
     }
-    const float ts = -fmaf(cr, ui, ci * ur);
-    kadd(sx, ex, (float)kx * ts);
-    kadd(sy, ey, (float)ky * ts);
-    kadd(sz, ez, -fmaf(cr, vi, ci * vr));
+#pragma unroll
+    for (int u = 0; u < NS; ++u) {
+      const float ts = -fmaf(cr[u], ui[u], ci[u] * ur[u]);
+      kadd(sx[u], ex[u], (float)kx * ts);
+      kadd(sy[u], ey[u], (float)ky * ts);
+      kadd(sz[u], ez[u], -fmaf(cr[u], vi[u], ci[u] * vr[u]));
+    }
   }
-  red[(wg * MF_S + sl) * 3] = (double)sx - (double)ex;
-  red[(wg * MF_S + sl) * 3 + 1] = (double)sy - (double)ey;
-  red[(wg * MF_S + sl) * 3 + 2] = (double)sz - (double)ez;
+#pragma unroll
+  for (int u = 0; u < NS; ++u) {
+    const int so = sl + 32 * u;
+    red[(wg * BS + so) * 3] = (double)sx[u] - (double)ex[u];
+    red[(wg * BS + so) * 3 + 1] = (double)sy[u] - (double)ey[u];
+    red[(wg * BS + so) * 3 + 2] = (double)sz[u] - (double)ez[u];
+  }
   __syncthreads();
-  if (t < 3 * MF_S) {
-    const int s2 = t / 3, d = t % 3;
+  for (int w2 = t; w2 < 3 * BS; w2 += 32 * MF_G) {
+    const int s2 = w2 / 3, d = w2 % 3;
     double f = 0.0;
-    for (int w = 0; w < MF_G; ++w) f += red[(w * MF_S + s2) * 3 + d];
+    for (int w = 0; w < MF_G; ++w) f += red[(w * BS + s2) * 3 + d];
     if (i0 + s2 < na) g[((long long)c * na + i0 + s2) * 3 + d] += (d == 0 ? lat.x : d == 1 ? lat.y : lat.z) * f;
   }
 }
@@ -544,8 +566,10 @@ void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, in
 }
 
 size_t recip_sk_smem_mx(int kmax) { return sizeof(float2) * MSK_CHUNK * 3 * (kmax + 1); }
-size_t recip_force_smem_mx(int kmax, int nkp_staged) {
-  return sizeof(float4) * ((3 * (kmax + 1) * MF_S + 1) / 2 + (MF_GMAX * MF_S * 3 + 1) / 2 + 2 * (size_t)nkp_staged);
+// dynamic shared memory of k_recip_force_mx<., g, ns>
+size_t recip_force_smem_mx(int kmax, int nkp_staged, int g, int ns) {
+  const int bs = MF_S * ns;
+  return sizeof(float4) * ((3 * (kmax + 1) * bs + 1) / 2 + (g * bs * 3 + 1) / 2 + 2 * (size_t)nkp_staged);
 }
 
 // partial sums need nconf * nchunk * nkp float4 (half of the FP64 layout)
@@ -578,30 +602,45 @@ void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc) 
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
   if (c->nkp == 0) return;
   const int kmax = c->P.kmax;
-  dim3 grid(nblk(c->na, MF_S), B);
-  const size_t staged = recip_force_smem_mx(kmax, c->nkp);
-  auto go = [&](auto Gc) {
-    constexpr int G = decltype(Gc)::value;
+  auto go = [&](auto Gc, auto NSc) {
+    constexpr int G = decltype(Gc)::value, NS = decltype(NSc)::value;
+    static_assert(G <= MF_GMAX, "column shares");
+    const size_t staged = recip_force_smem_mx(kmax, c->nkp, G, NS);
+    dim3 grid(nblk(c->na, MF_S * NS), B);
     if (staged <= 160 * 1024)
-      k_recip_force_mx<true, G><<<grid, MF_S * G, staged, s>>>(
+      k_recip_force_mx<true, G, NS><<<grid, 32 * G, staged, s>>>(
           reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
           reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
     else
-      k_recip_force_mx<false, G><<<grid, MF_S * G, recip_force_smem_mx(kmax, 0), s>>>(
+      k_recip_force_mx<false, G, NS><<<grid, 32 * G, recip_force_smem_mx(kmax, 0, G, NS), s>>>(
           reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
           reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
   };
-  if (c->tune.rf_g == 16) go(std::integral_constant<int, 16>());
-  else go(std::integral_constant<int, 8>());
+  using I8 = std::integral_constant<int, 8>;
+  using I16 = std::integral_constant<int, 16>;
+  using N1 = std::integral_constant<int, 1>;
+  using N2 = std::integral_constant<int, 2>;
+  const bool g16 = c->tune.rf_g == 16, two = c->tune.rf_ns == 2;
+  if (g16) {
+    if (two) go(I16(), N2());
+    else go(I16(), N1());
+  } else {
+    if (two) go(I8(), N2());
+    else go(I8(), N1());
+  }
 }
 
 void recip_set_attributes_mx() {
   static bool done = false;
   if (done) return;
   cudaFuncSetAttribute(k_recip_sk_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<true, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<false, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<true, 16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<false, 16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<true, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<false, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<true, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_force_mx<false, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   done = true;
 }

@@ -7,7 +7,8 @@
 // reduction work for large ones), the molecules per block of the fused MTS
 // kernel (occupancy against the one-wave grid), and the pair-list skin (larger
 // lists against fewer rebuilds), the warps that share a block's sites in the
-// FP32 k-space force kernel.  gbrpmd_ctx_autotune times evolve_pi steps of
+// FP32 k-space force kernel and the sites each of its lanes carries (more
+// sites share each table load, fewer blocks fill the SMs).  gbrpmd_ctx_autotune times evolve_pi steps of
 // the context itself with candidate shapes, one parameter at a time from the
 // defaults (coordinate descent), restores the trajectory state after every
 // trial and keeps the fastest shape.  Results are cached for the process per
@@ -136,22 +137,23 @@ extern "C" {
 
 // Chooses the launch shapes of `ctx` for steps of (dt, beta) by timing
 // `steps` evolve_pi steps per candidate; the trajectory state is the same
-// afterwards.  out5 (optional): lanes per site (Ewald), lanes per oxygen (LJ),
+// afterwards.  out6 (optional): lanes per site (Ewald), lanes per oxygen (LJ),
 // molecules per MTS block (0: one wave over the SMs), skin fraction, warps per
-// k-space force block.
-int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double *out5) {
+// k-space force block, sites per lane of the k-space force kernel.
+int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double *out6) {
   if (!c) return ctx_set_error(GB_E_ARG, "null context");
   if (steps < 1) return ctx_set_error(GB_E_ARG, "steps must be >= 1");
   const gb_params &P = c->P;
   const bool tunable = !ctx_rigid(c) && !c->nbaro &&
                        (c->rng_mode == GB_RNG_DEVICE || (P.therm != GB_THERM_PRG && P.therm != GB_THERM_PRL));
   auto report = [&]() {
-    if (out5) {
-      out5[0] = c->tune.ew_np;
-      out5[1] = c->tune.lj_np;
-      out5[2] = c->tune.mts_mpb;
-      out5[3] = c->list_skin;
-      out5[4] = c->tune.rf_g;
+    if (out6) {
+      out6[0] = c->tune.ew_np;
+      out6[1] = c->tune.lj_np;
+      out6[2] = c->tune.mts_mpb;
+      out6[3] = c->list_skin;
+      out6[4] = c->tune.rf_g;
+      out6[5] = c->tune.rf_ns;
     }
     return GB_OK;
   };
@@ -198,6 +200,11 @@ int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double
     {
       Shape cand = best;
       cand.tune.rf_g = 16;
+      probe(cand);
+    }
+    {
+      Shape cand = best;
+      cand.tune.rf_ns = 2;
       probe(cand);
     }
   }

@@ -336,9 +336,10 @@ class Context:
 
     def autotune(self, dt, beta, steps=10):
         """Launch shapes timed on this context (gbrpmd_ctx_autotune); returns the choice."""
-        out = np.zeros(5)
+        out = np.zeros(6)
         _check(load().gbrpmd_ctx_autotune(self.h, C.c_double(dt), C.c_double(beta), int(steps), _ptr(out)))
-        return dict(ew_np=int(out[0]), lj_np=int(out[1]), mts_mpb=int(out[2]), skin=float(out[3]), rf_g=int(out[4]))
+        return dict(ew_np=int(out[0]), lj_np=int(out[1]), mts_mpb=int(out[2]), skin=float(out[3]), rf_g=int(out[4]),
+                    rf_ns=int(out[5]))
 
     def set_rng(self, idum):
         """Context-owned random stream for the PRG / PRL kicks of evolve()."""

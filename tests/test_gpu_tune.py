@@ -49,7 +49,7 @@ def test_autotune_keeps_state_and_trajectory(precision):
     choice = tuned.autotune(s["dt"], s["beta"], steps=4)
     assert choice["ew_np"] in (8, 16, 32) and choice["lj_np"] in (2, 4, 8)
     assert choice["mts_mpb"] in (0, 4, 8, 14, 28) and choice["skin"] in (0.05, 0.1, 0.15, 0.2)
-    assert choice["rf_g"] in (8, 16)
+    assert choice["rf_g"] in (8, 16) and choice["rf_ns"] in (1, 2)
     after = tuned.download()
     for a, b in zip(after, before):
         assert np.array_equal(a, b)
