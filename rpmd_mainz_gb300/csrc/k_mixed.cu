@@ -10,13 +10,17 @@
 //    real-space kernel walks the skin list itself and drops pairs beyond the
 //    cut-off with its FP32 distance (no per-step exact filter);
 //  * force and energy sums are compensated (Kahan) FP32 per thread, virials
-//    plain FP32 per thread; all of them FP64 across threads;
-//  * the reciprocal-space power tables come from the FP64 recurrence rounded
-//    to FP32; structure-factor partials are FP32 over 32 sites and FP64 over
-//    chunks; energy, virial and the k-space totals stay FP64.
+//    plain FP32 per thread; energies df (two-float) and virials FP32 within a
+//    warp, FP64 across warps (block_sum_df: no per-thread FP64 instruction);
+//  * the reciprocal-space power tables are FP32 sines and cosines of phases
+//    reduced in two-float arithmetic; structure-factor partials are FP32 over
+//    a chunk of sites and df over chunks; energy, virial and the k-space
+//    totals stay FP64.
+#include <cmath>
 #include <type_traits>
 
 #include "gb_common.cuh"
+#include "gb_df.cuh"
 #include "gb_kernels.h"
 
 namespace {
@@ -46,63 +50,6 @@ GB_D float dmin(float hi_a, float lo_a, float hi_b, float lo_b) {
   return (d - rintf(d)) + (lo_a - lo_b);
 }
 
-GB_D float warp_sum_f(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// block sums into acc[0] (energy: FP64 across lanes) and acc[1..NV-1]
-// (virial entries: FP32 within a warp, FP64 across warps); dst[k] < 0 skips
-template <int NV>
-GB_D void block_sum_mx(double e, const float (&v)[NV - 1], double *sh, double *acc, const int (&dst)[NV],
-                       const int (&dst2)[NV]) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  const double ew = warp_sum(e);
-  if (lane == 0) sh[warp * NV] = ew;
-#pragma unroll
-  for (int k = 1; k < NV; ++k) {
-    const float w = warp_sum_f(v[k - 1]);
-    if (lane == 0) sh[warp * NV + k] = (double)w;
-  }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double s2 = lane < nw ? sh[lane * NV + k] : 0.0;
-      s2 = warp_sum(s2);
-      if (lane == 0 && s2 != 0.0) {
-        atomicAdd(acc + dst[k], s2);
-        if (dst2[k] >= 0) atomicAdd(acc + dst2[k], s2);
-      }
-    }
-  }
-}
-
-// block sums of (v, xx, yx, zx, yy, zy, zz) into v, vir(1..3, 1..3) column-major
-GB_D void block_sum_sym7_mx(double (&vals)[7], double *sh, double *acc) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int k = 0; k < 7; ++k) {
-    const double v = warp_sum(vals[k]);
-    if (lane == 0) sh[warp * 7 + k] = v;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    constexpr int dst0[7] = {0, 1, 2, 3, 5, 6, 9};
-    constexpr int dst1[7] = {-1, -1, 4, 7, -1, 8, -1};
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-      double s2 = lane < nw ? sh[lane * 7 + k] : 0.0;
-      s2 = warp_sum(s2);
-      if (lane == 0 && s2 != 0.0) {
-        atomicAdd(acc + dst0[k], s2);
-        if (dst1[k] >= 0) atomicAdd(acc + dst1[k], s2);
-      }
-    }
-  }
-}
-
 // rwald (ewald_cubic.f90:78-233) in FP32 over a full list; g += gradient
 // (single writer per site), energy and virial halved for the double count.
 // The charge rides in hi.w.  Each lane takes every NP-th partner, four at a
@@ -115,11 +62,11 @@ template <int NP>
 __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                                                         int na, const int *__restrict__ count,
                                                         const int *__restrict__ idx, int cap, float alpha,
-                                                        float rcutsq, float3 bx, double *g, double *acc) {
-  __shared__ double sh[32 * 7];
+                                                        float sfac, float rcutsq, float3 bx, double *g,
+                                                        double *acc) {
+  __shared__ float sh[32 * 8];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
-  const float sfac = (float)(-2.0 / sqrt(acos(-1.0))) * alpha;
   const int c = blockIdx.y;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int i = (int)(tid / NP), sub = (int)(tid % NP);
@@ -182,14 +129,14 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
   const float fz = group_sum_f<NP>(sz - cz);
   if (active && sub == 0) {
     double *G = g + ((long long)c * na + i) * 3;
-    G[0] += (double)fx;
-    G[1] += (double)fy;
-    G[2] += (double)fz;
+    G[0] += f2d(fx);
+    G[1] += f2d(fy);
+    G[2] += f2d(fz);
   }
-  const float vir6[6] = {0.5f * vxx, 0.5f * vyx, 0.5f * vzx, 0.5f * vyy, 0.5f * vzy, 0.5f * vzz};
+  const float vir6[6] = {vxx, vyx, vzx, vyy, vzy, vzz};
   constexpr int dst[7] = {0, 1, 2, 3, 5, 6, 9};       // v, xx, yx, zx, yy, zy, zz
   constexpr int dst2[7] = {-1, -1, 4, 7, -1, 8, -1};  // mirrored xy, xz, yz
-  block_sum_mx<7>(0.5 * ((double)ev - (double)evc), vir6, sh, acc, dst, dst2);
+  block_sum_df<7>(ev, -evc, vir6, sh, acc, dst, dst2, 0.5, 0.5);  // halved: each pair from both ends
 }
 
 // lj_list / lj_basic (ljones.f90) in FP32 over a full oxygen list; bead pairs
@@ -199,7 +146,7 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
                                                 int npt, int nconf_list, const int *__restrict__ count,
                                                 const int *__restrict__ idx, int cap, float sigsq, float rcutsq,
                                                 float3 box, double dscale, double *out, double *acc) {
-  __shared__ double sh[32 * 10];
+  __shared__ float sh[32 * 11];
   const int c = blockIdx.y;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int o = (int)(tid / NP), sub = (int)(tid % NP);
@@ -253,16 +200,13 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
   const float fz = group_sum_f<NP>(sz - cz);
   if (active && sub == 0) {
     double *F = out + (long long)c * na * 3 + 9LL * o;
-    F[0] += dscale * (double)fx;
-    F[1] += dscale * (double)fy;
-    F[2] += dscale * (double)fz;
+    F[0] += dscale * f2d(fx);
+    F[1] += dscale * f2d(fy);
+    F[2] += dscale * f2d(fz);
   }
-  float vir9[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) vir9[k] = 0.5f * w[k];
   constexpr int dst[10] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9};
   constexpr int dst2[10] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
-  block_sum_mx<10>(0.5 * ((double)vsum - (double)vcmp), vir9, sh, acc, dst, dst2);
+  block_sum_df<10>(vsum, -vcmp, w, sh, acc, dst, dst2, 0.5, 0.5);  // halved: each pair from both ends
 }
 
 // ---- reciprocal space (kwald, ewald_cubic.f90:235-533), FP32 ----
@@ -275,27 +219,31 @@ constexpr int SIGN32 = (int)0x80000000u;
 
 GB_D float flipf(float v, int mask) { return __int_as_float(__float_as_int(v) ^ mask); }
 
-// FP64 recurrence (ewald_cubic.f90:254-286, ewald_noncubic.f90:296-336)
-// rounded to FP32; lat as in k_recip_tables
-__global__ void k_recip_tables_mx(const double *rs, const double *q, int na, int B, int kmax, double3 lat,
+// The power tables of ewald_cubic.f90:254-286 / ewald_noncubic.f90:296-336,
+// q e^{i k lat x} (x component) and e^{i k lat y}, e^{i k lat z}, one thread
+// per entry: the phase in periods, t = k x lat / (2 pi), is reduced modulo 1
+// in two-float arithmetic (exact product k * hi by FMA) and the entry is
+// sincospif(2 t) in FP32.  The reference's recurrence over k in FP64 rounded
+// to FP32 and this direct form differ by a few FP32 ulps.  per = lat / (2 pi).
+__global__ void k_recip_tables_mx(const double *rs, const double *q, int na, int B, int kmax, double3 per,
                                   float2 *tab) {
-  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= 3LL * na * B) return;
+  const int K1 = kmax + 1;
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= 3LL * na * B * K1) return;
+  const long long w = g / K1;
+  const int k = (int)(g - w * K1);
   const int ax = (int)(w % 3);
   const int s = (int)((w / 3) % na);
-  const double arg = (ax == 0 ? lat.x : ax == 1 ? lat.y : lat.z) * rs[w];
-  double sn, cs;
-  sincos(arg, &sn, &cs);
-  double pr = ax == 0 ? q[s] : 1.0, pi = 0.0;
-  float2 *t = tab + w * (kmax + 1);
-  t[0] = make_float2((float)pr, 0.f);
-  for (int k = 1; k <= kmax; ++k) {
-    const double nr = cs * pr - sn * pi;
-    const double ni = sn * pr + cs * pi;
-    pr = nr;
-    pi = ni;
-    t[k] = make_float2((float)pr, (float)pi);
-  }
+  float fh, fl;
+  d2df((ax == 0 ? per.x : ax == 1 ? per.y : per.z) * rs[w], fh, fl);
+  const float kf = (float)k;
+  const float pr = kf * fh;
+  const float pe = fmaf(kf, fh, -pr);  // k fh = pr + pe exactly
+  const float t = (pr - rintf(pr)) + fmaf(kf, fl, pe);
+  float sn, cs;
+  sincospif(2.0f * t, &sn, &cs);
+  const float a = ax == 0 ? __double2float_rn(q[s]) : 1.0f;
+  tab[g] = k == 0 ? make_float2(a, 0.f) : make_float2(a * cs, a * sn);
 }
 
 __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na, int kmax, int ngrp,
@@ -340,7 +288,8 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
     if (g < len) out[g] = make_float4(pr[g], pi[g], qr[g], qi[g]);
 }
 
-// FP64 sums of the chunk partials, energy and virial; FP32 force tables
+// df (two-float) sums of the chunk partials, FP64 energy and virial per k
+// pair (one warp per block), FP32 force tables
 // chunk slices per k pair in the weights kernel (SL warps per block): 16 for
 // many chunks, fewer when the configuration has few sites (idle warps otherwise)
 
@@ -348,35 +297,37 @@ template <int MW_SL>
 __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *sk_part, int nchunk, int nkp,
                                                                 const int4 *kpair, const double *kw, const double *kvir,
                                                                 float4 *sk, double *acc) {
-  __shared__ double part[4][MW_SL][32];
-  __shared__ double sh[MW_SL * 10];
+  __shared__ float part[8][MW_SL][32];  // df (hi, lo) of the four sums per slice
   const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
   const int c = blockIdx.y;
   const int k = blockIdx.x * 32 + lane;
-  double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
   if (k < nkp) {
     for (int ch = slice; ch < nchunk; ch += MW_SL) {
       const float4 p = sk_part[((long long)c * nchunk + ch) * nkp + k];
-      a0 += p.x;
-      a1 += p.y;
-      a2 += p.z;
-      a3 += p.w;
+      df_acc(h[0], l[0], p.x);
+      df_acc(h[1], l[1], p.y);
+      df_acc(h[2], l[2], p.z);
+      df_acc(h[3], l[3], p.w);
     }
   }
-  part[0][slice][lane] = a0;
-  part[1][slice][lane] = a1;
-  part[2][slice][lane] = a2;
-  part[3][slice][lane] = a3;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    part[2 * q][slice][lane] = h[q];
+    part[2 * q + 1][slice][lane] = l[q];
+  }
   __syncthreads();
+  if (slice != 0) return;  // warp 0 finishes: one FP64 chain per k pair
   double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  if (slice == 0 && k < nkp) {
-    double Pr = 0, Pi = 0, Qr = 0, Qi = 0;
-    for (int j = 0; j < MW_SL; ++j) {
-      Pr += part[0][j][lane];
-      Pi += part[1][j][lane];
-      Qr += part[2][j][lane];
-      Qi += part[3][j][lane];
+  if (k < nkp) {
+    double P[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float H = part[2 * q][0][lane], L = part[2 * q + 1][0][lane];
+      for (int j = 1; j < MW_SL; ++j) df_add(H, L, part[2 * q][j][lane], part[2 * q + 1][j][lane]);
+      P[q] = df2d(H, L);
     }
+    const double Pr = P[0], Pi = P[1], Qr = P[2], Qi = P[3];
     const int4 kv = kpair[k];
     const double w = kw[k];
     double et, ed = 0.0, Ar, Ai, Dr, Di;  // ed: et(+m) - et(-m)
@@ -413,12 +364,16 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
     o[0] = make_float4((float)Ar, (float)-Ai, (float)Dr, (float)Di);
     o[1] = make_float4((float)(m * Dr), (float)(m * Ai), (float)(-m * Di), (float)(m * Ar));
   }
-  block_sum_atomic<10>(vals, sh, acc);
+#pragma unroll
+  for (int e = 0; e < 10; ++e) {
+    const double v = warp_sum(vals[e]);
+    if (lane == 0 && v != 0.0) atomicAdd(acc + e, v);
+  }
 }
 
 // one block per 32 sites: its site tables are loaded into shared memory once,
 // and each of its MF_G warps takes a share of the columns (by k-pair count);
-// the warps' per-site sums are added in FP64 in a fixed order
+// the warps' per-site sums are added as df pairs in a fixed order
 // STAGED: the whole k-pair table (8 floats per pair) is copied to shared
 // memory first, so that the inner loop reads it with shared-memory broadcasts
 // NS sites per lane (block of 32 NS sites): every k-pair table entry loaded
@@ -430,7 +385,7 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
                                                                        const float4 *__restrict__ sk, double3 lat,
                                                                        double *g) {
   constexpr int BS = MF_S * NS;  // sites per block
-  // [3][K1][BS] float2 site tables, [MF_G][BS][3] double sums, then
+  // [3][K1][BS] float2 site tables, [MF_G][BS][3] df sums, then
   // (STAGED) the k-pair table [nkp][2] float4
   extern __shared__ float4 smf[];
   float2 *stf = reinterpret_cast<float2 *>(smf);
@@ -444,7 +399,7 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
     stf[w] = tab[((long long)c * na + si) * K3 + e];
   }
   const int tab_f4 = (K3 * BS + 1) / 2;                       // float4 slots of the site tables
-  double *red = reinterpret_cast<double *>(smf + tab_f4);     // MF_G * BS * 3 doubles
+  float2 *red = reinterpret_cast<float2 *>(smf + tab_f4);     // MF_G * BS * 3 df pairs
   float4 *sT = smf + tab_f4 + (MF_G * BS * 3 + 1) / 2;        // [nkp][2]
   if (STAGED) {
     const float4 *src = sk + (long long)c * nkp * 2;
@@ -512,16 +467,19 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
 #pragma unroll
   for (int u = 0; u < NS; ++u) {
     const int so = sl + 32 * u;
-    red[(wg * BS + so) * 3] = (double)sx[u] - (double)ex[u];
-    red[(wg * BS + so) * 3 + 1] = (double)sy[u] - (double)ey[u];
-    red[(wg * BS + so) * 3 + 2] = (double)sz[u] - (double)ez[u];
+    red[(wg * BS + so) * 3] = make_float2(sx[u], -ex[u]);
+    red[(wg * BS + so) * 3 + 1] = make_float2(sy[u], -ey[u]);
+    red[(wg * BS + so) * 3 + 2] = make_float2(sz[u], -ez[u]);
   }
   __syncthreads();
   for (int w2 = t; w2 < 3 * BS; w2 += 32 * MF_G) {
     const int s2 = w2 / 3, d = w2 % 3;
-    double f = 0.0;
-    for (int w = 0; w < MF_G; ++w) f += red[(w * BS + s2) * 3 + d];
-    if (i0 + s2 < na) g[((long long)c * na + i0 + s2) * 3 + d] += (d == 0 ? lat.x : d == 1 ? lat.y : lat.z) * f;
+    float H = 0.f, L = 0.f;
+    for (int w = 0; w < MF_G; ++w) {
+      const float2 r = red[(w * BS + s2) * 3 + d];
+      df_add(H, L, r.x, r.y);
+    }
+    if (i0 + s2 < na) g[((long long)c * na + i0 + s2) * 3 + d] += (d == 0 ? lat.x : d == 1 ? lat.y : lat.z) * df2d(H, L);
   }
 }
 
@@ -542,8 +500,9 @@ void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, in
   auto go = [&](auto NPc) {
     constexpr int NP = decltype(NPc)::value;
     dim3 grid(nblk((long long)na * NP, MX_T), B);
-    k_ewald_real_mx<NP><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, (float)rcutsq, bx,
-                                              g, acc);
+    const float sfac = (float)(-2.0 * alpha / std::sqrt(std::acos(-1.0)));  // d erfc(alpha r) / dr factor
+    k_ewald_real_mx<NP><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
+                                              (float)rcutsq, bx, g, acc);
   };
   if (np == 8) go(std::integral_constant<int, 8>());
   else if (np == 32) go(std::integral_constant<int, 32>());
@@ -578,7 +537,10 @@ void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const d
   const int kmax = c->P.kmax;
   const long long nw = 3LL * c->na * B;
   float2 *tab = reinterpret_cast<float2 *>(c->ktab);
-  k_recip_tables_mx<<<nblk(nw, 128), 128, 0, s>>>(rs, q, c->na, B, kmax, recip_lat(c), tab);
+  const double3 lat = recip_lat(c);
+  const double ot = 0.5 / std::acos(-1.0);
+  k_recip_tables_mx<<<nblk(nw * (kmax + 1), 256), 256, 0, s>>>(rs, q, c->na, B, kmax,
+                                                               make_double3(lat.x * ot, lat.y * ot, lat.z * ot), tab);
   const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
   dim3 grid(nblk(c->ngrp, MSK_T), nchunk, B);
   k_recip_sk_mx<<<grid, MSK_T, recip_sk_smem_mx(kmax), s>>>(tab, c->na, kmax, c->ngrp, c->kgrp, c->nkp, nchunk,

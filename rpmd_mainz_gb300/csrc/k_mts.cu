@@ -13,6 +13,7 @@
 // one read of p, r, dvdr, dvdr2 (dvdr once more per substep for the estimator)
 // and one write of p, r, rnm, dvdr2.
 #include "gb_common.cuh"
+#include "gb_df.cuh"
 #include "gb_fft.cuh"
 #include "gb_intra.cuh"
 #include "gb_kernels.h"
@@ -42,6 +43,7 @@ struct MtsArgs {
   double *acc_int, *acc_ke;
   int na, nm, mts, model, mpb;
   double halfdt, dtsmall, halfdtsmall;
+  float hdt_h, hdt_l, hds_h, hds_l;  // halfdt and halfdtsmall as FP32 pairs (mixed kernel)
   IntraPar ip;
 };
 
@@ -301,7 +303,7 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
     x0 = to_modes(xf);
   }
 
-  double e_last = 0.0, q1 = 0.0, q2 = 0.0;
+  float e_lh = 0.f, e_ll = 0.f, q1h = 0.f, q1l = 0.f, q2h = 0.f, q2l = 0.f;  // df sums
   float vir[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float off = 0.f;  // this row's centroid minus its oxygen's centroid
   for (int im = 1; im <= a.mts; ++im) {
@@ -321,7 +323,11 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
     const double cen = sc * x0;
     s_cen[t] = cen;
     __syncthreads();
-    off = (float)(cen - s_cen[orow]);
+    {
+      float oh, ol;
+      d2df(cen - s_cen[orow], oh, ol);
+      off = oh + ol;
+    }
     {  // bead positions relative to the oxygen centroid (evolve_pi.f90:141-145)
       float *dst = s_dev + t * C::LD;
       if (im == a.mts) {  // the last substep's positions are the new state: split tables,
@@ -330,7 +336,7 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
         gb_hc2r_s<NB, float, true>([&](int j) { return j ? xf[j] : 0.f; },
                                    [&](int k, float v) {
                                      dst[k] = off + v;
-                                     if (valid) gr[S * k] = cen + (double)v;
+                                     if (valid) gr[S * k] = cen + f2d(v);
                                    },
                                    s_tw, s_twi, s_tw_l, s_twi_l);
       } else {
@@ -339,7 +345,7 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
       }
     }
     __syncthreads();
-    double e_sub = 0.0;
+    float esh = 0.f, esl = 0.f;
     for (int idx = t; idx < mpb * NB; idx += T) {
       const int mm = idx / NB, j = idx % NB;
       const bool w = m0 + mm < a.nm;
@@ -350,12 +356,12 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
 #pragma unroll
       for (int d = 0; d < 9; ++d) s_f2[(mm * 9 + d) * C::LD + j] = fm[d];
       if (w) {
-        e_sub += (double)e;
+        df_acc(esh, esl, e);
 #pragma unroll
         for (int d = 0; d < 9; ++d) vir[d] += vm[d];
       }
     }
-    if (im == a.mts) e_last = e_sub;
+    if (im == a.mts) e_lh = esh, e_ll = esl;
     __syncthreads();
     {
       const float *dev_row = s_dev + t * C::LD;
@@ -368,8 +374,8 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
           a1 += dr * dv_row[j];
           a2 += dr * f2_row[j];
         }
-        q1 += (double)a1;
-        q2 += (double)a2;
+        df_acc(q1h, q1l, a1);
+        df_acc(q2h, q2l, a2);
       }
       if (im != a.mts) {  // FT(dvdr2) and p -= dtsmall dvdr2 (evolve_pi.f90:156-159)
         const float dtsf = (float)a.dtsmall;
@@ -380,7 +386,7 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
                                else f0 = v;
                              },
                              s_tw, s_twf);
-        p0 = p0 - a.dtsmall * (double)f0;
+        p0 = p0 - a.dtsmall * f2d(f0);
       }
     }
     if (im != a.mts) __syncthreads();
@@ -394,38 +400,51 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
     double *gp = a.p + row;
     gb_hc2r_s<NB, float, true>([&](int j) { return j ? pf[j] : 0.f; },
                                [&](int k, float v) {
-                                 if (valid) gp[S * k] = pc + (double)fmaf(-hds, f2_row[k], v);
+                                 if (valid) gp[S * k] = pc + f2d(fmaf(-hds, f2_row[k], v));
                                },
                                s_tw, s_twi, s_tw_l, s_twi_l);
     if (valid) {
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
-        a.rnm[row + S * j] = j ? (double)xf[j] : x0;
-        a.dvdr2[row + S * j] = (double)f2_row[j];
+        a.rnm[row + S * j] = j ? f2d(xf[j]) : x0;
+        a.dvdr2[row + S * j] = f2d(f2_row[j]);
       }
     }
   }
-  double red[18];
-  red[0] = e_last;
-#pragma unroll
-  for (int d = 0; d < 9; ++d) red[1 + d] = (double)vir[d];
-  red[10] = q1;
-  red[11] = q2;
+  // block totals: df / FP32 warp sums, FP64 across warps (threads 0..17)
+  float rh[9], rl[9];  // energy, q1, q2, q1 by axis, q2 by axis
+  rh[0] = e_lh, rl[0] = e_ll;
+  rh[1] = q1h, rl[1] = q1l;
+  rh[2] = q2h, rl[2] = q2l;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    red[12 + d] = d == xyz ? q1 : 0.0;
-    red[15 + d] = d == xyz ? q2 : 0.0;
+    rh[3 + d] = d == xyz ? q1h : 0.f, rl[3 + d] = d == xyz ? q1l : 0.f;
+    rh[6 + d] = d == xyz ? q2h : 0.f, rl[6 + d] = d == xyz ? q2l : 0.f;
   }
   const int lane = t & 31, warp = t >> 5, nw = (T + 31) / 32;
+  float *s_rf = reinterpret_cast<float *>(s_red);  // [32 warps][36] floats in the [32][18] doubles
 #pragma unroll
-  for (int i = 0; i < 18; ++i) {
-    double v = warp_sum(red[i]);
-    if (lane == 0) s_red[warp * 18 + i] = v;
+  for (int i = 0; i < 9; ++i) warp_sum_df(rh[i], rl[i]);
+#pragma unroll
+  for (int d = 0; d < 9; ++d) vir[d] = warp_sum_f32(vir[d]);
+  if (lane == 0) {
+    float *o = s_rf + warp * 36;
+    // slots 2i, 2i+1: df values in the order of the 18 totals below
+    o[0] = rh[0], o[1] = rl[0];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) o[2 + 2 * d] = vir[d], o[3 + 2 * d] = 0.f;
+    o[20] = rh[1], o[21] = rl[1];
+    o[22] = rh[2], o[23] = rl[2];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      o[24 + 2 * d] = rh[3 + d], o[25 + 2 * d] = rl[3 + d];
+      o[30 + 2 * d] = rh[6 + d], o[31 + 2 * d] = rl[6 + d];
+    }
   }
   __syncthreads();
-  if (t < 18) {
+  if (t < 18) {  // 0 energy, 1..9 virial, 10, 11 q1, q2, 12..14 q1 by axis, 15..17 q2 by axis
     double s2 = 0.0;
-    for (int w = 0; w < nw; ++w) s2 += s_red[w * 18 + t];
+    for (int w = 0; w < nw; ++w) s2 += df2d(s_rf[w * 36 + 2 * t], s_rf[w * 36 + 2 * t + 1]);
     if (s2 != 0.0) {
       if (t < 10) atomicAdd(a.acc_int + t, s2);
       else if (t < 12) atomicAdd(a.acc_ke + (t - 10), s2);
@@ -503,6 +522,12 @@ void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used) {
   a.halfdt = 0.5 * dt;
   a.dtsmall = dt / (double)c->P.mts;
   a.halfdtsmall = 0.5 * a.dtsmall;
+  auto split = [](double v, float &h, float &l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+  };
+  split(a.halfdt, a.hdt_h, a.hdt_l);
+  split(a.halfdtsmall, a.hds_h, a.hds_l);
   a.ip.reoh = c->P.reoh;
   a.ip.theta = c->P.theta;
   a.ip.rehh = 2.0 * sin(0.5 * c->P.theta) * c->P.reoh;
