@@ -187,8 +187,9 @@ void ctx_free(gb_context *c) {
                   (void *)c->kpair, (void *)c->kw, (void *)c->kvir, (void *)c->ktab, (void *)c->sk_part, (void *)c->sk,
                   (void *)c->tw_nb, (void *)c->tw_c1, (void *)c->tw_c2})
     if (p) cudaFree(p);
-  for (SkinList &L : c->sl)
-    for (void *p : {(void *)L.pl.idx, (void *)L.pl.count, (void *)L.ref, (void *)L.flag, (void *)L.rebuilds})
+  for (SkinList &L : c->sl)  // the cell offsets and per-point cell arrays live in ccount and spos
+    for (void *p : {(void *)L.pl.idx, (void *)L.pl.count, (void *)L.ref, (void *)L.flag, (void *)L.rebuilds,
+                    (void *)L.cells.ccount, (void *)L.cells.spos, (void *)L.cells.ticket})
       if (p) cudaFree(p);
   if (c->h_acc) cudaFreeHost(c->h_acc);
   if (c->h_status) cudaFreeHost(c->h_status);

@@ -26,8 +26,22 @@ struct PairList {
 // A pair list kept at cut-off + skin and rebuilt only when some point has moved
 // more than skin/2 since its last rebuild (the decision is taken on the device);
 // every use filters it into the exact list of pairs within the cut-off.
+// cell sort of a superset build (k_pairs.cu): on when list_cell_grid finds a
+// stencil that covers a small enough share of the box
+struct CellSort {
+  bool on = false;
+  int nc[3] = {0, 0, 0}, R = 1;
+  int *ccount = nullptr;         // [nconf][ncell], zero between steps
+  int *cstart = nullptr;         // [nconf][ncell + 1]
+  int *cellid = nullptr, *crank = nullptr, *sidx = nullptr;  // [nconf][npt]
+  float4 *spos = nullptr;        // [nconf][npt]
+  unsigned *ticket = nullptr;    // blocks done in the count kernel
+  size_t cell_bytes = 0, pt_bytes = 0;
+};
+
 struct SkinList {
   PairList pl;                   // superset: pairs within cut-off + skin at the last rebuild
+  CellSort cells;
   size_t idx_bytes = 0, cnt_bytes = 0;
   double *ref = nullptr;         // [nconf][npt][3] positions at the last rebuild
   size_t ref_bytes = 0;

@@ -15,6 +15,9 @@
 // list, keep the point's own force in registers and scatter the partner's force
 // with FP64 atomics; energy and virial are reduced per block and added to an
 // accumulator slot.
+#include <algorithm>
+#include <cmath>
+
 #include "gb_common.cuh"
 #include "gb_kernels.h"
 
@@ -145,6 +148,179 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
   }
   if (i < npt && nst > 0) flush();
   if (over) atomicOr(status, ST_LIST_OVERFLOW);
+}
+
+// ---- cell-sorted build (skin supersets) ----
+// The wrapped fractional box is cut into nx * ny * nz cells of side at least
+// 1/R of the largest accepted distance, so that every pair within it joins
+// points whose cells differ by at most R per axis (R = 1..3, nx, ny, nz >=
+// 2R + 1: the (2R+1)^3 stencil cells are distinct).  Every step k_cell_count
+// takes the skin test (moved points) and counts the points per cell; its last
+// block turns the counts into cell offsets when a rebuild is due and clears
+// them.  On a rebuild k_cell_scatter writes the points in cell order and
+// k_build_sorted runs one warp per point: the (2R+1)^2 x-rows of stencil
+// cells are contiguous runs of the cell order, which the lanes read in
+// coalesced 32-slot steps; hits are appended through a ballot (no atomics).
+// The FP32 prefilter and the FP64 band test are those of k_build_list2.
+struct CellSortDev {
+  int nx, ny, nz, R;
+  int *ccount;     // [nconf][ncell], zero between steps
+  int *cstart;     // [nconf][ncell + 1]
+  int *cellid;     // [nconf][npt]
+  int *crank;      // [nconf][npt] rank in the cell (arbitrary order)
+  float4 *spos;    // [nconf][npt] fractional positions in cell order
+  int *sidx;       // [nconf][npt] point of each cell-order slot
+  unsigned *ticket;
+};
+
+GB_D int cell_of(float u, int n) { return min((int)(u * (float)n), n - 1); }
+
+__global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, const float4 *frac, CellSortDev cs,
+                                                    const double *ref, double lim2, int check, unsigned *flag) {
+  __shared__ bool last;
+  __shared__ int part[256];
+  const long long n = (long long)nconf * g.npt;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int ncell = cs.nx * cs.ny * cs.nz;
+  bool moved = false;
+  if (t < n) {
+    const int c = (int)(t / g.npt), i = (int)(t % g.npt);
+    if (check) {
+      const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
+      const double *r0 = ref + 3 * t;
+      const double dx = x[0] - r0[0], dy = x[1] - r0[1], dz = x[2] - r0[2];
+      moved = !(dx * dx + dy * dy + dz * dz <= lim2);  // NaN counts as moved
+    }
+    const float4 f = frac[t];
+    const int cell = (cell_of(f.z, cs.nz) * cs.ny + cell_of(f.y, cs.ny)) * cs.nx + cell_of(f.x, cs.nx);
+    cs.cellid[t] = cell;
+    cs.crank[t] = atomicAdd(cs.ccount + (long long)c * ncell + cell, 1);
+  }
+  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(cs.ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const bool rebuild = *(volatile unsigned *)flag != 0u;
+  volatile int *cnt = cs.ccount;
+  for (int c = 0; c < nconf; ++c) {
+    volatile int *cc = cnt + (long long)c * ncell;
+    if (rebuild) {  // exclusive scan: contiguous chunks per thread, then the chunk offsets
+      const int per = (ncell + 255) / 256, a = threadIdx.x * per, b = min(ncell, a + per);
+      int sum = 0;
+      for (int k = a; k < b; ++k) sum += cc[k];
+      part[threadIdx.x] = sum;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int run = 0;
+        for (int k = 0; k < 256; ++k) {
+          const int v = part[k];
+          part[k] = run;
+          run += v;
+        }
+      }
+      __syncthreads();
+      int run = part[threadIdx.x];
+      int *st = cs.cstart + (long long)c * (ncell + 1);
+      for (int k = a; k < b; ++k) {
+        st[k] = run;
+        run += cc[k];
+      }
+      if (threadIdx.x == 255) st[ncell] = run;
+      __syncthreads();
+    }
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) cc[k] = 0;
+  }
+  if (threadIdx.x == 0) *cs.ticket = 0u;
+}
+
+__global__ void k_cell_scatter(int npt, int nconf, const float4 *frac, CellSortDev cs, int *lcount,
+                               const unsigned *gate) {
+  if (*gate == 0u) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nconf * npt) return;
+  lcount[t] = 0;
+  const int c = (int)(t / npt), i = (int)(t % npt);
+  const int ncell = cs.nx * cs.ny * cs.nz;
+  const long long pos = (long long)c * npt + cs.cstart[(long long)c * (ncell + 1) + cs.cellid[t]] + cs.crank[t];
+  cs.spos[pos] = frac[t];
+  cs.sidx[pos] = i;
+}
+
+template <bool FULL, bool EXCL>
+__global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, CellSortDev cs, int *count, int *idx,
+                                                       int cap, float3 len, float thr_lo, float thr_hi,
+                                                       unsigned *status, const unsigned *gate) {
+  if (*gate == 0u) return;
+  const int npt = g.npt;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per point
+  const int lane = threadIdx.x & 31;
+  if (w >= (long long)nconf * npt) return;  // the whole warp
+  const int c = (int)(w / npt);
+  const int kk = (int)(w - (long long)c * npt);
+  const int ncell = cs.nx * cs.ny * cs.nz;
+  const float4 *sp = cs.spos + (long long)c * npt;
+  const int *si = cs.sidx + (long long)c * npt;
+  const int *st = cs.cstart + (long long)c * (ncell + 1);
+  const int i = si[kk];
+  const float4 fi = sp[kk];
+  const double *base = g.pos + c * g.cstride;
+  const double *xi = base + (long long)i * g.pstride;
+  const double pi[3] = {xi[0], xi[1], xi[2]};
+  const int x0 = cell_of(fi.x, cs.nx), y0 = cell_of(fi.y, cs.ny), z0 = cell_of(fi.z, cs.nz);
+  int *my = idx + ((long long)c * npt + i) * cap;
+  int n = 0;  // the same in every lane
+  // lanes take consecutive cell-order slots (coalesced); hits keep slot order
+  auto scan = [&](int k0, int k1) {
+    for (int kb = k0; kb < k1; kb += 32) {
+      const int k = kb + lane;
+      bool hit = false;
+      int j = 0;
+      if (k < k1) {
+        const float4 fj = sp[k];
+        float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
+        dx = (dx - rintf(dx)) * len.x;
+        dy = (dy - rintf(dy)) * len.y;
+        dz = (dz - rintf(dz)) * len.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 < thr_hi) {
+          j = si[k];
+          hit = j != i && (FULL || (i < j) == (((i + j) & 1) != 0)) && (!EXCL || (i / 3) != (j / 3)) &&
+                (d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride));
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (hit) {
+        const int pos = n + __popc(m & ((1u << lane) - 1u));
+        if (pos < cap) my[pos] = j;
+      }
+      n += __popc(m);
+    }
+  };
+  const int R = cs.R;
+  for (int oz = -R; oz <= R; ++oz) {
+    const int z = (z0 + oz + cs.nz) % cs.nz;
+    for (int oy = -R; oy <= R; ++oy) {
+      const int y = (y0 + oy + cs.ny) % cs.ny;
+      const int row = (z * cs.ny + y) * cs.nx;
+      const int xa = x0 - R, xb = x0 + R;  // the x cells, wrapped into one or two runs
+      if (xa >= 0 && xb < cs.nx) {
+        scan(st[row + xa], st[row + xb + 1]);
+      } else if (xa < 0) {
+        scan(st[row], st[row + xb + 1]);
+        scan(st[row + cs.nx + xa], st[row + cs.nx]);
+      } else {
+        scan(st[row + xa], st[row + cs.nx]);
+        scan(st[row], st[row + xb - cs.nx + 1]);
+      }
+    }
+  }
+  if (lane == 0) {
+    count[(long long)c * npt + i] = n;
+    if (n > cap) atomicOr(status, ST_LIST_OVERFLOW);
+  }
 }
 
 // ---- skin lists ----
@@ -620,6 +796,69 @@ void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref,
                       unsigned *rebuilds) {
   const long long n = (long long)nconf * g.npt;
   k_skin_save<<<nblk(n, 256), 256, 0, s>>>(g, nconf, ref, flag, rebuilds);
+}
+
+// The cell grid of a superset build: R = 1..3 cells per largest accepted
+// distance, the R whose stencil covers the smallest share of the box; false
+// when no R gives 2R + 1 cells per axis or the stencil would cover more than
+// 60 % of the box (the all-pairs build is used)
+bool list_cell_grid(const PairGeom &g, int nc[3], int *R) {
+  float3 len;
+  float thr_lo, thr_hi;
+  list_thresholds(g, &len, &thr_lo, &thr_hi);
+  const double side = std::sqrt((double)thr_hi) * (1.0 + 1e-5);
+  const double L[3] = {len.x, len.y, len.z};
+  double best = 0.6;
+  bool found = false;
+  for (int r = 1; r <= 3; ++r) {
+    int n[3];
+    double share = 1.0;
+    bool ok = true;
+    for (int d = 0; d < 3; ++d) {
+      n[d] = (int)std::min(std::floor(L[d] * r / side), 128.0);
+      ok = ok && n[d] >= 2 * r + 1;
+      share *= (2.0 * r + 1.0) / std::max(n[d], 1);
+    }
+    if (ok && share < best) {
+      best = share;
+      found = true;
+      *R = r;
+      for (int d = 0; d < 3; ++d) nc[d] = n[d];
+    }
+  }
+  return found;
+}
+
+// skin test and cell counts (every step), then, gated by flag, the cell-order
+// scatter (which also zeroes the list counts) and the build
+void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, const CellSort &cs,
+                       const double *ref, double lim2, int check, unsigned *flag) {
+  CellSortDev d{cs.nc[0], cs.nc[1], cs.nc[2], cs.R, cs.ccount, cs.cstart, cs.cellid, cs.crank, cs.spos, cs.sidx,
+                cs.ticket};
+  const long long n = (long long)nconf * g.npt;
+  k_cell_count<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, d, ref, lim2, check, flag);
+}
+
+void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
+                         unsigned *status, const unsigned *gate, const CellSort &cs) {
+  float3 len;
+  float thr_lo, thr_hi;
+  list_thresholds(g, &len, &thr_lo, &thr_hi);
+  CellSortDev d{cs.nc[0], cs.nc[1], cs.nc[2], cs.R, cs.ccount, cs.cstart, cs.cellid, cs.crank, cs.spos, cs.sidx,
+                cs.ticket};
+  const long long n = (long long)nconf * g.npt;
+  k_cell_scatter<<<nblk(n, 256), 256, 0, s>>>(g.npt, nconf, frac, d, pl.count, gate);
+  auto go = [&](auto kern) {
+    kern<<<nblk(32 * n, LB_T), LB_T, 0, s>>>(g, nconf, d, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status,
+                                             gate);
+  };
+  if (g.full) {
+    if (g.excl_mol) go(k_build_sorted<true, true>);
+    else go(k_build_sorted<true, false>);
+  } else {
+    if (g.excl_mol) go(k_build_sorted<false, true>);
+    else go(k_build_sorted<false, false>);
+  }
 }
 
 void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,

@@ -232,17 +232,60 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     S.pl.nconf = nconf;
     S.pl.npt = g.npt;
     S.pl.cap = cap;
+    // cell sort for the rebuilds when a stencil covers a small share of the box
+    PairGeom gsc = g;
+    gsc.rcutsq = scut * scut;
+    CellSort &cs = S.cells;
+    cs.on = list_cell_grid(gsc, cs.nc, &cs.R);
+    if (cs.on) {
+      const size_t ncell = (size_t)cs.nc[0] * cs.nc[1] * cs.nc[2];
+      const size_t need_cell = sizeof(int) * (size_t)nconf * (2 * ncell + 1);  // counts, then offsets
+      const size_t need_pt = (3 * sizeof(int) + sizeof(float4)) * (size_t)nconf * g.npt;
+      if (need_cell > cs.cell_bytes) {
+        if (cs.ccount) cudaFree(cs.ccount);
+        cs.ccount = nullptr;
+        cs.cell_bytes = 0;
+        CK(cudaMalloc(&cs.ccount, need_cell));
+        cs.cell_bytes = need_cell;
+      }
+      if (need_pt > cs.pt_bytes) {
+        if (cs.spos) cudaFree(cs.spos);
+        cs.spos = nullptr;
+        cs.pt_bytes = 0;
+        CK(cudaMalloc(&cs.spos, need_pt));
+        cs.pt_bytes = need_pt;
+      }
+      if (!cs.ticket) CK(cudaMalloc(&cs.ticket, sizeof(unsigned)));
+      cs.cstart = cs.ccount + (size_t)nconf * ncell;
+      const size_t np = (size_t)nconf * g.npt;
+      cs.cellid = reinterpret_cast<int *>(cs.spos + np);
+      cs.crank = cs.cellid + np;
+      cs.sidx = cs.crank + np;
+      CK(cudaMemsetAsync(cs.ccount, 0, need_cell, c->stream));
+      CK(cudaMemsetAsync(cs.ticket, 0, sizeof(unsigned), c->stream));
+    }
   }
   CK(cudaMemsetAsync(S.flag, same ? 0 : 1, sizeof(unsigned), c->stream));
   int n = 1;
-  if (same) {  // rebuild when a point moved by more than skin/2 (a hair less, for rounding)
-    const double lim = 0.5 * skin * (1.0 - 1e-9);
-    launch_skin_check(c->stream, g, nconf, S.ref, lim * lim, S.flag);
-    n += 1;
-  }
+  // rebuild when a point moved by more than skin/2 (a hair less, for rounding)
+  const double lim = 0.5 * skin * (1.0 - 1e-9);
   PairGeom gs = g;
   gs.rcutsq = scut * scut;
-  launch_build_list(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag);
+  if (S.cells.on) {  // skin test and cell counts in one kernel, then the gated sort and build
+    cudaError_t e0 = cudaGetLastError();
+    if (e0 != cudaSuccess) return ctx_check_cuda(e0, "a launch before the cell count");
+    launch_cell_count(c->stream, g, nconf, c->rs32, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag);
+    if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell count launch");
+    launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells);
+    if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell build launch");
+    n += 1;
+  } else {
+    if (same) {
+      launch_skin_check(c->stream, g, nconf, S.ref, lim * lim, S.flag);
+      n += 1;
+    }
+    launch_build_list(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag);
+  }
   launch_skin_save(c->stream, g, nconf, S.ref, S.flag, S.rebuilds);
   n += 3;
   if (superset && use) {
