@@ -1,7 +1,11 @@
 // k_modes.cu -- normal-mode transforms, free ring-polymer propagation,
 // ring-polymer contraction, intramolecular forces and the virial kinetic
 // energy estimator (FP64), one thread per coordinate row or per molecule.
+#include <cmath>
+#include <type_traits>
+
 #include "gb_common.cuh"
+#include "gb_df.cuh"
 #include "gb_fft.cuh"
 #include "gb_intra.cuh"
 #include "gb_kernels.h"
@@ -66,7 +70,7 @@ __global__ void k_copy(double *dst, const double *src, long long n) {
 // ring_contract (evolve_pi.f90:405-431): keep modes 0, 1..h, nb-h..nb-1 of
 // rnm, HC2R of length nbc, scale 1/sqrt(nbc) then sqrt(nbc/nb)
 __global__ void k_ring_contract(const double *rnm, double *rb, int na, int nb, int nbc,
-                                const double *tw_c) {
+                                const double *tw_c, double s1, double s2) {
   const long long S = 3LL * na;
   const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= S) return;
@@ -78,7 +82,6 @@ __global__ void k_ring_contract(const double *rnm, double *rb, int na, int nb, i
     x[nbc - k] = rnm[row + S * (nb - k)];
   }
   gb_hc2r_direct(x, y, nbc, tw_c);
-  const double s1 = sqrt(1.0 / (double)nbc), s2 = sqrt((double)nbc / (double)nb);
   for (int j = 0; j < nbc; ++j) rb[row + S * j] = s2 * (s1 * y[j]);
 }
 
@@ -136,12 +139,14 @@ __global__ void k_expand_forces(double *dvdr, const double *fb1, int nbc1, const
 // (force_contract, evolve_pi.f90:377-403), and each bead's value is the dot
 // product with a per-bead table E[j] = sqrt(1/nb) (1, 2 cos(2 pi jk/nb),
 // -2 sin(2 pi jk/nb), k = 1..HM) held in shared memory.  R = float runs the
-// dot product in FP32 (mixed precision); the kick stays FP64.
+// contraction and the dot product in FP32 (mixed precision; FP64 loads and
+// stores through the integer conversions of gb_df.cuh); the kick stays FP64.
 // A block takes XR coordinate rows: XR threads reduce the rows' contracted
 // forces to coefficients (shared memory), then all XT threads expand them, four
 // threads per row each over a quarter of the beads, consecutive rows in
 // consecutive lanes so that every bead plane is written coalesced.
-// sc[t] = (sqrt(1/nbc_t), sqrt(nb/nbc_t)) of the two contracted terms.
+// sc[t] = (sqrt(1/nbc_t), sqrt(nb/nbc_t)) of the two contracted terms, sc =
+// sqrt(1/nb) (from the host: no per-thread FP64 square roots).
 constexpr int XR = 32;
 constexpr int XT = 4 * XR;
 
@@ -150,12 +155,12 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
                                                      const double *fb2, int nbc2, const double *tw_c2,
                                                      const double *e1, const double *e2, const double *e3, double *p,
                                                      double halfdt, int na, int nb, const double *tw_nb,
-                                                     double2 sc1, double2 sc2) {
+                                                     double2 sc1, double2 sc2, double sc) {
   constexpr int NQ = 2 * HM + 1;
+  constexpr bool F32 = std::is_same<R, float>::value;
   extern __shared__ double smx[];
   R *E = reinterpret_cast<R *>(smx);  // [nb][NQ]
   R *CF = E + nb * NQ;                // [XR][NQ]
-  const double sc = sqrt(1.0 / (double)nb);
   for (int w = threadIdx.x; w < nb * NQ; w += blockDim.x) {
     const int j = w / NQ, q = w % NQ;
     double v = sc;
@@ -163,16 +168,17 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
       const int k = (q + 1) / 2, m = (j * k) % nb;
       v = (q & 1) ? 2.0 * sc * tw_nb[m] : -2.0 * sc * tw_nb[nb + m];
     }
-    E[w] = (R)v;
+    if constexpr (F32) E[w] = d2f(v);
+    else E[w] = v;
   }
   const long long S = 3LL * na;
   const bool any = fb1 || fb2;
   const int lr = threadIdx.x % XR, grp = threadIdx.x / XR;
   const long long row = (long long)blockIdx.x * XR + lr;
   if (grp == 0 && row < S) {
-    double cf[NQ];
+    R cf[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) cf[q] = 0.0;
+    for (int q = 0; q < NQ; ++q) cf[q] = (R)0;
     const double *fbs[2] = {fb1, fb2};
     const int nbcs[2] = {nbc1, nbc2};
     const double *tws[2] = {tw_c1, tw_c2};
@@ -180,10 +186,29 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
     for (int t = 0; t < 2; ++t) {
       if (!fbs[t]) continue;
       const int nbc = nbcs[t], h = (nbc - 1) / 2;
-      double tmp[NQ + 1], hc[NQ + 1];  // nbc <= 2 HM + 2
-      for (int j = 0; j < nbc; ++j) tmp[j] = fbs[t][row + S * j];
-      gb_r2hc_direct(tmp, hc, nbc, tws[t]);
-      const double s1 = scs[t].x, s2 = scs[t].y;
+      R hc[NQ + 1];  // nbc <= 2 HM + 2
+      if constexpr (F32) {  // r2hc of the contracted forces in FP32 (gb_r2hc_direct's sums)
+        float tmp[NQ + 1];
+        for (int j = 0; j < nbc; ++j) tmp[j] = d2f(fbs[t][row + S * j]);
+        const double *tw = tws[t];
+        for (int k = 0; k <= h; ++k) {
+          float re = 0.f, im = 0.f;
+          int m = 0;
+          for (int j = 0; j < nbc; ++j) {
+            re = fmaf(tmp[j], d2f(tw[m]), re);
+            im = fmaf(-tmp[j], d2f(tw[nbc + m]), im);
+            m += k;
+            if (m >= nbc) m -= nbc;
+          }
+          hc[k] = re;
+          if (k > 0) hc[nbc - k] = im;
+        }
+      } else {
+        double tmp[NQ + 1];
+        for (int j = 0; j < nbc; ++j) tmp[j] = fbs[t][row + S * j];
+        gb_r2hc_direct(tmp, hc, nbc, tws[t]);
+      }
+      const R s1 = F32 ? (R)d2f(scs[t].x) : (R)scs[t].x, s2 = F32 ? (R)d2f(scs[t].y) : (R)scs[t].y;
       cf[0] += s2 * (s1 * hc[0]);
 #pragma unroll
       for (int k = 1; k <= HM; ++k) {
@@ -194,7 +219,7 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
       }
     }
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) CF[lr * NQ + q] = (R)cf[q];
+    for (int q = 0; q < NQ; ++q) CF[lr * NQ + q] = cf[q];
   }
   __syncthreads();
   if (row >= S) return;
@@ -202,15 +227,20 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
 #pragma unroll
   for (int q = 0; q < NQ; ++q) cr[q] = CF[lr * NQ + q];
   const int j0 = grp * nb / 4, j1 = (grp + 1) * nb / 4;
+  const bool extras = e1 || e2 || e3;
   for (int j = j0; j < j1; ++j) {
     R s = (R)0;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) s += cr[q] * E[j * NQ + q];
-    double v = any ? (double)s : 0.0;
+    double v;
+    if constexpr (F32) v = any ? f2d(s) : 0.0;
+    else v = any ? s : 0.0;
     const long long o = row + S * j;
-    if (e1) v += e1[o];
-    if (e2) v += e2[o];
-    if (e3) v += e3[o];
+    if (extras) {
+      if (e1) v += e1[o];
+      if (e2) v += e2[o];
+      if (e3) v += e3[o];
+    }
     dvdr[o] = v;
     if (p) p[o] = p[o] - halfdt * v;
   }
@@ -303,7 +333,9 @@ void launch_copy(cudaStream_t s, double *dst, const double *src, long long n) {
 void launch_ring_contract(cudaStream_t s, const double *rnm, double *rb, int na, int nb, int nbc,
                           const double *tw_c) {
   long long n = 3LL * na;
-  k_ring_contract<<<nblk(n, 128), 128, 0, s>>>(rnm, rb, na, nb, nbc, tw_c);
+  // scales 1/sqrt(nbc), sqrt(nbc/nb) (evolve_pi.f90:405-431), from the host
+  k_ring_contract<<<nblk(n, 128), 128, 0, s>>>(rnm, rb, na, nb, nbc, tw_c, std::sqrt(1.0 / (double)nbc),
+                                               std::sqrt((double)nbc / (double)nb));
 }
 
 template <int HM>
@@ -316,12 +348,13 @@ void launch_expand_hm(cudaStream_t s, bool mixed, double *dvdr, const double *fb
     return nbc > 0 ? make_double2(sqrt(1.0 / (double)nbc), sqrt((double)nb / (double)nbc)) : make_double2(0.0, 0.0);
   };
   const double2 sc1 = scale(fb1 ? nbc1 : 0), sc2 = scale(fb2 ? nbc2 : 0);
+  const double sc = sqrt(1.0 / (double)nb);
   if (mixed)
     k_expand_table<HM, float><<<nblk(n, XR), XT, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p,
-                                                            halfdt, na, nb, tw_nb, sc1, sc2);
+                                                            halfdt, na, nb, tw_nb, sc1, sc2, sc);
   else
     k_expand_table<HM, double><<<nblk(n, XR), XT, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3,
-                                                             p, halfdt, na, nb, tw_nb, sc1, sc2);
+                                                             p, halfdt, na, nb, tw_nb, sc1, sc2, sc);
 }
 
 void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int nbc1,
