@@ -80,6 +80,7 @@ struct gb_context {
   // force scratch
   double *f_a = nullptr, *f_b = nullptr, *f_c = nullptr;  // bead-rep term forces [nb][na][3]
   double *rb1 = nullptr, *fb1 = nullptr;  // contracted Ewald configurations and forces
+  bool rb1_ready = false, rb2_ready = false;  // rb1 / rb2 written by the fused MTS kernel of this step
   double *rb2 = nullptr, *fb2 = nullptr;  // contracted LJ configurations and forces
   double *fb3 = nullptr;                  // contracted TEM forces
   double *g = nullptr;     // unit-box gradient scratch [nb][na][3]

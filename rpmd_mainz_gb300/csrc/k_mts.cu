@@ -19,6 +19,7 @@
 #include "gb_kernels.h"
 
 #include <algorithm>
+#include <cmath>
 
 namespace {
 
@@ -44,8 +45,17 @@ struct MtsArgs {
   int na, nm, mts, model, mpb;
   double halfdt, dtsmall, halfdtsmall;
   float hdt_h, hdt_l, hds_h, hds_l;  // halfdt and halfdtsmall as FP32 pairs (mixed kernel)
+  double sc;                          // sqrt(1/nb)
+  // mixed kernel: ring_contract (evolve_pi.f90:405-431) of the new positions
+  // into rb1 / rb2 (nullptr: not fused) with nbc1 / nbc2 <= MTS_NBC beads,
+  // twiddles tw_c1 / tw_c2, scale s12 = sqrt(1/nbc) sqrt(nbc/nb)
+  double *rb1, *rb2;
+  int nbc1, nbc2;
+  const double *tw_c1, *tw_c2;
+  double s12_1, s12_2;
   IntraPar ip;
 };
+constexpr int MTS_NBC = 9;  // longest contracted ring written by the mixed kernel
 
 template <int NB>
 __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_fused(MtsArgs a) {
@@ -61,7 +71,7 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_fused(MtsArgs a) {
   double *s_twi = s_twf + 2 * NB;                  // [2*NB] scaled by sqrt(1/nb) (inverse)
   double *s_red = s_twi + 2 * NB;                  // [32 warps][18]
   const int t = threadIdx.x;
-  const double sc = sqrt(1.0 / (double)NB);
+  const double sc = a.sc;
   for (int i = t; i < 12 * NB; i += T) s_mono[i] = a.monod[i];
   for (int i = t; i < 2 * NB; i += T) {
     const double w = a.tw[i];
@@ -238,8 +248,9 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
   float *s_tw_l = s_twi + 2 * NB;                  // lo parts of the three tables
   float *s_twf_l = s_tw_l + 2 * NB;
   float *s_twi_l = s_twf_l + 2 * NB;
+  float *s_ct = s_twi_l + 2 * NB;                  // [2][2*MTS_NBC] contraction cos, sin
   const int t = threadIdx.x;
-  const double sc = sqrt(1.0 / (double)NB);
+  const double sc = a.sc;
   for (int i = t; i < 12 * NB; i += T) {
     const double w = a.monod[i];
     const float h = (float)w;
@@ -255,6 +266,13 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
     s_tw_l[i] = (float)(w - (double)s_tw[i]);
     s_twf_l[i] = (float)(wf - (double)s_twf[i]);
     s_twi_l[i] = (float)(wi - (double)s_twi[i]);
+  }
+  for (int i = t; i < 4 * MTS_NBC; i += T) {
+    const int q = i / (2 * MTS_NBC), e = i % (2 * MTS_NBC);
+    const double *tw = q ? a.tw_c2 : a.tw_c1;
+    const int nbc = q ? a.nbc2 : a.nbc1;
+    const double *rb = q ? a.rb2 : a.rb1;
+    s_ct[i] = rb && e < 2 * nbc ? d2f(tw[e]) : 0.f;
   }
   const int mpb = a.mpb;
   const int m0 = blockIdx.x * mpb;
@@ -409,6 +427,29 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
         a.rnm[row + S * j] = j ? f2d(xf[j]) : x0;
         a.dvdr2[row + S * j] = f2d(f2_row[j]);
       }
+      // contracted rings of the new positions (gb_hc2r_direct over modes 0..h,
+      // the FP32 modes summed in FP32): rb_j = s12 x0 + s12 y_j
+      auto contract = [&](double *rb, int nbc, const float *ct, double s12) {
+        if (!rb) return;
+        const int h = (nbc - 1) / 2;
+        const double base = s12 * x0;
+        const float sf = d2f(s12);
+        for (int j = 0; j < nbc; ++j) {
+          float y = 0.f;
+          int mm = 0;
+#pragma unroll
+          for (int k = 1; k <= (MTS_NBC - 1) / 2; ++k) {
+            if (k <= h && k < NB) {
+              mm += j;
+              if (mm >= nbc) mm -= nbc;
+              y += 2.f * (xf[k] * ct[mm] - xf[NB - k] * ct[nbc + mm]);
+            }
+          }
+          rb[row + S * j] = base + f2d(sf * y);
+        }
+      };
+      contract(a.rb1, a.nbc1, s_ct, a.s12_1);
+      contract(a.rb2, a.nbc2, s_ct + 2 * MTS_NBC, a.s12_2);
     }
   }
   // block totals: df / FP32 warp sums, FP64 across warps (threads 0..17)
@@ -458,7 +499,8 @@ size_t mts_smem_mixed(int T) {
   using C = MtsCfg<NB>;
   const int nrow = (T + 8) / 9 * 9;
   const int nf = (3 * nrow * C::LD + 1) & ~1;
-  return sizeof(float) * nf + sizeof(double) * (nrow + 12 + 32 * 18) + sizeof(float) * (24 * NB + 12 * NB);
+  return sizeof(float) * nf + sizeof(double) * (nrow + 12 + 32 * 18) +
+         sizeof(float) * (24 * NB + 12 * NB + 4 * MTS_NBC);
 }
 
 template <int NB>
@@ -528,6 +570,29 @@ void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used) {
   };
   split(a.halfdt, a.hdt_h, a.hdt_l);
   split(a.halfdtsmall, a.hds_h, a.hds_l);
+  a.sc = std::sqrt(1.0 / (double)nb);
+  // the mixed kernel writes the contracted rings when the forces follow the
+  // propagation directly (no barostat shift in between)
+  a.rb1 = a.rb2 = nullptr;
+  a.nbc1 = a.nbc2 = 0;
+  a.tw_c1 = c->tw_c1;
+  a.tw_c2 = c->tw_c2;
+  a.s12_1 = a.s12_2 = 0.0;
+  c->rb1_ready = c->rb2_ready = false;
+  const bool mixed_k = c->P.precision == GB_PREC_MIXED;
+  auto fuse = [&](int nbc) { return mixed_k && !c->nbaro && nb > 1 && nbc > 0 && nbc <= MTS_NBC && nbc <= nb && (nbc & 1); };
+  if (fuse(c->P.nbdf1)) {
+    a.rb1 = c->rb1;
+    a.nbc1 = c->P.nbdf1;
+    a.s12_1 = std::sqrt((double)a.nbc1 / (double)nb) * std::sqrt(1.0 / (double)a.nbc1);
+    c->rb1_ready = true;
+  }
+  if (fuse(c->P.nbdf2)) {
+    a.rb2 = c->rb2;
+    a.nbc2 = c->P.nbdf2;
+    a.s12_2 = std::sqrt((double)a.nbc2 / (double)nb) * std::sqrt(1.0 / (double)a.nbc2);
+    c->rb2_ready = true;
+  }
   a.ip.reoh = c->P.reoh;
   a.ip.theta = c->P.theta;
   a.ip.rehh = 2.0 * sin(0.5 * c->P.theta) * c->P.reoh;

@@ -533,23 +533,27 @@ int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, 
   const double sig = c->P.sig;
   const bool con1 = nb > 1 && nbdf1 > 0, con2 = nb > 1 && nbdf2 > 0;
   int st;
+  struct Clear {  // the fused kernel's rings serve this evaluation only
+    gb_context *c;
+    ~Clear() { c->rb1_ready = c->rb2_ready = false; }
+  } clear{c};
   if (con1) {
     if ((nbdf1 - 1) % 2 != 0) return ctx_set_error(GB_E_CONTRACT, "* Beadiabatic factor must be ODD");
-    launch_ring_contract(c->stream, rnm, c->rb1, na, nb, nbdf1, c->tw_c1);
+    if (!c->rb1_ready) launch_ring_contract(c->stream, rnm, c->rb1, na, nb, nbdf1, c->tw_c1);
     if ((st = term_ewald(c, c->rb1, nbdf1, c->fb1, 1.0, 0, ACC_EW))) return st;
     c->plan.B_ew = nbdf1;
     if (sig > 0.0) {
       if ((st = term_tem(c, c->rb1, nbdf1, c->fb1, -1.0, 1, ACC_TEM))) return st;
       c->plan.B_tem = nbdf1;
     }
-    c->launches += 1;
+    if (!c->rb1_ready) c->launches += 1;
   }
   if (con2) {
     if ((nbdf2 - 1) % 2 != 0) return ctx_set_error(GB_E_CONTRACT, "* Beadiabatic factor must be ODD");
-    launch_ring_contract(c->stream, rnm, c->rb2, na, nb, nbdf2, c->tw_c2);
+    if (!c->rb2_ready) launch_ring_contract(c->stream, rnm, c->rb2, na, nb, nbdf2, c->tw_c2);
     if ((st = term_lj(c, c->rb2, nbdf2, c->fb2, 0, ACC_LJ))) return st;
     c->plan.B_lj = nbdf2;
-    c->launches += 1;
+    if (!c->rb2_ready) c->launches += 1;
   }
   const double *e1 = nullptr, *e2 = nullptr, *e3 = nullptr;
   if (nb == 1 || nbdf1 <= 0) {

@@ -8,15 +8,20 @@
 // kernel (occupancy against the one-wave grid), and the pair-list skin (larger
 // lists against fewer rebuilds), the warps that share a block's sites in the
 // FP32 k-space force kernel and the sites each of its lanes carries (more
-// sites share each table load, fewer blocks fill the SMs).  gbrpmd_ctx_autotune times evolve_pi steps of
-// the context itself with candidate shapes, one parameter at a time from the
-// defaults (coordinate descent), restores the trajectory state after every
-// trial and keeps the fastest shape.  Results are cached for the process per
+// sites share each table load, fewer blocks fill the SMs).
+// gbrpmd_ctx_autotune runs evolve_pi steps of the context itself with
+// candidate shapes, one parameter at a time from the defaults (coordinate
+// descent), restores the trajectory state after every trial and keeps the
+// fastest shape.  A kernel's launch shape is judged on the median CUDA-event
+// time of that kernel alone (list-rebuild steps do not decide); the skin, which
+// trades pair count against rebuild frequency, on the mean time of whole steps
+// over a longer trial.  Results are cached for the process per
 // shape key (atoms, beads, precision, MTS, contraction, box kind, model), so a
 // batch of many replicas tunes each distinct shape once.  The shapes change
 // results only through the order of floating-point sums.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -102,23 +107,51 @@ void apply(gb_context *c, const Shape &s) {
   dev_graph_reset(c);
 }
 
-// milliseconds per step of `steps` steps after three warm-up steps (plain,
-// captured, replayed), from the restored state; negative on failure
-int trial(gb_context *c, const Saved &S, const Shape &shape, double dt, double beta, int steps, cudaEvent_t a,
-          cudaEvent_t b, double *ms) {
+// milliseconds per step after three warm-up steps (plain, captured,
+// replayed), from the restored state.  region < 0: the mean over `steps` whole
+// steps; else the median CUDA-event time of that profiled region (its kernel
+// alone; steps run uncaptured with per-region events), which keeps the rare
+// pair-list rebuild steps out of the comparison.
+int trial(gb_context *c, const Saved &S, const Shape &shape, double dt, double beta, int steps, int region,
+          std::vector<cudaEvent_t> &ev, double *ms) {
   int st;
   if ((st = restore(c, S))) return st;
   apply(c, shape);
   for (int i = 0; i < 3; ++i)
     if ((st = dev_step(c, dt, beta))) return st;
-  TCK(cudaEventRecord(a, c->stream));
-  for (int i = 0; i < steps; ++i)
-    if ((st = dev_step(c, dt, beta))) return st;
-  TCK(cudaEventRecord(b, c->stream));
-  TCK(cudaEventSynchronize(b));
-  float t = 0.f;
-  TCK(cudaEventElapsedTime(&t, a, b));
-  *ms = (double)t / steps;
+  std::vector<double> t;
+  if (region < 0) {  // mean over whole steps (rebuilds included)
+    TCK(cudaEventRecord(ev[0], c->stream));
+    for (int i = 0; i < steps; ++i)
+      if ((st = dev_step(c, dt, beta))) return st;
+    TCK(cudaEventRecord(ev[1], c->stream));
+    TCK(cudaEventSynchronize(ev[1]));
+    float x = 0.f;
+    TCK(cudaEventElapsedTime(&x, ev[0], ev[1]));
+    *ms = (double)x / steps;
+    return GB_OK;
+  } else {
+    TCK(cudaStreamSynchronize(c->stream));
+    c->prof = 1;
+    c->marks.clear();
+    c->ev_next = 0;
+    for (int i = 0; i < steps && !st; ++i) st = dev_step(c, dt, beta);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    for (const gb_context::Mark &m : c->marks) {
+      float x = 0.f;
+      if (m.region == region && cudaEventElapsedTime(&x, m.a, m.b) == cudaSuccess) t.push_back(x);
+    }
+    c->prof = 0;
+    c->marks.clear();
+    c->ev_next = 0;
+    dev_graph_reset(c);
+    if (st) return st;
+    TCK(e);
+    if (t.empty()) return ctx_set_error(GB_E_ARG, "autotune: the timed region did not run");
+  }
+  std::sort(t.begin(), t.end());
+  const size_t n = t.size();
+  *ms = n % 2 ? t[n / 2] : 0.5 * (t[n / 2 - 1] + t[n / 2]);
   return GB_OK;
 }
 
@@ -169,59 +202,68 @@ int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double
   TCK(cudaStreamSynchronize(c->stream));
   Saved S;
   if ((st = save(c, S))) return st;
-  cudaEvent_t a = nullptr, b = nullptr;
-  TCK(cudaEventCreate(&a));
-  TCK(cudaEventCreate(&b));
+  std::vector<cudaEvent_t> ev(2, nullptr);
+  for (cudaEvent_t &e : ev) TCK(cudaEventCreate(&e));
   const bool mixed = P.precision == GB_PREC_MIXED;
   Shape best;
   best.skin = c->list_skin;  // 0 (lists rebuilt at every use) stays 0
   double best_ms = 0.0;
-  st = trial(c, S, best, dt, beta, steps, a, b, &best_ms);
+  // each parameter is compared on the time of the kernel it shapes (the
+  // region), the list skin on whole steps
+  int region = -1, nstep = steps;
+  auto baseline = [&](int reg) {
+    region = reg;
+    nstep = reg < 0 ? 4 * steps : steps;  // rebuilds are rare: whole-step means need longer trials
+    if (!st) st = trial(c, S, best, dt, beta, nstep, region, ev, &best_ms);
+  };
   auto probe = [&](Shape cand) {
     if (st) return;
     double ms = 0.0;
-    st = trial(c, S, cand, dt, beta, steps, a, b, &ms);
+    st = trial(c, S, cand, dt, beta, nstep, region, ev, &ms);
     if (!st && ms < 0.97 * best_ms) {  // a clear gain only
       best = cand;
       best_ms = ms;
     }
   };
   if (mixed) {
+    baseline(PR_EW_REAL);
     for (int np : {8, 32}) {
       Shape cand = best;
       cand.tune.ew_np = np;
       probe(cand);
     }
+    baseline(PR_LJ);
     for (int np : {2, 8}) {
       Shape cand = best;
       cand.tune.lj_np = np;
       probe(cand);
     }
-    {
-      Shape cand = best;
-      cand.tune.rf_g = 16;
-      probe(cand);
-    }
-    {
-      Shape cand = best;
-      cand.tune.rf_ns = 2;
-      probe(cand);
-    }
+    baseline(PR_RECIP_F);
+    for (int g : {8, 16})
+      for (int ns : {1, 2}) {
+        if (g == best.tune.rf_g && ns == best.tune.rf_ns) continue;
+        Shape cand = best;
+        cand.tune.rf_g = g;
+        cand.tune.rf_ns = ns;
+        probe(cand);
+      }
   }
+  baseline(PR_MTS);
   for (int mpb : {4, 8, 14, 28}) {
     if (mpb >= c->nm) continue;
     Shape cand = best;
     cand.tune.mts_mpb = mpb;
     probe(cand);
   }
-  if (best.skin > 0.0)
+  if (best.skin > 0.0) {
+    baseline(-1);
     for (double skin : {0.05, 0.15, 0.2}) {
       Shape cand = best;
       cand.skin = skin;
       probe(cand);
     }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
+  }
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
   int st2 = restore(c, S);
   cudaFree(S.dev);
   if (st) return st;
