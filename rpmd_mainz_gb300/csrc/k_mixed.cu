@@ -215,6 +215,7 @@ constexpr int MSK_G = 8;
 constexpr int MSK_T = 128;
 constexpr int MF_S = 32;  // sites per lane group of the force block (one warp's lanes; the kernel assumes 32)
 constexpr int MF_GMAX = 16;  // column shares (warps) per force block: 8 or 16 (tuned)
+constexpr int MF_KZ = 16;    // z powers held in registers when kmax < MF_KZ
 constexpr int SIGN32 = (int)0x80000000u;
 
 GB_D float flipf(float v, int mask) { return __int_as_float(__float_as_int(v) ^ mask); }
@@ -377,8 +378,12 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
 // STAGED: the whole k-pair table (8 floats per pair) is copied to shared
 // memory first, so that the inner loop reads it with shared-memory broadcasts
 // NS sites per lane (block of 32 NS sites): every k-pair table entry loaded
-// from shared memory serves NS sites
-template <bool STAGED, int MF_G, int NS>
+// from shared memory serves NS sites.  KZ > 0 (kmax < KZ): each lane keeps its
+// sites' z powers (m = 0..KZ-1) in registers, so that the inner loop over m,
+// unrolled with a uniform branch per m, loads only the k-pair table entries
+// (shared-memory broadcasts) and is FMA-bound; KZ = 0 reads them from shared
+// memory in a plain loop.
+template <bool STAGED, int MF_G, int NS, int KZ>
 __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__restrict__ tab, int na,
                                                                        int kmax, int ncol,
                                                                        const KCol *__restrict__ cols, int nkp,
@@ -419,6 +424,13 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
   const int col0 = first_col(kp_lo), col1 = first_col(kp_hi);
   __syncthreads();
   const float4 *T = STAGED ? sT : sk + (long long)c * nkp * 2;
+  float2 zr[KZ > 0 ? KZ : 1][NS];
+  if constexpr (KZ > 0) {
+#pragma unroll
+    for (int m = 0; m < KZ; ++m)
+#pragma unroll
+      for (int u = 0; u < NS; ++u) zr[m][u] = m < K1 ? stf[(2 * K1 + m) * BS + sl + 32 * u] : make_float2(0.f, 0.f);
+  }
   float sx[NS], sy[NS], sz[NS], ex[NS], ey[NS], ez[NS];
 #pragma unroll
   for (int u = 0; u < NS; ++u) sx[u] = sy[u] = sz[u] = ex[u] = ey[u] = ez[u] = 0.f;
@@ -436,9 +448,7 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
       ur[u] = ui[u] = vr[u] = vi[u] = 0.f;
     }
     const float4 *Tp = T + 2LL * (koff - mlo);
-    const float2 *Z = stf + 2 * K1 * BS + sl;
-#pragma unroll 4
-    for (int m = mlo; m <= mhi; ++m) {
+    auto step = [&](int m, const float2 (&z)[NS]) {
       float4 t0, t1;
       if (STAGED) {
         t0 = Tp[2 * m];
@@ -449,11 +459,38 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
       }
 #pragma unroll
       for (int u = 0; u < NS; ++u) {
-        const float2 z = Z[m * BS + 32 * u];
-        ur[u] = fmaf(z.x, t0.x, fmaf(z.y, t0.w, ur[u]));
-        ui[u] = fmaf(z.x, t0.y, fmaf(z.y, t0.z, ui[u]));
-        vr[u] = fmaf(z.x, t1.x, fmaf(z.y, t1.y, vr[u]));
-        vi[u] = fmaf(z.x, t1.z, fmaf(z.y, t1.w, vi[u]));
+        ur[u] = fmaf(z[u].x, t0.x, fmaf(z[u].y, t0.w, ur[u]));
+        ui[u] = fmaf(z[u].x, t0.y, fmaf(z[u].y, t0.z, ui[u]));
+        vr[u] = fmaf(z[u].x, t1.x, fmaf(z[u].y, t1.y, vr[u]));
+        vi[u] = fmaf(z[u].x, t1.z, fmaf(z[u].y, t1.w, vi[u]));
+      }
+    };
+    if constexpr (KZ > 0) {
+      static_assert(KZ == 16, "the jump below covers m = 0..15");
+      // enter at m = mhi and fall through to m = 1 (m = 0 when mlo = 0): one
+      // uniform indirect jump per column, no predicated-off steps
+      switch (mhi) {
+#define GB_ZSTEP(M) \
+  case M:           \
+    step(M, zr[M]); \
+    [[fallthrough]];
+        GB_ZSTEP(15) GB_ZSTEP(14) GB_ZSTEP(13) GB_ZSTEP(12) GB_ZSTEP(11) GB_ZSTEP(10) GB_ZSTEP(9) GB_ZSTEP(8)
+        GB_ZSTEP(7) GB_ZSTEP(6) GB_ZSTEP(5) GB_ZSTEP(4) GB_ZSTEP(3) GB_ZSTEP(2) GB_ZSTEP(1)
+#undef GB_ZSTEP
+        case 0:
+          if (mlo == 0) step(0, zr[0]);
+          break;
+        default:
+          break;
+      }
+    } else {
+      const float2 *Z = stf + 2 * K1 * BS + sl;
+#pragma unroll 4
+      for (int m = mlo; m <= mhi; ++m) {
+        float2 z[NS];
+#pragma unroll
+        for (int u = 0; u < NS; ++u) z[u] = Z[m * BS + 32 * u];
+        step(m, z);
       }
     }
 #pragma unroll
@@ -561,34 +598,40 @@ void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc) 
   else go(std::integral_constant<int, 16>());
 }
 
+template <bool STAGED, int G, int NS, int KZ>
+void force_attr() {
+  cudaFuncSetAttribute(k_recip_force_mx<STAGED, G, NS, KZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
+template <int G, int NS, int KZ>
+void force_launch(cudaStream_t s, gb_context *c, int B, double *g) {
+  static_assert(G <= MF_GMAX, "column shares");
+  const int kmax = c->P.kmax;
+  const size_t staged = recip_force_smem_mx(kmax, c->nkp, G, NS);
+  dim3 grid(nblk(c->na, MF_S * NS), B);
+  if (staged <= 160 * 1024)
+    k_recip_force_mx<true, G, NS, KZ><<<grid, 32 * G, staged, s>>>(
+        reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
+        reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
+  else
+    k_recip_force_mx<false, G, NS, KZ><<<grid, 32 * G, recip_force_smem_mx(kmax, 0, G, NS), s>>>(
+        reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
+        reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
+}
+
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
   if (c->nkp == 0) return;
-  const int kmax = c->P.kmax;
-  auto go = [&](auto Gc, auto NSc) {
-    constexpr int G = decltype(Gc)::value, NS = decltype(NSc)::value;
-    static_assert(G <= MF_GMAX, "column shares");
-    const size_t staged = recip_force_smem_mx(kmax, c->nkp, G, NS);
-    dim3 grid(nblk(c->na, MF_S * NS), B);
-    if (staged <= 160 * 1024)
-      k_recip_force_mx<true, G, NS><<<grid, 32 * G, staged, s>>>(
-          reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
-          reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
-    else
-      k_recip_force_mx<false, G, NS><<<grid, 32 * G, recip_force_smem_mx(kmax, 0, G, NS), s>>>(
-          reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
-          reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
-  };
-  using I8 = std::integral_constant<int, 8>;
-  using I16 = std::integral_constant<int, 16>;
-  using N1 = std::integral_constant<int, 1>;
-  using N2 = std::integral_constant<int, 2>;
-  const bool g16 = c->tune.rf_g == 16, two = c->tune.rf_ns == 2;
-  if (g16) {
-    if (two) go(I16(), N2());
-    else go(I16(), N1());
-  } else {
-    if (two) go(I8(), N2());
-    else go(I8(), N1());
+  const bool zr = c->P.kmax < MF_KZ;  // z powers in registers
+  const int v = (c->tune.rf_g == 16 ? 4 : 0) + (c->tune.rf_ns == 2 ? 2 : 0) + (zr ? 1 : 0);
+  switch (v) {
+    case 0: force_launch<8, 1, 0>(s, c, B, g); break;
+    case 1: force_launch<8, 1, MF_KZ>(s, c, B, g); break;
+    case 2: force_launch<8, 2, 0>(s, c, B, g); break;
+    case 3: force_launch<8, 2, MF_KZ>(s, c, B, g); break;
+    case 4: force_launch<16, 1, 0>(s, c, B, g); break;
+    case 5: force_launch<16, 1, MF_KZ>(s, c, B, g); break;
+    case 6: force_launch<16, 2, 0>(s, c, B, g); break;
+    default: force_launch<16, 2, MF_KZ>(s, c, B, g); break;
   }
 }
 
@@ -596,13 +639,21 @@ void recip_set_attributes_mx() {
   static bool done = false;
   if (done) return;
   cudaFuncSetAttribute(k_recip_sk_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<true, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<false, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<true, 16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<false, 16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<true, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<false, 8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<true, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(k_recip_force_mx<false, 16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  force_attr<true, 8, 1, 0>();
+  force_attr<false, 8, 1, 0>();
+  force_attr<true, 8, 1, MF_KZ>();
+  force_attr<false, 8, 1, MF_KZ>();
+  force_attr<true, 8, 2, 0>();
+  force_attr<false, 8, 2, 0>();
+  force_attr<true, 8, 2, MF_KZ>();
+  force_attr<false, 8, 2, MF_KZ>();
+  force_attr<true, 16, 1, 0>();
+  force_attr<false, 16, 1, 0>();
+  force_attr<true, 16, 1, MF_KZ>();
+  force_attr<false, 16, 1, MF_KZ>();
+  force_attr<true, 16, 2, 0>();
+  force_attr<false, 16, 2, 0>();
+  force_attr<true, 16, 2, MF_KZ>();
+  force_attr<false, 16, 2, MF_KZ>();
   done = true;
 }
