@@ -14,7 +14,7 @@
 //   KCol  per column: kx, ky, first k pair, m range, and kx, ky as doubles;
 //   kp    per k pair: kx, ky, m, kind;  kw per k pair: (4 pi / k^2) e^{-k^2 b};
 //   grp   structure-factor work items: up to G consecutive m of one column,
-//         full-length items first, then shorter ones by decreasing length.
+//         ordered by first m, then by decreasing length (gb_order_groups).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,6 +28,24 @@ struct alignas(16) KCol {
   double dkx, dky;
 };
 static_assert(sizeof(KCol) == 32, "KCol layout");
+
+// Stable order of the work items by first m, then by decreasing length: the
+// threads of a warp then read the same z powers of a site (shared-memory
+// broadcasts) and run loops of the same length.  Insertion sort (no heap).
+inline void gb_order_groups(int4 *grp, int n) {
+  auto before = [](const int4 &a, const int4 &b) {
+    return a.z != b.z ? a.z < b.z : (a.x >> 16) > (b.x >> 16);
+  };
+  for (int i = 1; i < n; ++i) {
+    const int4 v = grp[i];
+    int j = i;
+    while (j > 0 && before(v, grp[j - 1])) {
+      grp[j] = grp[j - 1];
+      --j;
+    }
+    grp[j] = v;
+  }
+}
 
 struct KTables {
   int ncol = 0, nkp = 0, ngrp = 0, nk = 0;  // nk: k vectors (both kz signs counted)
@@ -107,6 +125,7 @@ inline int gb_build_ktables(const gb_params &P, int G, KCol *col, int cap_col, i
       if (n % G == len && !add_grp(col[i], mlo + (n / G) * G, len)) return 1;
     }
   }
+  gb_order_groups(grp, t.ngrp);
   *out = t;
   return 0;
 }
@@ -191,6 +210,7 @@ inline int gb_build_ktables_nc(const gb_params &P, const double box[3], int G, K
       if (n % G == len && !add_grp(col[i], mlo + (n / G) * G, len)) return 1;
     }
   }
+  gb_order_groups(grp, t.ngrp);
   *out = t;
   return 0;
 }

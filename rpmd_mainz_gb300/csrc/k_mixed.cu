@@ -210,8 +210,9 @@ __global__ void __launch_bounds__(MX_T) k_lj_mx(const float4 *__restrict__ hi, c
 }
 
 // ---- reciprocal space (kwald, ewald_cubic.f90:235-533), FP32 ----
-constexpr int MSK_CHUNK = 128;  // sites per structure-factor block (FP32 partial sums)
-constexpr int MSK_G = 8;
+constexpr int MSK_CHUNK = 64;  // sites per structure-factor block (FP32 partial sums)
+constexpr int MSK_G = 8;   // m values per work item (the k tables' group length)
+constexpr int MSK_SP = 2;  // threads per work item
 constexpr int MSK_T = 128;
 constexpr int MF_S = 32;  // sites per lane group of the force block (one warp's lanes; the kernel assumes 32)
 constexpr int MF_GMAX = 16;  // column shares (warps) per force block: 8 or 16 (tuned)
@@ -247,8 +248,12 @@ __global__ void k_recip_tables_mx(const double *rs, const double *q, int na, int
   tab[g] = k == 0 ? make_float2(a, 0.f) : make_float2(a * cs, a * sn);
 }
 
+// SP threads share a work item, each taking MSK_G / SP of its m values (more
+// warps for the same work: the site loop is latency-bound at one thread per item)
+template <int SP>
 __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na, int kmax, int ngrp,
                                                        const int4 *grp, int nkp, int nchunk, float4 *sk_part) {
+  constexpr int GP = MSK_G / SP;  // m values per thread
   extern __shared__ float2 stf[];  // [MSK_CHUNK][3][K1]
   const int K1 = kmax + 1, K3 = 3 * K1;
   const int c = blockIdx.z, chunk = blockIdx.y;
@@ -256,15 +261,18 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
   const float2 *src = tab + ((long long)c * na + s0) * K3;
   for (int w = threadIdx.x; w < ns * K3; w += MSK_T) stf[w] = src[w];
   __syncthreads();
-  const int gi = blockIdx.x * MSK_T + threadIdx.x;
+  const int tg = blockIdx.x * MSK_T + threadIdx.x;
+  const int gi = tg / SP, part = tg % SP;
   if (gi >= ngrp) return;
   const int4 gr = __ldg(grp + gi);
-  const int kx = gr.x & 0xffff, len = gr.x >> 16, ky = gr.y, m0 = gr.z;
+  const int kx = gr.x & 0xffff, ky = gr.y;
+  const int len = min(GP, (gr.x >> 16) - part * GP), m0 = gr.z + part * GP;
+  if (len <= 0) return;
   const int aky = abs(ky);
   const int ymask = ky < 0 ? SIGN32 : 0;
-  float pr[MSK_G], pi[MSK_G], qr[MSK_G], qi[MSK_G];
+  float pr[GP], pi[GP], qr[GP], qi[GP];
 #pragma unroll
-  for (int g = 0; g < MSK_G; ++g) pr[g] = pi[g] = qr[g] = qi[g] = 0.f;
+  for (int g = 0; g < GP; ++g) pr[g] = pi[g] = qr[g] = qi[g] = 0.f;
   for (int s = 0; s < ns; ++s) {
     const float2 *S = stf + s * K3;
     const float2 X = S[kx], Y = S[K1 + aky];
@@ -273,7 +281,7 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
     const float ci = fmaf(X.x, yi, X.y * Y.x);
     const float2 *Z = S + 2 * K1 + m0;
 #pragma unroll
-    for (int g = 0; g < MSK_G; ++g) {
+    for (int g = 0; g < GP; ++g) {
       if (g < len) {
         const float2 z = Z[g];
         pr[g] = fmaf(cr, z.x, pr[g]);
@@ -283,9 +291,9 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
       }
     }
   }
-  float4 *out = sk_part + ((long long)c * nchunk + chunk) * nkp + gr.w;
+  float4 *out = sk_part + ((long long)c * nchunk + chunk) * nkp + gr.w + part * GP;
 #pragma unroll
-  for (int g = 0; g < MSK_G; ++g)
+  for (int g = 0; g < GP; ++g)
     if (g < len) out[g] = make_float4(pr[g], pi[g], qr[g], qi[g]);
 }
 
@@ -579,9 +587,10 @@ void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const d
   k_recip_tables_mx<<<nblk(nw * (kmax + 1), 256), 256, 0, s>>>(rs, q, c->na, B, kmax,
                                                                make_double3(lat.x * ot, lat.y * ot, lat.z * ot), tab);
   const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
-  dim3 grid(nblk(c->ngrp, MSK_T), nchunk, B);
-  k_recip_sk_mx<<<grid, MSK_T, recip_sk_smem_mx(kmax), s>>>(tab, c->na, kmax, c->ngrp, c->kgrp, c->nkp, nchunk,
-                                                            reinterpret_cast<float4 *>(c->sk_part));
+  static_assert(MSK_G % MSK_SP == 0, "work item split");
+  dim3 grid(nblk((long long)c->ngrp * MSK_SP, MSK_T), nchunk, B);
+  k_recip_sk_mx<MSK_SP><<<grid, MSK_T, recip_sk_smem_mx(kmax), s>>>(tab, c->na, kmax, c->ngrp, c->kgrp, c->nkp,
+                                                                   nchunk, reinterpret_cast<float4 *>(c->sk_part));
 }
 
 void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc) {
@@ -638,7 +647,7 @@ void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
 void recip_set_attributes_mx() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(k_recip_sk_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(k_recip_sk_mx<MSK_SP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   force_attr<true, 8, 1, 0>();
   force_attr<false, 8, 1, 0>();
   force_attr<true, 8, 1, MF_KZ>();
