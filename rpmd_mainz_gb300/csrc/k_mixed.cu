@@ -297,8 +297,9 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
     if (g < len) out[g] = make_float4(pr[g], pi[g], qr[g], qi[g]);
 }
 
-// df (two-float) sums of the chunk partials, FP64 energy and virial per k
-// pair (one warp per block), FP32 force tables
+// df (two-float) sums of the chunk partials; energy, virial and force tables
+// per k pair in FP32 (one warp per block), energy and virial summed as df
+// across the warp and in FP64 across blocks
 // chunk slices per k pair in the weights kernel (SL warps per block): 16 for
 // many chunks, fewer when the configuration has few sites (idle warps otherwise)
 
@@ -326,57 +327,59 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
     part[2 * q + 1][slice][lane] = l[q];
   }
   __syncthreads();
-  if (slice != 0) return;  // warp 0 finishes: one FP64 chain per k pair
-  double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (slice != 0) return;  // warp 0 finishes, in FP32: energy and virial terms per k pair
+  float vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (k < nkp) {
-    double P[4];
+    float P[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       float H = part[2 * q][0][lane], L = part[2 * q + 1][0][lane];
       for (int j = 1; j < MW_SL; ++j) df_add(H, L, part[2 * q][j][lane], part[2 * q + 1][j][lane]);
-      P[q] = df2d(H, L);
+      P[q] = H + L;
     }
-    const double Pr = P[0], Pi = P[1], Qr = P[2], Qi = P[3];
+    const float Pr = P[0], Pi = P[1], Qr = P[2], Qi = P[3];
     const int4 kv = kpair[k];
-    const double w = kw[k];
-    double et, ed = 0.0, Ar, Ai, Dr, Di;  // ed: et(+m) - et(-m)
+    const float w = d2f(kw[k]);
+    float et, ed = 0.f, Ar, Ai, Dr, Di;  // ed: et(+m) - et(-m)
     if (kv.w == 1) {
-      et = 2.0 * w * (Pr * Pr + Pi * Pi + Qr * Qr + Qi * Qi);
-      ed = 4.0 * w * (Pi * Qr - Pr * Qi);
-      Ar = 4.0 * w * Pr;
-      Ai = 4.0 * w * Pi;
-      Dr = -4.0 * w * Qi;
-      Di = 4.0 * w * Qr;
+      et = 2.f * w * (Pr * Pr + Pi * Pi + Qr * Qr + Qi * Qi);
+      ed = 4.f * w * (Pi * Qr - Pr * Qi);
+      Ar = 4.f * w * Pr;
+      Ai = 4.f * w * Pi;
+      Dr = -4.f * w * Qi;
+      Di = 4.f * w * Qr;
     } else if (kv.w == 2) {
-      const double sr = Pr - Qi, si = Pi + Qr;
+      const float sr = Pr - Qi, si = Pi + Qr;
       et = w * (sr * sr + si * si);
-      Ar = Dr = 2.0 * w * sr;
-      Ai = Di = 2.0 * w * si;
+      Ar = Dr = 2.f * w * sr;
+      Ai = Di = 2.f * w * si;
     } else {
       et = w * (Pr * Pr + Pi * Pi);
-      Ar = 2.0 * w * Pr;
-      Ai = 2.0 * w * Pi;
-      Dr = Di = 0.0;
+      Ar = 2.f * w * Pr;
+      Ai = 2.f * w * Pi;
+      Dr = Di = 0.f;
     }
     vals[0] = et;
     // virial factors (gb_kvec.h): [0..8] on the summed energy, [9], [10] on
     // the difference for xz, yz (non-cubic sum only)
     const double *kf = kvir + (long long)GB_KVIR * k;
 #pragma unroll
-    for (int e = 0; e < 9; ++e) vals[1 + e] = et * kf[e];
-    vals[1 + 6] += ed * kf[9];
-    vals[1 + 2] += ed * kf[9];
-    vals[1 + 7] += ed * kf[10];
-    vals[1 + 5] += ed * kf[10];
-    const double m = (double)kv.z;
+    for (int e = 0; e < 9; ++e) vals[1 + e] = et * d2f(kf[e]);
+    const float f9 = d2f(kf[9]), f10 = d2f(kf[10]);
+    vals[1 + 6] += ed * f9;
+    vals[1 + 2] += ed * f9;
+    vals[1 + 7] += ed * f10;
+    vals[1 + 5] += ed * f10;
+    const float m = (float)kv.z;
     float4 *o = sk + ((long long)c * nkp + k) * 2;
-    o[0] = make_float4((float)Ar, (float)-Ai, (float)Dr, (float)Di);
-    o[1] = make_float4((float)(m * Dr), (float)(m * Ai), (float)(-m * Di), (float)(m * Ar));
+    o[0] = make_float4(Ar, -Ai, Dr, Di);
+    o[1] = make_float4(m * Dr, m * Ai, -m * Di, m * Ar);
   }
 #pragma unroll
-  for (int e = 0; e < 10; ++e) {
-    const double v = warp_sum(vals[e]);
-    if (lane == 0 && v != 0.0) atomicAdd(acc + e, v);
+  for (int e = 0; e < 10; ++e) {  // df across the warp, FP64 atomics
+    float h = vals[e], l = 0.f;
+    warp_sum_df(h, l);
+    if (lane == 0 && h != 0.f) atomicAdd(acc + e, df2d(h, l));
   }
 }
 
