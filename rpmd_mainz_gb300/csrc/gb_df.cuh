@@ -43,10 +43,13 @@ GB_D void d2df(double d, float &hi, float &lo) {
   lo = nrm ? l : 0.f;
 }
 
-// d rounded to FP32 (halfway cases away from zero) by integer operations;
-// outside the FP32 normal range as d2df
+// d rounded to the nearest FP32 (ties to even, as the conversion instruction
+// rounds: differences of FP32 values meet exact ties often, and rounding them
+// away from zero drifts) by integer operations; outside the FP32 normal range
+// as d2df
 GB_D float d2f(double d) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(d) + 0x10000000ull;  // + half an FP32 ulp
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned long long u = b + 0x0fffffffull + ((b >> 29) & 1ull);  // half an FP32 ulp, less one on even
   const unsigned H = (unsigned)(u >> 32), L = (unsigned)u;
   const unsigned s = H & 0x80000000u;
   const int e = (int)((H >> 20) & 0x7ffu) - 896;
