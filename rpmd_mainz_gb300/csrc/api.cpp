@@ -152,6 +152,9 @@ int ctx_alloc(gb_context *c, int na, int nb) {
   if (const char *sk = std::getenv("GBRPMD_LIST_SKIN")) c->list_skin = std::max(0.0, std::atof(sk));
   if (const char *gr = std::getenv("GBRPMD_GRAPHS")) c->use_graphs = gr[0] != '0';
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
   const size_t N = 3 * (size_t)na * nb, S = 3 * (size_t)na;
   if ((st = dalloc(c, &c->p, N)) || (st = dalloc(c, &c->r, N)) || (st = dalloc(c, &c->dvdr, N)) ||
       (st = dalloc(c, &c->dvdr2, N)) || (st = dalloc(c, &c->rst, N)) || (st = dalloc(c, &c->rnm, N)) ||
@@ -161,6 +164,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
       (st = dalloc(c, &c->fb2, N)) || (st = dalloc(c, &c->g, N)) || (st = dalloc(c, &c->rs, N)) ||
       (st = dalloc(c, &c->rs32, (size_t)na * nb)) || (st = dalloc(c, &c->lo32, (size_t)na * nb)) ||
       (st = dalloc(c, &c->hi32, (size_t)na * nb / 3)) || (st = dalloc(c, &c->olo32, (size_t)na * nb / 3)) ||
+      (st = dalloc(c, &c->rs32_lj, (size_t)na * nb / 3)) ||
       (st = dalloc(c, &c->rc, S)) ||
       (st = dalloc(c, &c->monod, 12 * (size_t)nb)) ||
       (st = dalloc(c, &c->acc, (size_t)ACC_NSLOT * ACC_STRIDE)) || (st = dalloc(c, &c->status, 1)))
@@ -183,7 +187,8 @@ void ctx_free(gb_context *c) {
   if (c->d_count) cudaFree(c->d_count);
   for (void *p : c->allocs) cudaFree(p);
   c->allocs.clear();
-  for (void *p : {(void *)c->pl.idx, (void *)c->pl.count, (void *)c->kcol, (void *)c->kgrp,
+  for (void *p : {(void *)c->pl.idx, (void *)c->pl.count, (void *)c->pl_lj.idx, (void *)c->pl_lj.count, (void *)c->kcol,
+                  (void *)c->kgrp,
                   (void *)c->kpair, (void *)c->kw, (void *)c->kvir, (void *)c->ktab, (void *)c->sk_part, (void *)c->sk,
                   (void *)c->tw_nb, (void *)c->tw_c1, (void *)c->tw_c2})
     if (p) cudaFree(p);
@@ -200,6 +205,9 @@ void ctx_free(gb_context *c) {
   if (c->gauss_ev) cudaEventDestroy(c->gauss_ev);
   if (c->mid_ev) cudaEventDestroy(c->mid_ev);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->join_ev) cudaEventDestroy(c->join_ev);
+  if (c->aux_stream) cudaStreamDestroy(c->aux_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   c->stream = nullptr;
 }

@@ -89,6 +89,13 @@ struct gb_context {
   float4 *lo32 = nullptr;  // their FP32 remainders (mixed precision) [nb][na]
   float4 *hi32 = nullptr;  // bead oxygen coordinates for the FP32 LJ kernel [nb][nm]
   float4 *olo32 = nullptr; // and their remainders [nb][nm]
+  // the LJ term of evolve_pi runs beside the Ewald term on aux_stream (forked
+  // from and joined to the step's stream) with its own list and frac buffers
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  PairList pl_lj;
+  size_t pl_lj_idx_bytes = 0, pl_lj_cnt_bytes = 0;
+  float4 *rs32_lj = nullptr;  // [nb][nm]
   double *rc = nullptr;    // centroid scratch [na][3]
   PairList pl;             // exact pair list of the current term (re-sized on demand)
   size_t pl_idx_bytes = 0, pl_cnt_bytes = 0;

@@ -537,6 +537,46 @@ int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, 
     gb_context *c;
     ~Clear() { c->rb1_ready = c->rb2_ready = false; }
   } clear{c};
+  // The LJ term on the contracted ring needs neither the Ewald term's inputs
+  // nor its buffers: it runs on the aux stream (forked here, joined before the
+  // expansion), with the context's LJ list and frac buffers swapped in, so that
+  // its kernels fill the SMs the k-space kernels leave idle.  Not while
+  // profiling (regions are timed on the step's stream).
+  const bool branch = con2 && !c->prof && c->aux_stream;
+  bool joined = true;
+  struct Join {  // an error return still joins the branch (a capture needs it)
+    gb_context *c;
+    bool *joined;
+    ~Join() {
+      if (!*joined) cudaStreamWaitEvent(c->stream, c->join_ev, 0);
+    }
+  } join{c, &joined};
+  if (branch) {
+    if ((nbdf2 - 1) % 2 != 0) return ctx_set_error(GB_E_CONTRACT, "* Beadiabatic factor must be ODD");
+    CK(cudaEventRecord(c->fork_ev, c->stream));
+    CK(cudaStreamWaitEvent(c->aux_stream, c->fork_ev, 0));
+    struct Swap {  // the LJ branch's stream and buffers, restored on every exit
+      gb_context *c;
+      explicit Swap(gb_context *cc) : c(cc) { flip(); }
+      ~Swap() { flip(); }
+      void flip() {
+        std::swap(c->stream, c->aux_stream);
+        std::swap(c->pl, c->pl_lj);
+        std::swap(c->pl_idx_bytes, c->pl_lj_idx_bytes);
+        std::swap(c->pl_cnt_bytes, c->pl_lj_cnt_bytes);
+        std::swap(c->rs32, c->rs32_lj);
+      }
+    };
+    {
+      Swap sw(c);
+      if (!c->rb2_ready) launch_ring_contract(c->stream, rnm, c->rb2, na, nb, nbdf2, c->tw_c2);
+      if ((st = term_lj(c, c->rb2, nbdf2, c->fb2, 0, ACC_LJ))) return st;
+    }
+    CK(cudaEventRecord(c->join_ev, c->aux_stream));
+    joined = false;
+    c->plan.B_lj = nbdf2;
+    if (!c->rb2_ready) c->launches += 1;
+  }
   if (con1) {
     if ((nbdf1 - 1) % 2 != 0) return ctx_set_error(GB_E_CONTRACT, "* Beadiabatic factor must be ODD");
     if (!c->rb1_ready) launch_ring_contract(c->stream, rnm, c->rb1, na, nb, nbdf1, c->tw_c1);
@@ -548,7 +588,7 @@ int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, 
     }
     if (!c->rb1_ready) c->launches += 1;
   }
-  if (con2) {
+  if (con2 && !branch) {
     if ((nbdf2 - 1) % 2 != 0) return ctx_set_error(GB_E_CONTRACT, "* Beadiabatic factor must be ODD");
     if (!c->rb2_ready) launch_ring_contract(c->stream, rnm, c->rb2, na, nb, nbdf2, c->tw_c2);
     if ((st = term_lj(c, c->rb2, nbdf2, c->fb2, 0, ACC_LJ))) return st;
@@ -569,6 +609,10 @@ int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, 
     if ((st = term_lj(c, r, nb, c->f_c, 0, ACC_LJ2))) return st;
     c->plan.B_lj2 = nb;
     e3 = c->f_c;
+  }
+  if (!joined) {
+    joined = true;
+    CK(cudaStreamWaitEvent(c->stream, c->join_ev, 0));
   }
   prof_begin(c, PR_EXPAND);
   launch_expand_forces(c->stream, c->dvdr, con1 ? c->fb1 : nullptr, nbdf1, c->tw_c1,
