@@ -155,6 +155,9 @@ int ctx_alloc(gb_context *c, int na, int nb) {
   CK(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
+  CK(cudaStreamCreateWithFlags(&c->aux2_stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&c->fork2_ev, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->join2_ev, cudaEventDisableTiming));
   const size_t N = 3 * (size_t)na * nb, S = 3 * (size_t)na;
   if ((st = dalloc(c, &c->p, N)) || (st = dalloc(c, &c->r, N)) || (st = dalloc(c, &c->dvdr, N)) ||
       (st = dalloc(c, &c->dvdr2, N)) || (st = dalloc(c, &c->rst, N)) || (st = dalloc(c, &c->rnm, N)) ||
@@ -164,7 +167,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
       (st = dalloc(c, &c->fb2, N)) || (st = dalloc(c, &c->g, N)) || (st = dalloc(c, &c->rs, N)) ||
       (st = dalloc(c, &c->rs32, (size_t)na * nb)) || (st = dalloc(c, &c->lo32, (size_t)na * nb)) ||
       (st = dalloc(c, &c->hi32, (size_t)na * nb / 3)) || (st = dalloc(c, &c->olo32, (size_t)na * nb / 3)) ||
-      (st = dalloc(c, &c->rs32_lj, (size_t)na * nb / 3)) ||
+      (st = dalloc(c, &c->rs32_lj, (size_t)na * nb / 3)) || (st = dalloc(c, &c->g2, N)) ||
       (st = dalloc(c, &c->rc, S)) ||
       (st = dalloc(c, &c->monod, 12 * (size_t)nb)) ||
       (st = dalloc(c, &c->acc, (size_t)ACC_NSLOT * ACC_STRIDE)) || (st = dalloc(c, &c->status, 1)))
@@ -208,6 +211,9 @@ void ctx_free(gb_context *c) {
   if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   if (c->join_ev) cudaEventDestroy(c->join_ev);
   if (c->aux_stream) cudaStreamDestroy(c->aux_stream);
+  if (c->fork2_ev) cudaEventDestroy(c->fork2_ev);
+  if (c->join2_ev) cudaEventDestroy(c->join2_ev);
+  if (c->aux2_stream) cudaStreamDestroy(c->aux2_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   c->stream = nullptr;
 }

@@ -96,6 +96,11 @@ struct gb_context {
   PairList pl_lj;
   size_t pl_lj_idx_bytes = 0, pl_lj_cnt_bytes = 0;
   float4 *rs32_lj = nullptr;  // [nb][nm]
+  // the mixed Ewald term runs its k-space kernels on aux2_stream beside the
+  // real-space kernel, which writes its gradients into g2
+  cudaStream_t aux2_stream = nullptr;
+  cudaEvent_t fork2_ev = nullptr, join2_ev = nullptr;
+  double *g2 = nullptr;
   double *rc = nullptr;    // centroid scratch [na][3]
   PairList pl;             // exact pair list of the current term (re-sized on demand)
   size_t pl_idx_bytes = 0, pl_cnt_bytes = 0;

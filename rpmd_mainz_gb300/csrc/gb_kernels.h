@@ -75,17 +75,20 @@ void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const d
 // hi.w carries the site charge (launch_frac32 with q)
 // box: side lengths of the fractional coordinates (1, 1, 1 for the cubic sum);
 // np: lanes per site (8, 16, 32) / per oxygen (2, 4, 8)
+// add = false: g is overwritten (no zeroing pass needed)
 void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc);
+                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc,
+                          bool add = true);
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
                   double sigsq, double rcutsq, const double *box, double dscale, int np, double *out, double *acc);
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);
 void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc);
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g);
 void recip_set_attributes_mx();
-// out[b] = sign * chain_rule(scale * g[b]) (+= when accumulate)
+// out[b] = sign * chain_rule(scale * g[b]) (+= when accumulate); with g2,
+// of scale * (g[b] + g2[b])
 void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, int B, double alpha,
-                        double scale, double sign, int accumulate);
+                        double scale, double sign, int accumulate, const double *g2 = nullptr);
 
 // ---- Lennard-Jones O-O (k_pairs.cu) ----
 // r: [B][na][3] box units; list over oxygen points (shared if pl.nconf == 1)

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
                                                         int na, const int *__restrict__ count,
                                                         const int *__restrict__ idx, int cap, float alpha,
                                                         float sfac, float rcutsq, float3 bx, double *g,
-                                                        double *acc) {
+                                                        double *acc, int add) {
   __shared__ float sh[32 * 8];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
@@ -129,9 +129,9 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
   const float fz = group_sum_f<NP>(sz - cz);
   if (active && sub == 0) {
     double *G = g + ((long long)c * na + i) * 3;
-    G[0] += f2d(fx);
-    G[1] += f2d(fy);
-    G[2] += f2d(fz);
+    G[0] = (add ? G[0] : 0.0) + f2d(fx);
+    G[1] = (add ? G[1] : 0.0) + f2d(fy);
+    G[2] = (add ? G[2] : 0.0) + f2d(fz);
   }
   const float vir6[6] = {vxx, vyx, vzx, vyy, vzy, vzz};
   constexpr int dst[7] = {0, 1, 2, 3, 5, 6, 9};       // v, xx, yx, zx, yy, zy, zz
@@ -543,14 +543,15 @@ int sm_count_mx() {
 }  // namespace
 
 void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc) {
+                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc,
+                          bool add) {
   const float3 bx = make_float3((float)box[0], (float)box[1], (float)box[2]);
   auto go = [&](auto NPc) {
     constexpr int NP = decltype(NPc)::value;
     dim3 grid(nblk((long long)na * NP, MX_T), B);
     const float sfac = (float)(-2.0 * alpha / std::sqrt(std::acos(-1.0)));  // d erfc(alpha r) / dr factor
     k_ewald_real_mx<NP><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
-                                              (float)rcutsq, bx, g, acc);
+                                              (float)rcutsq, bx, g, acc, add ? 1 : 0);
   };
   if (np == 8) go(std::integral_constant<int, 8>());
   else if (np == 32) go(std::integral_constant<int, 32>());

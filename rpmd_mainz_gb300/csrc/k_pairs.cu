@@ -419,7 +419,7 @@ __global__ void k_msite(const double *r, double *rs, int nm, int B, double alpha
 }
 
 // out = sign * chain_rule(scale * g)  (md_forces.f90:206-215)
-__global__ void k_msite_chain(const double *g, double *out, int nm, int B, double alpha,
+__global__ void k_msite_chain(const double *g, const double *g2, double *out, int nm, int B, double alpha,
                               double alpha2, double scale, double sign, int accumulate) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nm * B * 3) return;
@@ -427,9 +427,16 @@ __global__ void k_msite_chain(const double *g, double *out, int nm, int B, doubl
   const long long mb = t / 3;
   const double *m = g + mb * 9;
   double *o = out + mb * 9;
-  const double go = scale * m[d];
-  const double h1 = scale * m[3 + d] + alpha2 * go;
-  const double h2 = scale * m[6 + d] + alpha2 * go;
+  double m0 = m[d], m1 = m[3 + d], m2 = m[6 + d];
+  if (g2) {  // a second gradient buffer (the real-space part, computed beside the k-space part)
+    const double *n = g2 + mb * 9;
+    m0 += n[d];
+    m1 += n[3 + d];
+    m2 += n[6 + d];
+  }
+  const double go = scale * m0;
+  const double h1 = scale * m1 + alpha2 * go;
+  const double h2 = scale * m2 + alpha2 * go;
   const double oo = alpha * go;
   if (accumulate) {
     o[d] += sign * oo;
@@ -879,10 +886,10 @@ void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, do
 }
 
 void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, int B, double alpha,
-                        double scale, double sign, int accumulate) {
+                        double scale, double sign, int accumulate, const double *g2) {
   int nm = na / 3;
   long long n = (long long)nm * B * 3;
-  k_msite_chain<<<nblk(n, 256), 256, 0, s>>>(g, out, nm, B, alpha, 0.5 * (1.0 - alpha), scale, sign,
+  k_msite_chain<<<nblk(n, 256), 256, 0, s>>>(g, g2, out, nm, B, alpha, 0.5 * (1.0 - alpha), scale, sign,
                                              accumulate);
 }
 
