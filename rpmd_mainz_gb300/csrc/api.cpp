@@ -155,7 +155,12 @@ int ctx_alloc(gb_context *c, int na, int nb) {
   CK(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
-  CK(cudaStreamCreateWithFlags(&c->aux2_stream, cudaStreamNonBlocking));
+  {  // the k-space chain (three dependent launches with few blocks each) goes
+     // first when SMs free up; the real-space and LJ kernels fill the rest
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&c->aux2_stream, cudaStreamNonBlocking, greatest));
+  }
   CK(cudaEventCreateWithFlags(&c->fork2_ev, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->join2_ev, cudaEventDisableTiming));
   const size_t N = 3 * (size_t)na * nb, S = 3 * (size_t)na;

@@ -203,7 +203,7 @@ int gbrpmd_batch_step(gb_batch *b, int nsteps) {
         return st;
       }
       if (e != cudaSuccess) return ctx_check_cuda(e, "cudaStreamEndCapture (batch)");
-      e = cudaGraphInstantiate(&b->exec, g, 0);
+      e = cudaGraphInstantiate(&b->exec, g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       if (e != cudaSuccess) {
         b->exec = nullptr;

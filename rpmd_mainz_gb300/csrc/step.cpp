@@ -972,7 +972,8 @@ int dev_step(gb_context *c, double dt, double beta) {
     return st;
   }
   if (e != cudaSuccess) return ctx_check_cuda(e, "cudaStreamEndCapture");
-  e = cudaGraphInstantiate(&G.exec, graph, 0);
+  // node priorities: the k-space branch keeps the priority of its stream
+  e = cudaGraphInstantiate(&G.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
     G.exec = nullptr;
