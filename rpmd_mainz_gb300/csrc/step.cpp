@@ -346,6 +346,26 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   g.excl_mol = 0;
   const bool mixed = c->P.precision == GB_PREC_MIXED;
   g.full = mixed ? 1 : 0;  // the FP32 kernel walks full lists
+  // mixed: the k-space kernels (low occupancy, and needing only the M-site
+  // positions) run on aux2 beside the list upkeep and the real-space kernel,
+  // which writes its own gradient buffer; joined before the chain rule
+  const bool branch = mixed && !c->prof && c->aux2_stream;
+  if (branch) {
+    recip_set_attributes_mx();
+    CK(cudaEventRecord(c->fork2_ev, c->stream));
+    CK(cudaStreamWaitEvent(c->aux2_stream, c->fork2_ev, 0));
+    launch_recip_sk_mx(c->aux2_stream, c, c->rs, c->z, B);
+    launch_recip_weights_mx(c->aux2_stream, c, B, slot(c, s));
+    launch_recip_force_mx(c->aux2_stream, c, B, c->g);
+    CK(cudaEventRecord(c->join2_ev, c->aux2_stream));
+  }
+  struct Join2 {  // an error return still joins the branch (a capture needs it)
+    gb_context *c;
+    bool on;
+    ~Join2() {
+      if (on) cudaStreamWaitEvent(c->stream, c->join2_ev, 0);
+    }
+  } join2{c, branch};
   int nl = 0;
   prof_begin(c, PR_LIST);
   PairList *pl = nullptr;  // mixed: the skin list itself, cut-off tested in the FP32 kernel
@@ -358,19 +378,10 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   // in-cut pairs, each once (profiling fills c->pl with the exact list)
   const double npairs = c->prof ? list_total(c->stream, c->pl) * (mixed ? 0.5 : 1.0) : 0.0;
   const double ksites = (double)c->nk * na * B;
-  const bool branch = mixed && !c->prof && c->aux2_stream;
   if (branch) {
-    // k-space kernels (low occupancy) on aux2 beside the real-space kernel,
-    // which writes its own gradient buffer; joined before the chain rule
-    recip_set_attributes_mx();
-    CK(cudaEventRecord(c->fork2_ev, c->stream));
-    CK(cudaStreamWaitEvent(c->aux2_stream, c->fork2_ev, 0));
-    launch_recip_sk_mx(c->aux2_stream, c, c->rs, c->z, B);
-    launch_recip_weights_mx(c->aux2_stream, c, B, slot(c, s));
-    launch_recip_force_mx(c->aux2_stream, c, B, c->g);
-    CK(cudaEventRecord(c->join2_ev, c->aux2_stream));
     launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
                          c->tune.ew_np, c->g2, slot(c, s), false);
+    join2.on = false;
     CK(cudaStreamWaitEvent(c->stream, c->join2_ev, 0));
     launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, gscale, sign, accumulate, c->g2);
     c->launches += 7;
