@@ -47,11 +47,11 @@ void launch_skin_check(cudaStream_t s, const PairGeom &g, int nconf, const doubl
 void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref, const unsigned *flag,
                       unsigned *rebuilds);
 // cell-sorted superset build: the cell grid (false: use the all-pairs build),
-// the per-step skin test with cell counts (check = 0: *flag already set), and
-// the gated scatter + build
+// the per-step skin test with cell counts (check = 0: *flag already set; also
+// writes frac / lo as launch_frac32), and the gated scatter + build
 bool list_cell_grid(const PairGeom &g, int nc[3], int *R);
-void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, const CellSort &cs,
-                       const double *ref, double lim2, int check, unsigned *flag);
+void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
+                       const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag);
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
                          unsigned *status, const unsigned *gate, const CellSort &cs);
 void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,

@@ -57,8 +57,8 @@ GB_D float dmin(float hi_a, float lo_a, float hi_b, float lo_b) {
 // four gathers are in flight per lane.
 // bx: side lengths that turn fractional differences into distances (1 in the
 // unit box of the cubic sum; the box in bohr for the non-cubic one,
-// rwald_basic / rwald_cell of ewald_noncubic.f90)
-template <int NP>
+// rwald_basic / rwald_cell of ewald_noncubic.f90); UNIT: all ones (no scaling)
+template <int NP, bool UNIT>
 __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                                                         int na, const int *__restrict__ count,
                                                         const int *__restrict__ idx, int cap, float alpha,
@@ -77,13 +77,18 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
   if (active) {
     const float4 hi_i = H[i], lo_i = Lo[i];
     const float qi = hi_i.w;
-    const int mi = i / 3;
+    const int m3 = (i / 3) * 3;  // first site of i's molecule
     const int n = min(count[(long long)c * na + i], cap);
     const int *L = idx + ((long long)c * na + i) * cap;
     auto pair = [&](int j, const float4 &hj, const float4 &lj) {
-      const float dx = bx.x * dmin(hi_i.x, lo_i.x, hj.x, lj.x);
-      const float dy = bx.y * dmin(hi_i.y, lo_i.y, hj.y, lj.y);
-      const float dz = bx.z * dmin(hi_i.z, lo_i.z, hj.z, lj.z);
+      float dx = dmin(hi_i.x, lo_i.x, hj.x, lj.x);
+      float dy = dmin(hi_i.y, lo_i.y, hj.y, lj.y);
+      float dz = dmin(hi_i.z, lo_i.z, hj.z, lj.z);
+      if (!UNIT) {
+        dx *= bx.x;
+        dy *= bx.y;
+        dz *= bx.z;
+      }
       const float drsq = dx * dx + dy * dy + dz * dz;
       if (!(drsq < rcutsq)) return;  // skin-list entry beyond the cut-off
       const float inv = rsqrtf(drsq);
@@ -91,7 +96,7 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
       const float e = expf(-x * x);
       const float tt = __fdividef(p, p + x);
       float erfc = e * tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5))));
-      if (mi == j / 3) erfc -= 1.0f;
+      if ((unsigned)(j - m3) < 3u) erfc -= 1.0f;  // same molecule
       const float du = erfc * inv;
       const float dur = (sfac * e - du) * (inv * inv);
       const float qij = qi * hj.w;
@@ -550,8 +555,12 @@ void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, in
     constexpr int NP = decltype(NPc)::value;
     dim3 grid(nblk((long long)na * NP, MX_T), B);
     const float sfac = (float)(-2.0 * alpha / std::sqrt(std::acos(-1.0)));  // d erfc(alpha r) / dr factor
-    k_ewald_real_mx<NP><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
-                                              (float)rcutsq, bx, g, acc, add ? 1 : 0);
+    if (bx.x == 1.f && bx.y == 1.f && bx.z == 1.f)
+      k_ewald_real_mx<NP, true><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
+                                                      (float)rcutsq, bx, g, acc, add ? 1 : 0);
+    else
+      k_ewald_real_mx<NP, false><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
+                                                       (float)rcutsq, bx, g, acc, add ? 1 : 0);
   };
   if (np == 8) go(std::integral_constant<int, 8>());
   else if (np == 32) go(std::integral_constant<int, 32>());

@@ -27,10 +27,8 @@ constexpr int LB_T = 128;
 
 // wrapped fractional coordinates u in [0, 1) as FP32 (frac); with lo, also the
 // remainder u - frac as a second FP32, so that frac + lo carries u to ~1e-14
-__global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nconf * g.npt) return;
-  int c = (int)(t / g.npt), i = (int)(t % g.npt);
+// point t = (c, i): frac[t] (and lo[t]) from g.pos; returns frac[t]
+GB_D float4 frac_point(const PairGeom &g, long long t, int c, int i, float4 *frac, float4 *lo, const double *q) {
   const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
   float f[3], e[3];
 #pragma unroll
@@ -43,8 +41,16 @@ __global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo, const 
     e[d] = (float)(u - (double)uf);
     f[d] = uf >= 1.0f ? 0.0f : uf;
   }
-  frac[t] = make_float4(f[0], f[1], f[2], q ? (float)q[i] : 0.0f);
+  const float4 h = make_float4(f[0], f[1], f[2], q ? (float)q[i] : 0.0f);
+  frac[t] = h;
   if (lo) lo[t] = make_float4(e[0], e[1], e[2], 0.0f);
+  return h;
+}
+
+__global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nconf * g.npt) return;
+  frac_point(g, t, (int)(t / g.npt), (int)(t % g.npt), frac, lo, q);
 }
 
 // exact FP64 minimum-image test, rounded as the reference rounds it
@@ -175,8 +181,10 @@ struct CellSortDev {
 
 GB_D int cell_of(float u, int n) { return min((int)(u * (float)n), n - 1); }
 
-__global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, const float4 *frac, CellSortDev cs,
-                                                    const double *ref, double lim2, int check, unsigned *flag) {
+// (also writes the points' fractional coordinates, as k_frac32)
+__global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q,
+                                                    CellSortDev cs, const double *ref, double lim2, int check,
+                                                    unsigned *flag) {
   __shared__ bool last;
   __shared__ int part[256];
   const long long n = (long long)nconf * g.npt;
@@ -191,7 +199,7 @@ __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, const
       const double dx = x[0] - r0[0], dy = x[1] - r0[1], dz = x[2] - r0[2];
       moved = !(dx * dx + dy * dy + dz * dz <= lim2);  // NaN counts as moved
     }
-    const float4 f = frac[t];
+    const float4 f = frac_point(g, t, c, i, frac, lo, q);
     const int cell = (cell_of(f.z, cs.nz) * cs.ny + cell_of(f.y, cs.ny)) * cs.nx + cell_of(f.x, cs.nx);
     cs.cellid[t] = cell;
     cs.crank[t] = atomicAdd(cs.ccount + (long long)c * ncell + cell, 1);
@@ -838,12 +846,12 @@ bool list_cell_grid(const PairGeom &g, int nc[3], int *R) {
 
 // skin test and cell counts (every step), then, gated by flag, the cell-order
 // scatter (which also zeroes the list counts) and the build
-void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, const CellSort &cs,
-                       const double *ref, double lim2, int check, unsigned *flag) {
+void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
+                       const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag) {
   CellSortDev d{cs.nc[0], cs.nc[1], cs.nc[2], cs.R, cs.ccount, cs.cstart, cs.cellid, cs.crank, cs.spos, cs.sidx,
                 cs.ticket};
   const long long n = (long long)nconf * g.npt;
-  k_cell_count<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, d, ref, lim2, check, flag);
+  k_cell_count<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q, d, ref, lim2, check, flag);
 }
 
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,

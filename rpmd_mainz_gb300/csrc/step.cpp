@@ -185,8 +185,8 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   if (use) *use = &c->pl;
   int st = ensure_list(c, nconf, g.npt, list_cap(g.npt, cut, vol));
   if (st) return st;
-  launch_frac32(c->stream, g, nconf, c->rs32, lo, q);
   if (c->list_skin <= 0.0) {
+    launch_frac32(c->stream, g, nconf, c->rs32, lo, q);
     launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
     *nl = 2;
     return GB_OK;
@@ -267,6 +267,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   }
   CK(cudaMemsetAsync(S.flag, same ? 0 : 1, sizeof(unsigned), c->stream));
   int n = 1;
+  if (!S.cells.on) launch_frac32(c->stream, g, nconf, c->rs32, lo, q);  // else in the cell count
   // rebuild when a point moved by more than skin/2 (a hair less, for rounding)
   const double lim = 0.5 * skin * (1.0 - 1e-9);
   PairGeom gs = g;
@@ -274,7 +275,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   if (S.cells.on) {  // skin test and cell counts in one kernel, then the gated sort and build
     cudaError_t e0 = cudaGetLastError();
     if (e0 != cudaSuccess) return ctx_check_cuda(e0, "a launch before the cell count");
-    launch_cell_count(c->stream, g, nconf, c->rs32, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag);
+    launch_cell_count(c->stream, g, nconf, c->rs32, lo, q, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell count launch");
     launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell build launch");
