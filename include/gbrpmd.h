@@ -405,6 +405,16 @@ int gbrpmd_server_poll(gb_server *server, int max, int64_t *ids, int *status, do
 int gbrpmd_run_md_eq(gb_context *ctx, int nsteps, double dt, double beta, double thresh,
                      int *irun, double *energies);
 
+/* Self-check of the conversions the mixed-precision kernels build from
+   integer operations instead of FP64 instructions (no counterpart in the
+   reference): for n doubles in[] (host arrays), f32 = in rounded to the
+   nearest FP32 (ties to even), hi + lo = in split into two FP32 (hi
+   truncated to 24 bits, lo the rest rounded; lo is zero below 2^-75), back
+   = f32 widened exactly.
+   Outside the FP32 normal range values flush to a signed zero or saturate to
+   an infinity. */
+int gbrpmd_selftest_conversions(const double *in, int n, float *f32, float *hi, float *lo, double *back);
+
 #ifdef __cplusplus
 }
 #endif

@@ -151,6 +151,8 @@ int ctx_alloc(gb_context *c, int na, int nb) {
   c->generic_mts = gen && gen[0] == '1';
   if (const char *sk = std::getenv("GBRPMD_LIST_SKIN")) c->list_skin = std::max(0.0, std::atof(sk));
   if (const char *gr = std::getenv("GBRPMD_GRAPHS")) c->use_graphs = gr[0] != '0';
+  if (const char *ce = std::getenv("GBRPMD_LIST_CELLS")) c->list_cells = ce[0] != '0';
+  if (const char *br = std::getenv("GBRPMD_BRANCHES")) c->use_branches = br[0] != '0';
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));

@@ -182,6 +182,8 @@ struct gb_context {
   cudaEvent_t mid_ev = nullptr;
   cudaStream_t copy_stream = nullptr;
   int use_graphs = 1;        // GBRPMD_GRAPHS=0 turns replay off
+  int list_cells = 1;        // GBRPMD_LIST_CELLS=0: all-pairs superset builds only
+  int use_branches = 1;      // GBRPMD_BRANCHES=0: the LJ and k-space kernels stay on the step's stream
   // launch shapes chosen by gbrpmd_ctx_autotune (tune.cpp); results depend on
   // them only through the order of floating-point sums
   struct Tune {

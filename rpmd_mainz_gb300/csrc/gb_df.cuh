@@ -28,7 +28,8 @@ GB_D double f2d(float f) {
 // d = hi + lo to ~2^-47 relative: hi = d truncated to 24 significant bits, lo =
 // the remaining 29 bits rounded to FP32 (same sign).  |d| below 2^-126 (FP32
 // normal range) splits to a signed zero, beyond the FP32 range (and NaN) to
-// an infinity.  Branch-free: the mixed kernels inline it many times.
+// an infinity; below 2^-75 lo is zero (its weight leaves the FP32 range).
+// Branch-free: the mixed kernels inline it many times.
 GB_D void d2df(double d, float &hi, float &lo) {
   const unsigned H = (unsigned)__double2hiint(d), L = (unsigned)__double2loint(d);
   const unsigned s = H & 0x80000000u;

@@ -219,18 +219,21 @@ __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float
       const int per = (ncell + 255) / 256, a = threadIdx.x * per, b = min(ncell, a + per);
       int sum = 0;
       for (int k = a; k < b; ++k) sum += cc[k];
-      part[threadIdx.x] = sum;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        int run = 0;
-        for (int k = 0; k < 256; ++k) {
-          const int v = part[k];
-          part[k] = run;
-          run += v;
-        }
+      // exclusive scan of the 256 chunk sums: within warps by shuffles, then
+      // the 8 warp totals
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      int inc = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
       }
+      if (lane == 31) part[wid] = inc;
       __syncthreads();
-      int run = part[threadIdx.x];
+      int woff = 0;
+      for (int w = 0; w < wid; ++w) woff += part[w];
+      int run = woff + inc - sum;
+      __syncthreads();
       int *st = cs.cstart + (long long)c * (ncell + 1);
       for (int k = a; k < b; ++k) {
         st[k] = run;

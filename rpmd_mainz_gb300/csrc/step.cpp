@@ -236,7 +236,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     PairGeom gsc = g;
     gsc.rcutsq = scut * scut;
     CellSort &cs = S.cells;
-    cs.on = list_cell_grid(gsc, cs.nc, &cs.R);
+    cs.on = c->list_cells && list_cell_grid(gsc, cs.nc, &cs.R);
     if (cs.on) {
       const size_t ncell = (size_t)cs.nc[0] * cs.nc[1] * cs.nc[2];
       const size_t need_cell = sizeof(int) * (size_t)nconf * (2 * ncell + 1);  // counts, then offsets
@@ -350,7 +350,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   // mixed: the k-space kernels (low occupancy, and needing only the M-site
   // positions) run on aux2 beside the list upkeep and the real-space kernel,
   // which writes its own gradient buffer; joined before the chain rule
-  const bool branch = mixed && !c->prof && c->aux2_stream;
+  const bool branch = mixed && !c->prof && c->use_branches && c->aux2_stream;
   if (branch) {
     recip_set_attributes_mx();
     CK(cudaEventRecord(c->fork2_ev, c->stream));
@@ -572,7 +572,7 @@ int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, 
   // expansion), with the context's LJ list and frac buffers swapped in, so that
   // its kernels fill the SMs the k-space kernels leave idle.  Not while
   // profiling (regions are timed on the step's stream).
-  const bool branch = con2 && !c->prof && c->aux_stream;
+  const bool branch = con2 && !c->prof && c->use_branches && c->aux_stream;
   bool joined = true;
   struct Join {  // an error return still joins the branch (a capture needs it)
     gb_context *c;
