@@ -78,6 +78,9 @@ int download(gb_context *c, double *dst, const double *src, size_t n) {
 // captured one)
 int set_masses(gb_context *c, const double *mass) {
   if (!mass) return GB_OK;
+  const size_t bytes = sizeof(double) * (size_t)c->na;
+  if (c->h_mass_all.size() == (size_t)c->na && std::memcmp(c->h_mass_all.data(), mass, bytes) == 0) return GB_OK;
+  c->h_mass_all.assign(mass, mass + c->na);
   const int n = std::min(3, c->na);
   bool same = true;
   for (int i = 0; i < n; ++i) same = same && c->h_mass3[i] == mass[i];
@@ -90,6 +93,9 @@ int set_masses(gb_context *c, const double *mass) {
 
 int set_charges(gb_context *c, const double *z) {
   if (!z) return GB_OK;
+  const size_t bytes = sizeof(double) * (size_t)c->na;
+  if (c->h_z_all.size() == (size_t)c->na && std::memcmp(c->h_z_all.data(), z, bytes) == 0) return GB_OK;
+  c->h_z_all.assign(z, z + c->na);
   double qq = 0.0;
   for (int i = 0; i < c->na; ++i) qq = qq + z[i] * z[i];
   c->qq = qq;

@@ -132,6 +132,10 @@ struct gb_context {
   int monod_mts = -1, monod_mass_version = -1;  // mts and masses
   double h_mass3[3] = {0, 0, 0};  // host copy of the O, H, H masses (ring_rpmd needs only these)
   int mass_version = 0;           // bumped when uploaded masses differ
+  // host copies of the last uploaded masses and charges: a drop-in call that
+  // passes the same arrays again copies nothing (a pageable copy would also
+  // hold the host until the state copies before it are done)
+  std::vector<double> h_mass_all, h_z_all;
   double *acc = nullptr;    // ACC_NSLOT * ACC_STRIDE
   double *est = nullptr;    // estimator sums [16] and per-molecule outputs [2][nm][3] (lazy)
 
