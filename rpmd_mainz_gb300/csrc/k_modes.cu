@@ -161,16 +161,6 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
   extern __shared__ double smx[];
   R *E = reinterpret_cast<R *>(smx);  // [nb][NQ]
   R *CF = E + nb * NQ;                // [XR][NQ]
-  for (int w = threadIdx.x; w < nb * NQ; w += blockDim.x) {
-    const int j = w / NQ, q = w % NQ;
-    double v = sc;
-    if (q > 0) {
-      const int k = (q + 1) / 2, m = (j * k) % nb;
-      v = (q & 1) ? 2.0 * sc * tw_nb[m] : -2.0 * sc * tw_nb[nb + m];
-    }
-    if constexpr (F32) E[w] = d2f(v);
-    else E[w] = v;
-  }
   const long long S = 3LL * na;
   const bool any = fb1 || fb2;
   const int lr = threadIdx.x % XR, grp = threadIdx.x / XR;
@@ -220,6 +210,18 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
     }
 #pragma unroll
     for (int q = 0; q < NQ; ++q) CF[lr * NQ + q] = cf[q];
+  }
+  // the expansion table, after the coefficients' loads are on their way (one
+  // barrier for both); FP32 variant without FP64 instructions
+  for (int w = threadIdx.x; w < nb * NQ; w += blockDim.x) {
+    const int j = w / NQ, q = w % NQ;
+    const int k = (q + 1) / 2, m = (j * k) % nb;
+    if constexpr (F32) {
+      const float scf = d2f(sc);
+      E[w] = q == 0 ? scf : ((q & 1) ? 2.f * scf * d2f(tw_nb[m]) : -2.f * scf * d2f(tw_nb[nb + m]));
+    } else {
+      E[w] = q == 0 ? sc : ((q & 1) ? 2.0 * sc * tw_nb[m] : -2.0 * sc * tw_nb[nb + m]);
+    }
   }
   __syncthreads();
   if (row >= S) return;

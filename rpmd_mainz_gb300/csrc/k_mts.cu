@@ -251,21 +251,18 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
   float *s_ct = s_twi_l + 2 * NB;                  // [2][2*MTS_NBC] contraction cos, sin
   const int t = threadIdx.x;
   const double sc = a.sc;
+  // FP32 hi + lo splits of the tables (d2df: integer operations, no FP64
+  // conversions)
   for (int i = t; i < 12 * NB; i += T) {
     const double w = a.monod[i];
-    const float h = (float)w;
-    s_mh[i] = h;
-    s_ml[i] = (float)(w - (double)h);
+    d2df(w, s_mh[i], s_ml[i]);
     if (i < 12) s_mono[i] = w;
   }
   for (int i = t; i < 2 * NB; i += T) {
     const double w = a.tw[i], wf = (0.5 * sc) * w, wi = sc * w;
-    s_tw[i] = (float)w;
-    s_twf[i] = (float)wf;
-    s_twi[i] = (float)wi;
-    s_tw_l[i] = (float)(w - (double)s_tw[i]);
-    s_twf_l[i] = (float)(wf - (double)s_twf[i]);
-    s_twi_l[i] = (float)(wi - (double)s_twi[i]);
+    d2df(w, s_tw[i], s_tw_l[i]);
+    d2df(wf, s_twf[i], s_twf_l[i]);
+    d2df(wi, s_twi[i], s_twi_l[i]);
   }
   for (int i = t; i < 4 * MTS_NBC; i += T) {
     const int q = i / (2 * MTS_NBC), e = i % (2 * MTS_NBC);
