@@ -284,30 +284,41 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
   int *my = idx + ((long long)c * npt + i) * cap;
   int n = 0;  // the same in every lane
   // lanes take consecutive cell-order slots (coalesced); hits keep slot order
+  // four 32-slot groups per round: their loads are issued together (the loop
+  // is otherwise bound by one L2 round trip per 32 slots)
   auto scan = [&](int k0, int k1) {
-    for (int kb = k0; kb < k1; kb += 32) {
-      const int k = kb + lane;
-      bool hit = false;
-      int j = 0;
-      if (k < k1) {
-        const float4 fj = sp[k];
-        float dx = fi.x - fj.x, dy = fi.y - fj.y, dz = fi.z - fj.z;
-        dx = (dx - rintf(dx)) * len.x;
-        dy = (dy - rintf(dy)) * len.y;
-        dz = (dz - rintf(dz)) * len.z;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        if (d2 < thr_hi) {
-          j = si[k];
-          hit = j != i && (FULL || (i < j) == (((i + j) & 1) != 0)) && (!EXCL || (i / 3) != (j / 3)) &&
-                (d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride));
+    for (int kb = k0; kb < k1; kb += 128) {
+      float4 fj[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + 32 * u + lane;
+        fj[u] = k < k1 ? sp[k] : make_float4(2.f, 2.f, 2.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (kb + 32 * u >= k1) break;  // the same in every lane
+        const int k = kb + 32 * u + lane;
+        bool hit = false;
+        int j = 0;
+        if (k < k1) {
+          float dx = fi.x - fj[u].x, dy = fi.y - fj[u].y, dz = fi.z - fj[u].z;
+          dx = (dx - rintf(dx)) * len.x;
+          dy = (dy - rintf(dy)) * len.y;
+          dz = (dz - rintf(dz)) * len.z;
+          const float d2 = dx * dx + dy * dy + dz * dz;
+          if (d2 < thr_hi) {
+            j = si[k];
+            hit = j != i && (FULL || (i < j) == (((i + j) & 1) != 0)) && (!EXCL || (i / 3) != (j / 3)) &&
+                  (d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride));
+          }
         }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+          const int pos = n + __popc(m & ((1u << lane) - 1u));
+          if (pos < cap) my[pos] = j;
+        }
+        n += __popc(m);
       }
-      const unsigned m = __ballot_sync(0xffffffffu, hit);
-      if (hit) {
-        const int pos = n + __popc(m & ((1u << lane) - 1u));
-        if (pos < cap) my[pos] = j;
-      }
-      n += __popc(m);
     }
   };
   const int R = cs.R;
