@@ -31,6 +31,7 @@ struct PairList {
 struct CellSort {
   bool on = false;
   int nc[3] = {0, 0, 0}, R = 1;
+  signed char reach[13 * 13] = {};  // stencil rows: largest |ox| within the cut-off, -1: none
   int *ccount = nullptr;         // [nconf][ncell], zero between steps
   int *cstart = nullptr;         // [nconf][ncell + 1]
   int *cellid = nullptr, *crank = nullptr, *sidx = nullptr;  // [nconf][npt]

@@ -49,7 +49,7 @@ void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref,
 // cell-sorted superset build: the cell grid (false: use the all-pairs build),
 // the per-step skin test with cell counts (check = 0: *flag already set; also
 // writes frac / lo as launch_frac32), and the gated scatter + build
-bool list_cell_grid(const PairGeom &g, int nc[3], int *R);
+bool list_cell_grid(const PairGeom &g, int nc[3], int *R, signed char *reach);
 void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
                        const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag);
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,

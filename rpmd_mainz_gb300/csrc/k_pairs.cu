@@ -17,6 +17,7 @@
 // accumulator slot.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "gb_common.cuh"
 #include "gb_kernels.h"
@@ -168,8 +169,12 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
 // cells are contiguous runs of the cell order, which the lanes read in
 // coalesced 32-slot steps; hits are appended through a ballot (no atomics).
 // The FP32 prefilter and the FP64 band test are those of k_build_list2.
+constexpr int CELL_RMAX = 6;  // largest stencil radius in cells
 struct CellSortDev {
   int nx, ny, nz, R;
+  // per stencil row (oz, oy): the largest |ox| whose cells can hold a pair
+  // within the cut-off, -1 when none can ([2R+1][2R+1])
+  signed char reach[(2 * CELL_RMAX + 1) * (2 * CELL_RMAX + 1)];
   int *ccount;     // [nconf][ncell], zero between steps
   int *cstart;     // [nconf][ncell + 1]
   int *cellid;     // [nconf][npt]
@@ -325,9 +330,11 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
   for (int oz = -R; oz <= R; ++oz) {
     const int z = (z0 + oz + cs.nz) % cs.nz;
     for (int oy = -R; oy <= R; ++oy) {
+      const int rx = cs.reach[(oz + R) * (2 * R + 1) + (oy + R)];
+      if (rx < 0) continue;  // no cell of this row is within the cut-off
       const int y = (y0 + oy + cs.ny) % cs.ny;
       const int row = (z * cs.ny + y) * cs.nx;
-      const int xa = x0 - R, xb = x0 + R;  // the x cells, wrapped into one or two runs
+      const int xa = x0 - rx, xb = x0 + rx;  // the x cells, wrapped into one or two runs
       if (xa >= 0 && xb < cs.nx) {
         scan(st[row + xa], st[row + xb + 1]);
       } else if (xa < 0) {
@@ -827,43 +834,86 @@ void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref,
   k_skin_save<<<nblk(n, 256), 256, 0, s>>>(g, nconf, ref, flag, rebuilds);
 }
 
-// The cell grid of a superset build: R = 1..3 cells per largest accepted
-// distance, the R whose stencil covers the smallest share of the box; false
-// when no R gives 2R + 1 cells per axis or the stencil would cover more than
-// 60 % of the box (the all-pairs build is used)
-bool list_cell_grid(const PairGeom &g, int nc[3], int *R) {
+// The cell grid of a superset build: cells of side >= 1/R of the largest
+// accepted distance (R = 1..CELL_RMAX, 2R + 1 cells per axis at least), the
+// stencil pruned to the cells that can hold a pair within that distance (with
+// a margin for the FP32 cell index), and the R of the lowest estimated scan
+// cost (stencil points plus a fixed cost per stencil row); false when even
+// that exceeds 60 % of an all-pairs scan (the all-pairs build is used).
+bool list_cell_grid(const PairGeom &g, int nc[3], int *R, signed char *reach) {
   float3 len;
   float thr_lo, thr_hi;
   list_thresholds(g, &len, &thr_lo, &thr_hi);
-  const double side = std::sqrt((double)thr_hi) * (1.0 + 1e-5);
+  const double cut = std::sqrt((double)thr_hi) * (1.0 + 1e-5);
+  const double cut2 = cut * cut * (1.0 + 1e-4);
   const double L[3] = {len.x, len.y, len.z};
-  double best = 0.6;
+  double best = 0.6;  // estimated cost per point, in all-pairs scans
   bool found = false;
-  for (int r = 1; r <= 3; ++r) {
+  for (int r = 1; r <= CELL_RMAX; ++r) {
     int n[3];
-    double share = 1.0;
     bool ok = true;
+    double side[3];
     for (int d = 0; d < 3; ++d) {
-      n[d] = (int)std::min(std::floor(L[d] * r / side), 128.0);
+      n[d] = (int)std::min(std::floor(L[d] * r / cut), 128.0);
       ok = ok && n[d] >= 2 * r + 1;
-      share *= (2.0 * r + 1.0) / std::max(n[d], 1);
+      side[d] = L[d] / std::max(n[d], 1) * (1.0 - 1e-5);
     }
-    if (ok && share < best) {
-      best = share;
+    if (!ok) continue;
+    const double ncell = (double)n[0] * n[1] * n[2];
+    auto gap = [](int o, double s) {
+      const double q = std::max(0, std::abs(o) - 1) * s;
+      return q * q;
+    };
+    signed char rr[(2 * CELL_RMAX + 1) * (2 * CELL_RMAX + 1)];
+    double cells = 0.0, rows = 0.0;
+    for (int oz = -r; oz <= r; ++oz)
+      for (int oy = -r; oy <= r; ++oy) {
+        const double dyz = gap(oy, side[1]) + gap(oz, side[2]);
+        int rx = -1;
+        for (int ox = 0; ox <= r; ++ox)
+          if (dyz + gap(ox, side[0]) < cut2) rx = ox;
+        rr[(oz + r) * (2 * r + 1) + (oy + r)] = (signed char)rx;
+        if (rx >= 0) {
+          cells += 2 * rx + 1;
+          rows += 1.0;
+        }
+      }
+    const double cost = cells / ncell + rows * 24.0 / std::max(1, g.npt);
+    if (cost < best) {
+      best = cost;
       found = true;
       *R = r;
       for (int d = 0; d < 3; ++d) nc[d] = n[d];
+      std::memcpy(reach, rr, sizeof rr);
     }
   }
   return found;
+}
+
+static_assert(sizeof(CellSort::reach) == sizeof(CellSortDev::reach), "stencil table sizes");
+
+CellSortDev dev_cells(const CellSort &cs) {
+  CellSortDev d{};
+  d.nx = cs.nc[0];
+  d.ny = cs.nc[1];
+  d.nz = cs.nc[2];
+  d.R = cs.R;
+  std::memcpy(d.reach, cs.reach, sizeof d.reach);
+  d.ccount = cs.ccount;
+  d.cstart = cs.cstart;
+  d.cellid = cs.cellid;
+  d.crank = cs.crank;
+  d.spos = cs.spos;
+  d.sidx = cs.sidx;
+  d.ticket = cs.ticket;
+  return d;
 }
 
 // skin test and cell counts (every step), then, gated by flag, the cell-order
 // scatter (which also zeroes the list counts) and the build
 void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
                        const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag) {
-  CellSortDev d{cs.nc[0], cs.nc[1], cs.nc[2], cs.R, cs.ccount, cs.cstart, cs.cellid, cs.crank, cs.spos, cs.sidx,
-                cs.ticket};
+  CellSortDev d = dev_cells(cs);
   const long long n = (long long)nconf * g.npt;
   k_cell_count<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q, d, ref, lim2, check, flag);
 }
@@ -873,8 +923,7 @@ void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const flo
   float3 len;
   float thr_lo, thr_hi;
   list_thresholds(g, &len, &thr_lo, &thr_hi);
-  CellSortDev d{cs.nc[0], cs.nc[1], cs.nc[2], cs.R, cs.ccount, cs.cstart, cs.cellid, cs.crank, cs.spos, cs.sidx,
-                cs.ticket};
+  CellSortDev d = dev_cells(cs);
   const long long n = (long long)nconf * g.npt;
   k_cell_scatter<<<nblk(n, 256), 256, 0, s>>>(g.npt, nconf, frac, d, pl.count, gate);
   auto go = [&](auto kern) {

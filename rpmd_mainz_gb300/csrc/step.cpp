@@ -236,7 +236,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     PairGeom gsc = g;
     gsc.rcutsq = scut * scut;
     CellSort &cs = S.cells;
-    cs.on = c->list_cells && list_cell_grid(gsc, cs.nc, &cs.R);
+    cs.on = c->list_cells && list_cell_grid(gsc, cs.nc, &cs.R, cs.reach);
     if (cs.on) {
       const size_t ncell = (size_t)cs.nc[0] * cs.nc[1] * cs.nc[2];
       const size_t need_cell = sizeof(int) * (size_t)nconf * (2 * ncell + 1);  // counts, then offsets
