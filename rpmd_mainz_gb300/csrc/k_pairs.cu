@@ -160,13 +160,14 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
 // ---- cell-sorted build (skin supersets) ----
 // The wrapped fractional box is cut into nx * ny * nz cells of side at least
 // 1/R of the largest accepted distance, so that every pair within it joins
-// points whose cells differ by at most R per axis (R = 1..3, nx, ny, nz >=
-// 2R + 1: the (2R+1)^3 stencil cells are distinct).  Every step k_cell_count
+// points whose cells differ by at most R per axis (R = 1..6, nx, ny, nz >=
+// 2R + 1: the (2R+1)^3 stencil cells are distinct; rows and row ends whose
+// cells lie wholly beyond that distance are pruned).  Every step k_cell_count
 // takes the skin test (moved points) and counts the points per cell; its last
 // block turns the counts into cell offsets when a rebuild is due and clears
 // them.  On a rebuild k_cell_scatter writes the points in cell order and
-// k_build_sorted runs one warp per point: the (2R+1)^2 x-rows of stencil
-// cells are contiguous runs of the cell order, which the lanes read in
+// k_build_sorted runs one warp per point: the x-rows of stencil cells are
+// contiguous runs of the cell order, which the lanes read in
 // coalesced 32-slot steps; hits are appended through a ballot (no atomics).
 // The FP32 prefilter and the FP64 band test are those of k_build_list2.
 constexpr int CELL_RMAX = 6;  // largest stencil radius in cells
@@ -269,7 +270,10 @@ template <bool FULL, bool EXCL>
 __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, CellSortDev cs, int *count, int *idx,
                                                        int cap, float3 len, float thr_lo, float thr_hi,
                                                        unsigned *status, const unsigned *gate) {
+  __shared__ signed char s_reach[sizeof(cs.reach)];
   if (*gate == 0u) return;
+  for (int t = threadIdx.x; t < (int)sizeof(cs.reach); t += blockDim.x) s_reach[t] = cs.reach[t];
+  __syncthreads();
   const int npt = g.npt;
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per point
   const int lane = threadIdx.x & 31;
@@ -327,12 +331,13 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
     }
   };
   const int R = cs.R;
+  auto wrap = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };  // |offset| <= R < n
   for (int oz = -R; oz <= R; ++oz) {
-    const int z = (z0 + oz + cs.nz) % cs.nz;
+    const int z = wrap(z0 + oz, cs.nz);
     for (int oy = -R; oy <= R; ++oy) {
-      const int rx = cs.reach[(oz + R) * (2 * R + 1) + (oy + R)];
+      const int rx = s_reach[(oz + R) * (2 * R + 1) + (oy + R)];
       if (rx < 0) continue;  // no cell of this row is within the cut-off
-      const int y = (y0 + oy + cs.ny) % cs.ny;
+      const int y = wrap(y0 + oy, cs.ny);
       const int row = (z * cs.ny + y) * cs.nx;
       const int xa = x0 - rx, xb = x0 + rx;  // the x cells, wrapped into one or two runs
       if (xa >= 0 && xb < cs.nx) {
