@@ -340,15 +340,18 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
       const int y = wrap(y0 + oy, cs.ny);
       const int row = (z * cs.ny + y) * cs.nx;
       const int xa = x0 - rx, xb = x0 + rx;  // the x cells, wrapped into one or two runs
+      int a0, a1, b0 = 0, b1 = 0;
       if (xa >= 0 && xb < cs.nx) {
-        scan(st[row + xa], st[row + xb + 1]);
+        a0 = st[row + xa], a1 = st[row + xb + 1];
       } else if (xa < 0) {
-        scan(st[row], st[row + xb + 1]);
-        scan(st[row + cs.nx + xa], st[row + cs.nx]);
+        a0 = st[row], a1 = st[row + xb + 1];
+        b0 = st[row + cs.nx + xa], b1 = st[row + cs.nx];
       } else {
-        scan(st[row + xa], st[row + cs.nx]);
-        scan(st[row], st[row + xb - cs.nx + 1]);
+        a0 = st[row + xa], a1 = st[row + cs.nx];
+        b0 = st[row], b1 = st[row + xb - cs.nx + 1];
       }
+#pragma unroll 1
+      for (int q = 0; q < 2; ++q) scan(q ? b0 : a0, q ? b1 : a1);  // one copy of the scan's code
     }
   }
   if (lane == 0) {
