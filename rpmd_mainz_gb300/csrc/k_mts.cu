@@ -345,19 +345,18 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
     }
     {  // bead positions relative to the oxygen centroid (evolve_pi.f90:141-145)
       float *dst = s_dev + t * C::LD;
-      if (im == a.mts) {  // the last substep's positions are the new state: split tables,
-                          // and r = centroid + deviation without the offset's rounding
-        double *gr = a.r + row;
-        gb_hc2r_s<NB, float, true>([&](int j) { return j ? xf[j] : 0.f; },
-                                   [&](int k, float v) {
-                                     dst[k] = off + v;
-                                     if (valid) gr[S * k] = cen + f2d(v);
-                                   },
-                                   s_tw, s_twi, s_tw_l, s_twi_l);
-      } else {
-        gb_hc2r_s<NB, float>([&](int j) { return j ? xf[j] : 0.f; }, [&](int k, float v) { dst[k] = off + v; },
-                             s_tw, s_twi);
-      }
+      // split tables in every substep (one copy of the transform's code: the
+      // kernel is large enough to stall on the instruction cache); the last
+      // substep's positions are the new state, r = centroid + deviation
+      // without the offset's rounding
+      const bool last = im == a.mts && valid;
+      double *gr = a.r + row;
+      gb_hc2r_s<NB, float, true>([&](int j) { return j ? xf[j] : 0.f; },
+                                 [&](int k, float v) {
+                                   dst[k] = off + v;
+                                   if (last) gr[S * k] = cen + f2d(v);
+                                 },
+                                 s_tw, s_twi, s_tw_l, s_twi_l);
     }
     __syncthreads();
     float esh = 0.f, esl = 0.f;
