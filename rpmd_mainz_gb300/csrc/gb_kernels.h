@@ -52,8 +52,10 @@ void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref,
 bool list_cell_grid(const PairGeom &g, int nc[3], int *R, signed char *reach);
 void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
                        const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag);
+// (also saves the reference positions and counts the rebuild, as launch_skin_save)
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
-                         unsigned *status, const unsigned *gate, const CellSort &cs);
+                         unsigned *status, const unsigned *gate, const CellSort &cs, double *ref,
+                         unsigned *rebuilds);
 void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
                         const PairList &skin, PairList &pl, unsigned *status);
 double list_total(cudaStream_t s, const PairList &pl);  // profiling only (synchronises)

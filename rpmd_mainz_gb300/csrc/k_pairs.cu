@@ -253,13 +253,21 @@ __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float
   if (threadIdx.x == 0) *cs.ticket = 0u;
 }
 
-__global__ void k_cell_scatter(int npt, int nconf, const float4 *frac, CellSortDev cs, int *lcount,
-                               const unsigned *gate) {
+// (also the skin-list bookkeeping of k_skin_save: reference positions and the
+// rebuild count)
+__global__ void k_cell_scatter(PairGeom g, int nconf, const float4 *frac, CellSortDev cs, int *lcount,
+                               const unsigned *gate, double *ref, unsigned *rebuilds) {
   if (*gate == 0u) return;
+  const int npt = g.npt;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) atomicAdd(rebuilds, 1u);
   if (t >= (long long)nconf * npt) return;
   lcount[t] = 0;
   const int c = (int)(t / npt), i = (int)(t % npt);
+  const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
+  ref[3 * t] = x[0];
+  ref[3 * t + 1] = x[1];
+  ref[3 * t + 2] = x[2];
   const int ncell = cs.nx * cs.ny * cs.nz;
   const long long pos = (long long)c * npt + cs.cstart[(long long)c * (ncell + 1) + cs.cellid[t]] + cs.crank[t];
   cs.spos[pos] = frac[t];
@@ -927,13 +935,14 @@ void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *fra
 }
 
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
-                         unsigned *status, const unsigned *gate, const CellSort &cs) {
+                         unsigned *status, const unsigned *gate, const CellSort &cs, double *ref,
+                         unsigned *rebuilds) {
   float3 len;
   float thr_lo, thr_hi;
   list_thresholds(g, &len, &thr_lo, &thr_hi);
   CellSortDev d = dev_cells(cs);
   const long long n = (long long)nconf * g.npt;
-  k_cell_scatter<<<nblk(n, 256), 256, 0, s>>>(g.npt, nconf, frac, d, pl.count, gate);
+  k_cell_scatter<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, d, pl.count, gate, ref, rebuilds);
   auto go = [&](auto kern) {
     kern<<<nblk(32 * n, LB_T), LB_T, 0, s>>>(g, nconf, d, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status,
                                              gate);

@@ -266,8 +266,8 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     }
   }
   CK(cudaMemsetAsync(S.flag, same ? 0 : 1, sizeof(unsigned), c->stream));
-  int n = 1;
-  if (!S.cells.on) launch_frac32(c->stream, g, nconf, c->rs32, lo, q);  // else in the cell count
+  int n = S.cells.on ? 0 : 1;  // the frac32 launch (else in the cell count)
+  if (!S.cells.on) launch_frac32(c->stream, g, nconf, c->rs32, lo, q);
   // rebuild when a point moved by more than skin/2 (a hair less, for rounding)
   const double lim = 0.5 * skin * (1.0 - 1e-9);
   PairGeom gs = g;
@@ -277,18 +277,17 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     if (e0 != cudaSuccess) return ctx_check_cuda(e0, "a launch before the cell count");
     launch_cell_count(c->stream, g, nconf, c->rs32, lo, q, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell count launch");
-    launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells);
+    launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells, S.ref, S.rebuilds);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell build launch");
-    n += 1;
   } else {
     if (same) {
       launch_skin_check(c->stream, g, nconf, S.ref, lim * lim, S.flag);
       n += 1;
     }
     launch_build_list(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag);
+    launch_skin_save(c->stream, g, nconf, S.ref, S.flag, S.rebuilds);
   }
-  launch_skin_save(c->stream, g, nconf, S.ref, S.flag, S.rebuilds);
-  n += 3;
+  n += 3;  // cells: count, scatter (+ save), build; else zero, build, save
   if (superset && use) {
     *use = &S.pl;
     // profiling counts in-cut pairs: the exact list is made for the count only
