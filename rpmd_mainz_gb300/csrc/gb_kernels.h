@@ -62,9 +62,10 @@ double list_total(cudaStream_t s, const PairList &pl);  // profiling only (synch
 int list_max(cudaStream_t s, const PairList &pl);       // diagnostics only (synchronises)
 
 // ---- Ewald, unit box (k_pairs.cu, k_recip.cu) ----
-// rs: M-site substituted positions scaled by 1/L, [B][na][3]
+// rs: M-site substituted positions scaled by 1/L, [B][na][3]; gz (optional,
+// [B][na][3]) is zeroed by the same launch
 void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, double alpha,
-                  double scale);
+                  double scale, double *gz = nullptr);
 // box: nullptr for unit-box positions (cubic sum), else the box in bohr (non-cubic)
 void launch_ewald_real(cudaStream_t s, const double *rs, const double *q, int na, int B,
                        const PairList &pl, double alpha, const double *box, double *g, double *acc);

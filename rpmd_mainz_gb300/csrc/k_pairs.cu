@@ -449,8 +449,10 @@ __global__ void __launch_bounds__(128) k_list_filter(PairGeom g, int nconf, cons
 }
 
 // ---- M-site substitution and scaling (md_forces.f90:179-188, ewald_cubic.f90:20-22) ----
+// (zeroes the same entries of gz when given: the gradient buffer the Ewald
+// kernels then accumulate into)
 __global__ void k_msite(const double *r, double *rs, int nm, int B, double alpha, double alpha2,
-                        double scale) {
+                        double scale, double *gz) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nm * B * 3) return;
   const int d = (int)(t % 3);
@@ -461,6 +463,12 @@ __global__ void k_msite(const double *r, double *rs, int nm, int B, double alpha
   o[d] = scale * ro;
   o[3 + d] = scale * m[3 + d];
   o[6 + d] = scale * m[6 + d];
+  if (gz) {
+    double *z = gz + mb * 9;
+    z[d] = 0.0;
+    z[3 + d] = 0.0;
+    z[6 + d] = 0.0;
+  }
 }
 
 // out = sign * chain_rule(scale * g)  (md_forces.f90:206-215)
@@ -967,10 +975,10 @@ void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const floa
 }
 
 void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, double alpha,
-                  double scale) {
+                  double scale, double *gz) {
   int nm = na / 3;
   long long n = (long long)nm * B * 3;
-  k_msite<<<nblk(n, 256), 256, 0, s>>>(r, rs, nm, B, alpha, 0.5 * (1.0 - alpha), scale);
+  k_msite<<<nblk(n, 256), 256, 0, s>>>(r, rs, nm, B, alpha, 0.5 * (1.0 - alpha), scale, gz);
 }
 
 void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, int B, double alpha,

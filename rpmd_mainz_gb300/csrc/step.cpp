@@ -329,8 +329,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   const double L = c->box[0], onboxl = 1.0 / L;
   const double pscale = cub ? onboxl : 1.0, gscale = cub ? onboxl * onboxl : 1.0;
   prof_begin(c, PR_MSITE);
-  launch_msite(c->stream, r, c->rs, na, B, c->P.alpha, pscale);
-  CK(cudaMemsetAsync(c->g, 0, sizeof(double) * 3 * (size_t)na * B, c->stream));
+  launch_msite(c->stream, r, c->rs, na, B, c->P.alpha, pscale, c->g);  // and g = 0
   prof_end(c, PR_MSITE, (double)na * B);
   PairGeom g{};
   g.pos = c->rs;
