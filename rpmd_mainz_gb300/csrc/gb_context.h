@@ -36,7 +36,7 @@ struct CellSort {
   int *cstart = nullptr;         // [nconf][ncell + 1]
   int *cellid = nullptr, *crank = nullptr, *sidx = nullptr;  // [nconf][npt]
   float4 *spos = nullptr;        // [nconf][npt]
-  unsigned *ticket = nullptr;    // blocks done in the count kernel
+  unsigned *ticket = nullptr;    // [2]: blocks done in the count kernel, a point moved
   size_t cell_bytes = 0, pt_bytes = 0;
 };
 

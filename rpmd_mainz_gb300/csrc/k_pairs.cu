@@ -182,7 +182,7 @@ struct CellSortDev {
   int *crank;      // [nconf][npt] rank in the cell (arbitrary order)
   float4 *spos;    // [nconf][npt] fractional positions in cell order
   int *sidx;       // [nconf][npt] point of each cell-order slot
-  unsigned *ticket;
+  unsigned *ticket;  // [0] blocks done in the count kernel, [1] a point moved
 };
 
 GB_D int cell_of(float u, int n) { return min((int)(u * (float)n), n - 1); }
@@ -210,14 +210,23 @@ __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float
     cs.cellid[t] = cell;
     cs.crank[t] = atomicAdd(cs.ccount + (long long)c * ncell + cell, 1);
   }
-  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(cs.ticket + 1, 1u);
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) last = atomicAdd(cs.ticket, 1u) == gridDim.x - 1;
   __syncthreads();
   if (!last) return;
   __threadfence();
-  const bool rebuild = *(volatile unsigned *)flag != 0u;
+  // the decision of this step: the gate of the scatter and build kernels;
+  // the moved word is cleared for the next step (no memset per step)
+  __shared__ bool s_rebuild;
+  if (threadIdx.x == 0) {
+    s_rebuild = !check || *(volatile unsigned *)(cs.ticket + 1) != 0u;
+    *flag = s_rebuild ? 1u : 0u;
+    cs.ticket[1] = 0u;
+  }
+  __syncthreads();
+  const bool rebuild = s_rebuild;
   volatile int *cnt = cs.ccount;
   for (int c = 0; c < nconf; ++c) {
     volatile int *cc = cnt + (long long)c * ncell;

@@ -255,17 +255,18 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
         CK(cudaMalloc(&cs.spos, need_pt));
         cs.pt_bytes = need_pt;
       }
-      if (!cs.ticket) CK(cudaMalloc(&cs.ticket, sizeof(unsigned)));
+      if (!cs.ticket) CK(cudaMalloc(&cs.ticket, 2 * sizeof(unsigned)));
       cs.cstart = cs.ccount + (size_t)nconf * ncell;
       const size_t np = (size_t)nconf * g.npt;
       cs.cellid = reinterpret_cast<int *>(cs.spos + np);
       cs.crank = cs.cellid + np;
       cs.sidx = cs.crank + np;
       CK(cudaMemsetAsync(cs.ccount, 0, need_cell, c->stream));
-      CK(cudaMemsetAsync(cs.ticket, 0, sizeof(unsigned), c->stream));
+      CK(cudaMemsetAsync(cs.ticket, 0, 2 * sizeof(unsigned), c->stream));
     }
   }
-  CK(cudaMemsetAsync(S.flag, same ? 0 : 1, sizeof(unsigned), c->stream));
+  // the cell count kernel writes the gate itself
+  if (!S.cells.on) CK(cudaMemsetAsync(S.flag, same ? 0 : 1, sizeof(unsigned), c->stream));
   int n = S.cells.on ? 0 : 1;  // the frac32 launch (else in the cell count)
   if (!S.cells.on) launch_frac32(c->stream, g, nconf, c->rs32, lo, q);
   // rebuild when a point moved by more than skin/2 (a hair less, for rounding)
