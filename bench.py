@@ -48,13 +48,20 @@ DEFAULT = "qspcfw_4096_nb32_mts5_contracted"
 BATCH_WORKLOADS = ("replicas_256", "served_stream", "qspcfw_216_nb32_nve")
 REGIONS = ["mts_block", "pair_lists", "ewald_real", "recip_sk", "recip_weights", "recip_force", "lj",
            "tem", "expand_kick", "msite", "rattle"]
-# algorithmic FP64 flops per work unit of a region (declared weights):
+# algorithmic flops per work unit of a region (declared weights):
 # real-space in-cut pair 60; reciprocal (k vector, site) 12 with kz and -kz
 # taken together: 4 in the structure-factor pass (two complex-times-real FMAs
 # per pair of vectors), 8 in the force pass (eight FMAs per pair of vectors);
 # LJ pair 45
 PROF_STEPS = 10
 FLOPS_PER_UNIT = {"ewald_real": 60.0, "recip_sk": 4.0, "recip_force": 8.0, "lj": 45.0}
+# the multiple-time-step block streams the FP64 state: r, p, dvdr, dvdr2 read
+# and written once per outer step, 8 arrays x 3 coordinates x 8 bytes per
+# bead-atom = 576 bytes per bead-molecule (its ALU work is a few flops per byte)
+BYTES_PER_BEAD_MOLECULE = {"mts_block": 576.0}
+# regions whose kernel can be watched inside the timed (graph-replayed) steps
+WATCHABLE = ("mts_block", "ewald_real", "recip_force", "lj")
+FALLBACK_HBM_GBS = 6800.0
 
 
 def log(*a):
@@ -94,6 +101,37 @@ def make_system(name):
     irun = C.c_int(-4711)
     s["p"] = system.sample_momenta(s["na"], s["nb"], s["mass"], s["beta"], irun)
     return s
+
+
+def make_system_oracle(name):
+    """The same workload set up by the oracle's own restatement of the
+    reference's set-up (setup_box_size, the CUB lattice, setup_ewald,
+    sample_rpmd from seed -4711): the reference arm loads no product code."""
+    from tests import oracle_lib as orc
+    from tests import systems
+
+    s = systems.build(param="param_qspcfw", **WORKLOADS[name])
+    s["p"] = orc.sample_rpmd(s["na"], s["nb"], s["mass"], s["beta"], orc.Rng(4711))
+    return s
+
+
+def workload_config(name, s):
+    """The `config` of both arms: the workload and its sizes only."""
+    return {"workload": name, "nm": s["nm"], "nb": s["nb"], "mts": s["params"].mts, "nbdf1": s["params"].nbdf1,
+            "nbdf2": s["params"].nbdf2,
+            "l2": "GPU arm: 256 MiB written between timed steps (L2 flush), outside the timed events",
+            "parallelism": "replicas only: one trajectory per GPU, one per host thread on the CPU"}
+
+
+def measured_hbm_peak():
+    """HBM copy bandwidth from MEASURED_PEAKS.json, else the fallback figure."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            v = float(json.load(f)["hbm_gbs"])
+        return v, "measured (MEASURED_PEAKS.json hbm_gbs: STREAM-style copy on this pool's GB300)"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback (no MEASURED_PEAKS.json): 6.8 TB/s, one earlier GB300 measurement"
 
 
 class ClockSampler:
@@ -218,7 +256,7 @@ def cpu_baseline(s, seconds_target=15.0):
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    s = make_system(args.workload)
+    s = make_system_oracle(args.workload)
     from tests import oracle_lib as orc
 
     orc.set_params(s["params"])
@@ -236,8 +274,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": "bead-molecule-steps/s", "value": value, "unit": "bead-molecule-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "nm": s["nm"], "nb": s["nb"], "mts": s["params"].mts,
-                   "nbdf1": s["params"].nbdf1, "nbdf2": s["params"].nbdf2, "parallelism": "replicas"},
+        "config": workload_config(args.workload, s),
         "cpu_baseline": {"value": value, "unit": "bead-molecule-steps/s", "cores": threads, "kind": "port",
                          "sample": f"each step: {threads} host threads advance one independent trajectory by one "
                                    f"evolve_pi step (C++ restatement of the Fortran reference)"},
@@ -290,6 +327,12 @@ def measure(args, s, prec, torch, world, local):
     regions = {REGIONS[i]: {"ms": float(ms[i]) / PROF_STEPS, "launches": int(cnt[i]) / PROF_STEPS,
                             "units": float(units[i]) / PROF_STEPS}
                for i in range(R) if cnt[i]}
+    # the dominant kernel region of the profiled pass is watched in the timed
+    # steps: timing events around its launch, captured into the step graph
+    dom = max((k for k in regions if k in WATCHABLE), key=lambda k: regions[k]["ms"])
+    ctx.watch(dom)
+    ctx.evolve(2, s["dt"], s["beta"])  # capture the graph with the watch events
+    ctx.sync()
 
     # timed region
     if world > 1:
@@ -297,7 +340,7 @@ def measure(args, s, prec, torch, world, local):
     torch.cuda.synchronize()
     launches0 = ctx.launches
     rebuilds0 = ctx.list_rebuilds()
-    step_ms = []
+    step_ms, kern_ms = [], []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             with torch.cuda.stream(stream):
@@ -309,8 +352,10 @@ def measure(args, s, prec, torch, world, local):
                 e1.record(stream)
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
+            kern_ms.append(ctx.watch_ms())
     ctx.sync()
     torch.cuda.synchronize()
+    ctx.watch(None)
     launches = ctx.launches - launches0
     rebuilds = [b - a for a, b in zip(rebuilds0, ctx.list_rebuilds())]
     total_ms = float(sum(step_ms))
@@ -337,31 +382,60 @@ def measure(args, s, prec, torch, world, local):
         e2e_times.append(time.perf_counter() - t0)
     e2e_value = world * nb * nm * len(e2e_times) / sum(e2e_times)
     nbytes = 4 * r_h.nbytes
+    evolved = ctx.download()  # an evolved (non-lattice) state for the parity and error checks
     ctx.close()
     del flush
     return dict(value=value, total_ms=total_ms, step_ms=step_ms, launches=launches, rebuilds=rebuilds,
                 energies=energies, regions=regions, clocks=clk.summary(), e2e_value=e2e_value, e2e_bytes=nbytes,
-                tune=tune, tune_s=t_tune)
+                tune=tune, tune_s=t_tune, dom=dom, kern_ms=kern_ms, evolved=evolved)
 
 
-def force_error(s):
-    """Relative RMS force error (total and low-frequency) and energy error of the
-    mixed path against the FP64 path on the workload's starting snapshot."""
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(b))
+
+
+def force_error(s, r, box, on):
+    """Relative RMS force error (total, low-frequency, worst bead) and energy and
+    virial errors of the mixed path against the FP64 path on positions r."""
     from rpmd_mainz_gb300 import lib
 
     out = []
     for prec in (0, 1):
         set_precision(s, prec)
-        out.append(lib.full_forces(s["r"], s["box"], s["z"]))
+        out.append(lib.full_forces(r, box, s["z"]))
     f64, fmx = out
-
-    def rel(a, b):
-        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
-
-    return {"force_rel_rms": rel(fmx["dvdr"] + fmx["dvdr2"], f64["dvdr"] + f64["dvdr2"]),
-            "lowfreq_force_rel_rms": rel(fmx["dvdr"], f64["dvdr"]),
+    t64, tmx = f64["dvdr"] + f64["dvdr2"], fmx["dvdr"] + fmx["dvdr2"]
+    return {"force_rel_rms": rel(tmx, t64), "lowfreq_force_rel_rms": rel(fmx["dvdr"], f64["dvdr"]),
+            "force_rel_rms_worst_bead": max(rel(tmx[k], t64[k]) for k in range(t64.shape[0])),
             "energy_rel": abs(fmx["v"] - f64["v"]) / abs(f64["v"]),
-            "virial_rel": rel(fmx["vir"], f64["vir"]), "bound": 1e-5}
+            "virial_rel": rel(fmx["vir"], f64["vir"]), "bound": 1e-5, "on": on}
+
+
+def parity_vs_oracle(s, state):
+    """One evolve_pi step of the plain-FP64 device path (the drop-in C ABI) and
+    of the oracle from the same evolved state: relative L2 errors of r, p, dvdr,
+    dvdr2 and of the energies and virial (bound 1e-10)."""
+    from rpmd_mainz_gb300 import lib
+    from tests import oracle_lib as orc
+
+    r, p, f, f2 = state
+    set_precision(s, 0)
+    orc.set_params(s["params"])
+    t0 = time.perf_counter()
+    so = orc.State(r, p, f, f2, s["box"])
+    eo = orc.evolve_pi(so, s["dt"], s["mass"], s["z"], s["beta"], orc.Rng(1))
+    t_orc = time.perf_counter() - t0
+    sd = lib.State(r, p, f, f2, s["box"])
+    ed = lib.evolve_pi(sd, s["dt"], s["mass"], s["z"], s["beta"])
+    errs = {k: rel(getattr(sd, k), getattr(so, k)) for k in ("r", "p", "dvdr", "dvdr2")}
+    for k in ("v", "vew", "vlj", "vint"):
+        errs[k] = abs(ed[k] - eo[k]) / max(abs(eo[k]), 1e-300)
+    errs["vir"] = rel(sd.vir, so.vir)
+    errs["vir_lf"] = rel(sd.vir_lf, so.vir_lf)
+    worst = max(errs.values())
+    return {"max_rel": worst, "bound": 1e-10, "ok": bool(worst <= 1e-10), "errors": errs,
+            "on": "one evolve_pi step from the FP64 arm's final (evolved) state, plain-FP64 drop-in call vs oracle",
+            "oracle_seconds": t_orc}
 
 
 def run_replicas(args, torch):
@@ -669,6 +743,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true", help="skip the plain-FP64 comparison arm")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of tuned ones")
+    ap.add_argument("--no-parity", action="store_true", help="skip the one-step oracle parity check")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -697,12 +772,17 @@ def main():
     prec = 1 if args.precision == "mixed" else 0
     m = measure(args, s, prec, torch, world, local)
     fp64 = None
-    if prec == 1 and not args.no_fp64_arm:
-        f = measure(args, s, 0, torch, world, local)
+    f = None
+    if prec == 0 or not args.no_fp64_arm:
+        f = m if prec == 0 else measure(args, s, 0, torch, world, local)
+    if prec == 1 and f is not None:
         fp64 = {"value": f["value"], "ms_per_step": f["total_ms"] / args.steps, "autotune": f["tune"],
                 "p50_ms": float(np.median(f["step_ms"])), "p99_ms": float(np.percentile(f["step_ms"], 99)),
                 "regions_ms_one_step": {k: v["ms"] for k, v in f["regions"].items()}}
-    err = force_error(s) if prec == 1 else None
+    evolved = (f or m)["evolved"]
+    err = force_error(s, evolved[0], s["box"], "the FP64 arm's final state (evolved from the lattice by the "
+                      "autotune, warm-up, profiled and timed steps)") if prec == 1 else None
+    parity = parity_vs_oracle(s, evolved) if (rank == 0 and not args.no_parity) else None
     regions = m["regions"]
     out = {
         "metric": "bead-molecule-steps/s", "value": m["value"], "unit": "bead-molecule-steps/s", "n_gpus": world,
@@ -710,10 +790,8 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64 mixed" if prec == 1 else "f64",
         "data": "synthetic (CUB lattice, Maxwell-Boltzmann momenta from the reference's ran2 stream)",
-        "config": {"workload": args.workload, "nm": s["nm"], "nb": s["nb"], "mts": s["params"].mts,
-                   "nbdf1": s["params"].nbdf1, "nbdf2": s["params"].nbdf2, "precision": args.precision,
-                   "l2": "256 MiB flush between steps, outside the timed events",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": workload_config(args.workload, s),
+        "precision": args.precision,
         "p50_ms": float(np.median(m["step_ms"])), "p99_ms": float(np.percentile(m["step_ms"], 99)),
         "gpu_launches": int(m["launches"]),
         "list_rebuilds": {"ewald": m["rebuilds"][0], "lj": m["rebuilds"][1], "tem": m["rebuilds"][2],
@@ -731,27 +809,40 @@ def main():
         out["mixed_over_fp64"] = m["value"] / fp64["value"]
     if err is not None:
         out["error_vs_fp64"] = err
+    if parity is not None:
+        out["parity_vs_oracle"] = parity
     if rank == 0:
-        # roofline of the dominant kernel region
-        dom = max((k for k in regions if k in FLOPS_PER_UNIT), key=lambda k: regions[k]["ms"])
+        # roofline of the dominant kernel region (largest in the profiled pass),
+        # its duration from the watch events around its launch in the timed steps
+        dom = m["dom"]
         rr = regions[dom]
-        per_launch_ms = rr["ms"] / rr["launches"]
-        flops_per_launch = FLOPS_PER_UNIT[dom] * rr["units"] / rr["launches"]
-        achieved = flops_per_launch / (per_launch_ms * 1e-3) / 1e12
-        if prec == 0:
-            peak = fp64_peak_tflops(torch)
-            out["roofline"] = {"bound": "fp64", "kernel_region": dom, "achieved": achieved, "peak": peak,
-                               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom, "fp64"),
-                               "peak_source": "measured in this run: cuBLAS DGEMM 8192^3 (FP64 rate; "
-                                              "MEASURED_PEAKS.json holds only HBM and BF16)",
-                               "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": rr["units"] / rr["launches"]}
+        kern_ms = float(np.mean(m["kern_ms"]))
+        pname = "mixed" if prec == 1 else "fp64"
+        common = {"kernel_region": dom, "kernel_ms_per_launch": kern_ms,
+                  "kernel_ms_source": "CUDA events around the kernel's launch on its own stream, recorded inside "
+                                      "each timed (graph-replayed) step; mean over the timed steps",
+                  "traffic": read_profile_traffic(dom, pname)}
+        if dom in BYTES_PER_BEAD_MOLECULE:
+            peak, src = measured_hbm_peak()
+            nbytes = BYTES_PER_BEAD_MOLECULE[dom] * s["nm"] * s["nb"]
+            achieved = nbytes / (kern_ms * 1e-3) / 1e9
+            out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                               "frac": achieved / peak, "peak_source": src, "bytes_per_launch": nbytes,
+                               "bytes_per_unit": BYTES_PER_BEAD_MOLECULE[dom], "unit_of_work": "bead-molecule",
+                               **common}
         else:
-            peak = fp32_peak_tflops(torch)
-            out["roofline"] = {"bound": "fp32", "kernel_region": dom, "achieved": achieved, "peak": peak,
-                               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": read_profile_traffic(dom, "mixed"),
-                               "peak_source": "measured in this run: cuBLAS SGEMM 8192^3 without TF32 (FP32 "
-                                              "CUDA-core rate; MEASURED_PEAKS.json holds only HBM and BF16)",
-                               "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": rr["units"] / rr["launches"]}
+            units = rr["units"] / rr["launches"]
+            achieved = FLOPS_PER_UNIT[dom] * units / (kern_ms * 1e-3) / 1e12
+            if prec == 0:
+                peak = fp64_peak_tflops(torch)
+                src = "measured in this run: cuBLAS DGEMM 8192^3 (FP64 rate; MEASURED_PEAKS.json holds only HBM and BF16)"
+            else:
+                peak = fp32_peak_tflops(torch)
+                src = ("measured in this run: cuBLAS SGEMM 8192^3 without TF32 (FP32 CUDA-core rate; "
+                       "MEASURED_PEAKS.json holds only HBM and BF16)")
+            out["roofline"] = {"bound": "fp64" if prec == 0 else "fp32", "achieved": achieved, "peak": peak,
+                               "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": src,
+                               "flops_per_unit": FLOPS_PER_UNIT[dom], "units_per_launch": units, **common}
         out["clocks"] = m["clocks"]
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(s)

@@ -130,6 +130,13 @@ int gbrpmd_init(const gb_params *params);
 /* Reads back the stored hidden inputs. */
 int gbrpmd_get_params(gb_params *params);
 
+/* Layout of gb_params as this library was compiled (no counterpart in the
+   reference): returns sizeof(gb_params) and writes the byte offset of each
+   field, in declaration order (oo_eps .. baro, 32 fields), into offsets[0 ..
+   min(nfield, 32) - 1], so that a binding (the Fortran bind(c) type, a ctypes
+   mirror) can check its own record against it. */
+int gbrpmd_params_layout(int64_t *offsets, int nfield);
+
 /* Message of the last failing call (static storage, never NULL). */
 const char *gbrpmd_last_error(void);
 
@@ -145,19 +152,27 @@ int gbrpmd_finalize(void);
 int gbrpmd_forces(double *r, double *v, double *dvdr, const int *nb, const int *na,
                   const double *boxlxyz, const double *z, double *virial, const int *iopt);
 
-/* No counterpart in the reference.  Same results as gbrpmd_forces with
+/* No counterpart in the reference.  The FP64 results of gbrpmd_forces with
    iopt = 2 (Ewald energy, gradient and virial of nb configurations, host
-   arrays in and out), for callers that cannot let the library allocate device
-   memory: hosts running under a device-memory budget owned by another
-   framework's pool, or code that must not trigger cudaMalloc / cudaFree (and
-   their implicit synchronisation) while its own streams are busy.  All device
-   work uses one 16 MiB array that the library reserves at load time on every
-   GPU that loads it (held until exit); nothing is allocated per call.  Its
-   device address is looked up on the first call made on each device, so make
-   that first call before any stream capture.  Calls share the array: each call
-   clears what must start at zero, and calls that overlap on the GPU race.
-   Limits: na*nb <= 8192 sites, nb <= 64, at most 2048 k vectors and 192
-   pair partners per site (GB_E_NOMEM / GB_E_LIST beyond them). */
+   arrays in and out; always FP64, whatever gb_params.precision says), for
+   callers that cannot let the library allocate device memory: hosts running
+   under a device-memory budget owned by another framework's pool, or code
+   that must not trigger cudaMalloc / cudaFree (and their implicit
+   synchronisation) while its own streams are busy.  All device work uses one
+   16 MiB array that the library reserves at load time on every GPU that loads
+   it (held until exit); nothing is allocated per call.  Its device address is
+   looked up on the first call made on each device, so make that first call
+   before any stream capture.  The work runs on the calling thread's per-thread
+   default stream (cudaStreamPerThread).  Calls share the array and the host-side
+   k tables, and the array keeps the last call's contents: each call clears
+   what must start at zero, and because calls in flight at the same time would
+   race on both, a process-wide lock serialises them (a call returns after its
+   device work is done).  Limits: na*nb <= 8192 sites, nb <= 64, at most 2048 k
+   vectors, and a working set within 16 MiB, mostly the pair list (4 bytes per
+   site and slot, slots for 1.1 times a uniform liquid's partners within the
+   real-space cut-off plus 48): 216 water molecules at nb = 8 take about 9 MiB
+   (GB_E_NOMEM beyond the limits; GB_E_LIST when a site has more partners than
+   its slots). */
 int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, const int *nb, const int *na,
                                const double *boxlxyz, const double *z, double *virial);
 
@@ -194,6 +209,14 @@ int gbrpmd_rattle_s1(double *r, const double *rold, double *p, const int *nm,
    (md_rattle.f90:164-271) for one bead. */
 int gbrpmd_rattle_s2(double *r, double *p, const int *nm, const double *mass,
                      const double *dt, double *dvdr, double *vir, const int *na);
+
+/* Sweep limit of both RATTLE stages (no counterpart in the reference, whose
+   md_rattle.f90 fixes it at 1000, the default here): rattle_s1 / rattle_s2 and
+   evolve_rig_pi report GB_E_RATTLE1 / GB_E_RATTLE2 when the last molecule
+   needed that many sweeps, as the reference stops.  Process-wide; steps
+   already captured in a CUDA graph keep the limit they were captured with.
+   Meant for tests of the error path (itmax >= 1). */
+int gbrpmd_rattle_set_itmax(const int *itmax);
 
 /* replaces subroutine evolve_rig_pi(p,r,v,v_lf,v_hf,dvdr,dvdr2,dt,mass,na,nb,
    boxlxyz,z,beta,vir,vir_lf,irun,nbaro)  (evolve_rigid.f90:100-224): rigid
@@ -326,6 +349,16 @@ int gbrpmd_ctx_set_profiling(gb_context *ctx, int on);
    3 structure factors, 4 k-space weights, 5 k-space forces, 6 Lennard-Jones,
    7 TEM correction, 8 contraction and kicks, 9 M-site, 10 RATTLE */
 int gbrpmd_ctx_region_times(gb_context *ctx, double *ms, double *units, int *counts, int nregion);
+/* Watched kernel (no counterpart in the reference): a pair of timing events
+   around the launch of one region's kernel (0 multiple-time-step block,
+   2 real-space Ewald, 5 k-space forces, 6 Lennard-Jones; -1 stops watching),
+   recorded on the stream the kernel is launched on and captured into the step
+   graph with it, so that ordinary (graph-replayed, forked) steps report that
+   kernel's own duration.  Setting it drops the step graph. */
+int gbrpmd_ctx_watch_region(gb_context *ctx, int region);
+/* milliseconds between the watch events of the last step that recorded them
+   (synchronises); GB_E_ARG when none was recorded */
+int gbrpmd_ctx_watch_ms(gb_context *ctx, float *ms);
 /* Pair-list skin (no counterpart in the reference, which rebuilds its cell
    lists at every call): each list of the context (real-space Ewald, LJ, TEM)
    keeps a superset at cut-off * (1 + fraction), rebuilt on the device only

@@ -1,5 +1,6 @@
 // api.cpp -- C ABI of the library (include/gbrpmd.h): parameter store,
 // device contexts, drop-in entry points and the serial random stream.
+#include <cstddef>
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -143,6 +144,16 @@ void prof_end(gb_context *c, int region, double units) {
   c->ev_next += 2;
 }
 
+int watch_mark(gb_context *c, int region, cudaStream_t s, int which) {
+  if (c->watch != region || !c->watch_ev[which]) return GB_OK;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(s, &cap));
+  if (cap == cudaStreamCaptureStatusActive) CK(cudaEventRecordWithFlags(c->watch_ev[which], s, cudaEventRecordExternal));
+  else CK(cudaEventRecord(c->watch_ev[which], s));
+  if (which == 1) c->watch_seen = true;
+  return GB_OK;
+}
+
 int ctx_alloc(gb_context *c, int na, int nb) {
   int st = check_sizes(na, nb);
   if (st) return st;
@@ -220,6 +231,8 @@ void ctx_free(gb_context *c) {
   if (c->d_rngctr) cudaFree(c->d_rngctr);
   if (c->gauss_ev) cudaEventDestroy(c->gauss_ev);
   if (c->mid_ev) cudaEventDestroy(c->mid_ev);
+  for (cudaEvent_t e : c->watch_ev)
+    if (e) cudaEventDestroy(e);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   if (c->join_ev) cudaEventDestroy(c->join_ev);
@@ -247,6 +260,23 @@ int gbrpmd_get_params(gb_params *params) {
   if (!g_init) return ctx_set_error(GB_E_NOINIT, "gbrpmd_init has not been called");
   *params = g_params;
   return GB_OK;
+}
+
+int gbrpmd_params_layout(int64_t *offsets, int nfield) {
+  static const int64_t off[] = {
+      offsetof(gb_params, oo_eps), offsetof(gb_params, oo_sig), offsetof(gb_params, oo_gam),
+      offsetof(gb_params, rcut), offsetof(gb_params, alpha), offsetof(gb_params, ecut), offsetof(gb_params, wm),
+      offsetof(gb_params, wh), offsetof(gb_params, wrcut), offsetof(gb_params, walpha), offsetof(gb_params, rkmax),
+      offsetof(gb_params, kmax), offsetof(gb_params, nbdf1), offsetof(gb_params, nbdf2), offsetof(gb_params, apot),
+      offsetof(gb_params, bpot), offsetof(gb_params, alp), offsetof(gb_params, alpb), offsetof(gb_params, theta),
+      offsetof(gb_params, reoh), offsetof(gb_params, sig), offsetof(gb_params, mts), offsetof(gb_params, iamcub),
+      offsetof(gb_params, nctot), offsetof(gb_params, nbond), offsetof(gb_params, therm), offsetof(gb_params, ttau),
+      offsetof(gb_params, taub), offsetof(gb_params, patm), offsetof(gb_params, intra_model),
+      offsetof(gb_params, precision), offsetof(gb_params, baro)};
+  constexpr int n = (int)(sizeof(off) / sizeof(off[0]));
+  static_assert(n == 32, "gb_params has 32 fields");
+  for (int i = 0; offsets && i < nfield && i < n; ++i) offsets[i] = off[i];
+  return (int)sizeof(gb_params);
 }
 
 const char *gbrpmd_last_error(void) { return g_err.c_str(); }
@@ -552,6 +582,27 @@ int gbrpmd_ctx_set_profiling(gb_context *c, int on) {
   return GB_OK;
 }
 
+int gbrpmd_ctx_watch_region(gb_context *c, int region) {
+  if (!c) return ctx_set_error(GB_E_ARG, "null context");
+  if (region != -1 && region != PR_MTS && region != PR_EW_REAL && region != PR_RECIP_F && region != PR_LJ)
+    return ctx_set_error(GB_E_ARG, "watched region must be -1, 0, 2, 5 or 6");
+  CK(cudaStreamSynchronize(c->stream));
+  for (cudaEvent_t &e : c->watch_ev)
+    if (!e) CK(cudaEventCreate(&e));
+  dev_graph_reset(c);
+  c->watch = region;
+  c->watch_seen = false;
+  return GB_OK;
+}
+
+int gbrpmd_ctx_watch_ms(gb_context *c, float *ms) {
+  if (!c || !ms) return ctx_set_error(GB_E_ARG, "null argument");
+  if (c->watch < 0 || !c->watch_seen) return ctx_set_error(GB_E_ARG, "no watched launch recorded");
+  CK(cudaEventSynchronize(c->watch_ev[1]));
+  CK(cudaEventElapsedTime(ms, c->watch_ev[0], c->watch_ev[1]));
+  return GB_OK;
+}
+
 int gbrpmd_ctx_set_list_skin(gb_context *c, double fraction) {
   if (!c) return ctx_set_error(GB_E_ARG, "null context");
   if (!(fraction >= 0.0) || fraction > 1.0) return ctx_set_error(GB_E_ARG, "list skin fraction must be in [0, 1]");
@@ -643,6 +694,7 @@ double gbrpmd_gaussian(int *idum, const double *sigma) { return rng_gaussian(g_r
 
 // ---- rigid path entry points (device implementation in rattle.cpp) ----
 int dev_rattle_setup(int nm, const gb_params &P);
+int dev_rattle_set_itmax(int itmax);
 int dev_rattle_s1(double *r, const double *rold, double *p, int nm, const double *mass, double dt,
                   double *dvdr, double *vir, int na);
 int dev_rattle_s2(double *r, double *p, int nm, const double *mass, double dt, double *dvdr,
@@ -656,6 +708,11 @@ int gbrpmd_rattle_setup(const int *nm) {
   g_params.nctot = 3 * (*nm);
   g_params.nbond = 3;
   return dev_rattle_setup(*nm, g_params);
+}
+
+int gbrpmd_rattle_set_itmax(const int *itmax) {
+  if (!itmax) return ctx_set_error(GB_E_ARG, "null argument");
+  return dev_rattle_set_itmax(*itmax);
 }
 
 int gbrpmd_rattle_s1(double *r, const double *rold, double *p, const int *nm, const double *mass,

@@ -19,6 +19,15 @@ GB_D double dsq3(double dx, double dy, double dz) {
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
+// non-finite test on the exponent bits (integer instructions: no FP64
+// comparison, which runs on the slow FP64 pipe)
+GB_D bool gb_nonfinite(double v) { return (__double2hiint(v) & 0x7ff00000) == 0x7ff00000; }
+GB_D bool gb_nonfinite(float v) { return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u; }
+// sets ST_NONFINITE in the status word when `bad` (status may be null)
+GB_D void gb_flag_nonfinite(unsigned *status, bool bad) {
+  if (bad && status) atomicOr(status, ST_NONFINITE);
+}
+
 GB_D double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -211,6 +211,10 @@ struct gb_context {
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_next = 0;
   int *d_count = nullptr;  // device scratch for pair counts (profiling only)
+  // watched kernel (gbrpmd_ctx_watch_region): events around one region's launch
+  int watch = -1;
+  cudaEvent_t watch_ev[2] = {nullptr, nullptr};
+  bool watch_seen = false;
 };
 
 // profiled regions
@@ -230,6 +234,9 @@ enum ProfRegion : int {
 };
 void prof_begin(gb_context *c, int region);
 void prof_end(gb_context *c, int region, double units);
+// records the watch event (0 before, 1 after) when `region` is watched, on the
+// stream its kernel runs on (an event node inside a capture)
+int watch_mark(gb_context *c, int region, cudaStream_t s, int which);
 
 // ---- context lifetime and helpers (api.cpp) ----
 int ctx_alloc(gb_context *c, int na, int nb);

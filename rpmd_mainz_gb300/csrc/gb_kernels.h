@@ -91,7 +91,8 @@ void recip_set_attributes_mx();
 // out[b] = sign * chain_rule(scale * g[b]) (+= when accumulate); with g2,
 // of scale * (g[b] + g2[b])
 void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, int B, double alpha,
-                        double scale, double sign, int accumulate, const double *g2 = nullptr);
+                        double scale, double sign, int accumulate, const double *g2 = nullptr,
+                        unsigned *status = nullptr);
 
 // ---- Lennard-Jones O-O (k_pairs.cu) ----
 // r: [B][na][3] box units; list over oxygen points (shared if pl.nconf == 1)
@@ -108,7 +109,7 @@ void launch_centroid(cudaStream_t s, const double *r, double *rc, int na, int B)
 // ---- per-molecule terms (k_modes.cu) ----
 // model: 0 intra_harmonic, 1 intra_spcfw, 2 intra_morse_harm
 void launch_intra(cudaStream_t s, const double *r, double *out, int na, int B, int model,
-                  const gb_params &P, double *acc, int accumulate);
+                  const gb_params &P, double *acc, int accumulate, unsigned *status);
 void launch_virial_ke(cudaStream_t s, const double *r, const double *dvdr, const double *dvdr2,
                       int na, int nb, double *acc);
 // thermostat kicks and Berendsen shift inside evolve_pi (k_therm.cu)
@@ -142,5 +143,5 @@ void launch_ring_contract(cudaStream_t s, const double *rnm, double *rb, int na,
 void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int nbc1,
                           const double *tw_c1, const double *fb2, int nbc2, const double *tw_c2,
                           const double *e1, const double *e2, const double *e3, double *p,
-                          double halfdt, int na, int nb, const double *tw_nb, bool mixed);
+                          double halfdt, int na, int nb, const double *tw_nb, bool mixed, unsigned *status);
 void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used);

@@ -91,7 +91,7 @@ __global__ void k_ring_contract(const double *rnm, double *rb, int na, int nb, i
 __global__ void k_expand_forces(double *dvdr, const double *fb1, int nbc1, const double *tw_c1,
                                 const double *fb2, int nbc2, const double *tw_c2, const double *e1,
                                 const double *e2, const double *e3, double *p, double halfdt,
-                                int na, int nb, const double *tw_nb) {
+                                int na, int nb, const double *tw_nb, unsigned *status) {
   const long long S = 3LL * na;
   const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= S) return;
@@ -116,6 +116,7 @@ __global__ void k_expand_forces(double *dvdr, const double *fb1, int nbc1, const
     hmax = max(hmax, h);
   }
   const double sc = sqrt(1.0 / (double)nb);
+  bool bad = false;
   for (int j = 0; j < nb; ++j) {
     double s = xr[0];
     int m = 0;
@@ -130,8 +131,10 @@ __global__ void k_expand_forces(double *dvdr, const double *fb1, int nbc1, const
     if (e2) v += e2[o];
     if (e3) v += e3[o];
     dvdr[o] = v;
+    bad |= gb_nonfinite(v);
     if (p) p[o] = p[o] - halfdt * v;
   }
+  gb_flag_nonfinite(status, bad);
 }
 
 // The same expansion for contracted rings of at most 2*HM+1 beads: the
@@ -155,7 +158,7 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
                                                      const double *fb2, int nbc2, const double *tw_c2,
                                                      const double *e1, const double *e2, const double *e3, double *p,
                                                      double halfdt, int na, int nb, const double *tw_nb,
-                                                     double2 sc1, double2 sc2, double sc) {
+                                                     double2 sc1, double2 sc2, double sc, unsigned *status) {
   constexpr int NQ = 2 * HM + 1;
   constexpr bool F32 = std::is_same<R, float>::value;
   extern __shared__ double smx[];
@@ -230,6 +233,7 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
   for (int q = 0; q < NQ; ++q) cr[q] = CF[lr * NQ + q];
   const int j0 = grp * nb / 4, j1 = (grp + 1) * nb / 4;
   const bool extras = e1 || e2 || e3;
+  bool bad = false;
   for (int j = j0; j < j1; ++j) {
     R s = (R)0;
 #pragma unroll
@@ -244,13 +248,15 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
       if (e3) v += e3[o];
     }
     dvdr[o] = v;
+    bad |= gb_nonfinite(v);
     if (p) p[o] = p[o] - halfdt * v;
   }
+  gb_flag_nonfinite(status, bad);
 }
 
 // intramolecular forces on B configurations (potenl_opt iopt = 4 path)
 __global__ void __launch_bounds__(128) k_intra(const double *r, double *out, int nm, int B, int model,
-                                               IntraPar ip, double *acc, int accumulate) {
+                                               IntraPar ip, double *acc, int accumulate, unsigned *status) {
   __shared__ double sh[32 * 10];
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double vals[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -260,8 +266,13 @@ __global__ void __launch_bounds__(128) k_intra(const double *r, double *out, int
 #pragma unroll
     for (int d = 0; d < 9; ++d) xl[d] = x[d];
     vals[0] = intra_molecule(model, xl, f, vir, ip);
+    bool bad = gb_nonfinite(vals[0]);
 #pragma unroll
-    for (int d = 0; d < 9; ++d) vals[1 + d] = vir[d];
+    for (int d = 0; d < 9; ++d) {
+      vals[1 + d] = vir[d];
+      bad |= gb_nonfinite(f[d]);
+    }
+    gb_flag_nonfinite(status, bad);
     double *o = out + t * 9;
     if (accumulate) {
 #pragma unroll
@@ -343,7 +354,8 @@ void launch_ring_contract(cudaStream_t s, const double *rnm, double *rb, int na,
 template <int HM>
 void launch_expand_hm(cudaStream_t s, bool mixed, double *dvdr, const double *fb1, int nbc1, const double *tw_c1,
                       const double *fb2, int nbc2, const double *tw_c2, const double *e1, const double *e2,
-                      const double *e3, double *p, double halfdt, int na, int nb, const double *tw_nb) {
+                      const double *e3, double *p, double halfdt, int na, int nb, const double *tw_nb,
+                      unsigned *status) {
   const long long n = 3LL * na;
   const size_t smem = sizeof(double) * (nb + XR) * (2 * HM + 1);
   auto scale = [&](int nbc) {  // sqrt(1/nbc), sqrt(nb/nbc) of a contraction (force_contract)
@@ -353,16 +365,16 @@ void launch_expand_hm(cudaStream_t s, bool mixed, double *dvdr, const double *fb
   const double sc = sqrt(1.0 / (double)nb);
   if (mixed)
     k_expand_table<HM, float><<<nblk(n, XR), XT, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p,
-                                                            halfdt, na, nb, tw_nb, sc1, sc2, sc);
+                                                            halfdt, na, nb, tw_nb, sc1, sc2, sc, status);
   else
     k_expand_table<HM, double><<<nblk(n, XR), XT, smem, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3,
-                                                             p, halfdt, na, nb, tw_nb, sc1, sc2, sc);
+                                                             p, halfdt, na, nb, tw_nb, sc1, sc2, sc, status);
 }
 
 void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int nbc1,
                           const double *tw_c1, const double *fb2, int nbc2, const double *tw_c2,
                           const double *e1, const double *e2, const double *e3, double *p,
-                          double halfdt, int na, int nb, const double *tw_nb, bool mixed) {
+                          double halfdt, int na, int nb, const double *tw_nb, bool mixed, unsigned *status) {
   int nbc = 1;
   if (fb1) nbc = max(nbc, nbc1);
   if (fb2) nbc = max(nbc, nbc2);
@@ -370,20 +382,20 @@ void launch_expand_forces(cudaStream_t s, double *dvdr, const double *fb1, int n
   // modes beyond nb/2 do not exist; the table form needs HM <= nb/2 and 2HM+1 <= nb
   if (2 * h + 1 <= nb && h <= 4) {
     switch (h) {
-      case 0: launch_expand_hm<0>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
-      case 1: launch_expand_hm<1>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
-      case 2: launch_expand_hm<2>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
-      case 3: launch_expand_hm<3>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
-      case 4: launch_expand_hm<4>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb); return;
+      case 0: launch_expand_hm<0>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb, status); return;
+      case 1: launch_expand_hm<1>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb, status); return;
+      case 2: launch_expand_hm<2>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb, status); return;
+      case 3: launch_expand_hm<3>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb, status); return;
+      case 4: launch_expand_hm<4>(s, mixed, dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p, halfdt, na, nb, tw_nb, status); return;
     }
   }
   long long n = 3LL * na;
   k_expand_forces<<<nblk(n, 64), 64, 0, s>>>(dvdr, fb1, nbc1, tw_c1, fb2, nbc2, tw_c2, e1, e2, e3, p,
-                                             halfdt, na, nb, tw_nb);
+                                             halfdt, na, nb, tw_nb, status);
 }
 
 void launch_intra(cudaStream_t s, const double *r, double *out, int na, int B, int model,
-                  const gb_params &P, double *acc, int accumulate) {
+                  const gb_params &P, double *acc, int accumulate, unsigned *status) {
   IntraPar ip;
   ip.reoh = P.reoh;
   ip.theta = P.theta;
@@ -393,7 +405,7 @@ void launch_intra(cudaStream_t s, const double *r, double *out, int na, int B, i
   ip.alp = P.alp;
   const int nm = na / 3;
   long long n = (long long)nm * B;
-  k_intra<<<nblk(n, 128), 128, 0, s>>>(r, out, nm, B, model, ip, acc, accumulate);
+  k_intra<<<nblk(n, 128), 128, 0, s>>>(r, out, nm, B, model, ip, acc, accumulate, status);
 }
 
 void launch_virial_ke(cudaStream_t s, const double *r, const double *dvdr, const double *dvdr2,

@@ -42,6 +42,7 @@ struct MtsArgs {
   const double *monod;  // monod(ic, c, k) at ic + 3*(c + 4*k)
   const double *tw;     // twiddles of length nb
   double *acc_int, *acc_ke;
+  unsigned *status;  // ST_NONFINITE when a force or momentum written is not finite
   int na, nm, mts, model, mpb;
   double halfdt, dtsmall, halfdtsmall;
   float hdt_h, hdt_l, hds_h, hds_l;  // halfdt and halfdtsmall as FP32 pairs (mixed kernel)
@@ -170,9 +171,12 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_fused(MtsArgs a) {
     const double *f2_row = s_f2 + (ml * 9 + lr) * C::LD;
     const double hds = a.halfdtsmall;
     double *gp = a.p + row;
+    bool bad = false;
     gb_hc2r_s<NB>([&](int j) { return p[j]; },
                   [&](int k, double v) {
-                    if (valid) gp[S * k] = v - hds * f2_row[k];
+                    const double pk = v - hds * f2_row[k];
+                    bad |= gb_nonfinite(pk);
+                    if (valid) gp[S * k] = pk;
                   }, s_tw, s_twi);
     if (valid) {
 #pragma unroll
@@ -180,8 +184,10 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 1) k_mts_fused(MtsArgs a) {
         a.r[row + S * j] = rs_row[j];
         a.rnm[row + S * j] = x[j];
         a.dvdr2[row + S * j] = f2_row[j];
+        bad |= gb_nonfinite(f2_row[j]);
       }
     }
+    gb_flag_nonfinite(a.status, bad && valid);
   }
   // block sums: [0] last-substep intra energy, [1..9] intra virial summed over
   // substeps, [10] tq1, [11] tq2, [12..14] tq1 per xyz, [15..17] tq2 per xyz
@@ -412,9 +418,12 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
     const float hds = (float)a.halfdtsmall;
     const double pc = sc * p0;
     double *gp = a.p + row;
+    bool bad = gb_nonfinite(pc);
     gb_hc2r_s<NB, float, true>([&](int j) { return j ? pf[j] : 0.f; },
                                [&](int k, float v) {
-                                 if (valid) gp[S * k] = pc + f2d(fmaf(-hds, f2_row[k], v));
+                                 const float dp = fmaf(-hds, f2_row[k], v);
+                                 bad |= gb_nonfinite(dp);
+                                 if (valid) gp[S * k] = pc + f2d(dp);
                                },
                                s_tw, s_twi, s_tw_l, s_twi_l);
     if (valid) {
@@ -422,7 +431,9 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
       for (int j = 0; j < NB; ++j) {
         a.rnm[row + S * j] = j ? f2d(xf[j]) : x0;
         a.dvdr2[row + S * j] = f2d(f2_row[j]);
+        bad |= gb_nonfinite(f2_row[j]);
       }
+      gb_flag_nonfinite(a.status, bad);
       // contracted rings of the new positions (gb_hc2r_direct over modes 0..h,
       // the FP32 modes summed in FP32): rb_j = s12 x0 + s12 y_j
       auto contract = [&](double *rb, int nbc, const float *ct, double s12) {
@@ -553,6 +564,7 @@ void launch_fused_mts(cudaStream_t s, gb_context *c, double dt, int *used) {
   a.tw = c->tw_nb;
   a.acc_int = c->acc + (size_t)ACC_INT * ACC_STRIDE;
   a.acc_ke = c->acc + (size_t)ACC_KE * ACC_STRIDE;
+  a.status = c->status;
   a.na = c->na;
   a.nm = c->nm;
   a.mts = c->P.mts;

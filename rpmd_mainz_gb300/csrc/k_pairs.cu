@@ -185,7 +185,9 @@ struct CellSortDev {
   unsigned *ticket;  // [0] blocks done in the count kernel, [1] a point moved
 };
 
-GB_D int cell_of(float u, int n) { return min((int)(u * (float)n), n - 1); }
+// (clamped both ways: a wrapped coordinate is in [0, 1], and a non-finite one
+// converts to 0, so no input can index outside the grid)
+GB_D int cell_of(float u, int n) { return max(min((int)(u * (float)n), n - 1), 0); }
 
 // (also writes the points' fractional coordinates, as k_frac32)
 __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q,
@@ -482,7 +484,7 @@ __global__ void k_msite(const double *r, double *rs, int nm, int B, double alpha
 
 // out = sign * chain_rule(scale * g)  (md_forces.f90:206-215)
 __global__ void k_msite_chain(const double *g, const double *g2, double *out, int nm, int B, double alpha,
-                              double alpha2, double scale, double sign, int accumulate) {
+                              double alpha2, double scale, double sign, int accumulate, unsigned *status) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nm * B * 3) return;
   const int d = (int)(t % 3);
@@ -500,6 +502,7 @@ __global__ void k_msite_chain(const double *g, const double *g2, double *out, in
   const double h1 = scale * m1 + alpha2 * go;
   const double h2 = scale * m2 + alpha2 * go;
   const double oo = alpha * go;
+  gb_flag_nonfinite(status, gb_nonfinite(oo) || gb_nonfinite(h1) || gb_nonfinite(h2));
   if (accumulate) {
     o[d] += sign * oo;
     o[3 + d] += sign * h1;
@@ -991,11 +994,11 @@ void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, do
 }
 
 void launch_msite_chain(cudaStream_t s, const double *g, double *out, int na, int B, double alpha,
-                        double scale, double sign, int accumulate, const double *g2) {
+                        double scale, double sign, int accumulate, const double *g2, unsigned *status) {
   int nm = na / 3;
   long long n = (long long)nm * B * 3;
   k_msite_chain<<<nblk(n, 256), 256, 0, s>>>(g, g2, out, nm, B, alpha, 0.5 * (1.0 - alpha), scale, sign,
-                                             accumulate);
+                                             accumulate, status);
 }
 
 void launch_ewald_real(cudaStream_t s, const double *rs, const double *q, int na, int B,

@@ -27,13 +27,16 @@
 
 namespace {
 
-constexpr int ITMAX = 1000;
 constexpr double RTOL = 1e-6;
+// sweep limit of both stages (md_rattle.f90 fixes maxit = 1000); lowered only
+// through gbrpmd_rattle_set_itmax, which tests use to reach the error path
+int g_rattle_itmax = 1000;
 
 struct RatPar {
   double rcb[3];  // squared constrained lengths: reoh^2, reoh^2, rehh^2
   double rm[3];   // 1/mass of O, H1, H2
   double g2[3];   // 1 / ((rm1 + rm2) rcb) per bond (stage-2 multiplier)
+  int itmax;      // sweep limit
 };
 
 // bond b of a molecule: atoms (ii, jj)
@@ -65,7 +68,7 @@ GB_D int rattle1_mol(double *r, const double *rold, double *p, double *f, double
   }
   bool done = false;
   int it = 0;
-  while (!done && it < ITMAX) {
+  while (!done && it < rp.itmax) {
     done = true;
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
@@ -136,7 +139,7 @@ GB_D int rattle2_mol(const double *r, double *p, double *f, double dt, const Rat
   }
   bool done = false;
   int it = 0;
-  while (!done && it <= ITMAX) {
+  while (!done && it <= rp.itmax) {
     done = true;
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
@@ -206,10 +209,10 @@ __global__ void k_rattle(int stage, double *r, const double *rold, double *p, do
 #pragma unroll
     for (int d = 0; d < 9; ++d) ro[d] = rold[t * 9 + d];
     it = rattle1_mol(rl, ro, pl, fl, dt, rp, rec);
-    if (m == nm - 1 && it >= ITMAX) atomicOr(status, ST_RATTLE1);
+    if (m == nm - 1 && it >= rp.itmax) atomicOr(status, ST_RATTLE1);
   } else {
     it = rattle2_mol(rl, pl, fl, dt, rp, rec);
-    if (m == nm - 1 && it >= ITMAX) atomicOr(status, ST_RATTLE2);
+    if (m == nm - 1 && it >= rp.itmax) atomicOr(status, ST_RATTLE2);
   }
 #pragma unroll
   for (int d = 0; d < 9; ++d) {
@@ -316,7 +319,7 @@ __global__ void k_rig_substeps(double *r, double *p, double *f2, int nm, int nb,
 #pragma unroll
       for (int d = 0; d < 8; ++d) rec[d] = 0.0;
       const int it = rattle1_mol(rl, ro, pl, fl, smalldt, rp, rec);
-      if (m == nm - 1 && it >= ITMAX) atomicOr(status, ST_RATTLE1);
+      if (m == nm - 1 && it >= rp.itmax) atomicOr(status, ST_RATTLE1);
     }
     springs();
     if (valid) {
@@ -325,7 +328,7 @@ __global__ void k_rig_substeps(double *r, double *p, double *f2, int nm, int nb,
 #pragma unroll
       for (int d = 0; d < 8; ++d) rec[d] = 0.0;
       const int it = rattle2_mol(rl, pl, fl, smalldt, rp, rec);
-      if (m == nm - 1 && it >= ITMAX) atomicOr(status, ST_RATTLE2);
+      if (m == nm - 1 && it >= rp.itmax) atomicOr(status, ST_RATTLE2);
     }
   }
   if (valid) {
@@ -357,6 +360,7 @@ struct RattleWs {
 
 RatPar make_rp(const gb_params &P, const double *mass3) {
   RatPar rp;
+  rp.itmax = g_rattle_itmax;
   const double rehh = 2.0 * std::sin(0.5 * P.theta) * P.reoh;
   rp.rcb[0] = P.reoh * P.reoh;
   rp.rcb[1] = P.reoh * P.reoh;
@@ -428,6 +432,12 @@ int rattle_dropin(int stage, double *r, const double *rold, double *p, int nm, c
 }
 
 }  // namespace
+
+int dev_rattle_set_itmax(int itmax) {
+  if (itmax < 1) return ctx_set_error(GB_E_ARG, "rattle sweep limit must be >= 1");
+  g_rattle_itmax = itmax;
+  return GB_OK;
+}
 
 int dev_rattle_setup(int nm, const gb_params &P) {
   (void)P;

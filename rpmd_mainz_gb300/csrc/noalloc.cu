@@ -1,31 +1,39 @@
 // noalloc.cu -- the Ewald force entry point that allocates no device memory.
 //
 // gbrpmd_forces_ewald_static computes what gbrpmd_forces computes for
-// iopt = 2 (M-site substitution, real-space and reciprocal Ewald sums, chain
-// rule; bead-averaged energy and virial), but every device buffer it needs --
-// positions, pair lists, structure factors, accumulators -- lives in one
-// file-scope __device__ array of STATIC_SCRATCH_BYTES (16 MiB).  It is meant for
-// callers that may not call cudaMalloc themselves or through us: hosts that run
-// under a fixed device-memory budget handed out by another framework's pool, or
-// codes that must not trigger allocation (and the implicit synchronisation a
-// cudaFree brings) in the middle of their own stream work.
+// iopt = 2 in FP64 (M-site substitution, real-space and reciprocal Ewald sums,
+// chain rule; bead-averaged energy and virial), whatever gb_params.precision
+// says, but every device buffer it needs -- positions, pair lists, structure
+// factors, accumulators -- lives in one file-scope __device__ array of
+// STATIC_SCRATCH_BYTES (16 MiB).  It is meant for callers that may not call
+// cudaMalloc themselves or through us: hosts that run under a fixed
+// device-memory budget handed out by another framework's pool, or codes that
+// must not trigger allocation (and the implicit synchronisation a cudaFree
+// brings) in the middle of their own stream work.
 //
 // The array is part of the module image: every GPU that loads the library
 // reserves the 16 MiB until the process exits.  Host code only knows a
 // host-side stand-in for the array's name, so the device address is fetched
 // once per device with cudaGetSymbolAddress, with that device current, on the
 // first call made on that device; make that first call before any stream
-// capture.  The buffer is shared by all calls: each call clears the parts that
-// must start at zero, and calls that overlap on the GPU (from several host
-// threads) race on it.
+// capture.  The work runs on the calling thread's per-thread default stream
+// (cudaStreamPerThread), which creates nothing and does not synchronise with
+// the caller's other streams.  The array keeps the last call's contents and is
+// shared by all calls, as are the host-side k tables below: each call clears
+// what must start at zero, and since two calls in flight at once would race on
+// both, a process-wide lock serialises the calls from the start of a call until
+// its device work has finished.
 //
 // Limits (rejected with GB_E_NOMEM and a message): na * nb <= 8192 sites,
 // nb <= 64, at most 2048 k vectors in 512 (kx, ky) columns, and every buffer
-// together within 16 MiB; pair lists hold at most 192 partners per site
-// (overflow is reported as GB_E_LIST).
+// together within 16 MiB -- mostly the pair list, 4 bytes per site and partner
+// slot, with slots for 1.1 times the partners a uniform liquid has within the
+// real-space cut-off, plus 48.  A configuration denser than that somewhere
+// returns GB_E_LIST.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "gb_common.cuh"
@@ -42,12 +50,14 @@ constexpr int MAX_SITES = 8192;
 constexpr int MAX_NB = 64;
 constexpr int MAX_NK = 2048;
 constexpr int MAX_NKXY = 512;
-constexpr int MAX_CAP = 192;
 constexpr int MAX_DEVICES = 64;
 
 __device__ __align__(256) unsigned char g_static_scratch[STATIC_SCRATCH_BYTES];
 
 unsigned char *g_scratch_ptr[MAX_DEVICES] = {nullptr};
+
+// serialises calls: the device array and the host tables below are shared
+std::mutex g_static_lock;
 
 // host-side k tables (fixed size: no heap allocation)
 KCol h_col[MAX_NKXY];
@@ -74,6 +84,12 @@ int cuda_fail(cudaError_t e, const char *what) {
 extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, const int *nb,
                                           const int *na, const double *boxlxyz, const double *z,
                                           double *virial) {
+  std::lock_guard<std::mutex> hold(g_static_lock);
+  cudaStream_t s = cudaStreamPerThread;  // per-thread default stream: no stream object is created
+  struct Drain {  // an error return still waits for the call's device work before the lock opens
+    cudaStream_t s;
+    ~Drain() { cudaStreamSynchronize(s); }
+  } drain{s};
   const gb_params &P = current_params();
   const int B = *nb, n = *na;
   if (n <= 0 || n % 3 != 0) return ctx_set_error(GB_E_ARG, "potenl 1: na is not 3*nm");
@@ -97,8 +113,10 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
     return ctx_set_error(GB_E_NOMEM, "static Ewald: more than 2048 k vectors or 512 (kx, ky) columns");
   const int nchunk = (n + recip_sk_chunk() - 1) / recip_sk_chunk();
   const size_t N = 3 * (size_t)n * B;
+  // partner slots per site: 1.1 times a uniform liquid's partners within the
+  // cut-off (unit box), plus 48, at most every other site
   double onepivol = (4.0 / 3.0) * PI * P.wrcut * P.wrcut * P.wrcut;
-  int cap = std::min(std::min((int)(1.1 * n * onepivol) + 48, n), MAX_CAP);
+  int cap = std::min((int)(1.1 * n * onepivol) + 48, n);
   // carve the buffer
   unsigned char *base = g_scratch_ptr[dev];
   size_t off = 0;
@@ -125,9 +143,10 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   double *d_sk = (double *)take(sizeof(double) * 8 * (size_t)kt.nkp * B);
   double *d_acc = (double *)take(sizeof(double) * ACC_STRIDE);
   unsigned *d_status = (unsigned *)take(sizeof(unsigned));
-  if (off > STATIC_SCRATCH_BYTES) return ctx_set_error(GB_E_NOMEM, "static Ewald: working set exceeds the 16 MiB buffer");
+  if (off > STATIC_SCRATCH_BYTES)
+    return ctx_set_error(GB_E_NOMEM, "static Ewald: working set (" + std::to_string(off >> 10) + " KiB, " +
+                                         std::to_string(cap) + " list slots per site) exceeds the 16 MiB buffer");
 
-  cudaStream_t s = 0;  // legacy default stream: no stream object is created
   SCK(cudaMemcpyAsync(d_r, r, sizeof(double) * N, cudaMemcpyHostToDevice, s));
   SCK(cudaMemcpyAsync(d_z, z, sizeof(double) * n, cudaMemcpyHostToDevice, s));
   SCK(cudaMemcpyAsync(d_col, h_col, sizeof(KCol) * kt.ncol, cudaMemcpyHostToDevice, s));
@@ -192,7 +211,8 @@ extern "C" int gbrpmd_forces_ewald_static(double *r, double *v, double *dvdr, co
   SCK(cudaMemcpyAsync(acc, d_acc, sizeof(double) * ACC_STRIDE, cudaMemcpyDeviceToHost, s));
   SCK(cudaMemcpyAsync(&status, d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   SCK(cudaStreamSynchronize(s));
-  if (status & ST_LIST_OVERFLOW) return ctx_set_error(GB_E_LIST, "static Ewald: more than 192 partners per site");
+  if (status & ST_LIST_OVERFLOW)
+    return ctx_set_error(GB_E_LIST, "static Ewald: a site has more than " + std::to_string(cap) + " partners");
   double qq = 0.0;
   for (int i = 0; i < n; ++i) qq = qq + z[i] * z[i];
   const double vself = P.walpha / std::sqrt(PI) * qq;

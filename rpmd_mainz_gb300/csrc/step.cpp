@@ -350,13 +350,16 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   // positions) run on aux2 beside the list upkeep and the real-space kernel,
   // which writes its own gradient buffer; joined before the chain rule
   const bool branch = mixed && !c->prof && c->use_branches && c->aux2_stream;
+  int st0;
   if (branch) {
     recip_set_attributes_mx();
     CK(cudaEventRecord(c->fork2_ev, c->stream));
     CK(cudaStreamWaitEvent(c->aux2_stream, c->fork2_ev, 0));
     launch_recip_sk_mx(c->aux2_stream, c, c->rs, c->z, B);
     launch_recip_weights_mx(c->aux2_stream, c, B, slot(c, s));
+    if ((st0 = watch_mark(c, PR_RECIP_F, c->aux2_stream, 0))) return st0;
     launch_recip_force_mx(c->aux2_stream, c, B, c->g);
+    if ((st0 = watch_mark(c, PR_RECIP_F, c->aux2_stream, 1))) return st0;
     CK(cudaEventRecord(c->join2_ev, c->aux2_stream));
   }
   struct Join2 {  // an error return still joins the branch (a capture needs it)
@@ -379,20 +382,24 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   const double npairs = c->prof ? list_total(c->stream, c->pl) * (mixed ? 0.5 : 1.0) : 0.0;
   const double ksites = (double)c->nk * na * B;
   if (branch) {
+    if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 0))) return st0;
     launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
                          c->tune.ew_np, c->g2, slot(c, s), false);
+    if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 1))) return st0;
     join2.on = false;
     CK(cudaStreamWaitEvent(c->stream, c->join2_ev, 0));
-    launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, gscale, sign, accumulate, c->g2);
+    launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, gscale, sign, accumulate, c->g2, c->status);
     c->launches += 7;
     return GB_OK;
   }
   if (mixed) {
     recip_set_attributes_mx();
     prof_begin(c, PR_EW_REAL);
+    if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 0))) return st0;
     launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
                          c->tune.ew_np, c->g,
                          slot(c, s));
+    if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 1))) return st0;
     prof_end(c, PR_EW_REAL, npairs);
     prof_begin(c, PR_RECIP_SK);
     launch_recip_sk_mx(c->stream, c, c->rs, c->z, B);
@@ -401,11 +408,15 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
     launch_recip_weights_mx(c->stream, c, B, slot(c, s));
     prof_end(c, PR_RECIP_W, (double)c->nkp * B);
     prof_begin(c, PR_RECIP_F);
+    if ((st0 = watch_mark(c, PR_RECIP_F, c->stream, 0))) return st0;
     launch_recip_force_mx(c->stream, c, B, c->g);
+    if ((st0 = watch_mark(c, PR_RECIP_F, c->stream, 1))) return st0;
     prof_end(c, PR_RECIP_F, ksites);
   } else {
     prof_begin(c, PR_EW_REAL);
+    if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 0))) return st0;
     launch_ewald_real(c->stream, c->rs, c->z, na, B, c->pl, c->P.walpha, cub ? nullptr : c->box, c->g, slot(c, s));
+    if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 1))) return st0;
     prof_end(c, PR_EW_REAL, npairs);
     prof_begin(c, PR_RECIP_SK);
     launch_recip_sk(c->stream, c, c->rs, c->z, B);
@@ -414,11 +425,13 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
     launch_recip_weights(c->stream, c, B, slot(c, s));
     prof_end(c, PR_RECIP_W, (double)c->nkp * B);
     prof_begin(c, PR_RECIP_F);
+    if ((st0 = watch_mark(c, PR_RECIP_F, c->stream, 0))) return st0;
     launch_recip_force(c->stream, c, c->rs, c->z, B, c->g);
+    if ((st0 = watch_mark(c, PR_RECIP_F, c->stream, 1))) return st0;
     prof_end(c, PR_RECIP_F, ksites);
   }
   prof_begin(c, PR_MSITE);
-  launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, gscale, sign, accumulate);
+  launch_msite_chain(c->stream, c->g, out, na, B, c->P.alpha, gscale, sign, accumulate, nullptr, c->status);
   prof_end(c, PR_MSITE, (double)na * B);
   c->launches += 7;
   return GB_OK;
@@ -472,13 +485,16 @@ int term_lj(gb_context *c, const double *r, int B, double *out, int accumulate, 
     go.pos = r;
     go.cstride = 3LL * na;
     launch_frac32(c->stream, go, B, c->hi32, c->olo32);
+    if ((st = watch_mark(c, PR_LJ, c->stream, 0))) return st;
     launch_lj_mx(c->stream, c->hi32, c->olo32, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut,
                  c->box, 48.0 * c->P.oo_eps, c->tune.lj_np, out, slot(c, s));
     c->launches += 1;
   } else {
+    if ((st = watch_mark(c, PR_LJ, c->stream, 0))) return st;
     launch_lj(c->stream, r, na, B, c->pl, c->P.oo_sig * c->P.oo_sig, c->P.rcut * c->P.rcut, c->box,
               48.0 * c->P.oo_eps, out, slot(c, s));
   }
+  if ((st = watch_mark(c, PR_LJ, c->stream, 1))) return st;
   prof_end(c, PR_LJ, npairs);
   c->launches += 1;
   return GB_OK;
@@ -535,7 +551,7 @@ int term_tem(gb_context *c, const double *r, int B, double *out, double sign, in
   prof_begin(c, PR_TEM);
   launch_tem(c->stream, c->rs, c->z, na, B, c->pl, sig, c->box, c->g, slot(c, s));
   prof_end(c, PR_TEM, 0.0);
-  launch_msite_chain(c->stream, c->g, out, na, B, alpha, 1.0, sign, accumulate);
+  launch_msite_chain(c->stream, c->g, out, na, B, alpha, 1.0, sign, accumulate, nullptr, c->status);
   c->launches += 3;
   return GB_OK;
 }
@@ -549,7 +565,7 @@ int intra_model(const gb_params &P) {
 int term_intra(gb_context *c, const double *r, int B, double *out, int accumulate, int s) {
   if (c->P.intra_model != GB_INTRA_SPCFW && c->P.alp != 0.0 && c->P.alpb != 0.0)
     return ctx_set_error(GB_E_UNSUPPORTED, "intra_morse is not on the device path");
-  launch_intra(c->stream, r, out, c->na, B, intra_model(c->P), c->P, slot(c, s), accumulate);
+  launch_intra(c->stream, r, out, c->na, B, intra_model(c->P), c->P, slot(c, s), accumulate, c->status);
   c->launches += 1;
   return GB_OK;
 }
@@ -646,7 +662,7 @@ int low_frequency(gb_context *c, const double *rnm, const double *r, double *p, 
   prof_begin(c, PR_EXPAND);
   launch_expand_forces(c->stream, c->dvdr, con1 ? c->fb1 : nullptr, nbdf1, c->tw_c1,
                        con2 ? c->fb2 : nullptr, nbdf2, c->tw_c2, e1, e2, e3, p, halfdt, na, nb,
-                       c->tw_nb, c->P.precision == GB_PREC_MIXED);
+                       c->tw_nb, c->P.precision == GB_PREC_MIXED, c->status);
   prof_end(c, PR_EXPAND, 3.0 * na * nb);
   c->launches += 1;
   return GB_OK;
@@ -874,7 +890,11 @@ int dev_evolve_pi(gb_context *c, double dt, double beta) {
   prof_begin(c, PR_MTS);
   // one fused kernel for power-of-two nb up to 64 (k_mts.cu)
   int fused = 0;
-  if (!c->generic_mts) launch_fused_mts(s, c, dt, &fused);
+  if (!c->generic_mts) {
+    if ((st = watch_mark(c, PR_MTS, s, 0))) return st;
+    launch_fused_mts(s, c, dt, &fused);
+    if (fused && (st = watch_mark(c, PR_MTS, s, 1))) return st;
+  }
   if (fused) {
     c->plan.B_int = nb;
     c->launches += 1;
@@ -1027,6 +1047,7 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
     if (stw & ST_LIST_OVERFLOW) return ctx_set_error(GB_E_LIST, "neighbour list too small");
     if (stw & ST_RATTLE1) return ctx_set_error(GB_E_RATTLE1, "max iterations exceeded in rattle stage 1");
     if (stw & ST_RATTLE2) return ctx_set_error(GB_E_RATTLE2, "max iterations exceeded in rattle stage 2");
+    if (stw & ST_NONFINITE) return ctx_set_error(GB_E_NONFINITE, "non-finite force");
     return ctx_set_error(GB_E_NONFINITE, "device status error");
   }
   const double *A = c->h_acc;

@@ -84,6 +84,8 @@ def load(path=None):
     lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
     lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
     lib.gbrpmd_ctx_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_ctx_watch_region.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_ctx_watch_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     lib.gbrpmd_ctx_list_occupancy.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     lib.gbrpmd_ctx_set_params.argtypes = [C.c_void_p, C.c_void_p]
     lib.gbrpmd_run_md_eq.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int),
@@ -414,6 +416,19 @@ class Context:
     def set_graphs(self, on):
         """CUDA-graph replay of evolve steps (on by default)."""
         _check(load().gbrpmd_ctx_set_graphs(self.h, 1 if on else 0))
+
+    WATCH = {"mts_block": 0, "ewald_real": 2, "recip_force": 5, "lj": 6}
+
+    def watch(self, region):
+        """Time one region's kernel inside ordinary (graph-replayed) steps:
+        a region name of WATCH, or None to stop."""
+        _check(load().gbrpmd_ctx_watch_region(self.h, -1 if region is None else self.WATCH[region]))
+
+    def watch_ms(self):
+        """Duration of the watched kernel in the last step (synchronises)."""
+        ms = C.c_float()
+        _check(load().gbrpmd_ctx_watch_ms(self.h, C.byref(ms)))
+        return ms.value
 
     def list_rebuilds(self):
         """Rebuilds of the (Ewald, LJ, TEM) skin lists since creation."""

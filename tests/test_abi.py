@@ -52,3 +52,29 @@ def test_ran2_gaussian_match_reference_stream(gb):
     a = [lib.ran2(idum) for _ in range(200)] + [lib.gaussian(idum, 1.5) for _ in range(201)]
     b = [ref.ran2() for _ in range(200)] + [ref.gaussian(1.5) for _ in range(201)]
     assert a == b
+
+
+def test_params_layout_matches_ctypes_mirror(gb):
+    # sizeof(gb_params) and every field offset as the C compiler laid them out
+    n = len(GbParams._fields_)
+    offs = (C.c_int64 * n)()
+    gb.gbrpmd_params_layout.argtypes = [C.POINTER(C.c_int64), C.c_int]
+    size = gb.gbrpmd_params_layout(offs, n)
+    assert size == C.sizeof(GbParams)
+    for i, (name, _) in enumerate(GbParams._fields_):
+        assert offs[i] == getattr(GbParams, name).offset, name
+
+
+def test_fortran_binding_lists_every_field():
+    # the bind(c) type of the Fortran shim in INTEGRATION.md declares the same
+    # fields in the same order (and so the same layout) as struct gb_params
+    import os
+    import re
+
+    text = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "INTEGRATION.md")).read()
+    block = re.search(r"type, bind\(c\) :: gb_params\n(.*?)\n\s*end type", text, re.S).group(1)
+    fields = []
+    for line in block.splitlines():
+        decl = line.split("::", 1)[1]
+        fields += [f.strip() for f in decl.split(",")]
+    assert fields == [name for name, _ in GbParams._fields_]

@@ -2,17 +2,20 @@
 let the library allocate device memory (a host whose device memory is handed
 out by another framework's pool, or code that must not cudaMalloc/cudaFree
 while its streams run).  It works in a fixed 16 MiB array reserved at load
-time.  Checked against gbrpmd_forces (iopt = 2) on two calls in a row, at the
-tolerance of the other device tests (1e-10 relative); sizes beyond its limit
-are refused before any device work.  Collected last (file name) so that a run
-stopping at the first failure has already run every other test."""
+time and always computes in FP64.  Checked against gbrpmd_forces (iopt = 2,
+FP64) on two calls in a row, at the tolerance of the other device tests (1e-10
+relative), on a small box and on 216 molecules at nb = 8 (about 9 MiB of the
+array); sizes beyond its limit are refused before any device work, and a
+crowded configuration (more partners per site than the list slots) returns
+GB_E_LIST.  Collected last (file name) so that a run stopping at the first
+failure has already run every other test."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
 from rpmd_mainz_gb300 import lib, system
-from rpmd_mainz_gb300.abi import GB_E_NOMEM
+from rpmd_mainz_gb300.abi import GB_E_LIST, GB_E_NOMEM
 
 pytestmark = pytest.mark.gpu
 
@@ -44,8 +47,9 @@ def built():
     g.build()
 
 
-def test_static_ewald_matches_forces_twice():
-    s = system.water_box(PARAM, ncell=(4, 4, 4), nb=4)
+@pytest.mark.parametrize("ncell, nb", [((4, 4, 4), 4), ((6, 6, 6), 8)])
+def test_static_ewald_matches_forces_twice(ncell, nb):
+    s = system.water_box(PARAM, ncell=ncell, nb=nb)
     lib.init(s["params"])
     rng = np.random.default_rng(7)
     for call in range(2):
@@ -64,3 +68,18 @@ def test_static_ewald_refuses_oversize():
     st, _, _, _ = static_forces(s["r"], s["box"], s["z"])
     assert st == GB_E_NOMEM
     assert "8192" in lib.load().gbrpmd_last_error().decode()
+
+
+def test_static_ewald_reports_crowded_lists():
+    s = system.water_box(PARAM, ncell=(6, 6, 6), nb=1)
+    lib.init(s["params"])
+    nm = s["nm"]
+    mol = s["r"].reshape(1, nm, 3, 3)
+    crowded = (mol - 0.75 * mol[:, :, :1, :]).reshape(s["r"].shape)  # 64 times the density
+    st, _, _, _ = static_forces(crowded, s["box"], s["z"])
+    assert st == GB_E_LIST
+    assert "partners" in lib.load().gbrpmd_last_error().decode()
+    st, v, f, vir = static_forces(s["r"], s["box"], s["z"])  # the next call is unaffected
+    assert st == 0
+    v0, f0, _ = lib.forces(s["r"], s["box"], s["z"], 2)
+    assert abs(v - v0) <= TOL * abs(v0)
