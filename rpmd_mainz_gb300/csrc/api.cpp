@@ -190,6 +190,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
       (st = dalloc(c, &c->rb1, N)) || (st = dalloc(c, &c->fb1, N)) || (st = dalloc(c, &c->rb2, N)) ||
       (st = dalloc(c, &c->fb2, N)) || (st = dalloc(c, &c->g, N)) || (st = dalloc(c, &c->rs, N)) ||
       (st = dalloc(c, &c->rs32, (size_t)na * nb)) || (st = dalloc(c, &c->lo32, (size_t)na * nb)) ||
+      (st = dalloc(c, &c->fx32, (size_t)na * nb)) ||
       (st = dalloc(c, &c->hi32, (size_t)na * nb / 3)) || (st = dalloc(c, &c->olo32, (size_t)na * nb / 3)) ||
       (st = dalloc(c, &c->rs32_lj, (size_t)na * nb / 3)) || (st = dalloc(c, &c->g2, N)) ||
       (st = dalloc(c, &c->rc, S)) ||

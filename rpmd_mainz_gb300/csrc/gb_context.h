@@ -19,6 +19,7 @@ struct PairList {
   int *count = nullptr;  // [nconf][npt]
   int *idx = nullptr;    // [nconf][npt][cap]
   size_t bytes = 0;
+  int i16 = 0;           // entries are unsigned short (npt <= 65535): idx is read as that type
 };
 
 // Which accumulator slots the last evaluation filled and with how many
@@ -52,6 +53,7 @@ struct SkinList {
   int nconf = 0, npt = 0, unit = 0, excl = 0, full = 0;
   long long pstride = 0, cstride = 0;
   double cutsq = 0.0, skin = 0.0, box[3] = {0, 0, 0};
+  bool want16 = false;           // unsigned short entries asked for (used with the cell-sorted build)
 };
 enum { LIST_EW = 0, LIST_LJ = 1, LIST_TEM = 2, LIST_N = 3 };
 
@@ -88,6 +90,7 @@ struct gb_context {
   double *rs = nullptr;    // site positions scratch [nb][na][3]
   float4 *rs32 = nullptr;  // FP32 fractional coordinates for list prefilters [nb][na]
   float4 *lo32 = nullptr;  // their FP32 remainders (mixed precision) [nb][na]
+  int4 *fx32 = nullptr;    // fixed-point fractional coordinates (2^-32) and charge bits (mixed real space) [nb][na]
   float4 *hi32 = nullptr;  // bead oxygen coordinates for the FP32 LJ kernel [nb][nm]
   float4 *olo32 = nullptr; // and their remainders [nb][nm]
   // the LJ term of evolve_pi runs beside the Ewald term on aux_stream (forked

@@ -304,3 +304,99 @@ GB_D void gb_hc2r_s(In in, Out out, const R *__restrict__ tw, const R *__restric
     }
   }
 }
+
+// Lane-pair forms of the scaled power-of-two transforms, FP32 (N >= 4, M =
+// N/2): two adjacent lanes (q = lane & 1) share one coordinate row.  Lane q
+// holds the beads j = 2i + q (i < M) and the half-complex elements h = qM + i:
+// lane 0 the real parts Re X_0 .. Re X_{M-1}, lane 1 Re X_M followed by the
+// imaginary parts Im X_{M-1} .. Im X_1 (element N - k of the R2HC order is
+// Im X_k).  Both lanes of a pair must call, with every lane of the warp.
+//
+// Forward: each lane takes the unscaled M-point R2HC of its beads (E_k from the
+// even beads, O_k from the odd ones), the lanes swap them (M shuffles), and
+// X_k = sc (E_k + w^k O_k), w = exp(-2 pi i / N), lane 0 forming the real
+// parts and lane 1 the imaginary ones.
+// Inverse: the lanes swap their elements (M shuffles); lane 0 forms E'_k =
+// sc (X_k + conj X_{M-k}) and lane 1 O'_k = sc (X_k - conj X_{M-k}) exp(2 pi i
+// k / N), k <= M/2, and each takes the unscaled M-point HC2R of its sequence
+// into its beads.
+// Tables (R = float): twm / twm_l: cos, sin of 2 pi m / M (hi, lo); twfm /
+// twfm_l: half of those (the M-point forward split); twi / twi_l: sc cos, sc
+// sin of 2 pi m / N.  SPLIT uses the lo parts (gb_tmul).
+template <int N, bool SPLIT, class In, class Out>
+GB_D void gb_r2hc_pair(int q, In in, Out out, const float *__restrict__ twm, const float *__restrict__ twfm,
+                       const float *__restrict__ twi, const float *__restrict__ twm_l = nullptr,
+                       const float *__restrict__ twfm_l = nullptr, const float *__restrict__ twi_l = nullptr) {
+  constexpr int M = N / 2;
+  float y[M];
+  gb_r2hc_s<M, float, SPLIT>(in, [&](int k, float v) { y[k] = v; }, twm, twfm, twm_l, twfm_l);
+  float e[M], o[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    const float other = __shfl_xor_sync(0xffffffffu, y[i], 1);
+    e[i] = q ? other : y[i];
+    o[i] = q ? y[i] : other;
+  }
+  // E_k, O_k for k < M from their half-complex forms (period M, conjugate
+  // symmetric); k and M - k are compile-time after unrolling
+  auto re = [&](const float(&z)[M], int k) { return k <= M / 2 ? z[k] : z[M - k]; };
+  auto im = [&](const float(&z)[M], int k) {
+    return (k == 0 || 2 * k == M) ? 0.f : (2 * k < M ? z[M - k] : -z[k]);
+  };
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    // lane 0: Re X_i = sc Re E_i + sc c_i Re O_i + sc s_i Im O_i
+    // lane 1 (i > 0, k = M - i): Im X_k = sc Im E_k + sc c_k Im O_k - sc s_k Re O_k
+    // lane 1, i = 0: Re X_M = sc E_0 - sc O_0 (c_M = -1, s_M = 0)
+    const int k1 = M - i;
+    float A, B, Cc;
+    int kt;
+    if (i == 0) {
+      A = e[0];
+      B = o[0];
+      Cc = 0.f;
+      kt = q ? M : 0;
+    } else {
+      A = q ? im(e, k1) : re(e, i);
+      B = q ? im(o, k1) : re(o, i);
+      Cc = q ? -re(o, k1) : im(o, i);
+      kt = q ? k1 : i;
+    }
+    out(i, gb_tmul<SPLIT, float>(twi, twi_l, 0, A) + gb_tmul<SPLIT, float>(twi, twi_l, kt, B) +
+               gb_tmul<SPLIT, float>(twi, twi_l, N + kt, Cc));
+  }
+}
+
+template <int N, bool SPLIT, class In, class Out>
+GB_D void gb_hc2r_pair(int q, In in, Out out, const float *__restrict__ twm, const float *__restrict__ twi,
+                       const float *__restrict__ twm_l = nullptr, const float *__restrict__ twi_l = nullptr) {
+  constexpr int M = N / 2;
+  float l0[M], l1[M];  // the elements of lane 0 and of lane 1
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    const float mine = in(i);
+    const float other = __shfl_xor_sync(0xffffffffu, mine, 1);
+    l0[i] = q ? other : mine;
+    l1[i] = q ? mine : other;
+  }
+  auto reX = [&](int k) { return k < M ? l0[k] : l1[0]; };
+  auto imX = [&](int k) { return (k == 0 || k == M) ? 0.f : l1[M - k]; };
+  float z[M];  // half-complex input of this lane's M-point HC2R
+#pragma unroll
+  for (int k = 0; 2 * k <= M; ++k) {
+    // lane 0: E'_k = sc (X_k + conj X_{M-k}); lane 1: with D = X_k - conj X_{M-k},
+    // O'_k = sc D (c_k + i s_k): Re = sc c Dr - sc s Di, Im = sc s Dr + sc c Di
+    const float pr = reX(k) + reX(M - k), pi = imX(k) - imX(M - k);
+    const float dr = reX(k) - reX(M - k), di = imX(k) + imX(M - k);
+    const int kc = q ? k : 0;  // twi[0] = sc
+    const float zr = gb_tmul<SPLIT, float>(twi, twi_l, kc, q ? dr : pr) +
+                     gb_tmul<SPLIT, float>(twi, twi_l, N + k, q ? -di : 0.f);
+    z[k] = zr;
+    if (k > 0 && 2 * k < M) {
+      const float zi = gb_tmul<SPLIT, float>(twi, twi_l, N + k, q ? dr : 0.f) +
+                       gb_tmul<SPLIT, float>(twi, twi_l, kc, q ? di : pi);
+      z[M - k] = zi;
+    }
+  }
+  gb_hc2r_s<M, float, SPLIT>([&](int k) { return z[k]; }, out, twm, twm, twm_l, twm_l);
+}

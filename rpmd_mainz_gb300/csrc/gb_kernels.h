@@ -35,7 +35,7 @@ struct PairGeom {
 // wrapped fractional coordinates; optional remainders lo and per-point values
 // q (stored in frac.w)
 void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo = nullptr,
-                   const double *q = nullptr);
+                   const double *q = nullptr, int4 *fx = nullptr);
 // every pair within g.rcutsq; with a gate word, only when *gate != 0 (counts
 // are then zeroed on the device, so the decision needs no host round trip)
 void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
@@ -51,7 +51,8 @@ void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref,
 // writes frac / lo as launch_frac32), and the gated scatter + build
 bool list_cell_grid(const PairGeom &g, int nc[3], int *R, signed char *reach);
 void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
-                       const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag);
+                       const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag,
+                       int4 *fx = nullptr);
 // (also saves the reference positions and counts the rebuild, as launch_skin_save)
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
                          unsigned *status, const unsigned *gate, const CellSort &cs, double *ref,
@@ -79,9 +80,9 @@ void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const d
 // box: side lengths of the fractional coordinates (1, 1, 1 for the cubic sum);
 // np: lanes per site (8, 16, 32) / per oxygen (2, 4, 8)
 // add = false: g is overwritten (no zeroing pass needed)
-void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc,
-                          bool add = true);
+// fx: fixed-point fractional coordinates with the charge bits in w (frac_point)
+void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, int na, int B, const PairList &pl, double alpha,
+                          double rcutsq, const double *box, int np, double *g, double *acc, bool add = true);
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
                   double sigsq, double rcutsq, const double *box, double dscale, int np, double *out, double *acc);
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);

@@ -52,18 +52,23 @@ GB_D float dmin(float hi_a, float lo_a, float hi_b, float lo_b) {
 
 // rwald (ewald_cubic.f90:78-233) in FP32 over a full list; g += gradient
 // (single writer per site), energy and virial halved for the double count.
-// The charge rides in hi.w.  Each lane takes every NP-th partner, four at a
-// time with their indices and positions loaded before any arithmetic, so that
-// four gathers are in flight per lane.
-// bx: side lengths that turn fractional differences into distances (1 in the
-// unit box of the cubic sum; the box in bohr for the non-cubic one,
-// rwald_basic / rwald_cell of ewald_noncubic.f90); UNIT: all ones (no scaling)
-template <int NP, bool UNIT>
-__global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
-                                                        int na, const int *__restrict__ count,
-                                                        const int *__restrict__ idx, int cap, float alpha,
-                                                        float sfac, float rcutsq, float3 bx, double *g,
-                                                        double *acc, int add) {
+// Positions are 32-bit fixed-point fractional coordinates (frac_point): the
+// wrapping difference of two, read as a signed integer, is the minimum-image
+// difference in units of 2^-32, and its conversion rounds it to FP32 relative
+// to its own size (the precision of the earlier hi + lo pair, with one 16-byte
+// gather per partner instead of two and no rint per component); the charge's
+// bits ride in w.  Each lane takes every NP-th partner, four at a time with
+// their indices and positions loaded before any arithmetic, so that four
+// gathers are in flight per lane.  IT: the list entry type (unsigned short
+// for up to 65535 sites halves the list's bytes).
+// bx: side lengths that turn fractional differences into distances, times
+// 2^-32 (1 * 2^-32 in the unit box of the cubic sum; the box in bohr for the
+// non-cubic one, rwald_basic / rwald_cell of ewald_noncubic.f90)
+template <int NP, typename IT>
+__global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__ fx, int na,
+                                                        const int *__restrict__ count, const IT *__restrict__ idx,
+                                                        int cap, float alpha, float sfac, float rcutsq, float3 bx,
+                                                        double *g, double *acc, int add) {
   __shared__ float sh[32 * 8];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
@@ -71,24 +76,19 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int i = (int)(tid / NP), sub = (int)(tid % NP);
   const bool active = i < na;
-  const float4 *H = hi + (long long)c * na, *Lo = lo + (long long)c * na;
+  const int4 *X = fx + (long long)c * na;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   float ev = 0.f, evc = 0.f, vxx = 0.f, vyx = 0.f, vzx = 0.f, vyy = 0.f, vzy = 0.f, vzz = 0.f;
   if (active) {
-    const float4 hi_i = H[i], lo_i = Lo[i];
-    const float qi = hi_i.w;
+    const int4 xi = X[i];
+    const float qi = __int_as_float(xi.w);
     const int m3 = (i / 3) * 3;  // first site of i's molecule
     const int n = min(count[(long long)c * na + i], cap);
-    const int *L = idx + ((long long)c * na + i) * cap;
-    auto pair = [&](int j, const float4 &hj, const float4 &lj) {
-      float dx = dmin(hi_i.x, lo_i.x, hj.x, lj.x);
-      float dy = dmin(hi_i.y, lo_i.y, hj.y, lj.y);
-      float dz = dmin(hi_i.z, lo_i.z, hj.z, lj.z);
-      if (!UNIT) {
-        dx *= bx.x;
-        dy *= bx.y;
-        dz *= bx.z;
-      }
+    const IT *L = idx + ((long long)c * na + i) * cap;
+    auto pair = [&](int j, const int4 &xj) {
+      const float dx = (float)(int)((unsigned)xi.x - (unsigned)xj.x) * bx.x;
+      const float dy = (float)(int)((unsigned)xi.y - (unsigned)xj.y) * bx.y;
+      const float dz = (float)(int)((unsigned)xi.z - (unsigned)xj.z) * bx.z;
       const float drsq = dx * dx + dy * dy + dz * dz;
       if (!(drsq < rcutsq)) return;  // skin-list entry beyond the cut-off
       const float inv = rsqrtf(drsq);
@@ -99,16 +99,16 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
       if ((unsigned)(j - m3) < 3u) erfc -= 1.0f;  // same molecule
       const float du = erfc * inv;
       const float dur = (sfac * e - du) * (inv * inv);
-      const float qij = qi * hj.w;
+      const float qij = qi * __int_as_float(xj.w);
       const float dvr = qij * dur;
-      const float fx = dvr * dx, fy = dvr * dy, fz = dvr * dz;
-      kadd(sx, cx, fx);
+      const float fx_ = dvr * dx, fy = dvr * dy, fz = dvr * dz;
+      kadd(sx, cx, fx_);
       kadd(sy, cy, fy);
       kadd(sz, cz, fz);
       kadd(ev, evc, qij * du);
-      vxx += dx * fx;
-      vyx += dy * fx;
-      vzx += dz * fx;
+      vxx += dx * fx_;
+      vyx += dy * fx_;
+      vzx += dz * fx_;
       vyy += dy * fy;
       vzy += dz * fy;
       vzz += dz * fz;
@@ -116,27 +116,26 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const float4 *__restrict
     int t = sub;
     for (; t + 3 * NP < n; t += 4 * NP) {
       const int j0 = L[t], j1 = L[t + NP], j2 = L[t + 2 * NP], j3 = L[t + 3 * NP];
-      const float4 h0 = H[j0], h1 = H[j1], h2 = H[j2], h3 = H[j3];
-      const float4 l0 = Lo[j0], l1 = Lo[j1], l2 = Lo[j2], l3 = Lo[j3];
-      pair(j0, h0, l0);
-      pair(j1, h1, l1);
-      pair(j2, h2, l2);
-      pair(j3, h3, l3);
+      const int4 x0 = X[j0], x1 = X[j1], x2 = X[j2], x3 = X[j3];
+      pair(j0, x0);
+      pair(j1, x1);
+      pair(j2, x2);
+      pair(j3, x3);
     }
     for (; t < n; t += NP) {
       const int j = L[t];
-      pair(j, H[j], Lo[j]);
+      pair(j, X[j]);
     }
   }
   // each lane's compensated sum, then FP32 across the site's lanes
-  const float fx = group_sum_f<NP>(sx - cx);
-  const float fy = group_sum_f<NP>(sy - cy);
-  const float fz = group_sum_f<NP>(sz - cz);
+  const float fx0 = group_sum_f<NP>(sx - cx);
+  const float fy0 = group_sum_f<NP>(sy - cy);
+  const float fz0 = group_sum_f<NP>(sz - cz);
   if (active && sub == 0) {
     double *G = g + ((long long)c * na + i) * 3;
-    G[0] = (add ? G[0] : 0.0) + f2d(fx);
-    G[1] = (add ? G[1] : 0.0) + f2d(fy);
-    G[2] = (add ? G[2] : 0.0) + f2d(fz);
+    G[0] = (add ? G[0] : 0.0) + f2d(fx0);
+    G[1] = (add ? G[1] : 0.0) + f2d(fy0);
+    G[2] = (add ? G[2] : 0.0) + f2d(fz0);
   }
   const float vir6[6] = {vxx, vyx, vzx, vyy, vzy, vzz};
   constexpr int dst[7] = {0, 1, 2, 3, 5, 6, 9};       // v, xx, yx, zx, yy, zy, zz
@@ -547,20 +546,21 @@ int sm_count_mx() {
 
 }  // namespace
 
-void launch_ewald_real_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
-                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc,
-                          bool add) {
-  const float3 bx = make_float3((float)box[0], (float)box[1], (float)box[2]);
+void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, int na, int B, const PairList &pl, double alpha,
+                          double rcutsq, const double *box, int np, double *g, double *acc, bool add) {
+  const float two32 = 2.3283064365386963e-10f;  // 2^-32: fixed-point units to fractions
+  const float3 bx = make_float3((float)box[0] * two32, (float)box[1] * two32, (float)box[2] * two32);
   auto go = [&](auto NPc) {
     constexpr int NP = decltype(NPc)::value;
     dim3 grid(nblk((long long)na * NP, MX_T), B);
     const float sfac = (float)(-2.0 * alpha / std::sqrt(std::acos(-1.0)));  // d erfc(alpha r) / dr factor
-    if (bx.x == 1.f && bx.y == 1.f && bx.z == 1.f)
-      k_ewald_real_mx<NP, true><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
-                                                      (float)rcutsq, bx, g, acc, add ? 1 : 0);
+    if (pl.i16)
+      k_ewald_real_mx<NP, unsigned short><<<grid, MX_T, 0, s>>>(
+          fx, na, pl.count, reinterpret_cast<const unsigned short *>(pl.idx), pl.cap, (float)alpha, sfac,
+          (float)rcutsq, bx, g, acc, add ? 1 : 0);
     else
-      k_ewald_real_mx<NP, false><<<grid, MX_T, 0, s>>>(hi, lo, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
-                                                       (float)rcutsq, bx, g, acc, add ? 1 : 0);
+      k_ewald_real_mx<NP, int><<<grid, MX_T, 0, s>>>(fx, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
+                                                     (float)rcutsq, bx, g, acc, add ? 1 : 0);
   };
   if (np == 8) go(std::integral_constant<int, 8>());
   else if (np == 32) go(std::integral_constant<int, 32>());

@@ -290,38 +290,56 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
   const int orow = ml * 9 + xyz;                   // oxygen row of the same coordinate
   float *dv_row = s_dvf + t * C::LD;
 
-  // kicks in FP64, then the modes: mode 0 = sc * (FP64 bead sum), modes k >= 1
-  // from the FP32 transform of the deviations from bead 0
+  // The opening kicks and the forward transforms without per-element FP64
+  // instructions.  Momenta: the forces become FP32 (integer-built rounding) and
+  // the kick p - halfdt dvdr - halfdtsmall dvdr2 (evolve_pi.f90:82-83) is
+  // formed in FP32 with hi + lo coefficients; the bead momenta of a ring are
+  // independent draws, so FP32 holds them to the precision of their spread.
+  // Positions: each bead's deviation from bead 0, (hi_j - hi_0) + (lo_j - lo_0)
+  // from integer-built hi + lo splits, so that FP32 keeps ~2^-24 of the
+  // deviation rather than of the coordinate.  The centroid modes take
+  // compensated (Kahan) FP32 bead sums and one FP64 product each; modes k >= 1
+  // come from the FP32 transform with split twiddles (the state's round trip:
+  // no systematic gain per step).
   double p0, x0;
   float pf[NB], xf[NB];
   {
-    double v[NB];
-    auto to_modes = [&](float (&out)[NB]) {
-      double sum = 0.0;
-#pragma unroll
-      for (int j = 0; j < NB; ++j) sum += v[j];
-      const double v0 = v[0];
-      float d[NB];
-#pragma unroll
-      for (int j = 0; j < NB; ++j) d[j] = (float)(v[j] - v0);
-      // the state's round trip (this forward transform, the inverse at the end
-      // of the step) uses split tables: no systematic gain per step
-      gb_r2hc_s<NB, float, true>([&](int j) { return d[j]; }, [&](int k, float val) { out[k] = val; }, s_tw, s_twf,
-                                 s_tw_l, s_twf_l);
-      return sc * sum;
+    float d[NB];
+    float ch = 0.f, cc = 0.f;  // Kahan sum and its running compensation
+    auto kahan = [&](float v) {
+      const float y = v - cc;
+      const float t2 = ch + y;
+      cc = (t2 - ch) - y;
+      ch = t2;
     };
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
-      const double dv = a.dvdr[row + S * j];
-      const double pj = a.p[row + S * j] - a.halfdt * dv;
-      v[j] = pj - a.halfdtsmall * a.dvdr2[row + S * j];
-      dv_row[j] = (float)dv;
+      const float dv = d2f(a.dvdr[row + S * j]), dv2 = d2f(a.dvdr2[row + S * j]);
+      dv_row[j] = dv;
+      const float kick = fmaf(a.hdt_h, dv, fmaf(a.hdt_l, dv, fmaf(a.hds_h, dv2, a.hds_l * dv2)));
+      d[j] = d2f(a.p[row + S * j]) - kick;
+      kahan(d[j]);
     }
     __syncthreads();  // the shared tables are written
-    p0 = to_modes(pf);
+    p0 = sc * (f2d(ch) - f2d(cc));
+    gb_r2hc_s<NB, float, true>([&](int j) { return d[j]; }, [&](int k, float val) { pf[k] = val; }, s_tw, s_twf,
+                               s_tw_l, s_twf_l);
+    const double r0 = a.r[row];
+    float h0, l0;
+    d2df(r0, h0, l0);
+    ch = 0.f;
+    cc = 0.f;
+    d[0] = 0.f;
 #pragma unroll
-    for (int j = 0; j < NB; ++j) v[j] = a.r[row + S * j];
-    x0 = to_modes(xf);
+    for (int j = 1; j < NB; ++j) {
+      float h, l;
+      d2df(a.r[row + S * j], h, l);
+      d[j] = (h - h0) + (l - l0);
+      kahan(d[j]);
+    }
+    x0 = sc * ((double)NB * r0 + (f2d(ch) - f2d(cc)));
+    gb_r2hc_s<NB, float, true>([&](int j) { return d[j]; }, [&](int k, float val) { xf[k] = val; }, s_tw, s_twf,
+                               s_tw_l, s_twf_l);
   }
 
   float e_lh = 0.f, e_ll = 0.f, q1h = 0.f, q1l = 0.f, q2h = 0.f, q2l = 0.f;  // df sums
@@ -501,6 +519,316 @@ __global__ void __launch_bounds__(MtsCfg<NB>::T_MAX, 2) k_mts_mixed(MtsArgs a) {
   }
 }
 
+// Mixed precision with two lanes per coordinate row (nb >= 8).  The same
+// step as k_mts_mixed, but a row's beads and normal modes are split over a
+// lane pair (gb_r2hc_pair / gb_hc2r_pair: lane q holds the beads 2i + q and
+// the half-complex elements qM + i, M = nb / 2), so that the grid has twice
+// the warps (one thread per row left the SMs latency-bound at ~8 warps each)
+// and each lane runs M-point transforms (half the code).  The centroid mode
+// (FP64) is kept by both lanes of a pair with the same operations, so the two
+// copies stay equal; lane 0's element 0 (the FP32 centroid slot) stays zero.
+template <int NB>
+struct MtsPairCfg {
+  static constexpr int M = NB / 2;
+  static constexpr int MPB_MAX = NB <= 32 ? 28 : 14;
+  static constexpr int T_MAX = (18 * MPB_MAX + 31) / 32 * 32;
+  static constexpr int LD = NB + 2;  // bead stride in shared memory: lanes (row r, q) hit banks 2r + q
+};
+
+template <int NB>
+__global__ void __launch_bounds__(MtsPairCfg<NB>::T_MAX, 1) k_mts_mixed_pair(MtsArgs a) {
+  using C = MtsPairCfg<NB>;
+  constexpr int M = C::M;
+  extern __shared__ double sm[];
+  const int T = blockDim.x;
+  const int nrow = (T / 2 + 8) / 9 * 9;
+  const int nf = (3 * nrow * C::LD + 1) & ~1;
+  float *s_dev = reinterpret_cast<float *>(sm);    // [nrow][LD] x_j - (oxygen centroid)
+  float *s_f2 = s_dev + nrow * C::LD;              // [nrow][LD] intramolecular forces
+  float *s_dvf = s_f2 + nrow * C::LD;              // [nrow][LD] dvdr for the estimator
+  double *s_cen = sm + nf / 2;                     // [nrow] row centroids
+  double *s_mono = s_cen + nrow;                   // [12] monodromy of the centroid mode
+  double *s_red = s_mono + 12;                     // [32 warps][18]
+  float *s_mh = reinterpret_cast<float *>(s_red + 32 * 18);  // [12*NB] coefficients, hi
+  float *s_ml = s_mh + 12 * NB;                    // [12*NB] lo
+  float *s_twm = s_ml + 12 * NB;                   // [2M] cos, sin of 2 pi m / M
+  float *s_twm_l = s_twm + 2 * M;
+  float *s_twfm = s_twm_l + 2 * M;                 // [2M] half of s_twm
+  float *s_twfm_l = s_twfm + 2 * M;
+  float *s_twi = s_twfm_l + 2 * M;                 // [2NB] sc cos, sc sin of 2 pi m / nb
+  float *s_twi_l = s_twi + 2 * NB;
+  float *s_ct = s_twi_l + 2 * NB;                  // [2][2*MTS_NBC] contraction cos, sin
+  const int t = threadIdx.x;
+  const double sc = a.sc;
+  for (int i = t; i < 12 * NB; i += T) {
+    const double w = a.monod[i];
+    d2df(w, s_mh[i], s_ml[i]);
+    if (i < 12) s_mono[i] = w;
+  }
+  for (int i = t; i < 2 * M; i += T) {  // length-M tables: every other entry of length nb
+    const int mm = i < M ? 2 * i : NB + 2 * (i - M);
+    float h, l;
+    d2df(a.tw[mm], h, l);
+    s_twm[i] = h, s_twm_l[i] = l;
+    s_twfm[i] = 0.5f * h, s_twfm_l[i] = 0.5f * l;
+  }
+  for (int i = t; i < 2 * NB; i += T) d2df(sc * a.tw[i], s_twi[i], s_twi_l[i]);
+  for (int i = t; i < 4 * MTS_NBC; i += T) {
+    const int qq = i / (2 * MTS_NBC), e = i % (2 * MTS_NBC);
+    const double *tw = qq ? a.tw_c2 : a.tw_c1;
+    const int nbc = qq ? a.nbc2 : a.nbc1;
+    const double *rb = qq ? a.rb2 : a.rb1;
+    s_ct[i] = rb && e < 2 * nbc ? d2f(tw[e]) : 0.f;
+  }
+  const int q = t & 1;   // beads 2i + q, half-complex elements qM + i
+  const int rl = t >> 1; // row of the block
+  const int mpb = a.mpb;
+  const int m0 = blockIdx.x * mpb;
+  const int ml = rl / 9, lr = rl % 9;
+  const int m = m0 + ml;
+  const bool valid = ml < mpb && m < a.nm;
+  const int mc = valid ? m : a.nm - 1;
+  const long long S = 3LL * a.na;
+  const long long row = 9LL * mc + lr;
+  const int ic = lr / 3;
+  const int xyz = lr % 3;
+  const int orow = ml * 9 + xyz;
+  float *dv_row = s_dvf + rl * C::LD;
+  auto bead = [&](int i) { return 2 * i + q; };
+
+  // opening kicks and forward transforms without per-element FP64 (as in
+  // k_mts_mixed); each lane's compensated bead sums are combined over the pair
+  double p0, x0;
+  float pf[M], xf[M];
+  {
+    float d[M];
+    float ch = 0.f, cc = 0.f;
+    auto kahan = [&](float v) {
+      const float y = v - cc;
+      const float t2 = ch + y;
+      cc = (t2 - ch) - y;
+      ch = t2;
+    };
+    auto pair_sum = [&]() {  // the same FP64 value on both lanes (addition commutes)
+      const float oh = __shfl_xor_sync(0xffffffffu, ch, 1), oc = __shfl_xor_sync(0xffffffffu, cc, 1);
+      return (f2d(ch) - f2d(cc)) + (f2d(oh) - f2d(oc));
+    };
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      const long long o = row + S * bead(i);
+      const float dv = d2f(a.dvdr[o]), dv2 = d2f(a.dvdr2[o]);
+      dv_row[bead(i)] = dv;
+      const float kick = fmaf(a.hdt_h, dv, fmaf(a.hdt_l, dv, fmaf(a.hds_h, dv2, a.hds_l * dv2)));
+      d[i] = d2f(a.p[o]) - kick;
+      kahan(d[i]);
+    }
+    __syncthreads();  // the shared tables are written
+    p0 = sc * pair_sum();
+    gb_r2hc_pair<NB, true>(q, [&](int i) { return d[i]; }, [&](int i, float v) { pf[i] = v; }, s_twm, s_twfm,
+                           s_twi, s_twm_l, s_twfm_l, s_twi_l);
+    const double r0 = a.r[row];
+    float h0, l0;
+    d2df(r0, h0, l0);
+    ch = 0.f;
+    cc = 0.f;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      float h, l;
+      d2df(a.r[row + S * bead(i)], h, l);
+      d[i] = (h - h0) + (l - l0);
+      kahan(d[i]);
+    }
+    x0 = sc * ((double)NB * r0 + pair_sum());
+    gb_r2hc_pair<NB, true>(q, [&](int i) { return d[i]; }, [&](int i, float v) { xf[i] = v; }, s_twm, s_twfm,
+                           s_twi, s_twm_l, s_twfm_l, s_twi_l);
+    if (q == 0) pf[0] = xf[0] = 0.f;  // the centroid is p0, x0
+  }
+
+  float e_lh = 0.f, e_ll = 0.f, q1h = 0.f, q1l = 0.f, q2h = 0.f, q2l = 0.f;  // df sums
+  float vir[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float off = 0.f;
+  for (int im = 1; im <= a.mts; ++im) {
+    {  // free ring-polymer rotation (evolve_pi.f90:109-125)
+      const double *mo = s_mono + ic;
+      const double pp = p0 * mo[0] + x0 * mo[3];
+      x0 = p0 * mo[6] + x0 * mo[9];
+      p0 = pp;
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        const int h = q * M + i;
+        const float *hh = s_mh + ic + 12 * h, *ll = s_ml + ic + 12 * h;
+        const float pk = pf[i], xk = xf[i];
+        pf[i] = fmaf(pk, hh[0], fmaf(xk, hh[3], fmaf(pk, ll[0], xk * ll[3])));
+        xf[i] = fmaf(pk, hh[6], fmaf(xk, hh[9], fmaf(pk, ll[6], xk * ll[9])));
+      }
+    }
+    const double cen = sc * x0;
+    if (q == 0) s_cen[rl] = cen;
+    __syncthreads();
+    {
+      float oh, ol;
+      d2df(cen - s_cen[orow], oh, ol);
+      off = oh + ol;
+    }
+    {  // bead positions relative to the oxygen centroid (evolve_pi.f90:141-145)
+      float *dst = s_dev + rl * C::LD;
+      const bool last = im == a.mts && valid;
+      double *gr = a.r + row;
+      gb_hc2r_pair<NB, true>(q, [&](int i) { return xf[i]; },
+                             [&](int i, float v) {
+                               dst[bead(i)] = off + v;
+                               if (last) gr[S * bead(i)] = cen + f2d(v);
+                             },
+                             s_twm, s_twi, s_twm_l, s_twi_l);
+    }
+    __syncthreads();
+    float esh = 0.f, esl = 0.f;
+    for (int idx = t; idx < mpb * NB; idx += T) {
+      const int mm = idx / NB, j = idx % NB;
+      const bool w = m0 + mm < a.nm;
+      float xr[9], fm[9], vm[9];
+#pragma unroll
+      for (int d = 0; d < 9; ++d) xr[d] = s_dev[(mm * 9 + d) * C::LD + j];
+      const float e = intra_molecule_t<float>(a.model, xr, fm, vm, a.ip);
+#pragma unroll
+      for (int d = 0; d < 9; ++d) s_f2[(mm * 9 + d) * C::LD + j] = fm[d];
+      if (w) {
+        df_acc(esh, esl, e);
+#pragma unroll
+        for (int d = 0; d < 9; ++d) vir[d] += vm[d];
+      }
+    }
+    if (im == a.mts) e_lh = esh, e_ll = esl;
+    __syncthreads();
+    {
+      const float *dev_row = s_dev + rl * C::LD;
+      const float *f2_row = s_f2 + rl * C::LD;
+      if (valid) {  // virial_ke partial sums (kinetic.f90:23-40) over this lane's beads
+        float a1 = 0.f, a2 = 0.f;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const float dr = dev_row[bead(i)] - off;
+          a1 += dr * dv_row[bead(i)];
+          a2 += dr * f2_row[bead(i)];
+        }
+        df_acc(q1h, q1l, a1);
+        df_acc(q2h, q2l, a2);
+      }
+      if (im != a.mts) {  // FT(dvdr2) and p -= dtsmall dvdr2 (evolve_pi.f90:156-159)
+        const float dtsf = (float)a.dtsmall;
+        float f0 = 0.f;
+        gb_r2hc_pair<NB, false>(q, [&](int i) { return f2_row[bead(i)]; },
+                                [&](int i, float v) {
+                                  if (q == 0 && i == 0) f0 = v;
+                                  else pf[i] = fmaf(-dtsf, v, pf[i]);
+                                },
+                                s_twm, s_twfm, s_twi);
+        f0 = __shfl_sync(0xffffffffu, f0, (t & 31) & ~1);  // lane 0's centroid force
+        p0 = p0 - a.dtsmall * f2d(f0);
+      }
+    }
+    if (im != a.mts) __syncthreads();
+  }
+  {
+    // back to beads: p = HC2R(p); r = rst (written in the last substep);
+    // p -= halfdtsmall dvdr2 (evolve_pi.f90:222-228)
+    const float *f2_row = s_f2 + rl * C::LD;
+    const float hds = (float)a.halfdtsmall;
+    const double pc = sc * p0;
+    double *gp = a.p + row;
+    bool bad = gb_nonfinite(pc);
+    gb_hc2r_pair<NB, true>(q, [&](int i) { return pf[i]; },
+                           [&](int i, float v) {
+                             const float dp = fmaf(-hds, f2_row[bead(i)], v);
+                             bad |= gb_nonfinite(dp);
+                             if (valid) gp[S * bead(i)] = pc + f2d(dp);
+                           },
+                           s_twm, s_twi, s_twm_l, s_twi_l);
+    if (valid) {
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        const int h = q * M + i;
+        a.rnm[row + S * h] = h ? f2d(xf[i]) : x0;
+        a.dvdr2[row + S * bead(i)] = f2d(f2_row[bead(i)]);
+        bad |= gb_nonfinite(f2_row[bead(i)]);
+      }
+      gb_flag_nonfinite(a.status, bad);
+    }
+    // contracted rings of the new positions: rb_j = s12 x0 + s12 y_j, y_j =
+    // sum_k 2 (Re X_k cos - Im X_k sin); lane 0 sums the real parts, lane 1 the
+    // imaginary ones, and the lane of the bead's parity stores
+    auto contract = [&](double *rb, int nbc, const float *ct, double s12) {
+      const int h = (nbc - 1) / 2;
+      const double base = s12 * x0;
+      const float sf = d2f(s12);
+      for (int j = 0; j < nbc; ++j) {
+        float y = 0.f;
+        int mm = 0;
+#pragma unroll
+        for (int k = 1; k <= (MTS_NBC - 1) / 2; ++k) {
+          if (k <= h && k < M) {
+            mm += j;
+            if (mm >= nbc) mm -= nbc;
+            y += q ? -2.f * xf[M - k] * ct[nbc + mm] : 2.f * xf[k] * ct[mm];
+          }
+        }
+        y += __shfl_xor_sync(0xffffffffu, y, 1);
+        if (valid && (j & 1) == q) rb[row + S * j] = base + f2d(sf * y);
+      }
+    };
+    if (a.rb1) contract(a.rb1, a.nbc1, s_ct, a.s12_1);
+    if (a.rb2) contract(a.rb2, a.nbc2, s_ct + 2 * MTS_NBC, a.s12_2);
+  }
+  // block totals: df / FP32 warp sums, FP64 across warps (threads 0..17)
+  float rh[9], rl9[9];  // energy, q1, q2, q1 by axis, q2 by axis
+  rh[0] = e_lh, rl9[0] = e_ll;
+  rh[1] = q1h, rl9[1] = q1l;
+  rh[2] = q2h, rl9[2] = q2l;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    rh[3 + d] = d == xyz ? q1h : 0.f, rl9[3 + d] = d == xyz ? q1l : 0.f;
+    rh[6 + d] = d == xyz ? q2h : 0.f, rl9[6 + d] = d == xyz ? q2l : 0.f;
+  }
+  const int lane = t & 31, warp = t >> 5, nw = (T + 31) / 32;
+  float *s_rf = reinterpret_cast<float *>(s_red);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) warp_sum_df(rh[i], rl9[i]);
+#pragma unroll
+  for (int d = 0; d < 9; ++d) vir[d] = warp_sum_f32(vir[d]);
+  if (lane == 0) {
+    float *o = s_rf + warp * 36;
+    o[0] = rh[0], o[1] = rl9[0];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) o[2 + 2 * d] = vir[d], o[3 + 2 * d] = 0.f;
+    o[20] = rh[1], o[21] = rl9[1];
+    o[22] = rh[2], o[23] = rl9[2];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      o[24 + 2 * d] = rh[3 + d], o[25 + 2 * d] = rl9[3 + d];
+      o[30 + 2 * d] = rh[6 + d], o[31 + 2 * d] = rl9[6 + d];
+    }
+  }
+  __syncthreads();
+  if (t < 18) {
+    double s2 = 0.0;
+    for (int w = 0; w < nw; ++w) s2 += df2d(s_rf[w * 36 + 2 * t], s_rf[w * 36 + 2 * t + 1]);
+    if (s2 != 0.0) {
+      if (t < 10) atomicAdd(a.acc_int + t, s2);
+      else if (t < 12) atomicAdd(a.acc_ke + (t - 10), s2);
+      else atomicAdd(a.acc_ke + 2 + (t - 12), s2);
+    }
+  }
+}
+
+template <int NB>
+size_t mts_smem_pair(int T) {
+  using C = MtsPairCfg<NB>;
+  const int nrow = (T / 2 + 8) / 9 * 9;
+  const int nf = (3 * nrow * C::LD + 1) & ~1;
+  return sizeof(float) * nf + sizeof(double) * (nrow + 12 + 32 * 18) +
+         sizeof(float) * (24 * NB + 8 * C::M + 4 * NB + 4 * MTS_NBC);
+}
+
 template <int NB>
 size_t mts_smem_mixed(int T) {
   using C = MtsCfg<NB>;
@@ -525,6 +853,9 @@ void launch_nb(cudaStream_t s, MtsArgs a, bool mixed) {
     cudaFuncSetAttribute(k_mts_fused<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mts_smem<NB>(C::T_MAX));
     cudaFuncSetAttribute(k_mts_mixed<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)mts_smem_mixed<NB>(C::T_MAX));
+    if constexpr (NB >= 8)
+      cudaFuncSetAttribute(k_mts_mixed_pair<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)mts_smem_pair<NB>(MtsPairCfg<NB>::T_MAX));
     attr = true;
   }
   int dev = 0, nsm = 1;
@@ -535,8 +866,15 @@ void launch_nb(cudaStream_t s, MtsArgs a, bool mixed) {
   // (gbrpmd_ctx_autotune) overrides it
   const int wave = std::max(nsm, 1) * (mixed ? 2 : 1);
   a.mpb = a.mpb > 0 ? std::min(C::MPB_MAX, a.mpb) : std::max(1, std::min(C::MPB_MAX, (a.nm + wave - 1) / wave));
-  const int T = (9 * a.mpb + 31) / 32 * 32;
   const unsigned grid = (unsigned)((a.nm + a.mpb - 1) / a.mpb);
+  if constexpr (NB >= 8) {
+    if (mixed) {  // two lanes per coordinate row
+      const int T2 = (18 * a.mpb + 31) / 32 * 32;
+      k_mts_mixed_pair<NB><<<grid, T2, mts_smem_pair<NB>(T2), s>>>(a);
+      return;
+    }
+  }
+  const int T = (9 * a.mpb + 31) / 32 * 32;
   if (mixed) k_mts_mixed<NB><<<grid, T, mts_smem_mixed<NB>(T), s>>>(a);
   else k_mts_fused<NB><<<grid, T, mts_smem<NB>(T), s>>>(a);
 }

@@ -28,14 +28,22 @@ constexpr int LB_T = 128;
 
 // wrapped fractional coordinates u in [0, 1) as FP32 (frac); with lo, also the
 // remainder u - frac as a second FP32, so that frac + lo carries u to ~1e-14
-// point t = (c, i): frac[t] (and lo[t]) from g.pos; returns frac[t]
-GB_D float4 frac_point(const PairGeom &g, long long t, int c, int i, float4 *frac, float4 *lo, const double *q) {
+// point t = (c, i): frac[t] (and lo[t]) from g.pos; returns frac[t].
+// fx (optional): the same coordinates in 32-bit fixed point, u * 2^32 rounded
+// and taken modulo 2^32, with the charge's FP32 bits in w.  A wrapping
+// difference of two of them, read as a signed integer, is the minimum-image
+// difference (|d| < 1/2) in units of 2^-32 exactly, so one integer subtraction
+// and one conversion give it to FP32 rounding of the difference itself.
+GB_D float4 frac_point(const PairGeom &g, long long t, int c, int i, float4 *frac, float4 *lo, const double *q,
+                       int4 *fx = nullptr) {
   const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
   float f[3], e[3];
+  unsigned fxd[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     double u = g.unit ? x[d] : x[d] * g.onbox[d];
     u -= floor(u);
+    fxd[d] = (unsigned)__double2ull_rn(u * 4294967296.0);  // u = 1 (rounded) wraps to 0
     const float uf = (float)u;
     // remainder against the rounded value, before 1.0f wraps to 0: hi + lo is
     // then u or u - 1, both the same point of the periodic box
@@ -45,13 +53,14 @@ GB_D float4 frac_point(const PairGeom &g, long long t, int c, int i, float4 *fra
   const float4 h = make_float4(f[0], f[1], f[2], q ? (float)q[i] : 0.0f);
   frac[t] = h;
   if (lo) lo[t] = make_float4(e[0], e[1], e[2], 0.0f);
+  if (fx) fx[t] = make_int4((int)fxd[0], (int)fxd[1], (int)fxd[2], __float_as_int(h.w));
   return h;
 }
 
-__global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q) {
+__global__ void k_frac32(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q, int4 *fx) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nconf * g.npt) return;
-  frac_point(g, t, (int)(t / g.npt), (int)(t % g.npt), frac, lo, q);
+  frac_point(g, t, (int)(t / g.npt), (int)(t % g.npt), frac, lo, q, fx);
 }
 
 // exact FP64 minimum-image test, rounded as the reference rounds it
@@ -192,7 +201,7 @@ GB_D int cell_of(float u, int n) { return max(min((int)(u * (float)n), n - 1), 0
 // (also writes the points' fractional coordinates, as k_frac32)
 __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q,
                                                     CellSortDev cs, const double *ref, double lim2, int check,
-                                                    unsigned *flag) {
+                                                    unsigned *flag, int4 *fx) {
   __shared__ bool last;
   __shared__ int part[256];
   const long long n = (long long)nconf * g.npt;
@@ -207,7 +216,7 @@ __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float
       const double dx = x[0] - r0[0], dy = x[1] - r0[1], dz = x[2] - r0[2];
       moved = !(dx * dx + dy * dy + dz * dz <= lim2);  // NaN counts as moved
     }
-    const float4 f = frac_point(g, t, c, i, frac, lo, q);
+    const float4 f = frac_point(g, t, c, i, frac, lo, q, fx);
     const int cell = (cell_of(f.z, cs.nz) * cs.ny + cell_of(f.y, cs.ny)) * cs.nx + cell_of(f.x, cs.nx);
     cs.cellid[t] = cell;
     cs.crank[t] = atomicAdd(cs.ccount + (long long)c * ncell + cell, 1);
@@ -285,8 +294,9 @@ __global__ void k_cell_scatter(PairGeom g, int nconf, const float4 *frac, CellSo
   cs.sidx[pos] = i;
 }
 
-template <bool FULL, bool EXCL>
-__global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, CellSortDev cs, int *count, int *idx,
+// IT: the list entry type (int, or unsigned short when npt <= 65535)
+template <bool FULL, bool EXCL, typename IT>
+__global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, CellSortDev cs, int *count, IT *idx,
                                                        int cap, float3 len, float thr_lo, float thr_hi,
                                                        unsigned *status, const unsigned *gate) {
   __shared__ signed char s_reach[sizeof(cs.reach)];
@@ -309,7 +319,7 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
   const double *xi = base + (long long)i * g.pstride;
   const double pi[3] = {xi[0], xi[1], xi[2]};
   const int x0 = cell_of(fi.x, cs.nx), y0 = cell_of(fi.y, cs.ny), z0 = cell_of(fi.z, cs.nz);
-  int *my = idx + ((long long)c * npt + i) * cap;
+  IT *my = idx + ((long long)c * npt + i) * cap;
   int n = 0;  // the same in every lane
   // lanes take consecutive cell-order slots (coalesced); hits keep slot order
   // four 32-slot groups per round: their loads are issued together (the loop
@@ -343,7 +353,7 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (hit) {
           const int pos = n + __popc(m & ((1u << lane) - 1u));
-          if (pos < cap) my[pos] = j;
+          if (pos < cap) my[pos] = (IT)j;
         }
         n += __popc(m);
       }
@@ -417,9 +427,10 @@ __global__ void k_skin_save(PairGeom g, int nconf, double *ref, const unsigned *
 
 // exact list from the superset: one warp per (configuration, point); the same
 // FP32 prefilter and reference-rounded FP64 band test as the full build, lanes
-// append in list order through a ballot
+// append in list order through a ballot (IT: the superset's entry type)
+template <typename IT>
 __global__ void __launch_bounds__(128) k_list_filter(PairGeom g, int nconf, const float4 *frac,
-                                                     const int *scount, const int *sidx, int scap,
+                                                     const int *scount, const IT *sidx, int scap,
                                                      int *count, int *idx, int cap, float3 len,
                                                      float thr_lo, float thr_hi, unsigned *status) {
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -431,7 +442,7 @@ __global__ void __launch_bounds__(128) k_list_filter(PairGeom g, int nconf, cons
   const float4 fi = fr[i];
   const double *pi = base + (long long)i * g.pstride;
   const int n = min(scount[w], scap);
-  const int *L = sidx + w * scap;
+  const IT *L = sidx + w * scap;
   int *out = idx + w * cap;
   int written = 0;
   for (int t0 = 0; t0 < n; t0 += 32) {
@@ -807,9 +818,10 @@ double list_total(cudaStream_t s, const PairList &pl) {
   return (double)h;
 }
 
-void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q) {
+void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
+                   int4 *fx) {
   long long n = (long long)nconf * g.npt;
-  k_frac32<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q);
+  k_frac32<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q, fx);
 }
 
 // FP32 thresholds around rcutsq: below lo accept, at or above hi reject,
@@ -948,10 +960,10 @@ CellSortDev dev_cells(const CellSort &cs) {
 // skin test and cell counts (every step), then, gated by flag, the cell-order
 // scatter (which also zeroes the list counts) and the build
 void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
-                       const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag) {
+                       const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag, int4 *fx) {
   CellSortDev d = dev_cells(cs);
   const long long n = (long long)nconf * g.npt;
-  k_cell_count<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q, d, ref, lim2, check, flag);
+  k_cell_count<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q, d, ref, lim2, check, flag, fx);
 }
 
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
@@ -963,16 +975,17 @@ void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const flo
   CellSortDev d = dev_cells(cs);
   const long long n = (long long)nconf * g.npt;
   k_cell_scatter<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, d, pl.count, gate, ref, rebuilds);
-  auto go = [&](auto kern) {
-    kern<<<nblk(32 * n, LB_T), LB_T, 0, s>>>(g, nconf, d, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status,
+  auto go = [&](auto kern, auto *idx) {
+    kern<<<nblk(32 * n, LB_T), LB_T, 0, s>>>(g, nconf, d, pl.count, idx, pl.cap, len, thr_lo, thr_hi, status,
                                              gate);
   };
+  unsigned short *i16 = reinterpret_cast<unsigned short *>(pl.idx);
   if (g.full) {
-    if (g.excl_mol) go(k_build_sorted<true, true>);
-    else go(k_build_sorted<true, false>);
+    if (g.excl_mol) pl.i16 ? go(k_build_sorted<true, true, unsigned short>, i16) : go(k_build_sorted<true, true, int>, pl.idx);
+    else pl.i16 ? go(k_build_sorted<true, false, unsigned short>, i16) : go(k_build_sorted<true, false, int>, pl.idx);
   } else {
-    if (g.excl_mol) go(k_build_sorted<false, true>);
-    else go(k_build_sorted<false, false>);
+    if (g.excl_mol) pl.i16 ? go(k_build_sorted<false, true, unsigned short>, i16) : go(k_build_sorted<false, true, int>, pl.idx);
+    else pl.i16 ? go(k_build_sorted<false, false, unsigned short>, i16) : go(k_build_sorted<false, false, int>, pl.idx);
   }
 }
 
@@ -982,8 +995,13 @@ void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const floa
   float thr_lo, thr_hi;
   list_thresholds(g, &len, &thr_lo, &thr_hi);
   const long long nw = (long long)nconf * g.npt;
-  k_list_filter<<<nblk(nw * 32, 128), 128, 0, s>>>(g, nconf, frac, skin.count, skin.idx, skin.cap, pl.count,
-                                                   pl.idx, pl.cap, len, thr_lo, thr_hi, status);
+  if (skin.i16)
+    k_list_filter<unsigned short><<<nblk(nw * 32, 128), 128, 0, s>>>(
+        g, nconf, frac, skin.count, reinterpret_cast<const unsigned short *>(skin.idx), skin.cap, pl.count, pl.idx,
+        pl.cap, len, thr_lo, thr_hi, status);
+  else
+    k_list_filter<int><<<nblk(nw * 32, 128), 128, 0, s>>>(g, nconf, frac, skin.count, skin.idx, skin.cap, pl.count,
+                                                        pl.idx, pl.cap, len, thr_lo, thr_hi, status);
 }
 
 void launch_msite(cudaStream_t s, const double *r, double *rs, int na, int B, double alpha,

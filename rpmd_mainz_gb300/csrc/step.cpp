@@ -180,13 +180,17 @@ int list_cap(int npt, double rc, double vol) {
 // Returns the number of launches through *nl.
 // With superset = true the filter is skipped and *use points at the skin list
 // itself (a consumer that tests the cut-off on its own); else *use = &c->pl.
+// fx (optional) receives the points' fixed-point coordinates every step
+// (frac_point); with want16 the superset stores unsigned short entries when the
+// cell-sorted build is used and the points number at most 65535.
 int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut, double vol, int *nl,
-              float4 *lo = nullptr, const double *q = nullptr, bool superset = false, PairList **use = nullptr) {
+              float4 *lo = nullptr, const double *q = nullptr, bool superset = false, PairList **use = nullptr,
+              int4 *fx = nullptr, bool want16 = false) {
   if (use) *use = &c->pl;
   int st = ensure_list(c, nconf, g.npt, list_cap(g.npt, cut, vol));
   if (st) return st;
   if (c->list_skin <= 0.0) {
-    launch_frac32(c->stream, g, nconf, c->rs32, lo, q);
+    launch_frac32(c->stream, g, nconf, c->rs32, lo, q, fx);
     launch_build_list(c->stream, g, nconf, c->rs32, c->pl, c->status);
     *nl = 2;
     return GB_OK;
@@ -195,7 +199,8 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   const double skin = c->list_skin * cut, scut = cut + skin;
   bool same = S.valid && S.nconf == nconf && S.npt == g.npt && S.unit == g.unit && S.excl == g.excl_mol &&
               S.full == g.full &&
-              S.pstride == g.pstride && S.cstride == g.cstride && S.cutsq == g.rcutsq && S.skin == skin;
+              S.pstride == g.pstride && S.cstride == g.cstride && S.cutsq == g.rcutsq && S.skin == skin &&
+              S.want16 == want16;
   for (int d = 0; d < 3; ++d) same = same && S.box[d] == g.box[d];
   if (!same) {
     S.valid = false;
@@ -237,6 +242,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     gsc.rcutsq = scut * scut;
     CellSort &cs = S.cells;
     cs.on = c->list_cells && list_cell_grid(gsc, cs.nc, &cs.R, cs.reach);
+    S.pl.i16 = want16 && cs.on && g.npt <= 65535 ? 1 : 0;
     if (cs.on) {
       const size_t ncell = (size_t)cs.nc[0] * cs.nc[1] * cs.nc[2];
       const size_t need_cell = sizeof(int) * (size_t)nconf * (2 * ncell + 1);  // counts, then offsets
@@ -268,7 +274,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   // the cell count kernel writes the gate itself
   if (!S.cells.on) CK(cudaMemsetAsync(S.flag, same ? 0 : 1, sizeof(unsigned), c->stream));
   int n = S.cells.on ? 0 : 1;  // the frac32 launch (else in the cell count)
-  if (!S.cells.on) launch_frac32(c->stream, g, nconf, c->rs32, lo, q);
+  if (!S.cells.on) launch_frac32(c->stream, g, nconf, c->rs32, lo, q, fx);
   // rebuild when a point moved by more than skin/2 (a hair less, for rounding)
   const double lim = 0.5 * skin * (1.0 - 1e-9);
   PairGeom gs = g;
@@ -276,7 +282,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   if (S.cells.on) {  // skin test and cell counts in one kernel, then the gated sort and build
     cudaError_t e0 = cudaGetLastError();
     if (e0 != cudaSuccess) return ctx_check_cuda(e0, "a launch before the cell count");
-    launch_cell_count(c->stream, g, nconf, c->rs32, lo, q, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag);
+    launch_cell_count(c->stream, g, nconf, c->rs32, lo, q, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag, fx);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell count launch");
     launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells, S.ref, S.rebuilds);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell build launch");
@@ -307,6 +313,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   S.cstride = g.cstride;
   S.cutsq = g.rcutsq;
   S.skin = skin;
+  S.want16 = want16;
   for (int d = 0; d < 3; ++d) S.box[d] = g.box[d];
   *nl = n;
   return GB_OK;
@@ -374,7 +381,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   PairList *pl = nullptr;  // mixed: the skin list itself, cut-off tested in the FP32 kernel
   const double vol = cub ? 1.0 : c->box[0] * c->box[1] * c->box[2];
   int st = make_list(c, LIST_EW, g, B, c->P.wrcut, vol, &nl, mixed ? c->lo32 : nullptr, mixed ? c->z : nullptr,
-                     mixed, &pl);
+                     mixed, &pl, mixed ? c->fx32 : nullptr, mixed);
   if (st) return st;
   prof_end(c, PR_LIST, (double)na * B);
   c->launches += nl;
@@ -383,7 +390,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   const double ksites = (double)c->nk * na * B;
   if (branch) {
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 0))) return st0;
-    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
+    launch_ewald_real_mx(c->stream, c->fx32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
                          c->tune.ew_np, c->g2, slot(c, s), false);
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 1))) return st0;
     join2.on = false;
@@ -396,9 +403,8 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
     recip_set_attributes_mx();
     prof_begin(c, PR_EW_REAL);
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 0))) return st0;
-    launch_ewald_real_mx(c->stream, c->rs32, c->lo32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
-                         c->tune.ew_np, c->g,
-                         slot(c, s));
+    launch_ewald_real_mx(c->stream, c->fx32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
+                         c->tune.ew_np, c->g, slot(c, s));
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 1))) return st0;
     prof_end(c, PR_EW_REAL, npairs);
     prof_begin(c, PR_RECIP_SK);
@@ -1114,7 +1120,7 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
 size_t dev_estimate_bytes(int na, int nb, const gb_params &P) {
   const size_t N = 3 * (size_t)na * nb, nm = na / 3;
   size_t b = sizeof(double) * (15 * N + 5 * (size_t)na + 12 * (size_t)nb + ACC_NSLOT * ACC_STRIDE);
-  b += sizeof(float4) * (2 * (size_t)na * nb + 2 * nm * nb);
+  b += sizeof(float4) * (3 * (size_t)na * nb + 2 * nm * nb);
   const int kmax = std::max(P.kmax, 0);
   const int cap_col = gb_kcap_col(kmax), cap_kp = gb_kcap_kp(kmax);
   std::vector<KCol> col(cap_col);
