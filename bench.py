@@ -498,10 +498,31 @@ def run_replicas(args, torch):
     batch.close()
     for c in ctxs:
         c.close()
-    # plain-FP64 loop over the same replicas, tuned the same way
+    # the same replicas in plain FP64, batched the same way (like for like)
     ctxs = contexts(0)
     for c, s in zip(ctxs, reps):
         c.autotune(s["dt"], s["beta"], steps=3)
+    batch = lib.Batch()
+    for i, (s, ctx) in enumerate(zip(reps, ctxs)):
+        batch.add(ctx, s["dt"], s["beta"], 0.01, -(5000 + i))
+    stream64 = torch.cuda.ExternalStream(batch.stream)
+    batch.step(args.warmup)
+    batch.sync()
+    b64_ms = []
+    for _ in range(max(2, args.steps // 4)):
+        with torch.cuda.stream(stream64):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream64)
+        batch.step(1)
+        with torch.cuda.stream(stream64):
+            e1.record(stream64)
+        e1.synchronize()
+        b64_ms.append(e0.elapsed_time(e1))
+    batch.sync()
+    batch.close()
+    fp64_batch_value = len(b64_ms) * work / (sum(b64_ms) * 1e-3)
+    # and as a plain host loop over the contexts (each on its own stream, all
+    # synchronised once per step)
     for c, s in zip(ctxs, reps):
         c.evolve(args.warmup, s["dt"], s["beta"])
     for c in ctxs:
@@ -540,7 +561,9 @@ def run_replicas(args, torch):
                    "l2": "inputs larger than L2 in aggregate", "parallelism": "one batch, one graph per step"},
         "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
         "autotune": {"seconds": t_tune, "distinct_shapes": len(shapes), "choices": shapes},
+        "fp64_batch": {"value": fp64_batch_value, "ms_per_step": float(np.mean(b64_ms))},
         "fp64_loop": {"value": fp64_value, "ms_per_step": float(np.mean(loop_ms))},
+        "batched_mixed_over_fp64_batch": value / fp64_batch_value,
         "batched_mixed_over_fp64_loop": value / fp64_value,
         "error_vs_fp64": {"force_rel_rms_max_of_8": max(errs), "bound": 1e-5,
                           "on": "the first 8 replicas after the timed steps"},

@@ -213,6 +213,7 @@ void ctx_free(gb_context *c) {
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   c->ev_pool.clear();
   if (c->d_count) cudaFree(c->d_count);
+  if (c->d_npair) cudaFree(c->d_npair);
   for (void *p : c->allocs) cudaFree(p);
   c->allocs.clear();
   for (void *p : {(void *)c->pl.idx, (void *)c->pl.count, (void *)c->pl_lj.idx, (void *)c->pl_lj.count, (void *)c->kcol,

@@ -14,7 +14,11 @@
 // step, every replica with thresh > 0 draws ran2 from its own stream (its own
 // saved generator state, so that it is the stream the replica would draw
 // alone) and, on a collision, momenta from sample_rpmd are copied in on the
-// batch stream.
+// batch stream.  Neither the draws nor the new momenta depend on the device
+// state, so the host does this work while the step it follows still runs:
+// the momenta go into a pinned staging buffer that is copied on the batch
+// stream behind that step, and a buffer is reused only once its copy is done
+// (an event per buffer).  No step waits for the host.
 //
 // Work runs on the batch stream: call gbrpmd_batch_sync before using a
 // replica's context directly (gbrpmd_ctx_sync, gbrpmd_ctx_download), and do
@@ -38,7 +42,7 @@ struct gb_batch {
     gb_context *c = nullptr;
     double dt = 0, beta = 0, thresh = 0;
     int irun = 0;
-    std::vector<double> hmass, hp;
+    std::vector<double> hmass;
     RngState rng;  // this replica's ran2 / gaussian state
     cudaEvent_t join = nullptr;
     int64_t launches = 0;  // this replica's kernels in the captured step
@@ -47,6 +51,14 @@ struct gb_batch {
   cudaStream_t s0 = nullptr;
   cudaEvent_t fork = nullptr;
   std::vector<Rep> reps;
+  // pinned staging buffers of resampled momenta, each free again once the
+  // copy recorded in its event has run
+  struct Stage {
+    double *h = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+  };
+  std::vector<Stage> stages;
   cudaGraphExec_t exec = nullptr;
   bool valid = false;
   int seen = 0;
@@ -82,14 +94,37 @@ int run_branches(gb_batch *b) {
   return GB_OK;
 }
 
+// a staging buffer of at least n doubles whose last copy has run
+int stage_for(gb_batch *b, size_t n, gb_batch::Stage **out) {
+  for (auto &st : b->stages) {
+    if (st.cap < n) continue;
+    const cudaError_t q = cudaEventQuery(st.done);
+    if (q == cudaSuccess) {
+      *out = &st;
+      return GB_OK;
+    }
+    if (q != cudaErrorNotReady) return ctx_check_cuda(q, "cudaEventQuery (batch staging)");
+  }
+  gb_batch::Stage st;
+  BCK(cudaHostAlloc((void **)&st.h, sizeof(double) * n, cudaHostAllocDefault));
+  st.cap = n;
+  BCK(cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming));
+  b->stages.push_back(st);
+  *out = &b->stages.back();
+  return GB_OK;
+}
+
 int andersen(gb_batch *b) {
   for (auto &r : b->reps) {
     if (!(r.thresh > 0.0)) continue;
     if (rng_ran2(r.rng, &r.irun, 0.0, 1.0) < r.thresh) {
-      r.hp.resize(3 * (size_t)r.c->na * r.c->nb);
-      rng_sample_rpmd(r.rng, r.hp.data(), r.c->na, r.c->nb, r.hmass.data(), r.beta, &r.irun);
-      BCK(cudaMemcpyAsync(r.c->p, r.hp.data(), sizeof(double) * r.hp.size(), cudaMemcpyHostToDevice, b->s0));
-      BCK(cudaStreamSynchronize(b->s0));  // hp is reused at the next collision
+      const size_t n = 3 * (size_t)r.c->na * r.c->nb;
+      gb_batch::Stage *st = nullptr;
+      int e = stage_for(b, n, &st);
+      if (e) return e;
+      rng_sample_rpmd(r.rng, st->h, r.c->na, r.c->nb, r.hmass.data(), r.beta, &r.irun);
+      BCK(cudaMemcpyAsync(r.c->p, st->h, sizeof(double) * n, cudaMemcpyHostToDevice, b->s0));
+      BCK(cudaEventRecord(st->done, b->s0));
     }
   }
   return GB_OK;
@@ -118,6 +153,10 @@ int gbrpmd_batch_destroy(gb_batch *b) {
   drop_graph(b);
   for (auto &r : b->reps)
     if (r.join) cudaEventDestroy(r.join);
+  for (auto &st : b->stages) {
+    cudaEventDestroy(st.done);
+    cudaFreeHost(st.h);
+  }
   cudaEventDestroy(b->fork);
   cudaStreamDestroy(b->s0);
   delete b;

@@ -20,6 +20,10 @@ struct PairList {
   int *idx = nullptr;    // [nconf][npt][cap]
   size_t bytes = 0;
   int i16 = 0;           // entries are unsigned short (npt <= 65535): idx is read as that type
+  // entries are cell-order slots of the last rebuild, bit 15 set for a pair of
+  // the same molecule (i16 lists of at most 32767 points; CellSort::fxs holds
+  // the positions in slot order)
+  int slots = 0;
 };
 
 // Which accumulator slots the last evaluation filled and with how many
@@ -39,6 +43,10 @@ struct CellSort {
   float4 *spos = nullptr;        // [nconf][npt]
   unsigned *ticket = nullptr;    // [2]: blocks done in the count kernel, a point moved
   size_t cell_bytes = 0, pt_bytes = 0;
+  // slot order (PairList::slots): each point's cell-order slot at the last
+  // rebuild and the fixed-point coordinates in that order, kept every step
+  int *slot_of = nullptr;        // [nconf][npt]
+  int4 *fxs = nullptr;           // [nconf][npt]
 };
 
 struct SkinList {
@@ -214,6 +222,7 @@ struct gb_context {
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_next = 0;
   int *d_count = nullptr;  // device scratch for pair counts (profiling only)
+  unsigned long long *d_npair = nullptr;  // in-cut pairs counted by the real-space kernel (profiling only)
   // watched kernel (gbrpmd_ctx_watch_region): events around one region's launch
   int watch = -1;
   cudaEvent_t watch_ev[2] = {nullptr, nullptr};

@@ -54,9 +54,11 @@ void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *fra
                        const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag,
                        int4 *fx = nullptr);
 // (also saves the reference positions and counts the rebuild, as launch_skin_save)
+// fx: the points' fixed-point coordinates (copied into cs.fxs in slot order
+// when the list stores slots)
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
                          unsigned *status, const unsigned *gate, const CellSort &cs, double *ref,
-                         unsigned *rebuilds);
+                         unsigned *rebuilds, const int4 *fx = nullptr);
 void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
                         const PairList &skin, PairList &pl, unsigned *status);
 double list_total(cudaStream_t s, const PairList &pl);  // profiling only (synchronises)
@@ -80,9 +82,12 @@ void launch_recip_force(cudaStream_t s, gb_context *c, const double *rs, const d
 // box: side lengths of the fractional coordinates (1, 1, 1 for the cubic sum);
 // np: lanes per site (8, 16, 32) / per oxygen (2, 4, 8)
 // add = false: g is overwritten (no zeroing pass needed)
-// fx: fixed-point fractional coordinates with the charge bits in w (frac_point)
-void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, int na, int B, const PairList &pl, double alpha,
-                          double rcutsq, const double *box, int np, double *g, double *acc, bool add = true);
+// fx: fixed-point fractional coordinates with the charge bits in w
+// (frac_point); fxs: the same in slot order (lists of slots, PairList::slots);
+// npair (profiling): in-cut entries counted
+void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, const int4 *fxs, int na, int B, const PairList &pl,
+                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc,
+                          bool add = true, unsigned long long *npair = nullptr);
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
                   double sigsq, double rcutsq, const double *box, double dscale, int np, double *out, double *acc);
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);

@@ -60,15 +60,20 @@ GB_D float dmin(float hi_a, float lo_a, float hi_b, float lo_b) {
 // bits ride in w.  Each lane takes every NP-th partner, four at a time with
 // their indices and positions loaded before any arithmetic, so that four
 // gathers are in flight per lane.  IT: the list entry type (unsigned short
-// for up to 65535 sites halves the list's bytes).
+// for up to 65535 sites halves the list's bytes).  SLOTS: the entries are
+// cell-order slots of the last list rebuild (bit 15: same molecule) and the
+// partners' positions come from fxs, the same coordinates in slot order, so
+// that consecutive entries of a list, mostly runs of the same cells, gather
+// from neighbouring addresses.  npair (profiling only): in-cut entries counted.
 // bx: side lengths that turn fractional differences into distances, times
 // 2^-32 (1 * 2^-32 in the unit box of the cubic sum; the box in bohr for the
 // non-cubic one, rwald_basic / rwald_cell of ewald_noncubic.f90)
-template <int NP, typename IT>
-__global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__ fx, int na,
-                                                        const int *__restrict__ count, const IT *__restrict__ idx,
-                                                        int cap, float alpha, float sfac, float rcutsq, float3 bx,
-                                                        double *g, double *acc, int add) {
+template <int NP, typename IT, bool SLOTS>
+__global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__ fx, const int4 *__restrict__ fxs,
+                                                        int na, const int *__restrict__ count,
+                                                        const IT *__restrict__ idx, int cap, float alpha, float sfac,
+                                                        float rcutsq, float3 bx, double *g, double *acc, int add,
+                                                        unsigned long long *npair) {
   __shared__ float sh[32 * 8];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
@@ -77,6 +82,8 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__
   const int i = (int)(tid / NP), sub = (int)(tid % NP);
   const bool active = i < na;
   const int4 *X = fx + (long long)c * na;
+  const int4 *XJ = SLOTS ? fxs + (long long)c * na : X;
+  int nin = 0;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   float ev = 0.f, evc = 0.f, vxx = 0.f, vyx = 0.f, vzx = 0.f, vyy = 0.f, vzy = 0.f, vzz = 0.f;
   if (active) {
@@ -85,18 +92,22 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__
     const int m3 = (i / 3) * 3;  // first site of i's molecule
     const int n = min(count[(long long)c * na + i], cap);
     const IT *L = idx + ((long long)c * na + i) * cap;
-    auto pair = [&](int j, const int4 &xj) {
+    // same molecule: bit 15 of a slot entry, else j within i's molecule
+    auto same = [&](int e) { return SLOTS ? (e & 0x8000) != 0 : (unsigned)(e - m3) < 3u; };
+    auto slot = [&](int e) { return SLOTS ? (e & 0x7fff) : e; };
+    auto pair = [&](int ent, const int4 &xj) {
       const float dx = (float)(int)((unsigned)xi.x - (unsigned)xj.x) * bx.x;
       const float dy = (float)(int)((unsigned)xi.y - (unsigned)xj.y) * bx.y;
       const float dz = (float)(int)((unsigned)xi.z - (unsigned)xj.z) * bx.z;
       const float drsq = dx * dx + dy * dy + dz * dz;
       if (!(drsq < rcutsq)) return;  // skin-list entry beyond the cut-off
+      if (npair) ++nin;
       const float inv = rsqrtf(drsq);
       const float x = alpha * (drsq * inv);
       const float e = expf(-x * x);
       const float tt = __fdividef(p, p + x);
       float erfc = e * tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5))));
-      if ((unsigned)(j - m3) < 3u) erfc -= 1.0f;  // same molecule
+      if (same(ent)) erfc -= 1.0f;  // same molecule
       const float du = erfc * inv;
       const float dur = (sfac * e - du) * (inv * inv);
       const float qij = qi * __int_as_float(xj.w);
@@ -115,17 +126,21 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__
     };
     int t = sub;
     for (; t + 3 * NP < n; t += 4 * NP) {
-      const int j0 = L[t], j1 = L[t + NP], j2 = L[t + 2 * NP], j3 = L[t + 3 * NP];
-      const int4 x0 = X[j0], x1 = X[j1], x2 = X[j2], x3 = X[j3];
-      pair(j0, x0);
-      pair(j1, x1);
-      pair(j2, x2);
-      pair(j3, x3);
+      const int e0 = L[t], e1 = L[t + NP], e2 = L[t + 2 * NP], e3 = L[t + 3 * NP];
+      const int4 x0 = XJ[slot(e0)], x1 = XJ[slot(e1)], x2 = XJ[slot(e2)], x3 = XJ[slot(e3)];
+      pair(e0, x0);
+      pair(e1, x1);
+      pair(e2, x2);
+      pair(e3, x3);
     }
     for (; t < n; t += NP) {
-      const int j = L[t];
-      pair(j, X[j]);
+      const int e = L[t];
+      pair(e, XJ[slot(e)]);
     }
+  }
+  if (npair) {  // one atomic per warp
+    const int tot = __reduce_add_sync(0xffffffffu, nin);
+    if ((threadIdx.x & 31) == 0 && tot) atomicAdd(npair, (unsigned long long)tot);
   }
   // each lane's compensated sum, then FP32 across the site's lanes
   const float fx0 = group_sum_f<NP>(sx - cx);
@@ -546,21 +561,25 @@ int sm_count_mx() {
 
 }  // namespace
 
-void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, int na, int B, const PairList &pl, double alpha,
-                          double rcutsq, const double *box, int np, double *g, double *acc, bool add) {
+void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, const int4 *fxs, int na, int B, const PairList &pl,
+                          double alpha, double rcutsq, const double *box, int np, double *g, double *acc, bool add,
+                          unsigned long long *npair) {
   const float two32 = 2.3283064365386963e-10f;  // 2^-32: fixed-point units to fractions
   const float3 bx = make_float3((float)box[0] * two32, (float)box[1] * two32, (float)box[2] * two32);
   auto go = [&](auto NPc) {
     constexpr int NP = decltype(NPc)::value;
     dim3 grid(nblk((long long)na * NP, MX_T), B);
     const float sfac = (float)(-2.0 * alpha / std::sqrt(std::acos(-1.0)));  // d erfc(alpha r) / dr factor
-    if (pl.i16)
-      k_ewald_real_mx<NP, unsigned short><<<grid, MX_T, 0, s>>>(
-          fx, na, pl.count, reinterpret_cast<const unsigned short *>(pl.idx), pl.cap, (float)alpha, sfac,
-          (float)rcutsq, bx, g, acc, add ? 1 : 0);
+    const unsigned short *i16 = reinterpret_cast<const unsigned short *>(pl.idx);
+    if (pl.slots)
+      k_ewald_real_mx<NP, unsigned short, true><<<grid, MX_T, 0, s>>>(
+          fx, fxs, na, pl.count, i16, pl.cap, (float)alpha, sfac, (float)rcutsq, bx, g, acc, add ? 1 : 0, npair);
+    else if (pl.i16)
+      k_ewald_real_mx<NP, unsigned short, false><<<grid, MX_T, 0, s>>>(
+          fx, fx, na, pl.count, i16, pl.cap, (float)alpha, sfac, (float)rcutsq, bx, g, acc, add ? 1 : 0, npair);
     else
-      k_ewald_real_mx<NP, int><<<grid, MX_T, 0, s>>>(fx, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
-                                                     (float)rcutsq, bx, g, acc, add ? 1 : 0);
+      k_ewald_real_mx<NP, int, false><<<grid, MX_T, 0, s>>>(fx, fx, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
+                                                            (float)rcutsq, bx, g, acc, add ? 1 : 0, npair);
   };
   if (np == 8) go(std::integral_constant<int, 8>());
   else if (np == 32) go(std::integral_constant<int, 32>());

@@ -191,6 +191,8 @@ struct CellSortDev {
   int *crank;      // [nconf][npt] rank in the cell (arbitrary order)
   float4 *spos;    // [nconf][npt] fractional positions in cell order
   int *sidx;       // [nconf][npt] point of each cell-order slot
+  int *slot_of;    // [nconf][npt] slot of each point at the last rebuild
+  int4 *fxs;       // [nconf][npt] fixed-point positions in slot order (null: not kept)
   unsigned *ticket;  // [0] blocks done in the count kernel, [1] a point moved
 };
 
@@ -217,6 +219,9 @@ __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float
       moved = !(dx * dx + dy * dy + dz * dz <= lim2);  // NaN counts as moved
     }
     const float4 f = frac_point(g, t, c, i, frac, lo, q, fx);
+    // slot-ordered copy under the last rebuild's order (a rebuild in this step
+    // rewrites it in k_cell_scatter)
+    if (cs.fxs) cs.fxs[(long long)c * g.npt + cs.slot_of[t]] = fx[t];
     const int cell = (cell_of(f.z, cs.nz) * cs.ny + cell_of(f.y, cs.ny)) * cs.nx + cell_of(f.x, cs.nx);
     cs.cellid[t] = cell;
     cs.crank[t] = atomicAdd(cs.ccount + (long long)c * ncell + cell, 1);
@@ -276,7 +281,7 @@ __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float
 // (also the skin-list bookkeeping of k_skin_save: reference positions and the
 // rebuild count)
 __global__ void k_cell_scatter(PairGeom g, int nconf, const float4 *frac, CellSortDev cs, int *lcount,
-                               const unsigned *gate, double *ref, unsigned *rebuilds) {
+                               const unsigned *gate, double *ref, unsigned *rebuilds, const int4 *fx) {
   if (*gate == 0u) return;
   const int npt = g.npt;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -292,10 +297,16 @@ __global__ void k_cell_scatter(PairGeom g, int nconf, const float4 *frac, CellSo
   const long long pos = (long long)c * npt + cs.cstart[(long long)c * (ncell + 1) + cs.cellid[t]] + cs.crank[t];
   cs.spos[pos] = frac[t];
   cs.sidx[pos] = i;
+  if (cs.fxs) {
+    cs.slot_of[t] = (int)(pos - (long long)c * npt);
+    cs.fxs[pos] = fx[t];
+  }
 }
 
 // IT: the list entry type (int, or unsigned short when npt <= 65535)
-template <bool FULL, bool EXCL, typename IT>
+// SLOTS: store the partner's cell-order slot, bit 15 set for the same
+// molecule (unsigned short entries, npt <= 32767), instead of its index
+template <bool FULL, bool EXCL, typename IT, bool SLOTS = false>
 __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, CellSortDev cs, int *count, IT *idx,
                                                        int cap, float3 len, float thr_lo, float thr_hi,
                                                        unsigned *status, const unsigned *gate) {
@@ -353,7 +364,7 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (hit) {
           const int pos = n + __popc(m & ((1u << lane) - 1u));
-          if (pos < cap) my[pos] = (IT)j;
+          if (pos < cap) my[pos] = SLOTS ? (IT)(k | ((i / 3) == (j / 3) ? 0x8000 : 0)) : (IT)j;
         }
         n += __popc(m);
       }
@@ -953,6 +964,8 @@ CellSortDev dev_cells(const CellSort &cs) {
   d.crank = cs.crank;
   d.spos = cs.spos;
   d.sidx = cs.sidx;
+  d.slot_of = cs.slot_of;
+  d.fxs = cs.fxs;
   d.ticket = cs.ticket;
   return d;
 }
@@ -968,19 +981,22 @@ void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *fra
 
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
                          unsigned *status, const unsigned *gate, const CellSort &cs, double *ref,
-                         unsigned *rebuilds) {
+                         unsigned *rebuilds, const int4 *fx) {
   float3 len;
   float thr_lo, thr_hi;
   list_thresholds(g, &len, &thr_lo, &thr_hi);
   CellSortDev d = dev_cells(cs);
   const long long n = (long long)nconf * g.npt;
-  k_cell_scatter<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, d, pl.count, gate, ref, rebuilds);
+  k_cell_scatter<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, d, pl.count, gate, ref, rebuilds, fx);
   auto go = [&](auto kern, auto *idx) {
     kern<<<nblk(32 * n, LB_T), LB_T, 0, s>>>(g, nconf, d, pl.count, idx, pl.cap, len, thr_lo, thr_hi, status,
                                              gate);
   };
   unsigned short *i16 = reinterpret_cast<unsigned short *>(pl.idx);
-  if (g.full) {
+  if (pl.slots) {  // never with exclusions
+    if (g.full) go(k_build_sorted<true, false, unsigned short, true>, i16);
+    else go(k_build_sorted<false, false, unsigned short, true>, i16);
+  } else if (g.full) {
     if (g.excl_mol) pl.i16 ? go(k_build_sorted<true, true, unsigned short>, i16) : go(k_build_sorted<true, true, int>, pl.idx);
     else pl.i16 ? go(k_build_sorted<true, false, unsigned short>, i16) : go(k_build_sorted<true, false, int>, pl.idx);
   } else {

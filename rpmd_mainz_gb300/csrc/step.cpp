@@ -243,10 +243,11 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     CellSort &cs = S.cells;
     cs.on = c->list_cells && list_cell_grid(gsc, cs.nc, &cs.R, cs.reach);
     S.pl.i16 = want16 && cs.on && g.npt <= 65535 ? 1 : 0;
+    S.pl.slots = S.pl.i16 && fx && !g.excl_mol && g.npt <= 32767 ? 1 : 0;
     if (cs.on) {
       const size_t ncell = (size_t)cs.nc[0] * cs.nc[1] * cs.nc[2];
       const size_t need_cell = sizeof(int) * (size_t)nconf * (2 * ncell + 1);  // counts, then offsets
-      const size_t need_pt = (3 * sizeof(int) + sizeof(float4)) * (size_t)nconf * g.npt;
+      const size_t need_pt = (4 * sizeof(int) + sizeof(float4) + sizeof(int4)) * (size_t)nconf * g.npt;
       if (need_cell > cs.cell_bytes) {
         if (cs.ccount) cudaFree(cs.ccount);
         cs.ccount = nullptr;
@@ -264,9 +265,16 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
       if (!cs.ticket) CK(cudaMalloc(&cs.ticket, 2 * sizeof(unsigned)));
       cs.cstart = cs.ccount + (size_t)nconf * ncell;
       const size_t np = (size_t)nconf * g.npt;
-      cs.cellid = reinterpret_cast<int *>(cs.spos + np);
+      int4 *fxs = reinterpret_cast<int4 *>(cs.spos + np);
+      cs.fxs = S.pl.slots ? fxs : nullptr;
+      cs.cellid = reinterpret_cast<int *>(fxs + np);
       cs.crank = cs.cellid + np;
       cs.sidx = cs.crank + np;
+      cs.slot_of = cs.sidx + np;
+      // slots of no rebuild yet: the first count writes every point to slot 0,
+      // in bounds, and the rebuild that always follows a reconfiguration
+      // rewrites them
+      CK(cudaMemsetAsync(cs.slot_of, 0, sizeof(int) * np, c->stream));
       CK(cudaMemsetAsync(cs.ccount, 0, need_cell, c->stream));
       CK(cudaMemsetAsync(cs.ticket, 0, 2 * sizeof(unsigned), c->stream));
     }
@@ -284,7 +292,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     if (e0 != cudaSuccess) return ctx_check_cuda(e0, "a launch before the cell count");
     launch_cell_count(c->stream, g, nconf, c->rs32, lo, q, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag, fx);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell count launch");
-    launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells, S.ref, S.rebuilds);
+    launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells, S.ref, S.rebuilds, fx);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell build launch");
   } else {
     if (same) {
@@ -298,7 +306,8 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   if (superset && use) {
     *use = &S.pl;
     // profiling counts in-cut pairs: the exact list is made for the count only
-    if (c->prof) launch_list_filter(c->stream, g, nconf, c->rs32, S.pl, c->pl, c->status);
+    // (a list of slots is counted by its consumer instead)
+    if (c->prof && !S.pl.slots) launch_list_filter(c->stream, g, nconf, c->rs32, S.pl, c->pl, c->status);
   } else {
     launch_list_filter(c->stream, g, nconf, c->rs32, S.pl, c->pl, c->status);
     n += 1;
@@ -385,12 +394,21 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   if (st) return st;
   prof_end(c, PR_LIST, (double)na * B);
   c->launches += nl;
-  // in-cut pairs, each once (profiling fills c->pl with the exact list)
-  const double npairs = c->prof ? list_total(c->stream, c->pl) * (mixed ? 0.5 : 1.0) : 0.0;
+  // in-cut pairs, each once (profiling fills c->pl with the exact list, or the
+  // real-space kernel counts the entries of a list of slots)
+  const bool count_in_kernel = c->prof && mixed && pl->slots;
+  double npairs = c->prof && !count_in_kernel ? list_total(c->stream, c->pl) * (mixed ? 0.5 : 1.0) : 0.0;
+  unsigned long long *npair_dev = nullptr;
+  if (count_in_kernel) {
+    if (!c->d_npair) CK(cudaMalloc(&c->d_npair, sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(c->d_npair, 0, sizeof(unsigned long long), c->stream));
+    npair_dev = c->d_npair;
+  }
+  const int4 *fxs = mixed && pl->slots ? c->sl[LIST_EW].cells.fxs : nullptr;
   const double ksites = (double)c->nk * na * B;
   if (branch) {
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 0))) return st0;
-    launch_ewald_real_mx(c->stream, c->fx32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
+    launch_ewald_real_mx(c->stream, c->fx32, fxs, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
                          c->tune.ew_np, c->g2, slot(c, s), false);
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 1))) return st0;
     join2.on = false;
@@ -403,10 +421,16 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
     recip_set_attributes_mx();
     prof_begin(c, PR_EW_REAL);
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 0))) return st0;
-    launch_ewald_real_mx(c->stream, c->fx32, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
-                         c->tune.ew_np, c->g, slot(c, s));
+    launch_ewald_real_mx(c->stream, c->fx32, fxs, na, B, *pl, c->P.walpha, c->P.wrcut * c->P.wrcut, g.box,
+                         c->tune.ew_np, c->g, slot(c, s), true, npair_dev);
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 1))) return st0;
     prof_end(c, PR_EW_REAL, npairs);
+    if (count_in_kernel) {  // profiling only: synchronises, after the region's end event
+      unsigned long long h = 0;
+      CK(cudaMemcpyAsync(&h, c->d_npair, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      if (!c->marks.empty()) c->marks.back().units = 0.5 * (double)h;
+    }
     prof_begin(c, PR_RECIP_SK);
     launch_recip_sk_mx(c->stream, c, c->rs, c->z, B);
     prof_end(c, PR_RECIP_SK, ksites);

@@ -281,10 +281,13 @@ def test_graph_replay_matches_plain_steps(precision):
     lib.init(prm)
     (a, ea, la), (b, eb, lb) = out
     # FP64: only the order of atomic additions differs; mixed: the pair-list
-    # order (atomic group appends) also reorders FP32 sums, at their rounding level
+    # order (atomic group appends) also reorders FP32 sums, at their rounding
+    # level, and 11 chaotic steps grow that; the forces (differences of large
+    # Coulomb terms) are compared at half the mixed path's 1e-5 force bound
     tol = 1e-12 if precision == 0 else 1e-6
-    for x, y in zip(a, b):
-        assert rel(x, y) < tol
+    ftol = 1e-12 if precision == 0 else 5e-6
+    for k, (x, y) in enumerate(zip(a, b)):
+        assert rel(x, y) < (tol if k < 2 else ftol), k
     for k in ("v", "vew", "vlj", "vint", "tv"):
         assert erel(eb[k], ea[k]) < 10 * tol
     assert la == lb
