@@ -208,6 +208,7 @@ struct gb_context {
     int mts_mpb = 0;  // molecules per block of the MTS kernel (0: one wave over the SMs)
     int rf_g = 8;     // column shares (warps) per block, FP32 k-space force kernel (8, 16)
     int rf_ns = 1;    // sites per lane, FP32 k-space force kernel (1, 2)
+    int rf_ks = 1;    // k-pair ranges (blocks per site tile), FP32 k-space force kernel (1..4)
     int done = 0;
   } tune;
 

@@ -17,6 +17,7 @@
 //    a chunk of sites and df over chunks; energy, virial and the k-space
 //    totals stay FP64.
 #include <cmath>
+#include <cstdlib>
 #include <type_traits>
 
 #include "gb_common.cuh"
@@ -413,6 +414,10 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
 // unrolled with a uniform branch per m, loads only the k-pair table entries
 // (shared-memory broadcasts) and is FMA-bound; KZ = 0 reads them from shared
 // memory in a plain loop.
+// gridDim.z splits the k pairs into that many ranges of whole columns (equal
+// k-pair counts), one per block of a site tile, so that the grid fills the SMs
+// in about even waves; each block stages only its range, and with more than
+// one range the blocks of a tile add their sums with FP64 atomics.
 template <bool STAGED, int MF_G, int NS, int KZ>
 __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__restrict__ tab, int na,
                                                                        int kmax, int ncol,
@@ -435,13 +440,7 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
   }
   const int tab_f4 = (K3 * BS + 1) / 2;                       // float4 slots of the site tables
   float2 *red = reinterpret_cast<float2 *>(smf + tab_f4);     // MF_G * BS * 3 df pairs
-  float4 *sT = smf + tab_f4 + (MF_G * BS * 3 + 1) / 2;        // [nkp][2]
-  if (STAGED) {
-    const float4 *src = sk + (long long)c * nkp * 2;
-    for (int w = t; w < 2 * nkp; w += 32 * MF_G) sT[w] = src[w];
-  }
-  const long long kp_lo = (long long)wg * nkp / MF_G;
-  const long long kp_hi = (long long)(wg + 1) * nkp / MF_G;
+  float4 *sT = smf + tab_f4 + (MF_G * BS * 3 + 1) / 2;        // [k pairs of the block][2]
   auto first_col = [&](long long kp) {
     int lo = 0, hi = ncol;
     while (lo < hi) {
@@ -451,9 +450,21 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
     }
     return lo;
   };
-  const int col0 = first_col(kp_lo), col1 = first_col(kp_hi);
+  // this block's whole columns and their k pairs [kb_lo, kb_hi)
+  const int KS = gridDim.z, ks = blockIdx.z;
+  const int bc0 = first_col((long long)ks * nkp / KS), bc1 = first_col((long long)(ks + 1) * nkp / KS);
+  const int kb_lo = bc0 < ncol ? __ldg(&cols[bc0].koff) : nkp;
+  const int kb_hi = bc1 < ncol ? __ldg(&cols[bc1].koff) : nkp;
+  if (STAGED) {
+    const float4 *src = sk + ((long long)c * nkp + kb_lo) * 2;
+    for (int w = t; w < 2 * (kb_hi - kb_lo); w += 32 * MF_G) sT[w] = src[w];
+  }
+  const long long kp_lo = kb_lo + (long long)wg * (kb_hi - kb_lo) / MF_G;
+  const long long kp_hi = kb_lo + (long long)(wg + 1) * (kb_hi - kb_lo) / MF_G;
+  const int col0 = max(first_col(kp_lo), bc0), col1 = min(first_col(kp_hi), bc1);
   __syncthreads();
-  const float4 *T = STAGED ? sT : sk + (long long)c * nkp * 2;
+  // k pair kp at T + 2 kp (staged: the block's range starts at sT)
+  const float4 *T = STAGED ? sT - 2LL * kb_lo : sk + (long long)c * nkp * 2;
   float2 zr[KZ > 0 ? KZ : 1][NS];
   if constexpr (KZ > 0) {
 #pragma unroll
@@ -546,7 +557,12 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
       const float2 r = red[(w * BS + s2) * 3 + d];
       df_add(H, L, r.x, r.y);
     }
-    if (i0 + s2 < na) g[((long long)c * na + i0 + s2) * 3 + d] += (d == 0 ? lat.x : d == 1 ? lat.y : lat.z) * df2d(H, L);
+    if (i0 + s2 < na) {
+      double *gd = g + ((long long)c * na + i0 + s2) * 3 + d;
+      const double v = (d == 0 ? lat.x : d == 1 ? lat.y : lat.z) * df2d(H, L);
+      if (KS > 1) atomicAdd(gd, v);
+      else *gd += v;
+    }
   }
 }
 
@@ -648,8 +664,12 @@ template <int G, int NS, int KZ>
 void force_launch(cudaStream_t s, gb_context *c, int B, double *g) {
   static_assert(G <= MF_GMAX, "column shares");
   const int kmax = c->P.kmax;
-  const size_t staged = recip_force_smem_mx(kmax, c->nkp, G, NS);
-  dim3 grid(nblk(c->na, MF_S * NS), B);
+  int ks = c->tune.rf_ks;
+  if (const char *e = std::getenv("GBRPMD_RF_KS")) ks = std::atoi(e);  // fixed k-pair ranges (measurements)
+  ks = std::max(1, std::min(ks, std::max(1, c->nkp / 64)));
+  // a block stages its share of the k pairs and at most one column more
+  const size_t staged = recip_force_smem_mx(kmax, (c->nkp + ks - 1) / ks + 2 * (kmax + 1) + 2, G, NS);
+  dim3 grid(nblk(c->na, MF_S * NS), B, ks);
   if (staged <= 160 * 1024)
     k_recip_force_mx<true, G, NS, KZ><<<grid, 32 * G, staged, s>>>(
         reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,

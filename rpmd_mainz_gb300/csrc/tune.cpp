@@ -248,6 +248,11 @@ int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double
         cand.tune.rf_ns = ns;
         probe(cand);
       }
+    for (int ks : {2, 3, 4, 6}) {
+      Shape cand = best;
+      cand.tune.rf_ks = ks;
+      probe(cand);
+    }
   }
   baseline(PR_MTS);
   for (int mpb : {4, 8, 14, 28}) {
