@@ -84,6 +84,7 @@ def load(path=None):
     lib.gbrpmd_ctx_set_list_skin.argtypes = [C.c_void_p, C.c_double]
     lib.gbrpmd_ctx_list_rebuilds.argtypes = [C.c_void_p, C.POINTER(C.c_uint)]
     lib.gbrpmd_ctx_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    lib.gbrpmd_bench_nm_transform.argtypes = [C.c_int, C.c_int, D]
     lib.gbrpmd_ctx_watch_region.argtypes = [C.c_void_p, C.c_int]
     lib.gbrpmd_ctx_watch_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     lib.gbrpmd_ctx_list_occupancy.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
@@ -435,6 +436,16 @@ class Context:
         out = (C.c_uint * 3)()
         _check(load().gbrpmd_ctx_list_rebuilds(self.h, out))
         return tuple(out)
+
+
+def bench_nm_transform(nrows, reps=6):
+    """Normal-mode transform of nrows rows of 32 beads: in-register FFT against
+    the tensor-core product (gbrpmd_bench_nm_transform)."""
+    out = np.zeros(8)
+    _check(load().gbrpmd_bench_nm_transform(int(nrows), int(reps), _ptr(out)))
+    keys = ("ms_per_transform_fft", "ms_per_transform_tensor", "roundtrip_rel_err_fft", "gain_per_roundtrip_fft",
+            "roundtrip_rel_err_tensor", "gain_per_roundtrip_tensor", "forward_rel_err_fft", "forward_rel_err_tensor")
+    return dict(zip(keys, out.tolist()))
 
 
 def ran2(idum: C.c_int, rmin=0.0, rmax=1.0):

@@ -14,8 +14,10 @@ from . import system
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PARAM_QSPCFW = os.path.join(os.path.dirname(HERE), "tests", "golden", "params", "param_qspcfw")
-# rigid 4-site TIP4P/2005 water (O-H 0.9572 A, HOH 104.52 deg, M-site 0.1546 A, qH 0.5897 e)
-PARAM_TIP05 = os.path.join(os.path.dirname(HERE), "tests", "golden", "params", "param_tip05_rigid")
+# rigid 4-site water of the served stream: O-H 0.9572 A, HOH 104.52 deg, M-site
+# 0.1546 A along the bisector, qH +0.5897 e, LJ sigma 3.1668 A, epsilon 0.21084
+# kcal/mol (TIP4P/Ice charges and LJ on the TIP4P/2005 geometry)
+PARAM_RIGID = os.path.join(HERE, "params", "param_tip4pice_msite01546_rigid")
 
 # CUB lattice cells per molecule count; 128 molecules need the anisotropic
 # 8 x 4 x 4 lattice (a non-cubic box, ewald_nc)
@@ -50,9 +52,9 @@ def request_stream(n=60, rate=50.0, seed=7, precision=1, sizes=(64, 216, 343, 51
                    beads=(4, 8, 16, 32, 64), nsteps=100, temp=298.0, rigid_fraction=0.5):
     """n trajectory requests with Poisson arrivals (mean `rate` per second):
     [(arrival_seconds, system, nsteps)], sizes and bead counts drawn per
-    request; a `rigid_fraction` of them are rigid TIP4P/2005 water (RATTLE,
-    at most 1666 molecules as the reference's bond table allows), the rest
-    flexible q-SPC/Fw."""
+    request; a `rigid_fraction` of them are rigid 4-site water (PARAM_RIGID,
+    RATTLE, at most 1666 molecules as the reference's bond table allows), the
+    rest flexible q-SPC/Fw."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
@@ -62,5 +64,5 @@ def request_stream(n=60, rate=50.0, seed=7, precision=1, sizes=(64, 216, 343, 51
         nb = int(rng.choice(beads))
         rigid = bool(rng.random() < rigid_fraction) and nm <= 1666
         out.append((t, _box(nm, nb, temp, precision, seed=100000 + 1000 * seed + i,
-                            param=PARAM_TIP05 if rigid else PARAM_QSPCFW), nsteps))
+                            param=PARAM_RIGID if rigid else PARAM_QSPCFW), nsteps))
     return out
