@@ -351,14 +351,16 @@ int gbrpmd_ctx_set_profiling(gb_context *ctx, int on);
 int gbrpmd_ctx_region_times(gb_context *ctx, double *ms, double *units, int *counts, int nregion);
 /* Measurement (no counterpart in the reference): the normal-mode transform of
    nrows rows of 32 beads (realft, fourier.f90:16-63, scaled by 1/sqrt(32)),
-   timed as the propagator runs it (lane-pair real FFT in FP32 registers with
-   split twiddles) and as a dense product on the tensor cores (mma.sync TF32,
+   timed as real FFTs in FP32 registers with split twiddles (two lanes per
+   row, and four) and as a dense product on the tensor cores (mma.sync TF32,
    rows split in two terms, transform matrices in three), reps forward +
-   inverse round trips per row between one load and one store.  out8: ms per
-   transform (FFT, tensor cores), round-trip relative error (FFT) and mean gain
-   per round trip, the same for the tensor cores, forward relative error
-   against an FP64 direct sum (FFT, tensor cores).  Allocates and synchronises. */
-int gbrpmd_bench_nm_transform(int nrows, int reps, double *out8);
+   inverse round trips per row between one load and one store.  out12: ms per
+   transform (lane-pair FFT, tensor cores), round-trip relative error (pair
+   FFT) and mean gain per round trip, the same for the tensor cores, forward
+   relative error against an FP64 direct sum (pair FFT, tensor cores); then ms
+   per transform, round-trip error, gain and forward error of the lane-quad
+   FFT.  Allocates and synchronises. */
+int gbrpmd_bench_nm_transform(int nrows, int reps, double *out12);
 /* Watched kernel (no counterpart in the reference): a pair of timing events
    around the launch of one region's kernel (0 multiple-time-step block,
    2 real-space Ewald, 5 k-space forces, 6 Lennard-Jones; -1 stops watching),

@@ -400,3 +400,162 @@ GB_D void gb_hc2r_pair(int q, In in, Out out, const float *__restrict__ twm, con
   }
   gb_hc2r_s<M, float, SPLIT>([&](int k) { return z[k]; }, out, twm, twm, twm_l, twm_l);
 }
+
+// Lane-quad forms for N = 32 (Q = 8 beads per lane), FP32: four adjacent lanes
+// (q = lane & 3) share a row.  Lane q holds the beads j = 4i + q (i < 8) and
+// eight half-complex elements, gb_quad_hc(q, e): lane p = 1, 2, 3 the complex
+// values X_p, X_{8-p}, X_{8+p}, X_{16-p} (each as Re, Im), lane 0 X_0, X_16
+// (real), X_8, X_4 and X_12.  Every lane of the warp must call.
+//
+// Forward: each lane takes the unscaled 8-point R2HC of its beads (Y_q); the
+// lanes exchange the values Y_q[r] each needs (three shuffle rounds of two
+// values), and lane p forms, with B_q = w^{q p} Y_q[p] (w = exp(-2 pi i / 32)),
+// the 4-point DFT F_m = sum_q B_q (-i)^{q m}: X_p = F_0, X_{8+p} = F_1,
+// X_{16-p} = conj F_2, X_{8-p} = conj F_3 (X_{r + 8m} = sum_q w^{q r}
+// (-i)^{q m} Y_q[r]); lane 0 does the same for r = 0 and r = 4.
+// Inverse: lane p forms G_s = sum_m F_m i^{s m} and Z_s[p] = w^{-s p} G_s for
+// each lane s, the lanes exchange them back, and lane s takes the unscaled
+// 8-point HC2R of Z_s into its beads (x_{4i+s} = sum_r Z_s[r] e^{2 pi i i r/8}).
+// Tables (float): tw8 / tw8_l: cos, sin of 2 pi m / 8 (hi, lo); twf8 / twf8_l:
+// half of those; twi / twi_l: sc cos, sc sin of 2 pi m / 32 (sc = 1/sqrt(32)).
+GB_HD int gb_quad_hc(int q, int e) {
+  if (q == 0) {
+    const int h0[8] = {0, 16, 8, 24, 4, 28, 12, 20};
+    return h0[e];
+  }
+  const int hp[8] = {q, 32 - q, 8 - q, 24 + q, 8 + q, 24 - q, 16 - q, 16 + q};
+  return hp[e];
+}
+
+template <bool SPLIT>
+GB_D void gb_quad_cmul(const float *twi, const float *twi_l, int m, bool conj, float ar, float ai, float &br,
+                       float &bi) {
+  // (c -+ i s)(ar + i ai) with c, s = sc cos, sc sin of 2 pi m / 32
+  const float cr = gb_tmul<SPLIT, float>(twi, twi_l, m, ar), ci = gb_tmul<SPLIT, float>(twi, twi_l, m, ai);
+  const float sr = gb_tmul<SPLIT, float>(twi, twi_l, 32 + m, ar), si = gb_tmul<SPLIT, float>(twi, twi_l, 32 + m, ai);
+  br = conj ? cr - si : cr + si;
+  bi = conj ? ci + sr : ci - sr;
+}
+
+// z * (-i)^s (rot = s & 3): 0: z, 1: (zi, -zr), 2: -z, 3: (-zi, zr)
+GB_D void gb_rot_mi(int s, float zr, float zi, float &outr, float &outi) {
+  const int k = s & 3;
+  outr = k == 0 ? zr : k == 1 ? zi : k == 2 ? -zr : -zi;
+  outi = k == 0 ? zi : k == 1 ? -zr : k == 2 ? -zi : zr;
+}
+
+template <bool SPLIT, class In, class Out>
+GB_D void gb_r2hc_quad32(int q, In in, Out out, const float *__restrict__ tw8, const float *__restrict__ twf8,
+                         const float *__restrict__ twi, const float *__restrict__ tw8_l = nullptr,
+                         const float *__restrict__ twf8_l = nullptr, const float *__restrict__ twi_l = nullptr) {
+  float y[8];
+  gb_r2hc_s<8, float, SPLIT>(in, [&](int k, float v) { y[k] = v; }, tw8, twf8, tw8_l, twf8_l);
+  // the pair a lane sends to lane d: d = 0: (Y[0], Y[4]); d > 0: (Re Y[d], Im Y[d]) = (y[d], y[8 - d])
+  auto pick0 = [&](int d) { return d == 0 ? y[0] : d == 1 ? y[1] : d == 2 ? y[2] : y[3]; };
+  auto pick1 = [&](int d) { return d == 0 ? y[4] : d == 1 ? y[7] : d == 2 ? y[6] : y[5]; };
+  // F_0..F_3 of the lane's group (r = q; lane 0: r = 0 with real inputs), and
+  // lane 0's second group (r = 4): G_0, G_1
+  float f0r = 0.f, f0i = 0.f, f1r = 0.f, f1i = 0.f, f2r = 0.f, f2i = 0.f, f3r = 0.f, f3i = 0.f;
+  float g0r = 0.f, g0i = 0.f, g1r = 0.f, g1i = 0.f;
+#pragma unroll
+  for (int x = 0; x < 4; ++x) {
+    const int src = q ^ x;
+    float ar = pick0(src), ai = pick1(src);
+    if (x) {
+      ar = __shfl_xor_sync(0xffffffffu, ar, x);
+      ai = __shfl_xor_sync(0xffffffffu, ai, x);
+    }
+    // B = w^{src q} A (lane 0: A = Y_src[0], real)
+    float br, bi;
+    gb_quad_cmul<SPLIT>(twi, twi_l, (src * q) & 31, false, ar, q ? ai : 0.f, br, bi);
+    float tr, ti;
+    f0r += br, f0i += bi;
+    gb_rot_mi(src, br, bi, tr, ti);  // (-i)^src B
+    f1r += tr, f1i += ti;
+    gb_rot_mi(2 * src, br, bi, tr, ti);  // (-1)^src B
+    f2r += tr, f2i += ti;
+    gb_rot_mi(3 * src, br, bi, tr, ti);  // i^src B
+    f3r += tr, f3i += ti;
+    // lane 0, r = 4: B = w^{4 src} Y_src[4]
+    gb_quad_cmul<SPLIT>(twi, twi_l, (4 * src) & 31, false, ai, 0.f, br, bi);
+    g0r += br, g0i += bi;
+    gb_rot_mi(src, br, bi, tr, ti);
+    g1r += tr, g1i += ti;
+  }
+  if (q) {
+    out(0, f0r), out(1, f0i);   // X_p
+    out(2, f3r), out(3, -f3i);  // X_{8-p} = conj F_3
+    out(4, f1r), out(5, f1i);   // X_{8+p}
+    out(6, f2r), out(7, -f2i);  // X_{16-p} = conj F_2
+  } else {
+    out(0, f0r), out(1, f2r);   // X_0, X_16
+    out(2, f1r), out(3, f1i);   // X_8
+    out(4, g0r), out(5, g0i);   // X_4
+    out(6, g1r), out(7, g1i);   // X_12
+  }
+}
+
+template <bool SPLIT, class In, class Out>
+GB_D void gb_hc2r_quad32(int q, In in, Out out, const float *__restrict__ tw8, const float *__restrict__ twi,
+                         const float *__restrict__ tw8_l = nullptr, const float *__restrict__ twi_l = nullptr) {
+  float e[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) e[k] = in(k);
+  // F_m of the lane's group: general X_{r+8m}; lane 0, r = 0: (X_0, X_8, X_16, conj X_8)
+  float f0r, f0i, f1r, f1i, f2r, f2i, f3r, f3i;
+  if (q) {
+    f0r = e[0], f0i = e[1];
+    f1r = e[4], f1i = e[5];
+    f2r = e[6], f2i = -e[7];
+    f3r = e[2], f3i = -e[3];
+  } else {
+    f0r = e[0], f0i = 0.f;
+    f1r = e[2], f1i = e[3];
+    f2r = e[1], f2i = 0.f;
+    f3r = e[2], f3i = -e[3];
+  }
+  // lane 0, r = 4: (X_4, X_12, conj X_12, conj X_4)
+  const float h0r = e[4], h0i = e[5], h1r = e[6], h1i = e[7];
+  float z[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) z[k] = 0.f;
+#pragma unroll
+  for (int x = 0; x < 4; ++x) {
+    const int s = q ^ x;  // destination lane of this round's values
+    // G_s = F_0 + i^s F_1 + (-1)^s F_2 + (-i)^s F_3
+    float t1r, t1i, t2r, t2i, t3r, t3i;
+    gb_rot_mi(3 * s, f1r, f1i, t1r, t1i);
+    gb_rot_mi(2 * s, f2r, f2i, t2r, t2i);
+    gb_rot_mi(s, f3r, f3i, t3r, t3i);
+    const float gr = f0r + t1r + t2r + t3r, gi = f0i + t1i + t2i + t3i;
+    float zr, zi;  // Z_s[q] = w^{-s q} G_s (lane 0: Z_s[0] = sc G_s, real)
+    gb_quad_cmul<SPLIT>(twi, twi_l, (s * q) & 31, true, gr, gi, zr, zi);
+    // lane 0, r = 4: G'_s = X_4 + i^s X_12 + (-1)^s conj X_12 + (-i)^s conj X_4; Z_s[4] = Re w^{-4s} G'_s
+    gb_rot_mi(3 * s, h1r, h1i, t1r, t1i);
+    gb_rot_mi(2 * s, h1r, -h1i, t2r, t2i);
+    gb_rot_mi(s, h0r, -h0i, t3r, t3i);
+    float z4r, z4i;
+    gb_quad_cmul<SPLIT>(twi, twi_l, (4 * s) & 31, true, h0r + t1r + t2r + t3r, h0i + t1i + t2i + t3i, z4r, z4i);
+    float v0 = q ? zr : zr, v1 = q ? zi : z4r;  // the pair for lane s
+    if (x) {
+      v0 = __shfl_xor_sync(0xffffffffu, v0, x);
+      v1 = __shfl_xor_sync(0xffffffffu, v1, x);
+    }
+    // from lane src = q ^ x: src > 0: (Re Z_q[src], Im Z_q[src]) -> z[src], z[8 - src];
+    // src = 0: (Z_q[0], Z_q[4]) -> z[0], z[4]
+    const int src = q ^ x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (src == k) {
+        if (k == 0) {
+          z[0] = v0;
+          z[4] = v1;
+        } else {
+          z[k] = v0;
+          z[8 - k] = v1;
+        }
+      }
+    }
+  }
+  gb_hc2r_s<8, float, SPLIT>([&](int k) { return z[k]; }, out, tw8, tw8, tw8_l, tw8_l);
+}

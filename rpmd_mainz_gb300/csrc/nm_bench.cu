@@ -97,6 +97,43 @@ __global__ void k_nm_fft_fwd(const float *in, float *out, int nrows, const float
                          twm, twfm, twi, twm_l, twfm_l, twi_l);
 }
 
+// ---- the in-register lane-quad FFT (four lanes per row, nb = 32) ----
+// tabs4: tw8, tw8_l, twf8, twf8_l (16 each), twi, twi_l (64 each)
+__global__ void __launch_bounds__(256) k_nm_fft4(const float *in, float *out, int nrows, int reps,
+                                                 const float *tabs4, int fwd_only) {
+  __shared__ float s_tab[4 * 16 + 2 * 64];
+  for (int i = threadIdx.x; i < 4 * 16 + 2 * 64; i += blockDim.x) s_tab[i] = tabs4[i];
+  __syncthreads();
+  const float *tw8 = s_tab, *tw8_l = s_tab + 16, *twf8 = s_tab + 32, *twf8_l = s_tab + 48;
+  const float *twi = s_tab + 64, *twi_l = s_tab + 128;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = (int)(t & 3);
+  const long long row = t >> 2;
+  const bool valid = row < nrows;
+  const long long rr = valid ? row : nrows - 1;
+  float x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = in[rr * NB + 4 * i + q];
+  if (fwd_only) {
+    gb_r2hc_quad32<true>(q, [&](int i) { return x[i]; },
+                         [&](int e, float v) {
+                           if (valid) out[row * NB + gb_quad_hc(q, e)] = v;
+                         },
+                         tw8, twf8, twi, tw8_l, twf8_l, twi_l);
+    return;
+  }
+  for (int r = 0; r < reps; ++r) {
+    float y[8];
+    gb_r2hc_quad32<true>(q, [&](int i) { return x[i]; }, [&](int e, float v) { y[e] = v; }, tw8, twf8, twi, tw8_l,
+                         twf8_l, twi_l);
+    gb_hc2r_quad32<true>(q, [&](int e) { return y[e]; }, [&](int i, float v) { x[i] = v; }, tw8, twi, tw8_l, twi_l);
+  }
+  if (valid) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[row * NB + 4 * i + q] = x[i];
+  }
+}
+
 // ---- the tensor-core product ----
 GB_D unsigned to_tf32(float x) {
   unsigned r;
@@ -206,8 +243,8 @@ int perm(int a) { return a < 4 ? 2 * a : 2 * (a - 4) + 1; }
 
 }  // namespace
 
-extern "C" int gbrpmd_bench_nm_transform(int nrows, int reps, double *out8) {
-  if (nrows < 16 || reps < 1 || !out8) return ctx_set_error(GB_E_ARG, "nm transform bench: nrows >= 16, reps >= 1");
+extern "C" int gbrpmd_bench_nm_transform(int nrows, int reps, double *out12) {
+  if (nrows < 16 || reps < 1 || !out12) return ctx_set_error(GB_E_ARG, "nm transform bench: nrows >= 16, reps >= 1");
   const double PI = 3.141592653589793238462643383279502884;
   const double sc = std::sqrt(1.0 / NB);
   // FFT tables as the propagator's pair kernel holds them
@@ -229,6 +266,22 @@ extern "C" int gbrpmd_bench_nm_transform(int nrows, int reps, double *out8) {
     tabs[8 * M + i] = h, tabs[8 * M + 2 * NB + i] = l;
     split(sc * std::sin(2.0 * PI * i / NB), h, l);
     tabs[8 * M + NB + i] = h, tabs[8 * M + 3 * NB + i] = l;
+  }
+  // the quad form's tables: length 8 (hi, lo, halves) and length 32 scaled
+  std::vector<float> tabs4(4 * 16 + 2 * 64);
+  for (int i = 0; i < 8; ++i) {
+    float h, l;
+    split(std::cos(2.0 * PI * i / 8), h, l);
+    tabs4[i] = h, tabs4[16 + i] = l, tabs4[32 + i] = 0.5f * h, tabs4[48 + i] = 0.5f * l;
+    split(std::sin(2.0 * PI * i / 8), h, l);
+    tabs4[8 + i] = h, tabs4[24 + i] = l, tabs4[40 + i] = 0.5f * h, tabs4[56 + i] = 0.5f * l;
+  }
+  for (int i = 0; i < NB; ++i) {
+    float h, l;
+    split(sc * std::cos(2.0 * PI * i / NB), h, l);
+    tabs4[64 + i] = h, tabs4[128 + i] = l;
+    split(sc * std::sin(2.0 * PI * i / NB), h, l);
+    tabs4[64 + NB + i] = h, tabs4[128 + NB + i] = l;
   }
   // dense matrices: Y = X Tf (R2HC order, scaled), X = Y Ti (HC2R, scaled)
   std::vector<double> Tf(NB * NB), Ti(NB * NB);
@@ -274,12 +327,12 @@ extern "C" int gbrpmd_bench_nm_transform(int nrows, int reps, double *out8) {
     st = st * 6364136223846793005ull + 1442695040888963407ull;
     hx[i] = (float)(((double)(st >> 11) / 9007199254740992.0 - 0.5) * 4.0);
   }
-  float *dx = nullptr, *dy = nullptr, *dtab = nullptr;
+  float *dx = nullptr, *dy = nullptr, *dtab = nullptr, *dtab4 = nullptr;
   uint2 *dfr = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int rc = GB_OK;
   auto done = [&]() {
-    cudaFree(dx), cudaFree(dy), cudaFree(dtab), cudaFree(dfr);
+    cudaFree(dx), cudaFree(dy), cudaFree(dtab), cudaFree(dfr), cudaFree(dtab4);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
   };
@@ -289,11 +342,12 @@ extern "C" int gbrpmd_bench_nm_transform(int nrows, int reps, double *out8) {
   };
   cudaError_t e;
   if ((e = cudaMalloc(&dx, n * 4)) || (e = cudaMalloc(&dy, n * 4)) || (e = cudaMalloc(&dtab, tabs.size() * 4)) ||
-      (e = cudaMalloc(&dfr, fr.size() * 4)))
+      (e = cudaMalloc(&dfr, fr.size() * 4)) || (e = cudaMalloc(&dtab4, tabs4.size() * 4)))
     return fail(e, "cudaMalloc (nm bench)");
   if ((e = cudaMemcpy(dx, hx.data(), n * 4, cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(dtab, tabs.data(), tabs.size() * 4, cudaMemcpyHostToDevice)) ||
-      (e = cudaMemcpy(dfr, fr.data(), fr.size() * 4, cudaMemcpyHostToDevice)) || (e = cudaEventCreate(&e0)) ||
+      (e = cudaMemcpy(dfr, fr.data(), fr.size() * 4, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(dtab4, tabs4.data(), tabs4.size() * 4, cudaMemcpyHostToDevice)) || (e = cudaEventCreate(&e0)) ||
       (e = cudaEventCreate(&e1)))
     return fail(e, "set-up (nm bench)");
   const size_t smem = sizeof(uint2) * 2 * PER;
@@ -302,19 +356,22 @@ extern "C" int gbrpmd_bench_nm_transform(int nrows, int reps, double *out8) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const unsigned gfft = (unsigned)((2LL * nrows + 255) / 256);
+  const unsigned gfft4 = (unsigned)((4LL * nrows + 255) / 256);
   const long long ntile = (nrows + 15) / 16;
   const unsigned gmma = (unsigned)std::min<long long>((ntile + 7) / 8, 8LL * nsm);
   std::vector<float> hy(n);
   auto timed = [&](int which, float *ms) -> cudaError_t {
     for (int w = 0; w < 3; ++w) {  // warm-up, then the best of three
       if (which == 0) k_nm_fft<<<gfft, 256>>>(dx, dy, nrows, reps, dtab);
-      else k_nm_mma<<<gmma, 256, smem>>>(dx, dy, nrows, reps, dfr, 0);
+      else if (which == 1) k_nm_mma<<<gmma, 256, smem>>>(dx, dy, nrows, reps, dfr, 0);
+      else k_nm_fft4<<<gfft4, 256>>>(dx, dy, nrows, reps, dtab4, 0);
     }
     float best = 1e30f;
     for (int k = 0; k < 3; ++k) {
       cudaEventRecord(e0);
       if (which == 0) k_nm_fft<<<gfft, 256>>>(dx, dy, nrows, reps, dtab);
-      else k_nm_mma<<<gmma, 256, smem>>>(dx, dy, nrows, reps, dfr, 0);
+      else if (which == 1) k_nm_mma<<<gmma, 256, smem>>>(dx, dy, nrows, reps, dfr, 0);
+      else k_nm_fft4<<<gfft4, 256>>>(dx, dy, nrows, reps, dtab4, 0);
       cudaEventRecord(e1);
       cudaError_t q = cudaEventSynchronize(e1);
       if (q != cudaSuccess) return q;
@@ -364,15 +421,25 @@ extern "C" int gbrpmd_bench_nm_transform(int nrows, int reps, double *out8) {
   k_nm_mma<<<gmma, 256, smem>>>(dx, dy, nrows, 1, dfr, 1);
   if ((e = cudaDeviceSynchronize())) return fail(e, "tensor-core forward (nm bench)");
   const double ferr_mma = fwd_err();
+  float ms_q = 0.f;
+  double err_q, gain_q;
+  if ((e = timed(2, &ms_q)) || (e = trip(&err_q, &gain_q))) return fail(e, "lane-quad transforms (nm bench)");
+  k_nm_fft4<<<gfft4, 256>>>(dx, dy, nrows, 1, dtab4, 1);
+  if ((e = cudaDeviceSynchronize())) return fail(e, "lane-quad forward (nm bench)");
+  const double ferr_q = fwd_err();
   // per transform (2 reps transforms per row)
-  out8[0] = ms_fft / (2.0 * reps);
-  out8[1] = ms_mma / (2.0 * reps);
-  out8[2] = err_fft;
-  out8[3] = gain_fft;
-  out8[4] = err_mma;
-  out8[5] = gain_mma;
-  out8[6] = ferr_fft;
-  out8[7] = ferr_mma;
+  out12[0] = ms_fft / (2.0 * reps);
+  out12[1] = ms_mma / (2.0 * reps);
+  out12[2] = err_fft;
+  out12[3] = gain_fft;
+  out12[4] = err_mma;
+  out12[5] = gain_mma;
+  out12[6] = ferr_fft;
+  out12[7] = ferr_mma;
+  out12[8] = ms_q / (2.0 * reps);
+  out12[9] = err_q;
+  out12[10] = gain_q;
+  out12[11] = ferr_q;
   done();
   return rc;
 }

@@ -441,10 +441,12 @@ class Context:
 def bench_nm_transform(nrows, reps=6):
     """Normal-mode transform of nrows rows of 32 beads: in-register FFT against
     the tensor-core product (gbrpmd_bench_nm_transform)."""
-    out = np.zeros(8)
+    out = np.zeros(12)
     _check(load().gbrpmd_bench_nm_transform(int(nrows), int(reps), _ptr(out)))
     keys = ("ms_per_transform_fft", "ms_per_transform_tensor", "roundtrip_rel_err_fft", "gain_per_roundtrip_fft",
-            "roundtrip_rel_err_tensor", "gain_per_roundtrip_tensor", "forward_rel_err_fft", "forward_rel_err_tensor")
+            "roundtrip_rel_err_tensor", "gain_per_roundtrip_tensor", "forward_rel_err_fft", "forward_rel_err_tensor",
+            "ms_per_transform_fft_quad", "roundtrip_rel_err_fft_quad", "gain_per_roundtrip_fft_quad",
+            "forward_rel_err_fft_quad")
     return dict(zip(keys, out.tolist()))
 
 

@@ -30,3 +30,6 @@ def test_nm_transform_forms():
     assert abs(out["gain_per_roundtrip_fft"]) < 1e-9
     assert out["roundtrip_rel_err_fft"] < 1e-6
     assert out["roundtrip_rel_err_tensor"] < 1e-5
+    assert out["forward_rel_err_fft_quad"] < 1e-6
+    assert abs(out["gain_per_roundtrip_fft_quad"]) < 1e-9
+    assert out["roundtrip_rel_err_fft_quad"] < 1e-6
