@@ -91,6 +91,10 @@ void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, const int4 *fxs, int n
 void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, int B, const PairList &pl,
                   double sigsq, double rcutsq, const double *box, double dscale, int np, double *out, double *acc);
 void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const double *q, int B);
+// the same structure-factor chunk partials on the tensor cores (k_recip_tc.cu);
+// false (nothing launched) when kmax is beyond its tiles
+bool launch_recip_sk_tc(cudaStream_t s, gb_context *c, int B, int nchunk);
+int recip_sk_tc_chunk();
 void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc);
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g);
 void recip_set_attributes_mx();

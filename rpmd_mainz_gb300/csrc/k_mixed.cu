@@ -635,6 +635,11 @@ void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const d
   k_recip_tables_mx<<<nblk(nw * (kmax + 1), 256), 256, 0, s>>>(rs, q, c->na, B, kmax,
                                                                make_double3(lat.x * ot, lat.y * ot, lat.z * ot), tab);
   const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
+  // GBRPMD_SK_TC=1 puts the structure factors on the tensor cores (k_recip_tc.cu;
+  // kmax < 16): measured at 4096 H2O, nb = 32 it takes 24-34 us per launch
+  // against 17 us for the CUDA-core kernel below, so it is not the default
+  const char *tc = std::getenv("GBRPMD_SK_TC");
+  if (tc && tc[0] == '1' && recip_sk_tc_chunk() == MSK_CHUNK && launch_recip_sk_tc(s, c, B, nchunk)) return;
   static_assert(MSK_G % MSK_SP == 0, "work item split");
   dim3 grid(nblk((long long)c->ngrp * MSK_SP, MSK_T), nchunk, B);
   k_recip_sk_mx<MSK_SP><<<grid, MSK_T, recip_sk_smem_mx(kmax), s>>>(tab, c->na, kmax, c->ngrp, c->kgrp, c->nkp,

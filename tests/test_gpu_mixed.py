@@ -131,3 +131,20 @@ def test_mixed_coordinate_just_below_box_edge():
     f64, fmx = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
     assert rel(fmx["dvdr"], f64["dvdr"]) < FORCE_TOL
     assert rel(fmx["dvdr"] + fmx["dvdr2"], f64["dvdr"] + f64["dvdr2"]) < FORCE_TOL
+
+
+def test_mixed_structure_factors_on_tensor_cores(monkeypatch):
+    """GBRPMD_SK_TC=1: the k-space structure factors as split-TF32 mma.sync
+    products (k_recip_tc.cu) keep the mixed path's force and energy bounds and
+    agree with the CUDA-core structure factors."""
+    s = systems.build(param="param_qspcfw", ncell=(6, 6, 6), nb=8)
+    r = systems.perturbed(s, seed=131)
+    f64, fcc = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
+    monkeypatch.setenv("GBRPMD_SK_TC", "1")
+    _, ftc = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
+    monkeypatch.delenv("GBRPMD_SK_TC")
+    assert rel(ftc["dvdr"], f64["dvdr"]) < FORCE_TOL
+    assert rel(ftc["dvdr"], fcc["dvdr"]) < FORCE_TOL
+    for k in ("v", "vew"):
+        assert abs(ftc[k] - f64[k]) <= ENERGY_TOL * abs(f64[k]) + 1e-12, (k, ftc[k], f64[k])
+    assert rel(ftc["vir"], f64["vir"]) < VIRIAL_TOL
