@@ -330,6 +330,8 @@ def measure(args, s, prec, torch, world, local):
     # the dominant kernel region of the profiled pass is watched in the timed
     # steps: timing events around its launch, captured into the step graph
     dom = max((k for k in regions if k in WATCHABLE), key=lambda k: regions[k]["ms"])
+    if args.watch != "auto" and args.watch in regions:
+        dom = args.watch
     ctx.watch(dom)
     ctx.evolve(2, s["dt"], s["beta"])  # capture the graph with the watch events
     ctx.sync()
@@ -792,6 +794,8 @@ def main():
     ap.add_argument("--no-fp64-arm", action="store_true", help="skip the plain-FP64 comparison arm")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of tuned ones")
     ap.add_argument("--no-parity", action="store_true", help="skip the one-step oracle parity check")
+    ap.add_argument("--watch", default="auto", choices=("auto",) + WATCHABLE,
+                    help="kernel region timed inside the timed steps (auto: the largest of the profiled pass)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

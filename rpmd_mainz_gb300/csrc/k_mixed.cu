@@ -2,13 +2,15 @@
 //
 // Same pair sets and formulas as the FP64 kernels (k_pairs.cu, k_recip.cu),
 // with the per-pair and per-(k, site) arithmetic in FP32:
-//  * positions enter as two FP32 numbers per wrapped fractional coordinate
+//  * LJ positions enter as two FP32 numbers per wrapped fractional coordinate
 //    (hi + lo, k_frac32), so a minimum-image displacement
 //    (hi_i - hi_j - rint(hi_i - hi_j)) + (lo_i - lo_j) keeps ~1e-14 of the box;
+//    real-space Ewald positions as 32-bit fixed-point fractions (frac_point);
 //  * pair kernels walk full lists (each pair from both ends), so every point's
 //    force is summed by its own lanes and no atomics are needed; the
 //    real-space kernel walks the skin list itself and drops pairs beyond the
-//    cut-off with its FP32 distance (no per-step exact filter);
+//    cut-off with its FP32 distance (no per-step exact filter), two entries at
+//    a time in paired FP32 arithmetic (FFMA2 / FADD2 / FMUL2);
 //  * force and energy sums are compensated (Kahan) FP32 per thread, virials
 //    plain FP32 per thread; energies df (two-float) and virials FP32 within a
 //    warp, FP64 across warps (block_sum_df: no per-thread FP64 instruction);
@@ -16,17 +18,22 @@
 //    reduced in two-float arithmetic; structure-factor partials are FP32 over
 //    a chunk of sites and df over chunks; energy, virial and the k-space
 //    totals stay FP64.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <type_traits>
 
 #include "gb_common.cuh"
 #include "gb_df.cuh"
+#include "gb_f2.cuh"
 #include "gb_kernels.h"
 
 namespace {
 
 constexpr int MX_T = 64;     // threads per block of the pair kernels
+// resident blocks per SM asked of the real-space kernel: a register bound of
+// 80 per thread (fewer spill)
+constexpr int MX_MINB = 12;
 // lanes per site (real-space Ewald: 8, 16 or 32, default 16) and per oxygen
 // (LJ: 2, 4 or 8, default 4) are template parameters; the launchers take them
 // from the context's tuning (gbrpmd_ctx_autotune)
@@ -56,25 +63,31 @@ GB_D float dmin(float hi_a, float lo_a, float hi_b, float lo_b) {
 // Positions are 32-bit fixed-point fractional coordinates (frac_point): the
 // wrapping difference of two, read as a signed integer, is the minimum-image
 // difference in units of 2^-32, and its conversion rounds it to FP32 relative
-// to its own size (the precision of the earlier hi + lo pair, with one 16-byte
-// gather per partner instead of two and no rint per component); the charge's
-// bits ride in w.  Each lane takes every NP-th partner, four at a time with
-// their indices and positions loaded before any arithmetic, so that four
-// gathers are in flight per lane.  IT: the list entry type (unsigned short
-// for up to 65535 sites halves the list's bytes).  SLOTS: the entries are
-// cell-order slots of the last list rebuild (bit 15: same molecule) and the
-// partners' positions come from fxs, the same coordinates in slot order, so
-// that consecutive entries of a list, mostly runs of the same cells, gather
-// from neighbouring addresses.  npair (profiling only): in-cut entries counted.
-// bx: side lengths that turn fractional differences into distances, times
-// 2^-32 (1 * 2^-32 in the unit box of the cubic sum; the box in bohr for the
-// non-cubic one, rwald_basic / rwald_cell of ewald_noncubic.f90)
+// to its own size (the precision of a hi + lo pair of floats, with one 16-byte
+// gather per partner and no rint per component); the charge's bits ride in w.
+// IT: the list entry type (unsigned short for up to 65535 sites halves the
+// list's bytes).  SLOTS: the entries are cell-order slots of the last list
+// rebuild (bit 15: same molecule) and the partners' positions come from fxs,
+// the same coordinates in slot order, so that consecutive entries of a list,
+// mostly runs of the same cells, gather from neighbouring addresses.
+// Each lane takes every NP-th quad of consecutive entries and evaluates two
+// entries at a time in paired FP32 arithmetic (gb_f2.cuh: one instruction, two
+// correctly rounded operations); entries beyond the cut-off (and the missing
+// partners of the list's tail) get a zero charge product instead of a branch.
+// exp(-x^2) is the fast exponential (__expf): its error, a few ulp, is below
+// that of the erfc polynomial it multiplies.  A quad's terms are summed plainly
+// and added to the lane's compensated (Kahan) force and energy sums.
+// npair (profiling only): in-cut entries counted.  bx: side lengths that turn
+// fractional differences into distances, times 2^-32 (1 * 2^-32 in the unit
+// box of the cubic sum; the box in bohr for the non-cubic one, rwald_basic /
+// rwald_cell of ewald_noncubic.f90)
 template <int NP, typename IT, bool SLOTS>
-__global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__ fx, const int4 *__restrict__ fxs,
-                                                        int na, const int *__restrict__ count,
-                                                        const IT *__restrict__ idx, int cap, float alpha, float sfac,
-                                                        float rcutsq, float3 bx, double *g, double *acc, int add,
-                                                        unsigned long long *npair) {
+__global__ void __launch_bounds__(MX_T, MX_MINB) k_ewald_real_mx(const int4 *__restrict__ fx,
+                                                              const int4 *__restrict__ fxs, int na,
+                                                              const int *__restrict__ count,
+                                                              const IT *__restrict__ idx, int cap, float alpha,
+                                                              float sfac, float rcutsq, float3 bx, double *g,
+                                                              double *acc, int add, unsigned long long *npair) {
   __shared__ float sh[32 * 8];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
@@ -85,58 +98,91 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__
   const int4 *X = fx + (long long)c * na;
   const int4 *XJ = SLOTS ? fxs + (long long)c * na : X;
   int nin = 0;
-  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-  float ev = 0.f, evc = 0.f, vxx = 0.f, vyx = 0.f, vzx = 0.f, vyy = 0.f, vzy = 0.f, vzz = 0.f;
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, ev = 0.f, evc = 0.f;
+  const float2 z2 = f2s(0.f);
+  float2 vxx = z2, vyx = z2, vzx = z2, vyy = z2, vzy = z2, vzz = z2;
   if (active) {
     const int4 xi = X[i];
-    const float qi = __int_as_float(xi.w);
+    const float mqi = -__int_as_float(xi.w);  // the pair terms carry -q_i q_j
     const int m3 = (i / 3) * 3;  // first site of i's molecule
     const int n = min(count[(long long)c * na + i], cap);
     const IT *L = idx + ((long long)c * na + i) * cap;
-    // same molecule: bit 15 of a slot entry, else j within i's molecule
     auto same = [&](int e) { return SLOTS ? (e & 0x8000) != 0 : (unsigned)(e - m3) < 3u; };
     auto slot = [&](int e) { return SLOTS ? (e & 0x7fff) : e; };
-    auto pair = [&](int ent, const int4 &xj) {
-      const float dx = (float)(int)((unsigned)xi.x - (unsigned)xj.x) * bx.x;
-      const float dy = (float)(int)((unsigned)xi.y - (unsigned)xj.y) * bx.y;
-      const float dz = (float)(int)((unsigned)xi.z - (unsigned)xj.z) * bx.z;
-      const float drsq = dx * dx + dy * dy + dz * dz;
-      if (!(drsq < rcutsq)) return;  // skin-list entry beyond the cut-off
-      if (npair) ++nin;
-      const float inv = rsqrtf(drsq);
-      const float x = alpha * (drsq * inv);
-      const float e = expf(-x * x);
-      const float tt = __fdividef(p, p + x);
-      float erfc = e * tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5))));
-      if (same(ent)) erfc -= 1.0f;  // same molecule
-      const float du = erfc * inv;
-      const float dur = (sfac * e - du) * (inv * inv);
-      const float qij = qi * __int_as_float(xj.w);
-      const float dvr = qij * dur;
-      const float fx_ = dvr * dx, fy = dvr * dy, fz = dvr * dz;
-      kadd(sx, cx, fx_);
-      kadd(sy, cy, fy);
-      kadd(sz, cz, fz);
-      kadd(ev, evc, qij * du);
-      vxx += dx * fx_;
-      vyx += dy * fx_;
-      vzx += dz * fx_;
-      vyy += dy * fy;
-      vzy += dz * fy;
-      vzz += dz * fz;
+    const float2 bxx = f2s(bx.x), bxy = f2s(bx.y), bxz = f2s(bx.z), al2 = f2s(alpha), p2 = f2s(p);
+    const float2 msf = f2s(-sfac);
+    // two entries ea, eb (va, vb false: no partner, the tail of the list);
+    // returns the gradient terms and -q_i q_j du, adds the virial terms
+    auto pair2 = [&](int ea, int eb, const int4 &xa, const int4 &xb, bool va, bool vb, float2 &fxv, float2 &fyv,
+                     float2 &fzv, float2 &eu) {
+      const float2 dx = mul2(f2((float)(int)((unsigned)xi.x - (unsigned)xa.x), (float)(int)((unsigned)xi.x - (unsigned)xb.x)), bxx);
+      const float2 dy = mul2(f2((float)(int)((unsigned)xi.y - (unsigned)xa.y), (float)(int)((unsigned)xi.y - (unsigned)xb.y)), bxy);
+      const float2 dz = mul2(f2((float)(int)((unsigned)xi.z - (unsigned)xa.z), (float)(int)((unsigned)xi.z - (unsigned)xb.z)), bxz);
+      const float2 drsq = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+      const bool ina = va && drsq.x < rcutsq, inb = vb && drsq.y < rcutsq;
+      if (npair) nin += (int)ina + (int)inb;
+      // -q_i q_j, zero for an entry beyond the cut-off
+      const float2 mq = f2(ina ? mqi * __int_as_float(xa.w) : 0.f, inb ? mqi * __int_as_float(xb.w) : 0.f);
+      // an entry beyond the cut-off may be far: keep its arithmetic finite
+      const float2 d2 = f2(ina ? drsq.x : 1.f, inb ? drsq.y : 1.f);
+      const float2 inv = f2(rsqrtf(d2.x), rsqrtf(d2.y));
+      const float2 x = mul2(al2, mul2(d2, inv));
+      const float2 xx = mul2(x, x);
+      const float2 e = f2(__expf(-xx.x), __expf(-xx.y));
+      const float2 den = add2(p2, x);
+      const float2 tt = f2(__fdividef(p, den.x), __fdividef(p, den.y));
+      const float2 poly = fma2(tt, fma2(tt, fma2(tt, fma2(tt, f2s(a5), f2s(a4)), f2s(a3)), f2s(a2)), f2s(a1));
+      float2 erfc = mul2(mul2(e, tt), poly);
+      erfc = add2(erfc, f2(same(ea) ? -1.f : 0.f, same(eb) ? -1.f : 0.f));  // same molecule
+      const float2 du = mul2(erfc, inv);
+      const float2 w = fma2(msf, e, du);                    // du - sfac e = -dur r^2
+      const float2 dvr = mul2(mq, mul2(w, mul2(inv, inv)));  // q_i q_j dur
+      fxv = mul2(dvr, dx);
+      fyv = mul2(dvr, dy);
+      fzv = mul2(dvr, dz);
+      eu = mul2(mq, du);
+      vxx = fma2(dx, fxv, vxx);
+      vyx = fma2(dy, fxv, vyx);
+      vzx = fma2(dz, fxv, vzx);
+      vyy = fma2(dy, fyv, vyy);
+      vzy = fma2(dz, fyv, vzy);
+      vzz = fma2(dz, fzv, vzz);
     };
-    int t = sub;
-    for (; t + 3 * NP < n; t += 4 * NP) {
-      const int e0 = L[t], e1 = L[t + NP], e2 = L[t + 2 * NP], e3 = L[t + 3 * NP];
+    // lane sub takes the quads of consecutive entries sub, sub + NP, ...: one
+    // 8-byte (16-byte for int entries) load per quad, loaded two quads ahead
+    // of their arithmetic; entries past n (the list rows hold a multiple of
+    // four) are read but not used
+    using Q = typename std::conditional<sizeof(IT) == 2, uint2, uint4>::type;
+    const Q *LQ = reinterpret_cast<const Q *>(L);
+    auto ent = [&](const Q &w, int k) -> int {
+      if constexpr (sizeof(IT) == 2) {
+        const unsigned h = k < 2 ? w.x : w.y;
+        return (k & 1) ? (int)(h >> 16) : (int)(h & 0xffffu);
+      } else {
+        return (int)(k == 0 ? w.x : k == 1 ? w.y : k == 2 ? w.z : w.w);
+      }
+    };
+    const int nq = (n + 3) >> 2;
+    int qd = sub;
+    Q w0{}, w1{};
+    if (qd < nq) w0 = LQ[qd];
+    if (qd + NP < nq) w1 = LQ[qd + NP];
+    for (; qd < nq; qd += NP) {
+      const int b = 4 * qd;
+      const bool v1 = b + 1 < n, v2 = b + 2 < n, v3 = b + 3 < n;
+      const int e0 = ent(w0, 0), e1 = v1 ? ent(w0, 1) : e0, e2 = v2 ? ent(w0, 2) : e0, e3 = v3 ? ent(w0, 3) : e0;
       const int4 x0 = XJ[slot(e0)], x1 = XJ[slot(e1)], x2 = XJ[slot(e2)], x3 = XJ[slot(e3)];
-      pair(e0, x0);
-      pair(e1, x1);
-      pair(e2, x2);
-      pair(e3, x3);
-    }
-    for (; t < n; t += NP) {
-      const int e = L[t];
-      pair(e, XJ[slot(e)]);
+      w0 = w1;
+      if (qd + 2 * NP < nq) w1 = LQ[qd + 2 * NP];
+      float2 fa, fb, fc, fd, ga, gb, gc, gd;
+      pair2(e0, e1, x0, x1, true, v1, fa, fb, fc, fd);
+      pair2(e2, e3, x2, x3, v2, v3, ga, gb, gc, gd);
+      // the quad's four terms summed plainly, then one compensated add
+      const float2 qx = add2(fa, ga), qy = add2(fb, gb), qz = add2(fc, gc), qe = add2(fd, gd);
+      kadd(sx, cx, qx.x + qx.y);
+      kadd(sy, cy, qy.x + qy.y);
+      kadd(sz, cz, qz.x + qz.y);
+      kadd(ev, evc, qe.x + qe.y);
     }
   }
   if (npair) {  // one atomic per warp
@@ -153,10 +199,11 @@ __global__ void __launch_bounds__(MX_T) k_ewald_real_mx(const int4 *__restrict__
     G[1] = (add ? G[1] : 0.0) + f2d(fy0);
     G[2] = (add ? G[2] : 0.0) + f2d(fz0);
   }
-  const float vir6[6] = {vxx, vyx, vzx, vyy, vzy, vzz};
+  const float vir6[6] = {vxx.x + vxx.y, vyx.x + vyx.y, vzx.x + vzx.y, vyy.x + vyy.y, vzy.x + vzy.y, vzz.x + vzz.y};
   constexpr int dst[7] = {0, 1, 2, 3, 5, 6, 9};       // v, xx, yx, zx, yy, zy, zz
   constexpr int dst2[7] = {-1, -1, 4, 7, -1, 8, -1};  // mirrored xy, xz, yz
-  block_sum_df<7>(ev, -evc, vir6, sh, acc, dst, dst2, 0.5, 0.5);  // halved: each pair from both ends
+  // energy: the sum holds -q_i q_j du; halved: each pair from both ends
+  block_sum_df<7>(-ev, evc, vir6, sh, acc, dst, dst2, 0.5, 0.5);
 }
 
 // lj_list / lj_basic (ljones.f90) in FP32 over a full oxygen list; bead pairs
@@ -333,6 +380,7 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
   const int k = blockIdx.x * 32 + lane;
   float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
   if (k < nkp) {
+#pragma unroll 4
     for (int ch = slice; ch < nchunk; ch += MW_SL) {
       const float4 p = sk_part[((long long)c * nchunk + ch) * nkp + k];
       df_acc(h[0], l[0], p.x);
@@ -391,8 +439,11 @@ __global__ void __launch_bounds__(32 * MW_SL) k_recip_weights_mx(const float4 *s
     vals[1 + 7] += ed * f10;
     vals[1 + 5] += ed * f10;
     const float m = (float)kv.z;
+    // ordered for the force pass's paired products: (Ar, Di) and (-Ai, Dr)
+    // multiply (cos, sin) of m z into the real and imaginary parts of the x, y
+    // term, (m Dr, m Ai) and (-m Di, m Ar) into those of the z term
     float4 *o = sk + ((long long)c * nkp + k) * 2;
-    o[0] = make_float4(Ar, -Ai, Dr, Di);
+    o[0] = make_float4(Ar, Di, -Ai, Dr);
     o[1] = make_float4(m * Dr, m * Ai, -m * Di, m * Ar);
   }
 #pragma unroll
@@ -478,7 +529,10 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
   for (int col = col0; col < col1; ++col) {
     const int4 ci4 = __ldg(reinterpret_cast<const int4 *>(cols + col));
     const int kx = ci4.x, ky = ci4.y, koff = ci4.z, mlo = ci4.w & 0xffff, mhi = ci4.w >> 16;
-    float cr[NS], ci[NS], ur[NS], ui[NS], vr[NS], vi[NS];
+    // paired sums over m: the two components of each are the cos and sin
+    // halves of one sum (added at the column's end)
+    float cr[NS], ci[NS];
+    float2 ur[NS], ui[NS], vr[NS], vi[NS];
 #pragma unroll
     for (int u = 0; u < NS; ++u) {
       const int so = sl + 32 * u;
@@ -486,7 +540,7 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
       const float yi = flipf(Y.y, ky < 0 ? SIGN32 : 0);
       cr[u] = fmaf(X.x, Y.x, -X.y * yi);
       ci[u] = fmaf(X.x, yi, X.y * Y.x);
-      ur[u] = ui[u] = vr[u] = vi[u] = 0.f;
+      ur[u] = ui[u] = vr[u] = vi[u] = make_float2(0.f, 0.f);
     }
     const float4 *Tp = T + 2LL * (koff - mlo);
     auto step = [&](int m, const float2 (&z)[NS]) {
@@ -500,10 +554,10 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
       }
 #pragma unroll
       for (int u = 0; u < NS; ++u) {
-        ur[u] = fmaf(z[u].x, t0.x, fmaf(z[u].y, t0.w, ur[u]));
-        ui[u] = fmaf(z[u].x, t0.y, fmaf(z[u].y, t0.z, ui[u]));
-        vr[u] = fmaf(z[u].x, t1.x, fmaf(z[u].y, t1.y, vr[u]));
-        vi[u] = fmaf(z[u].x, t1.z, fmaf(z[u].y, t1.w, vi[u]));
+        ur[u] = fma2(z[u], make_float2(t0.x, t0.y), ur[u]);
+        ui[u] = fma2(z[u], make_float2(t0.z, t0.w), ui[u]);
+        vr[u] = fma2(z[u], make_float2(t1.x, t1.y), vr[u]);
+        vi[u] = fma2(z[u], make_float2(t1.z, t1.w), vi[u]);
       }
     };
     if constexpr (KZ > 0) {
@@ -536,10 +590,12 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
     }
 #pragma unroll
     for (int u = 0; u < NS; ++u) {
-      const float ts = -fmaf(cr[u], ui[u], ci[u] * ur[u]);
+      const float urs = ur[u].x + ur[u].y, uis = ui[u].x + ui[u].y;
+      const float vrs = vr[u].x + vr[u].y, vis = vi[u].x + vi[u].y;
+      const float ts = -fmaf(cr[u], uis, ci[u] * urs);
       kadd(sx[u], ex[u], (float)kx * ts);
       kadd(sy[u], ey[u], (float)ky * ts);
-      kadd(sz[u], ez[u], -fmaf(cr[u], vi[u], ci[u] * vr[u]));
+      kadd(sz[u], ez[u], -fmaf(cr[u], vis, ci[u] * vrs));
     }
   }
 #pragma unroll
@@ -582,11 +638,11 @@ void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, const int4 *fxs, int n
                           unsigned long long *npair) {
   const float two32 = 2.3283064365386963e-10f;  // 2^-32: fixed-point units to fractions
   const float3 bx = make_float3((float)box[0] * two32, (float)box[1] * two32, (float)box[2] * two32);
+  const float sfac = (float)(-2.0 * alpha / std::sqrt(std::acos(-1.0)));  // d erfc(alpha r) / dr factor
+  const unsigned short *i16 = reinterpret_cast<const unsigned short *>(pl.idx);
   auto go = [&](auto NPc) {
     constexpr int NP = decltype(NPc)::value;
     dim3 grid(nblk((long long)na * NP, MX_T), B);
-    const float sfac = (float)(-2.0 * alpha / std::sqrt(std::acos(-1.0)));  // d erfc(alpha r) / dr factor
-    const unsigned short *i16 = reinterpret_cast<const unsigned short *>(pl.idx);
     if (pl.slots)
       k_ewald_real_mx<NP, unsigned short, true><<<grid, MX_T, 0, s>>>(
           fx, fxs, na, pl.count, i16, pl.cap, (float)alpha, sfac, (float)rcutsq, bx, g, acc, add ? 1 : 0, npair);
@@ -657,7 +713,8 @@ void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc) 
   };
   if (nchunk <= 4) go(std::integral_constant<int, 4>());
   else if (nchunk <= 8) go(std::integral_constant<int, 8>());
-  else go(std::integral_constant<int, 16>());
+  else if (nchunk <= 32) go(std::integral_constant<int, 16>());
+  else go(std::integral_constant<int, 32>());  // more loads in flight per k pair
 }
 
 template <bool STAGED, int G, int NS, int KZ>
@@ -705,6 +762,7 @@ void recip_set_attributes_mx() {
   static bool done = false;
   if (done) return;
   cudaFuncSetAttribute(k_recip_sk_mx<MSK_SP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+
   force_attr<true, 8, 1, 0>();
   force_attr<false, 8, 1, 0>();
   force_attr<true, 8, 1, MF_KZ>();

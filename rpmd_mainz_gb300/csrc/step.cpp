@@ -170,7 +170,8 @@ int ensure_list(gb_context *c, int nconf, int npt, int cap) {
 int list_cap(int npt, double rc, double vol) {
   double full = (double)npt * (4.0 / 3.0) * PI * rc * rc * rc / vol;
   int cap = (int)(1.1 * full) + 48;
-  return std::min(cap, std::max(npt, 1));
+  cap = std::min(cap, std::max(npt, 1));
+  return (cap + 7) & ~7;  // rows of whole 16-byte groups (vector loads of the entries)
 }
 
 // c->pl = every pair within g.rcutsq (rounded as the reference rounds it) for
