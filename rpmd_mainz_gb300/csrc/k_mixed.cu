@@ -337,31 +337,32 @@ __global__ void __launch_bounds__(MSK_T) k_recip_sk_mx(const float2 *tab, int na
   if (len <= 0) return;
   const int aky = abs(ky);
   const int ymask = ky < 0 ? SIGN32 : 0;
-  float pr[GP], pi[GP], qr[GP], qi[GP];
+  // paired sums: (P_r, Q_r) and (P_i, Q_i) of each m, the (cos, sin) of m z
+  // times the real or imaginary part of the column's factor
+  float2 rq[GP], iq[GP];
 #pragma unroll
-  for (int g = 0; g < GP; ++g) pr[g] = pi[g] = qr[g] = qi[g] = 0.f;
+  for (int g = 0; g < GP; ++g) rq[g] = iq[g] = make_float2(0.f, 0.f);
   for (int s = 0; s < ns; ++s) {
     const float2 *S = stf + s * K3;
     const float2 X = S[kx], Y = S[K1 + aky];
     const float yi = flipf(Y.y, ymask);
     const float cr = fmaf(X.x, Y.x, -X.y * yi);
     const float ci = fmaf(X.x, yi, X.y * Y.x);
+    const float2 cr2 = make_float2(cr, cr), ci2 = make_float2(ci, ci);
     const float2 *Z = S + 2 * K1 + m0;
 #pragma unroll
     for (int g = 0; g < GP; ++g) {
       if (g < len) {
         const float2 z = Z[g];
-        pr[g] = fmaf(cr, z.x, pr[g]);
-        pi[g] = fmaf(ci, z.x, pi[g]);
-        qr[g] = fmaf(cr, z.y, qr[g]);
-        qi[g] = fmaf(ci, z.y, qi[g]);
+        rq[g] = fma2(cr2, z, rq[g]);
+        iq[g] = fma2(ci2, z, iq[g]);
       }
     }
   }
   float4 *out = sk_part + ((long long)c * nchunk + chunk) * nkp + gr.w + part * GP;
 #pragma unroll
   for (int g = 0; g < GP; ++g)
-    if (g < len) out[g] = make_float4(pr[g], pi[g], qr[g], qi[g]);
+    if (g < len) out[g] = make_float4(rq[g].x, iq[g].x, rq[g].y, iq[g].y);
 }
 
 // df (two-float) sums of the chunk partials; energy, virial and force tables
@@ -491,12 +492,17 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
   }
   const int tab_f4 = (K3 * BS + 1) / 2;                       // float4 slots of the site tables
   float2 *red = reinterpret_cast<float2 *>(smf + tab_f4);     // MF_G * BS * 3 df pairs
-  float4 *sT = smf + tab_f4 + (MF_G * BS * 3 + 1) / 2;        // [k pairs of the block][2]
+  int4 *scol = reinterpret_cast<int4 *>(smf + tab_f4 + (MF_G * BS * 3 + 1) / 2);  // [ncol] column records
+  float4 *sT = reinterpret_cast<float4 *>(scol + ncol);       // [k pairs of the block][2]
+  // the column records in shared memory: the range searches and the loop read
+  // them there instead of through dependent global loads
+  for (int w = t; w < ncol; w += 32 * MF_G) scol[w] = __ldg(reinterpret_cast<const int4 *>(cols + w));
+  __syncthreads();
   auto first_col = [&](long long kp) {
     int lo = 0, hi = ncol;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if (__ldg(&cols[mid].koff) < kp) lo = mid + 1;
+      if (scol[mid].z < kp) lo = mid + 1;
       else hi = mid;
     }
     return lo;
@@ -504,8 +510,8 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
   // this block's whole columns and their k pairs [kb_lo, kb_hi)
   const int KS = gridDim.z, ks = blockIdx.z;
   const int bc0 = first_col((long long)ks * nkp / KS), bc1 = first_col((long long)(ks + 1) * nkp / KS);
-  const int kb_lo = bc0 < ncol ? __ldg(&cols[bc0].koff) : nkp;
-  const int kb_hi = bc1 < ncol ? __ldg(&cols[bc1].koff) : nkp;
+  const int kb_lo = bc0 < ncol ? scol[bc0].z : nkp;
+  const int kb_hi = bc1 < ncol ? scol[bc1].z : nkp;
   if (STAGED) {
     const float4 *src = sk + ((long long)c * nkp + kb_lo) * 2;
     for (int w = t; w < 2 * (kb_hi - kb_lo); w += 32 * MF_G) sT[w] = src[w];
@@ -527,7 +533,7 @@ __global__ void __launch_bounds__(32 * MF_G) k_recip_force_mx(const float2 *__re
 #pragma unroll
   for (int u = 0; u < NS; ++u) sx[u] = sy[u] = sz[u] = ex[u] = ey[u] = ez[u] = 0.f;
   for (int col = col0; col < col1; ++col) {
-    const int4 ci4 = __ldg(reinterpret_cast<const int4 *>(cols + col));
+    const int4 ci4 = scol[col];
     const int kx = ci4.x, ky = ci4.y, koff = ci4.z, mlo = ci4.w & 0xffff, mhi = ci4.w >> 16;
     // paired sums over m: the two components of each are the cos and sin
     // halves of one sum (added at the column's end)
@@ -675,9 +681,10 @@ void launch_lj_mx(cudaStream_t s, const float4 *hi, const float4 *lo, int na, in
 
 size_t recip_sk_smem_mx(int kmax) { return sizeof(float2) * MSK_CHUNK * 3 * (kmax + 1); }
 // dynamic shared memory of k_recip_force_mx<., g, ns>
-size_t recip_force_smem_mx(int kmax, int nkp_staged, int g, int ns) {
+size_t recip_force_smem_mx(int kmax, int nkp_staged, int g, int ns, int ncol) {
   const int bs = MF_S * ns;
-  return sizeof(float4) * ((3 * (kmax + 1) * bs + 1) / 2 + (g * bs * 3 + 1) / 2 + 2 * (size_t)nkp_staged);
+  return sizeof(float4) * ((3 * (kmax + 1) * bs + 1) / 2 + (g * bs * 3 + 1) / 2 + (size_t)ncol +
+                           2 * (size_t)nkp_staged);
 }
 
 // partial sums need nconf * nchunk * nkp float4 (half of the FP64 layout)
@@ -730,14 +737,14 @@ void force_launch(cudaStream_t s, gb_context *c, int B, double *g) {
   if (const char *e = std::getenv("GBRPMD_RF_KS")) ks = std::atoi(e);  // fixed k-pair ranges (measurements)
   ks = std::max(1, std::min(ks, std::max(1, c->nkp / 64)));
   // a block stages its share of the k pairs and at most one column more
-  const size_t staged = recip_force_smem_mx(kmax, (c->nkp + ks - 1) / ks + 2 * (kmax + 1) + 2, G, NS);
+  const size_t staged = recip_force_smem_mx(kmax, (c->nkp + ks - 1) / ks + 2 * (kmax + 1) + 2, G, NS, c->ncol);
   dim3 grid(nblk(c->na, MF_S * NS), B, ks);
   if (staged <= 160 * 1024)
     k_recip_force_mx<true, G, NS, KZ><<<grid, 32 * G, staged, s>>>(
         reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
         reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
   else
-    k_recip_force_mx<false, G, NS, KZ><<<grid, 32 * G, recip_force_smem_mx(kmax, 0, G, NS), s>>>(
+    k_recip_force_mx<false, G, NS, KZ><<<grid, 32 * G, recip_force_smem_mx(kmax, 0, G, NS, c->ncol), s>>>(
         reinterpret_cast<const float2 *>(c->ktab), c->na, kmax, c->ncol, c->kcol, c->nkp,
         reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
 }
