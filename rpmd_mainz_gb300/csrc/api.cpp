@@ -170,6 +170,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
   if (const char *gr = std::getenv("GBRPMD_GRAPHS")) c->use_graphs = gr[0] != '0';
   if (const char *ce = std::getenv("GBRPMD_LIST_CELLS")) c->list_cells = ce[0] != '0';
   if (const char *br = std::getenv("GBRPMD_BRANCHES")) c->use_branches = br[0] != '0';
+  if (const char *es = std::getenv("GBRPMD_EW_SHARED")) c->ew_share = es[0] != '0';
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
@@ -190,7 +191,8 @@ int ctx_alloc(gb_context *c, int na, int nb) {
       (st = dalloc(c, &c->rb1, N)) || (st = dalloc(c, &c->fb1, N)) || (st = dalloc(c, &c->rb2, N)) ||
       (st = dalloc(c, &c->fb2, N)) || (st = dalloc(c, &c->g, N)) || (st = dalloc(c, &c->rs, N)) ||
       (st = dalloc(c, &c->rs32, (size_t)na * nb)) || (st = dalloc(c, &c->lo32, (size_t)na * nb)) ||
-      (st = dalloc(c, &c->fx32, (size_t)na * nb)) ||
+      (st = dalloc(c, &c->fx32, (size_t)na * nb)) || (st = dalloc(c, &c->fxs_b, (size_t)na * nb)) ||
+      (st = dalloc(c, &c->rcen, S)) || (st = dalloc(c, &c->spread, 4)) ||
       (st = dalloc(c, &c->hi32, (size_t)na * nb / 3)) || (st = dalloc(c, &c->olo32, (size_t)na * nb / 3)) ||
       (st = dalloc(c, &c->rs32_lj, (size_t)na * nb / 3)) || (st = dalloc(c, &c->g2, N)) ||
       (st = dalloc(c, &c->rc, S)) ||
@@ -198,6 +200,7 @@ int ctx_alloc(gb_context *c, int na, int nb) {
       (st = dalloc(c, &c->acc, (size_t)ACC_NSLOT * ACC_STRIDE)) || (st = dalloc(c, &c->status, 1)))
     return st;
   CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  CK(cudaMemsetAsync(c->spread, 0, 4 * sizeof(float), c->stream));
   CK(cudaMemsetAsync(c->dvdr, 0, sizeof(double) * N, c->stream));
   CK(cudaMemsetAsync(c->dvdr2, 0, sizeof(double) * N, c->stream));
   CK(cudaMemsetAsync(c->p, 0, sizeof(double) * N, c->stream));

@@ -62,6 +62,8 @@ struct SkinList {
   long long pstride = 0, cstride = 0;
   double cutsq = 0.0, skin = 0.0, box[3] = {0, 0, 0};
   bool want16 = false;           // unsigned short entries asked for (used with the cell-sorted build)
+  double extra = 0.0;            // margin added to cut-off + skin (a shared list's bead spread, twice)
+  bool shared = false;           // built on the centroids of several configurations (ListSpread)
 };
 enum { LIST_EW = 0, LIST_LJ = 1, LIST_TEM = 2, LIST_N = 3 };
 
@@ -114,6 +116,14 @@ struct gb_context {
   cudaEvent_t fork2_ev = nullptr, join2_ev = nullptr;
   double *g2 = nullptr;
   double *rc = nullptr;    // centroid scratch [na][3]
+  // mixed real space of several configurations: one skin list on the site
+  // centroids (superset radius cut-off + skin + twice the bead spread), the
+  // configurations' fixed-point coordinates in its slot order, and the
+  // spread words (ListSpread)
+  double *rcen = nullptr;  // [na][3]
+  int4 *fxs_b = nullptr;   // [nb][na]
+  float *spread = nullptr; // [4]
+  int ew_share = 1;        // GBRPMD_EW_SHARED=0: a list per configuration
   PairList pl;             // exact pair list of the current term (re-sized on demand)
   size_t pl_idx_bytes = 0, pl_cnt_bytes = 0;
   SkinList sl[LIST_N];     // per-term skin lists (Ewald real space, LJ, TEM)

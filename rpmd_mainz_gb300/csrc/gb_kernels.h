@@ -38,8 +38,10 @@ void launch_frac32(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, f
                    const double *q = nullptr, int4 *fx = nullptr);
 // every pair within g.rcutsq; with a gate word, only when *gate != 0 (counts
 // are then zeroed on the device, so the decision needs no host round trip)
+// thr_dev (device): the superset radius squared of a shared list (ListSpread::w + 2)
 void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
-                       PairList &pl, unsigned *status, const unsigned *gate = nullptr);
+                       PairList &pl, unsigned *status, const unsigned *gate = nullptr,
+                       const float *thr_dev = nullptr);
 // skin lists: displacement test against the rebuild positions, position save
 // on a rebuild, and the filter from the superset to the exact list
 void launch_skin_check(cudaStream_t s, const PairGeom &g, int nconf, const double *ref, double lim2,
@@ -50,15 +52,38 @@ void launch_skin_save(cudaStream_t s, const PairGeom &g, int nconf, double *ref,
 // the per-step skin test with cell counts (check = 0: *flag already set; also
 // writes frac / lo as launch_frac32), and the gated scatter + build
 bool list_cell_grid(const PairGeom &g, int nc[3], int *R, signed char *reach);
+// A list shared by B configurations, built on their centroids (mixed real
+// space): w (device, 4 floats) holds [0] the step's largest squared distance
+// of a site from its centroid, [1] the squared margin of the current list,
+// [2] its squared superset radius (the build threshold); base: cut-off +
+// skin, dcap: the largest margin the stencil and capacity allow, dmin: the
+// smallest margin; all in the list geometry's units.  w = nullptr: off.
+struct ListSpread {
+  float *w = nullptr;
+  float base = 0.f, dcap = 0.f, dmin = 0.f;
+};
 void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
                        const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag,
-                       int4 *fx = nullptr);
+                       int4 *fx = nullptr, const ListSpread &sp = ListSpread());
+// site centroids of B configurations and their spread (ListSpread); a spread
+// beyond the list's margin sets *moved (a rebuild), beyond dcap sets
+// ST_LIST_OVERFLOW in status
+void launch_site_centroid(cudaStream_t s, const double *r, double *cen, int na, int B, const ListSpread &sp,
+                          unsigned *moved, unsigned *status);
+// at a rebuild (*flag): the shared list's margin and superset radius from the
+// step's spread; clears the spread word
+void launch_spread_update(cudaStream_t s, const unsigned *flag, const ListSpread &sp);
+// fixed-point coordinates of B configurations, and in slot order when slot_of
+// and fxs are given
+void launch_fx_slots(cudaStream_t s, const PairGeom &g, int B, const double *q, const int *slot_of, int4 *fx,
+                     int4 *fxs);
 // (also saves the reference positions and counts the rebuild, as launch_skin_save)
 // fx: the points' fixed-point coordinates (copied into cs.fxs in slot order
 // when the list stores slots)
+// thr_dev (device): the superset radius squared of a shared list (ListSpread::w + 2)
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
                          unsigned *status, const unsigned *gate, const CellSort &cs, double *ref,
-                         unsigned *rebuilds, const int4 *fx = nullptr);
+                         unsigned *rebuilds, const int4 *fx = nullptr, const float *thr_dev = nullptr);
 void launch_list_filter(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
                         const PairList &skin, PairList &pl, unsigned *status);
 double list_total(cudaStream_t s, const PairList &pl);  // profiling only (synchronises)

@@ -87,7 +87,8 @@ __global__ void __launch_bounds__(MX_T, MX_MINB) k_ewald_real_mx(const int4 *__r
                                                               const int *__restrict__ count,
                                                               const IT *__restrict__ idx, int cap, float alpha,
                                                               float sfac, float rcutsq, float3 bx, double *g,
-                                                              double *acc, int add, unsigned long long *npair) {
+                                                              double *acc, int add, unsigned long long *npair,
+                                                              int lconf) {
   __shared__ float sh[32 * 8];
   const float p = 3.0525860f, a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f,
               a4 = -1.453152027f, a5 = 1.061405429f;
@@ -105,8 +106,11 @@ __global__ void __launch_bounds__(MX_T, MX_MINB) k_ewald_real_mx(const int4 *__r
     const int4 xi = X[i];
     const float mqi = -__int_as_float(xi.w);  // the pair terms carry -q_i q_j
     const int m3 = (i / 3) * 3;  // first site of i's molecule
-    const int n = min(count[(long long)c * na + i], cap);
-    const IT *L = idx + ((long long)c * na + i) * cap;
+    // the list of i: its configuration's, or with lconf = 0 the one list the
+    // configurations share (built on their centroids)
+    const long long row = (long long)(lconf ? c : 0) * na + i;
+    const int n = min(count[row], cap);
+    const IT *L = idx + row * cap;
     auto same = [&](int e) { return SLOTS ? (e & 0x8000) != 0 : (unsigned)(e - m3) < 3u; };
     auto slot = [&](int e) { return SLOTS ? (e & 0x7fff) : e; };
     const float2 bxx = f2s(bx.x), bxy = f2s(bx.y), bxz = f2s(bx.z), al2 = f2s(alpha), p2 = f2s(p);
@@ -649,15 +653,18 @@ void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, const int4 *fxs, int n
   auto go = [&](auto NPc) {
     constexpr int NP = decltype(NPc)::value;
     dim3 grid(nblk((long long)na * NP, MX_T), B);
+    const int lconf = pl.nconf == 1 ? 0 : 1;  // one list shared by the B configurations
     if (pl.slots)
       k_ewald_real_mx<NP, unsigned short, true><<<grid, MX_T, 0, s>>>(
-          fx, fxs, na, pl.count, i16, pl.cap, (float)alpha, sfac, (float)rcutsq, bx, g, acc, add ? 1 : 0, npair);
+          fx, fxs, na, pl.count, i16, pl.cap, (float)alpha, sfac, (float)rcutsq, bx, g, acc, add ? 1 : 0, npair,
+          lconf);
     else if (pl.i16)
       k_ewald_real_mx<NP, unsigned short, false><<<grid, MX_T, 0, s>>>(
-          fx, fx, na, pl.count, i16, pl.cap, (float)alpha, sfac, (float)rcutsq, bx, g, acc, add ? 1 : 0, npair);
+          fx, fx, na, pl.count, i16, pl.cap, (float)alpha, sfac, (float)rcutsq, bx, g, acc, add ? 1 : 0, npair,
+          lconf);
     else
       k_ewald_real_mx<NP, int, false><<<grid, MX_T, 0, s>>>(fx, fx, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
-                                                            (float)rcutsq, bx, g, acc, add ? 1 : 0, npair);
+                                                            (float)rcutsq, bx, g, acc, add ? 1 : 0, npair, lconf);
   };
   if (np == 8) go(std::integral_constant<int, 8>());
   else if (np == 32) go(std::integral_constant<int, 32>());

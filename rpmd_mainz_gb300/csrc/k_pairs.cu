@@ -34,6 +34,18 @@ constexpr int LB_T = 128;
 // difference of two of them, read as a signed integer, is the minimum-image
 // difference (|d| < 1/2) in units of 2^-32 exactly, so one integer subtraction
 // and one conversion give it to FP32 rounding of the difference itself.
+GB_D int4 fixed_point(const PairGeom &g, int c, int i, const double *q) {
+  const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
+  unsigned fxd[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double u = g.unit ? x[d] : x[d] * g.onbox[d];
+    u -= floor(u);
+    fxd[d] = (unsigned)__double2ull_rn(u * 4294967296.0);  // u = 1 (rounded) wraps to 0
+  }
+  return make_int4((int)fxd[0], (int)fxd[1], (int)fxd[2], __float_as_int(q ? (float)q[i] : 0.0f));
+}
+
 GB_D float4 frac_point(const PairGeom &g, long long t, int c, int i, float4 *frac, float4 *lo, const double *q,
                        int4 *fx = nullptr) {
   const double *x = g.pos + c * g.cstride + (long long)i * g.pstride;
@@ -92,10 +104,14 @@ template <bool FULL, bool EXCL>
 __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *frac, int *count,
                                                       int *idx, int cap, float3 len, float thr_lo,
                                                       float thr_hi, unsigned *status, const unsigned *gate,
-                                                      int jchunk) {
+                                                      int jchunk, const float *thr_dev) {
   __shared__ float4 tile[LB_T];
   __shared__ int stage[LB_T][LB_STAGE + 1];
   if (gate && *gate == 0u) return;  // skin list still valid: nothing to rebuild
+  // thr_dev: a superset radius chosen on the device (a shared list); every
+  // pair inside it is taken, without the exact band test
+  const bool dev_thr = thr_dev != nullptr;
+  if (dev_thr) thr_hi = thr_dev[0];
   const int c = blockIdx.z;
   const int i = blockIdx.x * LB_T + threadIdx.x;
   const int npt = g.npt;
@@ -135,7 +151,7 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
     if (j == i) return;
     if (!FULL && (i < j) != (((i + j) & 1) != 0)) return;
     if (EXCL && (i / 3) == (j / 3)) return;
-    if (d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride)) {
+    if (dev_thr || d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride)) {
       st[nst++] = j;
       if (nst == LB_STAGE) flush();
     }
@@ -203,7 +219,7 @@ GB_D int cell_of(float u, int n) { return max(min((int)(u * (float)n), n - 1), 0
 // (also writes the points' fractional coordinates, as k_frac32)
 __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q,
                                                     CellSortDev cs, const double *ref, double lim2, int check,
-                                                    unsigned *flag, int4 *fx) {
+                                                    unsigned *flag, int4 *fx, ListSpread sp) {
   __shared__ bool last;
   __shared__ int part[256];
   const long long n = (long long)nconf * g.npt;
@@ -240,6 +256,16 @@ __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float
     s_rebuild = !check || *(volatile unsigned *)(cs.ticket + 1) != 0u;
     *flag = s_rebuild ? 1u : 0u;
     cs.ticket[1] = 0u;
+    if (sp.w) {  // a shared list: its margin for the bead spread, chosen at each rebuild
+      volatile float *w = sp.w;
+      if (s_rebuild) {
+        const float dres = fminf(sp.dcap, 1.25f * sqrtf(w[0]) + sp.dmin);
+        const float rl = sp.base + 2.0f * dres;
+        w[1] = dres * dres;
+        w[2] = rl * rl * (1.0f + 1e-5f);
+      }
+      w[0] = 0.0f;  // the next step's spread
+    }
   }
   __syncthreads();
   const bool rebuild = s_rebuild;
@@ -297,10 +323,8 @@ __global__ void k_cell_scatter(PairGeom g, int nconf, const float4 *frac, CellSo
   const long long pos = (long long)c * npt + cs.cstart[(long long)c * (ncell + 1) + cs.cellid[t]] + cs.crank[t];
   cs.spos[pos] = frac[t];
   cs.sidx[pos] = i;
-  if (cs.fxs) {
-    cs.slot_of[t] = (int)(pos - (long long)c * npt);
-    cs.fxs[pos] = fx[t];
-  }
+  if (cs.slot_of) cs.slot_of[t] = (int)(pos - (long long)c * npt);
+  if (cs.fxs) cs.fxs[pos] = fx[t];
 }
 
 // IT: the list entry type (int, or unsigned short when npt <= 65535)
@@ -309,9 +333,14 @@ __global__ void k_cell_scatter(PairGeom g, int nconf, const float4 *frac, CellSo
 template <bool FULL, bool EXCL, typename IT, bool SLOTS = false>
 __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, CellSortDev cs, int *count, IT *idx,
                                                        int cap, float3 len, float thr_lo, float thr_hi,
-                                                       unsigned *status, const unsigned *gate) {
+                                                       unsigned *status, const unsigned *gate,
+                                                       const float *thr_dev) {
   __shared__ signed char s_reach[sizeof(cs.reach)];
   if (*gate == 0u) return;
+  // thr_dev: a superset radius chosen on the device (a shared list); every
+  // pair inside it is taken, without the exact band test
+  const bool dev_thr = thr_dev != nullptr;
+  if (dev_thr) thr_hi = thr_dev[0];
   for (int t = threadIdx.x; t < (int)sizeof(cs.reach); t += blockDim.x) s_reach[t] = cs.reach[t];
   __syncthreads();
   const int npt = g.npt;
@@ -358,7 +387,7 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
           if (d2 < thr_hi) {
             j = si[k];
             hit = j != i && (FULL || (i < j) == (((i + j) & 1) != 0)) && (!EXCL || (i / 3) != (j / 3)) &&
-                  (d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride));
+                  (dev_thr || d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride));
           }
         }
         const unsigned m = __ballot_sync(0xffffffffu, hit);
@@ -784,6 +813,64 @@ __global__ void k_centroid(const double *r, double *rc, int na, int B) {
   rc[t] = s / (double)B;
 }
 
+// Shared list of B configurations (ListSpread): each site's centroid over the
+// configurations (as k_centroid), and the largest squared distance of a
+// configuration's site from its centroid, max-reduced into sp.w[0].  A site
+// beyond the list's margin (sp.w[1]) asks for a rebuild (moved); one beyond
+// the stencil's cap (the largest margin the list can take) is an error.
+__global__ void k_site_centroid(const double *r, double *cen, int na, int B, ListSpread sp, unsigned *moved,
+                                unsigned *status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float d2 = 0.0f;
+  if (i < na) {
+    const long long S = 3LL * na;
+    double c[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      double s = 0.0;
+      for (int b = 0; b < B; ++b) s = s + r[S * b + 3 * i + d];
+      c[d] = s / (double)B;
+      cen[3 * i + d] = c[d];
+    }
+    for (int b = 0; b < B; ++b) {
+      const double *x = r + S * b + 3 * i;
+      const float dx = (float)(x[0] - c[0]), dy = (float)(x[1] - c[1]), dz = (float)(x[2] - c[2]);
+      d2 = fmaxf(d2, dx * dx + dy * dy + dz * dz);
+    }
+    if (!(d2 <= sp.dcap * sp.dcap)) atomicOr(status, ST_LIST_OVERFLOW);  // NaN too
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(0xffffffffu, d2, o));
+  if ((threadIdx.x & 31) == 0) {
+    if (d2 > 0.0f) atomicMax(reinterpret_cast<int *>(sp.w), __float_as_int(d2));  // non-negative: int order
+    if (d2 > *(volatile float *)(sp.w + 1)) atomicOr(moved, 1u);
+  }
+}
+
+// the margin of a shared list at a rebuild (the all-pairs build; the
+// cell-sorted one takes it in k_cell_count), and the next step's spread word
+__global__ void k_spread_update(const unsigned *flag, ListSpread sp) {
+  volatile float *w = sp.w;
+  if (*flag) {
+    const float dres = fminf(sp.dcap, 1.25f * sqrtf(w[0]) + sp.dmin);
+    const float rl = sp.base + 2.0f * dres;
+    w[1] = dres * dres;
+    w[2] = rl * rl * (1.0f + 1e-5f);
+  }
+  w[0] = 0.0f;
+}
+
+// fixed-point coordinates of B configurations (fx [B][npt]) and, with slot_of
+// (the shared list's cell-order slots), the same in slot order (fxs)
+__global__ void k_fx_slots(PairGeom g, int B, const double *q, const int *slot_of, int4 *fx, int4 *fxs) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)B * g.npt) return;
+  const int c = (int)(t / g.npt), i = (int)(t % g.npt);
+  const int4 v = fixed_point(g, c, i, q);
+  fx[t] = v;
+  if (fxs) fxs[(long long)c * g.npt + slot_of[i]] = v;
+}
+
 __global__ void k_sum_counts(const int *count, long long n, unsigned long long *out) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long v = t < n ? (unsigned long long)count[t] : 0ull;
@@ -854,7 +941,7 @@ void list_thresholds(const PairGeom &g, float3 *len, float *lo, float *hi) {
 }
 
 void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac,
-                       PairList &pl, unsigned *status, const unsigned *gate) {
+                       PairList &pl, unsigned *status, const unsigned *gate, const float *thr_dev) {
   float3 len;
   float thr_lo, thr_hi;
   list_thresholds(g, &len, &thr_lo, &thr_hi);
@@ -870,7 +957,8 @@ void launch_build_list(cudaStream_t s, const PairGeom &g, int nconf, const float
   while (jchunk > LB_T && bi * (long long)nblk(g.npt, jchunk) < 4LL * nsm) jchunk /= 2;
   dim3 grid(nblk(g.npt, LB_T), nblk(g.npt, jchunk), nconf);
   auto go = [&](auto kern) {
-    kern<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status, gate, jchunk);
+    kern<<<grid, LB_T, 0, s>>>(g, frac, pl.count, pl.idx, pl.cap, len, thr_lo, thr_hi, status, gate, jchunk,
+                               thr_dev);
   };
   if (g.full) {
     if (g.excl_mol) go(k_build_list2<true, true>);
@@ -973,15 +1061,30 @@ CellSortDev dev_cells(const CellSort &cs) {
 // skin test and cell counts (every step), then, gated by flag, the cell-order
 // scatter (which also zeroes the list counts) and the build
 void launch_cell_count(cudaStream_t s, const PairGeom &g, int nconf, float4 *frac, float4 *lo, const double *q,
-                       const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag, int4 *fx) {
+                       const CellSort &cs, const double *ref, double lim2, int check, unsigned *flag, int4 *fx,
+                       const ListSpread &sp) {
   CellSortDev d = dev_cells(cs);
   const long long n = (long long)nconf * g.npt;
-  k_cell_count<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q, d, ref, lim2, check, flag, fx);
+  k_cell_count<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, lo, q, d, ref, lim2, check, flag, fx, sp);
+}
+
+void launch_site_centroid(cudaStream_t s, const double *r, double *cen, int na, int B, const ListSpread &sp,
+                          unsigned *moved, unsigned *status) {
+  k_site_centroid<<<nblk(na, 128), 128, 0, s>>>(r, cen, na, B, sp, moved, status);
+}
+
+void launch_spread_update(cudaStream_t s, const unsigned *flag, const ListSpread &sp) {
+  k_spread_update<<<1, 1, 0, s>>>(flag, sp);
+}
+
+void launch_fx_slots(cudaStream_t s, const PairGeom &g, int B, const double *q, const int *slot_of, int4 *fx,
+                     int4 *fxs) {
+  k_fx_slots<<<nblk((long long)B * g.npt, 256), 256, 0, s>>>(g, B, q, slot_of, fx, fxs);
 }
 
 void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const float4 *frac, PairList &pl,
                          unsigned *status, const unsigned *gate, const CellSort &cs, double *ref,
-                         unsigned *rebuilds, const int4 *fx) {
+                         unsigned *rebuilds, const int4 *fx, const float *thr_dev) {
   float3 len;
   float thr_lo, thr_hi;
   list_thresholds(g, &len, &thr_lo, &thr_hi);
@@ -990,7 +1093,7 @@ void launch_build_sorted(cudaStream_t s, const PairGeom &g, int nconf, const flo
   k_cell_scatter<<<nblk(n, 256), 256, 0, s>>>(g, nconf, frac, d, pl.count, gate, ref, rebuilds, fx);
   auto go = [&](auto kern, auto *idx) {
     kern<<<nblk(32 * n, LB_T), LB_T, 0, s>>>(g, nconf, d, pl.count, idx, pl.cap, len, thr_lo, thr_hi, status,
-                                             gate);
+                                             gate, thr_dev);
   };
   unsigned short *i16 = reinterpret_cast<unsigned short *>(pl.idx);
   if (pl.slots) {  // never with exclusions

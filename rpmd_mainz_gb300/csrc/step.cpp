@@ -184,9 +184,21 @@ int list_cap(int npt, double rc, double vol) {
 // fx (optional) receives the points' fixed-point coordinates every step
 // (frac_point); with want16 the superset stores unsigned short entries when the
 // cell-sorted build is used and the points number at most 65535.
+// shared (superset use only): the list is built on g, the centroids of
+// shared->B configurations (computed here from shared->r into g.pos, every
+// step), with extra = twice the largest spread margin added to its radius;
+// the build takes the radius the device chose (ListSpread); fx is then not
+// written (the caller writes the configurations' coordinates in slot order).
+struct SharedList {
+  ListSpread sp;
+  const double *r = nullptr;
+  int B = 0;
+  double *cen = nullptr;
+};
+
 int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut, double vol, int *nl,
               float4 *lo = nullptr, const double *q = nullptr, bool superset = false, PairList **use = nullptr,
-              int4 *fx = nullptr, bool want16 = false) {
+              int4 *fx = nullptr, bool want16 = false, const SharedList *shared = nullptr, double extra = 0.0) {
   if (use) *use = &c->pl;
   int st = ensure_list(c, nconf, g.npt, list_cap(g.npt, cut, vol));
   if (st) return st;
@@ -197,11 +209,11 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     return GB_OK;
   }
   SkinList &S = c->sl[which];
-  const double skin = c->list_skin * cut, scut = cut + skin;
+  const double skin = c->list_skin * cut, scut = cut + skin + extra;
   bool same = S.valid && S.nconf == nconf && S.npt == g.npt && S.unit == g.unit && S.excl == g.excl_mol &&
               S.full == g.full &&
               S.pstride == g.pstride && S.cstride == g.cstride && S.cutsq == g.rcutsq && S.skin == skin &&
-              S.want16 == want16;
+              S.want16 == want16 && S.extra == extra && S.shared == (shared != nullptr);
   for (int d = 0; d < 3; ++d) same = same && S.box[d] == g.box[d];
   if (!same) {
     S.valid = false;
@@ -244,7 +256,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
     CellSort &cs = S.cells;
     cs.on = c->list_cells && list_cell_grid(gsc, cs.nc, &cs.R, cs.reach);
     S.pl.i16 = want16 && cs.on && g.npt <= 65535 ? 1 : 0;
-    S.pl.slots = S.pl.i16 && fx && !g.excl_mol && g.npt <= 32767 ? 1 : 0;
+    S.pl.slots = S.pl.i16 && (fx || shared) && !g.excl_mol && g.npt <= 32767 ? 1 : 0;
     if (cs.on) {
       const size_t ncell = (size_t)cs.nc[0] * cs.nc[1] * cs.nc[2];
       const size_t need_cell = sizeof(int) * (size_t)nconf * (2 * ncell + 1);  // counts, then offsets
@@ -267,7 +279,7 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
       cs.cstart = cs.ccount + (size_t)nconf * ncell;
       const size_t np = (size_t)nconf * g.npt;
       int4 *fxs = reinterpret_cast<int4 *>(cs.spos + np);
-      cs.fxs = S.pl.slots ? fxs : nullptr;
+      cs.fxs = S.pl.slots && fx ? fxs : nullptr;
       cs.cellid = reinterpret_cast<int *>(fxs + np);
       cs.crank = cs.cellid + np;
       cs.sidx = cs.crank + np;
@@ -282,8 +294,14 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   }
   // the cell count kernel writes the gate itself
   if (!S.cells.on) CK(cudaMemsetAsync(S.flag, same ? 0 : 1, sizeof(unsigned), c->stream));
+  if (shared && nconf != 1) return ctx_set_error(GB_E_ARG, "a shared list has one configuration");
   int n = S.cells.on ? 0 : 1;  // the frac32 launch (else in the cell count)
-  if (!S.cells.on) launch_frac32(c->stream, g, nconf, c->rs32, lo, q, fx);
+  if (shared) {  // the centroids of this step (the list's points) and their spread (ListSpread)
+    launch_site_centroid(c->stream, shared->r, shared->cen, g.npt, shared->B, shared->sp,
+                         S.cells.on ? S.cells.ticket + 1 : S.flag, c->status);
+    n += 1;
+  }
+  if (!S.cells.on) launch_frac32(c->stream, g, nconf, c->rs32, lo, q, shared ? nullptr : fx);
   // rebuild when a point moved by more than skin/2 (a hair less, for rounding)
   const double lim = 0.5 * skin * (1.0 - 1e-9);
   PairGeom gs = g;
@@ -291,16 +309,22 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   if (S.cells.on) {  // skin test and cell counts in one kernel, then the gated sort and build
     cudaError_t e0 = cudaGetLastError();
     if (e0 != cudaSuccess) return ctx_check_cuda(e0, "a launch before the cell count");
-    launch_cell_count(c->stream, g, nconf, c->rs32, lo, q, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag, fx);
+    launch_cell_count(c->stream, g, nconf, c->rs32, lo, q, S.cells, S.ref, lim * lim, same ? 1 : 0, S.flag,
+                      shared ? nullptr : fx, shared ? shared->sp : ListSpread());
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell count launch");
-    launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells, S.ref, S.rebuilds, fx);
+    launch_build_sorted(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, S.cells, S.ref, S.rebuilds,
+                        shared ? nullptr : fx, shared ? shared->sp.w + 2 : nullptr);
     if ((e0 = cudaGetLastError()) != cudaSuccess) return ctx_check_cuda(e0, "cell build launch");
   } else {
     if (same) {
       launch_skin_check(c->stream, g, nconf, S.ref, lim * lim, S.flag);
       n += 1;
     }
-    launch_build_list(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag);
+    if (shared) {
+      launch_spread_update(c->stream, S.flag, shared->sp);
+      n += 1;
+    }
+    launch_build_list(c->stream, gs, nconf, c->rs32, S.pl, c->status, S.flag, shared ? shared->sp.w + 2 : nullptr);
     launch_skin_save(c->stream, g, nconf, S.ref, S.flag, S.rebuilds);
   }
   n += 3;  // cells: count, scatter (+ save), build; else zero, build, save
@@ -324,6 +348,8 @@ int make_list(gb_context *c, int which, const PairGeom &g, int nconf, double cut
   S.cutsq = g.rcutsq;
   S.skin = skin;
   S.want16 = want16;
+  S.extra = extra;
+  S.shared = shared != nullptr;
   for (int d = 0; d < 3; ++d) S.box[d] = g.box[d];
   *nl = n;
   return GB_OK;
@@ -390,9 +416,40 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   prof_begin(c, PR_LIST);
   PairList *pl = nullptr;  // mixed: the skin list itself, cut-off tested in the FP32 kernel
   const double vol = cub ? 1.0 : c->box[0] * c->box[1] * c->box[2];
-  int st = make_list(c, LIST_EW, g, B, c->P.wrcut, vol, &nl, mixed ? c->lo32 : nullptr, mixed ? c->z : nullptr,
-                     mixed, &pl, mixed ? c->fx32 : nullptr, mixed);
+  // mixed, several configurations: one list on the site centroids serves them
+  // all (a superset whose radius adds twice the beads' largest distance from
+  // their centroid, chosen on the device at each rebuild and bounded by dcap;
+  // the kernel tests each configuration's own distances)
+  bool share = false;
+  double extra = 0.0;
+  SharedList sh;
+  PairGeom gc = g;
+  if (mixed && B > 1 && c->ew_share && c->list_skin > 0.0) {
+    const double unit = cub ? L : 1.0;                    // bohr per length unit of g
+    const double rcu = c->P.wrcut, skinu = c->list_skin * rcu;
+    const double dcap = std::max(3.0 / unit, 0.12 * rcu);  // at most 3 bohr, or 12 % of the cut-off, of spread
+    extra = 2.0 * dcap;
+    gc.pos = c->rcen;
+    gc.cstride = 0;
+    share = true;
+    sh.sp.w = c->spread;
+    sh.sp.base = (float)(rcu + skinu);
+    sh.sp.dcap = (float)dcap;
+    sh.sp.dmin = (float)(0.1 / unit);
+    sh.r = c->rs;
+    sh.B = B;
+    sh.cen = c->rcen;
+  }
+  int st = share ? make_list(c, LIST_EW, gc, 1, c->P.wrcut, vol, &nl, nullptr, c->z, true, &pl, nullptr, true, &sh,
+                             extra)
+                 : make_list(c, LIST_EW, g, B, c->P.wrcut, vol, &nl, mixed ? c->lo32 : nullptr,
+                             mixed ? c->z : nullptr, mixed, &pl, mixed ? c->fx32 : nullptr, mixed);
   if (st) return st;
+  if (share) {  // the configurations' fixed-point coordinates, in the shared list's slot order
+    launch_fx_slots(c->stream, g, B, c->z, pl->slots ? c->sl[LIST_EW].cells.slot_of : nullptr, c->fx32,
+                    pl->slots ? c->fxs_b : nullptr);
+    nl += 1;
+  }
   prof_end(c, PR_LIST, (double)na * B);
   c->launches += nl;
   // in-cut pairs, each once (profiling fills c->pl with the exact list, or the
@@ -405,7 +462,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
     CK(cudaMemsetAsync(c->d_npair, 0, sizeof(unsigned long long), c->stream));
     npair_dev = c->d_npair;
   }
-  const int4 *fxs = mixed && pl->slots ? c->sl[LIST_EW].cells.fxs : nullptr;
+  const int4 *fxs = mixed && pl->slots ? (share ? c->fxs_b : c->sl[LIST_EW].cells.fxs) : nullptr;
   const double ksites = (double)c->nk * na * B;
   if (branch) {
     if ((st0 = watch_mark(c, PR_EW_REAL, c->stream, 0))) return st0;
@@ -1146,6 +1203,7 @@ size_t dev_estimate_bytes(int na, int nb, const gb_params &P) {
   const size_t N = 3 * (size_t)na * nb, nm = na / 3;
   size_t b = sizeof(double) * (15 * N + 5 * (size_t)na + 12 * (size_t)nb + ACC_NSLOT * ACC_STRIDE);
   b += sizeof(float4) * (3 * (size_t)na * nb + 2 * nm * nb);
+  b += sizeof(int4) * (size_t)na * nb + sizeof(double) * 3 * (size_t)na + 4 * sizeof(float);  // shared-list buffers
   const int kmax = std::max(P.kmax, 0);
   const int cap_col = gb_kcap_col(kmax), cap_kp = gb_kcap_kp(kmax);
   std::vector<KCol> col(cap_col);

@@ -148,3 +148,42 @@ def test_mixed_structure_factors_on_tensor_cores(monkeypatch):
     for k in ("v", "vew"):
         assert abs(ftc[k] - f64[k]) <= ENERGY_TOL * abs(f64[k]) + 1e-12, (k, ftc[k], f64[k])
     assert rel(ftc["vir"], f64["vir"]) < VIRIAL_TOL
+
+
+@pytest.mark.parametrize("case", [
+    dict(param="param_qspcfw", ncell=(6, 6, 6), nb=8),
+    dict(param="param_qspcfw", ncell=(8, 8, 8), nb=16, mts=1, dtfs=0.5),
+])
+def test_shared_centroid_list_matches_per_bead_lists(monkeypatch, case):
+    """Mixed real space of several beads walks one list built on the site
+    centroids (radius widened by twice the bead spread, the cut-off tested per
+    bead): forces, energies and virial equal those of per-bead lists
+    (GBRPMD_EW_SHARED=0) to FP32 summation order, over steps with rebuilds."""
+    s = systems.build(**case)
+    r = systems.perturbed(s, seed=141)
+    out = []
+    for shared in ("1", "0"):
+        monkeypatch.setenv("GBRPMD_EW_SHARED", shared)
+        p = s["params"]
+        p.precision = 1
+        lib.init(p)
+        ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+        ctx.set_params(p)
+        ctx.upload(r=r, box=s["box"])
+        en = ctx.full_forces()
+        f0 = ctx.download()[2]
+        ctx.evolve(30, s["dt"], s["beta"])
+        rr, pp, f1, f2 = ctx.download()
+        out.append((en, f0, rr, pp, f1, ctx.list_rebuilds()))
+        ctx.close()
+    monkeypatch.delenv("GBRPMD_EW_SHARED")
+    s["params"].precision = 0
+    lib.init(s["params"])
+    (ea, f0a, ra, pa, fa, nra), (eb, f0b, rb, pb, fb, nrb) = out
+    assert rel(f0a, f0b) < 1e-6
+    assert abs(ea["vew"] - eb["vew"]) <= 1e-6 * abs(eb["vew"])
+    assert rel(ea["vir"], eb["vir"]) < 1e-6
+    # 30 steps later: the FP32 summation-order differences, amplified by the
+    # dynamics (a missed pair would show in the forces above at once)
+    assert rel(ra, rb) < 1e-7 and rel(pa, pb) < 1e-4 and rel(fa, fb) < 1e-4, (rel(ra, rb), rel(pa, pb), rel(fa, fb))
+    assert nra[0] >= 1  # the shared list was built (and rebuilt) on the device
