@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(LB_T) k_build_list2(PairGeom g, const float4 *
 // coalesced 32-slot steps; hits are appended through a ballot (no atomics).
 // The FP32 prefilter and the FP64 band test are those of k_build_list2.
 constexpr int CELL_RMAX = 6;  // largest stencil radius in cells
+constexpr int BUILD_RUNS_MAX = 2 * (2 * CELL_RMAX + 1) * (2 * CELL_RMAX + 1);  // slot runs of a stencil
 struct CellSortDev {
   int nx, ny, nz, R;
   // per stencil row (oz, oy): the largest |ox| whose cells can hold a pair
@@ -205,7 +206,7 @@ struct CellSortDev {
   int *cstart;     // [nconf][ncell + 1]
   int *cellid;     // [nconf][npt]
   int *crank;      // [nconf][npt] rank in the cell (arbitrary order)
-  float4 *spos;    // [nconf][npt] fractional positions in cell order
+  float4 *spos;    // [nconf][npt] fractional positions in cell order, the point's index in w (int bits)
   int *sidx;       // [nconf][npt] point of each cell-order slot
   int *slot_of;    // [nconf][npt] slot of each point at the last rebuild
   int4 *fxs;       // [nconf][npt] fixed-point positions in slot order (null: not kept)
@@ -215,6 +216,13 @@ struct CellSortDev {
 // (clamped both ways: a wrapped coordinate is in [0, 1], and a non-finite one
 // converts to 0, so no input can index outside the grid)
 GB_D int cell_of(float u, int n) { return max(min((int)(u * (float)n), n - 1), 0); }
+
+// fractional distance from u to cell c (unwrapped index, may lie outside
+// 0..n-1) of an axis of n cells; 0 inside it
+GB_D float cell_gap(float u, int c, int n) {
+  const float lo = (float)c / (float)n, hi = (float)(c + 1) / (float)n;
+  return fmaxf(fmaxf(lo - u, u - hi), 0.0f);
+}
 
 // (also writes the points' fractional coordinates, as k_frac32)
 __global__ void __launch_bounds__(256) k_cell_count(PairGeom g, int nconf, float4 *frac, float4 *lo, const double *q,
@@ -321,7 +329,8 @@ __global__ void k_cell_scatter(PairGeom g, int nconf, const float4 *frac, CellSo
   ref[3 * t + 2] = x[2];
   const int ncell = cs.nx * cs.ny * cs.nz;
   const long long pos = (long long)c * npt + cs.cstart[(long long)c * (ncell + 1) + cs.cellid[t]] + cs.crank[t];
-  cs.spos[pos] = frac[t];
+  const float4 f = frac[t];
+  cs.spos[pos] = make_float4(f.x, f.y, f.z, __int_as_float(i));  // the point's index rides in w
   cs.sidx[pos] = i;
   if (cs.slot_of) cs.slot_of[t] = (int)(pos - (long long)c * npt);
   if (cs.fxs) cs.fxs[pos] = fx[t];
@@ -336,11 +345,13 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
                                                        unsigned *status, const unsigned *gate,
                                                        const float *thr_dev) {
   __shared__ signed char s_reach[sizeof(cs.reach)];
+  __shared__ int s_run[LB_T / 32][BUILD_RUNS_MAX], s_pre[LB_T / 32][BUILD_RUNS_MAX];
   if (*gate == 0u) return;
   // thr_dev: a superset radius chosen on the device (a shared list); every
   // pair inside it is taken, without the exact band test
   const bool dev_thr = thr_dev != nullptr;
   if (dev_thr) thr_hi = thr_dev[0];
+  const float thr_row = thr_hi * (1.0f + 1e-4f);  // the row trimming's bound, with a margin for rounding
   for (int t = threadIdx.x; t < (int)sizeof(cs.reach); t += blockDim.x) s_reach[t] = cs.reach[t];
   __syncthreads();
   const int npt = g.npt;
@@ -361,66 +372,119 @@ __global__ void __launch_bounds__(LB_T) k_build_sorted(PairGeom g, int nconf, Ce
   const int x0 = cell_of(fi.x, cs.nx), y0 = cell_of(fi.y, cs.ny), z0 = cell_of(fi.z, cs.nz);
   IT *my = idx + ((long long)c * npt + i) * cap;
   int n = 0;  // the same in every lane
-  // lanes take consecutive cell-order slots (coalesced); hits keep slot order
-  // four 32-slot groups per round: their loads are issued together (the loop
-  // is otherwise bound by one L2 round trip per 32 slots)
-  auto scan = [&](int k0, int k1) {
-    for (int kb = k0; kb < k1; kb += 128) {
-      float4 fj[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int k = kb + 32 * u + lane;
-        fj[u] = k < k1 ? sp[k] : make_float4(2.f, 2.f, 2.f, 0.f);
+  // The stencil rows' runs of cell-order slots (one or two per row, the x
+  // cells wrapped) are staged first: each lane takes a row and loads its cell
+  // offsets, so that the offsets of all rows arrive in one round trip; the
+  // runs, kept in scan order, are then walked as one sequence of candidate
+  // slots, four 32-slot groups per round (their loads issued together) across
+  // run boundaries.  Hits keep the scan order (rows in (oz, oy) order, runs in
+  // x order, slots in cell order), the order of the single-row walk.
+  const int wl = threadIdx.x >> 5;
+  int *runs = s_run[wl];    // [nrun] first slot of each run
+  int *pre = s_pre[wl];     // [nrun] inclusive prefix sums of the run lengths
+  const int R = cs.R, W = 2 * R + 1, nrows = W * W;
+  auto wrap = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };  // |offset| <= R < n
+  int nrun = 0;  // the same in every lane
+  for (int q0 = 0; q0 < nrows; q0 += 32) {
+    const int q = q0 + lane;
+    int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+    if (q < nrows) {
+      const int rx = s_reach[q];
+      // the row's cells (unwrapped indices zz, yy) as far as this point can
+      // reach them: its distance to the row in y and z leaves an x extent
+      const int zz = z0 + q / W - R, yy = y0 + q % W - R;
+      const float gy = cell_gap(fi.y, yy, cs.ny) * len.y, gz = cell_gap(fi.z, zz, cs.nz) * len.z;
+      const float rem = thr_row - gy * gy - gz * gz;
+      int xa = 0, xb = -1;
+      if (rx >= 0 && rem > 0.0f) {  // else no cell of this row is within the cut-off
+        const float ex = sqrtf(rem) / len.x * (float)cs.nx;  // x extent in cells
+        const float cx = fi.x * (float)cs.nx;
+        xa = max(x0 - rx, (int)floorf(cx - ex - 1e-3f));
+        xb = min(x0 + rx, (int)floorf(cx + ex + 1e-3f));
       }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (kb + 32 * u >= k1) break;  // the same in every lane
-        const int k = kb + 32 * u + lane;
-        bool hit = false;
-        int j = 0;
-        if (k < k1) {
-          float dx = fi.x - fj[u].x, dy = fi.y - fj[u].y, dz = fi.z - fj[u].z;
-          dx = (dx - rintf(dx)) * len.x;
-          dy = (dy - rintf(dy)) * len.y;
-          dz = (dz - rintf(dz)) * len.z;
-          const float d2 = dx * dx + dy * dy + dz * dz;
-          if (d2 < thr_hi) {
-            j = si[k];
-            hit = j != i && (FULL || (i < j) == (((i + j) & 1) != 0)) && (!EXCL || (i / 3) != (j / 3)) &&
-                  (dev_thr || d2 < thr_lo || exact_pair_in(g, pi, base + (long long)j * g.pstride));
-          }
+      if (xa <= xb) {  // the x cells, wrapped into one or two runs
+        const int z = wrap(zz, cs.nz), y = wrap(yy, cs.ny);
+        const int row = (z * cs.ny + y) * cs.nx;
+        if (xa >= 0 && xb < cs.nx) {
+          a0 = st[row + xa], a1 = st[row + xb + 1];
+        } else if (xa < 0) {
+          a0 = st[row], a1 = st[row + xb + 1];
+          b0 = st[row + cs.nx + xa], b1 = st[row + cs.nx];
+        } else {
+          a0 = st[row + xa], a1 = st[row + cs.nx];
+          b0 = st[row], b1 = st[row + xb - cs.nx + 1];
         }
-        const unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (hit) {
-          const int pos = n + __popc(m & ((1u << lane) - 1u));
-          if (pos < cap) my[pos] = SLOTS ? (IT)(k | ((i / 3) == (j / 3) ? 0x8000 : 0)) : (IT)j;
-        }
-        n += __popc(m);
       }
     }
-  };
-  const int R = cs.R;
-  auto wrap = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };  // |offset| <= R < n
-  for (int oz = -R; oz <= R; ++oz) {
-    const int z = wrap(z0 + oz, cs.nz);
-    for (int oy = -R; oy <= R; ++oy) {
-      const int rx = s_reach[(oz + R) * (2 * R + 1) + (oy + R)];
-      if (rx < 0) continue;  // no cell of this row is within the cut-off
-      const int y = wrap(y0 + oy, cs.ny);
-      const int row = (z * cs.ny + y) * cs.nx;
-      const int xa = x0 - rx, xb = x0 + rx;  // the x cells, wrapped into one or two runs
-      int a0, a1, b0 = 0, b1 = 0;
-      if (xa >= 0 && xb < cs.nx) {
-        a0 = st[row + xa], a1 = st[row + xb + 1];
-      } else if (xa < 0) {
-        a0 = st[row], a1 = st[row + xb + 1];
-        b0 = st[row + cs.nx + xa], b1 = st[row + cs.nx];
-      } else {
-        a0 = st[row + xa], a1 = st[row + cs.nx];
-        b0 = st[row], b1 = st[row + xb - cs.nx + 1];
+    const bool ha = a1 > a0, hb = b1 > b0;
+    const int cnt = (int)ha + (int)hb;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    int pos = nrun + incl - cnt;
+    if (ha) runs[pos] = a0, pre[pos++] = a1 - a0;
+    if (hb) runs[pos] = b0, pre[pos] = b1 - b0;
+    nrun += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  __syncwarp();
+  // inclusive prefix of the lengths, 32 runs at a time with a carry
+  int carry = 0;
+  for (int r0 = 0; r0 < nrun; r0 += 32) {
+    const int r = r0 + lane;
+    int v = r < nrun ? pre[r] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    if (r < nrun) pre[r] = carry + v;
+    carry += __shfl_sync(0xffffffffu, v, 31);
+  }
+  __syncwarp();
+  const int total = carry;
+  int j = 0;  // this lane's run: its candidate index only grows
+  for (int kb = 0; kb < total; kb += 128) {
+    float4 fj[4];
+    int ks[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int gi = kb + 32 * u + lane;
+      ks[u] = -1;
+      fj[u] = make_float4(2.f, 2.f, 2.f, 0.f);
+      if (gi < total) {
+        while (pre[j] <= gi) ++j;
+        const int k = runs[j] + gi - (j ? pre[j - 1] : 0);
+        ks[u] = k;
+        fj[u] = sp[k];
       }
-#pragma unroll 1
-      for (int q = 0; q < 2; ++q) scan(q ? b0 : a0, q ? b1 : a1);  // one copy of the scan's code
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (kb + 32 * u >= total) break;  // the same in every lane
+      const int k = ks[u];
+      bool hit = false;
+      int jj = 0;
+      if (k >= 0) {
+        float dx = fi.x - fj[u].x, dy = fi.y - fj[u].y, dz = fi.z - fj[u].z;
+        dx = (dx - rintf(dx)) * len.x;
+        dy = (dy - rintf(dy)) * len.y;
+        dz = (dz - rintf(dz)) * len.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 < thr_hi) {
+          jj = __float_as_int(fj[u].w);
+          hit = jj != i && (FULL || (i < jj) == (((i + jj) & 1) != 0)) && (!EXCL || (i / 3) != (jj / 3)) &&
+                (dev_thr || d2 < thr_lo || exact_pair_in(g, pi, base + (long long)jj * g.pstride));
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (hit) {
+        const int pos = n + __popc(m & ((1u << lane) - 1u));
+        if (pos < cap) my[pos] = SLOTS ? (IT)(k | ((i / 3) == (jj / 3) ? 0x8000 : 0)) : (IT)jj;
+      }
+      n += __popc(m);
     }
   }
   if (lane == 0) {
