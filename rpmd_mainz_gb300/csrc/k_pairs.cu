@@ -17,6 +17,7 @@
 // accumulator slot.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "gb_common.cuh"
