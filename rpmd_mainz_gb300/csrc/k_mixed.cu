@@ -300,23 +300,28 @@ GB_D float flipf(float v, int mask) { return __int_as_float(__float_as_int(v) ^ 
 // to FP32 and this direct form differ by a few FP32 ulps.  per = lat / (2 pi).
 __global__ void k_recip_tables_mx(const double *rs, const double *q, int na, int B, int kmax, double3 per,
                                   float2 *tab) {
+  // one thread per (configuration, site, axis): the FP64 product and its
+  // two-float split once, then the K1 powers (the same FP32 operations per m
+  // as one thread per entry, without repeating the FP64 work K1 times)
   const int K1 = kmax + 1;
-  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= 3LL * na * B * K1) return;
-  const long long w = g / K1;
-  const int k = (int)(g - w * K1);
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= 3LL * na * B) return;
   const int ax = (int)(w % 3);
   const int s = (int)((w / 3) % na);
   float fh, fl;
   d2df((ax == 0 ? per.x : ax == 1 ? per.y : per.z) * rs[w], fh, fl);
-  const float kf = (float)k;
-  const float pr = kf * fh;
-  const float pe = fmaf(kf, fh, -pr);  // k fh = pr + pe exactly
-  const float t = (pr - rintf(pr)) + fmaf(kf, fl, pe);
-  float sn, cs;
-  sincospif(2.0f * t, &sn, &cs);
   const float a = ax == 0 ? __double2float_rn(q[s]) : 1.0f;
-  tab[g] = k == 0 ? make_float2(a, 0.f) : make_float2(a * cs, a * sn);
+  float2 *o = tab + w * K1;
+  o[0] = make_float2(a, 0.f);
+  for (int k = 1; k < K1; ++k) {
+    const float kf = (float)k;
+    const float pr = kf * fh;
+    const float pe = fmaf(kf, fh, -pr);  // k fh = pr + pe exactly
+    const float t = (pr - rintf(pr)) + fmaf(kf, fl, pe);
+    float sn, cs;
+    sincospif(2.0f * t, &sn, &cs);
+    o[k] = make_float2(a * cs, a * sn);
+  }
 }
 
 // SP threads share a work item, each taking MSK_G / SP of its m values (more
@@ -702,8 +707,8 @@ void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const d
   float2 *tab = reinterpret_cast<float2 *>(c->ktab);
   const double3 lat = recip_lat(c);
   const double ot = 0.5 / std::acos(-1.0);
-  k_recip_tables_mx<<<nblk(nw * (kmax + 1), 256), 256, 0, s>>>(rs, q, c->na, B, kmax,
-                                                               make_double3(lat.x * ot, lat.y * ot, lat.z * ot), tab);
+  k_recip_tables_mx<<<nblk(nw, 128), 128, 0, s>>>(rs, q, c->na, B, kmax,
+                                                 make_double3(lat.x * ot, lat.y * ot, lat.z * ot), tab);
   const int nchunk = (c->na + MSK_CHUNK - 1) / MSK_CHUNK;
   // GBRPMD_SK_TC=1 puts the structure factors on the tensor cores (k_recip_tc.cu;
   // kmax < 16): measured at 4096 H2O, nb = 32 it takes 24-34 us per launch
