@@ -521,7 +521,7 @@ GB_D void gb_hc2r_quad32(int q, In in, Out out, const float *__restrict__ tw8, c
   for (int k = 0; k < 8; ++k) z[k] = 0.f;
 #pragma unroll
   for (int x = 0; x < 4; ++x) {
-    const int s = q ^ x;  // destination lane of this round's values
+    const int s = q ^ x;  // destination lane of this exchange step's values
     // G_s = F_0 + i^s F_1 + (-1)^s F_2 + (-i)^s F_3
     float t1r, t1i, t2r, t2i, t3r, t3i;
     gb_rot_mi(3 * s, f1r, f1i, t1r, t1i);
