@@ -763,6 +763,8 @@ void force_launch(cudaStream_t s, gb_context *c, int B, double *g) {
 
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
   if (c->nkp == 0) return;
+  static const bool tc = [] { const char *v = std::getenv("GBRPMD_RF_TC"); return v && v[0] == '1'; }();
+  if (tc && launch_recip_force_tc(s, c, B, g)) return;
   const bool zr = c->P.kmax < MF_KZ;  // z powers in registers
   const int v = (c->tune.rf_g == 16 ? 4 : 0) + (c->tune.rf_ns == 2 ? 2 : 0) + (zr ? 1 : 0);
   switch (v) {

@@ -187,3 +187,23 @@ def test_shared_centroid_list_matches_per_bead_lists(monkeypatch, case):
     # dynamics (a missed pair would show in the forces above at once)
     assert rel(ra, rb) < 1e-7 and rel(pa, pb) < 1e-4 and rel(fa, fb) < 1e-4, (rel(ra, rb), rel(pa, pb), rel(fa, fb))
     assert nra[0] >= 1  # the shared list was built (and rebuilt) on the device
+
+
+@pytest.mark.parametrize("case", [
+    dict(param="param_qspcfw", ncell=(6, 6, 6), nb=8),
+    dict(param="param_qspcfw", ncell=(16, 16, 16), nb=4, mts=5, dtfs=1.25, nbdf1=1, nbdf2=3),
+])
+def test_mixed_force_pass_on_tensor_cores(monkeypatch, case):
+    """GBRPMD_RF_TC=1: the k-space force pass as split-TF32 mma.sync products
+    (k_recip_tc.cu) keeps the mixed path's bounds and agrees with the CUDA-core
+    force pass."""
+    s = systems.build(**case)
+    r = systems.perturbed(s, seed=151)
+    f64, fcc = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
+    monkeypatch.setenv("GBRPMD_RF_TC", "1")
+    _, ftc = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
+    monkeypatch.delenv("GBRPMD_RF_TC")
+    assert rel(ftc["dvdr"], f64["dvdr"]) < FORCE_TOL
+    assert rel(ftc["dvdr"], fcc["dvdr"]) < FORCE_TOL
+    for k in ("v", "vew"):
+        assert abs(ftc[k] - f64[k]) <= ENERGY_TOL * abs(f64[k]) + 1e-12, (k, ftc[k], f64[k])
