@@ -120,9 +120,10 @@ void launch_recip_sk_mx(cudaStream_t s, gb_context *c, const double *rs, const d
 // false (nothing launched) when kmax is beyond its tiles
 bool launch_recip_sk_tc(cudaStream_t s, gb_context *c, int B, int nchunk);
 int recip_sk_tc_chunk();
-// the force pass on the tensor cores (k_recip_tc.cu; GBRPMD_RF_TC=1); false
-// (nothing launched) when kmax is beyond its K of 32
+// the force pass on the tensor cores (k_recip_tc.cu; the default, GBRPMD_RF_TC=0
+// for the CUDA-core pass); false (nothing launched) when kmax is beyond its K of 32
 bool launch_recip_force_tc(cudaStream_t s, gb_context *c, int B, double *g);
+bool recip_force_tc_on(const gb_context *c);  // the mixed force pass runs on the tensor cores
 void launch_recip_weights_mx(cudaStream_t s, gb_context *c, int B, double *acc);
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g);
 void recip_set_attributes_mx();

@@ -761,10 +761,17 @@ void force_launch(cudaStream_t s, gb_context *c, int B, double *g) {
         reinterpret_cast<const float4 *>(c->sk), recip_lat(c), g);
 }
 
+bool recip_force_tc_on(const gb_context *c) {
+  const char *v = std::getenv("GBRPMD_RF_TC");
+  return !(v && v[0] == '0') && c->P.kmax + 1 <= 16;
+}
+
 void launch_recip_force_mx(cudaStream_t s, gb_context *c, int B, double *g) {
   if (c->nkp == 0) return;
-  static const bool tc = [] { const char *v = std::getenv("GBRPMD_RF_TC"); return v && v[0] == '1'; }();
-  if (tc && launch_recip_force_tc(s, c, B, g)) return;
+  // the force pass on the tensor cores (k_recip_tc.cu) unless GBRPMD_RF_TC=0
+  // asks for the CUDA-core pass below (also taken when kmax + 1 > 16)
+  const char *tcv = std::getenv("GBRPMD_RF_TC");
+  if (!(tcv && tcv[0] == '0') && launch_recip_force_tc(s, c, B, g)) return;
   const bool zr = c->P.kmax < MF_KZ;  // z powers in registers
   const int v = (c->tune.rf_g == 16 ? 4 : 0) + (c->tune.rf_ns == 2 ? 2 : 0) + (zr ? 1 : 0);
   switch (v) {

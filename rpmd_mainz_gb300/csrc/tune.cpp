@@ -32,6 +32,7 @@
 
 int ctx_set_error(int code, const std::string &msg);
 int ctx_check_cuda(cudaError_t e, const char *what);
+bool recip_force_tc_on(const gb_context *c);  // k_mixed.cu
 
 namespace {
 
@@ -240,18 +241,20 @@ int gbrpmd_ctx_autotune(gb_context *c, double dt, double beta, int steps, double
       probe(cand);
     }
     baseline(PR_RECIP_F);
-    for (int g : {8, 16})
-      for (int ns : {1, 2}) {
-        if (g == best.tune.rf_g && ns == best.tune.rf_ns) continue;
+    if (!recip_force_tc_on(c)) {  // the CUDA-core pass's shapes (the tensor-core pass has none to tune)
+      for (int g : {8, 16})
+        for (int ns : {1, 2}) {
+          if (g == best.tune.rf_g && ns == best.tune.rf_ns) continue;
+          Shape cand = best;
+          cand.tune.rf_g = g;
+          cand.tune.rf_ns = ns;
+          probe(cand);
+        }
+      for (int ks : {2, 3, 4, 6}) {
         Shape cand = best;
-        cand.tune.rf_g = g;
-        cand.tune.rf_ns = ns;
+        cand.tune.rf_ks = ks;
         probe(cand);
       }
-    for (int ks : {2, 3, 4, 6}) {
-      Shape cand = best;
-      cand.tune.rf_ks = ks;
-      probe(cand);
     }
   }
   baseline(PR_MTS);

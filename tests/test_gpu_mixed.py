@@ -194,14 +194,14 @@ def test_shared_centroid_list_matches_per_bead_lists(monkeypatch, case):
     dict(param="param_qspcfw", ncell=(16, 16, 16), nb=4, mts=5, dtfs=1.25, nbdf1=1, nbdf2=3),
 ])
 def test_mixed_force_pass_on_tensor_cores(monkeypatch, case):
-    """GBRPMD_RF_TC=1: the k-space force pass as split-TF32 mma.sync products
-    (k_recip_tc.cu) keeps the mixed path's bounds and agrees with the CUDA-core
-    force pass."""
+    """The k-space force pass as split-TF32 mma.sync products (k_recip_tc.cu,
+    the default) keeps the mixed path's bounds and agrees with the CUDA-core
+    force pass (GBRPMD_RF_TC=0)."""
     s = systems.build(**case)
     r = systems.perturbed(s, seed=151)
-    f64, fcc = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
-    monkeypatch.setenv("GBRPMD_RF_TC", "1")
-    _, ftc = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
+    f64, ftc = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
+    monkeypatch.setenv("GBRPMD_RF_TC", "0")
+    _, fcc = both(s, lambda: lib.full_forces(r, s["box"], s["z"]))
     monkeypatch.delenv("GBRPMD_RF_TC")
     assert rel(ftc["dvdr"], f64["dvdr"]) < FORCE_TOL
     assert rel(ftc["dvdr"], fcc["dvdr"]) < FORCE_TOL
