@@ -671,6 +671,7 @@ void launch_ewald_real_mx(cudaStream_t s, const int4 *fx, const int4 *fxs, int n
       k_ewald_real_mx<NP, int, false><<<grid, MX_T, 0, s>>>(fx, fx, na, pl.count, pl.idx, pl.cap, (float)alpha, sfac,
                                                             (float)rcutsq, bx, g, acc, add ? 1 : 0, npair, lconf);
   };
+  if (const char *e = std::getenv("GBRPMD_EW_NP")) np = std::atoi(e);  // fixed lanes per site (measurements)
   if (np == 8) go(std::integral_constant<int, 8>());
   else if (np == 32) go(std::integral_constant<int, 32>());
   else go(std::integral_constant<int, 16>());
