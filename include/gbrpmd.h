@@ -56,7 +56,8 @@ extern "C" {
 /* barostat selector (module barostat, `baro`, module_barostat.f90:5), used when
    evolve_pi is called with nbaro = 1 (md_eq.f90:55-58: ens = 'NPT') */
 #define GB_BARO_NONE 0
-#define GB_BARO_BER 1   /* Berendsen, beren_baro (module_barostat.f90:88-129), cubic boxes */
+#define GB_BARO_BER 1   /* Berendsen, beren_driver (module_barostat.f90:8-129): beren_baro on cubic
+                           boxes, beren_baro_nc (one scale per axis) on the others */
 #define GB_BARO_MCI 2   /* Monte Carlo volume moves (mc_baro): not on the device path  */
 
 /* intramolecular model selector */
@@ -187,8 +188,9 @@ int gbrpmd_full_forces(double *r, const int *na, const int *nb, double *v, doubl
    boxlxyz,z,beta,vir,vir_lf,irun,nbaro)  (evolve_pi.f90:1-322): one outer
    multiple-time-step RPMD step in the normal-mode representation, with the
    PRG / PRL thermostat kicks (drawing the process-wide random stream with irun)
-   and, for nbaro = 1, the Berendsen barostat (baro = GB_BARO_BER, cubic box),
-   which scales boxlxyz in place and reads vir_lf as the previous call left it. */
+   and, for nbaro = 1, the Berendsen barostat (baro = GB_BARO_BER; isotropic
+   on cubic boxes, per axis on the others), which scales boxlxyz in place and
+   reads vir_lf as the previous call left it. */
 int gbrpmd_evolve_pi(double *p, double *r, double *v, double *vew, double *vlj,
                      double *vint, double *dvdr, double *dvdr2, const double *dt,
                      const double *mass, const int *na, const int *nb, double *boxlxyz,
@@ -221,7 +223,10 @@ int gbrpmd_rattle_set_itmax(const int *itmax);
 /* replaces subroutine evolve_rig_pi(p,r,v,v_lf,v_hf,dvdr,dvdr2,dt,mass,na,nb,
    boxlxyz,z,beta,vir,vir_lf,irun,nbaro)  (evolve_rigid.f90:100-224): rigid
    ring-polymer step with primitive bead springs and RATTLE, with the PRG / PRL
-   thermostat kicks.  nbaro must be 0 (its barostat is not on the device path). */
+   thermostat kicks, and, for nbaro = 1, the Berendsen barostat on the bead
+   positions after the step (evolve_rigid.f90:203-213; baro = GB_BARO_BER),
+   which reads vir = vir_lf + vir_hf + the caller's vir (the value returned)
+   and scales boxlxyz in place; v and vir_lf are those of the box before it. */
 int gbrpmd_evolve_rig_pi(double *p, double *r, double *v, double *v_lf, double *v_hf,
                          double *dvdr, double *dvdr2, const double *dt, const double *mass,
                          const int *na, const int *nb, double *boxlxyz, const double *z,
@@ -316,7 +321,9 @@ int gbrpmd_ctx_set_rng(gb_context *ctx, int idum);
 int gbrpmd_ctx_set_rng_mode(gb_context *ctx, int mode, uint64_t seed);
 /* evolve_pi's nbaro for gbrpmd_ctx_evolve / gbrpmd_run_md_eq on this context
    (md_eq.f90:55-58: 1 when ens = 'NPT'): the Berendsen barostat scales the box
-   and the water centroids inside every step (one synchronisation per step). */
+   and the water centroids inside every step (one synchronisation per step).
+   Rigid water: the virial the barostat reads accumulates over the context's
+   barostat steps, as the caller's vir does over evolve_rig_pi calls. */
 int gbrpmd_ctx_set_nbaro(gb_context *ctx, int nbaro);
 /* the context's current box (changed by the barostat) */
 int gbrpmd_ctx_box(gb_context *ctx, double *box3);

@@ -95,7 +95,11 @@ void virial_ke(const double *r, const double *dvdr, const double *dvdr2, double 
                double tvxyz[3], double &tq1, double &tq2, double beta, int na, int nb);
 void kinetic_rpmd(const double *p, int na, double &tk, const double *mass, int nb);
 double pressure(const double vir[9], double tv, int na, const double box[3]);
+double pres_lj_tail(const double box[3], int na);
 void beren_baro(const double vir[9], double tv, double dt, double *r, double box[3], int na, int nb);
+void beren_baro_nc(const double vir[9], const double tvxyz[3], double dt, double *r, double box[3], int na, int nb);
+void beren_driver(const double vir[9], double tv, const double tvxyz[3], double dt, double *r, double box[3], int na,
+                  int nb);
 // md_eq's step loops (md_eq.f90:55-323) without file output: for ens != NVT
 // the nq-step NVT pre-equilibration, then ne steps with nbaro = npt; per step
 // the values md_eq prints (see orc_md_eq)

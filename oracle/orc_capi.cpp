@@ -76,6 +76,11 @@ void orc_virial_ke(const double *r, const double *dvdr, const double *dvdr2, dou
                    double *tvxyz, double *tq1, double *tq2, double beta, int na, int nb) {
   virial_ke(r, dvdr, dvdr2, *tv, tvxyz, *tq1, *tq2, beta, na, nb);
 }
+double orc_pressure(const double *vir, double tv, int na, const double *box) { return pressure(vir, tv, na, box); }
+void orc_beren_driver(const double *vir, double tv, const double *tvxyz, double dt, double *r, double *box, int na,
+                      int nb) {
+  beren_driver(vir, tv, tvxyz, dt, r, box, na, nb);
+}
 void orc_kinetic_rpmd(const double *p, int na, double *tk, const double *mass, int nb) {
   kinetic_rpmd(p, na, *tk, mass, nb);
 }

@@ -3,8 +3,9 @@
 //
 // Restates evolve_pi.f90, kinetic.f90 (virial_ke, kinetic_rpmd),
 // module_thermostat.f90 (sample_rpmd, pshift, parinello_therm,
-// parinello_therm_loc), md_rattle.f90 and evolve_rigid.f90 (evolve_rig_pi,
-// bead_forces).
+// parinello_therm_loc), module_barostat.f90 (beren_driver, beren_baro,
+// beren_baro_nc), md_pressure.f90 (pressure, pres_lj_tail), md_rattle.f90 and
+// evolve_rigid.f90 (evolve_rig_pi, bead_forces).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -286,20 +287,24 @@ void parinello_therm_loc(double *p, const double *mass, double tau, int na, int 
     }
 }
 
-// pressure (md_pressure.f90:1-30) with pres_lj_tail (md_pressure.f90:32-56)
+// pres_lj_tail (md_pressure.f90:37-56): LJ tail correction to the pressure
+double pres_lj_tail(const double box[3], int na) {
+  int nm = na / 3;
+  double pi = std::acos(-1.0);
+  double vol = box[0] * box[1] * box[2];
+  double rho = (double)nm / vol;
+  double prefac = (16.0 * pi * (rho * rho) * P.oo_eps * (P.oo_sig * P.oo_sig * P.oo_sig)) / 3.0;
+  return prefac * ((2.0 / 3.0) * std::pow(P.oo_sig / P.rcut, 9) - std::pow(P.oo_sig / P.rcut, 3));
+}
+
+// pressure (md_pressure.f90:1-30) with pres_lj_tail
 double pressure(const double vir[9], double tv, int na, const double box[3]) {
   double w = vir[0] + vir[4] + vir[8];
   w = -w / 3.0;
   double vol = box[0] * box[1] * box[2];
   double pres = (2.0 * tv / 3.0 + w) / vol;
   double ptail = 0.0;
-  if (P.oo_gam == 0.0) {
-    int nm = na / 3;
-    double pi = std::acos(-1.0);
-    double rho = (double)nm / vol;
-    double prefac = (16.0 * pi * (rho * rho) * P.oo_eps * (P.oo_sig * P.oo_sig * P.oo_sig)) / 3.0;
-    ptail = prefac * ((2.0 / 3.0) * std::pow(P.oo_sig / P.rcut, 9) - std::pow(P.oo_sig / P.rcut, 3));
-  }
+  if (P.oo_gam == 0.0) ptail = pres_lj_tail(box, na);
   return pres + ptail;
 }
 
@@ -328,6 +333,50 @@ void beren_baro(const double vir[9], double tv, double dt, double *r, double box
         double *q = r + 3 * ((size_t)(3 * i + a) + (size_t)na * k);
         for (int x = 0; x < 3; ++x) q[x] = q[x] + rcm[3 * (size_t)i + x] * (scale - 1.0);
       }
+}
+
+// beren_baro_nc (module_barostat.f90:28-86): each box axis scaled by the
+// pressure along it, (-vir(j,j) + 2 tvxyz(j)) / vol plus the LJ tail (the
+// reference skips the tail for oo_gam != 0 and for RPMDDFT runs, which this
+// path does not have), and each water's center_water vector per axis
+void beren_baro_nc(const double vir[9], const double tvxyz[3], double dt, double *r, double box[3], int na, int nb) {
+  double ptail = 0.0;
+  if (P.oo_gam == 0.0) ptail = pres_lj_tail(box, na);
+  double vol = box[0] * box[1] * box[2];
+  double pres[3];
+  for (int j = 0; j < 3; ++j) {
+    pres[j] = (-vir[4 * j] + 2.0 * tvxyz[j]) / vol;
+    pres[j] = pres[j] + ptail;
+  }
+  int nm = na / 3;
+  double compi = 13531.0;
+  double bstat = compi / (3.0 * P.taub);
+  double scale[3];
+  for (int j = 0; j < 3; ++j) scale[j] = std::fabs(1.0 - (dt * bstat) * (P.patm - pres[j]));
+  for (int j = 0; j < 3; ++j) box[j] = scale[j] * box[j];
+  std::vector<double> rcm(3 * (size_t)nm, 0.0);
+  double wt = 1.0 / (double)nb;
+  for (int i = 0; i < nm; ++i) {
+    double pc[3] = {0, 0, 0};
+    for (int k = 0; k < nb; ++k) {
+      const double *q = r + 9 * (size_t)i + 3 * (size_t)na * k;
+      for (int x = 0; x < 3; ++x) pc[x] = pc[x] + q[x] + q[3 + x] + q[6 + x];
+    }
+    for (int x = 0; x < 3; ++x) rcm[3 * (size_t)i + x] = pc[x] * wt;
+  }
+  for (int i = 0; i < nm; ++i)
+    for (int k = 0; k < nb; ++k)
+      for (int a = 0; a < 3; ++a) {
+        double *q = r + 3 * ((size_t)(3 * i + a) + (size_t)na * k);
+        for (int j = 0; j < 3; ++j) q[j] = q[j] + rcm[3 * (size_t)i + j] * (scale[j] - 1.0);
+      }
+}
+
+// beren_driver (module_barostat.f90:8-26)
+void beren_driver(const double vir[9], double tv, const double tvxyz[3], double dt, double *r, double box[3], int na,
+                  int nb) {
+  if (P.iamcub) beren_baro(vir, tv, dt, r, box, na, nb);
+  else beren_baro_nc(vir, tvxyz, dt, r, box, na, nb);
 }
 
 // evolve_pi (evolve_pi.f90:1-322), type = 'RPMD'
@@ -393,8 +442,8 @@ Status evolve_pi(double *p, double *r, double &v, double &vew, double &vlj, doub
   if (tv_out) *tv_out = tv;
 
   if (nbaro == 1) {  // evolve_pi.f90:176-189: beren_driver on the bead positions rst
-    if (P.baro != GB_BARO_BER || !P.iamcub) return GB_E_UNSUPPORTED;  // mc_baro, beren_baro_nc
-    beren_baro(vir, tv, dt, rst.data(), box, na, nb);
+    if (P.baro != GB_BARO_BER) return GB_E_UNSUPPORTED;  // mc_baro
+    beren_driver(vir, tv, tvxyz, dt, rst.data(), box, na, nb);
     std::memcpy(r, rst.data(), sizeof(double) * N);
     realft(r, 3 * na, nb, +1);
   }
@@ -623,7 +672,9 @@ void bead_forces(const double *r, int na, int nb, double *dvdrb, double beta,
   }
 }
 
-// evolve_rig_pi (evolve_rigid.f90:100-224)
+// evolve_rig_pi (evolve_rigid.f90:100-224); with nbaro = 1 the Berendsen
+// barostat on the bead positions, its kinetic term from virial_ke with the
+// zeroed dvdr2 (evolve_rigid.f90:203-213)
 Status evolve_rig_pi(const Rattle &rt, double *p, double *r, double &v, double &v_lf,
                      double &v_hf, double *dvdr, double *dvdr2, double dt, const double *mass,
                      int na, int nb, double box[3], const double *z, double beta,
@@ -675,7 +726,12 @@ Status evolve_rig_pi(const Rattle &rt, double *p, double *r, double &v, double &
   for (int i = 0; i < 9; ++i) vir_hf[i] = vir_hf[i] / (double)nb;
   for (int i = 0; i < 9; ++i) vir[i] = vir_lf[i] + vir_hf[i] + vir[i];
   std::memset(dvdr2, 0, sizeof(double) * N);
-  if (nbaro == 1) return GB_E_UNSUPPORTED;
+  if (nbaro == 1) {
+    if (P.baro != GB_BARO_BER) return GB_E_UNSUPPORTED;  // mc_baro
+    double tv, tvxyz[3], tq1, tq2;
+    virial_ke(r, dvdr, dvdr2, tv, tvxyz, tq1, tq2, beta, na, nb);
+    beren_driver(vir, tv, tvxyz, dt, r, box, na, nb);
+  }
   v_lf = v;
   v_hf = 0.0;
   return GB_OK;

@@ -752,6 +752,7 @@ int gbrpmd_evolve_rig_pi(double *p, double *r, double *v, double *v_lf, double *
   c->th_rng = nullptr;
   c->th_idum = nullptr;
   if (st) return st;
+  std::memcpy(boxlxyz, c->box, sizeof(double) * 3);  // scaled by the barostat
   if ((st = download(c, p, c->p, N)) || (st = download(c, r, c->r, N)) ||
       (st = download(c, dvdr, c->dvdr, N)) || (st = download(c, dvdr2, c->dvdr2, N)))
     return st;

@@ -184,6 +184,12 @@ struct gb_context {
   double e_v = 0, e_vew = 0, e_vlj = 0, e_vint = 0, e_tv = 0;
   double e_vir[9] = {0}, e_vir_lf[9] = {0}, e_vir_hf[9] = {0};
   double vir_lf_in[9] = {0};
+  // rigid water with the barostat on a resident context: the virial the
+  // barostat reads (evolve_rigid.f90:200, vir = vir_lf + vir_hf + vir, the
+  // caller's vir accumulating over the calls; md_eq zeroes it once,
+  // md_eq.f90:60) accumulates here over the context's barostat steps
+  double rig_vir[9] = {0};
+  double acc_L = 0.0;  // box[0] of the last Ewald term launched (its sums are in that unit box)
 
   int64_t launches = 0;
   std::vector<void *> allocs;
@@ -288,3 +294,6 @@ size_t ctx_device_bytes(const gb_context *c);  // device bytes the context holds
 void dev_graph_reset(gb_context *c);
 int dev_forces(gb_context *c, const double *r, int B, double *out, int iopt);  // drop-in `forces`
 int dev_collect(gb_context *c, int mode, double dt, double beta);  // sync, read accumulators
+// beren_driver (module_barostat.f90:8-26): box on the host, waters of r (and
+// the centroid row of rnm, when given) on the device
+int beren_driver(gb_context *c, const double vir[9], double tv, const double tvxyz[3], double dt, double *rnm);

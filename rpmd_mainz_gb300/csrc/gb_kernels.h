@@ -163,7 +163,7 @@ void launch_prl_dev(cudaStream_t s, double *p, const double *mass, int na, int n
 void launch_prg_draw(cudaStream_t s, long long ndof, const unsigned long long *ctr, unsigned long long seed,
                      double *aux);
 void launch_ctr_next(cudaStream_t s, unsigned long long *ctr);
-void launch_baro_shift(cudaStream_t s, double *r, double *rnm, int na, int nb, double sm1);
+void launch_baro_shift(cudaStream_t s, double *r, double *rnm, int na, int nb, const double sm1[3]);
 // md_eq's output-step estimators (k_est.cu): acc[14] sums, optional rcm / mdip [nm][3]
 void launch_estimators(cudaStream_t s, const double *r, const double *p, const double *dvdr, const double *dvdr2,
                        const double *mass, const double *z, int na, int nb, double alpha, double *acc, double *rcm,

@@ -458,8 +458,8 @@ int dev_rattle_s2(double *r, double *p, int nm, const double *mass, double dt, d
 int term_forces_rigid(gb_context *c);  // step.cpp: forces(r, v, dvdr, nb, ..., 1)
 
 int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) {
-  (void)vir_inout;
-  if (c->nbaro) return ctx_set_error(GB_E_UNSUPPORTED, "barostats of evolve_rig_pi are not on the device path");
+  if (c->nbaro && c->P.baro != GB_BARO_BER)
+    return ctx_set_error(GB_E_UNSUPPORTED, "only the Berendsen barostat (baro = BER) is on the device path");
   if (3 * c->nm != c->P.nctot) return ctx_set_error(GB_E_ARG, "number of bonds inconsistent in shake/rattle routine");
   const int nb = c->nb, nm = c->nm;
   const long long N = 3LL * c->na * nb;
@@ -496,5 +496,28 @@ int dev_evolve_rig_pi(gb_context *c, double dt, double beta, double *vir_inout) 
   c->launches += 6;
   if ((st = therm_kick(c, halfdt, beta))) return st;  // evolve_rigid.f90:192-196
   CK(cudaGetLastError());
+  if (c->nbaro) {
+    // Berendsen barostat (evolve_rigid.f90:203-213): vir = vir_lf + vir_hf +
+    // the caller's vir; tv, tvxyz from virial_ke with the zeroed dvdr2 (one
+    // call, kinetic.f90:1-54); the accumulators are read on the host
+    double *ke = c->acc + (size_t)ACC_KE * ACC_STRIDE;
+    CK(cudaMemsetAsync(ke, 0, sizeof(double) * ACC_STRIDE, s));
+    launch_virial_ke(s, c->r, c->dvdr, c->dvdr2, c->na, nb, ke);
+    c->launches += 1;
+    if ((st = dev_collect(c, 2, dt, beta))) return st;
+    double *vin = vir_inout ? vir_inout : c->rig_vir;
+    double vir[9];
+    for (int i = 0; i < 9; ++i) vir[i] = c->e_vir_lf[i] + c->e_vir_hf[i] + vin[i];
+    if (!vir_inout)  // the drop-in caller updates its own vir
+      for (int i = 0; i < 9; ++i) c->rig_vir[i] = vir[i];
+    const double *K = c->h_acc + (size_t)ACC_KE * ACC_STRIDE;
+    const double tq1 = 0.5 * K[0] / nb, tq2 = 0.5 * K[1] / nb;
+    const double tc = 0.5 * (3 * c->na - 3 - c->P.nctot) / beta;
+    const double tv = tc + tq1 + tq2;
+    double tvxyz[3];
+    for (int j = 0; j < 3; ++j) tvxyz[j] = tc / 3 + 0.5 * K[2 + j] / nb + 0.5 * K[5 + j] / nb;
+    if ((st = beren_driver(c, vir, tv, tvxyz, dt, nullptr))) return st;
+    CK(cudaGetLastError());
+  }
   return GB_OK;
 }

@@ -121,13 +121,14 @@ __global__ void __launch_bounds__(256) k_prg_scale(double *__restrict__ p, long 
     p[i] = alpha * p[i];
 }
 
-// beren_baro's molecule shift (module_barostat.f90:111-126): every atom of water
-// m on every bead moves by rcm_m (scale - 1), rcm = center_water
+// beren_baro's molecule shift (module_barostat.f90:111-126; per axis in
+// beren_baro_nc, 67-82): every atom of water m on every bead moves by
+// rcm_m (scale - 1), scale of the axis, rcm = center_water
 // (md_tools.f90:367-390: the bead average of the sum of the three atoms'
 // positions).  The shift is the same on every bead, so in the normal-mode
 // positions rnm (when given) only the centroid row changes, by sqrt(nb) times it.
 __global__ void __launch_bounds__(128) k_baro_shift(double *__restrict__ r, double *__restrict__ rnm, int nm, int nb,
-                                                    double sm1, double sqnb) {
+                                                    double3 sm1, double sqnb) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= 3 * nm) return;
   const int m = idx / 3, x = idx % 3;
@@ -136,7 +137,7 @@ __global__ void __launch_bounds__(128) k_baro_shift(double *__restrict__ r, doub
   double pc = 0.0;
   for (int k = 0; k < nb; ++k) pc = pc + r[o + S * k] + r[o + 3 + S * k] + r[o + 6 + S * k];
   pc = pc * (1.0 / (double)nb);
-  const double d = __dmul_rn(pc, sm1);
+  const double d = __dmul_rn(pc, x == 0 ? sm1.x : x == 1 ? sm1.y : sm1.z);
   for (int k = 0; k < nb; ++k)
 #pragma unroll
     for (int a = 0; a < 3; ++a) r[o + 3 * a + S * k] = r[o + 3 * a + S * k] + d;
@@ -180,7 +181,8 @@ void launch_prg_draw(cudaStream_t s, long long ndof, const unsigned long long *c
 
 void launch_ctr_next(cudaStream_t s, unsigned long long *ctr) { k_ctr_next<<<1, 1, 0, s>>>(ctr); }
 
-void launch_baro_shift(cudaStream_t s, double *r, double *rnm, int na, int nb, double sm1) {
+void launch_baro_shift(cudaStream_t s, double *r, double *rnm, int na, int nb, const double sm1[3]) {
   const int nm = na / 3;
-  k_baro_shift<<<nblk(3LL * nm, 128), 128, 0, s>>>(r, rnm, nm, nb, sm1, sqrt((double)nb));
+  k_baro_shift<<<nblk(3LL * nm, 128), 128, 0, s>>>(r, rnm, nm, nb, make_double3(sm1[0], sm1[1], sm1[2]),
+                                                   sqrt((double)nb));
 }

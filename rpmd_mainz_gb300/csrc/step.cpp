@@ -371,6 +371,7 @@ int term_ewald(gb_context *c, const double *r, int B, double *out, double sign, 
   const int na = c->na;
   const bool cub = c->P.iamcub != 0;
   const double L = c->box[0], onboxl = 1.0 / L;
+  c->acc_L = L;  // the box the accumulated Ewald sums are scaled by (dev_collect)
   const double pscale = cub ? onboxl : 1.0, gscale = cub ? onboxl * onboxl : 1.0;
   prof_begin(c, PR_MSITE);
   launch_msite(c->stream, r, c->rs, na, B, c->P.alpha, pscale, c->g);  // and g = 0
@@ -909,42 +910,73 @@ int therm_kick(gb_context *c, double dtk, double beta) {
   return GB_OK;
 }
 
-// Berendsen barostat of evolve_pi with nbaro = 1 (evolve_pi.f90:163-189):
-// pressure from this step's MTS-averaged virial kinetic energy and virial
-// (the previous call's vir_lf plus this step's high-frequency virial), box and
-// water centroids scaled (beren_baro, module_barostat.f90:88-129).  Needs the
-// step's accumulators on the host: one synchronisation.
+// beren_driver (module_barostat.f90:8-26) on the context's bead positions r
+// (and the centroid row of the normal-mode positions rnm, when given): the
+// pressure from vir and the virial kinetic energy tv (beren_baro,
+// module_barostat.f90:88-129, with pressure, md_pressure.f90:1-30) or, on
+// non-cubic boxes, one pressure per axis from the virial's diagonal and tvxyz
+// (beren_baro_nc, module_barostat.f90:28-86); the LJ tail (pres_lj_tail,
+// md_pressure.f90:37-56) unless the O-O term is Buckingham.  The box scales on
+// the host, the waters on the device.
+int beren_driver(gb_context *c, const double vir[9], double tv, const double tvxyz[3], double dt, double *rnm) {
+  const gb_params &P = c->P;
+  if (P.baro != GB_BARO_BER)
+    return ctx_set_error(GB_E_UNSUPPORTED, "only the Berendsen barostat (baro = BER) is on the device path");
+  const int na = c->na, nm = na / 3;
+  const double vol = c->box[0] * c->box[1] * c->box[2];
+  double ptail = 0.0;
+  if (P.oo_gam == 0.0) {
+    const double pi = std::acos(-1.0), rho = (double)nm / vol;
+    const double prefac = (16.0 * pi * (rho * rho) * P.oo_eps * (P.oo_sig * P.oo_sig * P.oo_sig)) / 3.0;
+    ptail = prefac * ((2.0 / 3.0) * std::pow(P.oo_sig / P.rcut, 9) - std::pow(P.oo_sig / P.rcut, 3));
+  }
+  double pres[3];
+  if (P.iamcub) {
+    double w = vir[0] + vir[4] + vir[8];
+    w = -w / 3.0;
+    const double pc = (2.0 * tv / 3.0 + w) / vol + ptail;
+    pres[0] = pres[1] = pres[2] = pc;
+  } else {
+    for (int j = 0; j < 3; ++j) pres[j] = (-vir[4 * j] + 2.0 * tvxyz[j]) / vol + ptail;
+  }
+  const double compi = 13531.0, bstat = compi / (3.0 * P.taub);
+  double sm1[3];
+  for (int j = 0; j < 3; ++j) {
+    const double scale = std::fabs(1.0 - (dt * bstat) * (P.patm - pres[j]));
+    c->box[j] = scale * c->box[j];
+    sm1[j] = scale - 1.0;
+  }
+  launch_baro_shift(c->stream, c->r, rnm, na, c->nb, sm1);
+  c->launches += 1;
+  return GB_OK;
+}
+
+// Barostat of evolve_pi with nbaro = 1 (evolve_pi.f90:163-189): tv and tvxyz
+// averaged over the MTS substeps, the virial as the previous call's vir_lf
+// plus this step's high-frequency virial.  Needs the step's accumulators on
+// the host: one synchronisation.
 int barostat(gb_context *c, double dt) {
   const gb_params &P = c->P;
   if (P.baro != GB_BARO_BER)
     return ctx_set_error(GB_E_UNSUPPORTED, "only the Berendsen barostat (baro = BER) is on the device path");
-  if (!P.iamcub) return ctx_set_error(GB_E_UNSUPPORTED, "beren_baro_nc (non-cubic boxes) is not on the device path");
   CK(cudaMemcpyAsync(c->h_acc, c->acc, sizeof(double) * ACC_NSLOT * ACC_STRIDE, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   const double *A = c->h_acc;
-  const int na = c->na, nb = c->nb, mts = P.mts, nm = na / 3;
+  const double *K = A + (size_t)ACC_KE * ACC_STRIDE;
+  const int na = c->na, nb = c->nb, mts = P.mts;
   double vir[9];
   for (int i = 0; i < 9; ++i)
     vir[i] = c->vir_lf_in[i] + A[(size_t)ACC_INT * ACC_STRIDE + 1 + i] / nb / (double)mts;
-  const double tq1 = 0.5 * A[(size_t)ACC_KE * ACC_STRIDE + 0] / nb, tq2 = 0.5 * A[(size_t)ACC_KE * ACC_STRIDE + 1] / nb;
+  const double tq1 = 0.5 * K[0] / nb, tq2 = 0.5 * K[1] / nb;
   const double tc = 0.5 * (3 * na - 3 - P.nctot) / c->last_beta;
   const double tv = tc + (tq1 + tq2) / mts;
-  // pressure (md_pressure.f90:1-56)
-  double w = vir[0] + vir[4] + vir[8];
-  w = -w / 3.0;
-  const double vol = c->box[0] * c->box[1] * c->box[2];
-  double pres = (2.0 * tv / 3.0 + w) / vol;
-  if (P.oo_gam == 0.0) {
-    const double pi = std::acos(-1.0), rho = (double)nm / vol;
-    const double prefac = (16.0 * pi * (rho * rho) * P.oo_eps * (P.oo_sig * P.oo_sig * P.oo_sig)) / 3.0;
-    pres = pres + prefac * ((2.0 / 3.0) * std::pow(P.oo_sig / P.rcut, 9) - std::pow(P.oo_sig / P.rcut, 3));
-  }
-  const double compi = 13531.0, bstat = compi / (3.0 * P.taub);
-  const double scale = std::fabs(1.0 - (dt * bstat) * (P.patm - pres));
-  for (int d = 0; d < 3; ++d) c->box[d] = scale * c->box[d];
-  launch_baro_shift(c->stream, c->r, nb > 1 ? c->rnm : nullptr, na, nb, scale - 1.0);
-  c->launches += 1;
-  return GB_OK;
+  double tvxyz[3];
+  for (int j = 0; j < 3; ++j) tvxyz[j] = tc / 3 + (0.5 * K[2 + j] / nb + 0.5 * K[5 + j] / nb) / mts;
+  int st = beren_driver(c, vir, tv, tvxyz, dt, nb > 1 ? c->rnm : nullptr);
+  if (st) return st;
+  // this step's low-frequency forces see the new box: the non-cubic k vectors
+  // (bohr^-1) are rebuilt now (the cubic ones are in the unit box)
+  return c->P.iamcub ? GB_OK : dev_prepare(c, 0.0, 0.0);
 }
 
 // r and dvdr2 are final once the MTS block (and the barostat) ran
@@ -1140,7 +1172,9 @@ int dev_collect(gb_context *c, int mode, double dt, double beta) {
   }
   const double *A = c->h_acc;
   auto S = [&](int s) { return A + (size_t)s * ACC_STRIDE; };
-  const double L = c->box[0];
+  // the box of the step's Ewald evaluation: a barostat after the forces (the
+  // rigid step) has scaled c->box since
+  const double L = c->acc_L > 0.0 ? c->acc_L : c->box[0];
   const double qq = c->qq;
   const double vself = c->P.walpha / std::sqrt(PI) * qq;
   const EnergyPlan &pl = c->plan;

@@ -275,7 +275,10 @@ def rattle_s2(r, p, mass, dt, dvdr):
     return vir.reshape(3, 3, order="F")
 
 
-def evolve_rig_pi(state: State, dt, mass, z, beta, irun=0):
+def evolve_rig_pi(state: State, dt, mass, z, beta, irun=0, nbaro=0):
+    """evolve_rig_pi(p,r,v,v_lf,v_hf,dvdr,dvdr2,dt,mass,na,nb,boxlxyz,z,beta,vir,vir_lf,irun,nbaro);
+    state.vir accumulates as the reference's caller's vir does; state.box is
+    scaled in place by the barostat (nbaro = 1)."""
     nb, na, _ = state.r.shape
     v, v_lf, v_hf = C.c_double(), C.c_double(), C.c_double()
     _check(load().gbrpmd_evolve_rig_pi(_ptr(state.p), _ptr(state.r), C.byref(v), C.byref(v_lf), C.byref(v_hf),
@@ -283,7 +286,7 @@ def evolve_rig_pi(state: State, dt, mass, z, beta, irun=0):
                                        _ptr(_arr(mass)), C.byref(C.c_int(na)), C.byref(C.c_int(nb)),
                                        _ptr(state.box), _ptr(_arr(z)), C.byref(C.c_double(beta)),
                                        _ptr(state.vir), _ptr(state.vir_lf), C.byref(C.c_int(irun)),
-                                       C.byref(C.c_int(0))))
+                                       C.byref(C.c_int(nbaro))))
     return dict(v=v.value)
 
 

@@ -41,6 +41,7 @@ def load():
     lib.orc_ran2.restype = C.c_double
     lib.orc_gaussian.restype = C.c_double
     lib.orc_bench_replicas.restype = C.c_double
+    lib.orc_pressure.restype = C.c_double
     assert lib.orc_params_size() == C.sizeof(GbParams), "gb_params layout mismatch"
     _lib = lib
     return lib
@@ -196,6 +197,20 @@ def virial_ke(r, dvdr, dvdr2, beta):
     return tv.value, tvxyz, tq1.value, tq2.value
 
 
+def pressure(vir, tv, na, box):
+    """md_pressure.f90's isotropic pressure with the LJ tail (vir column-major 3x3)."""
+    return load().orc_pressure(_ptr(np.ascontiguousarray(vir, float)), C.c_double(tv), C.c_int(na),
+                               _ptr(np.ascontiguousarray(box, float)))
+
+
+def beren_driver(vir, tv, tvxyz, dt, r, box):
+    """beren_driver (module_barostat.f90:8-26) on r [nb][na][3] and box, both in place."""
+    nb, na, _ = r.shape
+    load().orc_beren_driver(_ptr(np.ascontiguousarray(vir, float)), C.c_double(tv),
+                            _ptr(np.ascontiguousarray(tvxyz, float)), C.c_double(dt), _ptr(r), _ptr(box),
+                            C.c_int(na), C.c_int(nb))
+
+
 ESTIMATORS = ("tk", "vrp", "econs", "temp", "tv", "tvx", "tvy", "tvz", "pres", "dipx", "dipy", "dipz", "dip2",
               "dipm", "den", "v")
 
@@ -219,14 +234,14 @@ def rattle_setup(nm):
     load().orc_rattle_setup(C.c_int(nm))
 
 
-def evolve_rig_pi(state: State, dt, mass, z, beta, rng: Rng):
+def evolve_rig_pi(state: State, dt, mass, z, beta, rng: Rng, nbaro=0):
     nb, na, _ = state.r.shape
     v, v_lf, v_hf = C.c_double(), C.c_double(), C.c_double()
     st = load().orc_evolve_rig_pi(_ptr(state.p), _ptr(state.r), C.byref(v), C.byref(v_lf), C.byref(v_hf),
                                   _ptr(state.dvdr), _ptr(state.dvdr2), C.c_double(dt), _ptr(np.asarray(mass, float)),
                                   C.c_int(na), C.c_int(nb), _ptr(state.box), _ptr(np.asarray(z, float)),
                                   C.c_double(beta), _ptr(state.vir), _ptr(state.vir_lf), rng.buf,
-                                  C.byref(rng.irun), C.c_int(0))
+                                  C.byref(rng.irun), C.c_int(nbaro))
     return dict(status=st, v=v.value)
 
 

@@ -1,7 +1,8 @@
 """The thermostat kicks and the barostat inside evolve_pi on the device,
 through the drop-in C ABI, against the oracle: PRL (parinello_therm_loc) and
 PRG (parinello_therm) kicks drawing the reference's random stream, and the
-Berendsen barostat (nbaro = 1); then the reference's own gentest equilibration
+Berendsen barostat (nbaro = 1: beren_baro on cubic boxes, beren_baro_nc on
+the others, and the barostat of evolve_rig_pi); then the reference's own gentest equilibration
 (100 NVT + 1000 NPT steps, Andersen collisions, md_eq.f90) replayed on the
 device from the lattice against every series the reference printed.
 
@@ -74,6 +75,49 @@ def test_berendsen_barostat_matches_oracle(case):
     assert rel(dev.r, ref.r) < TOL
     assert rel(dev.p, ref.p) < TOL
     assert rel(dev.dvdr + dev.dvdr2, ref.dvdr + ref.dvdr2) < TOL
+
+
+def test_berendsen_barostat_noncubic_matches_oracle():
+    # beren_baro_nc (module_barostat.f90:28-86): one scale per axis
+    s = systems.build(param="param_qspcfw", ncell=(8, 4, 4), nb=4, mts=5, dtfs=1.25, nbdf1=1, nbdf2=3,
+                      therm="NON", baro="BER", taufs=200.0)
+    assert s["params"].iamcub == 0
+    ref, dev = run_both(s, 4, nbaro=1)
+    scale = ref.box / s["box"]
+    assert np.ptp(scale) > 1e-9  # the axes moved by different factors
+    assert np.abs(dev.box - ref.box).max() <= TOL * ref.box.max()
+    assert rel(dev.r, ref.r) < TOL
+    assert rel(dev.p, ref.p) < TOL
+    assert rel(dev.dvdr + dev.dvdr2, ref.dvdr + ref.dvdr2) < TOL
+
+
+@pytest.mark.parametrize("ncell", [(4, 4, 4), (6, 4, 4)])
+def test_rigid_barostat_matches_oracle(ncell):
+    # evolve_rig_pi with nbaro = 1 (evolve_rigid.f90:203-213): virial_ke with
+    # the zeroed dvdr2, then beren_driver on the bead positions; the caller's
+    # vir accumulates over the calls
+    s = systems.build(param="param_tip05_rigid", ncell=ncell, nb=4, therm="NON", baro="BER", taufs=100.0)
+    lib.rattle_setup(s["nm"])
+    lib.init(orc.get_params())
+    r = s["r"].copy()
+    rng = np.random.default_rng(71)
+    p = rng.normal(size=r.shape) * np.sqrt(s["mass"][None, :, None] * s["nb"] / s["beta"]) * 0.1
+    st0, v0, f0, vir0 = orc.forces(r, s["box"], s["z"], 1)
+    assert st0 == 0
+    ref = orc.State(r, p, f0, np.zeros_like(r), s["box"].copy())
+    dev = lib.State(r, p, f0, np.zeros_like(r), s["box"].copy())
+    g = orc.Rng(1)
+    for _ in range(3):
+        eo = orc.evolve_rig_pi(ref, s["dt"], s["mass"], s["z"], s["beta"], g, nbaro=1)
+        assert eo["status"] == 0
+        ed = lib.evolve_rig_pi(dev, s["dt"], s["mass"], s["z"], s["beta"], nbaro=1)
+    assert np.abs(ref.box - s["box"]).max() > 1e-9  # the box moved
+    assert np.abs(dev.box - ref.box).max() <= TOL * ref.box.max()
+    for a, b in ((dev.r, ref.r), (dev.p, ref.p), (dev.dvdr, ref.dvdr)):
+        assert rel(a, b) < TOL
+    assert abs(ed["v"] - eo["v"]) <= TOL * abs(eo["v"])
+    assert rel(dev.vir, ref.vir) < TOL
+    assert rel(dev.vir_lf, ref.vir_lf) < TOL
 
 
 def test_device_replays_gentest_equilibration():
