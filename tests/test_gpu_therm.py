@@ -120,6 +120,33 @@ def test_rigid_barostat_matches_oracle(ncell):
     assert rel(dev.vir_lf, ref.vir_lf) < TOL
 
 
+def test_rigid_barostat_resident_context_matches_dropin():
+    # a resident context's rigid NPT steps: the virial the barostat reads
+    # accumulates over its barostat steps as the drop-in caller's vir does
+    s = systems.build(param="param_tip05_rigid", ncell=(6, 4, 4), nb=4, therm="NON", baro="BER", taufs=100.0)
+    lib.rattle_setup(s["nm"])
+    lib.init(orc.get_params())
+    r = s["r"].copy()
+    rng = np.random.default_rng(72)
+    p = rng.normal(size=r.shape) * np.sqrt(s["mass"][None, :, None] * s["nb"] / s["beta"]) * 0.1
+    f0 = orc.forces(r, s["box"], s["z"], 1)[2]
+    dev = lib.State(r, p, f0, np.zeros_like(r), s["box"].copy())
+    for _ in range(3):
+        lib.evolve_rig_pi(dev, s["dt"], s["mass"], s["z"], s["beta"], nbaro=1)
+    ctx = lib.Context(s["na"], s["nb"], s["mass"], s["z"])
+    try:
+        ctx.upload(r=r, p=p, dvdr=f0, dvdr2=np.zeros_like(r), box=s["box"])
+        ctx.set_nbaro(1)
+        ctx.evolve(3, s["dt"], s["beta"])
+        ctx.sync()
+        rr, pp, ff, _ = ctx.download()
+        box = ctx.box
+    finally:
+        ctx.close()
+    assert np.abs(box - dev.box).max() <= 1e-12 * box.max()
+    assert rel(rr, dev.r) < 1e-12 and rel(pp, dev.p) < 1e-12 and rel(ff, dev.dvdr) < 1e-12
+
+
 def test_device_replays_gentest_equilibration():
     # main.f90:298-299 seeding, full_forces, sample, then md_eq (100 NVT steps,
     # then 1000 NPT steps with the Berendsen barostat), all on the device
