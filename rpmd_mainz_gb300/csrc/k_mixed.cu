@@ -293,10 +293,11 @@ constexpr int SIGN32 = (int)0x80000000u;
 GB_D float flipf(float v, int mask) { return __int_as_float(__float_as_int(v) ^ mask); }
 
 // The power tables of ewald_cubic.f90:254-286 / ewald_noncubic.f90:296-336,
-// q e^{i k lat x} (x component) and e^{i k lat y}, e^{i k lat z}, one thread
-// per entry: the phase in periods, t = k x lat / (2 pi), is reduced modulo 1
-// in two-float arithmetic (exact product k * hi by FMA) and the entry is
-// sincospif(2 t) in FP32.  The reference's recurrence over k in FP64 rounded
+// q e^{i k lat x} (x component) and e^{i k lat y}, e^{i k lat z}: for each
+// entry the phase in periods, t = k x lat / (2 pi), is reduced modulo 1 in
+// two-float arithmetic (exact product k * hi by FMA) and the entry is
+// sincospif(2 t) in FP32 (one thread per site axis and its K1 entries: one
+// thread per entry, repeating the FP64 product, measured 10 % slower).  The reference's recurrence over k in FP64 rounded
 // to FP32 and this direct form differ by a few FP32 ulps.  per = lat / (2 pi).
 __global__ void k_recip_tables_mx(const double *rs, const double *q, int na, int B, int kmax, double3 per,
                                   float2 *tab) {
