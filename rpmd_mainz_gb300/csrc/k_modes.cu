@@ -152,6 +152,15 @@ __global__ void k_expand_forces(double *dvdr, const double *fb1, int nbc1, const
 // sqrt(1/nb) (from the host: no per-thread FP64 square roots).
 constexpr int XR = 32;
 constexpr int XT = 4 * XR;
+constexpr int XPJ = 8;  // momenta per thread staged in shared memory (rings of nb <= 4 XPJ)
+
+// 8-byte asynchronous copy global -> shared (cp.async, sm_80 and later): no
+// register holds the value, so the copy runs while the thread computes
+GB_D void cp_async8(double *smem, const double *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+GB_D void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <int HM, typename R>
 __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double *fb1, int nbc1, const double *tw_c1,
@@ -168,6 +177,18 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
   const bool any = fb1 || fb2;
   const int lr = threadIdx.x % XR, grp = threadIdx.x / XR;
   const long long row = (long long)blockIdx.x * XR + lr;
+  const int j0 = grp * nb / 4, j1 = (grp + 1) * nb / 4;
+  // the momenta this thread kicks, copied to shared memory asynchronously
+  // first: their loads are all in flight at once and overlap the
+  // coefficients' computation, instead of one load round trip per bead in
+  // the bead loop (rings of at most 4 XPJ beads; longer ones load them there,
+  // and the launch leaves the staging area out of their shared memory)
+  double *PS = smx + (size_t)(nb + XR) * NQ;  // [XPJ][XT], after E and CF
+  const bool pre = p != nullptr && row < S && nb <= 4 * XPJ;
+  if (pre) {
+#pragma unroll 1
+    for (int u = 0; u < j1 - j0; ++u) cp_async8(PS + u * XT + threadIdx.x, p + row + S * (j0 + u));
+  }
   if (grp == 0 && row < S) {
     R cf[NQ];
 #pragma unroll
@@ -226,12 +247,12 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
       E[w] = q == 0 ? sc : ((q & 1) ? 2.0 * sc * tw_nb[m] : -2.0 * sc * tw_nb[nb + m]);
     }
   }
+  cp_async_wait_all();  // this thread's momenta are in PS (only it reads them)
   __syncthreads();
   if (row >= S) return;
   R cr[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) cr[q] = CF[lr * NQ + q];
-  const int j0 = grp * nb / 4, j1 = (grp + 1) * nb / 4;
   const bool extras = e1 || e2 || e3;
   bool bad = false;
   for (int j = j0; j < j1; ++j) {
@@ -249,7 +270,7 @@ __global__ void __launch_bounds__(XT) k_expand_table(double *dvdr, const double 
     }
     dvdr[o] = v;
     bad |= gb_nonfinite(v);
-    if (p) p[o] = p[o] - halfdt * v;
+    if (p) p[o] = (pre ? PS[(j - j0) * XT + threadIdx.x] : p[o]) - halfdt * v;
   }
   gb_flag_nonfinite(status, bad);
 }
@@ -357,7 +378,7 @@ void launch_expand_hm(cudaStream_t s, bool mixed, double *dvdr, const double *fb
                       const double *e3, double *p, double halfdt, int na, int nb, const double *tw_nb,
                       unsigned *status) {
   const long long n = 3LL * na;
-  const size_t smem = sizeof(double) * (nb + XR) * (2 * HM + 1);
+  const size_t smem = sizeof(double) * ((nb + XR) * (2 * HM + 1) + (nb <= 4 * XPJ ? XT * XPJ : 0));
   auto scale = [&](int nbc) {  // sqrt(1/nbc), sqrt(nb/nbc) of a contraction (force_contract)
     return nbc > 0 ? make_double2(sqrt(1.0 / (double)nbc), sqrt((double)nb / (double)nbc)) : make_double2(0.0, 0.0);
   };
